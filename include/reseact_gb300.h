@@ -1,0 +1,220 @@
+/*
+ * reseact_gb300.h -- C ABI of the GB300 operator-split step (libreseact_gb300.so).
+ *
+ * One Lie-Trotter macro step of ReSEACT: SSPRK43 flux-form PPM transport over [t0, t1]
+ * followed by Rosenbrock23 block-diagonal chemistry over [t0, t1], each with its own
+ * adaptive PI controller and a clamp to >= 0 of every accepted state.
+ *
+ * Reference interfaces this ABI replaces (paths relative to the reference repository):
+ *   rs_macro_step      <- OpSplit.lie_trotter_solve            tools/reactant_handoff/op_split.jl:100-164
+ *                         and the device-resident twin adv(...)  run_reseact_reactant.jl:310-355
+ *                         (dtT/dtC carried in and out exactly as adv returns dtTend/dtCend)
+ *   rs_set_forcing     <- refresh_forcing + sync_forcing!       run_reseact_reactant.jl:360-366,434-440
+ *   rs_set_state /     <- the cell-major state vector u[(c-1)*NS+s]
+ *   rs_get_state          (cellmajor_perm, prototypes/reseact_3d_chem/block_jac.jl:18-40;
+ *                          state dump layout run_reseact.jl:378-391)
+ *   rs_rhs_transport   <- f_trans! (transport half of the split, split_common.jl:530-533)
+ *   rs_rhs_chem        <- f_chem!  (chemistry half, split_common.jl:530-533)
+ *   rs_block_jac       <- block_ad_jac / symbolic block Jacobian
+ *                         prototypes/reseact_3d_chem/block_jac.jl:108-136,
+ *                         tools/reactant_handoff/rx_sym_block_jac.jl:205-233
+ *   rs_single_step     <- ssprk43_step / ros23_step             rx_traced_integrator.jl:362-400 / 279-349
+ *   rs_get_rate_constants <- the per-cell rate constants of the .esm mechanism
+ *                         (prototypes/g2_depsink/g2_nodep.esm:450-1780,1861)
+ *
+ * Conventions
+ *   - Every entry point returns rs_status (0 = RS_OK); no C++ exception crosses the ABI.
+ *     rs_last_error(h) returns the text of the handle's last failure.
+ *   - Host pointers are borrowed for the duration of the call only; the handle owns all
+ *     device memory and its CUDA stream.  Calls are synchronous on return.
+ *   - One handle per host thread.
+ *   - Gridded host arrays use the reference's Julia array order (lon fastest):
+ *     a field of shape (NLON, NLAT, NLEV) is the C array [NLEV][NLAT][NLON].
+ *   - The state is CELL-MAJOR as in the reference: u[c*NS + s] with cells sorted by
+ *     (i_lon, j_lat, k_lev) tuples, i.e. c = (i*NLAT + j)*NLEV + k (0-based), and species
+ *     sorted by name with the air mass "m" last (when has_air_mass = 1).
+ */
+#ifndef RESEACT_GB300_H
+#define RESEACT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RS_API_VERSION 1
+
+typedef enum rs_status {
+  RS_OK = 0,
+  RS_ERR_INVALID = 1,     /* bad argument or configuration */
+  RS_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+  RS_ERR_MAXITERS = 3,    /* adaptive loop hit maxiters before t1 (reference: maxiters cap) */
+  RS_ERR_NONFINITE = 4,   /* non-finite state after a macro step */
+  RS_ERR_NOMEM = 5,       /* device allocation failed */
+  RS_ERR_STATE = 6,       /* call out of order (e.g. no forcing set) */
+  RS_ERR_UNSUPPORTED = 7  /* feature not available in this build */
+} rs_status;
+
+/* lateral boundary kinds */
+enum { RS_BC_PERIODIC = 0, RS_BC_OPEN = 1, RS_BC_CLOSED = 2 };
+/* arithmetic of the transport half */
+enum { RS_PREC_FP64 = 0, RS_PREC_MIXED = 1 };
+/* chemistry step-size control: one global dt (reference) or per-cell adaptive substeps */
+enum { RS_CHEM_GLOBAL_DT = 0, RS_CHEM_PER_CELL = 1 };
+/* rs_single_step operators */
+enum { RS_OP_TRANSPORT = 0, RS_OP_CHEMISTRY = 1 };
+
+/* rate-program opcodes (postfix), one program per reaction */
+enum {
+  RS_OP_CONST = 0, RS_OP_TEMP = 1, RS_OP_PRES = 2, RS_OP_PARAM = 3,
+  RS_OP_ADD = 10, RS_OP_SUB = 11, RS_OP_MUL = 12, RS_OP_DIV = 13, RS_OP_POW = 14, RS_OP_NEG = 15,
+  RS_OP_EXP = 20, RS_OP_LOG = 21, RS_OP_LOG10 = 22, RS_OP_SQRT = 23
+};
+
+/* A mass-action mechanism, lowered from an .esm reaction_systems entry.
+ * Species are the n_species non-constant species (sorted by name); constant species are
+ * folded into the rate programs.  Reaction r consumes react_species[react_ptr[r]..react_ptr[r+1])
+ * with integer stoichiometry react_nu and produces prod_species with coefficients prod_coef.
+ * Its rate constant is the postfix program prog_op/prog_val[prog_ptr[r]..prog_ptr[r+1]),
+ * evaluated per cell from T, P and params[].  combinatoric = 1 divides the mass-action
+ * product by prod(nu!) (Catalyst's default rate law). */
+typedef struct rs_mechanism {
+  int32_t n_species;
+  int32_t n_reactions;
+  int32_t n_params;
+  int32_t combinatoric;
+  const int32_t* react_ptr;     /* [n_reactions+1] */
+  const int32_t* react_species; /* [react_ptr[n_reactions]] */
+  const int32_t* react_nu;
+  const int32_t* prod_ptr;      /* [n_reactions+1] */
+  const int32_t* prod_species;
+  const double* prod_coef;
+  const int32_t* prog_ptr;      /* [n_reactions+1] */
+  const int32_t* prog_op;
+  const double* prog_val;
+  const double* params;         /* [n_params] */
+} rs_mechanism;
+
+/* Lat-lon grid.  Cell centres lon0 + i*dlon, lat0 + j*dlat (degrees); latitude edges are
+ * centre +- dlat/2 clamped to [-90, 90] (half-width polar caps for pole-centred grids). */
+typedef struct rs_grid {
+  int32_t nlon, nlat, nlev;
+  int32_t lon_bc;  /* RS_BC_PERIODIC (global) or RS_BC_OPEN (regional inflow/outflow) */
+  int32_t lat_bc;  /* RS_BC_CLOSED (poles, zero flux) or RS_BC_OPEN (regional) */
+  double lon0_deg, dlon_deg;
+  double lat0_deg, dlat_deg;
+} rs_grid;
+
+/* PI controller constants (rx_traced_integrator.jl:86-99). */
+typedef struct rs_controller {
+  double beta1, beta2, qmin, qmax, gamma, qsteady_min, qsteady_max, qoldinit;
+} rs_controller;
+
+typedef struct rs_config {
+  int32_t api_version;     /* RS_API_VERSION */
+  int32_t device;          /* CUDA device ordinal */
+  rs_grid grid;
+  int32_t has_air_mass;    /* 1: state carries a trailing air-mass species m (transport) */
+  int32_t do_transport;    /* 1: run the SSPRK43 half */
+  int32_t do_chemistry;    /* 1: run the Rosenbrock23 half */
+  rs_mechanism mech;
+  double rtol_T, atol_T;   /* transport tolerances (reference: 1e-4, 1e-6) */
+  double rtol_C, atol_C;   /* chemistry tolerances (reference: 1e-4, 1e-9) */
+  rs_controller ctrl_T;    /* SSPRK43: beta1 7/30, beta2 2/15, qsteady_max 1 */
+  rs_controller ctrl_C;    /* ROS23:   beta1 7/20, beta2 1/5,  qsteady_max 6/5 */
+  double maxiters;         /* per adaptive solve (reference: 2e4) */
+  int32_t clamp_nonneg;    /* clamp accepted states to >= 0 (reference: true) */
+  int32_t precision;       /* RS_PREC_FP64 or RS_PREC_MIXED */
+  int32_t chem_mode;       /* RS_CHEM_GLOBAL_DT or RS_CHEM_PER_CELL */
+} rs_config;
+
+/* Forcing for one macro step (refresh_forcing).  NULL members keep their previous value
+ * (zero before the first call).  Horizontal air-mass fluxes are on the unit sphere
+ * (Mx = dp_face*U_face/a, Pa/s); Mz (Pa/s) is at the LOWER edge of each level, +ve upward,
+ * level 0 at the surface.  All three scale in time by cos(flux_omega*t). */
+typedef struct rs_forcing {
+  const double* mx;          /* [nlev][nlat][nlon+1] west-face zonal flux */
+  const double* my;          /* [nlev][nlat+1][nlon] south-face meridional flux */
+  const double* mz;          /* [nlev+1][nlat][nlon] */
+  double flux_omega;         /* rad/s; 0 = steady fluxes */
+  const double* dp;          /* [nlev][nlat][nlon] pressure thickness (vertical PPM geometry) */
+  const double* qbc_w;       /* [n_species][nlev][nlat] west-halo mixing ratios (open lon BC) */
+  const double* qbc_e;       /* [n_species][nlev][nlat] */
+  const double* qbc_s;       /* [n_species][nlev][nlon] south-halo mixing ratios (open lat BC) */
+  const double* qbc_n;       /* [n_species][nlev][nlon] */
+  const double* temperature; /* [nlev][nlat][nlon] K */
+  const double* pressure;    /* [nlev][nlat][nlon] Pa */
+  const double* emission;    /* [n_species][nlev][nlat][nlon] source added to d(species)/dt */
+} rs_forcing;
+
+/* Per-macro-step statistics (op_split.jl:159-163 return tuple plus the carried dts). */
+typedef struct rs_stats {
+  double naT, nrT;       /* transport accepted / rejected attempts */
+  double naC, nrC;       /* chemistry accepted / rejected attempts (global-dt mode) */
+  double dtT_end, dtC_end;
+  double tT_end, tC_end; /* time reached by each half (== t1 on success) */
+  double chem_cell_steps;  /* per-cell mode: sum over cells of accepted substeps */
+  int32_t status;
+} rs_stats;
+
+typedef struct rs_handle rs_handle;
+
+/* Fill *cfg with the reference defaults (tolerances, controllers, clamp, maxiters). */
+void rs_default_config(rs_config* cfg);
+
+rs_status rs_create(const rs_config* cfg, rs_handle** out);
+void rs_destroy(rs_handle* h);
+const char* rs_last_error(const rs_handle* h);
+
+/* Number of state values (cells * species) and of species per cell. */
+size_t rs_state_size(const rs_handle* h);
+int32_t rs_species_per_cell(const rs_handle* h);
+
+rs_status rs_set_state(rs_handle* h, const double* u_cellmajor, size_t n);
+rs_status rs_get_state(rs_handle* h, double* u_cellmajor, size_t n);
+rs_status rs_set_forcing(rs_handle* h, const rs_forcing* f);
+
+/* Rate constants k[r][cell] (cell in grid order [nlev][nlat][nlon]).  rs_rates recomputes
+ * them from T/P/params; rs_set_rate_constants installs caller-provided values (e.g. per-cell
+ * photolysis) until the next forcing change of T or P. */
+rs_status rs_get_rate_constants(rs_handle* h, double* k, size_t n);
+rs_status rs_set_rate_constants(rs_handle* h, const double* k, size_t n);
+
+/* One Lie-Trotter macro step over [t0, t1] on the resident state.  *dtT / *dtC are the
+ * carried step sizes in and out.  Returns RS_ERR_MAXITERS / RS_ERR_NONFINITE on failure
+ * (the state then holds whatever the halves reached; bisection stays with the caller, as
+ * in op_split.jl:219-241). */
+rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double* dtC,
+                        rs_stats* out);
+
+/* Single evaluations for parity tests (host arrays in the cell-major state layout). */
+rs_status rs_rhs_transport(rs_handle* h, double t, const double* u, double* du, size_t n);
+rs_status rs_rhs_chem(rs_handle* h, double t, const double* u, double* du, size_t n);
+/* J[c][r][s] = d f_chem(cell c, species r) / d u(cell c, species s) */
+rs_status rs_block_jac(rs_handle* h, const double* u, double* jac, size_t n_jac);
+/* One unclamped attempt of the chosen integrator from u_in; writes u_out and the hairer
+ * error estimate. */
+rs_status rs_single_step(rs_handle* h, int32_t op, double t, double dt, const double* u_in,
+                         double* u_out, double* eest, size_t n);
+
+/* Device view of the resident state for zero-copy callers: species-major planes
+ * [species][nlev][nlat][nlon] of doubles.  Valid until the next rs_macro_step. */
+rs_status rs_state_device_ptr(rs_handle* h, void** d_state);
+/* The handle's CUDA stream (cudaStream_t), for callers timing with CUDA events. */
+void* rs_stream(rs_handle* h);
+
+/* Per-kernel launch statistics, collected while profiling is on. */
+rs_status rs_set_profiling(rs_handle* h, int32_t on);
+/* names: ';'-separated kernel family names written into buf (size buf_len); counts and
+ * milliseconds per family into the arrays (length max_kernels).  Returns the family count
+ * in *n_out. */
+rs_status rs_get_profile(rs_handle* h, char* buf, size_t buf_len, double* launches,
+                         double* total_ms, int32_t max_kernels, int32_t* n_out);
+rs_status rs_reset_profile(rs_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RESEACT_GB300_H */

@@ -1,0 +1,855 @@
+// ORACLE -- CPU FP64 restatement of ReSEACT's operator-split step.  TEST INFRASTRUCTURE ONLY:
+// only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load this library,
+// and only as the checker / the timed CPU baseline.  The product (libreseact_gb300.so) never
+// links, loads or calls it.
+//
+// The reference is Julia and cannot run here (no julia, un-vendored EarthSciAST /
+// OrdinaryDiffEq stack).  This file restates, in plain C++ FP64 with -ffp-contract=off:
+//   * ROS23 attempt           tools/reactant_handoff/rx_traced_integrator.jl:255-349
+//   * pivot-free blocksolve   rx_traced_integrator.jl:101-135  (dense, natural order)
+//   * SSPRK43 attempt         rx_traced_integrator.jl:351-437
+//   * PI controller + loop    rx_traced_integrator.jl:85-99, 439-507
+//   * Lie-Trotter macro step  run_reseact_reactant.jl:310-355 (adv), op_split.jl:100-164
+//   * mass-action chemistry   prototypes/g2_depsink/g2_nodep.esm:450-1780 (tables built by
+//                             reseact/esm_gb300/mechanism.py from that schema)
+//   * CWC flux-form transport reseact.esm:1535 (continuity), :2083 (species, mixing-ratio
+//                             form), prototypes/transport_3d/transport_3d.esm (analytic winds)
+//   * CW84 monotone PPM       Colella & Woodward 1984 eqs. 1.6-1.8, 1.10 (the reference's PPM
+//                             rule files are absent; only their slope form is quoted in
+//                             tools/diag/ppm_limiter_kink_repro.jl:3-8 and the extremum test
+//                             in tools/diag/rhs_kink_probe.jl:9-14) -- PARITY FOR THE PPM
+//                             ARITHMETIC IS UNPINNED against the reference; it is pinned by the
+//                             CWC freestream invariant (transport_3d.esm tests, tools/cwc_gate.jl).
+//
+// Layout: grid SoA, u[s*NC + c] with c = (k*nlat + j)*nlon + i.  The global hairer norm uses
+// the fixed two-level reduction tree documented at reduce_fixed() below.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "../include/reseact_gb300.h"
+
+namespace {
+
+constexpr double kD2R = 0.017453292519943295;
+constexpr double kOneSixth = 1.0 / 6.0;
+
+// ------------------------------------------------------------------ mechanism (dense form)
+struct Mech {
+  int ns = 0, nr = 0, np = 0, comb = 1;
+  std::vector<int> rptr, rsp, rnu, pptr, pops;
+  std::vector<double> pvals, params, net;  // net[r*ns + s]
+  std::vector<int> prptr, prsp;
+  std::vector<double> prcoef;
+};
+
+Mech make_mech(const rs_mechanism* m) {
+  Mech M;
+  M.ns = m->n_species; M.nr = m->n_reactions; M.np = m->n_params; M.comb = m->combinatoric;
+  M.rptr.assign(m->react_ptr, m->react_ptr + M.nr + 1);
+  M.rsp.assign(m->react_species, m->react_species + M.rptr[M.nr]);
+  M.rnu.assign(m->react_nu, m->react_nu + M.rptr[M.nr]);
+  M.prptr.assign(m->prod_ptr, m->prod_ptr + M.nr + 1);
+  M.prsp.assign(m->prod_species, m->prod_species + M.prptr[M.nr]);
+  M.prcoef.assign(m->prod_coef, m->prod_coef + M.prptr[M.nr]);
+  M.pptr.assign(m->prog_ptr, m->prog_ptr + M.nr + 1);
+  M.pops.assign(m->prog_op, m->prog_op + M.pptr[M.nr]);
+  M.pvals.assign(m->prog_val, m->prog_val + M.pptr[M.nr]);
+  M.params.assign(m->params, m->params + M.np);
+  M.net.assign((size_t)M.nr * M.ns, 0.0);
+  for (int r = 0; r < M.nr; ++r) {
+    for (int e = M.rptr[r]; e < M.rptr[r + 1]; ++e) M.net[(size_t)r * M.ns + M.rsp[e]] -= M.rnu[e];
+    for (int e = M.prptr[r]; e < M.prptr[r + 1]; ++e) M.net[(size_t)r * M.ns + M.prsp[e]] += M.prcoef[e];
+  }
+  return M;
+}
+
+// Postfix rate program (one per reaction), evaluated per cell.
+double eval_prog(const Mech& M, int r, double T, double P) {
+  double st[64];
+  int sp = 0;
+  for (int e = M.pptr[r]; e < M.pptr[r + 1]; ++e) {
+    int op = M.pops[e];
+    double v = M.pvals[e];
+    switch (op) {
+      case RS_OP_CONST: st[sp++] = v; break;
+      case RS_OP_TEMP: st[sp++] = T; break;
+      case RS_OP_PRES: st[sp++] = P; break;
+      case RS_OP_PARAM: st[sp++] = M.params[(int)v]; break;
+      case RS_OP_ADD: --sp; st[sp - 1] = st[sp - 1] + st[sp]; break;
+      case RS_OP_SUB: --sp; st[sp - 1] = st[sp - 1] - st[sp]; break;
+      case RS_OP_MUL: --sp; st[sp - 1] = st[sp - 1] * st[sp]; break;
+      case RS_OP_DIV: --sp; st[sp - 1] = st[sp - 1] / st[sp]; break;
+      case RS_OP_POW: --sp; st[sp - 1] = std::pow(st[sp - 1], st[sp]); break;
+      case RS_OP_NEG: st[sp - 1] = -st[sp - 1]; break;
+      case RS_OP_EXP: st[sp - 1] = std::exp(st[sp - 1]); break;
+      case RS_OP_LOG: st[sp - 1] = std::log(st[sp - 1]); break;
+      case RS_OP_LOG10: st[sp - 1] = std::log10(st[sp - 1]); break;
+      case RS_OP_SQRT: st[sp - 1] = std::sqrt(st[sp - 1]); break;
+      default: return NAN;
+    }
+  }
+  double k = st[0];
+  if (M.comb) {  // mass-action product divided by prod(nu!)
+    for (int e = M.rptr[r]; e < M.rptr[r + 1]; ++e) {
+      double f = 1.0;
+      for (int t = 2; t <= M.rnu[e]; ++t) f *= t;
+      if (f != 1.0) k = k * (1.0 / f);
+    }
+  }
+  return k;
+}
+
+// reaction velocity v_r = k * prod x^nu (reactant entries in table order)
+inline double velocity(const Mech& M, int r, double k, const double* x) {
+  double v = k;
+  for (int e = M.rptr[r]; e < M.rptr[r + 1]; ++e)
+    for (int t = 0; t < M.rnu[e]; ++t) v = v * x[M.rsp[e]];
+  return v;
+}
+
+// d v_r / d x_q
+inline double dvel(const Mech& M, int r, double k, const double* x, int q) {
+  double d = k;
+  for (int e = M.rptr[r]; e < M.rptr[r + 1]; ++e) {
+    int s = M.rsp[e], nu = M.rnu[e];
+    if (s == q) {
+      if (nu >= 2) {
+        double f = (double)nu;
+        for (int t = 1; t < nu; ++t) f = f * x[s];
+        d = d * f;
+      }
+    } else {
+      for (int t = 0; t < nu; ++t) d = d * x[s];
+    }
+  }
+  return d;
+}
+
+// chemistry RHS of one cell: f_s = sum_r net[r,s] v_r (+ emission)
+void chem_rhs_cell(const Mech& M, const double* k, const double* x, const double* emis,
+                   double* f, double* vbuf) {
+  for (int r = 0; r < M.nr; ++r) vbuf[r] = velocity(M, r, k[r], x);
+  for (int s = 0; s < M.ns; ++s) {
+    double acc = 0.0;
+    for (int r = 0; r < M.nr; ++r) {
+      double c = M.net[(size_t)r * M.ns + s];
+      if (c != 0.0) acc = acc + c * vbuf[r];
+    }
+    f[s] = emis ? acc + emis[s] : acc;
+  }
+}
+
+// dense analytic block Jacobian J[s*ns+q] (the exact Jacobian the reference obtains by
+// forward-mode AD / symbolic differentiation, block_jac.jl:108-136)
+void chem_jac_cell(const Mech& M, const double* k, const double* x, double* J) {
+  int ns = M.ns;
+  std::fill(J, J + ns * ns, 0.0);
+  for (int s = 0; s < ns; ++s) {
+    for (int q = 0; q < ns; ++q) {
+      double acc = 0.0;
+      bool any = false;
+      for (int r = 0; r < M.nr; ++r) {
+        double c = M.net[(size_t)r * ns + s];
+        if (c == 0.0) continue;
+        bool has = false;
+        for (int e = M.rptr[r]; e < M.rptr[r + 1]; ++e) has |= (M.rsp[e] == q);
+        if (!has) continue;
+        acc = acc + c * dvel(M, r, k[r], x, q);
+        any = true;
+      }
+      J[s * ns + q] = any ? acc : 0.0;
+    }
+  }
+}
+
+// Pivot-free Gaussian elimination (rx_traced_integrator.jl:110-135): factor W in place,
+// recording the multipliers in the lower triangle; solve() replays the same elimination on b.
+void lu_factor(int n, double* W) {
+  for (int k = 0; k < n; ++k) {
+    double piv = 1.0 / W[k * n + k];
+    for (int i = k + 1; i < n; ++i) {
+      double m = W[i * n + k] * piv;
+      for (int j = k + 1; j < n; ++j) {
+        double mw = m * W[k * n + j];
+        W[i * n + j] = W[i * n + j] - mw;
+      }
+      W[i * n + k] = m;
+    }
+  }
+}
+void lu_solve(int n, const double* LU, const double* b, double* x) {
+  double y[64];
+  for (int i = 0; i < n; ++i) y[i] = b[i];
+  for (int k = 0; k < n; ++k)
+    for (int i = k + 1; i < n; ++i) {
+      double mb = LU[i * n + k] * y[k];
+      y[i] = y[i] - mb;
+    }
+  for (int i = n - 1; i >= 0; --i) {
+    double acc = y[i];
+    for (int j = i + 1; j < n; ++j) {
+      double wx = LU[i * n + j] * x[j];
+      acc = acc - wx;
+    }
+    x[i] = acc / LU[i * n + i];
+  }
+}
+
+// ------------------------------------------------------------------ fixed reduction tree
+// Level 1: blocks of 1024 cells; thread t (of 256) sums e[b*1024 + t + 256*q], q = 0..3, in
+// order starting from 0.0, then a pairwise tree v[t] += v[t+s] for s = 128, 64, ..., 1.
+// Level 2: one block of 256; thread t sums partial[t + 256*q] for q = 0, 1, ... in order,
+// then the same pairwise tree.  The CUDA kernels reduce with exactly this tree.
+double tree256(double* v) {
+  for (int s = 128; s > 0; s >>= 1)
+    for (int t = 0; t < s; ++t) v[t] = v[t] + v[t + s];
+  return v[0];
+}
+double reduce_fixed(const double* e, size_t n) {
+  size_t nb = (n + 1023) / 1024;
+  std::vector<double> part(nb);
+  for (size_t b = 0; b < nb; ++b) {
+    double v[256];
+    for (int t = 0; t < 256; ++t) {
+      double acc = 0.0;
+      for (int q = 0; q < 4; ++q) {
+        size_t idx = b * 1024 + t + 256 * q;
+        if (idx < n) acc = acc + e[idx];
+      }
+      v[t] = acc;
+    }
+    part[b] = tree256(v);
+  }
+  double v[256];
+  for (int t = 0; t < 256; ++t) {
+    double acc = 0.0;
+    for (size_t q = t; q < nb; q += 256) acc = acc + part[q];
+    v[t] = acc;
+  }
+  return tree256(v);
+}
+
+// ------------------------------------------------------------------ grid + transport
+struct Grid {
+  int nlon, nlat, nlev, lon_bc, lat_bc;
+  size_t nc;
+  std::vector<double> gx, gylo, gyhi;  // per lat row
+};
+
+Grid make_grid(const rs_grid* g) {
+  Grid G;
+  G.nlon = g->nlon; G.nlat = g->nlat; G.nlev = g->nlev;
+  G.lon_bc = g->lon_bc; G.lat_bc = g->lat_bc;
+  G.nc = (size_t)g->nlon * g->nlat * g->nlev;
+  std::vector<double> phie(g->nlat + 1), ce(g->nlat + 1);
+  for (int j = 0; j <= g->nlat; ++j) {
+    double p = g->lat0_deg + (j - 0.5) * g->dlat_deg;
+    p = std::min(90.0, std::max(-90.0, p));
+    phie[j] = p;
+    ce[j] = (std::fabs(p) >= 90.0) ? 0.0 : std::cos(p * kD2R);
+  }
+  double dlon = g->dlon_deg * kD2R;
+  G.gx.resize(g->nlat); G.gylo.resize(g->nlat); G.gyhi.resize(g->nlat);
+  for (int j = 0; j < g->nlat; ++j) {
+    double dS = std::sin(phie[j + 1] * kD2R) - std::sin(phie[j] * kD2R);
+    double dphi = (phie[j + 1] - phie[j]) * kD2R;
+    G.gx[j] = dphi / (dlon * dS);
+    G.gylo[j] = ce[j] / dS;
+    G.gyhi[j] = ce[j + 1] / dS;
+  }
+  return G;
+}
+
+struct Forcing {
+  std::vector<double> mx, my, mz, dp, qw, qe, qs, qn, T, P, emis;
+  double omega = 0.0;
+  // vertical PPM coefficients per column: slope (sA,sB) for cells -1..nlev, edge (eAB,eC,eD)
+  // for edges 0..nlev (edge e lies between cells e-1 and e)
+  std::vector<double> vs, ve;
+};
+
+inline double dp_mirror(const double* dpcol_stride, int nlev, size_t stride, int k) {
+  int kk = k < 0 ? -1 - k : (k >= nlev ? 2 * nlev - 1 - k : k);
+  return dpcol_stride[(size_t)kk * stride];
+}
+
+void vertical_coefs(const Grid& G, Forcing& F) {
+  int nlev = G.nlev;
+  size_t ncol = (size_t)G.nlon * G.nlat;
+  F.vs.assign(ncol * (nlev + 2) * 2, 0.0);
+  F.ve.assign(ncol * (nlev + 1) * 3, 0.0);
+  for (size_t col = 0; col < ncol; ++col) {
+    const double* d = F.dp.data() + col;
+    size_t st = ncol;
+    for (int k = -1; k <= nlev; ++k) {  // slope coefficients (CW84 eq. 1.7)
+      double D0 = dp_mirror(d, nlev, st, k - 1), D1 = dp_mirror(d, nlev, st, k),
+             D2 = dp_mirror(d, nlev, st, k + 1);
+      double c = D1 / (D0 + D1 + D2);
+      double sA = c * (2.0 * D0 + D1) / (D2 + D1);
+      double sB = c * (D1 + 2.0 * D2) / (D0 + D1);
+      F.vs[(col * (nlev + 2) + (k + 1)) * 2 + 0] = sA;
+      F.vs[(col * (nlev + 2) + (k + 1)) * 2 + 1] = sB;
+    }
+    for (int e = 0; e <= nlev; ++e) {  // edge coefficients (CW84 eq. 1.6), cells e-1 | e
+      int k = e - 1;
+      double Dm = dp_mirror(d, nlev, st, k - 1), D0 = dp_mirror(d, nlev, st, k),
+             D1 = dp_mirror(d, nlev, st, k + 1), D2 = dp_mirror(d, nlev, st, k + 2);
+      double S = Dm + D0 + D1 + D2;
+      double eA = D0 / (D0 + D1);
+      double t1 = (Dm + D0) / (2.0 * D0 + D1);
+      double t2 = (D2 + D1) / (2.0 * D1 + D0);
+      double eB = (2.0 * D1 * D0 / (D0 + D1)) * (t1 - t2) / S;
+      double eC = -(D0 * t1) / S;
+      double eD = D1 * (D1 + D2) / (D0 + 2.0 * D1) / S;
+      F.ve[(col * (nlev + 1) + e) * 3 + 0] = eA + eB;
+      F.ve[(col * (nlev + 1) + e) * 3 + 1] = eC;
+      F.ve[(col * (nlev + 1) + e) * 3 + 2] = eD;
+    }
+  }
+}
+
+// uniform-grid monotonised slope (CW84 eq. 1.7-1.8)
+inline double slope_u(double am, double a, double ap) {
+  double d0 = a - am, d1 = ap - a;
+  if (d1 * d0 > 0.0) {
+    double da = 0.5 * (ap - am);
+    double lim = std::min(2.0 * std::fabs(d0), 2.0 * std::fabs(d1));
+    return std::copysign(std::min(std::fabs(da), lim), da);
+  }
+  return 0.0;
+}
+inline double slope_n(double am, double a, double ap, double sA, double sB) {
+  double d0 = a - am, d1 = ap - a;
+  if (d1 * d0 > 0.0) {
+    double da = sA * d1 + sB * d0;
+    double lim = std::min(2.0 * std::fabs(d0), 2.0 * std::fabs(d1));
+    return std::copysign(std::min(std::fabs(da), lim), da);
+  }
+  return 0.0;
+}
+// CW84 eq. 1.10 parabola limiter; returns (aL, aR) of cell with mean a
+inline void limit(double a, double& aL, double& aR) {
+  if ((aR - a) * (a - aL) <= 0.0) {
+    aL = a; aR = a;
+  } else {
+    double dA = aR - aL;
+    double a6 = 6.0 * (a - 0.5 * (aL + aR));
+    if (dA * a6 > dA * dA) aL = 3.0 * a - 2.0 * aR;
+    else if (-(dA * dA) > dA * a6) aR = 3.0 * a - 2.0 * aL;
+  }
+}
+// Uniform PPM face value from the upwind cell: vals[0..4] = a_{u-2..u+2}; side = +1 takes the
+// right edge (flow in +direction), -1 the left edge.
+inline double ppm_face_u(const double* v, int right) {
+  double dm1 = slope_u(v[0], v[1], v[2]);
+  double d0 = slope_u(v[1], v[2], v[3]);
+  double dp1 = slope_u(v[2], v[3], v[4]);
+  double aL = v[1] + 0.5 * (v[2] - v[1]) - (d0 - dm1) * kOneSixth;
+  double aR = v[2] + 0.5 * (v[3] - v[2]) - (dp1 - d0) * kOneSixth;
+  limit(v[2], aL, aR);
+  return right ? aR : aL;
+}
+
+struct Model {
+  Grid G;
+  Mech M;
+  int nsp;  // species per cell in the state (chem species + air mass)
+  int has_m;
+  rs_config cfg;
+  Forcing F;
+  std::vector<double> krates;  // [nr][nc]
+};
+
+// value of species s (state plane q) at lon index i (ghosts per BC), lat j, lev k
+inline double qx(const Model& md, const double* q, int s, int i, int j, int k) {
+  const Grid& G = md.G;
+  if (i < 0 || i >= G.nlon) {
+    if (G.lon_bc == RS_BC_PERIODIC) i = ((i % G.nlon) + G.nlon) % G.nlon;
+    else {
+      const std::vector<double>& b = (i < 0) ? md.F.qw : md.F.qe;
+      return b[((size_t)s * G.nlev + k) * G.nlat + j];
+    }
+  }
+  return q[((size_t)k * G.nlat + j) * G.nlon + i];
+}
+inline double qy(const Model& md, const double* q, int s, int i, int j, int k) {
+  const Grid& G = md.G;
+  if (j < 0 || j >= G.nlat) {
+    if (G.lat_bc == RS_BC_OPEN) {
+      const std::vector<double>& b = (j < 0) ? md.F.qs : md.F.qn;
+      return b[((size_t)s * G.nlev + k) * G.nlon + i];
+    }
+    j = j < 0 ? -1 - j : 2 * G.nlat - 1 - j;
+  }
+  return q[((size_t)k * G.nlat + j) * G.nlon + i];
+}
+inline double qz(const Model& md, const double* q, int i, int j, int k) {
+  const Grid& G = md.G;
+  int kk = k < 0 ? -1 - k : (k >= G.nlev ? 2 * G.nlev - 1 - k : k);
+  return q[((size_t)kk * G.nlat + j) * G.nlon + i];
+}
+
+// face fluxes of tracer s at cell (i,j,k): west/east, south/north, bottom/top
+double xflux(const Model& md, const double* q, int s, int i, int j, int k, double g) {
+  const Grid& G = md.G;
+  double M = g * md.F.mx[((size_t)k * G.nlat + j) * (G.nlon + 1) + i];
+  int up = M > 0.0 ? i - 1 : i;
+  double v[5];
+  for (int o = 0; o < 5; ++o) v[o] = qx(md, q, s, up - 2 + o, j, k);
+  return M * ppm_face_u(v, M > 0.0);
+}
+double yflux(const Model& md, const double* q, int s, int i, int j, int k, double g) {
+  const Grid& G = md.G;
+  if (G.lat_bc != RS_BC_OPEN && (j == 0 || j == G.nlat)) return 0.0;
+  double M = g * md.F.my[((size_t)k * (G.nlat + 1) + j) * G.nlon + i];
+  int up = M > 0.0 ? j - 1 : j;
+  double v[5];
+  for (int o = 0; o < 5; ++o) v[o] = qy(md, q, s, i, up - 2 + o, k);
+  return M * ppm_face_u(v, M > 0.0);
+}
+double zflux(const Model& md, const double* q, int i, int j, int kf, double g) {
+  const Grid& G = md.G;
+  if (kf == 0 || kf == G.nlev) return 0.0;
+  size_t ncol = (size_t)G.nlon * G.nlat, col = (size_t)j * G.nlon + i;
+  double M = g * md.F.mz[(size_t)kf * ncol + col];
+  int up = M > 0.0 ? kf - 1 : kf;
+  double v[5];
+  for (int o = 0; o < 5; ++o) v[o] = qz(md, q, i, j, up - 2 + o);
+  const double* vs = md.F.vs.data() + col * (G.nlev + 2) * 2;
+  const double* ve = md.F.ve.data() + col * (G.nlev + 1) * 3;
+  auto sl = [&](int c, double am, double a, double ap) {
+    return slope_n(am, a, ap, vs[(c + 1) * 2], vs[(c + 1) * 2 + 1]);
+  };
+  double dm1 = sl(up - 1, v[0], v[1], v[2]);
+  double d0 = sl(up, v[1], v[2], v[3]);
+  double dp1 = sl(up + 1, v[2], v[3], v[4]);
+  const double* eL = ve + (size_t)up * 3;        // edge between up-1 | up
+  const double* eR = ve + (size_t)(up + 1) * 3;  // edge between up | up+1
+  double aL = v[1] + eL[0] * (v[2] - v[1]) + eL[1] * d0 + eL[2] * dm1;
+  double aR = v[2] + eR[0] * (v[3] - v[2]) + eR[1] * dp1 + eR[2] * d0;
+  limit(v[2], aL, aR);
+  return M * (M > 0.0 ? aR : aL);
+}
+
+// Transport RHS (CWC mixing-ratio form, reseact.esm:2083; continuity reseact.esm:1535).
+void transport_rhs(const Model& md, const double* u, double t, double* du) {
+  const Grid& G = md.G;
+  double g = md.F.omega != 0.0 ? std::cos(md.F.omega * t) : 1.0;
+  size_t nc = G.nc;
+  int ntr = md.has_m ? md.nsp - 1 : md.nsp;
+  const double* m = md.has_m ? u + (size_t)(md.nsp - 1) * nc : nullptr;
+#pragma omp parallel for collapse(2) schedule(static)
+  for (int k = 0; k < G.nlev; ++k)
+    for (int j = 0; j < G.nlat; ++j)
+      for (int i = 0; i < G.nlon; ++i) {
+        size_t c = ((size_t)k * G.nlat + j) * G.nlon + i;
+        size_t ncol = (size_t)G.nlon * G.nlat, col = (size_t)j * G.nlon + i;
+        double mxw = g * md.F.mx[((size_t)k * G.nlat + j) * (G.nlon + 1) + i];
+        double mxe = g * md.F.mx[((size_t)k * G.nlat + j) * (G.nlon + 1) + i + 1];
+        double mys = (G.lat_bc != RS_BC_OPEN && j == 0) ? 0.0
+                   : g * md.F.my[((size_t)k * (G.nlat + 1) + j) * G.nlon + i];
+        double myn = (G.lat_bc != RS_BC_OPEN && j + 1 == G.nlat) ? 0.0
+                   : g * md.F.my[((size_t)k * (G.nlat + 1) + j + 1) * G.nlon + i];
+        double mzb = (k == 0) ? 0.0 : g * md.F.mz[(size_t)k * ncol + col];
+        double mzt = (k + 1 == G.nlev) ? 0.0 : g * md.F.mz[(size_t)(k + 1) * ncol + col];
+        double DxM = (mxe - mxw) * G.gx[j];
+        double DyM = myn * G.gyhi[j] - mys * G.gylo[j];
+        double DzM = mzt - mzb;
+        double divM = (DxM + DyM) + DzM;
+        for (int s = 0; s < ntr; ++s) {
+          const double* q = u + (size_t)s * nc;
+          double fw = xflux(md, q, s, i, j, k, g), fe = xflux(md, q, s, i + 1, j, k, g);
+          double fs = yflux(md, q, s, i, j, k, g), fn = yflux(md, q, s, i, j + 1, k, g);
+          double fb = zflux(md, q, i, j, k, g), ft = zflux(md, q, i, j, k + 1, g);
+          double Dx = (fe - fw) * G.gx[j];
+          double Dy = fn * G.gyhi[j] - fs * G.gylo[j];
+          double Dz = ft - fb;
+          double a = -((Dx + Dy) + Dz);
+          double b = q[c] * divM;
+          du[(size_t)s * nc + c] = m ? (a + b) / m[c] : a + b;
+        }
+        if (md.has_m) du[(size_t)(md.nsp - 1) * nc + c] = -divM;
+      }
+}
+
+// per-cell contribution to the hairer norm: sum over species of (err/den)^2
+inline double cell_err(const Model& md, const double* u, const double* unew, const double* err,
+                       size_t c, double atol, double rtol) {
+  double acc = 0.0;
+  for (int s = 0; s < md.nsp; ++s) {
+    size_t x = (size_t)s * md.G.nc + c;
+    double am = std::max(std::fabs(u[x]), std::fabs(unew[x]));
+    double den = am * rtol + atol;
+    double at = err[x] / den;
+    acc = acc + at * at;
+  }
+  return acc;
+}
+
+// SSPRK43 attempt (rx_traced_integrator.jl:362-400).  Returns EEst.
+double ssprk43_step(const Model& md, const double* u, double t, double dt, double* unew,
+                    std::vector<double>& w) {
+  size_t n = (size_t)md.nsp * md.G.nc;
+  w.resize(3 * n);
+  double* u3 = w.data();
+  double* k = w.data() + n;
+  double* ut = w.data() + 2 * n;
+  double dt_2 = dt / 2;
+  std::copy(u, u + n, u3);
+  for (int i = 1; i <= 3; ++i) {
+    double ci = 0.5 * (i - 1);
+    transport_rhs(md, u3, t + ci * dt, k);
+#pragma omp parallel for schedule(static)
+    for (size_t x = 0; x < n; ++x) u3[x] = u3[x] + dt_2 * k[x];
+  }
+  std::vector<double> u4(n);
+#pragma omp parallel for schedule(static)
+  for (size_t x = 0; x < n; ++x) {
+    ut[x] = (1.0 / 3.0) * u[x] + (2.0 / 3.0) * u3[x];
+    u4[x] = (2.0 / 3.0) * u[x] + (1.0 / 3.0) * u3[x];
+  }
+  transport_rhs(md, u4.data(), t + dt_2, k);
+#pragma omp parallel for schedule(static)
+  for (size_t x = 0; x < n; ++x) {
+    unew[x] = u4[x] + dt_2 * k[x];
+    ut[x] = 0.5 * (ut[x] - unew[x]);
+  }
+  std::vector<double> e(md.G.nc);
+#pragma omp parallel for schedule(static)
+  for (size_t c = 0; c < md.G.nc; ++c) e[c] = cell_err(md, u, unew, ut, c, md.cfg.atol_T, md.cfg.rtol_T);
+  double sse = reduce_fixed(e.data(), md.G.nc);
+  return std::sqrt(sse / (double)n);
+}
+
+const double kRosD = 1.0 / (2.0 + std::sqrt(2.0));
+const double kRosC32 = 6.0 + std::sqrt(2.0);
+
+// ROS23 attempt of one cell (rx_traced_integrator.jl:279-349), writes unew and the cell's
+// error residual utilde; chemistry never couples cells.
+void ros23_cell(const Model& md, const double* kr, const double* x, const double* emis, double t,
+                double dt, double* unew, double* ut) {
+  const Mech& M = md.M;
+  int n = M.ns;
+  double f0[64], f1[64], f2[64], k1[64], k2[64], k3[64], b[64], u1[64], xn[64], vb[256];
+  std::vector<double> J(n * n), W(n * n);
+  chem_rhs_cell(M, kr, x, emis, f0, vb);
+  chem_jac_cell(M, kr, x, J.data());
+  double dtgamma = dt * kRosD;
+  for (int r = 0; r < n; ++r)
+    for (int s = 0; s < n; ++s) {
+      double tmp = dtgamma * J[r * n + s];
+      W[r * n + s] = r == s ? 1.0 - tmp : 0.0 - tmp;
+    }
+  lu_factor(n, W.data());
+  lu_solve(n, W.data(), f0, k1);
+  double dto2 = dt / 2;
+  for (int s = 0; s < n; ++s) u1[s] = x[s] + dto2 * k1[s];
+  chem_rhs_cell(M, kr, u1, emis, f1, vb);
+  for (int s = 0; s < n; ++s) b[s] = f1[s] - k1[s];
+  lu_solve(n, W.data(), b, k2);
+  for (int s = 0; s < n; ++s) k2[s] = k2[s] + k1[s];
+  for (int s = 0; s < n; ++s) xn[s] = x[s] + dt * k2[s];
+  chem_rhs_cell(M, kr, xn, emis, f2, vb);
+  for (int s = 0; s < n; ++s) {
+    double a = kRosC32 * (k2[s] - f1[s]);
+    double c = 2.0 * (k1[s] - f0[s]);
+    b[s] = (f2[s] - a) - c;
+  }
+  lu_solve(n, W.data(), b, k3);
+  double dto6 = dt / 6;
+  for (int s = 0; s < n; ++s) {
+    unew[s] = xn[s];
+    ut[s] = dto6 * ((k1[s] - 2.0 * k2[s]) + k3[s]);
+  }
+  (void)t;
+}
+
+double ros23_step(const Model& md, const double* u, double t, double dt, double* unew,
+                  std::vector<double>& w) {
+  size_t nc = md.G.nc, n = (size_t)md.nsp * nc;
+  int ns = md.M.ns;
+  w.resize(n);
+  double* ut = w.data();
+  const bool has_emis = !md.F.emis.empty();
+#pragma omp parallel for schedule(static)
+  for (size_t c = 0; c < nc; ++c) {
+    double x[64], xn[64], e[64], kr[256], em[64];
+    for (int s = 0; s < ns; ++s) x[s] = u[(size_t)s * nc + c];
+    for (int r = 0; r < md.M.nr; ++r) kr[r] = md.krates[(size_t)r * nc + c];
+    if (has_emis)
+      for (int s = 0; s < ns; ++s) em[s] = md.F.emis[(size_t)s * nc + c];
+    ros23_cell(md, kr, x, has_emis ? em : nullptr, t, dt, xn, e);
+    for (int s = 0; s < ns; ++s) {
+      unew[(size_t)s * nc + c] = xn[s];
+      ut[(size_t)s * nc + c] = e[s];
+    }
+    for (int s = ns; s < md.nsp; ++s) {  // inert air mass: f = 0, J row = 0
+      unew[(size_t)s * nc + c] = u[(size_t)s * nc + c];
+      ut[(size_t)s * nc + c] = 0.0;
+    }
+  }
+  std::vector<double> e(nc);
+#pragma omp parallel for schedule(static)
+  for (size_t c = 0; c < nc; ++c) e[c] = cell_err(md, u, unew, ut, c, md.cfg.atol_C, md.cfg.rtol_C);
+  double sse = reduce_fixed(e.data(), nc);
+  return std::sqrt(sse / (double)n);
+}
+
+// adaptive_solve (rx_traced_integrator.jl:455-507)
+struct SolveOut { double t, dt, nacc, nrej, iters; };
+template <class Step>
+SolveOut adaptive_solve(Step step, std::vector<double>& u, double t0, double tend, double dt0,
+                        const rs_controller& c, double maxiters, bool clamp) {
+  size_t n = u.size();
+  std::vector<double> unew(n);
+  double beta1 = c.beta1, beta2 = c.beta2;
+  double invqmax = 1.0 / c.qmax, invqmin = 1.0 / c.qmin, gamma = c.gamma;
+  double t = t0, dt = dt0, qold = c.qoldinit, nacc = 0, nrej = 0, iters = 0;
+  double tlim = tend - 1.0e-9;
+  while ((t < tlim) && (iters < maxiters)) {
+    double dtc = std::min(dt, tend - t);
+    double EEst = step(u.data(), t, dtc, unew.data());
+    if (clamp)
+      for (size_t x = 0; x < n; ++x) unew[x] = std::max(unew[x], 0.0);
+    if (std::isnan(EEst)) EEst = 1.0e10;
+    double q11 = std::pow(std::max(EEst, 1.0e-35), beta1);
+    double qden = std::pow(qold, beta2);
+    double q = q11 / qden;
+    q = std::max(invqmax, std::min(invqmin, q / gamma));
+    bool accept = EEst <= 1.0;
+    bool insteady = (c.qsteady_min <= q) && (q <= c.qsteady_max);
+    double qa = insteady ? 1.0 : q;
+    double dt_acc = dtc / qa;
+    double qr = std::min(invqmin, q11 / gamma);
+    double dt_rej = dtc / qr;
+    if (accept) {
+      u.swap(unew);
+      t = t + dtc;
+      dt = dt_acc;
+      qold = std::max(EEst, c.qoldinit);
+      nacc += 1.0;
+    } else {
+      dt = dt_rej;
+      nrej += 1.0;
+    }
+    iters += 1.0;
+  }
+  return {t, dt, nacc, nrej, iters};
+}
+
+void compute_rates(Model& md) {
+  size_t nc = md.G.nc;
+  md.krates.assign((size_t)md.M.nr * nc, 0.0);
+#pragma omp parallel for schedule(static)
+  for (size_t c = 0; c < nc; ++c) {
+    double T = md.F.T.empty() ? 298.0 : md.F.T[c];
+    double P = md.F.P.empty() ? 101325.0 : md.F.P[c];
+    for (int r = 0; r < md.M.nr; ++r) md.krates[(size_t)r * nc + c] = eval_prog(md.M, r, T, P);
+  }
+}
+
+void copy_opt(std::vector<double>& dst, const double* src, size_t n) {
+  if (src) dst.assign(src, src + n);
+  else if (dst.empty()) dst.assign(n, 0.0);
+}
+
+}  // namespace
+
+// ====================================================================== C API (oracle)
+extern "C" {
+
+struct or_model;
+
+or_model* or_create(const rs_config* cfg) {
+  Model* md = new Model();
+  md->cfg = *cfg;
+  md->G = make_grid(&cfg->grid);
+  md->M = make_mech(&cfg->mech);
+  md->has_m = cfg->has_air_mass;
+  md->nsp = md->M.ns + (cfg->has_air_mass ? 1 : 0);
+  return reinterpret_cast<or_model*>(md);
+}
+
+void or_destroy(or_model* h) { delete reinterpret_cast<Model*>(h); }
+
+int or_set_forcing(or_model* h, const rs_forcing* f) {
+  Model& md = *reinterpret_cast<Model*>(h);
+  const Grid& G = md.G;
+  size_t nc = G.nc;
+  int ns = md.M.ns;
+  copy_opt(md.F.mx, f->mx, (size_t)G.nlev * G.nlat * (G.nlon + 1));
+  copy_opt(md.F.my, f->my, (size_t)G.nlev * (G.nlat + 1) * G.nlon);
+  copy_opt(md.F.mz, f->mz, (size_t)(G.nlev + 1) * G.nlat * G.nlon);
+  md.F.omega = f->flux_omega;
+  if (f->dp) md.F.dp.assign(f->dp, f->dp + nc);
+  else if (md.F.dp.empty()) md.F.dp.assign(nc, 1.0);
+  copy_opt(md.F.qw, f->qbc_w, (size_t)ns * G.nlev * G.nlat);
+  copy_opt(md.F.qe, f->qbc_e, (size_t)ns * G.nlev * G.nlat);
+  copy_opt(md.F.qs, f->qbc_s, (size_t)ns * G.nlev * G.nlon);
+  copy_opt(md.F.qn, f->qbc_n, (size_t)ns * G.nlev * G.nlon);
+  bool tp = f->temperature || f->pressure || md.krates.empty();
+  if (f->temperature) md.F.T.assign(f->temperature, f->temperature + nc);
+  if (f->pressure) md.F.P.assign(f->pressure, f->pressure + nc);
+  if (f->emission) md.F.emis.assign(f->emission, f->emission + (size_t)ns * nc);
+  vertical_coefs(G, md.F);
+  if (tp) compute_rates(md);
+  return 0;
+}
+
+void or_set_rates(or_model* h, const double* k) {
+  Model& md = *reinterpret_cast<Model*>(h);
+  md.krates.assign(k, k + (size_t)md.M.nr * md.G.nc);
+}
+void or_get_rates(or_model* h, double* k) {
+  Model& md = *reinterpret_cast<Model*>(h);
+  std::copy(md.krates.begin(), md.krates.end(), k);
+}
+
+// single-cell chemistry helpers (box model / golden tests): k from T, P
+void or_cell_rates(or_model* h, double T, double P, double* k) {
+  Model& md = *reinterpret_cast<Model*>(h);
+  for (int r = 0; r < md.M.nr; ++r) k[r] = eval_prog(md.M, r, T, P);
+}
+
+// state arrays below are grid SoA [species][nlev][nlat][nlon]
+void or_rhs_transport(or_model* h, double t, const double* u, double* du) {
+  transport_rhs(*reinterpret_cast<Model*>(h), u, t, du);
+}
+
+void or_rhs_chem(or_model* h, const double* u, double* du) {
+  Model& md = *reinterpret_cast<Model*>(h);
+  size_t nc = md.G.nc;
+  int ns = md.M.ns;
+  bool he = !md.F.emis.empty();
+#pragma omp parallel for schedule(static)
+  for (size_t c = 0; c < nc; ++c) {
+    double x[64], f[64], kr[256], vb[256], em[64];
+    for (int s = 0; s < ns; ++s) x[s] = u[(size_t)s * nc + c];
+    for (int r = 0; r < md.M.nr; ++r) kr[r] = md.krates[(size_t)r * nc + c];
+    if (he)
+      for (int s = 0; s < ns; ++s) em[s] = md.F.emis[(size_t)s * nc + c];
+    chem_rhs_cell(md.M, kr, x, he ? em : nullptr, f, vb);
+    for (int s = 0; s < ns; ++s) du[(size_t)s * nc + c] = f[s];
+    for (int s = ns; s < md.nsp; ++s) du[(size_t)s * nc + c] = 0.0;
+  }
+}
+
+// J[c][r][s], ns_state x ns_state per cell (air-mass row/column zero)
+void or_block_jac(or_model* h, const double* u, double* J) {
+  Model& md = *reinterpret_cast<Model*>(h);
+  size_t nc = md.G.nc;
+  int ns = md.M.ns, nsp = md.nsp;
+#pragma omp parallel for schedule(static)
+  for (size_t c = 0; c < nc; ++c) {
+    double x[64], kr[256];
+    std::vector<double> Jc(ns * ns);
+    for (int s = 0; s < ns; ++s) x[s] = u[(size_t)s * nc + c];
+    for (int r = 0; r < md.M.nr; ++r) kr[r] = md.krates[(size_t)r * nc + c];
+    chem_jac_cell(md.M, kr, x, Jc.data());
+    double* out = J + c * nsp * nsp;
+    std::fill(out, out + nsp * nsp, 0.0);
+    for (int r = 0; r < ns; ++r)
+      for (int s = 0; s < ns; ++s) out[r * nsp + s] = Jc[r * ns + s];
+  }
+}
+
+double or_single_step(or_model* h, int op, double t, double dt, const double* u, double* unew) {
+  Model& md = *reinterpret_cast<Model*>(h);
+  std::vector<double> w;
+  return op == RS_OP_TRANSPORT ? ssprk43_step(md, u, t, dt, unew, w)
+                               : ros23_step(md, u, t, dt, unew, w);
+}
+
+// One Lie-Trotter macro step (adv, run_reseact_reactant.jl:310-355): transport adaptive
+// solve over [t0,t1] then chemistry adaptive solve over [t0,t1], clamp inside both.
+// stats: naT, nrT, naC, nrC, dtT_end, dtC_end, tT_end, tC_end
+int or_macro_step(or_model* h, double* u, double t0, double t1, double* dtT, double* dtC,
+                  double* stats) {
+  Model& md = *reinterpret_cast<Model*>(h);
+  size_t n = (size_t)md.nsp * md.G.nc;
+  std::vector<double> uv(u, u + n), w;
+  bool clamp = md.cfg.clamp_nonneg != 0;
+  SolveOut oT{t1, *dtT, 0, 0, 0}, oC{t1, *dtC, 0, 0, 0};
+  if (md.cfg.do_transport) {
+    oT = adaptive_solve([&](const double* x, double t, double dt, double* xn) {
+      return ssprk43_step(md, x, t, dt, xn, w); }, uv, t0, t1, *dtT, md.cfg.ctrl_T,
+      md.cfg.maxiters, clamp);
+  }
+  if (md.cfg.do_chemistry) {
+    oC = adaptive_solve([&](const double* x, double t, double dt, double* xn) {
+      return ros23_step(md, x, t, dt, xn, w); }, uv, t0, t1, *dtC, md.cfg.ctrl_C,
+      md.cfg.maxiters, clamp);
+  }
+  std::copy(uv.begin(), uv.end(), u);
+  *dtT = oT.dt; *dtC = oC.dt;
+  stats[0] = oT.nacc; stats[1] = oT.nrej; stats[2] = oC.nacc; stats[3] = oC.nrej;
+  stats[4] = oT.dt; stats[5] = oC.dt; stats[6] = oT.t; stats[7] = oC.t;
+  bool okT = !md.cfg.do_transport || oT.t >= t1 - 1e-9;
+  bool okC = !md.cfg.do_chemistry || oC.t >= t1 - 1e-9;
+  if (!okT || !okC) return RS_ERR_MAXITERS;
+  for (size_t x = 0; x < n; ++x)
+    if (!std::isfinite(u[x])) return RS_ERR_NONFINITE;
+  return 0;
+}
+
+// Per-cell adaptive chemistry (each cell its own ROS23 + PI controller over [t0,t1]), the
+// algorithm of the batched persistent kernel; error norm over the cell's own states.
+int or_chem_per_cell(or_model* h, double* u, double t0, double t1, double dt0, double* dt_out,
+                     double* steps_out) {
+  Model& md = *reinterpret_cast<Model*>(h);
+  size_t nc = md.G.nc;
+  int ns = md.M.ns, nsp = md.nsp;
+  const rs_controller c = md.cfg.ctrl_C;
+  int fail = 0;
+  bool he = !md.F.emis.empty();
+#pragma omp parallel for schedule(dynamic, 64) reduction(| : fail)
+  for (size_t cell = 0; cell < nc; ++cell) {
+    double x[64], xn[64], e[64], kr[256], em[64];
+    for (int s = 0; s < ns; ++s) x[s] = u[(size_t)s * nc + cell];
+    for (int r = 0; r < md.M.nr; ++r) kr[r] = md.krates[(size_t)r * nc + cell];
+    if (he)
+      for (int s = 0; s < ns; ++s) em[s] = md.F.emis[(size_t)s * nc + cell];
+    double t = t0, dt = dt0, qold = c.qoldinit, iters = 0, nacc = 0;
+    double tlim = t1 - 1.0e-9;
+    double invqmax = 1.0 / c.qmax, invqmin = 1.0 / c.qmin;
+    while ((t < tlim) && (iters < md.cfg.maxiters)) {
+      double dtc = std::min(dt, t1 - t);
+      ros23_cell(md, kr, x, he ? em : nullptr, t, dtc, xn, e);
+      double sse = 0.0;
+      for (int s = 0; s < ns; ++s) {
+        double am = std::max(std::fabs(x[s]), std::fabs(xn[s]));
+        double den = am * md.cfg.rtol_C + md.cfg.atol_C;
+        double at = e[s] / den;
+        sse = sse + at * at;
+      }
+      double EEst = std::sqrt(sse / (double)nsp);
+      if (std::isnan(EEst)) EEst = 1.0e10;
+      double q11 = std::pow(std::max(EEst, 1.0e-35), c.beta1);
+      double q = q11 / std::pow(qold, c.beta2);
+      q = std::max(invqmax, std::min(invqmin, q / c.gamma));
+      if (EEst <= 1.0) {
+        for (int s = 0; s < ns; ++s) x[s] = md.cfg.clamp_nonneg ? std::max(xn[s], 0.0) : xn[s];
+        t = t + dtc;
+        bool insteady = (c.qsteady_min <= q) && (q <= c.qsteady_max);
+        dt = dtc / (insteady ? 1.0 : q);
+        qold = std::max(EEst, c.qoldinit);
+        nacc += 1.0;
+      } else {
+        dt = dtc / std::min(invqmin, q11 / c.gamma);
+      }
+      iters += 1.0;
+    }
+    if (t < tlim) fail |= 1;
+    for (int s = 0; s < ns; ++s) u[(size_t)s * nc + cell] = x[s];
+    if (dt_out) dt_out[cell] = dt;
+    if (steps_out) steps_out[cell] = nacc;
+  }
+  return fail ? RS_ERR_MAXITERS : 0;
+}
+
+double or_reduce_fixed(const double* e, size_t n) { return reduce_fixed(e, n); }
+
+}  // extern "C"
