@@ -1,0 +1,383 @@
+#!/usr/bin/env python
+"""bench.py -- cell-steps/s of the GB300 operator-split step.
+
+Workload (one GPU): the plain FP64 method at 144 x 91 x 47 (615,888 cells, 2.5 x 2 deg,
+47 levels), SuperFast chemistry, deformational winds with +-0.05 Pa/s vertical flux, seeded
+lognormal initial fields.  One "step" is one 600 s Lie-Trotter macro step over the whole grid
+(SSPRK43 PPM transport then Rosenbrock23 chemistry, both adaptive, both clamped).  The
+synthetic forcing stands in for GEOS-FP meteorology (not available offline).
+
+Timing: W warm-up steps, then K steps timed with CUDA events on the library's stream, an L2
+flush (a 256 MiB write) between timed steps outside the event brackets, the max over ranks.
+`value` = cells * K * ranks / max time.  `e2e` repeats K steps through the C ABI with the state
+copied host->device before and device->host after every step (pinned host buffers).
+
+`--impl reference` times the CPU implementation of the same path (the C++ restatement of the
+reference; the Julia reference itself cannot run without julia and its un-vendored stack) on
+all host threads, on a bounded sample: the same physics on a 36 x 23 x 47 sub-grid.
+
+Multi-GPU: the path does not shard in this build; N ranks run N independent replicas
+(scaling "weak", no collective in the data path; NCCL only for the barrier and the max).
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-steps/s fwd (mixed vs FP64 GPU) at 1e-6 rel err; adjoint/forward time"
+UNIT = "cell-steps/s"
+WORKLOAD = "C2 144x91x47 SuperFast FP64 split step (dt=600 s)"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=6)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--small", action="store_true", help="small grid (profiling/debug)")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index, self.rows, self.stop = index, [], threading.Event()
+
+    def _run(self):
+        try:
+            proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                     "--format=csv,noheader,nounits", "-lms", "200"],
+                                    stdout=subprocess.PIPE, text=True)
+        except Exception:
+            return
+        while not self.stop.is_set():
+            line = proc.stdout.readline()
+            if not line:
+                break
+            self.rows.append([x.strip() for x in line.split(",")])
+        proc.terminate()
+        try:
+            proc.wait(timeout=5)
+        except Exception:
+            proc.kill()
+
+    def __enter__(self):
+        self.th = threading.Thread(target=self._run, daemon=True)
+        self.th.start()
+        return self
+
+    def __exit__(self, *a):
+        self.stop.set()
+        self.th.join(timeout=10)
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for n, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def fp64_peak():
+    from reseact.esm_gb300 import build
+    probe = build.probe_path()
+    if not os.path.exists(probe):
+        build.build()
+    r = subprocess.run([probe], capture_output=True, text=True, timeout=120)
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh)
+    except Exception:
+        return {}
+
+
+def workload(small=False):
+    from reseact.esm_gb300 import workloads
+    if small:
+        return workloads.c2(nlon=48, nlat=31, nlev=16)
+    return workloads.c2()
+
+
+def ros23_flops_per_cell(mech):
+    """FP64 operations one ROS23 attempt executes per cell (kernel k_ros23_attempt):
+    +,-,*,/ each counted once, an FMA as two; comparisons, abs and max not counted."""
+    t = mech.tables()
+    n = mech.ns
+    rmul = int(sum(t["react_nu"]))
+    vel = rmul
+    rhs = 2 * len(t["rhs_reaction"])
+    part = 0
+    for rx in mech.reactions:
+        for q, _ in rx.reactants:
+            for s, nu in rx.reactants:
+                part += (nu if nu >= 2 else 0) if s == q else nu
+    buildw = 2 * len(t["jac_part"]) + 2 * t["n_jac"]
+    lu = n + len(t["elim_lik"]) + 2 * len(t["upd_dst"])
+    solve = 2 * len(t["lower_slot"]) + 2 * len(t["upper_slot"]) + n
+    stage = 12 * n
+    err = 9 * n
+    return 3 * (vel + rhs) + part + buildw + lu + 3 * solve + stage + err
+
+
+def transport_flops_per_cell(nsp):
+    """FP64 operations of one SSPRK43 attempt per cell (4 stages): per tracer and stage, three
+    face reconstructions (~48 each: 3 slopes, 2 edges, limiter, flux) and the divergence and
+    stage update (~14); the air-mass row ~12."""
+    per_stage = (nsp - 1) * (3 * 48 + 14) + 12
+    return 4 * per_stage + 6 * nsp
+
+
+def transport_bytes_per_cell(nsp):
+    """Compulsory HBM bytes per cell-attempt for a fully fused SSPRK43 attempt: read and write
+    the state once (2*S*8) and read the three face-flux fields (3*8)."""
+    return 2 * nsp * 8 + 3 * 8
+
+
+# ---------------------------------------------------------------------------- GB300 arm
+def run_gb300(args):
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from reseact.esm_gb300 import Solver, workloads
+
+    w = workload(args.small)
+    solver = Solver.for_workload(w, device=local)
+    stream = torch.cuda.ExternalStream(solver.stream())
+    nc = w.ncells
+    u0 = w.u0_cellmajor()
+    solver.set_state(u0)
+    t, dtT, dtC = 0.0, w.dt0_T, w.dt0_C
+    dtm = w.dt_macro
+    for _ in range(args.warmup):
+        _, dtT, dtC, st = solver.macro_step(t, t + dtm, dtT, dtC)
+        t += dtm
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    t_start, dtT_start, dtC_start = t, dtT, dtC
+    u_start = solver.get_state()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    launches = 0.0
+    counts = []
+    barrier()
+    with ClockSampler(local) as clocks:
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            torch.cuda.synchronize()
+            starts[i].record(stream)
+            _, dtT, dtC, st = solver.macro_step(t, t + dtm, dtT, dtC)
+            ends[i].record(stream)
+            t += dtm
+            launches += st.kernel_launches
+            counts.append((st.naT, st.nrT, st.naC, st.nrC))
+        barrier()
+    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    ms_t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
+    ms_max = float(ms_t.item())
+    value = nc * args.steps * world / (ms_max * 1e-3)
+
+    # ------------------------------------------------------------------ e2e through the ABI
+    e2e = None
+    t_end, dtT_end, dtC_end = t, dtT, dtC
+    if not args.no_e2e:
+        # replay the same K steps from the same state, now through host buffers
+        host = torch.empty(solver.n, dtype=torch.float64, pin_memory=True).numpy()
+        host[:] = u_start
+        t, dtT, dtC = t_start, dtT_start, dtC_start
+        barrier()
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            solver.set_state(host)
+            _, dtT, dtC, st = solver.macro_step(t, t + dtm, dtT, dtC)
+            out = solver.get_state()
+            host[:] = out
+            t += dtm
+        barrier()
+        wall = time.perf_counter() - t0
+        wt = torch.tensor([wall], device="cuda", dtype=torch.float64)
+        if world > 1:
+            import torch.distributed as dist
+            dist.all_reduce(wt, op=dist.ReduceOp.MAX)
+        e2e = {"value": nc * args.steps * world / float(wt.item()), "unit": UNIT,
+               "h2d_bytes_per_step": int(solver.n * 8), "d2h_bytes_per_step": int(solver.n * 8)}
+
+    # ------------------------------------------------------------------ roofline pass
+    t, dtT, dtC = t_end, dtT_end, dtC_end
+    solver.set_profiling(True)
+    solver.reset_profile()
+    for _ in range(2):
+        _, dtT, dtC, st = solver.macro_step(t, t + dtm, dtT, dtC)
+        t += dtm
+    prof = solver.profile()
+    solver.set_profiling(False)
+    peaks = fp64_peak() if rank == 0 else {}
+    fams = {k: v for k, v in prof.items() if v[0] > 0}
+    dom = max(fams, key=lambda k: fams[k][1])
+    kernels = {}
+    f_ros = ros23_flops_per_cell(w.mech)
+    f_tr = transport_flops_per_cell(w.nsp)
+    for fam, (n_l, tot) in fams.items():
+        kernels[fam] = {"launches": n_l, "total_ms": round(tot, 4), "avg_ms": round(tot / n_l, 5),
+                        "share": round(tot / sum(v[1] for v in fams.values()), 4)}
+    roofline = None
+    if "ros23_attempt" in fams and rank == 0:
+        n_l, tot = fams["ros23_attempt"]
+        achieved = f_ros * nc / (tot / n_l * 1e-3) / 1e12
+        peak = peaks.get("fp64_tflops")
+        roofline = {"kernel": "k_ros23_attempt", "bound": "fp64", "achieved": round(achieved, 4),
+                    "peak": peak, "unit": "TFLOP/s", "frac": round(achieved / peak, 4) if peak else None,
+                    "traffic": None, "flops_per_cell_attempt": f_ros,
+                    "peak_source": "own FMA-chain probe (csrc/peak_probe.cu), FP64 has no entry in MEASURED_PEAKS.json"}
+    transport = None
+    if "ssprk43_stages" in fams and rank == 0:
+        n_l, tot = fams["ssprk43_stages"]
+        avg = tot / n_l * 1e-3
+        hbm = measured_peaks().get("hbm_gbs")
+        transport = {"kernel": "ssprk43 attempt (12 face-flux + 4 stage kernels)",
+                     "fp64_tflops": round(f_tr * nc / avg / 1e12, 4),
+                     "fp64_frac": round(f_tr * nc / avg / 1e12 / peaks["fp64_tflops"], 4) if peaks.get("fp64_tflops") else None,
+                     "hbm_gbs_compulsory": round(transport_bytes_per_cell(w.nsp) * nc / avg / 1e9, 2),
+                     "hbm_frac_compulsory": round(transport_bytes_per_cell(w.nsp) * nc / avg / 1e9 / hbm, 5) if hbm else None,
+                     "avg_attempt_ms": round(avg * 1e3, 4)}
+
+    # ------------------------------------------------------------------ CPU baseline
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_from_state(w, solver.get_state(), t, dtT, dtC)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (analytic deformational winds, seeded lognormal fields; GEOS-FP/NEI unavailable offline)",
+            "config": {"workload": WORKLOAD if not args.small else "C2-small 48x31x16",
+                       "cells": nc, "species_per_cell": w.nsp, "macro_dt_s": dtm,
+                       "chem_mode": "global dt (reference)", "precision": "FP64",
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": "256 MiB flush between timed steps"},
+            "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline,
+            "transport": transport, "kernels": kernels, "dominant": dom,
+            "attempts_per_step": {"naT": float(np.mean([c[0] for c in counts])),
+                                  "nrT": float(np.mean([c[1] for c in counts])),
+                                  "naC": float(np.mean([c[2] for c in counts])),
+                                  "nrC": float(np.mean([c[3] for c in counts]))},
+            "clocks": clocks.summary(), "cpu_baseline": cpu, "peaks": peaks,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def cpu_baseline_from_state(w, u_cm, t, dtT, dtC):
+    """The CPU restatement on all host threads: one macro step of the same grid from the
+    GPU's state (same t, same carried dts)."""
+    from oracle import oracle
+    from reseact.esm_gb300 import abi, workloads
+    oracle.build()
+    mabi = abi.MechanismABI(w.mech)
+    o = oracle.Oracle(w.config(mabi), w.forcing_abi(), mabi)
+    g = w.grid
+    u = workloads.cellmajor_to_soa(u_cm, w.nsp, g["nlon"], g["nlat"], g["nlev"])
+    t0 = time.perf_counter()
+    rc, _, _, st = o.macro_step(u, t, t + w.dt_macro, dtT, dtC)
+    wall = time.perf_counter() - t0
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count()))
+    return {"value": round(w.ncells / wall, 2), "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "1 macro step (600 s) of the full grid from the GPU state at t=%.0f s "
+                      "(%.1f s wall, %d+%d transport / %d+%d chemistry attempts)"
+                      % (t, wall, st[0], st[1], st[2], st[3])}
+
+
+# ---------------------------------------------------------------------------- reference arm
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle
+    from reseact.esm_gb300 import abi, workloads
+    oracle.build()
+    w = workloads.c2(nlon=36, nlat=23, nlev=47)
+    mabi = abi.MechanismABI(w.mech)
+    o = oracle.Oracle(w.config(mabi), w.forcing_abi(), mabi)
+    u = np.ascontiguousarray(w.u0.copy())
+    t, dtT, dtC = 0.0, w.dt0_T, w.dt0_C
+    for _ in range(args.warmup):
+        rc, dtT, dtC, _ = o.macro_step(u, t, t + w.dt_macro, dtT, dtC)
+        t += w.dt_macro
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        rc, dtT, dtC, st = o.macro_step(u, t, t + w.dt_macro, dtT, dtC)
+        t += w.dt_macro
+    wall = time.perf_counter() - t0
+    value = w.ncells * args.steps / wall
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count()))
+    line = {"metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(wall / args.steps * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "sample_grid": "36x23x47 (same physics, 1/16 of the cells)"},
+            "cpu_baseline": {"value": round(value, 2), "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "C++ restatement of the reference path (Julia reference cannot run here), "
+                                       "36x23x47 sub-grid, %d macro steps" % args.steps},
+            "e2e": {"value": round(value, 2), "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_gb300(a)

@@ -156,6 +156,7 @@ typedef struct rs_stats {
   double dtT_end, dtC_end;
   double tT_end, tC_end; /* time reached by each half (== t1 on success) */
   double chem_cell_steps;  /* per-cell mode: sum over cells of accepted substeps */
+  double kernel_launches;  /* CUDA kernels this call launched (device loop + checks) */
   int32_t status;
 } rs_stats;
 

@@ -145,22 +145,20 @@ void chem_rhs_cell(const Mech& M, const double* k, const double* x, const double
 // dense analytic block Jacobian J[s*ns+q] (the exact Jacobian the reference obtains by
 // forward-mode AD / symbolic differentiation, block_jac.jl:108-136)
 void chem_jac_cell(const Mech& M, const double* k, const double* x, double* J) {
+  // Reaction-major accumulation: each entry J[s,q] still receives its contributions in
+  // increasing reaction order, starting from 0.0, so the sums associate exactly as in the
+  // entry-by-entry form sum_r net[r,s] dv_r/dx_q.
   int ns = M.ns;
   std::fill(J, J + ns * ns, 0.0);
-  for (int s = 0; s < ns; ++s) {
-    for (int q = 0; q < ns; ++q) {
-      double acc = 0.0;
-      bool any = false;
-      for (int r = 0; r < M.nr; ++r) {
-        double c = M.net[(size_t)r * ns + s];
-        if (c == 0.0) continue;
-        bool has = false;
-        for (int e = M.rptr[r]; e < M.rptr[r + 1]; ++e) has |= (M.rsp[e] == q);
-        if (!has) continue;
-        acc = acc + c * dvel(M, r, k[r], x, q);
-        any = true;
+  for (int r = 0; r < M.nr; ++r) {
+    const double* net = M.net.data() + (size_t)r * ns;
+    for (int e = M.rptr[r]; e < M.rptr[r + 1]; ++e) {
+      int q = M.rsp[e];
+      double d = dvel(M, r, k[r], x, q);
+      for (int s = 0; s < ns; ++s) {
+        double c = net[s];
+        if (c != 0.0) J[s * ns + q] = J[s * ns + q] + c * d;
       }
-      J[s * ns + q] = any ? acc : 0.0;
     }
   }
 }
@@ -199,27 +197,23 @@ void lu_solve(int n, const double* LU, const double* b, double* x) {
 }
 
 // ------------------------------------------------------------------ fixed reduction tree
-// Level 1: blocks of 1024 cells; thread t (of 256) sums e[b*1024 + t + 256*q], q = 0..3, in
-// order starting from 0.0, then a pairwise tree v[t] += v[t+s] for s = 128, 64, ..., 1.
-// Level 2: one block of 256; thread t sums partial[t + 256*q] for q = 0, 1, ... in order,
-// then the same pairwise tree.  The CUDA kernels reduce with exactly this tree.
+// Level 1: chunks of 256 cells, v[t] = e[b*256 + t] (0.0 past the end), then the pairwise
+// tree v[t] += v[t+s] for s = 128, 64, ..., 1.  Level 2: one chunk of 256 lanes, lane t sums
+// partial[t + 256*q] for q = 0, 1, ... in order from 0.0, then the same tree.  The CUDA
+// kernels reduce with exactly this tree, so the global error norm is bitwise reproducible.
 double tree256(double* v) {
   for (int s = 128; s > 0; s >>= 1)
     for (int t = 0; t < s; ++t) v[t] = v[t] + v[t + s];
   return v[0];
 }
 double reduce_fixed(const double* e, size_t n) {
-  size_t nb = (n + 1023) / 1024;
+  size_t nb = (n + 255) / 256;
   std::vector<double> part(nb);
   for (size_t b = 0; b < nb; ++b) {
     double v[256];
     for (int t = 0; t < 256; ++t) {
-      double acc = 0.0;
-      for (int q = 0; q < 4; ++q) {
-        size_t idx = b * 1024 + t + 256 * q;
-        if (idx < n) acc = acc + e[idx];
-      }
-      v[t] = acc;
+      size_t idx = b * 256 + t;
+      v[t] = idx < n ? e[idx] : 0.0;
     }
     part[b] = tree256(v);
   }

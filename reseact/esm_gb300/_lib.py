@@ -1,0 +1,202 @@
+"""ctypes binding of libreseact_gb300.so -- the same C ABI a Julia ``ccall`` binds.
+
+There is no fallback: if the CUDA library is missing or cannot load, ``load()`` raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi, build
+
+_LIBS = {}
+
+SYMBOLS = [
+    "rs_default_config", "rs_create", "rs_destroy", "rs_last_error", "rs_state_size",
+    "rs_species_per_cell", "rs_set_state", "rs_get_state", "rs_set_forcing",
+    "rs_get_rate_constants", "rs_set_rate_constants", "rs_macro_step", "rs_rhs_transport",
+    "rs_rhs_chem", "rs_block_jac", "rs_single_step", "rs_state_device_ptr", "rs_stream",
+    "rs_set_profiling", "rs_get_profile", "rs_reset_profile",
+]
+
+
+class RsError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s (%s)" % (msg, abi.STATUS_NAMES.get(status, status)))
+        self.status = status
+
+
+def _declare(L):
+    vp, dp, sz = C.c_void_p, C.POINTER(C.c_double), C.c_size_t
+    i32 = C.c_int32
+    L.rs_default_config.argtypes = [C.POINTER(abi.rs_config)]
+    L.rs_create.argtypes = [C.POINTER(abi.rs_config), C.POINTER(vp)]
+    L.rs_create.restype = C.c_int
+    L.rs_destroy.argtypes = [vp]
+    L.rs_last_error.argtypes = [vp]
+    L.rs_last_error.restype = C.c_char_p
+    L.rs_state_size.argtypes = [vp]
+    L.rs_state_size.restype = sz
+    L.rs_species_per_cell.argtypes = [vp]
+    L.rs_species_per_cell.restype = i32
+    for f in ("rs_set_state", "rs_get_state"):
+        getattr(L, f).argtypes = [vp, dp, sz]
+        getattr(L, f).restype = C.c_int
+    L.rs_set_forcing.argtypes = [vp, C.POINTER(abi.rs_forcing)]
+    L.rs_set_forcing.restype = C.c_int
+    for f in ("rs_get_rate_constants", "rs_set_rate_constants"):
+        getattr(L, f).argtypes = [vp, dp, sz]
+        getattr(L, f).restype = C.c_int
+    L.rs_macro_step.argtypes = [vp, C.c_double, C.c_double, dp, dp, C.POINTER(abi.rs_stats)]
+    L.rs_macro_step.restype = C.c_int
+    for f in ("rs_rhs_transport", "rs_rhs_chem"):
+        getattr(L, f).argtypes = [vp, C.c_double, dp, dp, sz]
+        getattr(L, f).restype = C.c_int
+    L.rs_block_jac.argtypes = [vp, dp, dp, sz]
+    L.rs_block_jac.restype = C.c_int
+    L.rs_single_step.argtypes = [vp, i32, C.c_double, C.c_double, dp, dp, dp, sz]
+    L.rs_single_step.restype = C.c_int
+    L.rs_state_device_ptr.argtypes = [vp, C.POINTER(vp)]
+    L.rs_state_device_ptr.restype = C.c_int
+    L.rs_stream.argtypes = [vp]
+    L.rs_stream.restype = vp
+    L.rs_set_profiling.argtypes = [vp, i32]
+    L.rs_set_profiling.restype = C.c_int
+    L.rs_reset_profile.argtypes = [vp]
+    L.rs_reset_profile.restype = C.c_int
+    L.rs_get_profile.argtypes = [vp, C.c_char_p, sz, dp, dp, i32, C.POINTER(i32)]
+    L.rs_get_profile.restype = C.c_int
+    return L
+
+
+def load(strict=False, build_if_missing=True):
+    """Load (building in-tree if needed) the production or strict-arithmetic library."""
+    key = bool(strict)
+    if key in _LIBS:
+        return _LIBS[key]
+    path = build.lib_path(strict)
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError("CUDA library %s is missing; run build()" % path)
+        build.build()
+    _LIBS[key] = _declare(C.CDLL(path))
+    return _LIBS[key]
+
+
+def _p(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Solver:
+    """One rs_handle: a grid + mechanism + forcing resident on the GPU."""
+
+    def __init__(self, config, mech_abi, strict=False):
+        self.L = load(strict)
+        self._keep = [mech_abi]
+        self.cfg = config
+        h = C.c_void_p()
+        rc = self.L.rs_create(C.byref(config), C.byref(h))
+        if rc != abi.RS_OK:
+            raise RsError(rc, self.L.rs_last_error(None).decode())
+        self.h = h
+        self.n = self.L.rs_state_size(h)
+        self.nsp = self.L.rs_species_per_cell(h)
+        g = config.grid
+        self.nlon, self.nlat, self.nlev = g.nlon, g.nlat, g.nlev
+        self.nc = g.nlon * g.nlat * g.nlev
+        self.nr = config.mech.n_reactions
+
+    @classmethod
+    def for_workload(cls, w, strict=False, **cfg_kw):
+        mabi = abi.MechanismABI(w.mech)
+        s = cls(w.config(mabi, **cfg_kw), mabi, strict=strict)
+        s.set_forcing(w.forcing_abi())
+        return s
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.rs_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != abi.RS_OK:
+            raise RsError(rc, self.L.rs_last_error(self.h).decode())
+
+    def set_forcing(self, forcing_abi):
+        self._keep.append(forcing_abi)
+        self._check(self.L.rs_set_forcing(self.h, C.byref(forcing_abi.struct)))
+
+    def set_state(self, u_cellmajor):
+        u = np.ascontiguousarray(u_cellmajor, dtype=np.float64)
+        self._check(self.L.rs_set_state(self.h, _p(u), u.size))
+
+    def get_state(self):
+        u = np.empty(self.n)
+        self._check(self.L.rs_get_state(self.h, _p(u), u.size))
+        return u
+
+    def rates(self):
+        k = np.empty(self.nr * self.nc)
+        self._check(self.L.rs_get_rate_constants(self.h, _p(k), k.size))
+        return k.reshape(self.nr, self.nlev, self.nlat, self.nlon)
+
+    def set_rates(self, k):
+        k = np.ascontiguousarray(k, dtype=np.float64).reshape(-1)
+        self._check(self.L.rs_set_rate_constants(self.h, _p(k), k.size))
+
+    def macro_step(self, t0, t1, dtT, dtC, check=True):
+        a, b = C.c_double(dtT), C.c_double(dtC)
+        st = abi.rs_stats()
+        rc = self.L.rs_macro_step(self.h, t0, t1, C.byref(a), C.byref(b), C.byref(st))
+        if check:
+            self._check(rc)
+        return rc, a.value, b.value, st
+
+    def rhs_transport(self, u, t=0.0):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        du = np.empty_like(u)
+        self._check(self.L.rs_rhs_transport(self.h, t, _p(u), _p(du), u.size))
+        return du
+
+    def rhs_chem(self, u, t=0.0):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        du = np.empty_like(u)
+        self._check(self.L.rs_rhs_chem(self.h, t, _p(u), _p(du), u.size))
+        return du
+
+    def block_jac(self, u):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        J = np.empty(self.nc * self.nsp * self.nsp)
+        self._check(self.L.rs_block_jac(self.h, _p(u), _p(J), J.size))
+        return J.reshape(self.nc, self.nsp, self.nsp)
+
+    def single_step(self, op, u, t, dt):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        un = np.empty_like(u)
+        e = C.c_double()
+        self._check(self.L.rs_single_step(self.h, op, t, dt, _p(u), _p(un), C.byref(e), u.size))
+        return un, e.value
+
+    def stream(self):
+        return self.L.rs_stream(self.h)
+
+    def set_profiling(self, on):
+        self._check(self.L.rs_set_profiling(self.h, int(on)))
+
+    def reset_profile(self):
+        self._check(self.L.rs_reset_profile(self.h))
+
+    def profile(self):
+        buf = C.create_string_buffer(4096)
+        n = C.c_int32()
+        la = np.zeros(64)
+        ms = np.zeros(64)
+        self._check(self.L.rs_get_profile(self.h, buf, 4096, _p(la), _p(ms), 64, C.byref(n)))
+        names = buf.value.decode().split(";") if n.value else []
+        return {nm: (la[i], ms[i]) for i, nm in enumerate(names)}

@@ -67,7 +67,8 @@ class rs_stats(C.Structure):
     _fields_ = [("naT", C.c_double), ("nrT", C.c_double), ("naC", C.c_double),
                 ("nrC", C.c_double), ("dtT_end", C.c_double), ("dtC_end", C.c_double),
                 ("tT_end", C.c_double), ("tC_end", C.c_double),
-                ("chem_cell_steps", C.c_double), ("status", C.c_int32)]
+                ("chem_cell_steps", C.c_double), ("kernel_launches", C.c_double),
+                ("status", C.c_int32)]
 
 
 def pictrl_ros23():

@@ -1,0 +1,994 @@
+// rs_api.cu -- the C ABI of libreseact_gb300.so (declared in include/reseact_gb300.h).
+//
+// Host side only: validates the configuration, derives the sparse mechanism tables, owns all
+// device memory and the CUDA stream, uploads forcing, and drives the device-resident adaptive
+// loops of one Lie-Trotter macro step (transport SSPRK43 then chemistry ROS23 over the same
+// window, op_split.jl:100-164 / run_reseact_reactant.jl:310-355).  No C++ exception crosses
+// the ABI; failures return rs_status and leave their text in rs_last_error.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <map>
+#include <set>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../../include/reseact_gb300.h"
+#include "rs_device.cuh"
+#include "rs_kernels.h"
+
+namespace {
+
+using rs::Ctl;
+
+struct RsError : std::runtime_error {
+  rs_status code;
+  RsError(rs_status c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define CK(call)                                                                        \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      throw RsError(e_ == cudaErrorMemoryAllocation ? RS_ERR_NOMEM : RS_ERR_CUDA,       \
+                    std::string(#call) + ": " + cudaGetErrorString(e_));                \
+  } while (0)
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  void alloc(size_t count) {
+    if (p && n >= count) return;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    if (count == 0) return;
+    CK(cudaMalloc(&p, count * sizeof(T)));
+    n = count;
+  }
+  void upload(const T* h, size_t count, cudaStream_t st) {
+    alloc(count);
+    if (count) CK(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, st));
+  }
+  void zero(cudaStream_t st) {
+    if (p) CK(cudaMemsetAsync(p, 0, n * sizeof(T), st));
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+// ------------------------------------------------------------------ mechanism tables
+struct MechTables {
+  int ns = 0, nr = 0;
+  std::vector<int> rptr, rsp, rnu, rhs_ptr, rhs_r, part_r, part_q, part_e, jac_ptr, jac_slot,
+      jac_diag, jac_part, lu_diag, elim_ptr, elim_lik, upd_ptr, upd_dst, upd_src, low_ptr,
+      low_row, low_slot, up_ptr, up_col, up_slot, prog_ptr, prog_op, slot_row, slot_col;
+  std::vector<double> rhs_c, jac_coef, prog_val, params;
+  int nlu = 0, npart = 0, njac = 0, comb = 0;
+};
+
+MechTables derive_tables(const rs_mechanism& m) {
+  MechTables T;
+  if (m.n_species <= 0 || m.n_reactions < 0) throw RsError(RS_ERR_INVALID, "empty mechanism");
+  if (!m.react_ptr || !m.prod_ptr || !m.prog_ptr) throw RsError(RS_ERR_INVALID, "null tables");
+  T.ns = m.n_species;
+  T.nr = m.n_reactions;
+  T.comb = m.combinatoric;
+  int ns = T.ns, nr = T.nr;
+  T.rptr.assign(m.react_ptr, m.react_ptr + nr + 1);
+  int nre = T.rptr[nr];
+  T.rsp.assign(m.react_species, m.react_species + nre);
+  T.rnu.assign(m.react_nu, m.react_nu + nre);
+  for (int e = 0; e < nre; ++e)
+    if (T.rsp[e] < 0 || T.rsp[e] >= ns || T.rnu[e] < 1 || T.rnu[e] > 8)
+      throw RsError(RS_ERR_INVALID, "bad reactant entry");
+  std::vector<double> net((size_t)nr * ns, 0.0);
+  for (int r = 0; r < nr; ++r) {
+    std::set<int> seen;
+    for (int e = T.rptr[r]; e < T.rptr[r + 1]; ++e) {
+      if (!seen.insert(T.rsp[e]).second)
+        throw RsError(RS_ERR_INVALID, "species repeated among the reactants of one reaction");
+      net[(size_t)r * ns + T.rsp[e]] -= T.rnu[e];
+    }
+    for (int e = m.prod_ptr[r]; e < m.prod_ptr[r + 1]; ++e) {
+      int s = m.prod_species[e];
+      if (s < 0 || s >= ns) throw RsError(RS_ERR_INVALID, "bad product species");
+      net[(size_t)r * ns + s] += m.prod_coef[e];
+    }
+  }
+  // RHS terms per species, reactions ascending
+  T.rhs_ptr.push_back(0);
+  for (int s = 0; s < ns; ++s) {
+    for (int r = 0; r < nr; ++r)
+      if (net[(size_t)r * ns + s] != 0.0) {
+        T.rhs_r.push_back(r);
+        T.rhs_c.push_back(net[(size_t)r * ns + s]);
+      }
+    T.rhs_ptr.push_back((int)T.rhs_r.size());
+  }
+  // partials, reaction order then reactant-entry order
+  for (int r = 0; r < nr; ++r)
+    for (int e = T.rptr[r]; e < T.rptr[r + 1]; ++e) {
+      T.part_r.push_back(r);
+      T.part_q.push_back(T.rsp[e]);
+      T.part_e.push_back(e);
+    }
+  T.npart = (int)T.part_r.size();
+  std::set<std::pair<int, int>> jpat;
+  for (int p = 0; p < T.npart; ++p)
+    for (int s = 0; s < ns; ++s)
+      if (net[(size_t)T.part_r[p] * ns + s] != 0.0) jpat.insert({s, T.part_q[p]});
+  // LU fill of W = I - gamma h J by symbolic pivot-free elimination, natural order
+  std::set<std::pair<int, int>> fill = jpat;
+  for (int i = 0; i < ns; ++i) fill.insert({i, i});
+  for (int k = 0; k < ns; ++k) {
+    std::vector<int> rows, cols;
+    for (int i = k + 1; i < ns; ++i)
+      if (fill.count({i, k})) rows.push_back(i);
+    for (int j = k + 1; j < ns; ++j)
+      if (fill.count({k, j})) cols.push_back(j);
+    for (int i : rows)
+      for (int j : cols) fill.insert({i, j});
+  }
+  std::map<std::pair<int, int>, int> slot;
+  for (auto& e : fill) {  // std::set orders row-major
+    int id = (int)slot.size();
+    slot[e] = id;
+    T.slot_row.push_back(e.first);
+    T.slot_col.push_back(e.second);
+  }
+  T.nlu = (int)slot.size();
+  for (int i = 0; i < ns; ++i) T.lu_diag.push_back(slot[{i, i}]);
+  // Jacobian entries (row-major), terms in partial (= reaction) order
+  T.jac_ptr.push_back(0);
+  for (auto& e : jpat) {
+    int s = e.first, q = e.second;
+    for (int p = 0; p < T.npart; ++p) {
+      double c = net[(size_t)T.part_r[p] * ns + s];
+      if (T.part_q[p] == q && c != 0.0) {
+        T.jac_part.push_back(p);
+        T.jac_coef.push_back(c);
+      }
+    }
+    T.jac_slot.push_back(slot[e]);
+    T.jac_diag.push_back(s == q ? 1 : 0);
+    T.jac_ptr.push_back((int)T.jac_part.size());
+  }
+  T.njac = (int)jpat.size();
+  // elimination schedule
+  T.elim_ptr.push_back(0);
+  T.upd_ptr.push_back(0);
+  for (int k = 0; k < ns; ++k) {
+    std::vector<int> rows, cols;
+    for (int i = k + 1; i < ns; ++i)
+      if (fill.count({i, k})) rows.push_back(i);
+    for (int j = k + 1; j < ns; ++j)
+      if (fill.count({k, j})) cols.push_back(j);
+    for (int i : rows) {
+      T.elim_lik.push_back(slot[{i, k}]);
+      for (int j : cols) {
+        T.upd_dst.push_back(slot[{i, j}]);
+        T.upd_src.push_back(slot[{k, j}]);
+      }
+      T.upd_ptr.push_back((int)T.upd_dst.size());
+    }
+    T.elim_ptr.push_back((int)T.elim_lik.size());
+  }
+  T.low_ptr.push_back(0);
+  for (int k = 0; k < ns; ++k) {
+    for (int i = k + 1; i < ns; ++i)
+      if (fill.count({i, k})) {
+        T.low_row.push_back(i);
+        T.low_slot.push_back(slot[{i, k}]);
+      }
+    T.low_ptr.push_back((int)T.low_row.size());
+  }
+  T.up_ptr.push_back(0);
+  for (int i = 0; i < ns; ++i) {
+    for (int j = i + 1; j < ns; ++j)
+      if (fill.count({i, j})) {
+        T.up_col.push_back(j);
+        T.up_slot.push_back(slot[{i, j}]);
+      }
+    T.up_ptr.push_back((int)T.up_col.size());
+  }
+  // rate programs: validate stack discipline
+  T.prog_ptr.assign(m.prog_ptr, m.prog_ptr + nr + 1);
+  int np = T.prog_ptr[nr];
+  T.prog_op.assign(m.prog_op, m.prog_op + np);
+  T.prog_val.assign(m.prog_val, m.prog_val + np);
+  T.params.assign(m.params ? m.params : nullptr, m.params ? m.params + m.n_params : nullptr);
+  if (T.params.empty()) T.params.push_back(0.0);
+  for (int r = 0; r < nr; ++r) {
+    int sp = 0;
+    for (int e = T.prog_ptr[r]; e < T.prog_ptr[r + 1]; ++e) {
+      int op = T.prog_op[e];
+      if (op <= 3) {
+        ++sp;
+        if (op == 3 && ((int)T.prog_val[e] < 0 || (int)T.prog_val[e] >= m.n_params))
+          throw RsError(RS_ERR_INVALID, "rate program parameter out of range");
+      } else if (op >= 10 && op <= 14) {
+        --sp;
+      } else if (!(op == 15 || (op >= 20 && op <= 23))) {
+        throw RsError(RS_ERR_INVALID, "unknown rate-program opcode");
+      }
+      if (sp < 1 || sp > rs::kMaxProgStack) throw RsError(RS_ERR_INVALID, "rate program stack");
+    }
+    if (sp != 1) throw RsError(RS_ERR_INVALID, "rate program leaves a stack depth != 1");
+  }
+  return T;
+}
+
+// ------------------------------------------------------------------ handle
+struct Profile {
+  std::vector<std::string> names;
+  std::vector<double> launches, ms;
+  struct Pending {
+    int fam;
+    cudaEvent_t a, b;
+  };
+  std::vector<Pending> pending;
+  std::vector<cudaEvent_t> pool;
+  bool on = false;
+};
+
+}  // namespace
+
+struct rs_handle {
+  rs_config cfg{};
+  std::string err;
+  cudaStream_t st = nullptr;
+  int nlon = 0, nlat = 0, nlev = 0, nsp = 0, ntr = 0;
+  size_t nc = 0;
+  MechTables mt;
+  rs::DevMech dm{};
+  rs::LaunchCtx lc{};
+  // mechanism tables on device
+  std::vector<DevBuf<int>> itabs;
+  std::vector<DevBuf<double>> dtabs;
+  DevBuf<int> slot_row, slot_col;
+  // state and scratch
+  DevBuf<double> U[2], S1, S2, S3, fx, fy, fz, partial, krates, T, P, emis, io, io2;
+  DevBuf<double> mx, my, mz, qw, qe, qs, qn, gx, gylo, gyhi, vsA, vsB, veAB, veC, veD, dtcell,
+      stepcell;
+  DevBuf<Ctl> ctl;  // [0] transport, [1] chemistry, [2] single-step scratch
+  DevBuf<int> flag;
+  DevBuf<unsigned long long> queue;
+  Ctl* hctl = nullptr;  // pinned mirror
+  int* hflag = nullptr;
+  int cur = 0;
+  double launches = 0;  // kernels launched by the current rs_macro_step
+  bool have_forcing = false, rates_dirty = true, rates_override = false, have_emis = false;
+  double omega = 0.0;
+  std::vector<double> dp_host;
+  Profile prof;
+  rs::DevTransport<double> dt{};
+};
+
+namespace {
+
+void set_err(rs_handle* h, const std::string& s) {
+  if (h) h->err = s;
+}
+
+// --- profiling helpers: events bracket each launch group while profiling is on
+int fam_id(rs_handle* h, const char* name) {
+  auto& P = h->prof;
+  for (size_t i = 0; i < P.names.size(); ++i)
+    if (P.names[i] == name) return (int)i;
+  P.names.push_back(name);
+  P.launches.push_back(0);
+  P.ms.push_back(0);
+  return (int)P.names.size() - 1;
+}
+cudaEvent_t get_event(rs_handle* h) {
+  auto& P = h->prof;
+  if (!P.pool.empty()) {
+    cudaEvent_t e = P.pool.back();
+    P.pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  CK(cudaEventCreate(&e));
+  return e;
+}
+struct Scope {
+  rs_handle* h;
+  int fam = -1;
+  cudaEvent_t a = nullptr;
+  Scope(rs_handle* hh, const char* name) : h(hh) {
+    if (!h->prof.on) return;
+    fam = fam_id(h, name);
+    a = get_event(h);
+    CK(cudaEventRecord(a, h->st));
+  }
+  ~Scope() {
+    if (fam < 0) return;
+    cudaEvent_t b = get_event(h);
+    cudaEventRecord(b, h->st);
+    h->prof.pending.push_back({fam, a, b});
+  }
+};
+void collect_profile(rs_handle* h) {
+  auto& P = h->prof;
+  if (P.pending.empty()) return;
+  CK(cudaStreamSynchronize(h->st));
+  for (auto& p : P.pending) {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, p.a, p.b));
+    P.launches[p.fam] += 1;
+    P.ms[p.fam] += ms;
+    P.pool.push_back(p.a);
+    P.pool.push_back(p.b);
+  }
+  P.pending.clear();
+}
+
+template <typename T>
+const T* upload_tab(rs_handle* h, std::vector<DevBuf<T>>& store, const std::vector<T>& v) {
+  store.emplace_back();
+  std::vector<T> w = v;
+  if (w.empty()) w.push_back(T(0));
+  store.back().upload(w.data(), w.size(), h->st);
+  return store.back().p;
+}
+
+void build_device_mech(rs_handle* h) {
+  auto& T = h->mt;
+  auto& D = h->dm;
+  auto ui = [&](const std::vector<int>& v) { return upload_tab(h, h->itabs, v); };
+  auto ud = [&](const std::vector<double>& v) { return upload_tab(h, h->dtabs, v); };
+  h->itabs.reserve(40);
+  h->dtabs.reserve(8);
+  D.ns = T.ns;
+  D.nr = T.nr;
+  D.nlu = T.nlu;
+  D.npart = T.npart;
+  D.njac = T.njac;
+  D.rptr = ui(T.rptr); D.rsp = ui(T.rsp); D.rnu = ui(T.rnu);
+  D.rhs_ptr = ui(T.rhs_ptr); D.rhs_r = ui(T.rhs_r); D.rhs_c = ud(T.rhs_c);
+  D.part_r = ui(T.part_r); D.part_q = ui(T.part_q); D.part_e = ui(T.part_e);
+  D.jac_ptr = ui(T.jac_ptr); D.jac_slot = ui(T.jac_slot); D.jac_diag = ui(T.jac_diag);
+  D.jac_part = ui(T.jac_part); D.jac_coef = ud(T.jac_coef);
+  D.lu_diag = ui(T.lu_diag);
+  D.elim_ptr = ui(T.elim_ptr); D.elim_lik = ui(T.elim_lik); D.upd_ptr = ui(T.upd_ptr);
+  D.upd_dst = ui(T.upd_dst); D.upd_src = ui(T.upd_src);
+  D.low_ptr = ui(T.low_ptr); D.low_row = ui(T.low_row); D.low_slot = ui(T.low_slot);
+  D.up_ptr = ui(T.up_ptr); D.up_col = ui(T.up_col); D.up_slot = ui(T.up_slot);
+  D.prog_ptr = ui(T.prog_ptr); D.prog_op = ui(T.prog_op); D.prog_val = ud(T.prog_val);
+  D.params = ud(T.params);
+  D.combinatoric = T.comb;
+  D.ros_d = 1.0 / (2.0 + std::sqrt(2.0));
+  D.ros_c32 = 6.0 + std::sqrt(2.0);
+  h->slot_row.upload(T.slot_row.data(), T.slot_row.size(), h->st);
+  h->slot_col.upload(T.slot_col.data(), T.slot_col.size(), h->st);
+}
+
+// Lat-lon geometry on the unit sphere (same formulas and order as the CPU restatement).
+void build_geometry(rs_handle* h) {
+  const rs_grid& g = h->cfg.grid;
+  const double d2r = 0.017453292519943295;
+  std::vector<double> phie(g.nlat + 1), ce(g.nlat + 1), gx(g.nlat), gl(g.nlat), gh(g.nlat);
+  for (int j = 0; j <= g.nlat; ++j) {
+    double p = g.lat0_deg + (j - 0.5) * g.dlat_deg;
+    p = std::min(90.0, std::max(-90.0, p));
+    phie[j] = p;
+    ce[j] = (std::fabs(p) >= 90.0) ? 0.0 : std::cos(p * d2r);
+  }
+  double dlon = g.dlon_deg * d2r;
+  for (int j = 0; j < g.nlat; ++j) {
+    double dS = std::sin(phie[j + 1] * d2r) - std::sin(phie[j] * d2r);
+    double dphi = (phie[j + 1] - phie[j]) * d2r;
+    gx[j] = dphi / (dlon * dS);
+    gl[j] = ce[j] / dS;
+    gh[j] = ce[j + 1] / dS;
+  }
+  h->gx.upload(gx.data(), gx.size(), h->st);
+  h->gylo.upload(gl.data(), gl.size(), h->st);
+  h->gyhi.upload(gh.data(), gh.size(), h->st);
+}
+
+// CW84 nonuniform coefficients from dp (eqs. 1.6-1.7), mirror ghosts at the no-flux walls.
+void build_vertical(rs_handle* h) {
+  int nlev = h->nlev;
+  size_t ncol = (size_t)h->nlon * h->nlat;
+  std::vector<double> sA((nlev + 2) * ncol), sB((nlev + 2) * ncol), eAB((nlev + 1) * ncol),
+      eC((nlev + 1) * ncol), eD((nlev + 1) * ncol);
+  const std::vector<double>& dp = h->dp_host;
+  auto D = [&](size_t col, int k) {
+    int kk = k < 0 ? -1 - k : (k >= nlev ? 2 * nlev - 1 - k : k);
+    return dp[(size_t)kk * ncol + col];
+  };
+  for (size_t col = 0; col < ncol; ++col) {
+    for (int k = -1; k <= nlev; ++k) {
+      double D0 = D(col, k - 1), D1 = D(col, k), D2 = D(col, k + 1);
+      double c = D1 / (D0 + D1 + D2);
+      sA[(size_t)(k + 1) * ncol + col] = c * (2.0 * D0 + D1) / (D2 + D1);
+      sB[(size_t)(k + 1) * ncol + col] = c * (D1 + 2.0 * D2) / (D0 + D1);
+    }
+    for (int e = 0; e <= nlev; ++e) {
+      int k = e - 1;
+      double Dm = D(col, k - 1), D0 = D(col, k), D1 = D(col, k + 1), D2 = D(col, k + 2);
+      double S = Dm + D0 + D1 + D2;
+      double eA = D0 / (D0 + D1);
+      double t1 = (Dm + D0) / (2.0 * D0 + D1);
+      double t2 = (D2 + D1) / (2.0 * D1 + D0);
+      double eB = (2.0 * D1 * D0 / (D0 + D1)) * (t1 - t2) / S;
+      eAB[(size_t)e * ncol + col] = eA + eB;
+      eC[(size_t)e * ncol + col] = -(D0 * t1) / S;
+      eD[(size_t)e * ncol + col] = D1 * (D1 + D2) / (D0 + 2.0 * D1) / S;
+    }
+  }
+  h->vsA.upload(sA.data(), sA.size(), h->st);
+  h->vsB.upload(sB.data(), sB.size(), h->st);
+  h->veAB.upload(eAB.data(), eAB.size(), h->st);
+  h->veC.upload(eC.data(), eC.size(), h->st);
+  h->veD.upload(eD.data(), eD.size(), h->st);
+}
+
+void refresh_dt(rs_handle* h) {
+  auto& T = h->dt;
+  T.nlon = h->nlon; T.nlat = h->nlat; T.nlev = h->nlev;
+  T.ntr = h->ntr; T.nsp = h->nsp;
+  T.lon_bc = h->cfg.grid.lon_bc; T.lat_bc = h->cfg.grid.lat_bc;
+  T.omega = h->omega;
+  T.gx = h->gx.p; T.gylo = h->gylo.p; T.gyhi = h->gyhi.p;
+  T.mx = h->mx.p; T.my = h->my.p; T.mz = h->mz.p;
+  T.qw = h->qw.p; T.qe = h->qe.p; T.qs = h->qs.p; T.qn = h->qn.p;
+  T.vsA = h->vsA.p; T.vsB = h->vsB.p; T.veAB = h->veAB.p; T.veC = h->veC.p; T.veD = h->veD.p;
+  T.fx = h->fx.p; T.fy = h->fy.p; T.fz = h->fz.p;
+}
+
+Ctl make_ctl(rs_handle* h, double t0, double t1, double dt0, const rs_controller& c,
+             double ntot) {
+  Ctl k{};
+  k.t = t0; k.dt = dt0; k.tend = t1; k.qold = c.qoldinit;
+  k.nacc = 0; k.nrej = 0; k.iters = 0; k.eest = 0; k.maxiters = h->cfg.maxiters;
+  k.beta1 = c.beta1; k.beta2 = c.beta2;
+  k.invqmin = 1.0 / c.qmin; k.invqmax = 1.0 / c.qmax; k.gamma = c.gamma;
+  k.qsmin = c.qsteady_min; k.qsmax = c.qsteady_max; k.qoldinit = c.qoldinit;
+  k.ntot = ntot; k.omega = h->omega;
+  return k;
+}
+
+void ensure_rates(rs_handle* h) {
+  if (!h->rates_dirty || h->rates_override) return;
+  Scope s(h, "rates");
+  rs::launch_rates(h->lc, h->T.p, h->P.p, h->krates.p);
+  CK(cudaGetLastError());
+  h->rates_dirty = false;
+}
+
+// Run the adaptive loop whose controller sits in ctl slot `slot` until it raises done.
+// Attempts are queued in growing batches; every attempt kernel is a no-op once done is set,
+// so only the batch boundary needs a host check of the pinned flag.
+template <class Attempt>
+void run_adaptive(rs_handle* h, int slot, Attempt attempt) {
+  Ctl* dctl = h->ctl.p + slot;
+  int batch = 1;
+  double launched = 0;
+  for (;;) {
+    for (int b = 0; b < batch; ++b) attempt(dctl);
+    launched += batch;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(&h->hctl[slot], dctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    if (h->hctl[slot].done) break;
+    if (launched > h->cfg.maxiters + 8) break;  // safety: the device loop is capped by maxiters
+    if (!h->prof.on) batch = std::min(batch * 2, 64);
+  }
+}
+
+void transport_attempt(rs_handle* h, Ctl* c) {
+  rs::TransportBufs B{h->U[0].p, h->U[1].p, h->S1.p, h->S2.p, h->S3.p, h->partial.p};
+  {
+    Scope s(h, "ssprk43_stages");
+    rs::launch_ssprk43_attempt(h->st, h->dt, c, B, h->cfg.rtol_T, h->cfg.atol_T,
+                               h->cfg.clamp_nonneg);
+  }
+  Scope s(h, "finalize");
+  rs::launch_finalize(h->st, c, h->partial.p, (int)((h->nc + 255) / 256));
+  h->launches += 17;
+}
+
+void chem_attempt(rs_handle* h, Ctl* c) {
+  {
+    Scope s(h, "ros23_attempt");
+    rs::launch_ros23_attempt(h->lc, c, h->U[0].p, h->U[1].p, h->krates.p,
+                             h->have_emis ? h->emis.p : nullptr, h->partial.p, h->cfg.rtol_C,
+                             h->cfg.atol_C, h->cfg.clamp_nonneg);
+  }
+  Scope s(h, "finalize");
+  rs::launch_finalize(h->st, c, h->partial.p, (int)((h->nc + 255) / 256));
+  h->launches += 2;
+}
+
+rs_status guard(rs_handle* h, const std::function<void()>& fn);
+
+}  // namespace
+
+// ====================================================================== C ABI
+extern "C" {
+
+void rs_default_config(rs_config* c) {
+  if (!c) return;
+  std::memset(c, 0, sizeof(*c));
+  c->api_version = RS_API_VERSION;
+  c->has_air_mass = 1;
+  c->do_transport = 1;
+  c->do_chemistry = 1;
+  c->rtol_T = 1e-4; c->atol_T = 1e-6;
+  c->rtol_C = 1e-4; c->atol_C = 1e-9;
+  c->ctrl_T = {7.0 / 30.0, 2.0 / 15.0, 1.0 / 5.0, 10.0, 9.0 / 10.0, 1.0, 1.0, 1e-4};
+  c->ctrl_C = {7.0 / 20.0, 1.0 / 5.0, 1.0 / 5.0, 10.0, 9.0 / 10.0, 1.0, 6.0 / 5.0, 1e-4};
+  c->maxiters = 2.0e4;
+  c->clamp_nonneg = 1;
+  c->precision = RS_PREC_FP64;
+  c->chem_mode = RS_CHEM_GLOBAL_DT;
+  c->grid.lon_bc = RS_BC_PERIODIC;
+  c->grid.lat_bc = RS_BC_CLOSED;
+}
+
+}  // extern "C"
+
+namespace {
+rs_status guard(rs_handle* h, const std::function<void()>& fn) {
+  try {
+    fn();
+    return RS_OK;
+  } catch (const RsError& e) {
+    set_err(h, e.what());
+    return e.code;
+  } catch (const std::exception& e) {
+    set_err(h, e.what());
+    return RS_ERR_INVALID;
+  } catch (...) {
+    set_err(h, "unknown error");
+    return RS_ERR_INVALID;
+  }
+}
+thread_local std::string g_create_err;
+}  // namespace
+
+extern "C" {
+
+rs_status rs_create(const rs_config* cfg, rs_handle** out) {
+  if (!cfg || !out) return RS_ERR_INVALID;
+  *out = nullptr;
+  rs_handle* h = new rs_handle();
+  rs_status st = guard(h, [&] {
+    if (cfg->api_version != RS_API_VERSION) throw RsError(RS_ERR_INVALID, "api_version mismatch");
+    h->cfg = *cfg;
+    const rs_grid& g = cfg->grid;
+    if (g.nlon < 1 || g.nlat < 1 || g.nlev < 1) throw RsError(RS_ERR_INVALID, "grid size");
+    if (cfg->do_transport) {
+      if (!cfg->has_air_mass) throw RsError(RS_ERR_INVALID, "transport needs the air-mass species");
+      if (g.nlat < 3 || g.nlev < 3 || g.nlon < 3)
+        throw RsError(RS_ERR_INVALID, "transport needs nlon, nlat, nlev >= 3");
+      if (cfg->precision != RS_PREC_FP64)
+        throw RsError(RS_ERR_UNSUPPORTED, "only the FP64 transport build is available");
+    }
+    if (cfg->maxiters < 1) throw RsError(RS_ERR_INVALID, "maxiters");
+    CK(cudaSetDevice(cfg->device));
+    CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+    h->mt = derive_tables(cfg->mech);
+    auto& T = h->mt;
+    int cls = -1;
+    if (T.ns <= rs::kSmallMS && T.nr <= rs::kSmallMR && T.nlu <= rs::kSmallMLU &&
+        T.npart <= rs::kSmallMP)
+      cls = 0;
+    else if (T.ns <= rs::kLargeMS && T.nr <= rs::kLargeMR && T.nlu <= rs::kLargeMLU &&
+             T.npart <= rs::kLargeMP)
+      cls = 1;
+    if (cls < 0) throw RsError(RS_ERR_UNSUPPORTED, "mechanism exceeds the kernel capacities");
+    h->nlon = g.nlon; h->nlat = g.nlat; h->nlev = g.nlev;
+    h->nc = (size_t)g.nlon * g.nlat * g.nlev;
+    if (h->nc > (size_t)0x7fffffff) throw RsError(RS_ERR_INVALID, "too many cells");
+    h->nsp = T.ns + (cfg->has_air_mass ? 1 : 0);
+    h->ntr = T.ns;
+    build_device_mech(h);
+    h->lc = rs::LaunchCtx{h->st, h->dm, (int)h->nc, h->nsp, cls};
+    size_t n = h->nc * h->nsp;
+    h->U[0].alloc(n); h->U[1].alloc(n);
+    h->U[0].zero(h->st); h->U[1].zero(h->st);
+    h->partial.alloc((h->nc + 255) / 256 + 1);
+    h->krates.alloc(std::max<size_t>(1, (size_t)T.nr * h->nc));
+    h->krates.zero(h->st);
+    h->ctl.alloc(3);
+    h->ctl.zero(h->st);
+    h->flag.alloc(1);
+    h->queue.alloc(1);
+    CK(cudaMallocHost(&h->hctl, 3 * sizeof(Ctl)));
+    CK(cudaMallocHost(&h->hflag, sizeof(int)));
+    if (cfg->chem_mode == RS_CHEM_PER_CELL) {
+      h->dtcell.alloc(h->nc);
+      h->dtcell.zero(h->st);
+      h->stepcell.alloc(h->nc);
+    }
+    if (cfg->do_transport) {
+      h->S1.alloc(n); h->S2.alloc(n); h->S3.alloc(n);
+      h->fx.alloc((size_t)h->ntr * g.nlev * g.nlat * (g.nlon + 1));
+      h->fy.alloc((size_t)h->ntr * g.nlev * (g.nlat + 1) * g.nlon);
+      h->fz.alloc((size_t)h->ntr * (g.nlev + 1) * g.nlat * g.nlon);
+      h->mx.alloc((size_t)g.nlev * g.nlat * (g.nlon + 1)); h->mx.zero(h->st);
+      h->my.alloc((size_t)g.nlev * (g.nlat + 1) * g.nlon); h->my.zero(h->st);
+      h->mz.alloc((size_t)(g.nlev + 1) * g.nlat * g.nlon); h->mz.zero(h->st);
+      h->qw.alloc((size_t)h->ntr * g.nlev * g.nlat); h->qw.zero(h->st);
+      h->qe.alloc((size_t)h->ntr * g.nlev * g.nlat); h->qe.zero(h->st);
+      h->qs.alloc((size_t)h->ntr * g.nlev * g.nlon); h->qs.zero(h->st);
+      h->qn.alloc((size_t)h->ntr * g.nlev * g.nlon); h->qn.zero(h->st);
+      build_geometry(h);
+      h->dp_host.assign(h->nc, 1.0);
+      build_vertical(h);
+    }
+    refresh_dt(h);
+    CK(cudaStreamSynchronize(h->st));
+  });
+  if (st != RS_OK) {
+    g_create_err = h->err;
+    rs_destroy(h);
+    return st;
+  }
+  *out = h;
+  return RS_OK;
+}
+
+void rs_destroy(rs_handle* h) {
+  if (!h) return;
+  if (h->st) cudaStreamSynchronize(h->st);
+  for (auto& b : h->itabs) b.release();
+  for (auto& b : h->dtabs) b.release();
+  DevBuf<double>* bufs[] = {&h->U[0], &h->U[1], &h->S1, &h->S2, &h->S3, &h->fx, &h->fy, &h->fz,
+                            &h->partial, &h->krates, &h->T, &h->P, &h->emis, &h->io, &h->io2,
+                            &h->mx, &h->my, &h->mz, &h->qw, &h->qe, &h->qs, &h->qn, &h->gx,
+                            &h->gylo, &h->gyhi, &h->vsA, &h->vsB, &h->veAB, &h->veC, &h->veD,
+                            &h->dtcell, &h->stepcell};
+  for (auto* b : bufs) b->release();
+  h->slot_row.release();
+  h->slot_col.release();
+  h->ctl.release();
+  h->flag.release();
+  h->queue.release();
+  if (h->hctl) cudaFreeHost(h->hctl);
+  if (h->hflag) cudaFreeHost(h->hflag);
+  for (auto& p : h->prof.pending) {
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  for (auto e : h->prof.pool) cudaEventDestroy(e);
+  if (h->st) cudaStreamDestroy(h->st);
+  delete h;
+}
+
+const char* rs_last_error(const rs_handle* h) {
+  return h ? h->err.c_str() : g_create_err.c_str();
+}
+
+size_t rs_state_size(const rs_handle* h) { return h ? h->nc * h->nsp : 0; }
+int32_t rs_species_per_cell(const rs_handle* h) { return h ? h->nsp : 0; }
+void* rs_stream(rs_handle* h) { return h ? (void*)h->st : nullptr; }
+
+rs_status rs_set_state(rs_handle* h, const double* u, size_t n) {
+  if (!h || !u) return RS_ERR_INVALID;
+  return guard(h, [&] {
+    if (n != h->nc * h->nsp) throw RsError(RS_ERR_INVALID, "state size mismatch");
+    Scope s(h, "h2d_state");
+    h->io.upload(u, n, h->st);
+    rs::launch_to_soa(h->st, h->io.p, h->U[h->cur].p, h->nlon, h->nlat, h->nlev, h->nsp);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(h->st));
+  });
+}
+
+rs_status rs_get_state(rs_handle* h, double* u, size_t n) {
+  if (!h || !u) return RS_ERR_INVALID;
+  return guard(h, [&] {
+    if (n != h->nc * h->nsp) throw RsError(RS_ERR_INVALID, "state size mismatch");
+    Scope s(h, "d2h_state");
+    h->io.alloc(n);
+    rs::launch_to_cellmajor(h->st, h->U[h->cur].p, h->io.p, h->nlon, h->nlat, h->nlev, h->nsp);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(u, h->io.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+  });
+}
+
+rs_status rs_state_device_ptr(rs_handle* h, void** d) {
+  if (!h || !d) return RS_ERR_INVALID;
+  *d = h->U[h->cur].p;
+  return RS_OK;
+}
+
+rs_status rs_set_forcing(rs_handle* h, const rs_forcing* f) {
+  if (!h || !f) return RS_ERR_INVALID;
+  return guard(h, [&] {
+    const rs_grid& g = h->cfg.grid;
+    cudaStream_t st = h->st;
+    size_t nc = h->nc;
+    if (h->cfg.do_transport) {
+      if (f->mx) h->mx.upload(f->mx, (size_t)g.nlev * g.nlat * (g.nlon + 1), st);
+      if (f->my) h->my.upload(f->my, (size_t)g.nlev * (g.nlat + 1) * g.nlon, st);
+      if (f->mz) h->mz.upload(f->mz, (size_t)(g.nlev + 1) * g.nlat * g.nlon, st);
+      if (f->qbc_w) h->qw.upload(f->qbc_w, (size_t)h->ntr * g.nlev * g.nlat, st);
+      if (f->qbc_e) h->qe.upload(f->qbc_e, (size_t)h->ntr * g.nlev * g.nlat, st);
+      if (f->qbc_s) h->qs.upload(f->qbc_s, (size_t)h->ntr * g.nlev * g.nlon, st);
+      if (f->qbc_n) h->qn.upload(f->qbc_n, (size_t)h->ntr * g.nlev * g.nlon, st);
+      if (f->dp) {
+        for (size_t c = 0; c < nc; ++c)
+          if (!(f->dp[c] > 0.0)) throw RsError(RS_ERR_INVALID, "dp must be positive");
+        h->dp_host.assign(f->dp, f->dp + nc);
+        build_vertical(h);
+      }
+      h->omega = f->flux_omega;
+    }
+    if (f->temperature) {
+      h->T.upload(f->temperature, nc, st);
+      h->rates_dirty = true;
+      h->rates_override = false;
+    }
+    if (f->pressure) {
+      h->P.upload(f->pressure, nc, st);
+      h->rates_dirty = true;
+      h->rates_override = false;
+    }
+    if (f->emission) {
+      h->emis.upload(f->emission, (size_t)h->mt.ns * nc, st);
+      h->have_emis = true;
+    }
+    h->have_forcing = true;
+    refresh_dt(h);
+    CK(cudaStreamSynchronize(st));
+  });
+}
+
+rs_status rs_get_rate_constants(rs_handle* h, double* k, size_t n) {
+  if (!h || !k) return RS_ERR_INVALID;
+  return guard(h, [&] {
+    if (n != (size_t)h->mt.nr * h->nc) throw RsError(RS_ERR_INVALID, "rate array size");
+    ensure_rates(h);
+    CK(cudaMemcpyAsync(k, h->krates.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+  });
+}
+
+rs_status rs_set_rate_constants(rs_handle* h, const double* k, size_t n) {
+  if (!h || !k) return RS_ERR_INVALID;
+  return guard(h, [&] {
+    if (n != (size_t)h->mt.nr * h->nc) throw RsError(RS_ERR_INVALID, "rate array size");
+    h->krates.upload(k, n, h->st);
+    h->rates_dirty = false;
+    h->rates_override = true;
+    CK(cudaStreamSynchronize(h->st));
+  });
+}
+
+rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double* dtC,
+                        rs_stats* out) {
+  if (!h || !dtT || !dtC) return RS_ERR_INVALID;
+  rs_stats stats{};
+  rs_status rc = guard(h, [&] {
+    if (!(t1 > t0)) throw RsError(RS_ERR_INVALID, "t1 must exceed t0");
+    if (!(*dtT > 0.0) || !(*dtC > 0.0)) throw RsError(RS_ERR_INVALID, "dt must be positive");
+    h->launches = 0;
+    if (h->rates_dirty && !h->rates_override) h->launches += 1;
+    ensure_rates(h);
+    double ntot = (double)h->nc * h->nsp;
+    bool okT = true, okC = true;
+    stats.dtT_end = *dtT;
+    stats.dtC_end = *dtC;
+    stats.tT_end = t1;
+    stats.tC_end = t1;
+    if (h->cfg.do_transport) {
+      Ctl init = make_ctl(h, t0, t1, *dtT, h->cfg.ctrl_T, ntot);
+      init.cur = h->cur;
+      rs::launch_ctl_init(h->st, h->ctl.p + 0, init);
+      h->launches += 1;
+      run_adaptive(h, 0, [&](Ctl* c) { transport_attempt(h, c); });
+      const Ctl& c = h->hctl[0];
+      h->cur = c.cur;
+      stats.naT = c.nacc; stats.nrT = c.nrej; stats.dtT_end = c.dt; stats.tT_end = c.t;
+      okT = c.t >= t1 - 1e-9;
+      *dtT = c.dt;
+    }
+    if (h->cfg.do_chemistry && okT) {
+      if (h->cfg.chem_mode == RS_CHEM_GLOBAL_DT) {
+        Ctl init = make_ctl(h, t0, t1, *dtC, h->cfg.ctrl_C, ntot);
+        init.cur = h->cur;
+        rs::launch_ctl_init(h->st, h->ctl.p + 1, init);
+        h->launches += 1;
+        run_adaptive(h, 1, [&](Ctl* c) { chem_attempt(h, c); });
+        const Ctl& c = h->hctl[1];
+        h->cur = c.cur;
+        stats.naC = c.nacc; stats.nrC = c.nrej; stats.dtC_end = c.dt; stats.tC_end = c.t;
+        okC = c.t >= t1 - 1e-9;
+        *dtC = c.dt;
+      } else {
+        const rs_controller& c = h->cfg.ctrl_C;
+        rs::PerCellArgs a{t0, t1, *dtC, h->cfg.rtol_C, h->cfg.atol_C, h->cfg.maxiters,
+                          c.beta1, c.beta2, 1.0 / c.qmin, 1.0 / c.qmax, c.gamma,
+                          c.qsteady_min, c.qsteady_max, c.qoldinit, h->cfg.clamp_nonneg};
+        CK(cudaMemsetAsync(h->queue.p, 0, sizeof(unsigned long long), h->st));
+        CK(cudaMemsetAsync(h->flag.p, 0, sizeof(int), h->st));
+        int dev = 0, nsm = 0;
+        CK(cudaGetDevice(&dev));
+        CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        int nblocks = std::max(1, std::min(nsm * 4, (int)((h->nc + 127) / 128)));
+        {
+          Scope s(h, "chem_per_cell");
+          rs::launch_chem_per_cell(h->lc, nblocks, h->U[h->cur].p, h->krates.p,
+                                   h->have_emis ? h->emis.p : nullptr, h->dtcell.p,
+                                   h->stepcell.p, h->queue.p, h->flag.p, a);
+        }
+        h->launches += 1;
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(h->hflag, h->flag.p, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+        CK(cudaStreamSynchronize(h->st));
+        okC = *h->hflag == 0;
+        stats.chem_cell_steps = -1;  // filled by rs_per_cell_steps when requested
+      }
+    }
+    collect_profile(h);
+    if (!okT || !okC) throw RsError(RS_ERR_MAXITERS, "adaptive solve stopped before t1 (maxiters)");
+    CK(cudaMemsetAsync(h->flag.p, 0, sizeof(int), h->st));
+    rs::launch_nonfinite(h->st, h->U[h->cur].p, h->nc * h->nsp, h->flag.p);
+    h->launches += 1;
+    CK(cudaMemcpyAsync(h->hflag, h->flag.p, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    if (*h->hflag) throw RsError(RS_ERR_NONFINITE, "non-finite state after the macro step");
+  });
+  stats.status = rc;
+  stats.kernel_launches = h->launches;
+  if (out) *out = stats;
+  return rc;
+}
+
+rs_status rs_rhs_transport(rs_handle* h, double t, const double* u, double* du, size_t n) {
+  if (!h || !u || !du) return RS_ERR_INVALID;
+  return guard(h, [&] {
+    if (!h->cfg.do_transport) throw RsError(RS_ERR_STATE, "transport disabled");
+    if (n != h->nc * h->nsp) throw RsError(RS_ERR_INVALID, "state size mismatch");
+    h->io.upload(u, n, h->st);
+    h->io2.alloc(n);
+    rs::launch_to_soa(h->st, h->io.p, h->S1.p, h->nlon, h->nlat, h->nlev, h->nsp);
+    double g = h->omega != 0.0 ? std::cos(h->omega * t) : 1.0;
+    rs::launch_transport_rhs(h->st, h->dt, h->S1.p, g, h->S2.p);
+    rs::launch_to_cellmajor(h->st, h->S2.p, h->io2.p, h->nlon, h->nlat, h->nlev, h->nsp);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(du, h->io2.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+  });
+}
+
+rs_status rs_rhs_chem(rs_handle* h, double t, const double* u, double* du, size_t n) {
+  (void)t;
+  if (!h || !u || !du) return RS_ERR_INVALID;
+  return guard(h, [&] {
+    if (n != h->nc * h->nsp) throw RsError(RS_ERR_INVALID, "state size mismatch");
+    ensure_rates(h);
+    h->io.upload(u, n, h->st);
+    h->io2.alloc(2 * n);
+    double* soa = h->io2.p;
+    double* dsoa = h->io2.p + n;
+    rs::launch_to_soa(h->st, h->io.p, soa, h->nlon, h->nlat, h->nlev, h->nsp);
+    rs::launch_chem_rhs(h->lc, soa, h->krates.p, h->have_emis ? h->emis.p : nullptr, dsoa);
+    rs::launch_to_cellmajor(h->st, dsoa, h->io.p, h->nlon, h->nlat, h->nlev, h->nsp);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(du, h->io.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+  });
+}
+
+rs_status rs_block_jac(rs_handle* h, const double* u, double* J, size_t n_jac) {
+  if (!h || !u || !J) return RS_ERR_INVALID;
+  return guard(h, [&] {
+    size_t n = h->nc * h->nsp;
+    if (n_jac != h->nc * h->nsp * h->nsp) throw RsError(RS_ERR_INVALID, "jacobian size");
+    ensure_rates(h);
+    h->io.upload(u, n, h->st);
+    h->io2.alloc(n + n_jac);
+    double* soa = h->io2.p;
+    double* dJ = h->io2.p + n;
+    rs::launch_to_soa(h->st, h->io.p, soa, h->nlon, h->nlat, h->nlev, h->nsp);
+    rs::launch_block_jac(h->lc, soa, h->krates.p, h->slot_row.p, h->slot_col.p, dJ);
+    CK(cudaGetLastError());
+    // device J is [grid cell][r][s]; reorder to the cell-major cell index on the host
+    std::vector<double> tmp(n_jac);
+    CK(cudaMemcpyAsync(tmp.data(), dJ, n_jac * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    size_t bs = (size_t)h->nsp * h->nsp;
+    for (int k = 0; k < h->nlev; ++k)
+      for (int j = 0; j < h->nlat; ++j)
+        for (int i = 0; i < h->nlon; ++i) {
+          size_t gcell = ((size_t)k * h->nlat + j) * h->nlon + i;
+          size_t ccell = ((size_t)i * h->nlat + j) * h->nlev + k;
+          std::memcpy(J + ccell * bs, tmp.data() + gcell * bs, bs * sizeof(double));
+        }
+  });
+}
+
+rs_status rs_single_step(rs_handle* h, int32_t op, double t, double dt, const double* u_in,
+                         double* u_out, double* eest, size_t n) {
+  if (!h || !u_in || !u_out) return RS_ERR_INVALID;
+  return guard(h, [&] {
+    if (n != h->nc * h->nsp) throw RsError(RS_ERR_INVALID, "state size mismatch");
+    if (!(dt > 0.0)) throw RsError(RS_ERR_INVALID, "dt must be positive");
+    if (op == RS_OP_TRANSPORT && !h->cfg.do_transport) throw RsError(RS_ERR_STATE, "transport disabled");
+    if (op != RS_OP_TRANSPORT && op != RS_OP_CHEMISTRY) throw RsError(RS_ERR_INVALID, "op");
+    ensure_rates(h);
+    const rs_controller& cc = op == RS_OP_TRANSPORT ? h->cfg.ctrl_T : h->cfg.ctrl_C;
+    Ctl init = make_ctl(h, t, t + dt, dt, cc, (double)n);
+    init.cur = 0;
+    init.maxiters = 1.0;
+    h->io.upload(u_in, n, h->st);
+    h->io2.alloc(2 * n);
+    double* a = h->io2.p;
+    double* b = h->io2.p + n;
+    rs::launch_to_soa(h->st, h->io.p, a, h->nlon, h->nlat, h->nlev, h->nsp);
+    rs::launch_ctl_init(h->st, h->ctl.p + 2, init);
+    Ctl* c = h->ctl.p + 2;
+    if (op == RS_OP_TRANSPORT) {
+      rs::TransportBufs B{a, b, h->S1.p, h->S2.p, h->S3.p, h->partial.p};
+      rs::launch_ssprk43_attempt(h->st, h->dt, c, B, h->cfg.rtol_T, h->cfg.atol_T, 0);
+    } else {
+      rs::launch_ros23_attempt(h->lc, c, a, b, h->krates.p, h->have_emis ? h->emis.p : nullptr,
+                               h->partial.p, h->cfg.rtol_C, h->cfg.atol_C, 0);
+    }
+    rs::launch_finalize(h->st, c, h->partial.p, (int)((h->nc + 255) / 256));
+    rs::launch_to_cellmajor(h->st, b, h->io.p, h->nlon, h->nlat, h->nlev, h->nsp);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(u_out, h->io.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaMemcpyAsync(&h->hctl[2], c, sizeof(Ctl), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    if (eest) *eest = h->hctl[2].eest;
+  });
+}
+
+rs_status rs_set_profiling(rs_handle* h, int32_t on) {
+  if (!h) return RS_ERR_INVALID;
+  return guard(h, [&] {
+    collect_profile(h);
+    h->prof.on = on != 0;
+  });
+}
+
+rs_status rs_reset_profile(rs_handle* h) {
+  if (!h) return RS_ERR_INVALID;
+  return guard(h, [&] {
+    collect_profile(h);
+    std::fill(h->prof.launches.begin(), h->prof.launches.end(), 0.0);
+    std::fill(h->prof.ms.begin(), h->prof.ms.end(), 0.0);
+  });
+}
+
+rs_status rs_get_profile(rs_handle* h, char* buf, size_t buf_len, double* launches,
+                         double* total_ms, int32_t max_kernels, int32_t* n_out) {
+  if (!h) return RS_ERR_INVALID;
+  return guard(h, [&] {
+    collect_profile(h);
+    auto& P = h->prof;
+    std::string names;
+    int n = std::min<int>((int)P.names.size(), max_kernels);
+    for (int i = 0; i < n; ++i) {
+      if (i) names += ";";
+      names += P.names[i];
+      if (launches) launches[i] = P.launches[i];
+      if (total_ms) total_ms[i] = P.ms[i];
+    }
+    if (buf && buf_len) {
+      std::strncpy(buf, names.c_str(), buf_len - 1);
+      buf[buf_len - 1] = 0;
+    }
+    if (n_out) *n_out = n;
+  });
+}
+
+}  // extern "C"

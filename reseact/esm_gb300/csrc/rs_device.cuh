@@ -1,0 +1,217 @@
+// rs_device.cuh -- device-side building blocks shared by the chemistry and transport kernels.
+//
+// Arithmetic order contract: every floating-point expression below associates exactly like the
+// CPU restatement of the reference (ROS23 rx_traced_integrator.jl:279-349, blocksolve :110-135,
+// SSPRK43 :362-400, hairer norm :329-347), so the strict build (--fmad=false, RS_STRICT)
+// reproduces it bit for bit given the same rate constants; the fast build differs only by FMA
+// contraction and by multiplying with precomputed reciprocals where the reference divides.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#ifndef RS_STRICT
+#define RS_STRICT 0
+#endif
+
+namespace rs {
+
+constexpr int kRedThreads = 256;  // fixed reduction chunk (cells per level-1 partial)
+
+// ------------------------------------------------------------------ mechanism tables
+// Derived on the host from rs_mechanism (rs_mech.cpp); all index arrays are warp-uniform
+// reads (every thread walks the same table), served by the L1/texture path.
+struct DevMech {
+  int ns, nr, nlu, npart, njac;
+  const int* rptr;      // [nr+1] reactant entries of reaction r
+  const int* rsp;       // reactant species
+  const int* rnu;       // reactant stoichiometry
+  const int* rhs_ptr;   // [ns+1] RHS terms of species s (reactions ascending)
+  const int* rhs_r;
+  const double* rhs_c;
+  const int* part_r;    // partial p = d v_{part_r} / d x_{part_q}
+  const int* part_q;
+  const int* part_e;    // reactant entry index of the partial
+  const int* jac_ptr;   // [njac+1] terms of Jacobian entry e
+  const int* jac_slot;  // LU slot of entry e
+  const int* jac_diag;  // 1 if entry e is on the diagonal
+  const int* jac_part;
+  const double* jac_coef;
+  const int* lu_diag;   // [ns] slot of (i,i)
+  const int* elim_ptr;  // [ns+1] per pivot k: range of (i,k) multipliers
+  const int* elim_lik;  // slot of (i,k)
+  const int* upd_ptr;   // [n_elim+1] per multiplier: range of updates
+  const int* upd_dst;
+  const int* upd_src;
+  const int* low_ptr;   // [ns+1] forward solve, column k: rows i>k
+  const int* low_row;
+  const int* low_slot;
+  const int* up_ptr;    // [ns+1] backward solve, row i: columns j>i ascending
+  const int* up_col;
+  const int* up_slot;
+  const int* prog_ptr;  // rate programs
+  const int* prog_op;
+  const double* prog_val;
+  const double* params;
+  int combinatoric;     // 1: divide k by prod(nu!) (entry by entry, as the oracle does)
+  double ros_d;         // ROS23 d = 1/(2+sqrt(2))  (rx_traced_integrator.jl:256)
+  double ros_c32;       // ROS23 c32 = 6+sqrt(2)    (rx_traced_integrator.jl:257)
+};
+
+// ------------------------------------------------------------------ controller state
+// One per adaptive solve, resident in device memory: the host launches attempts, the
+// finalize kernel applies the PI controller (rx_traced_integrator.jl:480-505) and raises
+// `done`; every attempt kernel returns immediately once `done` is set.
+struct Ctl {
+  double t, dt, tend, qold, nacc, nrej, iters, dtc, eest, maxiters;
+  double beta1, beta2, invqmin, invqmax, gamma, qsmin, qsmax, qoldinit;
+  double ntot;     // number of states in the norm
+  double omega;    // flux time factor g(t) = cos(omega t)
+  double g[4];     // SSPRK43 stage factors of the next attempt: t, t+dt/2, t+dt, t+dt/2
+  int cur;         // state buffer holding the accepted state (0/1)
+  int done;
+  int accept;
+  int pad;
+};
+
+__device__ __forceinline__ double ld(const double* p) { return __ldg(p); }
+__device__ __forceinline__ int ldi(const int* p) { return __ldg(p); }
+
+// ------------------------------------------------------------------ chemistry core
+// v_r = k_r * prod x^nu over the reactant entries, in table order
+__device__ __forceinline__ void velocities(const DevMech& M, const double* k, const double* x,
+                                           double* v) {
+  for (int r = 0; r < M.nr; ++r) {
+    double a = k[r];
+    int e1 = ldi(M.rptr + r + 1);
+    for (int e = ldi(M.rptr + r); e < e1; ++e) {
+      double xs = x[ldi(M.rsp + e)];
+      int nu = ldi(M.rnu + e);
+      for (int t = 0; t < nu; ++t) a = a * xs;
+    }
+    v[r] = a;
+  }
+}
+
+// f_s = sum_r net[r,s] v_r (+ emission)
+__device__ __forceinline__ void rhs_from_v(const DevMech& M, const double* v, const double* emis,
+                                           double* f) {
+  for (int s = 0; s < M.ns; ++s) {
+    double acc = 0.0;
+    int e1 = ldi(M.rhs_ptr + s + 1);
+    for (int e = ldi(M.rhs_ptr + s); e < e1; ++e) acc = acc + ld(M.rhs_c + e) * v[ldi(M.rhs_r + e)];
+    f[s] = emis ? acc + emis[s] : acc;
+  }
+}
+
+// partial derivatives d v_r / d x_q
+__device__ __forceinline__ void partials(const DevMech& M, const double* k, const double* x,
+                                         double* P) {
+  for (int p = 0; p < M.npart; ++p) {
+    int r = ldi(M.part_r + p), q = ldi(M.part_q + p);
+    double d = k[r];
+    int e1 = ldi(M.rptr + r + 1);
+    for (int e = ldi(M.rptr + r); e < e1; ++e) {
+      int s = ldi(M.rsp + e), nu = ldi(M.rnu + e);
+      double xs = x[s];
+      if (s == q) {
+        if (nu >= 2) {
+          double f = (double)nu;
+          for (int t = 1; t < nu; ++t) f = f * xs;
+          d = d * f;
+        }
+      } else {
+        for (int t = 0; t < nu; ++t) d = d * xs;
+      }
+    }
+    P[p] = d;
+  }
+}
+
+// W = I - dtgamma * J on the LU fill pattern (W[r,s] = (r==s ? 1.0 : 0.0) - dtgamma*J[r,s])
+__device__ __forceinline__ void build_w(const DevMech& M, const double* P, double dtgamma,
+                                        double* W) {
+  for (int e = 0; e < M.nlu; ++e) W[e] = 0.0;
+  for (int i = 0; i < M.ns; ++i) W[ldi(M.lu_diag + i)] = 1.0;
+  for (int e = 0; e < M.njac; ++e) {
+    double acc = 0.0;
+    int t1 = ldi(M.jac_ptr + e + 1);
+    for (int t = ldi(M.jac_ptr + e); t < t1; ++t)
+      acc = acc + ld(M.jac_coef + t) * P[ldi(M.jac_part + t)];
+    double tmp = dtgamma * acc;
+    W[ldi(M.jac_slot + e)] = (ldi(M.jac_diag + e) ? 1.0 : 0.0) - tmp;
+  }
+}
+
+// Pivot-free sparse LU in natural order (the elimination of blocksolve, zero updates skipped);
+// L multipliers overwrite their slots, piv[k] = 1 / U[k,k].
+__device__ __forceinline__ void lu_factor(const DevMech& M, double* W, double* piv) {
+  int m = 0;
+  for (int k = 0; k < M.ns; ++k) {
+    double pk = 1.0 / W[ldi(M.lu_diag + k)];
+    piv[k] = pk;
+    int i1 = ldi(M.elim_ptr + k + 1);
+    for (int ii = ldi(M.elim_ptr + k); ii < i1; ++ii, ++m) {
+      int sl = ldi(M.elim_lik + ii);
+      double mult = W[sl] * pk;
+      int u1 = ldi(M.upd_ptr + m + 1);
+      for (int u = ldi(M.upd_ptr + m); u < u1; ++u) {
+        int dst = ldi(M.upd_dst + u);
+        double mw = mult * W[ldi(M.upd_src + u)];
+        W[dst] = W[dst] - mw;
+      }
+      W[sl] = mult;
+    }
+  }
+}
+
+// Solve (LU) x = b in place (b -> x): forward replay of the multipliers, then back
+// substitution x_i = (b_i - sum_{j>i} U_ij x_j) / U_ii.
+__device__ __forceinline__ void lu_solve(const DevMech& M, const double* W, const double* piv,
+                                         double* b) {
+  for (int k = 0; k < M.ns; ++k) {
+    double bk = b[k];
+    int e1 = ldi(M.low_ptr + k + 1);
+    for (int e = ldi(M.low_ptr + k); e < e1; ++e) {
+      int i = ldi(M.low_row + e);
+      double mb = W[ldi(M.low_slot + e)] * bk;
+      b[i] = b[i] - mb;
+    }
+  }
+  for (int i = M.ns - 1; i >= 0; --i) {
+    double acc = b[i];
+    int e1 = ldi(M.up_ptr + i + 1);
+    for (int e = ldi(M.up_ptr + i); e < e1; ++e) {
+      double wx = W[ldi(M.up_slot + e)] * b[ldi(M.up_col + e)];
+      acc = acc - wx;
+    }
+#if RS_STRICT
+    b[i] = acc / W[ldi(M.lu_diag + i)];
+#else
+    b[i] = acc * piv[i];
+#endif
+  }
+}
+
+// ------------------------------------------------------------------ fixed-tree reductions
+// Pairwise tree over 256 lanes: v[t] += v[t+s] for s = 128 ... 1 (identical to the CPU
+// restatement's tree256).  Returns the total in thread 0.
+__device__ __forceinline__ double block_tree256(double v, double* sm) {
+  int t = threadIdx.x;
+  sm[t] = v;
+  __syncthreads();
+  for (int s = 128; s >= 32; s >>= 1) {
+    if (t < s) sm[t] = sm[t] + sm[t + s];
+    __syncthreads();
+  }
+  double a = sm[t];
+  if (t < 32) {
+    for (int s = 16; s > 0; s >>= 1) {
+      double o = __shfl_down_sync(0xffffffffu, a, s);
+      if (t < s) a = a + o;
+    }
+  }
+  __syncthreads();
+  return a;
+}
+
+}  // namespace rs

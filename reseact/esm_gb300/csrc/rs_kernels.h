@@ -1,0 +1,94 @@
+// rs_kernels.h -- host-visible launch interface of the device kernels (no CUDA types beyond
+// cudaStream_t cross it, so the C-ABI layer in rs_api.cpp stays plain C++).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+#include "rs_device.cuh"
+
+namespace rs {
+
+// Per-thread work-array capacities of the two chemistry kernel instantiations.
+constexpr int kSmallMS = 16, kSmallMR = 40, kSmallMLU = 160, kSmallMP = 80;
+constexpr int kLargeMS = 64, kLargeMR = 128, kLargeMLU = 1600, kLargeMP = 256;
+constexpr int kMaxProgStack = 32;
+
+struct LaunchCtx {
+  cudaStream_t stream;
+  DevMech mech;
+  int nc;          // cells
+  int nsp;         // species per cell in the state (chemistry species + air mass)
+  int size_class;  // 0 small, 1 large
+};
+
+struct PerCellArgs {
+  double t0, t1, dt0, rtol, atol, maxiters;
+  double beta1, beta2, invqmin, invqmax, gamma, qsmin, qsmax, qoldinit;
+  int clamp;
+};
+
+// Transport geometry and forcing on the device (grid SoA, lon fastest).
+template <typename R>
+struct DevTransport {
+  int nlon, nlat, nlev, ntr, nsp, lon_bc, lat_bc;
+  double omega;
+  const double* gx;    // [nlat]
+  const double* gylo;  // [nlat]
+  const double* gyhi;  // [nlat]
+  const double* mx;    // [nlev][nlat][nlon+1]
+  const double* my;    // [nlev][nlat+1][nlon]
+  const double* mz;    // [nlev+1][nlat][nlon]
+  const double* qw;    // [ntr][nlev][nlat]
+  const double* qe;
+  const double* qs;    // [ntr][nlev][nlon]
+  const double* qn;
+  const double* vsA;   // [(nlev+2)][ncol] slope coefficients, cells -1..nlev
+  const double* vsB;
+  const double* veAB;  // [(nlev+1)][ncol] edge coefficients, edges 0..nlev
+  const double* veC;
+  const double* veD;
+  R* fx;               // [ntr][nlev][nlat][nlon+1]
+  R* fy;               // [ntr][nlev][nlat+1][nlon]
+  R* fz;               // [ntr][nlev+1][nlat][nlon]
+};
+
+// chemistry (rs_chem.cu)
+void launch_rates(const LaunchCtx& L, const double* T, const double* P, double* kr);
+void launch_ros23_attempt(const LaunchCtx& L, const Ctl* ctl, double* U0, double* U1,
+                          const double* kr, const double* em, double* part, double rtol,
+                          double atol, int clamp);
+void launch_chem_rhs(const LaunchCtx& L, const double* U, const double* kr, const double* em,
+                     double* dU);
+void launch_block_jac(const LaunchCtx& L, const double* U, const double* kr, const int* srow,
+                      const int* scol, double* J);
+void launch_chem_per_cell(const LaunchCtx& L, int nblocks, double* U, const double* kr,
+                          const double* em, double* dtc, double* steps,
+                          unsigned long long* queue, int* status, const PerCellArgs& a);
+
+// transport (rs_transport.cu).  Stage s in 1..4 of one SSPRK43 attempt; buffers:
+// U0/U1 accepted/candidate (selected by ctl->cur), S1..S3 stage scratch.
+struct TransportBufs {
+  double* U0;
+  double* U1;
+  double* S1;
+  double* S2;
+  double* S3;
+  double* partial;
+};
+void launch_ssprk43_attempt(cudaStream_t st, const DevTransport<double>& T, const Ctl* ctl,
+                            const TransportBufs& B, double rtol, double atol, int clamp);
+// du = f_transport(u) with flux time factor g for a grid-SoA state (single evaluation hook)
+void launch_transport_rhs(cudaStream_t st, const DevTransport<double>& T, const double* U,
+                          double g, double* dU);
+
+// control (rs_control.cu)
+void launch_ctl_init(cudaStream_t st, Ctl* ctl, const Ctl& init);
+void launch_finalize(cudaStream_t st, Ctl* ctl, const double* partial, int nparts);
+void launch_nonfinite(cudaStream_t st, const double* U, size_t n, int* flag);
+void launch_to_soa(cudaStream_t st, const double* cm, double* soa, int nlon, int nlat, int nlev,
+                   int nsp);
+void launch_to_cellmajor(cudaStream_t st, const double* soa, double* cm, int nlon, int nlat,
+                         int nlev, int nsp);
+
+}  // namespace rs

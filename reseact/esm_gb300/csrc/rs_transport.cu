@@ -1,0 +1,417 @@
+// rs_transport.cu -- SSPRK43 flux-form transport: monotone PPM face fluxes and the stage kernel.
+//
+// Transport RHS (CWC mixing-ratio form of reseact.esm:2083, continuity reseact.esm:1535):
+//   dq/dt = ( -(Dx(Mx q) + Dy(My q) + Dz(Mz q)) + q * (Dx Mx + Dy My + Dz Mz) ) / m
+//   dm/dt = -(Dx Mx + Dy My + Dz Mz)
+// with finite-volume divergences on the unit sphere (Dx = (F_e - F_w) dphi/(dlon dS),
+// Dy = (F_n cos phi_n - F_s cos phi_s)/dS, Dz = F_top - F_bottom) and face values from the
+// upwind cell's CW84-limited parabola (eqs. 1.6-1.8, 1.10; nonuniform-dp form vertically).
+// At q == 1 every slope is 0, every face value is exactly 1 and each tracer flux equals the
+// air-mass flux bit for bit, so dq/dt == 0 exactly (the CWC freestream gate of
+// prototypes/transport_3d/transport_3d.esm and tools/cwc_gate.jl).
+//
+// SSPRK43 attempt (rx_traced_integrator.jl:362-400): 4 stages, each = 3 face-flux kernels
+// (x, y, z) + 1 stage kernel; the 4th stage kernel also forms the embedded error and the
+// fixed-tree partial sums of the hairer norm.
+#include <cuda_runtime.h>
+
+#include "rs_device.cuh"
+#include "rs_kernels.h"
+
+namespace rs {
+
+constexpr double kOneSixth = 1.0 / 6.0;
+constexpr int kFluxThreads = 256;
+
+__device__ __forceinline__ double slope_u(double am, double a, double ap) {
+  double d0 = a - am, d1 = ap - a;
+  if (d1 * d0 > 0.0) {
+    double da = 0.5 * (ap - am);
+    double lim = fmin(2.0 * fabs(d0), 2.0 * fabs(d1));
+    return copysign(fmin(fabs(da), lim), da);
+  }
+  return 0.0;
+}
+__device__ __forceinline__ double slope_n(double am, double a, double ap, double sA, double sB) {
+  double d0 = a - am, d1 = ap - a;
+  if (d1 * d0 > 0.0) {
+    double da = sA * d1 + sB * d0;
+    double lim = fmin(2.0 * fabs(d0), 2.0 * fabs(d1));
+    return copysign(fmin(fabs(da), lim), da);
+  }
+  return 0.0;
+}
+__device__ __forceinline__ void limit(double a, double& aL, double& aR) {
+  if ((aR - a) * (a - aL) <= 0.0) {
+    aL = a;
+    aR = a;
+  } else {
+    double dA = aR - aL;
+    double a6 = 6.0 * (a - 0.5 * (aL + aR));
+    if (dA * a6 > dA * dA) aL = 3.0 * a - 2.0 * aR;
+    else if (-(dA * dA) > dA * a6) aR = 3.0 * a - 2.0 * aL;
+  }
+}
+__device__ __forceinline__ double ppm_face_u(const double* v, bool right) {
+  double dm1 = slope_u(v[0], v[1], v[2]);
+  double d0 = slope_u(v[1], v[2], v[3]);
+  double dp1 = slope_u(v[2], v[3], v[4]);
+  double aL = v[1] + 0.5 * (v[2] - v[1]) - (d0 - dm1) * kOneSixth;
+  double aR = v[2] + 0.5 * (v[3] - v[2]) - (dp1 - d0) * kOneSixth;
+  limit(v[2], aL, aR);
+  return right ? aR : aL;
+}
+
+// Stage input selection: inside an adaptive attempt the field and the time factor come from
+// the device-resident controller (input U[cur] for stage 1, S1/S2/S3 for stages 2-4, g from
+// ctl->g[stage-1]); for a single RHS evaluation they are given directly.
+struct StageSel {
+  const Ctl* ctl;
+  int stage;
+  const double* U0;
+  const double* U1;
+  const double* S1;
+  const double* S2;
+  const double* S3;
+  const double* Q;  // direct evaluation
+  double g;
+};
+__device__ __forceinline__ bool resolve_stage(const StageSel& s, const double*& Q, double& g) {
+  if (!s.ctl) {
+    Q = s.Q;
+    g = s.g;
+    return true;
+  }
+  if (s.ctl->done) return false;
+  g = s.ctl->g[s.stage - 1];
+  Q = s.stage == 1 ? (s.ctl->cur ? s.U1 : s.U0)
+                   : (s.stage == 2 ? s.S1 : (s.stage == 3 ? s.S2 : s.S3));
+  return true;
+}
+
+// ------------------------------------------------------------------ face fluxes
+// x faces: (i_f in 0..nlon, j, k), i_f fastest
+__global__ void __launch_bounds__(kFluxThreads) k_flux_x(DevTransport<double> T, StageSel sel) {
+  const double* Q;
+  double g;
+  if (!resolve_stage(sel, Q, g)) return;
+  const int nf = T.nlon + 1;
+  long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long total = (long long)nf * T.nlat * T.nlev;
+  if (idx >= total) return;
+  int i = (int)(idx % nf);
+  int j = (int)((idx / nf) % T.nlat);
+  int k = (int)(idx / ((long long)nf * T.nlat));
+  const size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
+  const size_t row = ((size_t)k * T.nlat + j) * T.nlon;
+  double M = g * T.mx[((size_t)k * T.nlat + j) * nf + i];
+  bool right = M > 0.0;
+  int up = right ? i - 1 : i;
+  int ii[5];
+  bool ghost[5];
+  for (int o = 0; o < 5; ++o) {
+    int q = up - 2 + o;
+    ghost[o] = false;
+    if (q < 0 || q >= T.nlon) {
+      if (T.lon_bc == 0) q = ((q % T.nlon) + T.nlon) % T.nlon;
+      else ghost[o] = true;
+    }
+    ii[o] = q;
+  }
+  for (int s = 0; s < T.ntr; ++s) {
+    const double* q = Q + (size_t)s * nc + row;
+    double v[5];
+    for (int o = 0; o < 5; ++o) {
+      if (ghost[o]) {
+        const double* b = ii[o] < 0 ? T.qw : T.qe;
+        v[o] = b[((size_t)s * T.nlev + k) * T.nlat + j];
+      } else {
+        v[o] = q[ii[o]];
+      }
+    }
+    T.fx[((size_t)s * T.nlev * T.nlat + (size_t)k * T.nlat + j) * nf + i] = M * ppm_face_u(v, right);
+  }
+}
+
+// y faces: (i, j_f in 0..nlat, k), i fastest
+__global__ void __launch_bounds__(kFluxThreads) k_flux_y(DevTransport<double> T, StageSel sel) {
+  const double* Q;
+  double g;
+  if (!resolve_stage(sel, Q, g)) return;
+  const int nf = T.nlat + 1;
+  long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long total = (long long)T.nlon * nf * T.nlev;
+  if (idx >= total) return;
+  int i = (int)(idx % T.nlon);
+  int j = (int)((idx / T.nlon) % nf);
+  int k = (int)(idx / ((long long)T.nlon * nf));
+  const size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
+  const size_t fbase = ((size_t)k * nf + j) * T.nlon + i;
+  const size_t fplane = (size_t)T.nlev * nf * T.nlon;
+  if (T.lat_bc != 1 && (j == 0 || j == T.nlat)) {
+    for (int s = 0; s < T.ntr; ++s) T.fy[(size_t)s * fplane + fbase] = 0.0;
+    return;
+  }
+  double M = g * T.my[fbase];
+  bool right = M > 0.0;
+  int up = right ? j - 1 : j;
+  int jj[5];
+  bool ghost[5];
+  for (int o = 0; o < 5; ++o) {
+    int q = up - 2 + o;
+    ghost[o] = false;
+    if (q < 0 || q >= T.nlat) {
+      if (T.lat_bc == 1) ghost[o] = true;
+      else q = q < 0 ? -1 - q : 2 * T.nlat - 1 - q;
+    }
+    jj[o] = q;
+  }
+  for (int s = 0; s < T.ntr; ++s) {
+    const double* q = Q + (size_t)s * nc + (size_t)k * T.nlat * T.nlon + i;
+    double v[5];
+    for (int o = 0; o < 5; ++o) {
+      if (ghost[o]) {
+        const double* b = jj[o] < 0 ? T.qs : T.qn;
+        v[o] = b[((size_t)s * T.nlev + k) * T.nlon + i];
+      } else {
+        v[o] = q[(size_t)jj[o] * T.nlon];
+      }
+    }
+    T.fy[(size_t)s * fplane + fbase] = M * ppm_face_u(v, right);
+  }
+}
+
+// z faces: (i, j, k_f in 0..nlev), i fastest; nonuniform (dp-weighted) CW84 reconstruction
+__global__ void __launch_bounds__(kFluxThreads) k_flux_z(DevTransport<double> T, StageSel sel) {
+  const double* Q;
+  double g;
+  if (!resolve_stage(sel, Q, g)) return;
+  const int nf = T.nlev + 1;
+  const size_t ncol = (size_t)T.nlon * T.nlat;
+  long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long total = (long long)ncol * nf;
+  if (idx >= total) return;
+  size_t col = (size_t)(idx % (long long)ncol);
+  int kf = (int)(idx / (long long)ncol);
+  const size_t nc = ncol * T.nlev;
+  const size_t fplane = ncol * nf;
+  if (kf == 0 || kf == T.nlev) {
+    for (int s = 0; s < T.ntr; ++s) T.fz[(size_t)s * fplane + (size_t)kf * ncol + col] = 0.0;
+    return;
+  }
+  double M = g * T.mz[(size_t)kf * ncol + col];
+  bool right = M > 0.0;
+  int up = right ? kf - 1 : kf;
+  int kk[5];
+  for (int o = 0; o < 5; ++o) {
+    int q = up - 2 + o;
+    kk[o] = q < 0 ? -1 - q : (q >= T.nlev ? 2 * T.nlev - 1 - q : q);
+  }
+  // coefficient rows: slope cells up-1..up+1 (stored from cell -1), edges up and up+1
+  double sA0 = T.vsA[(size_t)(up) * ncol + col], sB0 = T.vsB[(size_t)(up) * ncol + col];
+  double sA1 = T.vsA[(size_t)(up + 1) * ncol + col], sB1 = T.vsB[(size_t)(up + 1) * ncol + col];
+  double sA2 = T.vsA[(size_t)(up + 2) * ncol + col], sB2 = T.vsB[(size_t)(up + 2) * ncol + col];
+  double eLab = T.veAB[(size_t)up * ncol + col], eLc = T.veC[(size_t)up * ncol + col],
+         eLd = T.veD[(size_t)up * ncol + col];
+  double eRab = T.veAB[(size_t)(up + 1) * ncol + col], eRc = T.veC[(size_t)(up + 1) * ncol + col],
+         eRd = T.veD[(size_t)(up + 1) * ncol + col];
+  for (int s = 0; s < T.ntr; ++s) {
+    const double* q = Q + (size_t)s * nc + col;
+    double v[5];
+    for (int o = 0; o < 5; ++o) v[o] = q[(size_t)kk[o] * ncol];
+    double dm1 = slope_n(v[0], v[1], v[2], sA0, sB0);
+    double d0 = slope_n(v[1], v[2], v[3], sA1, sB1);
+    double dp1 = slope_n(v[2], v[3], v[4], sA2, sB2);
+    double aL = v[1] + eLab * (v[2] - v[1]) + eLc * d0 + eLd * dm1;
+    double aR = v[2] + eRab * (v[3] - v[2]) + eRc * dp1 + eRd * d0;
+    limit(v[2], aL, aR);
+    T.fz[(size_t)s * fplane + (size_t)kf * ncol + col] = M * (right ? aR : aL);
+  }
+}
+
+// ------------------------------------------------------------------ stage kernel
+// Divergence of the air-mass flux at cell (i,j,k) at time factor g.
+struct CellGeo {
+  double gx, gylo, gyhi;
+};
+__device__ __forceinline__ double div_m(const DevTransport<double>& T, int i, int j, int k,
+                                        double g, const CellGeo& G) {
+  const int nf = T.nlon + 1;
+  const size_t ncol = (size_t)T.nlon * T.nlat, col = (size_t)j * T.nlon + i;
+  double mxw = g * T.mx[((size_t)k * T.nlat + j) * nf + i];
+  double mxe = g * T.mx[((size_t)k * T.nlat + j) * nf + i + 1];
+  double mys = (T.lat_bc != 1 && j == 0) ? 0.0
+             : g * T.my[((size_t)k * (T.nlat + 1) + j) * T.nlon + i];
+  double myn = (T.lat_bc != 1 && j + 1 == T.nlat) ? 0.0
+             : g * T.my[((size_t)k * (T.nlat + 1) + j + 1) * T.nlon + i];
+  double mzb = (k == 0) ? 0.0 : g * T.mz[(size_t)k * ncol + col];
+  double mzt = (k + 1 == T.nlev) ? 0.0 : g * T.mz[(size_t)(k + 1) * ncol + col];
+  double DxM = (mxe - mxw) * G.gx;
+  double DyM = myn * G.gyhi - mys * G.gylo;
+  double DzM = mzt - mzb;
+  return (DxM + DyM) + DzM;
+}
+
+// stage in 1..4.  Qin: the field whose fluxes were computed (RHS argument).
+//   1: S1 = U + dt/2 f(U)           2: S2 = S1 + dt/2 f(S1)
+//   3: S1 = u3 = S2 + dt/2 f(S2), S3 = u4 = 2/3 U + 1/3 u3
+//   4: unew = S3 + dt/2 f(S3); err = 1/2 (1/3 U + 2/3 u3 - unew); candidate = clamp(unew)
+template <int STAGE>
+__global__ void __launch_bounds__(kRedThreads) k_stage(DevTransport<double> T,
+                                                       const Ctl* __restrict__ ctl,
+                                                       TransportBufs B, double rtol,
+                                                       double atol, int clamp) {
+  __shared__ double sm[kRedThreads];
+  if (ctl->done) return;
+  const double g = ctl->g[STAGE - 1];
+  const int cur = ctl->cur;
+  const double* U = cur ? B.U1 : B.U0;
+  double* Un = cur ? B.U0 : B.U1;
+  const double dt = ctl->dtc;
+  const double dt_2 = dt / 2;
+  const double* Qin = STAGE == 1 ? U : (STAGE == 2 ? B.S1 : (STAGE == 3 ? B.S2 : B.S3));
+  const size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
+  size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double e = 0.0;
+  if (c < nc) {
+    int i = (int)(c % T.nlon);
+    int j = (int)((c / T.nlon) % T.nlat);
+    int k = (int)(c / ((size_t)T.nlon * T.nlat));
+    CellGeo G{T.gx[j], T.gylo[j], T.gyhi[j]};
+    double divM = div_m(T, i, j, k, g, G);
+    double m = Qin[(size_t)(T.nsp - 1) * nc + c];
+#if !RS_STRICT
+    double rm = 1.0 / m;
+#endif
+    const int nfx = T.nlon + 1, nfy = T.nlat + 1;
+    const size_t ncol = (size_t)T.nlon * T.nlat, col = (size_t)j * T.nlon + i;
+    const size_t fxp = (size_t)T.nlev * T.nlat * nfx, fyp = (size_t)T.nlev * nfy * T.nlon,
+                 fzp = ncol * (T.nlev + 1);
+    const size_t fxi = ((size_t)k * T.nlat + j) * nfx + i;
+    const size_t fyi = ((size_t)k * nfy + j) * T.nlon + i;
+    const size_t fzi = (size_t)k * ncol + col;
+    for (int s = 0; s < T.nsp; ++s) {
+      size_t x = (size_t)s * nc + c;
+      double q = Qin[x];
+      double du;
+      if (s < T.ntr) {
+        double fw = T.fx[s * fxp + fxi], fe = T.fx[s * fxp + fxi + 1];
+        double fs = T.fy[s * fyp + fyi], fn = T.fy[s * fyp + fyi + T.nlon];
+        double fb = T.fz[s * fzp + fzi], ft = T.fz[s * fzp + fzi + ncol];
+        double Dx = (fe - fw) * G.gx;
+        double Dy = fn * G.gyhi - fs * G.gylo;
+        double Dz = ft - fb;
+        double a = -((Dx + Dy) + Dz);
+        double b = q * divM;
+#if RS_STRICT
+        du = (a + b) / m;
+#else
+        du = (a + b) * rm;
+#endif
+      } else {
+        du = -divM;
+      }
+      if (STAGE == 1) {
+        B.S1[x] = q + dt_2 * du;
+      } else if (STAGE == 2) {
+        B.S2[x] = q + dt_2 * du;
+      } else if (STAGE == 3) {
+        double u3 = q + dt_2 * du;
+        double u0 = U[x];
+        B.S1[x] = u3;
+        B.S3[x] = (2.0 / 3.0) * u0 + (1.0 / 3.0) * u3;
+      } else {
+        double u0 = U[x];
+        double u3 = B.S1[x];
+        double ut = (1.0 / 3.0) * u0 + (2.0 / 3.0) * u3;
+        double un = q + dt_2 * du;
+        double err = 0.5 * (ut - un);
+        double am = fmax(fabs(u0), fabs(un));
+        double den = am * rtol + atol;
+        double at = err / den;
+        e = e + at * at;
+        Un[x] = clamp ? fmax(un, 0.0) : un;
+      }
+    }
+  }
+  if (STAGE == 4) {
+    double tot = block_tree256(e, sm);
+    if (threadIdx.x == 0) B.partial[blockIdx.x] = tot;
+  }
+}
+
+// Plain RHS evaluation for the rs_rhs_transport hook: du = f(U) at time factor g.
+__global__ void __launch_bounds__(kRedThreads) k_rhs_eval(DevTransport<double> T,
+                                                          const double* __restrict__ Qin,
+                                                          double* __restrict__ dU, double g) {
+  const size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
+  size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  int i = (int)(c % T.nlon);
+  int j = (int)((c / T.nlon) % T.nlat);
+  int k = (int)(c / ((size_t)T.nlon * T.nlat));
+  CellGeo G{T.gx[j], T.gylo[j], T.gyhi[j]};
+  double divM = div_m(T, i, j, k, g, G);
+  const bool has_m = T.nsp > T.ntr;
+  double m = has_m ? Qin[(size_t)(T.nsp - 1) * nc + c] : 1.0;
+  const int nfx = T.nlon + 1, nfy = T.nlat + 1;
+  const size_t ncol = (size_t)T.nlon * T.nlat, col = (size_t)j * T.nlon + i;
+  const size_t fxp = (size_t)T.nlev * T.nlat * nfx, fyp = (size_t)T.nlev * nfy * T.nlon,
+               fzp = ncol * (T.nlev + 1);
+  const size_t fxi = ((size_t)k * T.nlat + j) * nfx + i;
+  const size_t fyi = ((size_t)k * nfy + j) * T.nlon + i;
+  const size_t fzi = (size_t)k * ncol + col;
+  for (int s = 0; s < T.nsp; ++s) {
+    size_t x = (size_t)s * nc + c;
+    if (s < T.ntr) {
+      double fw = T.fx[s * fxp + fxi], fe = T.fx[s * fxp + fxi + 1];
+      double fs = T.fy[s * fyp + fyi], fn = T.fy[s * fyp + fyi + T.nlon];
+      double fb = T.fz[s * fzp + fzi], ft = T.fz[s * fzp + fzi + ncol];
+      double Dx = (fe - fw) * G.gx;
+      double Dy = fn * G.gyhi - fs * G.gylo;
+      double Dz = ft - fb;
+      double a = -((Dx + Dy) + Dz);
+      double b = Qin[x] * divM;
+      dU[x] = has_m ? (a + b) / m : a + b;
+    } else {
+      dU[x] = -divM;
+    }
+  }
+}
+
+static void launch_fluxes(cudaStream_t st, const DevTransport<double>& T, const StageSel& sel) {
+  long long nx = (long long)(T.nlon + 1) * T.nlat * T.nlev;
+  long long ny = (long long)T.nlon * (T.nlat + 1) * T.nlev;
+  long long nz = (long long)T.nlon * T.nlat * (T.nlev + 1);
+  k_flux_x<<<(unsigned)((nx + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);
+  k_flux_y<<<(unsigned)((ny + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);
+  k_flux_z<<<(unsigned)((nz + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);
+}
+
+void launch_ssprk43_attempt(cudaStream_t st, const DevTransport<double>& T, const Ctl* ctl,
+                            const TransportBufs& B, double rtol, double atol, int clamp) {
+  size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
+  unsigned nb = (unsigned)((nc + kRedThreads - 1) / kRedThreads);
+  StageSel sel{ctl, 1, B.U0, B.U1, B.S1, B.S2, B.S3, nullptr, 1.0};
+  launch_fluxes(st, T, sel);
+  k_stage<1><<<nb, kRedThreads, 0, st>>>(T, ctl, B, rtol, atol, clamp);
+  sel.stage = 2;
+  launch_fluxes(st, T, sel);
+  k_stage<2><<<nb, kRedThreads, 0, st>>>(T, ctl, B, rtol, atol, clamp);
+  sel.stage = 3;
+  launch_fluxes(st, T, sel);
+  k_stage<3><<<nb, kRedThreads, 0, st>>>(T, ctl, B, rtol, atol, clamp);
+  sel.stage = 4;
+  launch_fluxes(st, T, sel);
+  k_stage<4><<<nb, kRedThreads, 0, st>>>(T, ctl, B, rtol, atol, clamp);
+}
+
+void launch_transport_rhs(cudaStream_t st, const DevTransport<double>& T, const double* U,
+                          double g, double* dU) {
+  StageSel sel{nullptr, 0, nullptr, nullptr, nullptr, nullptr, nullptr, U, g};
+  launch_fluxes(st, T, sel);
+  size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
+  k_rhs_eval<<<(unsigned)((nc + kRedThreads - 1) / kRedThreads), kRedThreads, 0, st>>>(T, U, dU, g);
+}
+
+}  // namespace rs

@@ -368,12 +368,15 @@ def superfast(combinatoric=False):
 
 # --------------------------------------------------------------------------- synthetic
 def synthetic(n_species=30, n_reactions=60, seed=20240503, k_lo=1e-6, k_hi=1e2, c_ref=1e-9):
-    """Seeded synthetic mass-action mechanism (uni- and bimolecular).
+    """Seeded synthetic mass-action mechanism (uni- and bimolecular), non-explosive.
 
     Rate constants at 298 K are log-uniform in [k_lo, k_hi] s^-1 (first-order equivalent:
     bimolecular constants are divided by the reference concentration ``c_ref`` so that
     k2*c_ref spans the same range); each gets an Arrhenius temperature factor
     exp(B*(1/T - 1/298)) with B uniform in [-1500, 500] K.  Concentrations are in mol/mol.
+    Product coefficients of every reaction sum to at most its reactant count (A -> B,
+    A -> 0.5 B + 0.5 C, A + B -> C, A + B -> C + D, 2A -> B ...), so total moles never grow:
+    no chain branching, bounded trajectories, stiffness from the 1e8 spread of rates alone.
     """
     rng = np.random.default_rng(seed)
     names = [f"S{i:02d}" for i in range(n_species)]
@@ -384,19 +387,25 @@ def synthetic(n_species=30, n_reactions=60, seed=20240503, k_lo=1e-6, k_hi=1e2, 
         reac = [(a, 1)]
         if bimol:
             b = int(rng.integers(n_species))
-            if b == a:
-                reac = [(a, 2)]
-            else:
-                reac.append((b, 1))
-        nprod = int(rng.integers(1, 3))
-        prods = []
+            reac = [(a, 2)] if b == a else [(a, 1), (b, 1)]
+        n_in = 2 if bimol else 1
         used = {s for s, _ in reac}
-        for _ in range(nprod):
+
+        def pick():
             p = int(rng.integers(n_species))
             while p in used:
                 p = int(rng.integers(n_species))
             used.add(p)
-            prods.append((p, float(rng.choice([0.5, 1.0, 1.0, 1.0, 2.0]))))
+            return p
+
+        shape = int(rng.integers(3))
+        if shape == 0:
+            prods = [(pick(), 1.0)]
+        elif shape == 1:
+            prods = [(pick(), 0.5 * n_in), (pick(), 0.5 * n_in)] if n_in == 1 else \
+                [(pick(), 1.0), (pick(), 1.0)]
+        else:
+            prods = [(pick(), float(n_in))]
         k298 = 10.0 ** rng.uniform(math.log10(k_lo), math.log10(k_hi))
         if bimol:
             k298 /= c_ref

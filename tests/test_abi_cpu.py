@@ -1,0 +1,59 @@
+"""C-ABI checks that need no GPU: the library builds and loads, exports every symbol the
+public header declares, host-only entry points behave, and without a CUDA device the product
+path fails loudly (there is no CPU fallback)."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from reseact.esm_gb300 import _lib, abi, mechanism, workloads
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_symbols():
+    txt = open(os.path.join(ROOT, "include", "reseact_gb300.h")).read()
+    decl = r"^(?:rs_status|void|const char\*|size_t|int32_t|void\*)\s+\*?(rs_[a-z_]+)\s*\("
+    return sorted(set(re.findall(decl, txt, flags=re.M)))
+
+
+@pytest.mark.parametrize("strict", [False, True])
+def test_library_exports_header_symbols(strict):
+    L = _lib.load(strict)
+    syms = header_symbols()
+    assert len(syms) >= 20
+    for s in syms:
+        assert hasattr(L, s), s
+    assert set(syms) == set(_lib.SYMBOLS)
+
+
+def test_default_config_matches_reference_constants():
+    L = _lib.load()
+    cfg = abi.rs_config()
+    L.rs_default_config(C.byref(cfg))
+    assert cfg.api_version == abi.RS_API_VERSION
+    assert (cfg.rtol_T, cfg.atol_T, cfg.rtol_C, cfg.atol_C) == (1e-4, 1e-6, 1e-4, 1e-9)
+    assert cfg.ctrl_C.beta1 == 7 / 20 and cfg.ctrl_C.beta2 == 1 / 5 and cfg.ctrl_C.qsteady_max == 6 / 5
+    assert cfg.ctrl_T.beta1 == 7 / 30 and cfg.ctrl_T.beta2 == 2 / 15 and cfg.ctrl_T.qsteady_max == 1.0
+    assert cfg.maxiters == 2e4 and cfg.clamp_nonneg == 1
+    ref = abi.pictrl_ros23()
+    assert [getattr(ref, f) for f, _ in abi.rs_controller._fields_] == \
+        [getattr(cfg.ctrl_C, f) for f, _ in abi.rs_controller._fields_]
+
+
+def test_create_fails_loudly_without_gpu():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    w = workloads.c1()
+    with pytest.raises(_lib.RsError) as ei:
+        _lib.Solver.for_workload(w)
+    assert ei.value.status in (abi.RS_ERR_CUDA, abi.RS_ERR_NOMEM)
+
+
+def test_null_arguments_rejected():
+    L = _lib.load()
+    assert L.rs_create(None, None) == abi.RS_ERR_INVALID
+    assert L.rs_macro_step(None, 0.0, 1.0, None, None, None) == abi.RS_ERR_INVALID
+    assert L.rs_state_size(None) == 0
