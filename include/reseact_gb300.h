@@ -206,6 +206,18 @@ rs_status rs_state_device_ptr(rs_handle* h, void** d_state);
 /* The handle's CUDA stream (cudaStream_t), for callers timing with CUDA events. */
 void* rs_stream(rs_handle* h);
 
+/* One unclamped Rosenbrock23 attempt of step dt over all cells, reading d_u_in and writing
+ * d_u_out (DEVICE pointers, the grid-SoA layout of rs_state_device_ptr, n = the handle's
+ * state size), returning the hairer error estimate in *eest (host pointer, may be NULL).
+ * No counterpart in the reference.  It allocates nothing, for callers that cannot allocate
+ * device memory when they step (a host whose own memory pool owns the device, or a loop that
+ * must not synchronise on an allocation): its scratch is a 512 KiB array fixed in the
+ * library, resolved per device on the first call on that device (make that first call before
+ * any stream capture).  Limit: 16,777,216 cells (RS_ERR_INVALID beyond).  All calls share the
+ * scratch, so calls that overlap on the GPU (other threads or streams) race; serialise them. */
+rs_status rs_ros23_attempt_noalloc(rs_handle* h, double dt, const double* d_u_in,
+                                   double* d_u_out, double* eest);
+
 /* Per-kernel launch statistics, collected while profiling is on. */
 rs_status rs_set_profiling(rs_handle* h, int32_t on);
 /* names: ';'-separated kernel family names written into buf (size buf_len); counts and

@@ -16,7 +16,7 @@ SYMBOLS = [
     "rs_species_per_cell", "rs_set_state", "rs_get_state", "rs_set_forcing",
     "rs_get_rate_constants", "rs_set_rate_constants", "rs_macro_step", "rs_rhs_transport",
     "rs_rhs_chem", "rs_block_jac", "rs_single_step", "rs_state_device_ptr", "rs_stream",
-    "rs_set_profiling", "rs_get_profile", "rs_reset_profile",
+    "rs_set_profiling", "rs_get_profile", "rs_reset_profile", "rs_ros23_attempt_noalloc",
 ]
 
 
@@ -66,6 +66,8 @@ def _declare(L):
     L.rs_reset_profile.restype = C.c_int
     L.rs_get_profile.argtypes = [vp, C.c_char_p, sz, dp, dp, i32, C.POINTER(i32)]
     L.rs_get_profile.restype = C.c_int
+    L.rs_ros23_attempt_noalloc.argtypes = [vp, C.c_double, vp, vp, dp]
+    L.rs_ros23_attempt_noalloc.restype = C.c_int
     return L
 
 

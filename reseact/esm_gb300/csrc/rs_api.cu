@@ -13,6 +13,7 @@
 #include <cstring>
 #include <functional>
 #include <map>
+#include <mutex>
 #include <set>
 #include <stdexcept>
 #include <string>
@@ -992,3 +993,78 @@ rs_status rs_get_profile(rs_handle* h, char* buf, size_t buf_len, double* launch
 }
 
 }  // extern "C"
+
+// ====================================================================== allocation-free attempt
+// Some callers cannot allocate device memory at the point where they want to step the
+// chemistry: a host that runs its own memory pool (a Julia CUDA.jl or PyTorch caching
+// allocator that has already reserved the device), or a latency-critical loop where an
+// allocation would synchronise the device.  rs_ros23_attempt_noalloc serves them: its
+// scratch (the 256-cell partial sums of the error norm and the controller record) lives in
+// one file-scope device array that every GPU loading this library holds until exit.
+namespace {
+
+constexpr size_t kNoAllocMaxCells = (size_t)1 << 24;  // 16,777,216 cells
+constexpr size_t kNoAllocParts = kNoAllocMaxCells / rs::kRedThreads;  // 65,536 partial sums
+constexpr size_t kNoAllocBytes = kNoAllocParts * sizeof(double) + 256;  // + one Ctl record
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+void* g_noalloc_addr[kNoAllocMaxDevices] = {nullptr};
+std::mutex g_noalloc_mu;
+
+// Device address of the scratch array for device `dev`, resolved on first use with that
+// device current.  Host code must not take the array's address directly: on the host the
+// symbol is only a stand-in.
+void* noalloc_scratch(int dev) {
+  if (dev < 0 || dev >= kNoAllocMaxDevices) throw RsError(RS_ERR_INVALID, "device ordinal");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    g_noalloc_addr[dev] = p;
+  }
+  return g_noalloc_addr[dev];
+}
+
+}  // namespace
+
+extern "C" rs_status rs_ros23_attempt_noalloc(rs_handle* h, double dt, const double* d_u_in,
+                                              double* d_u_out, double* eest) {
+  if (!h || !d_u_in || !d_u_out) return RS_ERR_INVALID;
+  return guard(h, [&] {
+    if (!(dt > 0.0)) throw RsError(RS_ERR_INVALID, "dt must be positive");
+    if (h->nc > kNoAllocMaxCells)
+      throw RsError(RS_ERR_INVALID, "rs_ros23_attempt_noalloc handles at most 16,777,216 cells; "
+                                    "this grid has " + std::to_string(h->nc));
+    int prev = -1;
+    CK(cudaGetDevice(&prev));
+    if (prev != h->cfg.device) CK(cudaSetDevice(h->cfg.device));
+    struct Restore {
+      int d, p;
+      ~Restore() {
+        if (p >= 0 && p != d) cudaSetDevice(p);
+      }
+    } restore{h->cfg.device, prev};
+    unsigned char* base = static_cast<unsigned char*>(noalloc_scratch(h->cfg.device));
+    double* part = reinterpret_cast<double*>(base);
+    Ctl* ctl = reinterpret_cast<Ctl*>(base + kNoAllocParts * sizeof(double));
+    ensure_rates(h);
+    Ctl init = make_ctl(h, 0.0, dt, dt, h->cfg.ctrl_C, (double)h->nc * h->nsp);
+    init.cur = 0;
+    init.maxiters = 1.0;
+    rs::launch_ctl_init(h->st, ctl, init);  // every field of the record is rewritten
+    rs::launch_ros23_attempt(h->lc, ctl, const_cast<double*>(d_u_in), d_u_out, h->krates.p,
+                             h->have_emis ? h->emis.p : nullptr, part, h->cfg.rtol_C,
+                             h->cfg.atol_C, 0);
+    rs::launch_finalize(h->st, ctl, part, (int)((h->nc + rs::kRedThreads - 1) / rs::kRedThreads));
+    CK(cudaGetLastError());
+    if (eest) {
+      CK(cudaMemcpyAsync(&h->hctl[2], ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->st));
+      CK(cudaStreamSynchronize(h->st));
+      *eest = h->hctl[2].eest;
+    } else {
+      CK(cudaStreamSynchronize(h->st));
+    }
+  });
+}

@@ -14,7 +14,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def header_symbols():
     txt = open(os.path.join(ROOT, "include", "reseact_gb300.h")).read()
-    decl = r"^(?:rs_status|void|const char\*|size_t|int32_t|void\*)\s+\*?(rs_[a-z_]+)\s*\("
+    decl = r"^(?:rs_status|void|const char\*|size_t|int32_t|void\*)\s+\*?(rs_[a-z0-9_]+)\s*\("
     return sorted(set(re.findall(decl, txt, flags=re.M)))
 
 
