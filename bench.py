@@ -46,6 +46,7 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-forms", action="store_true", help="skip the mixed / batched forms")
     p.add_argument("--small", action="store_true", help="small grid (profiling/debug)")
     return p.parse_args()
 
@@ -250,6 +251,37 @@ def run_gb300(args):
         e2e = {"value": nc * args.steps * world / float(wt.item()), "unit": UNIT,
                "h2d_bytes_per_step": int(solver.n * 8), "d2h_bytes_per_step": int(solver.n * 8)}
 
+    # ------------------------------------------------------------------ other forms, same steps
+    u_fp64_end = solver.get_state()
+    forms = {}
+    if not args.no_forms:
+        from reseact.esm_gb300 import abi as _abi
+        for name, kw in (("mixed", dict(precision=_abi.RS_PREC_MIXED)),
+                         ("batched_mixed", dict(precision=_abi.RS_PREC_MIXED,
+                                                chem_mode=_abi.RS_CHEM_PER_CELL))):
+            alt = Solver.for_workload(w, device=local, **kw)
+            alt.set_state(u_start)
+            astream = torch.cuda.ExternalStream(alt.stream())
+            ta, a_T, a_C = t_start, dtT_start, dtC_start
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            barrier()
+            ev0.record(astream)
+            for _ in range(args.steps):
+                _, a_T, a_C, _ = alt.macro_step(ta, ta + dtm, a_T, a_C)
+                ta += dtm
+            ev1.record(astream)
+            barrier()
+            ms_a = ev0.elapsed_time(ev1)
+            ua = alt.get_state()
+            rel = np.abs(ua - u_fp64_end) / np.maximum(np.abs(u_fp64_end), 1e-9)
+            forms[name] = {"value": round(nc * args.steps / (ms_a * 1e-3), 2),
+                           "ms_per_step": round(ms_a / args.steps, 3),
+                           "speedup_vs_fp64": round(ms_max / ms_a, 3),
+                           "max_rel_err_vs_fp64": float(rel.max()),
+                           "median_rel_err_vs_fp64": float(np.median(rel))}
+            alt.close()
+
     # ------------------------------------------------------------------ roofline pass
     t, dtT, dtC = t_end, dtT_end, dtC_end
     solver.set_profiling(True)
@@ -305,7 +337,7 @@ def run_gb300(args):
                        "chem_mode": "global dt (reference)", "precision": "FP64",
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": "256 MiB flush between timed steps"},
-            "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline,
+            "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "forms": forms,
             "transport": transport, "kernels": kernels, "dominant": dom,
             "attempts_per_step": {"naT": float(np.mean([c[0] for c in counts])),
                                   "nrT": float(np.mean([c[1] for c in counts])),

@@ -347,7 +347,78 @@ inline double ppm_face_u(const double* v, int right) {
   return right ? aR : aL;
 }
 
+// ---- frozen-branch linearisation of the PPM face value (for the discrete adjoint) --------
+// The reconstruction is piecewise linear in the five stencil values: every branch (monotone
+// slope test, min/abs/copysign selections, CW84 limiter cases) is decided on VALUES, so with
+// the branches frozen at the primal the face value is v . w for a weight vector w.  Lin5
+// carries (value, d/dv_0..4) through the same operations to produce w.
+struct Lin5 {
+  double v, g[5];
+};
+inline Lin5 L5(double v) { Lin5 r{v, {0, 0, 0, 0, 0}}; return r; }
+inline Lin5 operator+(const Lin5& a, const Lin5& b) {
+  Lin5 r{a.v + b.v, {}}; for (int o = 0; o < 5; ++o) r.g[o] = a.g[o] + b.g[o]; return r; }
+inline Lin5 operator-(const Lin5& a, const Lin5& b) {
+  Lin5 r{a.v - b.v, {}}; for (int o = 0; o < 5; ++o) r.g[o] = a.g[o] - b.g[o]; return r; }
+inline Lin5 operator*(double c, const Lin5& a) {
+  Lin5 r{c * a.v, {}}; for (int o = 0; o < 5; ++o) r.g[o] = c * a.g[o]; return r; }
+inline Lin5 neg(const Lin5& a) { return (-1.0) * a; }
+inline Lin5 labs(const Lin5& a) { return a.v < 0.0 ? neg(a) : a; }
+inline Lin5 lmin(const Lin5& a, const Lin5& b) { return (b.v < a.v) ? b : a; }
+inline Lin5 lcopysign(const Lin5& mag, const Lin5& sgn) {
+  bool negs = std::signbit(sgn.v), negm = std::signbit(mag.v);
+  return negs == negm ? mag : neg(mag);
+}
+inline Lin5 slope_lu(const Lin5& am, const Lin5& a, const Lin5& ap) {
+  Lin5 d0 = a - am, d1 = ap - a;
+  if (d1.v * d0.v > 0.0) {
+    Lin5 da = 0.5 * (ap - am);
+    Lin5 lim = lmin(2.0 * labs(d0), 2.0 * labs(d1));
+    return lcopysign(lmin(labs(da), lim), da);
+  }
+  return L5(0.0);
+}
+inline Lin5 slope_ln(const Lin5& am, const Lin5& a, const Lin5& ap, double sA, double sB) {
+  Lin5 d0 = a - am, d1 = ap - a;
+  if (d1.v * d0.v > 0.0) {
+    Lin5 da = sA * d1 + sB * d0;
+    Lin5 lim = lmin(2.0 * labs(d0), 2.0 * labs(d1));
+    return lcopysign(lmin(labs(da), lim), da);
+  }
+  return L5(0.0);
+}
+inline void limit_l(const Lin5& a, Lin5& aL, Lin5& aR) {
+  if ((aR.v - a.v) * (a.v - aL.v) <= 0.0) {
+    aL = a; aR = a;
+  } else {
+    double dA = aR.v - aL.v;
+    double a6 = 6.0 * (a.v - 0.5 * (aL.v + aR.v));
+    if (dA * a6 > dA * dA) aL = 3.0 * a - 2.0 * aR;
+    else if (-(dA * dA) > dA * a6) aR = 3.0 * a - 2.0 * aL;
+  }
+}
+inline Lin5 seed(const double* v, int o) { Lin5 r = L5(v[o]); r.g[o] = 1.0; return r; }
+// weights of the uniform-grid upwind face value w.r.t. v[0..4]
+inline void face_weights_u(const double* v, bool right, double* w) {
+  Lin5 x[5];
+  for (int o = 0; o < 5; ++o) x[o] = seed(v, o);
+  Lin5 dm1 = slope_lu(x[0], x[1], x[2]), d0 = slope_lu(x[1], x[2], x[3]),
+       dp1 = slope_lu(x[2], x[3], x[4]);
+  Lin5 aL = x[1] + 0.5 * (x[2] - x[1]) - kOneSixth * (d0 - dm1);
+  Lin5 aR = x[2] + 0.5 * (x[3] - x[2]) - kOneSixth * (dp1 - d0);
+  limit_l(x[2], aL, aR);
+  const Lin5& r = right ? aR : aL;
+  for (int o = 0; o < 5; ++o) w[o] = r.g[o];
+}
+
+struct MacroRec {  // one recorded macro step (Ckpt of tools/adjoint_gradient.jl:621)
+  std::vector<double> u;
+  double t0, t1;
+  std::vector<std::pair<double, double>> seqT, seqC;
+};
+
 struct Model {
+  std::vector<MacroRec> recs;
   Grid G;
   Mech M;
   int nsp;  // species per cell in the state (chem species + air mass)
@@ -594,9 +665,12 @@ double ros23_step(const Model& md, const double* u, double t, double dt, double*
 
 // adaptive_solve (rx_traced_integrator.jl:455-507)
 struct SolveOut { double t, dt, nacc, nrej, iters; };
+using StepSeq = std::vector<std::pair<double, double>>;  // accepted (t, dt)
+
 template <class Step>
 SolveOut adaptive_solve(Step step, std::vector<double>& u, double t0, double tend, double dt0,
-                        const rs_controller& c, double maxiters, bool clamp) {
+                        const rs_controller& c, double maxiters, bool clamp,
+                        StepSeq* seq = nullptr) {
   size_t n = u.size();
   std::vector<double> unew(n);
   double beta1 = c.beta1, beta2 = c.beta2;
@@ -620,6 +694,7 @@ SolveOut adaptive_solve(Step step, std::vector<double>& u, double t0, double ten
     double qr = std::min(invqmin, q11 / gamma);
     double dt_rej = dtc / qr;
     if (accept) {
+      if (seq) seq->push_back({t, dtc});
       u.swap(unew);
       t = t + dtc;
       dt = dt_acc;
@@ -632,6 +707,291 @@ SolveOut adaptive_solve(Step step, std::vector<double>& u, double t0, double ten
     iters += 1.0;
   }
   return {t, dt, nacc, nrej, iters};
+}
+
+// ====================================================================== discrete adjoint
+// One-step VJPs at fixed dt with the clamp and the controller treated as the discrete
+// decisions they are (rx_traced_integrator.jl:509-623; tools/adjoint_gradient.jl:731-835):
+// lambda_in = (du_out/du_in)^T lambda_out, plus d/d(emission) for the chemistry steps.
+
+// stencil position p along x/y/z of cell (i,j,k) -> state cell index, or -1 for a boundary
+// ghost that carries no state (open walls)
+inline long map_x(const Grid& G, int p, int j, int k) {
+  if (p < 0 || p >= G.nlon) {
+    if (G.lon_bc != RS_BC_PERIODIC) return -1;
+    p = ((p % G.nlon) + G.nlon) % G.nlon;
+  }
+  return ((long)k * G.nlat + j) * G.nlon + p;
+}
+inline long map_y(const Grid& G, int i, int p, int k) {
+  if (p < 0 || p >= G.nlat) {
+    if (G.lat_bc == RS_BC_OPEN) return -1;
+    p = p < 0 ? -1 - p : 2 * G.nlat - 1 - p;
+  }
+  return ((long)k * G.nlat + p) * G.nlon + i;
+}
+inline long map_z(const Grid& G, int i, int j, int p) {
+  if (p < 0 || p >= G.nlev) p = p < 0 ? -1 - p : 2 * G.nlev - 1 - p;
+  return ((long)p * G.nlat + j) * G.nlon + i;
+}
+
+// ubar = (d f_transport / du)^T fbar at state u, time t (all species incl. air mass)
+void transport_rhs_vjp(const Model& md, const double* u, double t, const double* fbar,
+                       double* ubar) {
+  const Grid& G = md.G;
+  double g = md.F.omega != 0.0 ? std::cos(md.F.omega * t) : 1.0;
+  size_t nc = G.nc;
+  int ntr = md.nsp - 1;
+  const double* m = u + (size_t)ntr * nc;
+  std::vector<double> f((size_t)md.nsp * nc);
+  transport_rhs(md, u, t, f.data());
+  std::fill(ubar, ubar + (size_t)md.nsp * nc, 0.0);
+  std::vector<double> gq((size_t)ntr * nc);
+  size_t ncol = (size_t)G.nlon * G.nlat;
+  for (int k = 0; k < G.nlev; ++k)
+    for (int j = 0; j < G.nlat; ++j)
+      for (int i = 0; i < G.nlon; ++i) {
+        size_t c = ((size_t)k * G.nlat + j) * G.nlon + i, col = (size_t)j * G.nlon + i;
+        double mxw = g * md.F.mx[((size_t)k * G.nlat + j) * (G.nlon + 1) + i];
+        double mxe = g * md.F.mx[((size_t)k * G.nlat + j) * (G.nlon + 1) + i + 1];
+        double mys = (G.lat_bc != RS_BC_OPEN && j == 0) ? 0.0
+                   : g * md.F.my[((size_t)k * (G.nlat + 1) + j) * G.nlon + i];
+        double myn = (G.lat_bc != RS_BC_OPEN && j + 1 == G.nlat) ? 0.0
+                   : g * md.F.my[((size_t)k * (G.nlat + 1) + j + 1) * G.nlon + i];
+        double mzb = (k == 0) ? 0.0 : g * md.F.mz[(size_t)k * ncol + col];
+        double mzt = (k + 1 == G.nlev) ? 0.0 : g * md.F.mz[(size_t)(k + 1) * ncol + col];
+        double divM = ((mxe - mxw) * G.gx[j] + (myn * G.gyhi[j] - mys * G.gylo[j])) + (mzt - mzb);
+        double mb = 0.0;
+        for (int s = 0; s < ntr; ++s) {
+          double gs = fbar[(size_t)s * nc + c] / m[c];
+          gq[(size_t)s * nc + c] = gs;
+          ubar[(size_t)s * nc + c] += gs * divM;
+          mb -= gs * f[(size_t)s * nc + c];
+        }
+        ubar[(size_t)ntr * nc + c] += mb;
+      }
+  // x faces
+  for (int k = 0; k < G.nlev; ++k)
+    for (int j = 0; j < G.nlat; ++j)
+      for (int fi = 0; fi <= G.nlon; ++fi) {
+        double M = g * md.F.mx[((size_t)k * G.nlat + j) * (G.nlon + 1) + fi];
+        bool right = M > 0.0;
+        int up = right ? fi - 1 : fi;
+        for (int s = 0; s < ntr; ++s) {
+          const double* q = u + (size_t)s * nc;
+          double v[5], w[5];
+          for (int o = 0; o < 5; ++o) v[o] = qx(md, q, s, up - 2 + o, j, k);
+          face_weights_u(v, right, w);
+          double Fb = 0.0;
+          if (fi >= 1) Fb -= gq[(size_t)s * nc + ((size_t)k * G.nlat + j) * G.nlon + fi - 1] * G.gx[j];
+          if (fi < G.nlon) Fb += gq[(size_t)s * nc + ((size_t)k * G.nlat + j) * G.nlon + fi] * G.gx[j];
+          for (int o = 0; o < 5; ++o) {
+            long cc = map_x(G, up - 2 + o, j, k);
+            if (cc >= 0) ubar[(size_t)s * nc + cc] += Fb * M * w[o];
+          }
+        }
+      }
+  // y faces
+  for (int k = 0; k < G.nlev; ++k)
+    for (int fj = 0; fj <= G.nlat; ++fj) {
+      if (G.lat_bc != RS_BC_OPEN && (fj == 0 || fj == G.nlat)) continue;
+      for (int i = 0; i < G.nlon; ++i) {
+        double M = g * md.F.my[((size_t)k * (G.nlat + 1) + fj) * G.nlon + i];
+        bool right = M > 0.0;
+        int up = right ? fj - 1 : fj;
+        for (int s = 0; s < ntr; ++s) {
+          const double* q = u + (size_t)s * nc;
+          double v[5], w[5];
+          for (int o = 0; o < 5; ++o) v[o] = qy(md, q, s, i, up - 2 + o, k);
+          face_weights_u(v, right, w);
+          double Fb = 0.0;
+          if (fj >= 1) Fb -= gq[(size_t)s * nc + ((size_t)k * G.nlat + fj - 1) * G.nlon + i] * G.gyhi[fj - 1];
+          if (fj < G.nlat) Fb += gq[(size_t)s * nc + ((size_t)k * G.nlat + fj) * G.nlon + i] * G.gylo[fj];
+          for (int o = 0; o < 5; ++o) {
+            long cc = map_y(G, i, up - 2 + o, k);
+            if (cc >= 0) ubar[(size_t)s * nc + cc] += Fb * M * w[o];
+          }
+        }
+      }
+    }
+  // z faces (walls carry no flux)
+  for (int kf = 1; kf < G.nlev; ++kf)
+    for (int j = 0; j < G.nlat; ++j)
+      for (int i = 0; i < G.nlon; ++i) {
+        size_t col = (size_t)j * G.nlon + i;
+        double M = g * md.F.mz[(size_t)kf * ncol + col];
+        bool right = M > 0.0;
+        int up = right ? kf - 1 : kf;
+        const double* vs = md.F.vs.data() + col * (G.nlev + 2) * 2;
+        const double* ve = md.F.ve.data() + col * (G.nlev + 1) * 3;
+        for (int s = 0; s < ntr; ++s) {
+          const double* q = u + (size_t)s * nc;
+          Lin5 x[5];
+          for (int o = 0; o < 5; ++o) {
+            double vo = qz(md, q, i, j, up - 2 + o);
+            x[o] = L5(vo);
+            x[o].g[o] = 1.0;
+          }
+          auto sl = [&](int cidx, const Lin5& a0, const Lin5& a1, const Lin5& a2) {
+            return slope_ln(a0, a1, a2, vs[(cidx + 1) * 2], vs[(cidx + 1) * 2 + 1]);
+          };
+          Lin5 dm1 = sl(up - 1, x[0], x[1], x[2]), d0 = sl(up, x[1], x[2], x[3]),
+               dp1 = sl(up + 1, x[2], x[3], x[4]);
+          const double* eL = ve + (size_t)up * 3;
+          const double* eR = ve + (size_t)(up + 1) * 3;
+          Lin5 aL = x[1] + eL[0] * (x[2] - x[1]) + eL[1] * d0 + eL[2] * dm1;
+          Lin5 aR = x[2] + eR[0] * (x[3] - x[2]) + eR[1] * dp1 + eR[2] * d0;
+          limit_l(x[2], aL, aR);
+          const Lin5& r = right ? aR : aL;
+          double Fb = -gq[(size_t)s * nc + (size_t)(kf - 1) * ncol + col] +
+                      gq[(size_t)s * nc + (size_t)kf * ncol + col];
+          for (int o = 0; o < 5; ++o) {
+            long cc = map_z(G, i, j, up - 2 + o);
+            ubar[(size_t)s * nc + cc] += Fb * M * r.g[o];
+          }
+        }
+      }
+}
+
+// lam_in = (d unew / du)^T lam for one SSPRK43 step at fixed (t, dt)
+void ssprk43_vjp(const Model& md, const double* u, double t, double dt, const double* lam,
+                 double* lam_in) {
+  size_t n = (size_t)md.nsp * md.G.nc;
+  double h = dt / 2;
+  std::vector<double> f(n), u1(n), u2(n), u4(n), a(n), b(n), w(n);
+  transport_rhs(md, u, t, f.data());
+  for (size_t x = 0; x < n; ++x) u1[x] = u[x] + h * f[x];
+  transport_rhs(md, u1.data(), t + 0.5 * dt, f.data());
+  for (size_t x = 0; x < n; ++x) u2[x] = u1[x] + h * f[x];
+  transport_rhs(md, u2.data(), t + 1.0 * dt, f.data());
+  for (size_t x = 0; x < n; ++x) u4[x] = (2.0 / 3.0) * u[x] + (1.0 / 3.0) * (u2[x] + h * f[x]);
+  // unew = u4 + h f(u4)
+  for (size_t x = 0; x < n; ++x) w[x] = h * lam[x];
+  transport_rhs_vjp(md, u4.data(), t + h, w.data(), a.data());
+  for (size_t x = 0; x < n; ++x) a[x] += lam[x];          // ubar4
+  for (size_t x = 0; x < n; ++x) {
+    lam_in[x] = (2.0 / 3.0) * a[x];                        // via u4 = 2/3 u + 1/3 u3
+    b[x] = (1.0 / 3.0) * a[x];                             // ubar3 = ubar2 (+ f2 path)
+    w[x] = h * b[x];
+  }
+  transport_rhs_vjp(md, u2.data(), t + 1.0 * dt, w.data(), a.data());
+  for (size_t x = 0; x < n; ++x) { b[x] += a[x]; w[x] = h * b[x]; }   // ubar2 -> ubar1
+  transport_rhs_vjp(md, u1.data(), t + 0.5 * dt, w.data(), a.data());
+  for (size_t x = 0; x < n; ++x) { b[x] += a[x]; w[x] = h * b[x]; }   // ubar1 -> ubar0
+  transport_rhs_vjp(md, u, t, w.data(), a.data());
+  for (size_t x = 0; x < n; ++x) lam_in[x] += b[x] + a[x];
+}
+
+// d^2 v_r / dx_a dx_b (a, b species of reactant entries of r)
+inline double d2vel(const Mech& M, int r, double k, const double* x, int a, int b) {
+  double d = k;
+  for (int e = M.rptr[r]; e < M.rptr[r + 1]; ++e) {
+    int s = M.rsp[e], nu = M.rnu[e];
+    int order = (s == a) + (s == b);
+    if (order > nu) return 0.0;
+    double c = 1.0;
+    for (int t = 0; t < order; ++t) c *= (double)(nu - t);
+    for (int t = 0; t < nu - order; ++t) c *= x[s];
+    d *= c;
+  }
+  return d;
+}
+
+// one ROS23 step VJP of one cell: lam (d J / d unew) -> ubar (d J / d u), ebar += d J / d emis
+void ros23_vjp_cell(const Model& md, const double* kr, const double* x, const double* emis,
+                    double dt, const double* lam, double* ubar, double* ebar) {
+  const Mech& M = md.M;
+  int n = M.ns;
+  double f0[64], k1[64], u1[64], f1[64], b2[64], z2[64], vb[256];
+  std::vector<double> J(n * n), W(n * n), J1(n * n);
+  chem_rhs_cell(M, kr, x, emis, f0, vb);
+  chem_jac_cell(M, kr, x, J.data());
+  double dtgamma = dt * kRosD;
+  for (int r = 0; r < n; ++r)
+    for (int s = 0; s < n; ++s) W[r * n + s] = (r == s ? 1.0 : 0.0) - dtgamma * J[r * n + s];
+  std::vector<double> LU(W);
+  lu_factor(n, LU.data());
+  lu_solve(n, LU.data(), f0, k1);
+  for (int s = 0; s < n; ++s) u1[s] = x[s] + (dt / 2) * k1[s];
+  chem_rhs_cell(M, kr, u1, emis, f1, vb);
+  for (int s = 0; s < n; ++s) b2[s] = f1[s] - k1[s];
+  lu_solve(n, LU.data(), b2, z2);
+  // transposed solves with the same factors: W^T y = c
+  auto solveT = [&](const double* c, double* y) {
+    // W = L U (unit L); W^T = U^T L^T: forward with U^T, then backward with L^T
+    double t1[64];
+    for (int i = 0; i < n; ++i) {
+      double acc = c[i];
+      for (int j = 0; j < i; ++j) acc -= LU[j * n + i] * t1[j];
+      t1[i] = acc / LU[i * n + i];
+    }
+    for (int i = n - 1; i >= 0; --i) {
+      double acc = t1[i];
+      for (int j = i + 1; j < n; ++j) acc -= LU[j * n + i] * y[j];
+      y[i] = acc;
+    }
+  };
+  double k2b[64], k1b[64], b2b[64], f1b[64], u1b[64], f0b[64];
+  for (int s = 0; s < n; ++s) { ubar[s] = lam[s]; k2b[s] = dt * lam[s]; k1b[s] = k2b[s]; }
+  solveT(k2b, b2b);                       // b2bar = W^-T k2bar  (z2bar = k2bar)
+  for (int s = 0; s < n; ++s) { f1b[s] = b2b[s]; k1b[s] -= b2b[s]; }
+  chem_jac_cell(M, kr, u1, J1.data());
+  for (int q = 0; q < n; ++q) {           // u1bar = J(u1)^T f1bar
+    double acc = 0.0;
+    for (int i = 0; i < n; ++i) acc += J1[i * n + q] * f1b[i];
+    u1b[q] = acc;
+  }
+  for (int s = 0; s < n; ++s) { ubar[s] += u1b[s]; k1b[s] += (dt / 2) * u1b[s]; }
+  solveT(k1b, f0b);                       // f0bar = W^-T k1bar
+  for (int q = 0; q < n; ++q) {           // u += J(u)^T f0bar
+    double acc = 0.0;
+    for (int i = 0; i < n; ++i) acc += J[i * n + q] * f0b[i];
+    ubar[q] += acc;
+  }
+  if (ebar)
+    for (int s = 0; s < n; ++s) ebar[s] += f0b[s] + f1b[s];
+  // Jbar = -dtgamma * Wbar, Wbar = -(b2bar z2^T + f0bar k1^T)  =>  Jbar = dtgamma (...)
+  // u_q += sum_r sum_j (sum_i Jbar_ij net_ri) d2v_r/dx_j dx_q
+  for (int r = 0; r < M.nr; ++r) {
+    for (int ea = M.rptr[r]; ea < M.rptr[r + 1]; ++ea) {
+      int j = M.rsp[ea];
+      double gj = 0.0;
+      for (int i = 0; i < n; ++i) {
+        double c = M.net[(size_t)r * n + i];
+        if (c != 0.0) gj += c * dtgamma * (b2b[i] * z2[j] + f0b[i] * k1[j]);
+      }
+      if (gj == 0.0) continue;
+      for (int eb = M.rptr[r]; eb < M.rptr[r + 1]; ++eb) {
+        int q = M.rsp[eb];
+        ubar[q] += gj * d2vel(M, r, kr[r], x, j, q);
+      }
+    }
+  }
+}
+
+void ros23_vjp(const Model& md, const double* u, double dt, const double* lam, double* lam_in,
+               double* ebar) {
+  size_t nc = md.G.nc;
+  int ns = md.M.ns;
+  bool he = !md.F.emis.empty();
+#pragma omp parallel for schedule(static)
+  for (size_t c = 0; c < nc; ++c) {
+    double x[64], kr[256], em[64], l[64], ub[64], eb[64];
+    for (int s = 0; s < ns; ++s) {
+      x[s] = u[(size_t)s * nc + c];
+      l[s] = lam[(size_t)s * nc + c];
+      eb[s] = 0.0;
+    }
+    for (int r = 0; r < md.M.nr; ++r) kr[r] = md.krates[(size_t)r * nc + c];
+    if (he)
+      for (int s = 0; s < ns; ++s) em[s] = md.F.emis[(size_t)s * nc + c];
+    ros23_vjp_cell(md, kr, x, he ? em : nullptr, dt, l, ub, eb);
+    for (int s = 0; s < ns; ++s) {
+      lam_in[(size_t)s * nc + c] = ub[s];
+      if (ebar) ebar[(size_t)s * nc + c] += eb[s];
+    }
+    for (int s = ns; s < md.nsp; ++s) lam_in[(size_t)s * nc + c] = lam[(size_t)s * nc + c];
+  }
 }
 
 void compute_rates(Model& md) {
@@ -845,5 +1205,112 @@ int or_chem_per_cell(or_model* h, double* u, double t0, double t1, double dt0, d
 }
 
 double or_reduce_fixed(const double* e, size_t n) { return reduce_fixed(e, n); }
+
+// ---- discrete adjoint (tools/adjoint_gradient.jl:609-835) --------------------------------
+void or_record_clear(or_model* h) { reinterpret_cast<Model*>(h)->recs.clear(); }
+int or_record_count(or_model* h) { return (int)reinterpret_cast<Model*>(h)->recs.size(); }
+
+// macro step that also checkpoints its input and the accepted (t, dt) of both halves
+int or_record_macro_step(or_model* h, double* u, double t0, double t1, double* dtT, double* dtC,
+                         double* stats) {
+  Model& md = *reinterpret_cast<Model*>(h);
+  size_t n = (size_t)md.nsp * md.G.nc;
+  MacroRec rec;
+  rec.u.assign(u, u + n);
+  rec.t0 = t0;
+  rec.t1 = t1;
+  std::vector<double> uv(u, u + n), w;
+  bool clamp = md.cfg.clamp_nonneg != 0;
+  SolveOut oT{t1, *dtT, 0, 0, 0}, oC{t1, *dtC, 0, 0, 0};
+  if (md.cfg.do_transport)
+    oT = adaptive_solve([&](const double* x, double t, double dt, double* xn) {
+      return ssprk43_step(md, x, t, dt, xn, w); }, uv, t0, t1, *dtT, md.cfg.ctrl_T,
+      md.cfg.maxiters, clamp, &rec.seqT);
+  if (md.cfg.do_chemistry)
+    oC = adaptive_solve([&](const double* x, double t, double dt, double* xn) {
+      return ros23_step(md, x, t, dt, xn, w); }, uv, t0, t1, *dtC, md.cfg.ctrl_C,
+      md.cfg.maxiters, clamp, &rec.seqC);
+  std::copy(uv.begin(), uv.end(), u);
+  *dtT = oT.dt; *dtC = oC.dt;
+  stats[0] = oT.nacc; stats[1] = oT.nrej; stats[2] = oC.nacc; stats[3] = oC.nrej;
+  md.recs.push_back(std::move(rec));
+  return 0;
+}
+
+// replay one recorded macro step from u with its fixed sequences; optionally keep the tape
+// (input state of every accepted step) -- the fixed-sequence replay of
+// tools/adjoint_gradient.jl:647-669
+static void replay_rec(Model& md, const MacroRec& rec, std::vector<double>& u,
+                       std::vector<std::vector<double>>* tapeT,
+                       std::vector<std::vector<double>>* tapeC) {
+  size_t n = u.size();
+  std::vector<double> raw(n), w;
+  bool clamp = md.cfg.clamp_nonneg != 0;
+  for (auto& st : rec.seqT) {
+    if (tapeT) tapeT->push_back(u);
+    ssprk43_step(md, u.data(), st.first, st.second, raw.data(), w);
+    for (size_t x = 0; x < n; ++x) u[x] = clamp ? std::max(raw[x], 0.0) : raw[x];
+  }
+  for (auto& st : rec.seqC) {
+    if (tapeC) tapeC->push_back(u);
+    ros23_step(md, u.data(), st.first, st.second, raw.data(), w);
+    for (size_t x = 0; x < n; ++x) u[x] = clamp ? std::max(raw[x], 0.0) : raw[x];
+  }
+}
+
+// replay every recorded macro step (fixed step sequences) from u, in place
+void or_replay(or_model* h, double* u) {
+  Model& md = *reinterpret_cast<Model*>(h);
+  size_t n = (size_t)md.nsp * md.G.nc;
+  std::vector<double> uv(u, u + n);
+  for (auto& rec : md.recs) replay_rec(md, rec, uv, nullptr, nullptr);
+  std::copy(uv.begin(), uv.end(), u);
+}
+
+// backward sweep over all recorded macro steps: lam (d J / d u_end, in) -> d J / d u_0 (out);
+// ebar (grid SoA [ns][nc]) accumulates d J / d emission
+void or_adjoint_backward(or_model* h, double* lam, double* ebar) {
+  Model& md = *reinterpret_cast<Model*>(h);
+  size_t n = (size_t)md.nsp * md.G.nc;
+  std::vector<double> L(lam, lam + n), Lin(n), out;
+  bool clamp = md.cfg.clamp_nonneg != 0;
+  for (int k = (int)md.recs.size() - 1; k >= 0; --k) {
+    const MacroRec& rec = md.recs[k];
+    std::vector<std::vector<double>> tT, tC;
+    std::vector<double> u = rec.u;
+    replay_rec(md, rec, u, &tT, &tC);
+    // chemistry steps in reverse: clamp mask of each step's output, then the step VJP
+    for (int j = (int)rec.seqC.size() - 1; j >= 0; --j) {
+      const std::vector<double>& out_j = (j + 1 < (int)tC.size()) ? tC[j + 1] : u;
+      if (clamp)
+        for (size_t x = 0; x < n; ++x) if (!(out_j[x] > 0.0)) L[x] = 0.0;
+      ros23_vjp(md, tC[j].data(), rec.seqC[j].second, L.data(), Lin.data(), ebar);
+      L.swap(Lin);
+    }
+    for (int j = (int)rec.seqT.size() - 1; j >= 0; --j) {
+      const std::vector<double>& out_j =
+          (j + 1 < (int)tT.size()) ? tT[j + 1] : (tC.empty() ? u : tC[0]);
+      if (clamp)
+        for (size_t x = 0; x < n; ++x) if (!(out_j[x] > 0.0)) L[x] = 0.0;
+      ssprk43_vjp(md, tT[j].data(), rec.seqT[j].first, rec.seqT[j].second, L.data(), Lin.data());
+      L.swap(Lin);
+    }
+  }
+  std::copy(L.begin(), L.end(), lam);
+}
+
+// single-step VJPs (unit tests)
+void or_ssprk43_vjp(or_model* h, const double* u, double t, double dt, const double* lam,
+                    double* lam_in) {
+  ssprk43_vjp(*reinterpret_cast<Model*>(h), u, t, dt, lam, lam_in);
+}
+void or_ros23_vjp(or_model* h, const double* u, double dt, const double* lam, double* lam_in,
+                  double* ebar) {
+  ros23_vjp(*reinterpret_cast<Model*>(h), u, dt, lam, lam_in, ebar);
+}
+void or_transport_rhs_vjp(or_model* h, const double* u, double t, const double* fbar,
+                          double* ubar) {
+  transport_rhs_vjp(*reinterpret_cast<Model*>(h), u, t, fbar, ubar);
+}
 
 }  // extern "C"

@@ -48,6 +48,16 @@ def lib():
         L.or_chem_per_cell.argtypes = [vp, dp, C.c_double, C.c_double, C.c_double, dp, dp]
         L.or_reduce_fixed.restype = C.c_double
         L.or_reduce_fixed.argtypes = [dp, C.c_size_t]
+        L.or_record_clear.argtypes = [vp]
+        L.or_record_count.argtypes = [vp]
+        L.or_record_count.restype = C.c_int
+        L.or_record_macro_step.restype = C.c_int
+        L.or_record_macro_step.argtypes = [vp, dp, C.c_double, C.c_double, dp, dp, dp]
+        L.or_replay.argtypes = [vp, dp]
+        L.or_adjoint_backward.argtypes = [vp, dp, dp]
+        L.or_ssprk43_vjp.argtypes = [vp, dp, C.c_double, C.c_double, dp, dp]
+        L.or_ros23_vjp.argtypes = [vp, dp, C.c_double, dp, dp, dp]
+        L.or_transport_rhs_vjp.argtypes = [vp, dp, C.c_double, dp, dp]
         _lib = L
     return _lib
 
@@ -132,6 +142,51 @@ class Oracle:
         steps = np.empty(self.nc)
         rc = lib().or_chem_per_cell(self.h, _p(u), t0, t1, dt0, _p(dt), _p(steps))
         return rc, dt, steps
+
+
+    # ---------------------------------------------------------------- discrete adjoint
+    def record_clear(self):
+        lib().or_record_clear(self.h)
+
+    def record_macro_step(self, u, t0, t1, dtT, dtC):
+        assert u.flags.c_contiguous and u.dtype == np.float64
+        a, b = C.c_double(dtT), C.c_double(dtC)
+        st = np.zeros(8)
+        rc = lib().or_record_macro_step(self.h, _p(u), t0, t1, C.byref(a), C.byref(b), _p(st))
+        return rc, a.value, b.value, st
+
+    def replay(self, u):
+        u = np.ascontiguousarray(u, dtype=np.float64).copy()
+        lib().or_replay(self.h, _p(u))
+        return u
+
+    def adjoint_backward(self, lam_end):
+        lam = np.ascontiguousarray(lam_end, dtype=np.float64).copy()
+        ebar = np.zeros((self.ns,) + self.shape)
+        lib().or_adjoint_backward(self.h, _p(lam), _p(ebar))
+        return lam, ebar
+
+    def ssprk43_vjp(self, u, t, dt, lam):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        lam = np.ascontiguousarray(lam, dtype=np.float64)
+        out = np.empty_like(u)
+        lib().or_ssprk43_vjp(self.h, _p(u), t, dt, _p(lam), _p(out))
+        return out
+
+    def ros23_vjp(self, u, dt, lam):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        lam = np.ascontiguousarray(lam, dtype=np.float64)
+        out = np.empty_like(u)
+        ebar = np.zeros((self.ns,) + self.shape)
+        lib().or_ros23_vjp(self.h, _p(u), dt, _p(lam), _p(out), _p(ebar))
+        return out, ebar
+
+    def transport_rhs_vjp(self, u, t, fbar):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        fbar = np.ascontiguousarray(fbar, dtype=np.float64)
+        out = np.empty_like(u)
+        lib().or_transport_rhs_vjp(self.h, _p(u), t, _p(fbar), _p(out))
+        return out
 
 
 def reduce_fixed(e):

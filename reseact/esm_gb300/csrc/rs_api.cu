@@ -261,6 +261,7 @@ struct rs_handle {
   DevBuf<double> U[2], S1, S2, S3, fx, fy, fz, partial, krates, T, P, emis, io, io2;
   DevBuf<double> mx, my, mz, qw, qe, qs, qn, gx, gylo, gyhi, vsA, vsB, veAB, veC, veD, dtcell,
       stepcell;
+  DevBuf<float> qhi, qlo, vsA32, vsB32, veAB32, veC32, veD32;  // mixed-precision transport
   DevBuf<Ctl> ctl;  // [0] transport, [1] chemistry, [2] single-step scratch
   DevBuf<int> flag;
   DevBuf<unsigned long long> queue;
@@ -434,6 +435,15 @@ void build_vertical(rs_handle* h) {
   h->veAB.upload(eAB.data(), eAB.size(), h->st);
   h->veC.upload(eC.data(), eC.size(), h->st);
   h->veD.upload(eD.data(), eD.size(), h->st);
+  if (h->cfg.precision == RS_PREC_MIXED) {
+    auto f32 = [&](const std::vector<double>& v, DevBuf<float>& d) {
+      std::vector<float> w(v.begin(), v.end());
+      d.upload(w.data(), w.size(), h->st);
+      CK(cudaStreamSynchronize(h->st));  // w is a temporary
+    };
+    f32(sA, h->vsA32); f32(sB, h->vsB32); f32(eAB, h->veAB32); f32(eC, h->veC32); f32(eD, h->veD32);
+  }
+  CK(cudaStreamSynchronize(h->st));  // the host vectors above are temporaries
 }
 
 void refresh_dt(rs_handle* h) {
@@ -447,6 +457,10 @@ void refresh_dt(rs_handle* h) {
   T.qw = h->qw.p; T.qe = h->qe.p; T.qs = h->qs.p; T.qn = h->qn.p;
   T.vsA = h->vsA.p; T.vsB = h->vsB.p; T.veAB = h->veAB.p; T.veC = h->veC.p; T.veD = h->veD.p;
   T.fx = h->fx.p; T.fy = h->fy.p; T.fz = h->fz.p;
+  T.mixed = h->cfg.precision == RS_PREC_MIXED;
+  T.qhi = h->qhi.p; T.qlo = h->qlo.p;
+  T.vsA32 = h->vsA32.p; T.vsB32 = h->vsB32.p; T.veAB32 = h->veAB32.p; T.veC32 = h->veC32.p;
+  T.veD32 = h->veD32.p;
 }
 
 Ctl make_ctl(rs_handle* h, double t0, double t1, double dt0, const rs_controller& c,
@@ -458,6 +472,7 @@ Ctl make_ctl(rs_handle* h, double t0, double t1, double dt0, const rs_controller
   k.invqmin = 1.0 / c.qmin; k.invqmax = 1.0 / c.qmax; k.gamma = c.gamma;
   k.qsmin = c.qsteady_min; k.qsmax = c.qsteady_max; k.qoldinit = c.qoldinit;
   k.ntot = ntot; k.omega = h->omega;
+  k.ros_d = h->dm.ros_d;
   return k;
 }
 
@@ -498,7 +513,7 @@ void transport_attempt(rs_handle* h, Ctl* c) {
   }
   Scope s(h, "finalize");
   rs::launch_finalize(h->st, c, h->partial.p, (int)((h->nc + 255) / 256));
-  h->launches += 17;
+  h->launches += h->cfg.precision == RS_PREC_MIXED ? 18 : 17;
 }
 
 void chem_attempt(rs_handle* h, Ctl* c) {
@@ -575,8 +590,8 @@ rs_status rs_create(const rs_config* cfg, rs_handle** out) {
       if (!cfg->has_air_mass) throw RsError(RS_ERR_INVALID, "transport needs the air-mass species");
       if (g.nlat < 3 || g.nlev < 3 || g.nlon < 3)
         throw RsError(RS_ERR_INVALID, "transport needs nlon, nlat, nlev >= 3");
-      if (cfg->precision != RS_PREC_FP64)
-        throw RsError(RS_ERR_UNSUPPORTED, "only the FP64 transport build is available");
+      if (cfg->precision != RS_PREC_FP64 && cfg->precision != RS_PREC_MIXED)
+        throw RsError(RS_ERR_INVALID, "precision");
     }
     if (cfg->maxiters < 1) throw RsError(RS_ERR_INVALID, "maxiters");
     CK(cudaSetDevice(cfg->device));
@@ -627,6 +642,10 @@ rs_status rs_create(const rs_config* cfg, rs_handle** out) {
       h->qe.alloc((size_t)h->ntr * g.nlev * g.nlat); h->qe.zero(h->st);
       h->qs.alloc((size_t)h->ntr * g.nlev * g.nlon); h->qs.zero(h->st);
       h->qn.alloc((size_t)h->ntr * g.nlev * g.nlon); h->qn.zero(h->st);
+      if (cfg->precision == RS_PREC_MIXED) {
+        h->qhi.alloc((size_t)h->ntr * h->nc);
+        h->qlo.alloc((size_t)h->ntr * h->nc);
+      }
       build_geometry(h);
       h->dp_host.assign(h->nc, 1.0);
       build_vertical(h);
@@ -648,6 +667,9 @@ void rs_destroy(rs_handle* h) {
   if (h->st) cudaStreamSynchronize(h->st);
   for (auto& b : h->itabs) b.release();
   for (auto& b : h->dtabs) b.release();
+  DevBuf<float>* fbufs[] = {&h->qhi, &h->qlo, &h->vsA32, &h->vsB32, &h->veAB32, &h->veC32,
+                            &h->veD32};
+  for (auto* b : fbufs) b->release();
   DevBuf<double>* bufs[] = {&h->U[0], &h->U[1], &h->S1, &h->S2, &h->S3, &h->fx, &h->fy, &h->fz,
                             &h->partial, &h->krates, &h->T, &h->P, &h->emis, &h->io, &h->io2,
                             &h->mx, &h->my, &h->mz, &h->qw, &h->qe, &h->qs, &h->qn, &h->gx,

@@ -69,21 +69,27 @@ struct RosWork {
 
 // One attempt for one cell from x with step dt: xn (unclamped) and the cell's sum of squared
 // scaled errors over its chemistry species (the inert air-mass row contributes 0).
+struct StepScalars {
+  double dt, dto2, dto6, dtgamma;
+};
+__device__ __forceinline__ StepScalars step_scalars(const DevMech& M, double dt) {
+  return StepScalars{dt, dt / 2, dt / 6, dt * M.ros_d};
+}
+
 template <int MS, int MR, int MLU, int MP>
 __device__ __forceinline__ double ros23_cell(const DevMech& M, RosWork<MS, MR, MLU, MP>& w,
-                                             const double* emis, double dt, double rtol,
-                                             double atol) {
+                                             const double* emis, const StepScalars& h,
+                                             double rtol, double atol) {
   const int n = M.ns;
+  const double dt = h.dt;
   velocities(M, w.kc, w.x, w.v);
   rhs_from_v(M, w.v, emis, w.f0);
   partials(M, w.kc, w.x, w.P);
-  double dtgamma = dt * M.ros_d;
-  build_w(M, w.P, dtgamma, w.W);
+  build_w(M, w.P, h.dtgamma, w.W);
   lu_factor(M, w.W, w.piv);
   for (int s = 0; s < n; ++s) w.k1[s] = w.f0[s];
   lu_solve(M, w.W, w.piv, w.k1);  // k1 = W \ f0
-  double dto2 = dt / 2;
-  for (int s = 0; s < n; ++s) w.xn[s] = w.x[s] + dto2 * w.k1[s];  // u1
+  for (int s = 0; s < n; ++s) w.xn[s] = w.x[s] + h.dto2 * w.k1[s];  // u1
   velocities(M, w.kc, w.xn, w.v);
   rhs_from_v(M, w.v, emis, w.f1);  // f1 = f(u1)
   for (int s = 0; s < n; ++s) w.k2[s] = w.f1[s] - w.k1[s];
@@ -98,10 +104,9 @@ __device__ __forceinline__ double ros23_cell(const DevMech& M, RosWork<MS, MR, M
     w.b[s] = (w.b[s] - a) - c;
   }
   lu_solve(M, w.W, w.piv, w.b);  // k3
-  double dto6 = dt / 6;
   double acc = 0.0;
   for (int s = 0; s < n; ++s) {
-    double ut = dto6 * ((w.k1[s] - 2.0 * w.k2[s]) + w.b[s]);
+    double ut = h.dto6 * ((w.k1[s] - 2.0 * w.k2[s]) + w.b[s]);
     double am = fmax(fabs(w.x[s]), fabs(w.xn[s]));
     double den = am * rtol + atol;
     double at = ut / den;
@@ -121,7 +126,7 @@ __global__ void __launch_bounds__(256) k_ros23_attempt(
     double atol, int clamp) {
   __shared__ double sm[kRedThreads];
   if (ctl->done) return;
-  const double dt = ctl->dtc;
+  const StepScalars hs{ctl->dtc, ctl->dto2, ctl->dto6, ctl->dtgamma};
   const int cur = ctl->cur;
   const double* U = cur ? U1 : U0;
   double* Un = cur ? U0 : U1;
@@ -136,7 +141,7 @@ __global__ void __launch_bounds__(256) k_ros23_attempt(
       for (int s = 0; s < M.ns; ++s) w.em[s] = emission[(size_t)s * nc + c];
       em = w.em;
     }
-    e = ros23_cell(M, w, em, dt, rtol, atol);
+    e = ros23_cell(M, w, em, hs, rtol, atol);
     for (int s = 0; s < M.ns; ++s) {
       double xv = w.xn[s];
       Un[(size_t)s * nc + c] = clamp ? fmax(xv, 0.0) : xv;
@@ -224,7 +229,8 @@ __global__ void __launch_bounds__(128) k_chem_per_cell(
     }
     if ((t < tlim) && (iters < a.maxiters)) {
       double dtc = fmin(dt, a.t1 - t);
-      double sse = ros23_cell(M, w, emission ? w.em : nullptr, dtc, a.rtol, a.atol);
+      double sse = ros23_cell(M, w, emission ? w.em : nullptr, step_scalars(M, dtc), a.rtol,
+                              a.atol);
       double EEst = sqrt(sse / (double)nsp);
       if (isnan(EEst)) EEst = 1.0e10;
       double q11 = pow(fmax(EEst, 1.0e-35), a.beta1);

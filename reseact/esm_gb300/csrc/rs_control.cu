@@ -17,6 +17,9 @@ namespace rs {
 
 __device__ void prepare_next(Ctl* c) {
   c->dtc = fmin(c->dt, c->tend - c->t);
+  c->dto2 = c->dtc / 2;
+  c->dto6 = c->dtc / 6;
+  c->dtgamma = c->dtc * c->ros_d;
   double tlim = c->tend - 1.0e-9;
   c->done = !((c->t < tlim) && (c->iters < c->maxiters));
   if (c->omega != 0.0) {

@@ -67,6 +67,8 @@ struct Ctl {
   double ntot;     // number of states in the norm
   double omega;    // flux time factor g(t) = cos(omega t)
   double g[4];     // SSPRK43 stage factors of the next attempt: t, t+dt/2, t+dt, t+dt/2
+  double dto2, dto6, dtgamma;  // dtc/2, dtc/6, dtc*d of the next attempt (shared by all cells)
+  double ros_d;    // ROS23 d, for dtgamma
   int cur;         // state buffer holding the accepted state (0/1)
   int done;
   int accept;

@@ -51,6 +51,16 @@ struct DevTransport {
   R* fx;               // [ntr][nlev][nlat][nlon+1]
   R* fy;               // [ntr][nlev][nlat+1][nlon]
   R* fz;               // [ntr][nlev+1][nlat][nlon]
+  // mixed precision: the RHS input split into hi = fl(q), lo = fl(q - hi) planes [ntr][nc],
+  // and FP32 copies of the vertical coefficients
+  float* qhi;
+  float* qlo;
+  const float* vsA32;
+  const float* vsB32;
+  const float* veAB32;
+  const float* veC32;
+  const float* veD32;
+  int mixed;
 };
 
 // chemistry (rs_chem.cu)

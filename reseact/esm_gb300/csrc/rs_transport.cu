@@ -62,6 +62,56 @@ __device__ __forceinline__ double ppm_face_u(const double* v, bool right) {
   return right ? aR : aL;
 }
 
+// ---- mixed precision: the same reconstruction in FP32 on deviations from the upwind cell.
+// PPM is translation-equivariant (slopes, edges and limiter tests use differences only), so
+// subtracting the upwind value a2 from the stencil changes nothing in exact arithmetic; the
+// deviations d_o = (hi_o - hi_2) + (lo_o - lo_2) come from the split (hi, lo) state planes
+// without any FP64 instruction, FP32 then carries ~1e-7 relative error of the DEVIATION (not
+// of q), and the face value is a2 + dev in FP64.  q == 1 gives d == 0 and a face of exactly 1.
+__device__ __forceinline__ float slope_uf(float am, float a, float ap) {
+  float d0 = a - am, d1 = ap - a;
+  if (d1 * d0 > 0.0f) {
+    float da = 0.5f * (ap - am);
+    float lim = fminf(2.0f * fabsf(d0), 2.0f * fabsf(d1));
+    return copysignf(fminf(fabsf(da), lim), da);
+  }
+  return 0.0f;
+}
+__device__ __forceinline__ float slope_nf(float am, float a, float ap, float sA, float sB) {
+  float d0 = a - am, d1 = ap - a;
+  if (d1 * d0 > 0.0f) {
+    float da = sA * d1 + sB * d0;
+    float lim = fminf(2.0f * fabsf(d0), 2.0f * fabsf(d1));
+    return copysignf(fminf(fabsf(da), lim), da);
+  }
+  return 0.0f;
+}
+__device__ __forceinline__ void limitf(float a, float& aL, float& aR) {
+  if ((aR - a) * (a - aL) <= 0.0f) {
+    aL = a;
+    aR = a;
+  } else {
+    float dA = aR - aL;
+    float a6 = 6.0f * (a - 0.5f * (aL + aR));
+    if (dA * a6 > dA * dA) aL = 3.0f * a - 2.0f * aR;
+    else if (-(dA * dA) > dA * a6) aR = 3.0f * a - 2.0f * aL;
+  }
+}
+__device__ __forceinline__ float ppm_face_uf(const float* v, bool right) {
+  float dm1 = slope_uf(v[0], v[1], v[2]);
+  float d0 = slope_uf(v[1], v[2], v[3]);
+  float dp1 = slope_uf(v[2], v[3], v[4]);
+  float aL = v[1] + 0.5f * (v[2] - v[1]) - (d0 - dm1) * (1.0f / 6.0f);
+  float aR = v[2] + 0.5f * (v[3] - v[2]) - (dp1 - d0) * (1.0f / 6.0f);
+  limitf(v[2], aL, aR);
+  return right ? aR : aL;
+}
+// split a double into hi + lo floats (used only for boundary ghosts in the flux kernels)
+__device__ __forceinline__ void split_d(double x, float& hi, float& lo) {
+  hi = (float)x;
+  lo = (float)(x - (double)hi);
+}
+
 // Stage input selection: inside an adaptive attempt the field and the time factor come from
 // the device-resident controller (input U[cur] for stage 1, S1/S2/S3 for stages 2-4, g from
 // ctl->g[stage-1]); for a single RHS evaluation they are given directly.
@@ -118,6 +168,27 @@ __global__ void __launch_bounds__(kFluxThreads) k_flux_x(DevTransport<double> T,
     }
     ii[o] = q;
   }
+  if (T.mixed) {
+    for (int s = 0; s < T.ntr; ++s) {
+      const size_t pb = (size_t)s * nc + row;
+      float hi[5], lo[5];
+      for (int o = 0; o < 5; ++o) {
+        if (ghost[o]) {
+          const double* b = ii[o] < 0 ? T.qw : T.qe;
+          split_d(b[((size_t)s * T.nlev + k) * T.nlat + j], hi[o], lo[o]);
+        } else {
+          hi[o] = T.qhi[pb + ii[o]];
+          lo[o] = T.qlo[pb + ii[o]];
+        }
+      }
+      float d[5];
+      for (int o = 0; o < 5; ++o) d[o] = (hi[o] - hi[2]) + (lo[o] - lo[2]);
+      double a2 = ghost[2] ? (double)hi[2] + (double)lo[2] : Q[pb + ii[2]];
+      T.fx[((size_t)s * T.nlev * T.nlat + (size_t)k * T.nlat + j) * nf + i] =
+          M * (a2 + (double)ppm_face_uf(d, right));
+    }
+    return;
+  }
   for (int s = 0; s < T.ntr; ++s) {
     const double* q = Q + (size_t)s * nc + row;
     double v[5];
@@ -165,6 +236,26 @@ __global__ void __launch_bounds__(kFluxThreads) k_flux_y(DevTransport<double> T,
       else q = q < 0 ? -1 - q : 2 * T.nlat - 1 - q;
     }
     jj[o] = q;
+  }
+  if (T.mixed) {
+    for (int s = 0; s < T.ntr; ++s) {
+      const size_t pb = (size_t)s * nc + (size_t)k * T.nlat * T.nlon + i;
+      float hi[5], lo[5];
+      for (int o = 0; o < 5; ++o) {
+        if (ghost[o]) {
+          const double* b = jj[o] < 0 ? T.qs : T.qn;
+          split_d(b[((size_t)s * T.nlev + k) * T.nlon + i], hi[o], lo[o]);
+        } else {
+          hi[o] = T.qhi[pb + (size_t)jj[o] * T.nlon];
+          lo[o] = T.qlo[pb + (size_t)jj[o] * T.nlon];
+        }
+      }
+      float d[5];
+      for (int o = 0; o < 5; ++o) d[o] = (hi[o] - hi[2]) + (lo[o] - lo[2]);
+      double a2 = ghost[2] ? (double)hi[2] + (double)lo[2] : Q[pb + (size_t)jj[2] * T.nlon];
+      T.fy[(size_t)s * fplane + fbase] = M * (a2 + (double)ppm_face_uf(d, right));
+    }
+    return;
   }
   for (int s = 0; s < T.ntr; ++s) {
     const double* q = Q + (size_t)s * nc + (size_t)k * T.nlat * T.nlon + i;
@@ -215,6 +306,34 @@ __global__ void __launch_bounds__(kFluxThreads) k_flux_z(DevTransport<double> T,
          eLd = T.veD[(size_t)up * ncol + col];
   double eRab = T.veAB[(size_t)(up + 1) * ncol + col], eRc = T.veC[(size_t)(up + 1) * ncol + col],
          eRd = T.veD[(size_t)(up + 1) * ncol + col];
+  if (T.mixed) {
+    float fA0 = T.vsA32[(size_t)(up) * ncol + col], fB0 = T.vsB32[(size_t)(up) * ncol + col];
+    float fA1 = T.vsA32[(size_t)(up + 1) * ncol + col], fB1 = T.vsB32[(size_t)(up + 1) * ncol + col];
+    float fA2 = T.vsA32[(size_t)(up + 2) * ncol + col], fB2 = T.vsB32[(size_t)(up + 2) * ncol + col];
+    float fLab = T.veAB32[(size_t)up * ncol + col], fLc = T.veC32[(size_t)up * ncol + col],
+          fLd = T.veD32[(size_t)up * ncol + col];
+    float fRab = T.veAB32[(size_t)(up + 1) * ncol + col],
+          fRc = T.veC32[(size_t)(up + 1) * ncol + col], fRd = T.veD32[(size_t)(up + 1) * ncol + col];
+    for (int s = 0; s < T.ntr; ++s) {
+      const size_t pb = (size_t)s * nc + col;
+      float hi[5], lo[5];
+      for (int o = 0; o < 5; ++o) {
+        hi[o] = T.qhi[pb + (size_t)kk[o] * ncol];
+        lo[o] = T.qlo[pb + (size_t)kk[o] * ncol];
+      }
+      float d[5];
+      for (int o = 0; o < 5; ++o) d[o] = (hi[o] - hi[2]) + (lo[o] - lo[2]);
+      float dm1 = slope_nf(d[0], d[1], d[2], fA0, fB0);
+      float d0 = slope_nf(d[1], d[2], d[3], fA1, fB1);
+      float dp1 = slope_nf(d[2], d[3], d[4], fA2, fB2);
+      float aL = d[1] + fLab * (d[2] - d[1]) + fLc * d0 + fLd * dm1;
+      float aR = d[2] + fRab * (d[3] - d[2]) + fRc * dp1 + fRd * d0;
+      limitf(d[2], aL, aR);
+      double a2 = Q[pb + (size_t)kk[2] * ncol];
+      T.fz[(size_t)s * fplane + (size_t)kf * ncol + col] = M * (a2 + (double)(right ? aR : aL));
+    }
+    return;
+  }
   for (int s = 0; s < T.ntr; ++s) {
     const double* q = Q + (size_t)s * nc + col;
     double v[5];
@@ -230,6 +349,29 @@ __global__ void __launch_bounds__(kFluxThreads) k_flux_z(DevTransport<double> T,
 }
 
 // ------------------------------------------------------------------ stage kernel
+__device__ __forceinline__ void split_store(const DevTransport<double>& T, size_t x, double v) {
+  float hi = (float)v;
+  T.qhi[x] = hi;
+  T.qlo[x] = (float)(v - (double)hi);
+}
+
+// split the attempt's input state U[cur] (stage 1's RHS argument) into hi/lo planes
+__global__ void __launch_bounds__(kRedThreads) k_split_input(DevTransport<double> T,
+                                                             const Ctl* __restrict__ ctl,
+                                                             const double* __restrict__ U0,
+                                                             const double* __restrict__ U1,
+                                                             const double* __restrict__ Qd) {
+  const double* U;
+  if (ctl) {
+    if (ctl->done) return;
+    U = ctl->cur ? U1 : U0;
+  } else {
+    U = Qd;
+  }
+  size_t n = (size_t)T.ntr * T.nlon * T.nlat * T.nlev;
+  size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (x < n) split_store(T, x, U[x]);
+}
 // Divergence of the air-mass flux at cell (i,j,k) at time factor g.
 struct CellGeo {
   double gx, gylo, gyhi;
@@ -312,14 +454,20 @@ __global__ void __launch_bounds__(kRedThreads) k_stage(DevTransport<double> T,
         du = -divM;
       }
       if (STAGE == 1) {
-        B.S1[x] = q + dt_2 * du;
+        double nx = q + dt_2 * du;
+        B.S1[x] = nx;
+        if (T.mixed && s < T.ntr) split_store(T, x, nx);
       } else if (STAGE == 2) {
-        B.S2[x] = q + dt_2 * du;
+        double nx = q + dt_2 * du;
+        B.S2[x] = nx;
+        if (T.mixed && s < T.ntr) split_store(T, x, nx);
       } else if (STAGE == 3) {
         double u3 = q + dt_2 * du;
         double u0 = U[x];
         B.S1[x] = u3;
-        B.S3[x] = (2.0 / 3.0) * u0 + (1.0 / 3.0) * u3;
+        double u4 = (2.0 / 3.0) * u0 + (1.0 / 3.0) * u3;
+        B.S3[x] = u4;
+        if (T.mixed && s < T.ntr) split_store(T, x, u4);
       } else {
         double u0 = U[x];
         double u3 = B.S1[x];
@@ -393,6 +541,11 @@ void launch_ssprk43_attempt(cudaStream_t st, const DevTransport<double>& T, cons
   size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
   unsigned nb = (unsigned)((nc + kRedThreads - 1) / kRedThreads);
   StageSel sel{ctl, 1, B.U0, B.U1, B.S1, B.S2, B.S3, nullptr, 1.0};
+  if (T.mixed) {
+    size_t n = (size_t)T.ntr * nc;
+    k_split_input<<<(unsigned)((n + kRedThreads - 1) / kRedThreads), kRedThreads, 0, st>>>(
+        T, ctl, B.U0, B.U1, nullptr);
+  }
   launch_fluxes(st, T, sel);
   k_stage<1><<<nb, kRedThreads, 0, st>>>(T, ctl, B, rtol, atol, clamp);
   sel.stage = 2;
@@ -409,8 +562,13 @@ void launch_ssprk43_attempt(cudaStream_t st, const DevTransport<double>& T, cons
 void launch_transport_rhs(cudaStream_t st, const DevTransport<double>& T, const double* U,
                           double g, double* dU) {
   StageSel sel{nullptr, 0, nullptr, nullptr, nullptr, nullptr, nullptr, U, g};
-  launch_fluxes(st, T, sel);
   size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
+  if (T.mixed) {
+    size_t n = (size_t)T.ntr * nc;
+    k_split_input<<<(unsigned)((n + kRedThreads - 1) / kRedThreads), kRedThreads, 0, st>>>(
+        T, nullptr, nullptr, nullptr, U);
+  }
+  launch_fluxes(st, T, sel);
   k_rhs_eval<<<(unsigned)((nc + kRedThreads - 1) / kRedThreads), kRedThreads, 0, st>>>(T, U, dU, g);
 }
 

@@ -151,10 +151,12 @@ def test_macro_steps_adaptive(oracle_mod, wname):
     assert ok, worst
 
 
-@pytest.mark.parametrize("strict", [False, True])
-def test_cwc_freestream_exact(strict):
+@pytest.mark.parametrize("strict,precision", [(False, abi.RS_PREC_FP64), (True, abi.RS_PREC_FP64),
+                                              (False, abi.RS_PREC_MIXED)])
+def test_cwc_freestream_exact(strict, precision):
     """q == 1 with q_bc == 1 stays EXACTLY 1 under divergent open-wall flow
-    (prototypes/transport_3d/transport_3d.esm freestream test; tools/cwc_gate.jl)."""
+    (prototypes/transport_3d/transport_3d.esm freestream test; tools/cwc_gate.jl), in the
+    FP64 builds and in the mixed-precision transport."""
     from reseact.esm_gb300 import mechanism
     g, mx, my, mz, dp = workloads.regional_freestream()
     mech = mechanism.superfast()
@@ -164,7 +166,7 @@ def test_cwc_freestream_exact(strict):
     f = abi.ForcingABI(mx=mx, my=my, mz=mz, dp=dp3, qbc_w=qb_lon, qbc_e=qb_lon, qbc_s=qb_lon,
                        qbc_n=qb_lon)
     mabi = abi.MechanismABI(mech)
-    cfg = abi.make_config(g, mabi, do_chemistry=False)
+    cfg = abi.make_config(g, mabi, do_chemistry=False, precision=precision)
     s = Solver(cfg, mabi, strict=strict)
     s.set_forcing(f)
     u = np.concatenate([np.ones((mech.ns, n, n, n)), dp3[None] * (1 + 0.1 * np.random.default_rng(0).random((1, n, n, n)))])
@@ -258,3 +260,54 @@ def test_bad_arguments():
         s.set_state(np.zeros(3))
     with pytest.raises(RsError):
         s.macro_step(10.0, 5.0, 1.0, 1.0)
+
+
+def _tracer_masses(w, u_cm):
+    g = w.grid
+    u = workloads.cellmajor_to_soa(u_cm, w.nsp, g["nlon"], g["nlat"], g["nlev"])
+    phie = workloads.lat_edges(g)
+    area = (np.sin(np.radians(phie[1:])) - np.sin(np.radians(phie[:-1])))[None, :, None]
+    m = u[-1]
+    return np.array([(u[s] * m * area).sum() for s in range(w.nsp - 1)] + [(m * area).sum()])
+
+
+def test_mixed_precision_transport_error_and_mass(oracle_mod):
+    """FP32 reconstruction in deviation form with FP64 fluxes/divergence: agreement with the
+    FP64 oracle to < 1e-6 relative after three transport-only macro steps, air mass conserved
+    to roundoff and tracer-mass drift no worse than the FP64 scheme's own."""
+    w = workloads.c2(nlon=36, nlat=19, nlev=10)
+    s, o = make_pair(w, oracle_mod, do_chemistry=False, precision=abi.RS_PREC_MIXED)
+    s.set_state(w.u0_cellmajor())
+    u = np.ascontiguousarray(w.u0.copy())
+    M0 = _tracer_masses(w, w.u0_cellmajor())
+    t, dtT, dtTo = 0.0, 15.0, 15.0
+    for _ in range(3):
+        _, dtT, _, _ = s.macro_step(t, t + 600.0, dtT, 1.0)
+        orc, dtTo, _, _ = o.macro_step(u, t, t + 600.0, dtTo, 1.0)
+        t += 600.0
+    got, ref = s.get_state(), cm(w, u)
+    err = np.abs(got - ref) / np.maximum(np.abs(ref), 1e-6)
+    assert err.max() < 1e-6, err.max()
+    Mg, Mo = _tracer_masses(w, got), _tracer_masses(w, ref)
+    assert abs(Mg[-1] / M0[-1] - 1) < 1e-13
+    drift_fp64 = np.abs(Mo[:-1] / M0[:-1] - 1)
+    drift_mixed = np.abs(Mg[:-1] / M0[:-1] - 1)
+    assert np.all(drift_mixed <= 10 * drift_fp64 + 1e-12)
+
+
+def test_mixed_precision_full_step_within_1e6(oracle_mod):
+    """The whole split step with mixed-precision transport (chemistry FP64) against the FP64
+    oracle over three macro steps: max relative error < 1e-6 (atol floor)."""
+    w = small_c2()
+    s, o = make_pair(w, oracle_mod, precision=abi.RS_PREC_MIXED)
+    s.set_state(w.u0_cellmajor())
+    u = np.ascontiguousarray(w.u0.copy())
+    t, a, b, ao, bo = 0.0, 15.0, 0.5, 15.0, 0.5
+    for _ in range(3):
+        _, a, b, _ = s.macro_step(t, t + 600.0, a, b)
+        orc, ao, bo, _ = o.macro_step(u, t, t + 600.0, ao, bo)
+        assert orc == 0
+        t += 600.0
+    got, ref = s.get_state(), cm(w, u)
+    err = np.abs(got - ref) / np.maximum(np.abs(ref), 1e-9)
+    assert err.max() < 1e-6, err.max()
