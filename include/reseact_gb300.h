@@ -19,6 +19,10 @@
  *                         prototypes/reseact_3d_chem/block_jac.jl:108-136,
  *                         tools/reactant_handoff/rx_sym_block_jac.jl:205-233
  *   rs_single_step     <- ssprk43_step / ros23_step             rx_traced_integrator.jl:362-400 / 279-349
+ *   rs_record / rs_backward_macro_step / rs_adjoint_*  <- forward_pass (checkpoints +
+ *                         recorded (t,dt)), backward_sweep / backward_stage!, ros23_step_vjp and
+ *                         ssprk43_step_vjp (tools/adjoint_gradient.jl:609-835,
+ *                         rx_traced_integrator.jl:610-623)
  *   rs_get_rate_constants <- the per-cell rate constants of the .esm mechanism
  *                         (prototypes/g2_depsink/g2_nodep.esm:450-1780,1861)
  *
@@ -133,7 +137,8 @@ typedef struct rs_config {
 /* Forcing for one macro step (refresh_forcing).  NULL members keep their previous value
  * (zero before the first call).  Horizontal air-mass fluxes are on the unit sphere
  * (Mx = dp_face*U_face/a, Pa/s); Mz (Pa/s) is at the LOWER edge of each level, +ve upward,
- * level 0 at the surface.  All three scale in time by cos(flux_omega*t). */
+ * level 0 at the surface.  All three scale in time by cos(flux_omega*t); flux_omega is taken
+ * only from a call that passes at least one flux field. */
 typedef struct rs_forcing {
   const double* mx;          /* [nlev][nlat][nlon+1] west-face zonal flux */
   const double* my;          /* [nlev][nlat+1][nlon] south-face meridional flux */
@@ -205,6 +210,24 @@ rs_status rs_single_step(rs_handle* h, int32_t op, double t, double dt, const do
 rs_status rs_state_device_ptr(rs_handle* h, void** d_state);
 /* The handle's CUDA stream (cudaStream_t), for callers timing with CUDA events. */
 void* rs_stream(rs_handle* h);
+
+/* Discrete adjoint (tools/adjoint_gradient.jl:609-835; step VJPs rx_traced_integrator.jl:610-623).
+ * rs_record(h, 1) clears and starts recording: every rs_macro_step then keeps a device
+ * checkpoint of its input state and the accepted (t, dt) of both halves; rs_record(h, 0) stops.
+ * rs_adjoint_set_lambda loads dJ/du_end (cell-major); rs_backward_macro_step(h, k) replays
+ * recorded step k from its checkpoint with the FIXED step sequence and propagates lambda back
+ * through its chemistry steps, then its transport steps (clamp masks applied), accumulating
+ * dJ/d(emission) of every chemistry step; call it for k = count-1 ... 0 with the forcing of
+ * step k installed (the reference refreshes forcing per checkpoint the same way).  The
+ * adjoint differentiates the FP64 scheme; per-cell chemistry cannot be recorded. */
+rs_status rs_record(rs_handle* h, int32_t on);
+int32_t rs_record_count(const rs_handle* h);
+rs_status rs_adjoint_set_lambda(rs_handle* h, const double* lambda, size_t n);
+rs_status rs_adjoint_get_lambda(rs_handle* h, double* lambda, size_t n);
+rs_status rs_backward_macro_step(rs_handle* h, int32_t k);
+/* dJ/d(emission) accumulated so far, [n_species][nlev][nlat][nlon] (grid order) */
+rs_status rs_adjoint_get_grad_emission(rs_handle* h, double* grad, size_t n);
+rs_status rs_adjoint_reset_grad(rs_handle* h);
 
 /* One unclamped Rosenbrock23 attempt of step dt over all cells, reading d_u_in and writing
  * d_u_out (DEVICE pointers, the grid-SoA layout of rs_state_device_ptr, n = the handle's

@@ -1037,7 +1037,7 @@ int or_set_forcing(or_model* h, const rs_forcing* f) {
   copy_opt(md.F.mx, f->mx, (size_t)G.nlev * G.nlat * (G.nlon + 1));
   copy_opt(md.F.my, f->my, (size_t)G.nlev * (G.nlat + 1) * G.nlon);
   copy_opt(md.F.mz, f->mz, (size_t)(G.nlev + 1) * G.nlat * G.nlon);
-  md.F.omega = f->flux_omega;
+  if (f->mx || f->my || f->mz || md.F.mx.empty()) md.F.omega = f->flux_omega;
   if (f->dp) md.F.dp.assign(f->dp, f->dp + nc);
   else if (md.F.dp.empty()) md.F.dp.assign(nc, 1.0);
   copy_opt(md.F.qw, f->qbc_w, (size_t)ns * G.nlev * G.nlat);

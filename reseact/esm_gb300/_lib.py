@@ -17,6 +17,8 @@ SYMBOLS = [
     "rs_get_rate_constants", "rs_set_rate_constants", "rs_macro_step", "rs_rhs_transport",
     "rs_rhs_chem", "rs_block_jac", "rs_single_step", "rs_state_device_ptr", "rs_stream",
     "rs_set_profiling", "rs_get_profile", "rs_reset_profile", "rs_ros23_attempt_noalloc",
+    "rs_record", "rs_record_count", "rs_adjoint_set_lambda", "rs_adjoint_get_lambda",
+    "rs_backward_macro_step", "rs_adjoint_get_grad_emission", "rs_adjoint_reset_grad",
 ]
 
 
@@ -68,6 +70,17 @@ def _declare(L):
     L.rs_get_profile.restype = C.c_int
     L.rs_ros23_attempt_noalloc.argtypes = [vp, C.c_double, vp, vp, dp]
     L.rs_ros23_attempt_noalloc.restype = C.c_int
+    L.rs_record.argtypes = [vp, i32]
+    L.rs_record.restype = C.c_int
+    L.rs_record_count.argtypes = [vp]
+    L.rs_record_count.restype = i32
+    for f in ("rs_adjoint_set_lambda", "rs_adjoint_get_lambda", "rs_adjoint_get_grad_emission"):
+        getattr(L, f).argtypes = [vp, dp, sz]
+        getattr(L, f).restype = C.c_int
+    L.rs_backward_macro_step.argtypes = [vp, i32]
+    L.rs_backward_macro_step.restype = C.c_int
+    L.rs_adjoint_reset_grad.argtypes = [vp]
+    L.rs_adjoint_reset_grad.restype = C.c_int
     return L
 
 
@@ -184,6 +197,31 @@ class Solver:
         e = C.c_double()
         self._check(self.L.rs_single_step(self.h, op, t, dt, _p(u), _p(un), C.byref(e), u.size))
         return un, e.value
+
+    # ------------------------------------------------------------ discrete adjoint
+    def record(self, on=True):
+        self._check(self.L.rs_record(self.h, int(on)))
+
+    def record_count(self):
+        return self.L.rs_record_count(self.h)
+
+    def adjoint_backward(self, lam_end_cellmajor, steps=None, on_step=None):
+        """Backward sweep over the recorded macro steps (newest first).  Returns
+        (dJ/du_0 cell-major, dJ/d emission [ns][nlev][nlat][nlon])."""
+        lam = np.ascontiguousarray(lam_end_cellmajor, dtype=np.float64)
+        self._check(self.L.rs_adjoint_set_lambda(self.h, _p(lam), lam.size))
+        self._check(self.L.rs_adjoint_reset_grad(self.h))
+        n = self.record_count() if steps is None else steps
+        for k in range(self.record_count() - 1, self.record_count() - 1 - n, -1):
+            if on_step:
+                on_step(k)
+            self._check(self.L.rs_backward_macro_step(self.h, k))
+        out = np.empty(self.n)
+        self._check(self.L.rs_adjoint_get_lambda(self.h, _p(out), out.size))
+        ns = self.cfg.mech.n_species
+        g = np.empty(ns * self.nc)
+        self._check(self.L.rs_adjoint_get_grad_emission(self.h, _p(g), g.size))
+        return out, g.reshape(ns, self.nlev, self.nlat, self.nlon)
 
     def stream(self):
         return self.L.rs_stream(self.h)

@@ -17,7 +17,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
-SOURCES = ["rs_api.cu", "rs_chem.cu", "rs_transport.cu", "rs_control.cu"]
+SOURCES = ["rs_api.cu", "rs_chem.cu", "rs_transport.cu", "rs_control.cu", "rs_adjoint.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 LIBS = {"libreseact_gb300.so": ["--fmad=true", "-DRS_STRICT=0"],
         "libreseact_gb300_strict.so": ["--fmad=false", "-DRS_STRICT=1"]}

@@ -1,0 +1,487 @@
+// rs_adjoint.cu -- discrete-adjoint kernels of the split step (K4 transport, K5 chemistry).
+//
+// One-step VJPs at a fixed, recorded dt: lambda_in = (d u_out / d u_in)^T lambda_out and, for
+// chemistry, d J / d emission.  The controller's accept/reject and dt choices and the clamp are
+// the discrete decisions the adjoint is taken along (rx_traced_integrator.jl:540-547,
+// tools/adjoint_gradient.jl:736).  The exact ROS23 adjoint needs d(J v)/du because W is built
+// from J(u); for mass action that Hessian is exact and sparse (only reactant pairs of one
+// reaction), which is what replaces the reference's Enzyme second derivative.  PPM limiter
+// branches are frozen at the primal: the face value is then linear in its five stencil values
+// and its weights come from a forward-mode pass (Lin5) through the same reconstruction.
+// Sums are gathered per cell in a fixed order (no atomics): results are deterministic.
+#include <cuda_runtime.h>
+
+#include "rs_device.cuh"
+#include "rs_kernels.h"
+
+namespace rs {
+
+// ------------------------------------------------------------------ chemistry (K5)
+// Sparse transposed solve W^T x = b in place with the factors of lu_factor:
+// W^T = U^T L^T; U^T forward (right-looking over the rows of U), then L^T backward.
+__device__ __forceinline__ void lu_solve_T(const DevMech& M, const double* W, const double* piv,
+                                           double* b) {
+  for (int j = 0; j < M.ns; ++j) {
+#if RS_STRICT
+    double tj = b[j] / W[ldi(M.lu_diag + j)];
+#else
+    double tj = b[j] * piv[j];
+#endif
+    b[j] = tj;
+    int e1 = ldi(M.up_ptr + j + 1);
+    for (int e = ldi(M.up_ptr + j); e < e1; ++e) {
+      int i = ldi(M.up_col + e);
+      b[i] = b[i] - W[ldi(M.up_slot + e)] * tj;
+    }
+  }
+  for (int k = M.ns - 1; k >= 0; --k) {
+    double acc = b[k];
+    int e1 = ldi(M.low_ptr + k + 1);
+    for (int e = ldi(M.low_ptr + k); e < e1; ++e)
+      acc = acc - W[ldi(M.low_slot + e)] * b[ldi(M.low_row + e)];
+    b[k] = acc;
+  }
+}
+
+// a_r = sum_s net[r,s] y_s (through the per-species RHS term lists)
+template <int MR>
+__device__ __forceinline__ void reaction_sums(const DevMech& M, const double* y, double* a) {
+  for (int r = 0; r < M.nr; ++r) a[r] = 0.0;
+  for (int s = 0; s < M.ns; ++s) {
+    double ys = y[s];
+    int e1 = ldi(M.rhs_ptr + s + 1);
+    for (int e = ldi(M.rhs_ptr + s); e < e1; ++e) {
+      int r = ldi(M.rhs_r + e);
+      a[r] = a[r] + ld(M.rhs_c + e) * ys;
+    }
+  }
+}
+
+// out += J(x)^T y  given the partials P at x (P[p] = d v_{r_p} / d x_{q_p})
+template <int MR>
+__device__ __forceinline__ void jt_apply(const DevMech& M, const double* P, const double* y,
+                                         double* a, double* out) {
+  reaction_sums<MR>(M, y, a);
+  for (int p = 0; p < M.npart; ++p) {
+    int r = ldi(M.part_r + p), q = ldi(M.part_q + p);
+    out[q] = out[q] + a[r] * P[p];
+  }
+}
+
+// d^2 v_r / dx_a dx_b
+__device__ __forceinline__ double d2vel(const DevMech& M, int r, double k, const double* x, int a,
+                                        int b) {
+  double d = k;
+  int e1 = ldi(M.rptr + r + 1);
+  for (int e = ldi(M.rptr + r); e < e1; ++e) {
+    int s = ldi(M.rsp + e), nu = ldi(M.rnu + e);
+    int order = (s == a) + (s == b);
+    if (order > nu) return 0.0;
+    double c = 1.0;
+    for (int t = 0; t < order; ++t) c *= (double)(nu - t);
+    for (int t = 0; t < nu - order; ++t) c *= x[s];
+    d *= c;
+  }
+  return d;
+}
+
+template <int MS, int MR, int MLU, int MP>
+struct VjpWork {
+  double x[MS], f0[MS], k1[MS], u1[MS], f1[MS], z2[MS], bb[MS], f0b[MS], f1b[MS], ub[MS],
+      piv[MS], em[MS];
+  double kc[MR], v[MR], a0[MR], a1[MR], P[MP], P1[MP], W[MLU];
+};
+
+template <int MS, int MR, int MLU, int MP>
+__global__ void __launch_bounds__(128) k_ros23_vjp(
+    DevMech M, int nc, int nsp, const double* __restrict__ U, const double* __restrict__ Uout,
+    const double* __restrict__ lam, double* __restrict__ lam_out,
+    const double* __restrict__ krates, const double* __restrict__ emission,
+    double* __restrict__ ebar, double dt, int clamp) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  VjpWork<MS, MR, MLU, MP> w;
+  const int n = M.ns;
+  const double dto2 = dt / 2, dtgamma = dt * M.ros_d;
+  for (int s = 0; s < n; ++s) w.x[s] = U[(size_t)s * nc + c];
+  for (int r = 0; r < M.nr; ++r) w.kc[r] = krates[(size_t)r * nc + c];
+  const double* em = nullptr;
+  if (emission) {
+    for (int s = 0; s < n; ++s) w.em[s] = emission[(size_t)s * nc + c];
+    em = w.em;
+  }
+  // ---- forward recompute (the live part of ros23: unew = u + dt k2)
+  velocities(M, w.kc, w.x, w.v);
+  rhs_from_v(M, w.v, em, w.f0);
+  partials(M, w.kc, w.x, w.P);
+  build_w(M, w.P, dtgamma, w.W);
+  lu_factor(M, w.W, w.piv);
+  for (int s = 0; s < n; ++s) w.k1[s] = w.f0[s];
+  lu_solve(M, w.W, w.piv, w.k1);
+  for (int s = 0; s < n; ++s) w.u1[s] = w.x[s] + dto2 * w.k1[s];
+  velocities(M, w.kc, w.u1, w.v);
+  rhs_from_v(M, w.v, em, w.f1);
+  partials(M, w.kc, w.u1, w.P1);
+  for (int s = 0; s < n; ++s) w.z2[s] = w.f1[s] - w.k1[s];
+  lu_solve(M, w.W, w.piv, w.z2);
+  // ---- backward; lambda masked by the clamp of this step's output
+  for (int s = 0; s < n; ++s) {
+    double l = lam[(size_t)s * nc + c];
+    if (clamp && Uout && !(Uout[(size_t)s * nc + c] > 0.0)) l = 0.0;
+    w.ub[s] = l;
+    w.bb[s] = dt * l;  // k2bar
+  }
+  lu_solve_T(M, w.W, w.piv, w.bb);  // b2bar = W^-T k2bar
+  for (int s = 0; s < n; ++s) {
+    w.f1b[s] = w.bb[s];
+    w.f0b[s] = dt * w.ub[s] - w.bb[s];  // k1bar = k2bar - b2bar (held in f0b)
+  }
+  for (int s = 0; s < n; ++s) w.u1[s] = 0.0;  // u1bar = J(u1)^T f1bar
+  jt_apply<MR>(M, w.P1, w.f1b, w.a0, w.u1);
+  for (int s = 0; s < n; ++s) {
+    w.ub[s] = w.ub[s] + w.u1[s];
+    w.f0b[s] = w.f0b[s] + dto2 * w.u1[s];
+  }
+  lu_solve_T(M, w.W, w.piv, w.f0b);  // f0bar = W^-T k1bar
+  jt_apply<MR>(M, w.P, w.f0b, w.a0, w.ub);
+  // Hessian term: Jbar_ij = dtgamma (b2bar_i z2_j + f0bar_i k1_j)
+  reaction_sums<MR>(M, w.bb, w.a1);
+  reaction_sums<MR>(M, w.f0b, w.a0);
+  for (int r = 0; r < M.nr; ++r) {
+    int e1 = ldi(M.rptr + r + 1);
+    for (int ea = ldi(M.rptr + r); ea < e1; ++ea) {
+      int j = ldi(M.rsp + ea);
+      double gj = dtgamma * (w.a1[r] * w.z2[j] + w.a0[r] * w.k1[j]);
+      if (gj == 0.0) continue;
+      for (int eb = ldi(M.rptr + r); eb < e1; ++eb) {
+        int q = ldi(M.rsp + eb);
+        w.ub[q] = w.ub[q] + gj * d2vel(M, r, w.kc[r], w.x, j, q);
+      }
+    }
+  }
+  for (int s = 0; s < n; ++s) {
+    lam_out[(size_t)s * nc + c] = w.ub[s];
+    if (ebar) ebar[(size_t)s * nc + c] += w.f0b[s] + w.f1b[s];
+  }
+  for (int s = n; s < nsp; ++s) {  // inert air mass: identity, clamp mask only
+    double l = lam[(size_t)s * nc + c];
+    if (clamp && Uout && !(Uout[(size_t)s * nc + c] > 0.0)) l = 0.0;
+    lam_out[(size_t)s * nc + c] = l;
+  }
+}
+
+void launch_ros23_vjp(const LaunchCtx& L, const double* U, const double* Uout, const double* lam,
+                      double* lam_out, const double* kr, const double* em, double* ebar,
+                      double dt, int clamp) {
+  int nb = (L.nc + 127) / 128;
+  if (L.size_class == 0)
+    k_ros23_vjp<kSmallMS, kSmallMR, kSmallMLU, kSmallMP><<<nb, 128, 0, L.stream>>>(
+        L.mech, L.nc, L.nsp, U, Uout, lam, lam_out, kr, em, ebar, dt, clamp);
+  else
+    k_ros23_vjp<kLargeMS, kLargeMR, kLargeMLU, kLargeMP><<<nb, 128, 0, L.stream>>>(
+        L.mech, L.nc, L.nsp, U, Uout, lam, lam_out, kr, em, ebar, dt, clamp);
+}
+
+// ------------------------------------------------------------------ transport (K4)
+struct Lin5 {
+  double v, g[5];
+};
+__device__ __forceinline__ Lin5 l5(double v) {
+  Lin5 r;
+  r.v = v;
+  for (int o = 0; o < 5; ++o) r.g[o] = 0.0;
+  return r;
+}
+__device__ __forceinline__ Lin5 ladd(const Lin5& a, const Lin5& b) {
+  Lin5 r;
+  r.v = a.v + b.v;
+  for (int o = 0; o < 5; ++o) r.g[o] = a.g[o] + b.g[o];
+  return r;
+}
+__device__ __forceinline__ Lin5 lsub(const Lin5& a, const Lin5& b) {
+  Lin5 r;
+  r.v = a.v - b.v;
+  for (int o = 0; o < 5; ++o) r.g[o] = a.g[o] - b.g[o];
+  return r;
+}
+__device__ __forceinline__ Lin5 lscale(double c, const Lin5& a) {
+  Lin5 r;
+  r.v = c * a.v;
+  for (int o = 0; o < 5; ++o) r.g[o] = c * a.g[o];
+  return r;
+}
+__device__ __forceinline__ Lin5 labs5(const Lin5& a) { return a.v < 0.0 ? lscale(-1.0, a) : a; }
+__device__ __forceinline__ Lin5 lmin5(const Lin5& a, const Lin5& b) { return (b.v < a.v) ? b : a; }
+__device__ __forceinline__ Lin5 lcopysign5(const Lin5& mag, const Lin5& sgn) {
+  return (signbit(sgn.v) == signbit(mag.v)) ? mag : lscale(-1.0, mag);
+}
+__device__ __forceinline__ Lin5 lslope(const Lin5& am, const Lin5& a, const Lin5& ap, double sA,
+                                       double sB, bool uniform) {
+  Lin5 d0 = lsub(a, am), d1 = lsub(ap, a);
+  if (d1.v * d0.v > 0.0) {
+    Lin5 da = uniform ? lscale(0.5, lsub(ap, am)) : ladd(lscale(sA, d1), lscale(sB, d0));
+    Lin5 lim = lmin5(lscale(2.0, labs5(d0)), lscale(2.0, labs5(d1)));
+    return lcopysign5(lmin5(labs5(da), lim), da);
+  }
+  return l5(0.0);
+}
+__device__ __forceinline__ void llimit(const Lin5& a, Lin5& aL, Lin5& aR) {
+  if ((aR.v - a.v) * (a.v - aL.v) <= 0.0) {
+    aL = a;
+    aR = a;
+  } else {
+    double dA = aR.v - aL.v;
+    double a6 = 6.0 * (a.v - 0.5 * (aL.v + aR.v));
+    if (dA * a6 > dA * dA) aL = lsub(lscale(3.0, a), lscale(2.0, aR));
+    else if (-(dA * dA) > dA * a6) aR = lsub(lscale(3.0, a), lscale(2.0, aL));
+  }
+}
+// weights of the upwind face value w.r.t. the five stencil values; uniform (horizontal) or
+// dp-weighted (vertical: slope coefficients sA/sB of cells up-1..up+1, edge coefficients)
+__device__ __forceinline__ void face_weights(const double* v, bool right, bool uniform,
+                                             const double* sA, const double* sB,
+                                             const double* eL, const double* eR, double* w) {
+  Lin5 x[5];
+  for (int o = 0; o < 5; ++o) {
+    x[o] = l5(v[o]);
+    x[o].g[o] = 1.0;
+  }
+  const double k6 = 1.0 / 6.0;
+  Lin5 dm1 = lslope(x[0], x[1], x[2], sA[0], sB[0], uniform);
+  Lin5 d0 = lslope(x[1], x[2], x[3], sA[1], sB[1], uniform);
+  Lin5 dp1 = lslope(x[2], x[3], x[4], sA[2], sB[2], uniform);
+  Lin5 aL, aR;
+  if (uniform) {
+    aL = lsub(ladd(x[1], lscale(0.5, lsub(x[2], x[1]))), lscale(k6, lsub(d0, dm1)));
+    aR = lsub(ladd(x[2], lscale(0.5, lsub(x[3], x[2]))), lscale(k6, lsub(dp1, d0)));
+  } else {
+    aL = ladd(ladd(ladd(x[1], lscale(eL[0], lsub(x[2], x[1]))), lscale(eL[1], d0)),
+              lscale(eL[2], dm1));
+    aR = ladd(ladd(ladd(x[2], lscale(eR[0], lsub(x[3], x[2]))), lscale(eR[1], dp1)),
+              lscale(eR[2], d0));
+  }
+  llimit(x[2], aL, aR);
+  const Lin5& r = right ? aR : aL;
+  for (int o = 0; o < 5; ++o) w[o] = r.g[o];
+}
+
+// index maps of a stencil position p along a direction -> position in range, or -1 (open ghost)
+__device__ __forceinline__ int map_pos(int p, int n, int bc) {
+  if (p >= 0 && p < n) return p;
+  if (bc == 0) return ((p % n) + n) % n;  // periodic
+  if (bc == 1) return -1;                  // open: boundary data, no state
+  return p < 0 ? -1 - p : 2 * n - 1 - p;   // mirror (closed walls, vertical)
+}
+
+// per cell: g = fbar/m, ubar_direct = g divM, mbar = -sum g f
+__global__ void __launch_bounds__(256) k_adj_cell(DevTransport<double> T, const double* __restrict__ U,
+                                                  const double* __restrict__ F,
+                                                  const double* __restrict__ fbar,
+                                                  double* __restrict__ ubar,
+                                                  double* __restrict__ G, double g) {
+  const size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
+  size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  int i = (int)(c % T.nlon);
+  int j = (int)((c / T.nlon) % T.nlat);
+  int k = (int)(c / ((size_t)T.nlon * T.nlat));
+  const int nf = T.nlon + 1;
+  const size_t ncol = (size_t)T.nlon * T.nlat, col = (size_t)j * T.nlon + i;
+  double mxw = g * T.mx[((size_t)k * T.nlat + j) * nf + i];
+  double mxe = g * T.mx[((size_t)k * T.nlat + j) * nf + i + 1];
+  double mys = (T.lat_bc != 1 && j == 0) ? 0.0 : g * T.my[((size_t)k * (T.nlat + 1) + j) * T.nlon + i];
+  double myn = (T.lat_bc != 1 && j + 1 == T.nlat) ? 0.0
+             : g * T.my[((size_t)k * (T.nlat + 1) + j + 1) * T.nlon + i];
+  double mzb = (k == 0) ? 0.0 : g * T.mz[(size_t)k * ncol + col];
+  double mzt = (k + 1 == T.nlev) ? 0.0 : g * T.mz[(size_t)(k + 1) * ncol + col];
+  double divM = ((mxe - mxw) * T.gx[j] + (myn * T.gyhi[j] - mys * T.gylo[j])) + (mzt - mzb);
+  double m = U[(size_t)T.ntr * nc + c];
+  double mb = 0.0;
+  for (int s = 0; s < T.ntr; ++s) {
+    double gs = fbar[(size_t)s * nc + c] / m;
+    G[(size_t)s * nc + c] = gs;
+    ubar[(size_t)s * nc + c] = gs * divM;
+    mb = mb - gs * F[(size_t)s * nc + c];
+  }
+  ubar[(size_t)T.ntr * nc + c] = mb;
+}
+
+// per face (direction DIR): contributions C[s][face][o] = Fbar * M * w_o
+template <int DIR>
+__global__ void __launch_bounds__(256) k_adj_face(DevTransport<double> T, const double* __restrict__ U,
+                                                  const double* __restrict__ G,
+                                                  double* __restrict__ Cf, double g) {
+  const size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
+  const size_t ncol = (size_t)T.nlon * T.nlat;
+  long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  int n = DIR == 0 ? T.nlon : (DIR == 1 ? T.nlat : T.nlev);
+  int bc = DIR == 0 ? T.lon_bc : (DIR == 1 ? (T.lat_bc == 1 ? 1 : 2) : 2);
+  long long total = DIR == 0 ? (long long)(T.nlon + 1) * T.nlat * T.nlev
+                  : DIR == 1 ? (long long)T.nlon * (T.nlat + 1) * T.nlev
+                             : (long long)ncol * (T.nlev + 1);
+  if (idx >= total) return;
+  int i, j, k, f;
+  if (DIR == 0) {
+    f = (int)(idx % (T.nlon + 1)); j = (int)((idx / (T.nlon + 1)) % T.nlat);
+    k = (int)(idx / ((long long)(T.nlon + 1) * T.nlat)); i = f;
+  } else if (DIR == 1) {
+    i = (int)(idx % T.nlon); f = (int)((idx / T.nlon) % (T.nlat + 1));
+    k = (int)(idx / ((long long)T.nlon * (T.nlat + 1))); j = f;
+  } else {
+    i = (int)(idx % T.nlon); j = (int)((idx / T.nlon) % T.nlat); f = (int)(idx / (long long)ncol);
+    k = f;
+  }
+  const size_t fplane = (size_t)total;
+  bool wall = (DIR == 1 && T.lat_bc != 1 && (f == 0 || f == T.nlat)) ||
+              (DIR == 2 && (f == 0 || f == T.nlev));
+  double M = 0.0;
+  if (!wall) {
+    if (DIR == 0) M = g * T.mx[((size_t)k * T.nlat + j) * (T.nlon + 1) + f];
+    else if (DIR == 1) M = g * T.my[((size_t)k * (T.nlat + 1) + f) * T.nlon + i];
+    else M = g * T.mz[(size_t)f * ncol + (size_t)j * T.nlon + i];
+  }
+  bool right = M > 0.0;
+  int up = right ? f - 1 : f;
+  // cell index of position p along this direction (or -1 for a ghost)
+  auto cell_of = [&](int p) -> long long {
+    int q = map_pos(p, n, bc);
+    if (q < 0) return -1;
+    if (DIR == 0) return ((long long)k * T.nlat + j) * T.nlon + q;
+    if (DIR == 1) return ((long long)k * T.nlat + q) * T.nlon + i;
+    return (long long)q * ncol + (size_t)j * T.nlon + i;
+  };
+  // neighbours: cell before the face (f-1) sees +F, cell after (f) sees -F in D
+  long long cb = (f >= 1) ? cell_of(f - 1) : -1;
+  long long ca = (f < n) ? cell_of(f) : -1;
+  double cbw = DIR == 0 ? T.gx[j] : (DIR == 1 ? (f >= 1 ? T.gyhi[f - 1] : 0.0) : 1.0);
+  double caw = DIR == 0 ? T.gx[j] : (DIR == 1 ? (f < n ? T.gylo[f] : 0.0) : 1.0);
+  double sA[3] = {0, 0, 0}, sB[3] = {0, 0, 0}, eL[3] = {0, 0, 0}, eR[3] = {0, 0, 0};
+  if (DIR == 2 && !wall) {
+    size_t col = (size_t)j * T.nlon + i;
+    for (int o = 0; o < 3; ++o) {
+      sA[o] = T.vsA[(size_t)(up + o) * ncol + col];
+      sB[o] = T.vsB[(size_t)(up + o) * ncol + col];
+    }
+    eL[0] = T.veAB[(size_t)up * ncol + col]; eL[1] = T.veC[(size_t)up * ncol + col];
+    eL[2] = T.veD[(size_t)up * ncol + col];
+    eR[0] = T.veAB[(size_t)(up + 1) * ncol + col]; eR[1] = T.veC[(size_t)(up + 1) * ncol + col];
+    eR[2] = T.veD[(size_t)(up + 1) * ncol + col];
+  }
+  for (int s = 0; s < T.ntr; ++s) {
+    double* out = Cf + ((size_t)s * fplane + (size_t)idx) * 5;
+    if (wall) {
+      for (int o = 0; o < 5; ++o) out[o] = 0.0;
+      continue;
+    }
+    double v[5], w[5];
+    for (int o = 0; o < 5; ++o) {
+      long long cc = cell_of(up - 2 + o);
+      if (cc >= 0) {
+        v[o] = U[(size_t)s * nc + cc];
+      } else {  // open-wall ghost: the prescribed boundary value
+        int p = up - 2 + o;
+        if (DIR == 0) v[o] = (p < 0 ? T.qw : T.qe)[((size_t)s * T.nlev + k) * T.nlat + j];
+        else v[o] = (p < 0 ? T.qs : T.qn)[((size_t)s * T.nlev + k) * T.nlon + i];
+      }
+    }
+    face_weights(v, right, DIR != 2, sA, sB, eL, eR, w);
+    double Fb = 0.0;
+    if (cb >= 0) Fb = Fb - G[(size_t)s * nc + cb] * cbw;
+    if (ca >= 0) Fb = Fb + G[(size_t)s * nc + ca] * caw;
+    for (int o = 0; o < 5; ++o) out[o] = Fb * M * w[o];
+  }
+}
+
+// per cell: gather the face contributions whose stencil position maps to this cell
+template <int DIR>
+__global__ void __launch_bounds__(256) k_adj_gather(DevTransport<double> T, const double* __restrict__ U,
+                                                    const double* __restrict__ Cf,
+                                                    double* __restrict__ ubar, double g) {
+  const size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
+  const size_t ncol = (size_t)T.nlon * T.nlat;
+  size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  int i = (int)(c % T.nlon);
+  int j = (int)((c / T.nlon) % T.nlat);
+  int k = (int)(c / ncol);
+  int n = DIR == 0 ? T.nlon : (DIR == 1 ? T.nlat : T.nlev);
+  int bc = DIR == 0 ? T.lon_bc : (DIR == 1 ? (T.lat_bc == 1 ? 1 : 2) : 2);
+  int pos = DIR == 0 ? i : (DIR == 1 ? j : k);
+  long long total = DIR == 0 ? (long long)(T.nlon + 1) * T.nlat * T.nlev
+                  : DIR == 1 ? (long long)T.nlon * (T.nlat + 1) * T.nlev
+                             : (long long)ncol * (T.nlev + 1);
+  auto face_index = [&](int f) -> long long {
+    if (DIR == 0) return ((long long)k * T.nlat + j) * (T.nlon + 1) + f;
+    if (DIR == 1) return ((long long)k * (T.nlat + 1) + f) * T.nlon + i;
+    return (long long)f * ncol + (size_t)j * T.nlon + i;
+  };
+  auto mface = [&](int f) -> double {
+    if (DIR == 0) return g * T.mx[((size_t)k * T.nlat + j) * (T.nlon + 1) + f];
+    if (DIR == 1) return g * T.my[((size_t)k * (T.nlat + 1) + f) * T.nlon + i];
+    return g * T.mz[(size_t)f * ncol + (size_t)j * T.nlon + i];
+  };
+  // candidate faces: windows around pos (and around pos -+ n for a periodic seam), visited
+  // once each in a fixed order
+  int lo[3], hi[3], nw = 0;
+  if (bc == 0) {
+    lo[nw] = pos - n - 5; hi[nw] = pos - n + 5; ++nw;
+  }
+  lo[nw] = pos - 5; hi[nw] = pos + 5; ++nw;
+  if (bc == 0) {
+    lo[nw] = pos + n - 5; hi[nw] = pos + n + 5; ++nw;
+  }
+  for (int s = 0; s < T.ntr; ++s) {
+    double acc = 0.0;
+    int last = -1;
+    for (int wdw = 0; wdw < nw; ++wdw) {
+      int a = lo[wdw] < 0 ? 0 : lo[wdw];
+      int b = hi[wdw] > n ? n : hi[wdw];
+      for (int f = a; f <= b; ++f) {
+        if (f <= last) continue;
+        last = f;
+        double M = mface(f);
+        int up = (M > 0.0) ? f - 1 : f;
+        const double* cf = Cf + ((size_t)s * (size_t)total + (size_t)face_index(f)) * 5;
+        for (int o = 0; o < 5; ++o)
+          if (map_pos(up - 2 + o, n, bc) == pos) acc = acc + cf[o];
+      }
+    }
+    ubar[(size_t)s * nc + c] += acc;
+  }
+}
+
+// ubar = (d f_T / du)^T fbar at stage state U (whose RHS value is F), time factor g
+void launch_transport_rhs_vjp(cudaStream_t st, const DevTransport<double>& T, const double* U,
+                              const double* F, const double* fbar, double* ubar, double* G,
+                              double* Cf, double g) {
+  size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
+  unsigned nb = (unsigned)((nc + 255) / 256);
+  k_adj_cell<<<nb, 256, 0, st>>>(T, U, F, fbar, ubar, G, g);
+  long long nx = (long long)(T.nlon + 1) * T.nlat * T.nlev;
+  long long ny = (long long)T.nlon * (T.nlat + 1) * T.nlev;
+  long long nz = (long long)T.nlon * T.nlat * (T.nlev + 1);
+  k_adj_face<0><<<(unsigned)((nx + 255) / 256), 256, 0, st>>>(T, U, G, Cf, g);
+  k_adj_gather<0><<<nb, 256, 0, st>>>(T, U, Cf, ubar, g);
+  k_adj_face<1><<<(unsigned)((ny + 255) / 256), 256, 0, st>>>(T, U, G, Cf, g);
+  k_adj_gather<1><<<nb, 256, 0, st>>>(T, U, Cf, ubar, g);
+  k_adj_face<2><<<(unsigned)((nz + 255) / 256), 256, 0, st>>>(T, U, G, Cf, g);
+  k_adj_gather<2><<<nb, 256, 0, st>>>(T, U, Cf, ubar, g);
+}
+
+// out = a*x + b*y + c*z over n elements (null operands skipped)
+__global__ void k_lincomb(size_t n, double* __restrict__ out, double a, const double* x, double b,
+                          const double* y, double c, const double* z) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  double r = 0.0;
+  if (x) r = a * x[e];
+  if (y) r = r + b * y[e];
+  if (z) r = r + c * z[e];
+  out[e] = r;
+}
+void launch_lincomb(cudaStream_t st, size_t n, double* out, double a, const double* x, double b,
+                    const double* y, double c, const double* z) {
+  k_lincomb<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, out, a, x, b, y, c, z);
+}
+
+}  // namespace rs

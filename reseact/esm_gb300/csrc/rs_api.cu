@@ -274,6 +274,16 @@ struct rs_handle {
   std::vector<double> dp_host;
   Profile prof;
   rs::DevTransport<double> dt{};
+  // discrete adjoint: recorded macro steps (checkpoint + accepted (t, dt) of both halves)
+  struct Rec {
+    DevBuf<double> ck;
+    double t0 = 0, t1 = 0;
+    std::vector<double> seqT, seqC;  // flattened (t, dt) pairs
+  };
+  bool rec_on = false;
+  std::vector<Rec> recs;
+  DevBuf<double> seqbuf, lam, lam2, ebar, tape, adj, G, Cf;
+  DevBuf<int> nseq;
 };
 
 namespace {
@@ -473,6 +483,9 @@ Ctl make_ctl(rs_handle* h, double t0, double t1, double dt0, const rs_controller
   k.qsmin = c.qsteady_min; k.qsmax = c.qsteady_max; k.qoldinit = c.qoldinit;
   k.ntot = ntot; k.omega = h->omega;
   k.ros_d = h->dm.ros_d;
+  k.seq = nullptr;
+  k.nseq = nullptr;
+  k.seqcap = 0;
   return k;
 }
 
@@ -678,6 +691,11 @@ void rs_destroy(rs_handle* h) {
   for (auto* b : bufs) b->release();
   h->slot_row.release();
   h->slot_col.release();
+  for (auto& r : h->recs) r.ck.release();
+  DevBuf<double>* abufs[] = {&h->seqbuf, &h->lam, &h->lam2, &h->ebar, &h->tape, &h->adj, &h->G,
+                             &h->Cf};
+  for (auto* b : abufs) b->release();
+  h->nseq.release();
   h->ctl.release();
   h->flag.release();
   h->queue.release();
@@ -751,7 +769,7 @@ rs_status rs_set_forcing(rs_handle* h, const rs_forcing* f) {
         h->dp_host.assign(f->dp, f->dp + nc);
         build_vertical(h);
       }
-      h->omega = f->flux_omega;
+      if (f->mx || f->my || f->mz) h->omega = f->flux_omega;
     }
     if (f->temperature) {
       h->T.upload(f->temperature, nc, st);
@@ -810,9 +828,30 @@ rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double*
     stats.dtC_end = *dtC;
     stats.tT_end = t1;
     stats.tC_end = t1;
+    const int seqcap = (int)std::min(h->cfg.maxiters + 1.0, 1.0e6);
+    if (h->rec_on) {
+      if (h->cfg.chem_mode != RS_CHEM_GLOBAL_DT)
+        throw RsError(RS_ERR_UNSUPPORTED, "the adjoint records global-dt chemistry only");
+      h->recs.emplace_back();
+      auto& r = h->recs.back();
+      r.t0 = t0;
+      r.t1 = t1;
+      size_t n = h->nc * h->nsp;
+      r.ck.alloc(n);
+      CK(cudaMemcpyAsync(r.ck.p, h->U[h->cur].p, n * sizeof(double), cudaMemcpyDeviceToDevice,
+                         h->st));
+      h->seqbuf.alloc((size_t)4 * seqcap);
+      h->nseq.alloc(2);
+      CK(cudaMemsetAsync(h->nseq.p, 0, 2 * sizeof(int), h->st));
+    }
     if (h->cfg.do_transport) {
       Ctl init = make_ctl(h, t0, t1, *dtT, h->cfg.ctrl_T, ntot);
       init.cur = h->cur;
+      if (h->rec_on) {
+        init.seq = h->seqbuf.p;
+        init.nseq = h->nseq.p;
+        init.seqcap = seqcap;
+      }
       rs::launch_ctl_init(h->st, h->ctl.p + 0, init);
       h->launches += 1;
       run_adaptive(h, 0, [&](Ctl* c) { transport_attempt(h, c); });
@@ -826,6 +865,11 @@ rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double*
       if (h->cfg.chem_mode == RS_CHEM_GLOBAL_DT) {
         Ctl init = make_ctl(h, t0, t1, *dtC, h->cfg.ctrl_C, ntot);
         init.cur = h->cur;
+        if (h->rec_on) {
+          init.seq = h->seqbuf.p + (size_t)2 * seqcap;
+          init.nseq = h->nseq.p + 1;
+          init.seqcap = seqcap;
+        }
         rs::launch_ctl_init(h->st, h->ctl.p + 1, init);
         h->launches += 1;
         run_adaptive(h, 1, [&](Ctl* c) { chem_attempt(h, c); });
@@ -860,6 +904,21 @@ rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double*
       }
     }
     collect_profile(h);
+    if (h->rec_on) {
+      int ns_h[2] = {0, 0};
+      CK(cudaMemcpyAsync(ns_h, h->nseq.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+      CK(cudaStreamSynchronize(h->st));
+      auto& r = h->recs.back();
+      if (ns_h[0] > seqcap || ns_h[1] > seqcap) throw RsError(RS_ERR_INVALID, "step record overflow");
+      r.seqT.resize((size_t)2 * ns_h[0]);
+      r.seqC.resize((size_t)2 * ns_h[1]);
+      if (ns_h[0])
+        CK(cudaMemcpy(r.seqT.data(), h->seqbuf.p, r.seqT.size() * sizeof(double),
+                      cudaMemcpyDeviceToHost));
+      if (ns_h[1])
+        CK(cudaMemcpy(r.seqC.data(), h->seqbuf.p + (size_t)2 * seqcap,
+                      r.seqC.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    }
     if (!okT || !okC) throw RsError(RS_ERR_MAXITERS, "adaptive solve stopped before t1 (maxiters)");
     CK(cudaMemsetAsync(h->flag.p, 0, sizeof(int), h->st));
     rs::launch_nonfinite(h->st, h->U[h->cur].p, h->nc * h->nsp, h->flag.p);
@@ -1011,6 +1070,203 @@ rs_status rs_get_profile(rs_handle* h, char* buf, size_t buf_len, double* launch
       buf[buf_len - 1] = 0;
     }
     if (n_out) *n_out = n;
+  });
+}
+
+}  // extern "C"
+
+// ====================================================================== discrete adjoint
+namespace {
+
+// SSPRK43 step VJP at fixed (t, dt): recompute the stage states, then walk the stages back
+// (the transpose of rx_traced_integrator.jl:404-437).  Buffers: adj = 11 state-sized slabs.
+void transport_step_vjp(rs_handle* h, const double* u, double t, double dt, const double* lam,
+                        double* out) {
+  size_t n = h->nc * h->nsp;
+  double* V1 = h->adj.p + 0 * n;
+  double* V2 = h->adj.p + 1 * n;
+  double* V4 = h->adj.p + 2 * n;
+  double* F0 = h->adj.p + 3 * n;
+  double* F1 = h->adj.p + 4 * n;
+  double* F2 = h->adj.p + 5 * n;
+  double* F3 = h->adj.p + 6 * n;
+  double* A = h->adj.p + 7 * n;
+  double* B = h->adj.p + 8 * n;
+  double* Wb = h->adj.p + 9 * n;
+  rs::DevTransport<double> T = h->dt;
+  T.mixed = 0;  // the adjoint differentiates the FP64 scheme
+  auto gf = [&](double tt) { return h->omega != 0.0 ? std::cos(h->omega * tt) : 1.0; };
+  double h2 = dt / 2;
+  cudaStream_t st = h->st;
+  rs::launch_transport_rhs(st, T, u, gf(t), F0);
+  rs::launch_lincomb(st, n, V1, 1.0, u, h2, F0, 0.0, nullptr);
+  rs::launch_transport_rhs(st, T, V1, gf(t + 0.5 * dt), F1);
+  rs::launch_lincomb(st, n, V2, 1.0, V1, h2, F1, 0.0, nullptr);
+  rs::launch_transport_rhs(st, T, V2, gf(t + 1.0 * dt), F2);
+  rs::launch_lincomb(st, n, V4, 1.0, V2, h2, F2, 0.0, nullptr);        // u3
+  rs::launch_lincomb(st, n, V4, 2.0 / 3.0, u, 1.0 / 3.0, V4, 0.0, nullptr);  // u4
+  rs::launch_transport_rhs(st, T, V4, gf(t + h2), F3);
+  auto vjp = [&](const double* Us, const double* Fs, double g, const double* fbar, double* ub) {
+    rs::launch_transport_rhs_vjp(st, T, Us, Fs, fbar, ub, h->G.p, h->Cf.p, g);
+  };
+  rs::launch_lincomb(st, n, Wb, h2, lam, 0.0, nullptr, 0.0, nullptr);
+  vjp(V4, F3, gf(t + h2), Wb, A);
+  rs::launch_lincomb(st, n, A, 1.0, A, 1.0, lam, 0.0, nullptr);           // ubar4
+  rs::launch_lincomb(st, n, out, 2.0 / 3.0, A, 0.0, nullptr, 0.0, nullptr);
+  rs::launch_lincomb(st, n, B, 1.0 / 3.0, A, 0.0, nullptr, 0.0, nullptr);  // ubar3 = ubar2
+  rs::launch_lincomb(st, n, Wb, h2, B, 0.0, nullptr, 0.0, nullptr);
+  vjp(V2, F2, gf(t + 1.0 * dt), Wb, A);
+  rs::launch_lincomb(st, n, B, 1.0, B, 1.0, A, 0.0, nullptr);             // ubar2 -> ubar1
+  rs::launch_lincomb(st, n, Wb, h2, B, 0.0, nullptr, 0.0, nullptr);
+  vjp(V1, F1, gf(t + 0.5 * dt), Wb, A);
+  rs::launch_lincomb(st, n, B, 1.0, B, 1.0, A, 0.0, nullptr);             // ubar1 -> ubar0
+  rs::launch_lincomb(st, n, Wb, h2, B, 0.0, nullptr, 0.0, nullptr);
+  vjp(u, F0, gf(t), Wb, A);
+  rs::launch_lincomb(st, n, out, 1.0, out, 1.0, B, 1.0, A);
+}
+
+void ensure_adjoint_buffers(rs_handle* h) {
+  size_t n = h->nc * h->nsp;
+  h->lam.alloc(n);
+  h->lam2.alloc(n);
+  if (!h->ebar.p) {
+    h->ebar.alloc((size_t)h->mt.ns * h->nc);
+    h->ebar.zero(h->st);
+  }
+  if (h->cfg.do_transport) {
+    h->adj.alloc(11 * n);
+    h->G.alloc((size_t)h->ntr * h->nc);
+    const rs_grid& g = h->cfg.grid;
+    size_t fx = (size_t)(g.nlon + 1) * g.nlat * g.nlev, fy = (size_t)g.nlon * (g.nlat + 1) * g.nlev,
+           fz = (size_t)g.nlon * g.nlat * (g.nlev + 1);
+    h->Cf.alloc((size_t)h->ntr * std::max(fx, std::max(fy, fz)) * 5);
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+rs_status rs_record(rs_handle* h, int32_t on) {
+  if (!h) return RS_ERR_INVALID;
+  return guard(h, [&] {
+    if (on) {
+      if (h->cfg.chem_mode != RS_CHEM_GLOBAL_DT)
+        throw RsError(RS_ERR_UNSUPPORTED, "the adjoint records global-dt chemistry only");
+      for (auto& r : h->recs) r.ck.release();
+      h->recs.clear();
+    }
+    h->rec_on = on != 0;
+  });
+}
+
+int32_t rs_record_count(const rs_handle* h) { return h ? (int32_t)h->recs.size() : 0; }
+
+rs_status rs_adjoint_set_lambda(rs_handle* h, const double* lam, size_t n) {
+  if (!h || !lam) return RS_ERR_INVALID;
+  return guard(h, [&] {
+    if (n != h->nc * h->nsp) throw RsError(RS_ERR_INVALID, "state size mismatch");
+    ensure_adjoint_buffers(h);
+    h->io.upload(lam, n, h->st);
+    rs::launch_to_soa(h->st, h->io.p, h->lam.p, h->nlon, h->nlat, h->nlev, h->nsp);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(h->st));
+  });
+}
+
+rs_status rs_adjoint_get_lambda(rs_handle* h, double* lam, size_t n) {
+  if (!h || !lam) return RS_ERR_INVALID;
+  return guard(h, [&] {
+    if (n != h->nc * h->nsp) throw RsError(RS_ERR_INVALID, "state size mismatch");
+    if (!h->lam.p) throw RsError(RS_ERR_STATE, "no adjoint state (rs_adjoint_set_lambda first)");
+    h->io.alloc(n);
+    rs::launch_to_cellmajor(h->st, h->lam.p, h->io.p, h->nlon, h->nlat, h->nlev, h->nsp);
+    CK(cudaMemcpyAsync(lam, h->io.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+  });
+}
+
+rs_status rs_adjoint_get_grad_emission(rs_handle* h, double* g, size_t n) {
+  if (!h || !g) return RS_ERR_INVALID;
+  return guard(h, [&] {
+    if (n != (size_t)h->mt.ns * h->nc) throw RsError(RS_ERR_INVALID, "gradient size mismatch");
+    ensure_adjoint_buffers(h);
+    CK(cudaMemcpyAsync(g, h->ebar.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+  });
+}
+
+rs_status rs_adjoint_reset_grad(rs_handle* h) {
+  if (!h) return RS_ERR_INVALID;
+  return guard(h, [&] {
+    ensure_adjoint_buffers(h);
+    h->ebar.zero(h->st);
+    CK(cudaStreamSynchronize(h->st));
+  });
+}
+
+rs_status rs_backward_macro_step(rs_handle* h, int32_t k) {
+  if (!h) return RS_ERR_INVALID;
+  return guard(h, [&] {
+    if (k < 0 || k >= (int)h->recs.size()) throw RsError(RS_ERR_INVALID, "no such recorded step");
+    if (!h->lam.p) throw RsError(RS_ERR_STATE, "no adjoint state (rs_adjoint_set_lambda first)");
+    ensure_adjoint_buffers(h);
+    ensure_rates(h);
+    const auto& r = h->recs[k];
+    size_t n = h->nc * h->nsp;
+    int nT = (int)(r.seqT.size() / 2), nC = (int)(r.seqC.size() / 2);
+    h->tape.alloc((size_t)(nT + nC + 2) * n);
+    double* tape = h->tape.p;
+    double* R[2] = {tape + (size_t)(nT + nC) * n, tape + (size_t)(nT + nC + 1) * n};
+    cudaStream_t st = h->st;
+    const int clamp = h->cfg.clamp_nonneg;
+    // ---- fixed-sequence replay from the checkpoint, keeping every step's input
+    CK(cudaMemcpyAsync(R[0], r.ck.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    int cur = 0;
+    Ctl* c = h->ctl.p + 2;
+    double ntot = (double)n;
+    for (int j = 0; j < nT + nC; ++j) {
+      bool tr = j < nT;
+      double tj = tr ? r.seqT[2 * j] : r.seqC[2 * (j - nT)];
+      double dj = tr ? r.seqT[2 * j + 1] : r.seqC[2 * (j - nT) + 1];
+      CK(cudaMemcpyAsync(tape + (size_t)j * n, R[cur], n * sizeof(double),
+                         cudaMemcpyDeviceToDevice, st));
+      // tend well past t + dt so that dtc = min(dt, tend - t) is the recorded dt exactly
+      Ctl init = make_ctl(h, tj, tj + 4.0 * dj + 1.0, dj, tr ? h->cfg.ctrl_T : h->cfg.ctrl_C, ntot);
+      init.cur = cur;
+      rs::launch_ctl_init(st, c, init);
+      if (tr) {
+        rs::TransportBufs B{R[0], R[1], h->S1.p, h->S2.p, h->S3.p, h->partial.p};
+        rs::launch_ssprk43_attempt(st, h->dt, c, B, h->cfg.rtol_T, h->cfg.atol_T, clamp);
+      } else {
+        rs::launch_ros23_attempt(h->lc, c, R[0], R[1], h->krates.p,
+                                 h->have_emis ? h->emis.p : nullptr, h->partial.p,
+                                 h->cfg.rtol_C, h->cfg.atol_C, clamp);
+      }
+      rs::launch_replay_accept(st, c);
+      cur ^= 1;
+    }
+    // the final replayed state closes the tape (output of the last step)
+    double* fin = R[cur];
+    auto out_of = [&](int j) -> const double* {
+      return (j + 1 < nT + nC) ? tape + (size_t)(j + 1) * n : fin;
+    };
+    // ---- chemistry steps in reverse, then transport steps in reverse
+    for (int j = nC - 1; j >= 0; --j) {
+      int jj = nT + j;
+      rs::launch_ros23_vjp(h->lc, tape + (size_t)jj * n, clamp ? out_of(jj) : nullptr, h->lam.p,
+                           h->lam2.p, h->krates.p, h->have_emis ? h->emis.p : nullptr,
+                           h->ebar.p, r.seqC[2 * j + 1], clamp);
+      std::swap(h->lam.p, h->lam2.p);
+    }
+    for (int j = nT - 1; j >= 0; --j) {
+      if (clamp) rs::launch_clamp_mask(st, n, h->lam.p, out_of(j));
+      transport_step_vjp(h, tape + (size_t)j * n, r.seqT[2 * j], r.seqT[2 * j + 1], h->lam.p,
+                         h->lam2.p);
+      std::swap(h->lam.p, h->lam2.p);
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(st));
   });
 }
 

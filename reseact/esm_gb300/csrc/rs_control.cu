@@ -58,6 +58,14 @@ __global__ void __launch_bounds__(kRedThreads) k_finalize(Ctl* __restrict__ c,
   c->eest = EEst;
   c->accept = accept;
   if (accept) {
+    if (c->seq) {
+      int k = *c->nseq;
+      if (k < c->seqcap) {
+        c->seq[2 * k] = c->t;
+        c->seq[2 * k + 1] = dtc;
+      }
+      *c->nseq = k + 1;
+    }
     c->cur ^= 1;
     c->t = c->t + dtc;
     c->dt = dt_acc;
@@ -109,6 +117,21 @@ __global__ void k_to_cellmajor(const double* __restrict__ soa, double* __restric
   int j = (int)((c / nlev) % nlat);
   int i = (int)(c / ((size_t)nlev * nlat));
   cm[y] = soa[(size_t)s * nc + ((size_t)k * nlat + j) * nlon + i];
+}
+
+// fixed-sequence replay: accept the attempt unconditionally (tools/adjoint_gradient.jl:647-669)
+__global__ void k_replay_accept(Ctl* __restrict__ c) {
+  c->cur ^= 1;
+  c->t = c->t + c->dtc;
+}
+// lam *= (out > 0): adjoint of the clamp max(raw, 0) (tools/adjoint_gradient.jl:736)
+__global__ void k_clamp_mask(size_t n, double* __restrict__ lam, const double* __restrict__ out) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n && !(out[e] > 0.0)) lam[e] = 0.0;
+}
+void launch_replay_accept(cudaStream_t st, Ctl* ctl) { k_replay_accept<<<1, 1, 0, st>>>(ctl); }
+void launch_clamp_mask(cudaStream_t st, size_t n, double* lam, const double* out) {
+  k_clamp_mask<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, lam, out);
 }
 
 void launch_finalize(cudaStream_t st, Ctl* ctl, const double* partial, int nparts) {

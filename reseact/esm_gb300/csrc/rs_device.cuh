@@ -69,6 +69,9 @@ struct Ctl {
   double g[4];     // SSPRK43 stage factors of the next attempt: t, t+dt/2, t+dt, t+dt/2
   double dto2, dto6, dtgamma;  // dtc/2, dtc/6, dtc*d of the next attempt (shared by all cells)
   double ros_d;    // ROS23 d, for dtgamma
+  double* seq;     // if set: accepted (t, dt) pairs are appended here (adjoint recording)
+  int* nseq;
+  int seqcap;
   int cur;         // state buffer holding the accepted state (0/1)
   int done;
   int accept;

@@ -94,6 +94,18 @@ void launch_transport_rhs(cudaStream_t st, const DevTransport<double>& T, const 
 
 // control (rs_control.cu)
 void launch_ctl_init(cudaStream_t st, Ctl* ctl, const Ctl& init);
+void launch_replay_accept(cudaStream_t st, Ctl* ctl);
+void launch_clamp_mask(cudaStream_t st, size_t n, double* lam, const double* out);
+
+// discrete adjoint (rs_adjoint.cu)
+void launch_ros23_vjp(const LaunchCtx& L, const double* U, const double* Uout, const double* lam,
+                      double* lam_out, const double* kr, const double* em, double* ebar,
+                      double dt, int clamp);
+void launch_transport_rhs_vjp(cudaStream_t st, const DevTransport<double>& T, const double* U,
+                              const double* F, const double* fbar, double* ubar, double* G,
+                              double* Cf, double g);
+void launch_lincomb(cudaStream_t st, size_t n, double* out, double a, const double* x, double b,
+                    const double* y, double c, const double* z);
 void launch_finalize(cudaStream_t st, Ctl* ctl, const double* partial, int nparts);
 void launch_nonfinite(cudaStream_t st, const double* U, size_t n, int* flag);
 void launch_to_soa(cudaStream_t st, const double* cm, double* soa, int nlon, int nlat, int nlev,
