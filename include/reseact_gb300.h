@@ -234,7 +234,7 @@ rs_status rs_adjoint_reset_grad(rs_handle* h);
  * state size), returning the hairer error estimate in *eest (host pointer, may be NULL).
  * No counterpart in the reference.  It allocates nothing, for callers that cannot allocate
  * device memory when they step (a host whose own memory pool owns the device, or a loop that
- * must not synchronise on an allocation): its scratch is a 512 KiB array fixed in the
+ * must not synchronise on an allocation): its scratch is a 524,800-byte array fixed in the
  * library, resolved per device on the first call on that device (make that first call before
  * any stream capture).  Limit: 16,777,216 cells (RS_ERR_INVALID beyond).  All calls share the
  * scratch, so calls that overlap on the GPU (other threads or streams) race; serialise them. */

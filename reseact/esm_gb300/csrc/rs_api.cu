@@ -282,6 +282,7 @@ struct rs_handle {
   };
   bool rec_on = false;
   std::vector<Rec> recs;
+  std::vector<DevBuf<double>> ck_pool;  // checkpoint buffers kept for reuse across recordings
   DevBuf<double> seqbuf, lam, lam2, ebar, tape, adj, G, Cf;
   DevBuf<int> nseq;
 };
@@ -692,6 +693,7 @@ void rs_destroy(rs_handle* h) {
   h->slot_row.release();
   h->slot_col.release();
   for (auto& r : h->recs) r.ck.release();
+  for (auto& b : h->ck_pool) b.release();
   DevBuf<double>* abufs[] = {&h->seqbuf, &h->lam, &h->lam2, &h->ebar, &h->tape, &h->adj, &h->G,
                              &h->Cf};
   for (auto* b : abufs) b->release();
@@ -837,6 +839,10 @@ rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double*
       r.t0 = t0;
       r.t1 = t1;
       size_t n = h->nc * h->nsp;
+      if (!h->ck_pool.empty()) {
+        r.ck = h->ck_pool.back();
+        h->ck_pool.pop_back();
+      }
       r.ck.alloc(n);
       CK(cudaMemcpyAsync(r.ck.p, h->U[h->cur].p, n * sizeof(double), cudaMemcpyDeviceToDevice,
                          h->st));
@@ -1153,7 +1159,11 @@ rs_status rs_record(rs_handle* h, int32_t on) {
     if (on) {
       if (h->cfg.chem_mode != RS_CHEM_GLOBAL_DT)
         throw RsError(RS_ERR_UNSUPPORTED, "the adjoint records global-dt chemistry only");
-      for (auto& r : h->recs) r.ck.release();
+      for (auto& r : h->recs) {
+        h->ck_pool.push_back(r.ck);
+        r.ck.p = nullptr;
+        r.ck.n = 0;
+      }
       h->recs.clear();
     }
     h->rec_on = on != 0;
@@ -1283,7 +1293,9 @@ namespace {
 
 constexpr size_t kNoAllocMaxCells = (size_t)1 << 24;  // 16,777,216 cells
 constexpr size_t kNoAllocParts = kNoAllocMaxCells / rs::kRedThreads;  // 65,536 partial sums
-constexpr size_t kNoAllocBytes = kNoAllocParts * sizeof(double) + 256;  // + one Ctl record
+constexpr size_t kNoAllocCtlBytes = 512;  // room for one controller record
+static_assert(sizeof(Ctl) <= kNoAllocCtlBytes, "controller record outgrew its scratch slot");
+constexpr size_t kNoAllocBytes = kNoAllocParts * sizeof(double) + kNoAllocCtlBytes;  // 524,800 B
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
