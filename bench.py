@@ -47,6 +47,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-forms", action="store_true", help="skip the mixed / batched forms")
+    p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward ratio")
     p.add_argument("--small", action="store_true", help="small grid (profiling/debug)")
     return p.parse_args()
 
@@ -282,6 +283,9 @@ def run_gb300(args):
                            "median_rel_err_vs_fp64": float(np.median(rel))}
             alt.close()
 
+    # ------------------------------------------------------------------ adjoint / forward
+    adjoint = None if args.no_adjoint else measure_adjoint(args, local, barrier)
+
     # ------------------------------------------------------------------ roofline pass
     t, dtT, dtC = t_end, dtT_end, dtC_end
     solver.set_profiling(True)
@@ -338,6 +342,7 @@ def run_gb300(args):
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": "256 MiB flush between timed steps"},
             "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "forms": forms,
+            "adjoint": adjoint,
             "transport": transport, "kernels": kernels, "dominant": dom,
             "attempts_per_step": {"naT": float(np.mean([c[0] for c in counts])),
                                   "nrT": float(np.mean([c[1] for c in counts])),
@@ -349,6 +354,56 @@ def run_gb300(args):
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def measure_adjoint(args, local, barrier):
+    """Adjoint/forward time on the differentiation workload (72x46x47, surface NO emission):
+    after the same warm-up, K macro steps are run forward WITH recording (device checkpoint +
+    accepted step sequence per macro step), then the backward sweep over them (fixed-sequence
+    replay, chemistry then transport step VJPs, emission gradient), both timed with CUDA events
+    on the library stream; objective J = sum_surface (O3_end - O3_obs)^2."""
+    import torch
+    from reseact.esm_gb300 import Solver, workloads
+    w = workloads.c4()
+    g = w.grid
+    s = Solver.for_workload(w, device=local)
+    stream = torch.cuda.ExternalStream(s.stream())
+    s.set_state(w.u0_cellmajor())
+    t, a, b = 0.0, w.dt0_T, w.dt0_C
+    for _ in range(args.warmup):
+        _, a, b, _ = s.macro_step(t, t + w.dt_macro, a, b)
+        t += w.dt_macro
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    s.record(True)
+    barrier()
+    e0.record(stream)
+    for _ in range(args.steps):
+        _, a, b, _ = s.macro_step(t, t + w.dt_macro, a, b)
+        t += w.dt_macro
+    e1.record(stream)
+    s.record(False)
+    iO3 = w.mech.species.index("O3")
+    uend = workloads.cellmajor_to_soa(s.get_state(), w.nsp, g["nlon"], g["nlat"], g["nlev"])
+    obs = 30.0 * np.exp(0.3 * np.random.default_rng(44).standard_normal((g["nlat"], g["nlon"])))
+    lam = np.zeros_like(uend)
+    lam[iO3, 0] = 2 * (uend[iO3, 0] - obs)
+    lam_cm = workloads.soa_to_cellmajor(lam, g["nlon"], g["nlat"], g["nlev"])
+    barrier()
+    e1b = torch.cuda.Event(enable_timing=True)
+    e1b.record(stream)
+    _, grad = s.adjoint_backward(lam_cm)
+    e2.record(stream)
+    barrier()
+    fwd, bwd = e0.elapsed_time(e1), e1b.elapsed_time(e2)
+    iNO = w.mech.species.index("NO")
+    out = {"workload": "C4 72x46x47 SuperFast FP64, J = sum_surface (O3_end - O3_obs)^2, "
+                       "gradient w.r.t. surface NO emission",
+           "macro_steps": args.steps, "forward_ms": round(fwd, 3), "backward_ms": round(bwd, 3),
+           "adjoint_over_forward": round(bwd / fwd, 3),
+           "grad_norm": float(np.linalg.norm(grad[iNO, 0])),
+           "reference_adjoint_over_forward": 2.51}
+    s.close()
+    return out
 
 
 def cpu_baseline_from_state(w, u_cm, t, dtT, dtC):

@@ -1,0 +1,99 @@
+"""Size-independent properties at the benchmark's full sizes (C2 144x91x47, C3 2^20 cells),
+where the oracle cannot follow in seconds: exact CWC freestream, air-mass conservation,
+non-negativity, bitwise determinism of repeated steps, mixed precision within 1e-6 of FP64,
+and per-cell chemistry on 2^20 cells checked cell-for-cell on a sample against the oracle
+(chemistry never couples cells, so a sampled sub-grid is the same computation)."""
+import numpy as np
+import pytest
+
+from reseact.esm_gb300 import Solver, abi, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def c2():
+    return workloads.c2()
+
+
+def test_c2_fullsize_cwc_freestream(c2):
+    w = c2
+    s = Solver.for_workload(w, do_chemistry=False)
+    u = w.u0.copy()
+    u[:-1] = 1.0
+    g = w.grid
+    s.set_state(workloads.soa_to_cellmajor(u, g["nlon"], g["nlat"], g["nlev"]))
+    t, a = 0.0, 15.0
+    for _ in range(2):
+        _, a, _, _ = s.macro_step(t, t + 600.0, a, 1.0)
+        t += 600.0
+    out = s.get_state().reshape(-1, w.nsp)
+    assert np.all(out[:, :-1] == 1.0)
+
+
+def test_c2_fullsize_determinism_mass_nonneg(c2):
+    w = c2
+    g = w.grid
+    phie = workloads.lat_edges(g)
+    area = (np.sin(np.radians(phie[1:])) - np.sin(np.radians(phie[:-1])))[None, :, None]
+    res = []
+    for _ in range(2):
+        s = Solver.for_workload(w)
+        s.set_state(w.u0_cellmajor())
+        t, a, b = 0.0, 15.0, 0.5
+        for _ in range(2):
+            _, a, b, _ = s.macro_step(t, t + 600.0, a, b)
+            t += 600.0
+        res.append(s.get_state())
+        s.close()
+    assert np.array_equal(res[0], res[1])
+    u0 = w.u0
+    u1 = workloads.cellmajor_to_soa(res[0], w.nsp, g["nlon"], g["nlat"], g["nlev"])
+    m0, m1 = (u0[-1] * area).sum(), (u1[-1] * area).sum()
+    assert abs(m1 / m0 - 1) < 1e-13
+    assert np.all(u1 >= 0.0) and np.all(np.isfinite(u1))
+
+
+def test_c2_fullsize_mixed_within_1e6(c2):
+    w = c2
+    out = []
+    for prec in (abi.RS_PREC_FP64, abi.RS_PREC_MIXED):
+        s = Solver.for_workload(w, precision=prec)
+        s.set_state(w.u0_cellmajor())
+        t, a, b = 0.0, 15.0, 0.5
+        for _ in range(2):
+            _, a, b, _ = s.macro_step(t, t + 600.0, a, b)
+            t += 600.0
+        out.append(s.get_state())
+        s.close()
+    rel = np.abs(out[1] - out[0]) / np.maximum(np.abs(out[0]), 1e-9)
+    assert rel.max() < 1e-6, rel.max()
+
+
+def test_c3_fullsize_per_cell_sample_vs_oracle():
+    from oracle import oracle
+    w = workloads.c3()  # 2^20 cells, synthetic 30 x 60
+    s = Solver.for_workload(w)
+    s.set_state(w.u0_cellmajor())
+    rc, _, _, st = s.macro_step(0.0, 600.0, 1.0, 1e-3)
+    assert rc == 0
+    got = workloads.cellmajor_to_soa(s.get_state(), w.nsp, w.grid["nlon"], w.grid["nlat"], 1)
+    assert np.all(np.isfinite(got)) and np.all(got >= 0.0)
+    # oracle on 1024 sampled cells (one row of the 1024 x 1024 grid), same T and inputs
+    k = s.rates()
+    j = 517
+    sub = workloads.c3(ncells=1024)
+    sub.u0 = np.ascontiguousarray(w.u0[:, :, j:j + 1, :])
+    sub.forcing["temperature"] = w.forcing["temperature"][:, j:j + 1, :]
+    mabi = abi.MechanismABI(sub.mech)
+    cfg = sub.config(mabi)
+    o = oracle.Oracle(cfg, sub.forcing_abi(), mabi)
+    o.set_rates(np.ascontiguousarray(k[:, :, j:j + 1, :]))
+    u = np.ascontiguousarray(sub.u0.copy())
+    orc, _, steps = o.chem_per_cell(u, 0.0, 600.0, 1e-3)
+    assert orc == 0
+    ref = u
+    gsub = got[:, :, j:j + 1, :]
+    bound = cfg.rtol_C * np.abs(ref) + cfg.atol_C
+    assert np.all(np.abs(gsub - ref) <= 2.0 * bound)
+    assert np.median(np.abs(gsub - ref) / np.maximum(np.abs(ref), cfg.atol_C)) < 1e-9
