@@ -285,6 +285,16 @@ struct rs_handle {
   std::vector<DevBuf<double>> ck_pool;  // checkpoint buffers kept for reuse across recordings
   DevBuf<double> seqbuf, lam, lam2, ebar, tape, adj, G, Cf;
   DevBuf<int> nseq;
+  // device-driven adaptive loops: one CUDA graph per half, a conditional WHILE node whose body
+  // is one attempt + the controller; rebuilt when forcing or rate constants change
+  struct LoopGraph {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ex = nullptr;
+    bool valid = false;
+  };
+  LoopGraph loops[2];
+  cudaStream_t cap = nullptr;
+  bool use_graphs = true;
 };
 
 namespace {
@@ -542,6 +552,73 @@ void chem_attempt(rs_handle* h, Ctl* c) {
   h->launches += 2;
 }
 
+void drop_graph(rs_handle::LoopGraph& L) {
+  if (L.ex) cudaGraphExecDestroy(L.ex);
+  if (L.g) cudaGraphDestroy(L.g);
+  L.ex = nullptr;
+  L.g = nullptr;
+  L.valid = false;
+}
+
+void invalidate_graphs(rs_handle* h) {
+  for (auto& L : h->loops) L.valid = false;
+}
+
+// Build the device loop of one half: WHILE(cond) { attempt kernels; finalize + set cond }.
+void build_loop_graph(rs_handle* h, int slot) {
+  auto& L = h->loops[slot];
+  drop_graph(L);
+  if (!h->cap) CK(cudaStreamCreateWithFlags(&h->cap, cudaStreamNonBlocking));
+  CK(cudaGraphCreate(&L.g, 0));
+  cudaGraphConditionalHandle cond;
+  CK(cudaGraphConditionalHandleCreate(&cond, L.g, 1, cudaGraphCondAssignDefault));
+  // cudaGraphNodeParams has no default constructor (a union of non-trivial members):
+  // zero-initialised raw storage, then the conditional member
+  alignas(cudaGraphNodeParams) unsigned char raw[sizeof(cudaGraphNodeParams)];
+  std::memset(raw, 0, sizeof(raw));
+  cudaGraphNodeParams* np = reinterpret_cast<cudaGraphNodeParams*>(raw);
+  np->type = cudaGraphNodeTypeConditional;
+  np->conditional.handle = cond;
+  np->conditional.type = cudaGraphCondTypeWhile;
+  np->conditional.size = 1;
+  cudaGraphNode_t node;
+  CK(cudaGraphAddNode(&node, L.g, nullptr, nullptr, 0, np));
+  cudaGraph_t body = np->conditional.phGraph_out[0];
+  CK(cudaStreamBeginCaptureToGraph(h->cap, body, nullptr, nullptr, 0,
+                                   cudaStreamCaptureModeRelaxed));
+  Ctl* c = h->ctl.p + slot;
+  int nparts = (int)((h->nc + 255) / 256);
+  if (slot == 0) {
+    rs::TransportBufs B{h->U[0].p, h->U[1].p, h->S1.p, h->S2.p, h->S3.p, h->partial.p};
+    rs::launch_ssprk43_attempt(h->cap, h->dt, c, B, h->cfg.rtol_T, h->cfg.atol_T,
+                               h->cfg.clamp_nonneg);
+  } else {
+    rs::LaunchCtx lc = h->lc;
+    lc.stream = h->cap;
+    rs::launch_ros23_attempt(lc, c, h->U[0].p, h->U[1].p, h->krates.p,
+                             h->have_emis ? h->emis.p : nullptr, h->partial.p, h->cfg.rtol_C,
+                             h->cfg.atol_C, h->cfg.clamp_nonneg);
+  }
+  rs::launch_finalize_graph(h->cap, c, h->partial.p, nparts, cond);
+  cudaGraph_t captured = nullptr;
+  CK(cudaStreamEndCapture(h->cap, &captured));
+  CK(cudaGraphInstantiate(&L.ex, L.g, 0));
+  L.valid = true;
+}
+
+// Run one adaptive solve of half `slot` as a single graph launch; the host reads the
+// controller once at the end.
+void run_adaptive_graph(rs_handle* h, int slot) {
+  auto& L = h->loops[slot];
+  if (!L.valid) build_loop_graph(h, slot);
+  CK(cudaGraphLaunch(L.ex, h->st));
+  CK(cudaMemcpyAsync(&h->hctl[slot], h->ctl.p + slot, sizeof(Ctl), cudaMemcpyDeviceToHost,
+                     h->st));
+  CK(cudaStreamSynchronize(h->st));
+  h->launches += h->hctl[slot].iters *
+                 (slot == 0 ? (h->cfg.precision == RS_PREC_MIXED ? 18 : 17) : 2);
+}
+
 rs_status guard(rs_handle* h, const std::function<void()>& fn);
 
 }  // namespace
@@ -679,6 +756,8 @@ rs_status rs_create(const rs_config* cfg, rs_handle** out) {
 void rs_destroy(rs_handle* h) {
   if (!h) return;
   if (h->st) cudaStreamSynchronize(h->st);
+  for (auto& L : h->loops) drop_graph(L);
+  if (h->cap) cudaStreamDestroy(h->cap);
   for (auto& b : h->itabs) b.release();
   for (auto& b : h->dtabs) b.release();
   DevBuf<float>* fbufs[] = {&h->qhi, &h->qlo, &h->vsA32, &h->vsB32, &h->veAB32, &h->veC32,
@@ -789,6 +868,7 @@ rs_status rs_set_forcing(rs_handle* h, const rs_forcing* f) {
     }
     h->have_forcing = true;
     refresh_dt(h);
+    invalidate_graphs(h);
     CK(cudaStreamSynchronize(st));
   });
 }
@@ -810,6 +890,7 @@ rs_status rs_set_rate_constants(rs_handle* h, const double* k, size_t n) {
     h->krates.upload(k, n, h->st);
     h->rates_dirty = false;
     h->rates_override = true;
+    invalidate_graphs(h);
     CK(cudaStreamSynchronize(h->st));
   });
 }
@@ -860,7 +941,8 @@ rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double*
       }
       rs::launch_ctl_init(h->st, h->ctl.p + 0, init);
       h->launches += 1;
-      run_adaptive(h, 0, [&](Ctl* c) { transport_attempt(h, c); });
+      if (h->use_graphs && !h->prof.on) run_adaptive_graph(h, 0);
+      else run_adaptive(h, 0, [&](Ctl* c) { transport_attempt(h, c); });
       const Ctl& c = h->hctl[0];
       h->cur = c.cur;
       stats.naT = c.nacc; stats.nrT = c.nrej; stats.dtT_end = c.dt; stats.tT_end = c.t;
@@ -878,7 +960,8 @@ rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double*
         }
         rs::launch_ctl_init(h->st, h->ctl.p + 1, init);
         h->launches += 1;
-        run_adaptive(h, 1, [&](Ctl* c) { chem_attempt(h, c); });
+        if (h->use_graphs && !h->prof.on) run_adaptive_graph(h, 1);
+        else run_adaptive(h, 1, [&](Ctl* c) { chem_attempt(h, c); });
         const Ctl& c = h->hctl[1];
         h->cur = c.cur;
         stats.naC = c.nacc; stats.nrC = c.nrej; stats.dtC_end = c.dt; stats.tC_end = c.t;

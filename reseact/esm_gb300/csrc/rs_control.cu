@@ -33,10 +33,9 @@ __device__ void prepare_next(Ctl* c) {
   }
 }
 
-__global__ void __launch_bounds__(kRedThreads) k_finalize(Ctl* __restrict__ c,
-                                                          const double* __restrict__ partial,
-                                                          int nparts) {
-  __shared__ double sm[kRedThreads];
+// One attempt's close-out (all threads of one 256-thread block); returns in every thread.
+__device__ void finalize_body(Ctl* __restrict__ c, const double* __restrict__ partial,
+                              int nparts, double* sm) {
   if (c->done) return;
   double acc = 0.0;
   for (int q = threadIdx.x; q < nparts; q += kRedThreads) acc = acc + partial[q];
@@ -77,6 +76,25 @@ __global__ void __launch_bounds__(kRedThreads) k_finalize(Ctl* __restrict__ c,
   }
   c->iters += 1.0;
   prepare_next(c);
+}
+
+__global__ void __launch_bounds__(kRedThreads) k_finalize(Ctl* __restrict__ c,
+                                                          const double* __restrict__ partial,
+                                                          int nparts) {
+  __shared__ double sm[kRedThreads];
+  finalize_body(c, partial, nparts, sm);
+}
+
+// Graph-resident variant: also drives the conditional WHILE node of the device loop.  It sets
+// the loop condition on EVERY path (0 once the controller is done), and the controller raises
+// done after at most maxiters attempts, so the graph loop always terminates.
+__global__ void __launch_bounds__(kRedThreads) k_finalize_graph(
+    Ctl* __restrict__ c, const double* __restrict__ partial, int nparts,
+    cudaGraphConditionalHandle loop) {
+  __shared__ double sm[kRedThreads];
+  finalize_body(c, partial, nparts, sm);
+  __syncthreads();
+  if (threadIdx.x == 0) cudaGraphSetConditional(loop, c->done ? 0u : 1u);
 }
 
 __global__ void k_ctl_init(Ctl* __restrict__ c, Ctl init) {
@@ -136,6 +154,10 @@ void launch_clamp_mask(cudaStream_t st, size_t n, double* lam, const double* out
 
 void launch_finalize(cudaStream_t st, Ctl* ctl, const double* partial, int nparts) {
   k_finalize<<<1, kRedThreads, 0, st>>>(ctl, partial, nparts);
+}
+void launch_finalize_graph(cudaStream_t st, Ctl* ctl, const double* partial, int nparts,
+                           cudaGraphConditionalHandle loop) {
+  k_finalize_graph<<<1, kRedThreads, 0, st>>>(ctl, partial, nparts, loop);
 }
 void launch_ctl_init(cudaStream_t st, Ctl* ctl, const Ctl& init) {
   k_ctl_init<<<1, 1, 0, st>>>(ctl, init);

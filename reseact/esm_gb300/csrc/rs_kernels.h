@@ -107,6 +107,8 @@ void launch_transport_rhs_vjp(cudaStream_t st, const DevTransport<double>& T, co
 void launch_lincomb(cudaStream_t st, size_t n, double* out, double a, const double* x, double b,
                     const double* y, double c, const double* z);
 void launch_finalize(cudaStream_t st, Ctl* ctl, const double* partial, int nparts);
+void launch_finalize_graph(cudaStream_t st, Ctl* ctl, const double* partial, int nparts,
+                           cudaGraphConditionalHandle loop);
 void launch_nonfinite(cudaStream_t st, const double* U, size_t n, int* flag);
 void launch_to_soa(cudaStream_t st, const double* cm, double* soa, int nlon, int nlat, int nlev,
                    int nsp);
