@@ -348,6 +348,178 @@ __global__ void __launch_bounds__(kFluxThreads) k_flux_z(DevTransport<double> T,
   }
 }
 
+// ------------------------------------------------------------------ fused pencil kernels
+// FP64 face fluxes with each cell's monotone slope and each edge value computed ONCE per
+// stage (the per-face kernels above recompute three slopes and two edges for every face):
+// a block stages whole pencils (a lon row; or 32 adjacent columns of a lat line / vertical
+// column) in shared memory, then slopes, then edges, then the upwind limiter and flux of
+// each face.  Same expressions in the same order as ppm_face_u / the vertical branch, so the
+// fluxes are bit-identical to the per-face kernels.
+constexpr int kPencil = 32;  // pencils per block in the y / z kernels
+
+__global__ void __launch_bounds__(128) k_flux_x_fused(DevTransport<double> T, StageSel sel) {
+  const double* Q;
+  double g;
+  if (!resolve_stage(sel, Q, g)) return;
+  extern __shared__ double smx[];
+  const int n = T.nlon, nf = n + 1, L = n + 6;
+  double* V = smx;           // V[p+3], p in [-3, n+2]
+  double* D = smx + L;       // D[p+3], slopes p in [-2, n+1]
+  double* E = smx + 2 * L;   // E[f+3], edge between f-1 and f, f in [-1, n+1]
+  const int row = blockIdx.x;  // (k, j)
+  const int j = row % T.nlat, k = row / T.nlat;
+  const size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
+  const size_t rbase = ((size_t)k * T.nlat + j) * n;
+  for (int s = 0; s < T.ntr; ++s) {
+    const double* q = Q + (size_t)s * nc + rbase;
+    for (int p = threadIdx.x - 3; p <= n + 2; p += blockDim.x) {
+      double v;
+      if (p < 0 || p >= n) {
+        if (T.lon_bc == 0) v = q[((p % n) + n) % n];
+        else v = (p < 0 ? T.qw : T.qe)[((size_t)s * T.nlev + k) * T.nlat + j];
+      } else {
+        v = q[p];
+      }
+      V[p + 3] = v;
+    }
+    __syncthreads();
+    for (int p = threadIdx.x - 2; p <= n + 1; p += blockDim.x)
+      D[p + 3] = slope_u(V[p + 2], V[p + 3], V[p + 4]);
+    __syncthreads();
+    for (int f = threadIdx.x - 1; f <= n + 1; f += blockDim.x)
+      E[f + 3] = V[f + 2] + 0.5 * (V[f + 3] - V[f + 2]) - (D[f + 3] - D[f + 2]) * kOneSixth;
+    __syncthreads();
+    for (int f = threadIdx.x; f <= n; f += blockDim.x) {
+      double M = g * T.mx[((size_t)k * T.nlat + j) * nf + f];
+      bool right = M > 0.0;
+      int up = right ? f - 1 : f;
+      double aL = E[up + 3], aR = E[up + 4];
+      limit(V[up + 3], aL, aR);
+      T.fx[((size_t)s * T.nlev * T.nlat + (size_t)k * T.nlat + j) * nf + f] = M * (right ? aR : aL);
+    }
+    __syncthreads();
+  }
+}
+
+// y: block = 32 adjacent i at one level, all j; threads (32, 8)
+__global__ void __launch_bounds__(256) k_flux_y_fused(DevTransport<double> T, StageSel sel) {
+  const double* Q;
+  double g;
+  if (!resolve_stage(sel, Q, g)) return;
+  extern __shared__ double smy[];
+  const int n = T.nlat, nfj = n + 1, L = n + 6;
+  double* V = smy;                    // [L][kPencil]
+  double* D = smy + L * kPencil;
+  double* E = smy + 2 * L * kPencil;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int ntile = (T.nlon + kPencil - 1) / kPencil;
+  const int k = blockIdx.x / ntile;
+  const int i = (blockIdx.x % ntile) * kPencil + tx;
+  const bool live = i < T.nlon;
+  const size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
+  const size_t fplane = (size_t)T.nlev * nfj * T.nlon;
+  const bool open = T.lat_bc == 1;
+  for (int s = 0; s < T.ntr; ++s) {
+    const double* q = Q + (size_t)s * nc + (size_t)k * T.nlat * T.nlon;
+    for (int p = (int)ty - 3; p <= n + 2; p += blockDim.y) {
+      double v = 0.0;
+      if (live) {
+        if (p < 0 || p >= n) {
+          if (open) v = (p < 0 ? T.qs : T.qn)[((size_t)s * T.nlev + k) * T.nlon + i];
+          else v = q[(size_t)(p < 0 ? -1 - p : 2 * n - 1 - p) * T.nlon + i];
+        } else {
+          v = q[(size_t)p * T.nlon + i];
+        }
+      }
+      V[(p + 3) * kPencil + tx] = v;
+    }
+    __syncthreads();
+    for (int p = (int)ty - 2; p <= n + 1; p += blockDim.y)
+      D[(p + 3) * kPencil + tx] = slope_u(V[(p + 2) * kPencil + tx], V[(p + 3) * kPencil + tx],
+                                          V[(p + 4) * kPencil + tx]);
+    __syncthreads();
+    for (int f = (int)ty - 1; f <= n + 1; f += blockDim.y) {
+      double vl = V[(f + 2) * kPencil + tx], vr = V[(f + 3) * kPencil + tx];
+      E[(f + 3) * kPencil + tx] =
+          vl + 0.5 * (vr - vl) - (D[(f + 3) * kPencil + tx] - D[(f + 2) * kPencil + tx]) * kOneSixth;
+    }
+    __syncthreads();
+    if (live) {
+      for (int f = ty; f <= n; f += blockDim.y) {
+        size_t fb = ((size_t)k * nfj + f) * T.nlon + i;
+        if (!open && (f == 0 || f == n)) {
+          T.fy[(size_t)s * fplane + fb] = 0.0;
+          continue;
+        }
+        double M = g * T.my[fb];
+        bool right = M > 0.0;
+        int up = right ? f - 1 : f;
+        double aL = E[(up + 3) * kPencil + tx], aR = E[(up + 4) * kPencil + tx];
+        limit(V[(up + 3) * kPencil + tx], aL, aR);
+        T.fy[(size_t)s * fplane + fb] = M * (right ? aR : aL);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// z: block = 32 adjacent columns (same j), all levels; dp-weighted coefficients
+__global__ void __launch_bounds__(256) k_flux_z_fused(DevTransport<double> T, StageSel sel) {
+  const double* Q;
+  double g;
+  if (!resolve_stage(sel, Q, g)) return;
+  extern __shared__ double smz[];
+  const int n = T.nlev, L = n + 6;
+  double* V = smz;
+  double* D = smz + L * kPencil;
+  double* E = smz + 2 * L * kPencil;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const size_t ncol = (size_t)T.nlon * T.nlat;
+  const size_t col = (size_t)blockIdx.x * kPencil + tx;
+  const bool live = col < ncol;
+  const size_t nc = ncol * n;
+  const size_t fplane = ncol * (n + 1);
+  for (int s = 0; s < T.ntr; ++s) {
+    const double* q = Q + (size_t)s * nc;
+    for (int p = (int)ty - 3; p <= n + 2; p += blockDim.y) {
+      int pp = p < 0 ? -1 - p : (p >= n ? 2 * n - 1 - p : p);
+      V[(p + 3) * kPencil + tx] = live ? q[(size_t)pp * ncol + col] : 0.0;
+    }
+    __syncthreads();
+    for (int p = (int)ty - 1; p <= n; p += blockDim.y) {  // slopes of cells -1..n
+      double sA = live ? T.vsA[(size_t)(p + 1) * ncol + col] : 0.0;
+      double sB = live ? T.vsB[(size_t)(p + 1) * ncol + col] : 0.0;
+      D[(p + 3) * kPencil + tx] = slope_n(V[(p + 2) * kPencil + tx], V[(p + 3) * kPencil + tx],
+                                          V[(p + 4) * kPencil + tx], sA, sB);
+    }
+    __syncthreads();
+    for (int e = ty; e <= n; e += blockDim.y) {  // edges 0..n (cells e-1 | e)
+      double eab = live ? T.veAB[(size_t)e * ncol + col] : 0.0;
+      double ec = live ? T.veC[(size_t)e * ncol + col] : 0.0;
+      double ed = live ? T.veD[(size_t)e * ncol + col] : 0.0;
+      double vl = V[(e + 2) * kPencil + tx], vr = V[(e + 3) * kPencil + tx];
+      E[(e + 3) * kPencil + tx] =
+          vl + eab * (vr - vl) + ec * D[(e + 3) * kPencil + tx] + ed * D[(e + 2) * kPencil + tx];
+    }
+    __syncthreads();
+    if (live) {
+      for (int kf = ty; kf <= n; kf += blockDim.y) {
+        if (kf == 0 || kf == n) {
+          T.fz[(size_t)s * fplane + (size_t)kf * ncol + col] = 0.0;
+          continue;
+        }
+        double M = g * T.mz[(size_t)kf * ncol + col];
+        bool right = M > 0.0;
+        int up = right ? kf - 1 : kf;
+        double aL = E[(up + 3) * kPencil + tx], aR = E[(up + 4) * kPencil + tx];
+        limit(V[(up + 3) * kPencil + tx], aL, aR);
+        T.fz[(size_t)s * fplane + (size_t)kf * ncol + col] = M * (right ? aR : aL);
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // ------------------------------------------------------------------ stage kernel
 __device__ __forceinline__ void split_store(const DevTransport<double>& T, size_t x, double v) {
   float hi = (float)v;
@@ -528,12 +700,30 @@ __global__ void __launch_bounds__(kRedThreads) k_rhs_eval(DevTransport<double> T
 }
 
 static void launch_fluxes(cudaStream_t st, const DevTransport<double>& T, const StageSel& sel) {
-  long long nx = (long long)(T.nlon + 1) * T.nlat * T.nlev;
-  long long ny = (long long)T.nlon * (T.nlat + 1) * T.nlev;
-  long long nz = (long long)T.nlon * T.nlat * (T.nlev + 1);
-  k_flux_x<<<(unsigned)((nx + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);
-  k_flux_y<<<(unsigned)((ny + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);
-  k_flux_z<<<(unsigned)((nz + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);
+  if (T.mixed) {  // FP32 deviation-form reconstruction, one thread per face
+    long long nx = (long long)(T.nlon + 1) * T.nlat * T.nlev;
+    long long ny = (long long)T.nlon * (T.nlat + 1) * T.nlev;
+    long long nz = (long long)T.nlon * T.nlat * (T.nlev + 1);
+    k_flux_x<<<(unsigned)((nx + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);
+    k_flux_y<<<(unsigned)((ny + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);
+    k_flux_z<<<(unsigned)((nz + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);
+    return;
+  }
+  size_t shx = 3 * (size_t)(T.nlon + 6) * sizeof(double);
+  size_t shy = 3 * (size_t)(T.nlat + 6) * kPencil * sizeof(double);
+  size_t shz = 3 * (size_t)(T.nlev + 6) * kPencil * sizeof(double);
+  static bool attr_set = false;
+  if (!attr_set) {  // allow > 48 KB of dynamic shared memory for long pencils
+    cudaFuncSetAttribute(k_flux_x_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_flux_y_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_flux_z_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr_set = true;
+  }
+  unsigned ntile = (unsigned)((T.nlon + kPencil - 1) / kPencil);
+  size_t ncol = (size_t)T.nlon * T.nlat;
+  k_flux_x_fused<<<(unsigned)(T.nlat * T.nlev), 128, shx, st>>>(T, sel);
+  k_flux_y_fused<<<ntile * (unsigned)T.nlev, dim3(kPencil, 8), shy, st>>>(T, sel);
+  k_flux_z_fused<<<(unsigned)((ncol + kPencil - 1) / kPencil), dim3(kPencil, 8), shz, st>>>(T, sel);
 }
 
 void launch_ssprk43_attempt(cudaStream_t st, const DevTransport<double>& T, const Ctl* ctl,
