@@ -157,7 +157,8 @@ typedef struct rs_forcing {
 /* Per-macro-step statistics (op_split.jl:159-163 return tuple plus the carried dts). */
 typedef struct rs_stats {
   double naT, nrT;       /* transport accepted / rejected attempts */
-  double naC, nrC;       /* chemistry accepted / rejected attempts (global-dt mode) */
+  double naC, nrC;       /* chemistry accepted / rejected attempts (global-dt mode); in
+                            per-cell mode the accepted / rejected substeps summed over cells */
   double dtT_end, dtC_end;
   double tT_end, tC_end; /* time reached by each half (== t1 on success) */
   double chem_cell_steps;  /* per-cell mode: sum over cells of accepted substeps */
@@ -210,6 +211,13 @@ rs_status rs_single_step(rs_handle* h, int32_t op, double t, double dt, const do
 rs_status rs_state_device_ptr(rs_handle* h, void** d_state);
 /* The handle's CUDA stream (cudaStream_t), for callers timing with CUDA events. */
 void* rs_stream(rs_handle* h);
+
+/* Project-written autotuner (no reference counterpart): times candidate launch shapes on the
+ * handle's current state and forcing -- threads per block x blocks per SM ("cells per block")
+ * of the per-cell chemistry kernel (three attempts per cell on scratch copies), threads per
+ * lon row and pencil width x rows per block (the halo tile) of the transport kernels -- keeps
+ * the fastest for this handle and writes a JSON report of every candidate into buf. */
+rs_status rs_autotune(rs_handle* h, char* buf, size_t buf_len);
 
 /* Discrete adjoint (tools/adjoint_gradient.jl:609-835; step VJPs rx_traced_integrator.jl:610-623).
  * rs_record(h, 1) clears and starts recording: every rs_macro_step then keeps a device

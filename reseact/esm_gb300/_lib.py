@@ -19,6 +19,7 @@ SYMBOLS = [
     "rs_set_profiling", "rs_get_profile", "rs_reset_profile", "rs_ros23_attempt_noalloc",
     "rs_record", "rs_record_count", "rs_adjoint_set_lambda", "rs_adjoint_get_lambda",
     "rs_backward_macro_step", "rs_adjoint_get_grad_emission", "rs_adjoint_reset_grad",
+    "rs_autotune",
 ]
 
 
@@ -81,6 +82,8 @@ def _declare(L):
     L.rs_backward_macro_step.restype = C.c_int
     L.rs_adjoint_reset_grad.argtypes = [vp]
     L.rs_adjoint_reset_grad.restype = C.c_int
+    L.rs_autotune.argtypes = [vp, C.c_char_p, sz]
+    L.rs_autotune.restype = C.c_int
     return L
 
 
@@ -222,6 +225,13 @@ class Solver:
         g = np.empty(ns * self.nc)
         self._check(self.L.rs_adjoint_get_grad_emission(self.h, _p(g), g.size))
         return out, g.reshape(ns, self.nlev, self.nlat, self.nlon)
+
+    def autotune(self):
+        """Pick the launch shapes of this handle's kernels by timing; returns the report."""
+        import json
+        buf = C.create_string_buffer(16384)
+        self._check(self.L.rs_autotune(self.h, buf, 16384))
+        return json.loads(buf.value.decode())
 
     def stream(self):
         return self.L.rs_stream(self.h)

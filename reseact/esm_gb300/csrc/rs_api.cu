@@ -260,7 +260,7 @@ struct rs_handle {
   // state and scratch
   DevBuf<double> U[2], S1, S2, S3, fx, fy, fz, partial, krates, T, P, emis, io, io2;
   DevBuf<double> mx, my, mz, qw, qe, qs, qn, gx, gylo, gyhi, vsA, vsB, veAB, veC, veD, dtcell,
-      stepcell;
+      stepcell, totals;
   DevBuf<float> qhi, qlo, vsA32, vsB32, veAB32, veC32, veD32;  // mixed-precision transport
   DevBuf<Ctl> ctl;  // [0] transport, [1] chemistry, [2] single-step scratch
   DevBuf<int> flag;
@@ -295,6 +295,11 @@ struct rs_handle {
   LoopGraph loops[2];
   cudaStream_t cap = nullptr;
   bool use_graphs = true;
+  // launch shapes picked by rs_autotune (defaults until it runs)
+  struct Tune {
+    int pc_threads = 128, pc_blocks_per_sm = 4;      // per-cell chemistry kernel
+    int pencil = 32, rows = 8, xthreads = 128;        // transport pencil kernels
+  } tune;
 };
 
 namespace {
@@ -482,6 +487,9 @@ void refresh_dt(rs_handle* h) {
   T.qhi = h->qhi.p; T.qlo = h->qlo.p;
   T.vsA32 = h->vsA32.p; T.vsB32 = h->vsB32.p; T.veAB32 = h->veAB32.p; T.veC32 = h->veC32.p;
   T.veD32 = h->veD32.p;
+  T.pencil = h->tune.pencil;
+  T.rows = h->tune.rows;
+  T.xthreads = h->tune.xthreads;
 }
 
 Ctl make_ctl(rs_handle* h, double t0, double t1, double dt0, const rs_controller& c,
@@ -767,7 +775,7 @@ void rs_destroy(rs_handle* h) {
                             &h->partial, &h->krates, &h->T, &h->P, &h->emis, &h->io, &h->io2,
                             &h->mx, &h->my, &h->mz, &h->qw, &h->qe, &h->qs, &h->qn, &h->gx,
                             &h->gylo, &h->gyhi, &h->vsA, &h->vsB, &h->veAB, &h->veC, &h->veD,
-                            &h->dtcell, &h->stepcell};
+                            &h->dtcell, &h->stepcell, &h->totals};
   for (auto* b : bufs) b->release();
   h->slot_row.release();
   h->slot_col.release();
@@ -969,18 +977,23 @@ rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double*
         *dtC = c.dt;
       } else {
         const rs_controller& c = h->cfg.ctrl_C;
+        h->totals.alloc(2);
+        h->totals.zero(h->st);
         rs::PerCellArgs a{t0, t1, *dtC, h->cfg.rtol_C, h->cfg.atol_C, h->cfg.maxiters,
                           c.beta1, c.beta2, 1.0 / c.qmin, 1.0 / c.qmax, c.gamma,
-                          c.qsteady_min, c.qsteady_max, c.qoldinit, h->cfg.clamp_nonneg};
+                          c.qsteady_min, c.qsteady_max, c.qoldinit, h->cfg.clamp_nonneg,
+                          h->totals.p};
         CK(cudaMemsetAsync(h->queue.p, 0, sizeof(unsigned long long), h->st));
         CK(cudaMemsetAsync(h->flag.p, 0, sizeof(int), h->st));
         int dev = 0, nsm = 0;
         CK(cudaGetDevice(&dev));
         CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-        int nblocks = std::max(1, std::min(nsm * 4, (int)((h->nc + 127) / 128)));
+        int thr = h->tune.pc_threads;
+        int nblocks = std::max(1, std::min(nsm * h->tune.pc_blocks_per_sm,
+                                           (int)((h->nc + thr - 1) / thr)));
         {
           Scope s(h, "chem_per_cell");
-          rs::launch_chem_per_cell(h->lc, nblocks, h->U[h->cur].p, h->krates.p,
+          rs::launch_chem_per_cell(h->lc, nblocks, thr, h->U[h->cur].p, h->krates.p,
                                    h->have_emis ? h->emis.p : nullptr, h->dtcell.p,
                                    h->stepcell.p, h->queue.p, h->flag.p, a);
         }
@@ -989,7 +1002,11 @@ rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double*
         CK(cudaMemcpyAsync(h->hflag, h->flag.p, sizeof(int), cudaMemcpyDeviceToHost, h->st));
         CK(cudaStreamSynchronize(h->st));
         okC = *h->hflag == 0;
-        stats.chem_cell_steps = -1;  // filled by rs_per_cell_steps when requested
+        double tot[2] = {0, 0};
+        CK(cudaMemcpy(tot, h->totals.p, sizeof(tot), cudaMemcpyDeviceToHost));
+        stats.chem_cell_steps = tot[0];
+        stats.naC = tot[0];                 // per-cell mode: cell-steps, summed over cells
+        stats.nrC = tot[1] - tot[0];
       }
     }
     collect_profile(h);
@@ -1364,6 +1381,135 @@ rs_status rs_backward_macro_step(rs_handle* h, int32_t k) {
 }
 
 }  // extern "C"
+
+// ====================================================================== autotuner
+namespace {
+
+template <class F>
+float time_min(cudaStream_t st, int reps, F&& launch) {
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  float best = 1e30f;
+  for (int r = 0; r < reps; ++r) {
+    CK(cudaEventRecord(a, st));
+    launch();
+    CK(cudaEventRecord(b, st));
+    CK(cudaEventSynchronize(b));
+    CK(cudaGetLastError());
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, a, b));
+    best = std::min(best, ms);
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return best;
+}
+
+}  // namespace
+
+extern "C" rs_status rs_autotune(rs_handle* h, char* buf, size_t buf_len) {
+  if (!h) return RS_ERR_INVALID;
+  return guard(h, [&] {
+    ensure_rates(h);
+    std::string rep = "{";
+    char line[256];
+    int dev = 0, nsm = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    if (h->cfg.do_chemistry && h->cfg.chem_mode == RS_CHEM_PER_CELL) {
+      // three attempts per cell on scratch copies: the state and the carried dts are untouched
+      size_t n = h->nc * h->nsp;
+      h->io2.alloc(n);
+      h->io.alloc(h->nc);
+      h->totals.alloc(2);
+      const rs_controller& c = h->cfg.ctrl_C;
+      rs::PerCellArgs a{0.0, 1.0e30, 1.0, h->cfg.rtol_C, h->cfg.atol_C, 3.0, c.beta1, c.beta2,
+                        1.0 / c.qmin, 1.0 / c.qmax, c.gamma, c.qsteady_min, c.qsteady_max,
+                        c.qoldinit, h->cfg.clamp_nonneg, nullptr};
+      float best = 1e30f;
+      rep += "\"per_cell\": [";
+      bool first = true;
+      for (int thr : {64, 128, 256})
+        for (int bps : {1, 2, 4, 8}) {
+          int nb = std::max(1, std::min(nsm * bps, (int)((h->nc + thr - 1) / thr)));
+          float ms = time_min(h->st, 2, [&] {
+            cudaMemcpyAsync(h->io2.p, h->U[h->cur].p, n * sizeof(double),
+                            cudaMemcpyDeviceToDevice, h->st);
+            cudaMemsetAsync(h->io.p, 0, h->nc * sizeof(double), h->st);
+            cudaMemsetAsync(h->queue.p, 0, sizeof(unsigned long long), h->st);
+            rs::launch_chem_per_cell(h->lc, nb, thr, h->io2.p, h->krates.p,
+                                     h->have_emis ? h->emis.p : nullptr, h->io.p, nullptr,
+                                     h->queue.p, h->flag.p, a);
+          });
+          std::snprintf(line, sizeof line, "%s{\"threads\": %d, \"blocks_per_sm\": %d, \"ms\": %.4f}",
+                        first ? "" : ", ", thr, bps, ms);
+          rep += line;
+          first = false;
+          if (ms < best) {
+            best = ms;
+            h->tune.pc_threads = thr;
+            h->tune.pc_blocks_per_sm = bps;
+          }
+        }
+      std::snprintf(line, sizeof line, "], \"per_cell_choice\": {\"threads\": %d, \"blocks_per_sm\": %d}",
+                    h->tune.pc_threads, h->tune.pc_blocks_per_sm);
+      rep += line;
+    }
+    if (h->cfg.do_transport) {
+      const double* Q = h->U[h->cur].p;
+      rs::DevTransport<double> T = h->dt;
+      float bx = 1e30f;
+      rep += std::string(rep.size() > 1 ? ", " : "") + "\"lon_rows\": [";
+      bool first = true;
+      for (int xt : {64, 128, 256}) {
+        T.xthreads = xt;
+        float ms = time_min(h->st, 3, [&] { rs::launch_flux_dir(h->st, T, Q, 0); });
+        std::snprintf(line, sizeof line, "%s{\"threads\": %d, \"ms\": %.4f}", first ? "" : ", ", xt, ms);
+        rep += line;
+        first = false;
+        if (ms < bx) {
+          bx = ms;
+          h->tune.xthreads = xt;
+        }
+      }
+      rep += "], \"pencils\": [";
+      first = true;
+      float byz = 1e30f;
+      T.xthreads = h->tune.xthreads;
+      for (int pw : {16, 32})
+        for (int rows : {4, 8, 16}) {
+          T.pencil = pw;
+          T.rows = rows;
+          float ms = time_min(h->st, 3, [&] {
+            rs::launch_flux_dir(h->st, T, Q, 1);
+            rs::launch_flux_dir(h->st, T, Q, 2);
+          });
+          std::snprintf(line, sizeof line, "%s{\"pencil\": %d, \"rows\": %d, \"ms\": %.4f}",
+                        first ? "" : ", ", pw, rows, ms);
+          rep += line;
+          first = false;
+          if (ms < byz) {
+            byz = ms;
+            h->tune.pencil = pw;
+            h->tune.rows = rows;
+          }
+        }
+      std::snprintf(line, sizeof line,
+                    "], \"transport_choice\": {\"xthreads\": %d, \"pencil\": %d, \"rows\": %d}",
+                    h->tune.xthreads, h->tune.pencil, h->tune.rows);
+      rep += line;
+      refresh_dt(h);
+      invalidate_graphs(h);
+    }
+    rep += "}";
+    CK(cudaStreamSynchronize(h->st));
+    if (buf && buf_len) {
+      std::strncpy(buf, rep.c_str(), buf_len - 1);
+      buf[buf_len - 1] = 0;
+    }
+  });
+}
 
 // ====================================================================== allocation-free attempt
 // Some callers cannot allocate device memory at the point where they want to step the

@@ -203,12 +203,13 @@ __global__ void k_block_jac(DevMech M, int nc, int nsp, const double* __restrict
 // of a warp run the same attempt code on different cells, so uneven step counts do not idle
 // lanes: a lane whose cell finishes takes the next one from the queue.
 template <int MS, int MR, int MLU, int MP>
-__global__ void __launch_bounds__(128) k_chem_per_cell(
+__global__ void __launch_bounds__(256) k_chem_per_cell(
     DevMech M, int nc, int nsp, double* __restrict__ U, const double* __restrict__ krates,
     const double* __restrict__ emission, double* __restrict__ dt_cell,
     double* __restrict__ steps_cell, unsigned long long* __restrict__ queue,
     int* __restrict__ status, PerCellArgs a) {
   RosWork<MS, MR, MLU, MP> w;
+  double my_steps = 0.0, my_attempts = 0.0;  // this thread's totals (exact small integers)
   double t = 0, dt = 0, qold = 0, iters = 0, nacc = 0;
   int c = -1;
   const double tlim = a.t1 - 1.0e-9;
@@ -252,8 +253,15 @@ __global__ void __launch_bounds__(128) k_chem_per_cell(
       for (int s = 0; s < M.ns; ++s) U[(size_t)s * nc + c] = w.x[s];
       dt_cell[c] = dt;
       if (steps_cell) steps_cell[c] = nacc;
+      my_steps += nacc;
+      my_attempts += iters;
       c = -1;
     }
+  }
+  // integer-valued totals: atomic double adds are exact (far below 2^53), order-free
+  if (a.totals) {
+    atomicAdd(a.totals, my_steps);
+    atomicAdd(a.totals + 1, my_attempts);
   }
 }
 
@@ -278,10 +286,10 @@ struct ChemLaunch {
     k_block_jac<MS, MR, MLU, MP><<<nb, 128, 0, L.stream>>>(L.mech, L.nc, L.nsp, U, kr, srow,
                                                            scol, J);
   }
-  static void per_cell(const LaunchCtx& L, int nblocks, double* U, const double* kr,
-                       const double* em, double* dtc, double* steps,
+  static void per_cell(const LaunchCtx& L, int nblocks, int threads, double* U,
+                       const double* kr, const double* em, double* dtc, double* steps,
                        unsigned long long* queue, int* status, const PerCellArgs& a) {
-    k_chem_per_cell<MS, MR, MLU, MP><<<nblocks, 128, 0, L.stream>>>(
+    k_chem_per_cell<MS, MR, MLU, MP><<<nblocks, threads, 0, L.stream>>>(
         L.mech, L.nc, L.nsp, U, kr, em, dtc, steps, queue, status, a);
   }
 };
@@ -309,11 +317,13 @@ void launch_block_jac(const LaunchCtx& L, const double* U, const double* kr, con
   if (L.size_class == 0) Small::jac(L, U, kr, srow, scol, J);
   else Large::jac(L, U, kr, srow, scol, J);
 }
-void launch_chem_per_cell(const LaunchCtx& L, int nblocks, double* U, const double* kr,
-                          const double* em, double* dtc, double* steps,
+void launch_chem_per_cell(const LaunchCtx& L, int nblocks, int threads, double* U,
+                          const double* kr, const double* em, double* dtc, double* steps,
                           unsigned long long* queue, int* status, const PerCellArgs& a) {
-  if (L.size_class == 0) Small::per_cell(L, nblocks, U, kr, em, dtc, steps, queue, status, a);
-  else Large::per_cell(L, nblocks, U, kr, em, dtc, steps, queue, status, a);
+  if (L.size_class == 0)
+    Small::per_cell(L, nblocks, threads, U, kr, em, dtc, steps, queue, status, a);
+  else
+    Large::per_cell(L, nblocks, threads, U, kr, em, dtc, steps, queue, status, a);
 }
 
 }  // namespace rs

@@ -26,6 +26,7 @@ struct PerCellArgs {
   double t0, t1, dt0, rtol, atol, maxiters;
   double beta1, beta2, invqmin, invqmax, gamma, qsmin, qsmax, qoldinit;
   int clamp;
+  double* totals;  // [accepted substeps, attempts] summed over cells, or null
 };
 
 // Transport geometry and forcing on the device (grid SoA, lon fastest).
@@ -61,6 +62,10 @@ struct DevTransport {
   const float* veC32;
   const float* veD32;
   int mixed;
+  // launch shape of the FP64 pencil flux kernels (chosen by rs_autotune)
+  int pencil;    // pencils per block in the lat / vertical kernels: 16 or 32
+  int rows;      // threads along the pencil (blockDim.y): 4, 8 or 16
+  int xthreads;  // threads per lon row: 64, 128 or 256
 };
 
 // chemistry (rs_chem.cu)
@@ -72,8 +77,8 @@ void launch_chem_rhs(const LaunchCtx& L, const double* U, const double* kr, cons
                      double* dU);
 void launch_block_jac(const LaunchCtx& L, const double* U, const double* kr, const int* srow,
                       const int* scol, double* J);
-void launch_chem_per_cell(const LaunchCtx& L, int nblocks, double* U, const double* kr,
-                          const double* em, double* dtc, double* steps,
+void launch_chem_per_cell(const LaunchCtx& L, int nblocks, int threads, double* U,
+                          const double* kr, const double* em, double* dtc, double* steps,
                           unsigned long long* queue, int* status, const PerCellArgs& a);
 
 // transport (rs_transport.cu).  Stage s in 1..4 of one SSPRK43 attempt; buffers:
@@ -91,6 +96,8 @@ void launch_ssprk43_attempt(cudaStream_t st, const DevTransport<double>& T, cons
 // du = f_transport(u) with flux time factor g for a grid-SoA state (single evaluation hook)
 void launch_transport_rhs(cudaStream_t st, const DevTransport<double>& T, const double* U,
                           double g, double* dU);
+
+void launch_flux_dir(cudaStream_t st, const DevTransport<double>& T, const double* Q, int dir);
 
 // control (rs_control.cu)
 void launch_ctl_init(cudaStream_t st, Ctl* ctl, const Ctl& init);

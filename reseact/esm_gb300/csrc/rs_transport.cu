@@ -355,9 +355,7 @@ __global__ void __launch_bounds__(kFluxThreads) k_flux_z(DevTransport<double> T,
 // column) in shared memory, then slopes, then edges, then the upwind limiter and flux of
 // each face.  Same expressions in the same order as ppm_face_u / the vertical branch, so the
 // fluxes are bit-identical to the per-face kernels.
-constexpr int kPencil = 32;  // pencils per block in the y / z kernels
-
-__global__ void __launch_bounds__(128) k_flux_x_fused(DevTransport<double> T, StageSel sel) {
+__global__ void __launch_bounds__(256) k_flux_x_fused(DevTransport<double> T, StageSel sel) {
   const double* Q;
   double g;
   if (!resolve_stage(sel, Q, g)) return;
@@ -401,8 +399,9 @@ __global__ void __launch_bounds__(128) k_flux_x_fused(DevTransport<double> T, St
   }
 }
 
-// y: block = 32 adjacent i at one level, all j; threads (32, 8)
-__global__ void __launch_bounds__(256) k_flux_y_fused(DevTransport<double> T, StageSel sel) {
+// y: block = PW adjacent i at one level, all j; threads (PW, rows)
+template <int kPencil>
+__global__ void __launch_bounds__(512) k_flux_y_fused(DevTransport<double> T, StageSel sel) {
   const double* Q;
   double g;
   if (!resolve_stage(sel, Q, g)) return;
@@ -463,8 +462,9 @@ __global__ void __launch_bounds__(256) k_flux_y_fused(DevTransport<double> T, St
   }
 }
 
-// z: block = 32 adjacent columns (same j), all levels; dp-weighted coefficients
-__global__ void __launch_bounds__(256) k_flux_z_fused(DevTransport<double> T, StageSel sel) {
+// z: block = PW adjacent columns, all levels; dp-weighted coefficients
+template <int kPencil>
+__global__ void __launch_bounds__(512) k_flux_z_fused(DevTransport<double> T, StageSel sel) {
   const double* Q;
   double g;
   if (!resolve_stage(sel, Q, g)) return;
@@ -699,6 +699,19 @@ __global__ void __launch_bounds__(kRedThreads) k_rhs_eval(DevTransport<double> T
   }
 }
 
+// allow > 48 KB of dynamic shared memory for long pencils (once per process)
+static void allow_big_smem() {
+  static bool done = false;
+  if (done) return;
+  const int cap = 200 * 1024;
+  cudaFuncSetAttribute(k_flux_x_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_flux_y_fused<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_flux_y_fused<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_flux_z_fused<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_flux_z_fused<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  done = true;
+}
+
 static void launch_fluxes(cudaStream_t st, const DevTransport<double>& T, const StageSel& sel) {
   if (T.mixed) {  // FP32 deviation-form reconstruction, one thread per face
     long long nx = (long long)(T.nlon + 1) * T.nlat * T.nlev;
@@ -710,20 +723,49 @@ static void launch_fluxes(cudaStream_t st, const DevTransport<double>& T, const 
     return;
   }
   size_t shx = 3 * (size_t)(T.nlon + 6) * sizeof(double);
-  size_t shy = 3 * (size_t)(T.nlat + 6) * kPencil * sizeof(double);
-  size_t shz = 3 * (size_t)(T.nlev + 6) * kPencil * sizeof(double);
-  static bool attr_set = false;
-  if (!attr_set) {  // allow > 48 KB of dynamic shared memory for long pencils
-    cudaFuncSetAttribute(k_flux_x_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(k_flux_y_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(k_flux_z_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr_set = true;
-  }
-  unsigned ntile = (unsigned)((T.nlon + kPencil - 1) / kPencil);
+  allow_big_smem();
+  const int pw = T.pencil == 16 ? 16 : 32;
+  const int rows = (T.rows == 4 || T.rows == 16) ? T.rows : 8;
+  const int xt = (T.xthreads == 64 || T.xthreads == 256) ? T.xthreads : 128;
+  size_t shy = 3 * (size_t)(T.nlat + 6) * pw * sizeof(double);
+  size_t shz = 3 * (size_t)(T.nlev + 6) * pw * sizeof(double);
+  unsigned ntile = (unsigned)((T.nlon + pw - 1) / pw);
   size_t ncol = (size_t)T.nlon * T.nlat;
-  k_flux_x_fused<<<(unsigned)(T.nlat * T.nlev), 128, shx, st>>>(T, sel);
-  k_flux_y_fused<<<ntile * (unsigned)T.nlev, dim3(kPencil, 8), shy, st>>>(T, sel);
-  k_flux_z_fused<<<(unsigned)((ncol + kPencil - 1) / kPencil), dim3(kPencil, 8), shz, st>>>(T, sel);
+  unsigned nzb = (unsigned)((ncol + pw - 1) / pw);
+  k_flux_x_fused<<<(unsigned)(T.nlat * T.nlev), xt, shx, st>>>(T, sel);
+  if (pw == 16) {
+    k_flux_y_fused<16><<<ntile * (unsigned)T.nlev, dim3(16, rows), shy, st>>>(T, sel);
+    k_flux_z_fused<16><<<nzb, dim3(16, rows), shz, st>>>(T, sel);
+  } else {
+    k_flux_y_fused<32><<<ntile * (unsigned)T.nlev, dim3(32, rows), shy, st>>>(T, sel);
+    k_flux_z_fused<32><<<nzb, dim3(32, rows), shz, st>>>(T, sel);
+  }
+}
+
+// one direction of the flux computation on a given field (used by the autotuner)
+void launch_flux_dir(cudaStream_t st, const DevTransport<double>& T, const double* Q, int dir) {
+  StageSel sel{nullptr, 0, nullptr, nullptr, nullptr, nullptr, nullptr, Q, 1.0};
+  DevTransport<double> T1 = T;
+  T1.mixed = 0;
+  allow_big_smem();
+  const int pw = T.pencil == 16 ? 16 : 32;
+  const int rows = (T.rows == 4 || T.rows == 16) ? T.rows : 8;
+  const int xt = (T.xthreads == 64 || T.xthreads == 256) ? T.xthreads : 128;
+  size_t ncol = (size_t)T.nlon * T.nlat;
+  if (dir == 0) {
+    size_t shx = 3 * (size_t)(T.nlon + 6) * sizeof(double);
+    k_flux_x_fused<<<(unsigned)(T.nlat * T.nlev), xt, shx, st>>>(T1, sel);
+  } else if (dir == 1) {
+    size_t shy = 3 * (size_t)(T.nlat + 6) * pw * sizeof(double);
+    unsigned ntile = (unsigned)((T.nlon + pw - 1) / pw);
+    if (pw == 16) k_flux_y_fused<16><<<ntile * (unsigned)T.nlev, dim3(16, rows), shy, st>>>(T1, sel);
+    else k_flux_y_fused<32><<<ntile * (unsigned)T.nlev, dim3(32, rows), shy, st>>>(T1, sel);
+  } else {
+    size_t shz = 3 * (size_t)(T.nlev + 6) * pw * sizeof(double);
+    unsigned nzb = (unsigned)((ncol + pw - 1) / pw);
+    if (pw == 16) k_flux_z_fused<16><<<nzb, dim3(16, rows), shz, st>>>(T1, sel);
+    else k_flux_z_fused<32><<<nzb, dim3(32, rows), shz, st>>>(T1, sel);
+  }
 }
 
 void launch_ssprk43_attempt(cudaStream_t st, const DevTransport<double>& T, const Ctl* ctl,
