@@ -219,6 +219,27 @@ void* rs_stream(rs_handle* h);
  * the fastest for this handle and writes a JSON report of every candidate into buf. */
 rs_status rs_autotune(rs_handle* h, char* buf, size_t buf_len);
 
+/* Chemistry kernel selection (no reference counterpart; the reference compiles its RHS and
+ * Jacobian from the .esm system into native code, which the SPECIALIZED kernels mirror).
+ * SPECIALIZED: the mechanism's rate products, RHS, Jacobian, LU and solves are generated as
+ *   straight-line CUDA at rs_create and compiled for the device with NVRTC (mechanisms of up
+ *   to 32 species and 256 LU slots);
+ * TABLE: one kernel for every mechanism that walks the sparse tables;
+ * AUTO (the default): SPECIALIZED when it could be built, else TABLE.
+ * Both compute the same arithmetic in the same order.  rs_set_chem_kernel returns
+ * RS_ERR_UNSUPPORTED for SPECIALIZED when it could not be built (reason in rs_last_error). */
+enum { RS_CHEM_KERNEL_AUTO = 0, RS_CHEM_KERNEL_TABLE = 1, RS_CHEM_KERNEL_SPECIALIZED = 2 };
+rs_status rs_set_chem_kernel(rs_handle* h, int32_t kind);
+/* The kernel kind in use (TABLE or SPECIALIZED) and a one-line JSON description of it. */
+rs_status rs_get_chem_kernel(rs_handle* h, int32_t* kind, char* info, size_t info_len);
+/* The generated CUDA source of a mechanism's specialised kernels, and an NVRTC compile of it
+ * for sm_103a with ptxas's resource report in log; neither needs a device.  *len_out (may be
+ * NULL) receives the source length + 1; buf may be NULL to query it. */
+rs_status rs_chem_kernel_source(const rs_mechanism* mech, int32_t strict, char* buf,
+                                size_t buf_len, size_t* len_out);
+rs_status rs_chem_kernel_compile(const rs_mechanism* mech, int32_t strict, char* log,
+                                 size_t log_len);
+
 /* Discrete adjoint (tools/adjoint_gradient.jl:609-835; step VJPs rx_traced_integrator.jl:610-623).
  * rs_record(h, 1) clears and starts recording: every rs_macro_step then keeps a device
  * checkpoint of its input state and the accepted (t, dt) of both halves; rs_record(h, 0) stops.

@@ -19,8 +19,11 @@ SYMBOLS = [
     "rs_set_profiling", "rs_get_profile", "rs_reset_profile", "rs_ros23_attempt_noalloc",
     "rs_record", "rs_record_count", "rs_adjoint_set_lambda", "rs_adjoint_get_lambda",
     "rs_backward_macro_step", "rs_adjoint_get_grad_emission", "rs_adjoint_reset_grad",
-    "rs_autotune",
+    "rs_autotune", "rs_set_chem_kernel", "rs_get_chem_kernel", "rs_chem_kernel_source",
+    "rs_chem_kernel_compile",
 ]
+
+CHEM_KERNEL_AUTO, CHEM_KERNEL_TABLE, CHEM_KERNEL_SPECIALIZED = 0, 1, 2
 
 
 class RsError(RuntimeError):
@@ -84,6 +87,15 @@ def _declare(L):
     L.rs_adjoint_reset_grad.restype = C.c_int
     L.rs_autotune.argtypes = [vp, C.c_char_p, sz]
     L.rs_autotune.restype = C.c_int
+    L.rs_set_chem_kernel.argtypes = [vp, i32]
+    L.rs_set_chem_kernel.restype = C.c_int
+    L.rs_get_chem_kernel.argtypes = [vp, C.POINTER(i32), C.c_char_p, sz]
+    L.rs_get_chem_kernel.restype = C.c_int
+    L.rs_chem_kernel_source.argtypes = [C.POINTER(abi.rs_mechanism), i32, C.c_char_p, sz,
+                                        C.POINTER(sz)]
+    L.rs_chem_kernel_source.restype = C.c_int
+    L.rs_chem_kernel_compile.argtypes = [C.POINTER(abi.rs_mechanism), i32, C.c_char_p, sz]
+    L.rs_chem_kernel_compile.restype = C.c_int
     return L
 
 
@@ -103,6 +115,28 @@ def load(strict=False, build_if_missing=True):
 
 def _p(a):
     return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def chem_kernel_source(mech_abi, strict=False):
+    """The CUDA source generated for a mechanism's specialised chemistry kernels (no GPU)."""
+    L = load(strict)
+    n = C.c_size_t(0)
+    rc = L.rs_chem_kernel_source(C.byref(mech_abi.struct), int(strict), None, 0, C.byref(n))
+    if rc != abi.RS_OK:
+        raise RsError(rc, L.rs_last_error(None).decode())
+    buf = C.create_string_buffer(n.value)
+    L.rs_chem_kernel_source(C.byref(mech_abi.struct), int(strict), buf, n.value, None)
+    return buf.value.decode()
+
+
+def chem_kernel_compile(mech_abi, strict=False):
+    """NVRTC-compile the specialised kernels for sm_103a (no GPU); returns ptxas's report."""
+    L = load(strict)
+    buf = C.create_string_buffer(1 << 16)
+    rc = L.rs_chem_kernel_compile(C.byref(mech_abi.struct), int(strict), buf, 1 << 16)
+    if rc != abi.RS_OK:
+        raise RsError(rc, L.rs_last_error(None).decode())
+    return buf.value.decode()
 
 
 class Solver:
@@ -232,6 +266,18 @@ class Solver:
         buf = C.create_string_buffer(16384)
         self._check(self.L.rs_autotune(self.h, buf, 16384))
         return json.loads(buf.value.decode())
+
+    def set_chem_kernel(self, kind):
+        """CHEM_KERNEL_AUTO / _TABLE / _SPECIALIZED (raises if SPECIALIZED is unavailable)."""
+        self._check(self.L.rs_set_chem_kernel(self.h, int(kind)))
+
+    def chem_kernel(self):
+        """(kind in use, description dict) of the chemistry kernels."""
+        import json
+        k = C.c_int32(0)
+        buf = C.create_string_buffer(1024)
+        self._check(self.L.rs_get_chem_kernel(self.h, C.byref(k), buf, 1024))
+        return k.value, json.loads(buf.value.decode())
 
     def stream(self):
         return self.L.rs_stream(self.h)

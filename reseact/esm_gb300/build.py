@@ -17,7 +17,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
-SOURCES = ["rs_api.cu", "rs_chem.cu", "rs_transport.cu", "rs_control.cu", "rs_adjoint.cu"]
+SOURCES = ["rs_api.cu", "rs_chem.cu", "rs_transport.cu", "rs_control.cu", "rs_adjoint.cu",
+           "rs_jit.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 LIBS = {"libreseact_gb300.so": ["--fmad=true", "-DRS_STRICT=0"],
         "libreseact_gb300_strict.so": ["--fmad=false", "-DRS_STRICT=1"]}
@@ -77,7 +78,7 @@ def build(force=False, verbose=False, only=None):
                     print(err, file=sys.stderr)
     for path, objs in links:
         tmp = path + ".tmp"
-        cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
+        cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-ldl"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s" % r.stderr)

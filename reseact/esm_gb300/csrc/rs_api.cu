@@ -13,6 +13,7 @@
 #include <cstring>
 #include <functional>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <set>
 #include <stdexcept>
@@ -22,6 +23,8 @@
 #include "../../../include/reseact_gb300.h"
 #include "rs_device.cuh"
 #include "rs_kernels.h"
+#include "rs_jit.h"
+#include "rs_mech.h"
 
 namespace {
 
@@ -68,14 +71,7 @@ struct DevBuf {
 };
 
 // ------------------------------------------------------------------ mechanism tables
-struct MechTables {
-  int ns = 0, nr = 0;
-  std::vector<int> rptr, rsp, rnu, rhs_ptr, rhs_r, part_r, part_q, part_e, jac_ptr, jac_slot,
-      jac_diag, jac_part, lu_diag, elim_ptr, elim_lik, upd_ptr, upd_dst, upd_src, low_ptr,
-      low_row, low_slot, up_ptr, up_col, up_slot, prog_ptr, prog_op, slot_row, slot_col;
-  std::vector<double> rhs_c, jac_coef, prog_val, params;
-  int nlu = 0, npart = 0, njac = 0, comb = 0;
-};
+using rs::MechTables;
 
 MechTables derive_tables(const rs_mechanism& m) {
   MechTables T;
@@ -300,6 +296,10 @@ struct rs_handle {
     int pc_threads = 128, pc_blocks_per_sm = 4;      // per-cell chemistry kernel
     int pencil = 32, rows = 8, xthreads = 128;        // transport pencil kernels
   } tune;
+  // mechanism-specialised chemistry kernels (null: not built) and the kind in use
+  std::shared_ptr<rs::JitChem> jit;
+  std::string jit_why;
+  int chem_kernel = RS_CHEM_KERNEL_AUTO;
 };
 
 namespace {
@@ -712,6 +712,8 @@ rs_status rs_create(const rs_config* cfg, rs_handle** out) {
     h->ntr = T.ns;
     build_device_mech(h);
     h->lc = rs::LaunchCtx{h->st, h->dm, (int)h->nc, h->nsp, cls};
+    h->jit = rs::jit_chem_build(h->mt, h->dm.ros_d, h->dm.ros_c32, RS_STRICT != 0, &h->jit_why);
+    h->lc.jit = h->jit.get();
     size_t n = h->nc * h->nsp;
     h->U[0].alloc(n); h->U[1].alloc(n);
     h->U[0].zero(h->st); h->U[1].zero(h->st);
@@ -1382,6 +1384,96 @@ rs_status rs_backward_macro_step(rs_handle* h, int32_t k) {
 
 }  // extern "C"
 
+// ====================================================================== chemistry kernel kind
+extern "C" rs_status rs_set_chem_kernel(rs_handle* h, int32_t kind) {
+  if (!h) return RS_ERR_INVALID;
+  return guard(h, [&] {
+    if (kind != RS_CHEM_KERNEL_AUTO && kind != RS_CHEM_KERNEL_TABLE &&
+        kind != RS_CHEM_KERNEL_SPECIALIZED)
+      throw RsError(RS_ERR_INVALID, "unknown chemistry kernel kind");
+    if (kind == RS_CHEM_KERNEL_SPECIALIZED && !h->jit)
+      throw RsError(RS_ERR_UNSUPPORTED, "specialised chemistry kernels unavailable: " + h->jit_why);
+    h->chem_kernel = kind;
+    h->lc.jit = (kind == RS_CHEM_KERNEL_TABLE) ? nullptr : h->jit.get();
+    invalidate_graphs(h);
+  });
+}
+
+extern "C" rs_status rs_get_chem_kernel(rs_handle* h, int32_t* kind, char* info, size_t info_len) {
+  if (!h) return RS_ERR_INVALID;
+  return guard(h, [&] {
+    const bool spec = h->lc.jit != nullptr;
+    if (kind) *kind = spec ? RS_CHEM_KERNEL_SPECIALIZED : RS_CHEM_KERNEL_TABLE;
+    if (info && info_len) {
+      std::string why = h->jit_why;
+      for (char& ch : why)
+        if (ch == '"' || ch == '\\' || ch == '\n') ch = ' ';
+      char line[768];
+      if (h->jit)
+        std::snprintf(line, sizeof line,
+                      "{\"kind\": \"%s\", \"variant\": \"%s\", \"regs\": [%d, %d], "
+                      "\"smem_bytes\": %zu, \"compile_ms\": %.1f}",
+                      spec ? "specialized" : "table",
+                      h->jit->use_smem && h->jit->attempt[1][0] ? "smem" : "regs", h->jit->regs[0],
+                      h->jit->regs[1], h->jit->attempt_smem, h->jit->compile_ms);
+      else
+        std::snprintf(line, sizeof line, "{\"kind\": \"table\", \"why\": \"%.600s\"}", why.c_str());
+      std::strncpy(info, line, info_len - 1);
+      info[info_len - 1] = 0;
+    }
+  });
+}
+
+// Source and compile check of the specialised kernels for a mechanism (no device needed).
+namespace {
+rs_status nohandle(const std::function<void()>& fn) {
+  try {
+    fn();
+    g_create_err.clear();
+    return RS_OK;
+  } catch (const RsError& e) {
+    g_create_err = e.what();
+    return e.code;
+  } catch (const std::exception& e) {
+    g_create_err = e.what();
+    return RS_ERR_INVALID;
+  }
+}
+void copy_out(const std::string& s, char* buf, size_t len) {
+  if (!buf || !len) return;
+  size_t n = std::min(len - 1, s.size());
+  std::memcpy(buf, s.data(), n);
+  buf[n] = 0;
+}
+}  // namespace
+
+extern "C" rs_status rs_chem_kernel_source(const rs_mechanism* mech, int32_t strict, char* buf,
+                                           size_t buf_len, size_t* len_out) {
+  if (!mech) return RS_ERR_INVALID;
+  return nohandle([&] {
+    MechTables T = derive_tables(*mech);
+    if (!rs::jit_chem_eligible(T))
+      throw RsError(RS_ERR_UNSUPPORTED, "mechanism too large for straight-line kernels");
+    std::string src = rs::jit_chem_source(T, strict != 0);
+    if (len_out) *len_out = src.size() + 1;
+    copy_out(src, buf, buf_len);
+  });
+}
+
+extern "C" rs_status rs_chem_kernel_compile(const rs_mechanism* mech, int32_t strict, char* log,
+                                            size_t log_len) {
+  if (!mech) return RS_ERR_INVALID;
+  return nohandle([&] {
+    MechTables T = derive_tables(*mech);
+    if (!rs::jit_chem_eligible(T))
+      throw RsError(RS_ERR_UNSUPPORTED, "mechanism too large for straight-line kernels");
+    std::string text;
+    bool ok = rs::jit_compile(rs::jit_chem_source(T, strict != 0), strict != 0, true, nullptr, &text);
+    copy_out(text, log, log_len);
+    if (!ok) throw RsError(RS_ERR_UNSUPPORTED, text.substr(0, 2000));
+  });
+}
+
 // ====================================================================== autotuner
 namespace {
 
@@ -1455,6 +1547,37 @@ extern "C" rs_status rs_autotune(rs_handle* h, char* buf, size_t buf_len) {
       std::snprintf(line, sizeof line, "], \"per_cell_choice\": {\"threads\": %d, \"blocks_per_sm\": %d}",
                     h->tune.pc_threads, h->tune.pc_blocks_per_sm);
       rep += line;
+    }
+    if (h->cfg.do_chemistry && h->cfg.chem_mode == RS_CHEM_GLOBAL_DT && h->lc.jit &&
+        h->jit->attempt[1][0]) {
+      // register- vs shared-memory-resident W of the specialised attempt kernel: one attempt
+      // from the accepted state into the candidate buffer (the accepted state is untouched)
+      Ctl init = make_ctl(h, 0.0, 600.0, 60.0, h->cfg.ctrl_C, (double)h->nc * h->nsp);
+      init.cur = h->cur;
+      Ctl* c = h->ctl.p + 2;
+      rs::launch_ctl_init(h->st, c, init);
+      float best = 1e30f;
+      int pick = 0;
+      rep += std::string(rep.size() > 1 ? ", " : "") + "\"chem_attempt\": [";
+      for (int v = 0; v < 2; ++v) {
+        h->jit->use_smem = v;
+        float ms = time_min(h->st, 3, [&] {
+          rs::launch_ros23_attempt(h->lc, c, h->U[0].p, h->U[1].p, h->krates.p,
+                                   h->have_emis ? h->emis.p : nullptr, h->partial.p,
+                                   h->cfg.rtol_C, h->cfg.atol_C, h->cfg.clamp_nonneg);
+        });
+        std::snprintf(line, sizeof line, "%s{\"w_in\": \"%s\", \"ms\": %.4f}", v ? ", " : "",
+                      v ? "smem" : "regs", ms);
+        rep += line;
+        if (ms < best) {
+          best = ms;
+          pick = v;
+        }
+      }
+      h->jit->use_smem = pick;
+      std::snprintf(line, sizeof line, "], \"chem_choice\": \"%s\"", pick ? "smem" : "regs");
+      rep += line;
+      invalidate_graphs(h);
     }
     if (h->cfg.do_transport) {
       const double* Q = h->U[h->cur].p;

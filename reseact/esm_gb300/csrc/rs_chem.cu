@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include "rs_device.cuh"
+#include "rs_jit.h"
 #include "rs_kernels.h"
 
 namespace rs {
@@ -304,6 +305,11 @@ void launch_rates(const LaunchCtx& L, const double* T, const double* P, double* 
 void launch_ros23_attempt(const LaunchCtx& L, const Ctl* ctl, double* U0, double* U1,
                           const double* kr, const double* em, double* part, double rtol,
                           double atol, int clamp) {
+  if (L.jit) {
+    jit_launch_attempt(*L.jit, L.stream, L.nc, L.nsp, ctl, U0, U1, kr, em, part, rtol, atol,
+                       clamp);
+    return;
+  }
   if (L.size_class == 0) Small::attempt(L, ctl, U0, U1, kr, em, part, rtol, atol, clamp);
   else Large::attempt(L, ctl, U0, U1, kr, em, part, rtol, atol, clamp);
 }
@@ -320,6 +326,11 @@ void launch_block_jac(const LaunchCtx& L, const double* U, const double* kr, con
 void launch_chem_per_cell(const LaunchCtx& L, int nblocks, int threads, double* U,
                           const double* kr, const double* em, double* dtc, double* steps,
                           unsigned long long* queue, int* status, const PerCellArgs& a) {
+  if (L.jit) {
+    jit_launch_per_cell(*L.jit, L.stream, L.nc, L.nsp, nblocks, threads, U, kr, em, dtc, steps,
+                        queue, status, a);
+    return;
+  }
   if (L.size_class == 0)
     Small::per_cell(L, nblocks, threads, U, kr, em, dtc, steps, queue, status, a);
   else

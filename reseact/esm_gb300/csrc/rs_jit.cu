@@ -1,0 +1,598 @@
+// rs_jit.cu -- generator and NVRTC loader of the mechanism-specialised chemistry kernels.
+//
+// The generated kernels compute exactly what the table-walking kernels of rs_chem.cu compute
+// (ROS23 attempt, rx_traced_integrator.jl:279-349; blocksolve :110-135; hairer norm
+// :329-347; per-cell PI controller :455-507), term for term in the same association:
+//   v_r   = k_r * x_a * x_a * x_b ...             (reactant entries in table order)
+//   f_s   = sum_r net[r,s] v_r (+ emission_s)     (reactions ascending; x*1 and x*(-1) folded)
+//   P_p   = d v_r / d x_q                          (same product order as the tables)
+//   W     = I - dtgamma * J on the LU fill pattern
+//   LU    natural-order pivot-free elimination, zero updates skipped
+// so that a strict build (no FMA contraction, divides where the reference divides) is still
+// bit-compatible with the CPU restatement.  The only freedom taken is the sign of an exact
+// zero (an off-diagonal W entry is written -(dtgamma*acc) instead of 0.0 - dtgamma*acc).
+//
+// NVRTC is loaded with dlopen so that the library itself loads without it; a handle whose
+// kernels cannot be generated keeps the table-walking kernels (also CUDA).
+#include <cuda_runtime.h>
+#include <dlfcn.h>
+#include <nvrtc.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstddef>
+#include <cstdio>
+#include <cstdlib>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "rs_jit.h"
+#include "rs_kernels.h"
+
+namespace rs {
+
+static_assert(sizeof(PerCellArgs) == 128 && offsetof(PerCellArgs, clamp) == 112 &&
+                  offsetof(PerCellArgs, totals) == 120,
+              "PerCellArgs layout is restated in the generated source");
+
+namespace {
+
+// ------------------------------------------------------------------ NVRTC entry points
+struct Nvrtc {
+  decltype(&nvrtcCreateProgram) create = nullptr;
+  decltype(&nvrtcCompileProgram) compile = nullptr;
+  decltype(&nvrtcGetProgramLogSize) log_size = nullptr;
+  decltype(&nvrtcGetProgramLog) log = nullptr;
+  decltype(&nvrtcGetCUBINSize) cubin_size = nullptr;
+  decltype(&nvrtcGetCUBIN) cubin = nullptr;
+  decltype(&nvrtcDestroyProgram) destroy = nullptr;
+  decltype(&nvrtcGetErrorString) err = nullptr;
+  std::string why;
+  bool ok() const { return why.empty(); }
+};
+
+const Nvrtc& nvrtc() {
+  static const Nvrtc api = [] {
+    Nvrtc a;
+    std::vector<std::string> names = {"libnvrtc.so.13", "libnvrtc.so"};
+    if (const char* ch = std::getenv("CUDA_HOME")) names.push_back(std::string(ch) + "/lib64/libnvrtc.so.13");
+    names.push_back("/usr/local/cuda/lib64/libnvrtc.so.13");
+    void* h = nullptr;
+    for (const auto& n : names)
+      if ((h = dlopen(n.c_str(), RTLD_NOW | RTLD_LOCAL))) break;
+    if (!h) {
+      a.why = "libnvrtc.so.13 not found";
+      return a;
+    }
+    auto sym = [&](auto& fp, const char* name) {
+      fp = reinterpret_cast<std::remove_reference_t<decltype(fp)>>(dlsym(h, name));
+      if (!fp && a.why.empty()) a.why = std::string("libnvrtc lacks ") + name;
+    };
+    sym(a.create, "nvrtcCreateProgram");
+    sym(a.compile, "nvrtcCompileProgram");
+    sym(a.log_size, "nvrtcGetProgramLogSize");
+    sym(a.log, "nvrtcGetProgramLog");
+    sym(a.cubin_size, "nvrtcGetCUBINSize");
+    sym(a.cubin, "nvrtcGetCUBIN");
+    sym(a.destroy, "nvrtcDestroyProgram");
+    sym(a.err, "nvrtcGetErrorString");
+    return a;
+  }();
+  return api;
+}
+
+// ------------------------------------------------------------------ source generation
+std::string lit(double v) {  // exact hex-float literal
+  char b[64];
+  std::snprintf(b, sizeof b, "%a", v);
+  return std::signbit(v) ? "(" + std::string(b) + ")" : std::string(b);
+}
+
+// W storage: shared-memory variant only while NLU doubles per thread x 256 threads fit
+constexpr int kBlock = 256;
+constexpr size_t kSmemCap = 227 * 1024 - kBlock * sizeof(double);
+
+size_t smem_bytes(const MechTables& T) { return (size_t)T.nlu * kBlock * sizeof(double); }
+
+struct Gen {
+  const MechTables& T;
+  bool strict;
+  std::ostringstream o;
+
+  void vel(const char* x) {
+    for (int r = 0; r < T.nr; ++r) {
+      std::ostringstream e;
+      e << "K(" << r << ")";
+      for (int q = T.rptr[r]; q < T.rptr[r + 1]; ++q)
+        for (int t = 0; t < T.rnu[q]; ++t) e << "*" << x << "[" << T.rsp[q] << "]";
+      o << "  v[" << r << "] = " << e.str() << ";\n";
+    }
+  }
+  // acc = sum c_t * a[i_t], first term without the leading 0.0 +, +-1 coefficients folded
+  static void sum_terms(std::ostringstream& e, bool first, double c, const std::string& term) {
+    if (first) {
+      if (c == 1.0) e << term;
+      else if (c == -1.0) e << "-" << term;
+      else e << lit(c) << "*" << term;
+    } else {
+      if (c == 1.0) e << " + " << term;
+      else if (c == -1.0) e << " - " << term;
+      else e << " + " << lit(c) << "*" << term;
+    }
+  }
+  void rhs(const char* f) {
+    for (int s = 0; s < T.ns; ++s) {
+      std::ostringstream e;
+      bool first = true;
+      for (int t = T.rhs_ptr[s]; t < T.rhs_ptr[s + 1]; ++t) {
+        sum_terms(e, first, T.rhs_c[t], "v[" + std::to_string(T.rhs_r[t]) + "]");
+        first = false;
+      }
+      std::string ex = first ? std::string("0.0") : e.str();
+      o << "  { const double a_ = " << ex << "; " << f << "[" << s << "] = HE ? a_ + EM(" << s
+        << ") : a_; }\n";
+    }
+  }
+  void partials() {
+    for (int p = 0; p < T.npart; ++p) {
+      int r = T.part_r[p], qs = T.part_q[p];
+      std::ostringstream d;
+      d << "K(" << r << ")";
+      for (int q = T.rptr[r]; q < T.rptr[r + 1]; ++q) {
+        int s = T.rsp[q], nu = T.rnu[q];
+        if (s == qs) {
+          if (nu >= 2) {
+            std::ostringstream f;
+            f << lit((double)nu);
+            for (int t = 1; t < nu; ++t) f << "*x[" << s << "]";
+            d << "*(" << f.str() << ")";
+          }
+        } else {
+          for (int t = 0; t < nu; ++t) d << "*x[" << s << "]";
+        }
+      }
+      o << "  P[" << p << "] = " << d.str() << ";\n";
+    }
+  }
+  void build_w() {
+    std::vector<std::string> w(T.nlu, "0.0");
+    for (int i = 0; i < T.ns; ++i) w[T.lu_diag[i]] = "1.0";
+    for (int e = 0; e < T.njac; ++e) {
+      std::ostringstream acc;
+      bool first = true;
+      for (int t = T.jac_ptr[e]; t < T.jac_ptr[e + 1]; ++t) {
+        sum_terms(acc, first, T.jac_coef[t], "P[" + std::to_string(T.jac_part[t]) + "]");
+        first = false;
+      }
+      std::string a = first ? std::string("0.0") : acc.str();
+      w[T.jac_slot[e]] = T.jac_diag[e] ? "1.0 - dtg*(" + a + ")" : "-(dtg*(" + a + "))";
+    }
+    for (int e = 0; e < T.nlu; ++e) o << "  WV(" << e << ") = " << w[e] << ";\n";
+  }
+  void lu_factor() {
+    int m = 0;
+    for (int k = 0; k < T.ns; ++k) {
+      o << "  pv[" << k << "] = 1.0 / WV(" << T.lu_diag[k] << ");\n";
+      for (int ii = T.elim_ptr[k]; ii < T.elim_ptr[k + 1]; ++ii, ++m) {
+        int sl = T.elim_lik[ii];
+        o << "  { const double mu_ = WV(" << sl << ") * pv[" << k << "];\n";
+        for (int u = T.upd_ptr[m]; u < T.upd_ptr[m + 1]; ++u)
+          o << "    WV(" << T.upd_dst[u] << ") = WV(" << T.upd_dst[u] << ") - mu_ * WV("
+            << T.upd_src[u] << ");\n";
+        o << "    WV(" << sl << ") = mu_; }\n";
+      }
+    }
+  }
+  void lu_solve(const char* b) {
+    for (int k = 0; k < T.ns; ++k)
+      for (int e = T.low_ptr[k]; e < T.low_ptr[k + 1]; ++e)
+        o << "  " << b << "[" << T.low_row[e] << "] = " << b << "[" << T.low_row[e] << "] - WV("
+          << T.low_slot[e] << ") * " << b << "[" << k << "];\n";
+    for (int i = T.ns - 1; i >= 0; --i) {
+      std::ostringstream acc;
+      acc << b << "[" << i << "]";
+      for (int e = T.up_ptr[i]; e < T.up_ptr[i + 1]; ++e)
+        acc << " - WV(" << T.up_slot[e] << ") * " << b << "[" << T.up_col[e] << "]";
+      if (strict)
+        o << "  " << b << "[" << i << "] = (" << acc.str() << ") / WV(" << T.lu_diag[i] << ");\n";
+      else
+        o << "  " << b << "[" << i << "] = (" << acc.str() << ") * pv[" << i << "];\n";
+    }
+  }
+};
+
+const char* kPrelude = R"(
+typedef unsigned long long u64;
+struct PCA {
+  double t0, t1, dt0, rtol, atol, maxiters;
+  double beta1, beta2, invqmin, invqmax, gamma, qsmin, qsmax, qoldinit;
+  int clamp;
+  double* totals;
+};
+static_assert(sizeof(PCA) == 128, "PerCellArgs layout");
+
+// pairwise tree over 256 lanes, v[t] += v[t+s] for s = 128 ... 1; total in thread 0
+__device__ __forceinline__ double tree256(double v, double* sm) {
+  const int t = threadIdx.x;
+  sm[t] = v;
+  __syncthreads();
+  for (int s = 128; s >= 32; s >>= 1) {
+    if (t < s) sm[t] = sm[t] + sm[t + s];
+    __syncthreads();
+  }
+  double a = sm[t];
+  if (t < 32) {
+    for (int s = 16; s > 0; s >>= 1) {
+      const double o = __shfl_down_sync(0xffffffffu, a, s);
+      if (t < s) a = a + o;
+    }
+  }
+  __syncthreads();
+  return a;
+}
+)";
+
+std::string generate(const MechTables& T, double ros_d, double ros_c32, bool strict,
+                     bool with_smem) {
+  Gen g{T, strict, {}};
+  auto& o = g.o;
+  o << "// generated: " << T.ns << " species, " << T.nr << " reactions, " << T.nlu
+    << " LU slots\n";
+  o << "#define NS " << T.ns << "\n#define NRA " << (T.nr > 0 ? T.nr : 1) << "\n#define NPA "
+    << (T.npart > 0 ? T.npart : 1) << "\n#define NLU " << T.nlu << "\n";
+  o << "#define ROS_D " << lit(ros_d) << "\n#define ROS_C32 " << lit(ros_c32) << "\n";
+  o << "#define OFF_DONE " << offsetof(Ctl, done) << "\n#define OFF_CUR " << offsetof(Ctl, cur)
+    << "\n#define OFF_DTC " << offsetof(Ctl, dtc) << "\n#define OFF_DTO2 "
+    << offsetof(Ctl, dto2) << "\n#define OFF_DTO6 " << offsetof(Ctl, dto6)
+    << "\n#define OFF_DTG " << offsetof(Ctl, dtgamma) << "\n";
+  o << kPrelude;
+  // one ROS23 attempt of one cell: xn (unclamped) and the cell's sum of squared scaled errors
+  o << R"(
+template <bool HE, int WS>
+__device__ __forceinline__ double ros23_cell(const double* __restrict__ kr,
+    const double* __restrict__ em, u64 N, int c, const double* x, double* xn, double* W,
+    double dt, double dto2, double dto6, double dtg, double rtol, double atol) {
+#define K(r) __ldg(kr + (u64)(r) * N + c)
+#define EM(s) __ldg(em + (u64)(s) * N + c)
+#define WV(e) W[(e) * WS]
+  double v[NRA], P[NPA], f0[NS], k1[NS], f1[NS], k2[NS], b[NS], pv[NS];
+)";
+  g.vel("x");
+  g.rhs("f0");
+  g.partials();
+  g.build_w();
+  g.lu_factor();
+  o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) k1[s] = f0[s];\n";
+  g.lu_solve("k1");
+  o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) xn[s] = x[s] + dto2 * k1[s];\n";
+  g.vel("xn");
+  g.rhs("f1");
+  o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) k2[s] = f1[s] - k1[s];\n";
+  g.lu_solve("k2");
+  o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) k2[s] = k2[s] + k1[s];\n";
+  o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) xn[s] = x[s] + dt * k2[s];\n";
+  g.vel("xn");
+  g.rhs("b");
+  o << R"(#pragma unroll
+  for (int s = 0; s < NS; ++s) {
+    const double a = ROS_C32 * (k2[s] - f1[s]);
+    const double cc = 2.0 * (k1[s] - f0[s]);
+    b[s] = (b[s] - a) - cc;
+  }
+)";
+  g.lu_solve("b");
+  o << R"(  double acc = 0.0;
+#pragma unroll
+  for (int s = 0; s < NS; ++s) {
+    const double ut = dto6 * ((k1[s] - 2.0 * k2[s]) + b[s]);
+    const double am = fmax(fabs(x[s]), fabs(xn[s]));
+    const double den = am * rtol + atol;
+    const double at = ut / den;
+    acc = acc + at * at;
+  }
+  return acc;
+#undef K
+#undef EM
+#undef WV
+}
+
+// global-dt attempt: every cell steps with the controller's dtc; 256-cell block partials
+template <bool HE, bool SMEM>
+__device__ __forceinline__ void attempt_body(const unsigned char* __restrict__ ctl,
+    double* __restrict__ U0, double* __restrict__ U1, const double* __restrict__ kr,
+    const double* __restrict__ em, double* __restrict__ partial, int nc, int nsp,
+    double rtol, double atol, int clamp) {
+  __shared__ double red[256];
+  if (*(const int*)(ctl + OFF_DONE)) return;
+  const double dt = *(const double*)(ctl + OFF_DTC);
+  const double dto2 = *(const double*)(ctl + OFF_DTO2);
+  const double dto6 = *(const double*)(ctl + OFF_DTO6);
+  const double dtg = *(const double*)(ctl + OFF_DTG);
+  const int cur = *(const int*)(ctl + OFF_CUR);
+  const double* __restrict__ U = cur ? U1 : U0;
+  double* __restrict__ Un = cur ? U0 : U1;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const u64 N = (u64)nc;
+  double e = 0.0;
+  if (c < nc) {
+    double x[NS], xn[NS];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) x[s] = U[(u64)s * N + c];
+    if constexpr (SMEM) {
+      extern __shared__ double wsm[];
+      e = ros23_cell<HE, 256>(kr, em, N, c, x, xn, wsm + threadIdx.x, dt, dto2, dto6, dtg,
+                              rtol, atol);
+    } else {
+      double W[NLU];
+      e = ros23_cell<HE, 1>(kr, em, N, c, x, xn, W, dt, dto2, dto6, dtg, rtol, atol);
+    }
+#pragma unroll
+    for (int s = 0; s < NS; ++s) Un[(u64)s * N + c] = clamp ? fmax(xn[s], 0.0) : xn[s];
+    for (int s = NS; s < nsp; ++s) {
+      const double xv = U[(u64)s * N + c];
+      Un[(u64)s * N + c] = clamp ? fmax(xv, 0.0) : xv;
+    }
+  }
+  const double tot = tree256(e, red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = tot;
+}
+
+// per-cell adaptive form: persistent threads pull cells from a device work queue and
+// integrate each over [t0, t1] with its own PI controller
+template <bool HE>
+__device__ __forceinline__ void per_cell_body(int nc, int nsp, double* __restrict__ U,
+    const double* __restrict__ kr, const double* __restrict__ em,
+    double* __restrict__ dt_cell, double* __restrict__ steps_cell,
+    unsigned long long* __restrict__ queue, int* __restrict__ status, PCA a) {
+  double x[NS], xn[NS], W[NLU];
+  double my_steps = 0.0, my_attempts = 0.0;
+  double t = 0, dt = 0, qold = 0, iters = 0, nacc = 0;
+  int c = -1;
+  const u64 N = (u64)nc;
+  const double tlim = a.t1 - 1.0e-9;
+  for (;;) {
+    if (c < 0) {
+      const unsigned long long nxt = atomicAdd(queue, 1ull);
+      if (nxt >= (unsigned long long)nc) break;
+      c = (int)nxt;
+#pragma unroll
+      for (int s = 0; s < NS; ++s) x[s] = U[(u64)s * N + c];
+      t = a.t0;
+      dt = dt_cell[c] > 0.0 ? dt_cell[c] : a.dt0;
+      qold = a.qoldinit;
+      iters = 0;
+      nacc = 0;
+    }
+    if ((t < tlim) && (iters < a.maxiters)) {
+      const double dtc = fmin(dt, a.t1 - t);
+      const double sse = ros23_cell<HE, 1>(kr, em, N, c, x, xn, W, dtc, dtc / 2, dtc / 6,
+                                           dtc * ROS_D, a.rtol, a.atol);
+      double EEst = sqrt(sse / (double)nsp);
+      if (EEst != EEst) EEst = 1.0e10;
+      const double q11 = pow(fmax(EEst, 1.0e-35), a.beta1);
+      double q = q11 / pow(qold, a.beta2);
+      q = fmax(a.invqmax, fmin(a.invqmin, q / a.gamma));
+      if (EEst <= 1.0) {
+#pragma unroll
+        for (int s = 0; s < NS; ++s) x[s] = a.clamp ? fmax(xn[s], 0.0) : xn[s];
+        t = t + dtc;
+        const bool insteady = (a.qsmin <= q) && (q <= a.qsmax);
+        dt = dtc / (insteady ? 1.0 : q);
+        qold = fmax(EEst, a.qoldinit);
+        nacc += 1.0;
+      } else {
+        dt = dtc / fmin(a.invqmin, q11 / a.gamma);
+      }
+      iters += 1.0;
+    } else {
+      if (t < tlim) atomicOr(status, 1);
+#pragma unroll
+      for (int s = 0; s < NS; ++s) U[(u64)s * N + c] = x[s];
+      dt_cell[c] = dt;
+      if (steps_cell) steps_cell[c] = nacc;
+      my_steps += nacc;
+      my_attempts += iters;
+      c = -1;
+    }
+  }
+  if (a.totals) {
+    atomicAdd(a.totals, my_steps);
+    atomicAdd(a.totals + 1, my_attempts);
+  }
+}
+
+#define RS_ATTEMPT(NAME, HE, SMEM)                                                          \
+  extern "C" __global__ void __launch_bounds__(256) NAME(                                   \
+      const unsigned char* __restrict__ ctl, double* __restrict__ U0,                       \
+      double* __restrict__ U1, const double* __restrict__ kr,                               \
+      const double* __restrict__ em, double* __restrict__ partial, int nc, int nsp,         \
+      double rtol, double atol, int clamp) {                                                \
+    attempt_body<HE, SMEM>(ctl, U0, U1, kr, em, partial, nc, nsp, rtol, atol, clamp);       \
+  }
+RS_ATTEMPT(rs_jit_attempt_r0, false, false)
+RS_ATTEMPT(rs_jit_attempt_r1, true, false)
+)";
+  if (with_smem)
+    o << "RS_ATTEMPT(rs_jit_attempt_s0, false, true)\nRS_ATTEMPT(rs_jit_attempt_s1, true, true)\n";
+  o << R"(
+#define RS_PER_CELL(NAME, HE)                                                                \
+  extern "C" __global__ void __launch_bounds__(256) NAME(int nc, int nsp,                   \
+      double* __restrict__ U, const double* __restrict__ kr, const double* __restrict__ em,  \
+      double* __restrict__ dt_cell, double* __restrict__ steps_cell,                         \
+      unsigned long long* __restrict__ queue, int* __restrict__ status, PCA a) {             \
+    per_cell_body<HE>(nc, nsp, U, kr, em, dt_cell, steps_cell, queue, status, a);            \
+  }
+RS_PER_CELL(rs_jit_per_cell_0, false)
+RS_PER_CELL(rs_jit_per_cell_1, true)
+)";
+  return o.str();
+}
+
+// ------------------------------------------------------------------ compile cache
+struct Compiled {
+  cudaLibrary_t lib = nullptr;
+  double ms = 0;
+};
+std::mutex g_mu;
+std::map<std::string, Compiled> g_cache;  // source + options -> loaded library (process life)
+
+}  // namespace
+
+// NVRTC compile of generated source to an sm_103a cubin (no device needed).  With verbose
+// the log carries ptxas's resource usage (registers, spill stores/loads, shared memory).
+bool jit_compile(const std::string& src, bool strict, bool verbose, std::vector<char>* cubin,
+                 std::string* log) {
+  const Nvrtc& N = nvrtc();
+  if (!N.ok()) {
+    *log = N.why;
+    return false;
+  }
+  nvrtcProgram prog = nullptr;
+  nvrtcResult r = N.create(&prog, src.c_str(), "rs_chem_jit.cu", 0, nullptr, nullptr);
+  if (r != NVRTC_SUCCESS) {
+    *log = std::string("nvrtcCreateProgram: ") + N.err(r);
+    return false;
+  }
+  std::vector<const char*> opts = {"-arch=sm_103a", "-std=c++17",
+                                   strict ? "--fmad=false" : "--fmad=true"};
+  if (verbose) opts.push_back("--ptxas-options=-v");
+  r = N.compile(prog, (int)opts.size(), opts.data());
+  size_t n = 0;
+  N.log_size(prog, &n);
+  std::string text(n, '\0');
+  if (n) N.log(prog, &text[0]);
+  while (!text.empty() && text.back() == '\0') text.pop_back();
+  if (r != NVRTC_SUCCESS) {
+    *log = std::string("nvrtcCompileProgram: ") + N.err(r) + "\n" + text;
+    N.destroy(&prog);
+    return false;
+  }
+  *log = text;
+  if (cubin) {
+    size_t nb = 0;
+    N.cubin_size(prog, &nb);
+    cubin->resize(nb);
+    N.cubin(prog, cubin->data());
+  }
+  N.destroy(&prog);
+  return true;
+}
+
+namespace {
+
+bool compile_and_load(const std::string& src, bool strict, Compiled* out, std::string* why) {
+  auto t0 = std::chrono::steady_clock::now();
+  std::vector<char> cubin;
+  std::string log;
+  if (!jit_compile(src, strict, false, &cubin, &log)) {
+    *why = log.substr(0, 4000);
+    return false;
+  }
+  cudaError_t e = cudaLibraryLoadData(&out->lib, cubin.data(), nullptr, nullptr, 0, nullptr,
+                                      nullptr, 0);
+  if (e != cudaSuccess) {
+    *why = std::string("cudaLibraryLoadData: ") + cudaGetErrorString(e);
+    return false;
+  }
+  out->ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0)
+                .count();
+  return true;
+}
+
+}  // namespace
+
+bool jit_chem_eligible(const MechTables& T) {
+  return T.ns >= 1 && T.ns <= 32 && T.nlu <= 256 && T.nr <= 160 && T.npart <= 320;
+}
+
+std::string jit_chem_source(const MechTables& T, bool strict) {
+  return generate(T, 1.0 / (2.0 + std::sqrt(2.0)), 6.0 + std::sqrt(2.0), strict,
+                  smem_bytes(T) <= kSmemCap);
+}
+
+std::shared_ptr<JitChem> jit_chem_build(const MechTables& T, double ros_d, double ros_c32,
+                                        bool strict, std::string* why) {
+  if (!jit_chem_eligible(T)) {
+    *why = "mechanism too large for straight-line kernels";
+    return nullptr;
+  }
+  const bool with_smem = smem_bytes(T) <= kSmemCap;
+  std::string src = generate(T, ros_d, ros_c32, strict, with_smem);
+  std::string key = src + (strict ? "|strict" : "|fast");
+  Compiled cmp;
+  double ms = 0;
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_cache.find(key);
+    if (it != g_cache.end()) {
+      cmp = it->second;
+    } else {
+      if (!compile_and_load(src, strict, &cmp, why)) return nullptr;
+      g_cache[key] = cmp;
+      ms = cmp.ms;
+    }
+  }
+  auto J = std::make_shared<JitChem>();
+  J->compile_ms = ms;
+  auto get = [&](cudaKernel_t* k, const char* name) {
+    cudaError_t e = cudaLibraryGetKernel(k, cmp.lib, name);
+    if (e != cudaSuccess && why->empty())
+      *why = std::string("cudaLibraryGetKernel(") + name + "): " + cudaGetErrorString(e);
+    return e == cudaSuccess;
+  };
+  bool ok = get(&J->attempt[0][0], "rs_jit_attempt_r0") && get(&J->attempt[0][1], "rs_jit_attempt_r1") &&
+            get(&J->per_cell[0], "rs_jit_per_cell_0") && get(&J->per_cell[1], "rs_jit_per_cell_1");
+  if (!ok) return nullptr;
+  if (with_smem && get(&J->attempt[1][0], "rs_jit_attempt_s0") &&
+      get(&J->attempt[1][1], "rs_jit_attempt_s1")) {
+    J->attempt_smem = smem_bytes(T);
+    for (int he = 0; he < 2; ++he) {
+      cudaError_t e = cudaFuncSetAttribute((const void*)J->attempt[1][he],
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)J->attempt_smem);
+      if (e != cudaSuccess) {  // keep the register variant only
+        cudaGetLastError();
+        J->attempt[1][0] = J->attempt[1][1] = nullptr;
+        J->attempt_smem = 0;
+        break;
+      }
+    }
+  }
+  for (int v = 0; v < 2; ++v) {
+    cudaFuncAttributes fa{};
+    if (J->attempt[v][0] && cudaFuncGetAttributes(&fa, (const void*)J->attempt[v][0]) == cudaSuccess)
+      J->regs[v] = fa.numRegs;
+    else
+      cudaGetLastError();
+  }
+  why->clear();
+  return J;
+}
+
+void jit_launch_attempt(const JitChem& J, cudaStream_t st, int nc, int nsp, const Ctl* ctl,
+                        double* U0, double* U1, const double* kr, const double* em,
+                        double* part, double rtol, double atol, int clamp) {
+  const int sm = (J.use_smem && J.attempt[1][0]) ? 1 : 0;
+  cudaKernel_t k = J.attempt[sm][em ? 1 : 0];
+  const unsigned char* c = reinterpret_cast<const unsigned char*>(ctl);
+  void* args[] = {&c, &U0, &U1, &kr, &em, &part, &nc, &nsp, &rtol, &atol, &clamp};
+  int nb = (nc + kBlock - 1) / kBlock;
+  cudaLaunchKernel((const void*)k, dim3(nb), dim3(kBlock), args, sm ? J.attempt_smem : 0, st);
+}
+
+void jit_launch_per_cell(const JitChem& J, cudaStream_t st, int nc, int nsp, int nblocks,
+                         int threads, double* U, const double* kr, const double* em,
+                         double* dtc, double* steps, unsigned long long* queue, int* status,
+                         const PerCellArgs& a) {
+  cudaKernel_t k = J.per_cell[em ? 1 : 0];
+  PerCellArgs av = a;
+  void* args[] = {&nc, &nsp, &U, &kr, &em, &dtc, &steps, &queue, &status, &av};
+  cudaLaunchKernel((const void*)k, dim3(nblocks), dim3(threads), args, 0, st);
+}
+
+}  // namespace rs

@@ -1,0 +1,59 @@
+// rs_jit.h -- mechanism-specialised chemistry kernels (rs_jit.cu).
+//
+// At rs_create the host writes the mechanism's rate products, RHS sums, exact Jacobian, the
+// pivot-free LU of W = I - dt*d*J and its triangular solves out as straight-line CUDA C++
+// (constant indices, constant stoichiometric coefficients) and compiles it for sm_103a with
+// NVRTC.  Every work array then lives in registers (or, for W, in shared memory) and no
+// thread walks an index table, which removes the table loads and the local-memory traffic of
+// the table-walking kernels in rs_chem.cu.  The arithmetic follows the same association as
+// those kernels, so a strict-build handle stays bit-compatible with the CPU restatement.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "rs_device.cuh"
+#include "rs_mech.h"
+
+namespace rs {
+
+struct PerCellArgs;
+
+struct JitChem {
+  cudaKernel_t attempt[2][2] = {};  // [W in shared memory][has emission]; null: not built
+  cudaKernel_t per_cell[2] = {};    // [has emission]
+  size_t attempt_smem = 0;          // dynamic shared bytes of the shared-memory variant
+  int use_smem = 0;                 // variant used for global-dt attempts
+  double compile_ms = 0;            // NVRTC time (0 when the compiled image came from cache)
+  int regs[2] = {0, 0};             // registers per thread of the two attempt variants
+};
+
+// True when the mechanism is small enough for straight-line code (all work arrays of one
+// attempt fit the register file without a table walk).
+bool jit_chem_eligible(const MechTables& T);
+
+// Generate, compile (or fetch from the process-wide cache) and load the specialised kernels
+// for the current device.  Returns null and sets *why when NVRTC is unavailable or fails.
+std::shared_ptr<JitChem> jit_chem_build(const MechTables& T, double ros_d, double ros_c32,
+                                        bool strict, std::string* why);
+
+// The generated source (for inspection and tests).
+std::string jit_chem_source(const MechTables& T, bool strict);
+
+// NVRTC compile of generated source to an sm_103a cubin; needs no device.  With verbose the
+// log carries ptxas's resource usage.  Returns false with the error text in *log.
+bool jit_compile(const std::string& src, bool strict, bool verbose, std::vector<char>* cubin,
+                 std::string* log);
+
+// Same contracts as launch_ros23_attempt / launch_chem_per_cell in rs_kernels.h.
+void jit_launch_attempt(const JitChem& J, cudaStream_t st, int nc, int nsp, const Ctl* ctl,
+                        double* U0, double* U1, const double* kr, const double* em,
+                        double* part, double rtol, double atol, int clamp);
+void jit_launch_per_cell(const JitChem& J, cudaStream_t st, int nc, int nsp, int nblocks,
+                         int threads, double* U, const double* kr, const double* em,
+                         double* dtc, double* steps, unsigned long long* queue, int* status,
+                         const PerCellArgs& a);
+
+}  // namespace rs

@@ -14,12 +14,15 @@ constexpr int kSmallMS = 16, kSmallMR = 40, kSmallMLU = 160, kSmallMP = 80;
 constexpr int kLargeMS = 64, kLargeMR = 128, kLargeMLU = 1600, kLargeMP = 256;
 constexpr int kMaxProgStack = 32;
 
+struct JitChem;
+
 struct LaunchCtx {
   cudaStream_t stream;
   DevMech mech;
   int nc;          // cells
   int nsp;         // species per cell in the state (chemistry species + air mass)
   int size_class;  // 0 small, 1 large
+  const JitChem* jit = nullptr;  // mechanism-specialised kernels, or null: table-walking ones
 };
 
 struct PerCellArgs {
