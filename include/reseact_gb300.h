@@ -235,6 +235,18 @@ rs_status rs_get_chem_kernel(rs_handle* h, int32_t* kind, char* info, size_t inf
 /* The generated CUDA source of a mechanism's specialised kernels, and an NVRTC compile of it
  * for sm_103a with ptxas's resource report in log; neither needs a device.  *len_out (may be
  * NULL) receives the source length + 1; buf may be NULL to query it. */
+/* Elimination order of the pivot-free LU of W = I - gamma h J: ord[k] is the species
+ * eliminated at pivot k.  The strict build keeps the reference's natural order (blocksolve,
+ * rx_traced_integrator.jl:110-135); the production build eliminates in a greedy minimum-fill
+ * order (same symmetric permutation of rows and columns, fewer fill-in slots and updates).
+ * rs_mechanism_lu_order gives either order for a mechanism without a device. */
+rs_status rs_lu_order(rs_handle* h, int32_t* ord, int32_t n);
+rs_status rs_mechanism_lu_order(const rs_mechanism* mech, int32_t natural, int32_t* ord,
+                                int32_t n);
+/* The reciprocal the production build's specialised kernels use in place of IEEE division
+ * (Newton-Raphson from the hardware approximation; the strict build divides), applied to n
+ * host values on the handle's device: a numerics check, r[i] ~ 1/x[i] within a few ulp. */
+rs_status rs_chem_kernel_reciprocal(rs_handle* h, const double* x, double* r, size_t n);
 rs_status rs_chem_kernel_source(const rs_mechanism* mech, int32_t strict, char* buf,
                                 size_t buf_len, size_t* len_out);
 rs_status rs_chem_kernel_compile(const rs_mechanism* mech, int32_t strict, char* log,

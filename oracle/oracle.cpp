@@ -7,6 +7,7 @@
 // OrdinaryDiffEq stack).  This file restates, in plain C++ FP64 with -ffp-contract=off:
 //   * ROS23 attempt           tools/reactant_handoff/rx_traced_integrator.jl:255-349
 //   * pivot-free blocksolve   rx_traced_integrator.jl:101-135  (dense, natural order)
+//     (optionally on the symmetric permutation a production build eliminates in: or_set_lu_order)
 //   * SSPRK43 attempt         rx_traced_integrator.jl:351-437
 //   * PI controller + loop    rx_traced_integrator.jl:85-99, 439-507
 //   * Lie-Trotter macro step  run_reseact_reactant.jl:310-355 (adv), op_split.jl:100-164
@@ -194,6 +195,30 @@ void lu_solve(int n, const double* LU, const double* b, double* x) {
     }
     x[i] = acc / LU[i * n + i];
   }
+}
+
+// The same elimination on the symmetric permutation P W P^T, rows and columns in the order
+// `ord` (species eliminated at each pivot); with an empty order this is blocksolve exactly.
+// Used to check a production build that eliminates in a fill-reducing order.
+void lu_factor_ord(const std::vector<int>& ord, int n, std::vector<double>& W) {
+  if (!ord.empty()) {
+    std::vector<double> P((size_t)n * n);
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) P[(size_t)i * n + j] = W[(size_t)ord[i] * n + ord[j]];
+    W.swap(P);
+  }
+  lu_factor(n, W.data());
+}
+void lu_solve_ord(const std::vector<int>& ord, int n, const double* LU, const double* b,
+                  double* x) {
+  if (ord.empty()) {
+    lu_solve(n, LU, b, x);
+    return;
+  }
+  double bp[64], xp[64];
+  for (int i = 0; i < n; ++i) bp[i] = b[ord[i]];
+  lu_solve(n, LU, bp, xp);
+  for (int i = 0; i < n; ++i) x[ord[i]] = xp[i];
 }
 
 // ------------------------------------------------------------------ fixed reduction tree
@@ -426,6 +451,7 @@ struct Model {
   rs_config cfg;
   Forcing F;
   std::vector<double> krates;  // [nr][nc]
+  std::vector<int> ord;        // LU elimination order (species per pivot); empty: natural
 };
 
 // value of species s (state plane q) at lon index i (ghosts per BC), lat j, lev k
@@ -608,13 +634,13 @@ void ros23_cell(const Model& md, const double* kr, const double* x, const double
       double tmp = dtgamma * J[r * n + s];
       W[r * n + s] = r == s ? 1.0 - tmp : 0.0 - tmp;
     }
-  lu_factor(n, W.data());
-  lu_solve(n, W.data(), f0, k1);
+  lu_factor_ord(md.ord, n, W);
+  lu_solve_ord(md.ord, n, W.data(), f0, k1);
   double dto2 = dt / 2;
   for (int s = 0; s < n; ++s) u1[s] = x[s] + dto2 * k1[s];
   chem_rhs_cell(M, kr, u1, emis, f1, vb);
   for (int s = 0; s < n; ++s) b[s] = f1[s] - k1[s];
-  lu_solve(n, W.data(), b, k2);
+  lu_solve_ord(md.ord, n, W.data(), b, k2);
   for (int s = 0; s < n; ++s) k2[s] = k2[s] + k1[s];
   for (int s = 0; s < n; ++s) xn[s] = x[s] + dt * k2[s];
   chem_rhs_cell(M, kr, xn, emis, f2, vb);
@@ -623,7 +649,7 @@ void ros23_cell(const Model& md, const double* kr, const double* x, const double
     double c = 2.0 * (k1[s] - f0[s]);
     b[s] = (f2[s] - a) - c;
   }
-  lu_solve(n, W.data(), b, k3);
+  lu_solve_ord(md.ord, n, W.data(), b, k3);
   double dto6 = dt / 6;
   for (int s = 0; s < n; ++s) {
     unew[s] = xn[s];
@@ -910,16 +936,19 @@ void ros23_vjp_cell(const Model& md, const double* kr, const double* x, const do
   for (int r = 0; r < n; ++r)
     for (int s = 0; s < n; ++s) W[r * n + s] = (r == s ? 1.0 : 0.0) - dtgamma * J[r * n + s];
   std::vector<double> LU(W);
-  lu_factor(n, LU.data());
-  lu_solve(n, LU.data(), f0, k1);
+  const std::vector<int>& ord = md.ord;
+  lu_factor_ord(ord, n, LU);
+  lu_solve_ord(ord, n, LU.data(), f0, k1);
   for (int s = 0; s < n; ++s) u1[s] = x[s] + (dt / 2) * k1[s];
   chem_rhs_cell(M, kr, u1, emis, f1, vb);
   for (int s = 0; s < n; ++s) b2[s] = f1[s] - k1[s];
-  lu_solve(n, LU.data(), b2, z2);
+  lu_solve_ord(ord, n, LU.data(), b2, z2);
   // transposed solves with the same factors: W^T y = c
-  auto solveT = [&](const double* c, double* y) {
-    // W = L U (unit L); W^T = U^T L^T: forward with U^T, then backward with L^T
-    double t1[64];
+  auto solveT = [&](const double* cs, double* ys) {
+    // P W P^T = L U (unit L); W^T = P^T U^T L^T P: forward with U^T, then backward with L^T,
+    // on the permuted vectors
+    double c[64], y[64], t1[64];
+    for (int i = 0; i < n; ++i) c[i] = ord.empty() ? cs[i] : cs[ord[i]];
     for (int i = 0; i < n; ++i) {
       double acc = c[i];
       for (int j = 0; j < i; ++j) acc -= LU[j * n + i] * t1[j];
@@ -930,6 +959,7 @@ void ros23_vjp_cell(const Model& md, const double* kr, const double* x, const do
       for (int j = i + 1; j < n; ++j) acc -= LU[j * n + i] * y[j];
       y[i] = acc;
     }
+    for (int i = 0; i < n; ++i) ys[ord.empty() ? i : ord[i]] = y[i];
   };
   double k2b[64], k1b[64], b2b[64], f1b[64], u1b[64], f0b[64];
   for (int s = 0; s < n; ++s) { ubar[s] = lam[s]; k2b[s] = dt * lam[s]; k1b[s] = k2b[s]; }
@@ -1028,6 +1058,13 @@ or_model* or_create(const rs_config* cfg) {
 }
 
 void or_destroy(or_model* h) { delete reinterpret_cast<Model*>(h); }
+
+// LU elimination order (species eliminated at each pivot; null restores natural order)
+void or_set_lu_order(or_model* h, const int32_t* ord) {
+  Model& md = *reinterpret_cast<Model*>(h);
+  if (ord) md.ord.assign(ord, ord + md.M.ns);
+  else md.ord.clear();
+}
 
 int or_set_forcing(or_model* h, const rs_forcing* f) {
   Model& md = *reinterpret_cast<Model*>(h);

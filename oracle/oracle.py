@@ -33,6 +33,7 @@ def lib():
         L.or_create.restype = vp
         L.or_create.argtypes = [C.POINTER(abi.rs_config)]
         L.or_destroy.argtypes = [vp]
+        L.or_set_lu_order.argtypes = [vp, C.POINTER(C.c_int32)]
         L.or_set_forcing.argtypes = [vp, C.POINTER(abi.rs_forcing)]
         L.or_set_rates.argtypes = [vp, dp]
         L.or_get_rates.argtypes = [vp, dp]
@@ -85,6 +86,14 @@ class Oracle:
         if getattr(self, "h", None):
             lib().or_destroy(self.h)
             self.h = None
+
+    def set_lu_order(self, ord=None):
+        """Eliminate in this species order (as a production build does); None: natural."""
+        if ord is None:
+            lib().or_set_lu_order(self.h, None)
+        else:
+            self._ord = np.ascontiguousarray(ord, dtype=np.int32)
+            lib().or_set_lu_order(self.h, self._ord.ctypes.data_as(C.POINTER(C.c_int32)))
 
     def set_forcing(self, forcing_abi):
         self._keep = (self._keep[0], forcing_abi)

@@ -20,7 +20,8 @@ SYMBOLS = [
     "rs_record", "rs_record_count", "rs_adjoint_set_lambda", "rs_adjoint_get_lambda",
     "rs_backward_macro_step", "rs_adjoint_get_grad_emission", "rs_adjoint_reset_grad",
     "rs_autotune", "rs_set_chem_kernel", "rs_get_chem_kernel", "rs_chem_kernel_source",
-    "rs_chem_kernel_compile",
+    "rs_chem_kernel_compile", "rs_chem_kernel_reciprocal", "rs_lu_order",
+    "rs_mechanism_lu_order",
 ]
 
 CHEM_KERNEL_AUTO, CHEM_KERNEL_TABLE, CHEM_KERNEL_SPECIALIZED = 0, 1, 2
@@ -96,6 +97,12 @@ def _declare(L):
     L.rs_chem_kernel_source.restype = C.c_int
     L.rs_chem_kernel_compile.argtypes = [C.POINTER(abi.rs_mechanism), i32, C.c_char_p, sz]
     L.rs_chem_kernel_compile.restype = C.c_int
+    L.rs_lu_order.argtypes = [vp, C.POINTER(i32), i32]
+    L.rs_lu_order.restype = C.c_int
+    L.rs_mechanism_lu_order.argtypes = [C.POINTER(abi.rs_mechanism), i32, C.POINTER(i32), i32]
+    L.rs_mechanism_lu_order.restype = C.c_int
+    L.rs_chem_kernel_reciprocal.argtypes = [vp, dp, dp, sz]
+    L.rs_chem_kernel_reciprocal.restype = C.c_int
     return L
 
 
@@ -127,6 +134,18 @@ def chem_kernel_source(mech_abi, strict=False):
     buf = C.create_string_buffer(n.value)
     L.rs_chem_kernel_source(C.byref(mech_abi.struct), int(strict), buf, n.value, None)
     return buf.value.decode()
+
+
+def mechanism_lu_order(mech_abi, natural=False):
+    """The LU elimination order (species per pivot) a build uses for this mechanism: natural
+    for the strict build, minimum fill for the production build.  No GPU needed."""
+    L = load(False)
+    n = mech_abi.struct.n_species
+    ord_ = (C.c_int32 * n)()
+    rc = L.rs_mechanism_lu_order(C.byref(mech_abi.struct), int(natural), ord_, n)
+    if rc != abi.RS_OK:
+        raise RsError(rc, L.rs_last_error(None).decode())
+    return np.array(ord_[:], dtype=np.int32)
 
 
 def chem_kernel_compile(mech_abi, strict=False):
@@ -278,6 +297,20 @@ class Solver:
         buf = C.create_string_buffer(1024)
         self._check(self.L.rs_get_chem_kernel(self.h, C.byref(k), buf, 1024))
         return k.value, json.loads(buf.value.decode())
+
+    def lu_order(self):
+        """Species eliminated at each pivot of this handle's LU (natural in the strict build)."""
+        n = self.cfg.mech.n_species
+        ord_ = (C.c_int32 * n)()
+        self._check(self.L.rs_lu_order(self.h, ord_, n))
+        return np.array(ord_[:], dtype=np.int32)
+
+    def chem_kernel_reciprocal(self, x):
+        """The specialised kernels' production reciprocal of each x (numerics check)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        r = np.empty_like(x)
+        self._check(self.L.rs_chem_kernel_reciprocal(self.h, _p(x), _p(r), x.size))
+        return r
 
     def stream(self):
         return self.L.rs_stream(self.h)

@@ -22,12 +22,13 @@ namespace rs {
 __device__ __forceinline__ void lu_solve_T(const DevMech& M, const double* W, const double* piv,
                                            double* b) {
   for (int j = 0; j < M.ns; ++j) {
+    const int sj = ldi(M.ord + j);
 #if RS_STRICT
-    double tj = b[j] / W[ldi(M.lu_diag + j)];
+    double tj = b[sj] / W[ldi(M.lu_diag + j)];
 #else
-    double tj = b[j] * piv[j];
+    double tj = b[sj] * piv[j];
 #endif
-    b[j] = tj;
+    b[sj] = tj;
     int e1 = ldi(M.up_ptr + j + 1);
     for (int e = ldi(M.up_ptr + j); e < e1; ++e) {
       int i = ldi(M.up_col + e);
@@ -35,11 +36,12 @@ __device__ __forceinline__ void lu_solve_T(const DevMech& M, const double* W, co
     }
   }
   for (int k = M.ns - 1; k >= 0; --k) {
-    double acc = b[k];
+    const int sk = ldi(M.ord + k);
+    double acc = b[sk];
     int e1 = ldi(M.low_ptr + k + 1);
     for (int e = ldi(M.low_ptr + k); e < e1; ++e)
       acc = acc - W[ldi(M.low_slot + e)] * b[ldi(M.low_row + e)];
-    b[k] = acc;
+    b[sk] = acc;
   }
 }
 

@@ -4,7 +4,8 @@
 // CPU restatement of the reference (ROS23 rx_traced_integrator.jl:279-349, blocksolve :110-135,
 // SSPRK43 :362-400, hairer norm :329-347), so the strict build (--fmad=false, RS_STRICT)
 // reproduces it bit for bit given the same rate constants; the fast build differs only by FMA
-// contraction and by multiplying with precomputed reciprocals where the reference divides.
+// contraction, by multiplying with precomputed reciprocals where the reference divides, and by
+// the LU elimination order (minimum fill instead of natural; the same solution to roundoff).
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -18,7 +19,7 @@ namespace rs {
 constexpr int kRedThreads = 256;  // fixed reduction chunk (cells per level-1 partial)
 
 // ------------------------------------------------------------------ mechanism tables
-// Derived on the host from rs_mechanism (rs_mech.cpp); all index arrays are warp-uniform
+// Derived on the host from rs_mechanism (derive_tables in rs_api.cu); all index arrays are warp-uniform
 // reads (every thread walks the same table), served by the L1/texture path.
 struct DevMech {
   int ns, nr, nlu, npart, njac;
@@ -36,17 +37,18 @@ struct DevMech {
   const int* jac_diag;  // 1 if entry e is on the diagonal
   const int* jac_part;
   const double* jac_coef;
-  const int* lu_diag;   // [ns] slot of (i,i)
+  const int* lu_diag;   // [ns] slot of pivot k (elimination position k)
+  const int* ord;       // [ns] species eliminated at position k (identity: natural order)
   const int* elim_ptr;  // [ns+1] per pivot k: range of (i,k) multipliers
   const int* elim_lik;  // slot of (i,k)
   const int* upd_ptr;   // [n_elim+1] per multiplier: range of updates
   const int* upd_dst;
   const int* upd_src;
-  const int* low_ptr;   // [ns+1] forward solve, column k: rows i>k
-  const int* low_row;
+  const int* low_ptr;   // [ns+1] forward solve, pivot column k: rows after k
+  const int* low_row;   //   (species index of the row)
   const int* low_slot;
-  const int* up_ptr;    // [ns+1] backward solve, row i: columns j>i ascending
-  const int* up_col;
+  const int* up_ptr;    // [ns+1] backward solve, pivot row i: columns after i ascending
+  const int* up_col;    //   (species index of the column)
   const int* up_slot;
   const int* prog_ptr;  // rate programs
   const int* prog_op;
@@ -147,8 +149,8 @@ __device__ __forceinline__ void build_w(const DevMech& M, const double* P, doubl
   }
 }
 
-// Pivot-free sparse LU in natural order (the elimination of blocksolve, zero updates skipped);
-// L multipliers overwrite their slots, piv[k] = 1 / U[k,k].
+// Pivot-free sparse LU in elimination order (natural, as blocksolve, in the strict build; zero
+// updates skipped); L multipliers overwrite their slots, piv[k] = 1 / U[k,k] for pivot k.
 __device__ __forceinline__ void lu_factor(const DevMech& M, double* W, double* piv) {
   int m = 0;
   for (int k = 0; k < M.ns; ++k) {
@@ -169,12 +171,12 @@ __device__ __forceinline__ void lu_factor(const DevMech& M, double* W, double* p
   }
 }
 
-// Solve (LU) x = b in place (b -> x): forward replay of the multipliers, then back
-// substitution x_i = (b_i - sum_{j>i} U_ij x_j) / U_ii.
+// Solve (LU) x = b in place (b -> x, indexed by species): forward replay of the multipliers
+// in elimination order, then back substitution x_i = (b_i - sum_{j after i} U_ij x_j) / U_ii.
 __device__ __forceinline__ void lu_solve(const DevMech& M, const double* W, const double* piv,
                                          double* b) {
   for (int k = 0; k < M.ns; ++k) {
-    double bk = b[k];
+    double bk = b[ldi(M.ord + k)];
     int e1 = ldi(M.low_ptr + k + 1);
     for (int e = ldi(M.low_ptr + k); e < e1; ++e) {
       int i = ldi(M.low_row + e);
@@ -183,16 +185,17 @@ __device__ __forceinline__ void lu_solve(const DevMech& M, const double* W, cons
     }
   }
   for (int i = M.ns - 1; i >= 0; --i) {
-    double acc = b[i];
+    const int si = ldi(M.ord + i);
+    double acc = b[si];
     int e1 = ldi(M.up_ptr + i + 1);
     for (int e = ldi(M.up_ptr + i); e < e1; ++e) {
       double wx = W[ldi(M.up_slot + e)] * b[ldi(M.up_col + e)];
       acc = acc - wx;
     }
 #if RS_STRICT
-    b[i] = acc / W[ldi(M.lu_diag + i)];
+    b[si] = acc / W[ldi(M.lu_diag + i)];
 #else
-    b[i] = acc * piv[i];
+    b[si] = acc * piv[i];
 #endif
   }
 }

@@ -177,7 +177,10 @@ struct Gen {
   void lu_factor() {
     int m = 0;
     for (int k = 0; k < T.ns; ++k) {
-      o << "  pv[" << k << "] = 1.0 / WV(" << T.lu_diag[k] << ");\n";
+      if (strict)
+        o << "  pv[" << k << "] = 1.0 / WV(" << T.lu_diag[k] << ");\n";
+      else
+        o << "  pv[" << k << "] = rcp_nr(WV(" << T.lu_diag[k] << "));\n";
       for (int ii = T.elim_ptr[k]; ii < T.elim_ptr[k + 1]; ++ii, ++m) {
         int sl = T.elim_lik[ii];
         o << "  { const double mu_ = WV(" << sl << ") * pv[" << k << "];\n";
@@ -188,20 +191,22 @@ struct Gen {
       }
     }
   }
+  // pivots in elimination order, vector entries by species index (T.ord maps the two)
   void lu_solve(const char* b) {
     for (int k = 0; k < T.ns; ++k)
       for (int e = T.low_ptr[k]; e < T.low_ptr[k + 1]; ++e)
         o << "  " << b << "[" << T.low_row[e] << "] = " << b << "[" << T.low_row[e] << "] - WV("
-          << T.low_slot[e] << ") * " << b << "[" << k << "];\n";
+          << T.low_slot[e] << ") * " << b << "[" << T.ord[k] << "];\n";
     for (int i = T.ns - 1; i >= 0; --i) {
+      const int si = T.ord[i];
       std::ostringstream acc;
-      acc << b << "[" << i << "]";
+      acc << b << "[" << si << "]";
       for (int e = T.up_ptr[i]; e < T.up_ptr[i + 1]; ++e)
         acc << " - WV(" << T.up_slot[e] << ") * " << b << "[" << T.up_col[e] << "]";
       if (strict)
-        o << "  " << b << "[" << i << "] = (" << acc.str() << ") / WV(" << T.lu_diag[i] << ");\n";
+        o << "  " << b << "[" << si << "] = (" << acc.str() << ") / WV(" << T.lu_diag[i] << ");\n";
       else
-        o << "  " << b << "[" << i << "] = (" << acc.str() << ") * pv[" << i << "];\n";
+        o << "  " << b << "[" << si << "] = (" << acc.str() << ") * pv[" << i << "];\n";
     }
   }
 };
@@ -215,6 +220,19 @@ struct PCA {
   double* totals;
 };
 static_assert(sizeof(PCA) == 128, "PerCellArgs layout");
+
+// Reciprocal by Newton-Raphson iteration r <- r + r (1 - d r) from the hardware approximation
+// (PTX rcp.approx.ftz.f64); each step squares the relative error, two steps reach ~1 ulp.
+// Used by the production build in place of IEEE division; d > 0 and normal on every call site
+// (LU pivots 1 - dtgamma*J_ii, error-norm denominators >= atol).
+__device__ __forceinline__ double rcp_nr(double d) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(d));
+  double e = fma(-d, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-d, r, 1.0);
+  return fma(r, e, r);
+}
 
 // pairwise tree over 256 lanes, v[t] += v[t+s] for s = 128 ... 1; total in thread 0
 __device__ __forceinline__ double tree256(double v, double* sm) {
@@ -251,6 +269,7 @@ std::string generate(const MechTables& T, double ros_d, double ros_c32, bool str
     << offsetof(Ctl, dto2) << "\n#define OFF_DTO6 " << offsetof(Ctl, dto6)
     << "\n#define OFF_DTG " << offsetof(Ctl, dtgamma) << "\n";
   o << kPrelude;
+  o << (strict ? "#define RS_QUOT(a, b) ((a) / (b))\n" : "#define RS_QUOT(a, b) ((a) * rcp_nr(b))\n");
   // one ROS23 attempt of one cell: xn (unclamped) and the cell's sum of squared scaled errors
   o << R"(
 template <bool HE, int WS>
@@ -292,7 +311,7 @@ __device__ __forceinline__ double ros23_cell(const double* __restrict__ kr,
     const double ut = dto6 * ((k1[s] - 2.0 * k2[s]) + b[s]);
     const double am = fmax(fabs(x[s]), fabs(xn[s]));
     const double den = am * rtol + atol;
-    const double at = ut / den;
+    const double at = RS_QUOT(ut, den);
     acc = acc + at * at;
   }
   return acc;
@@ -406,19 +425,21 @@ __device__ __forceinline__ void per_cell_body(int nc, int nsp, double* __restric
   }
 }
 
-#define RS_ATTEMPT(NAME, HE, SMEM)                                                          \
-  extern "C" __global__ void __launch_bounds__(256) NAME(                                   \
+#define RS_ATTEMPT(NAME, HE, SMEM, MINB)                                                    \
+  extern "C" __global__ void __launch_bounds__(256, MINB) NAME(                             \
       const unsigned char* __restrict__ ctl, double* __restrict__ U0,                       \
       double* __restrict__ U1, const double* __restrict__ kr,                               \
       const double* __restrict__ em, double* __restrict__ partial, int nc, int nsp,         \
       double rtol, double atol, int clamp) {                                                \
     attempt_body<HE, SMEM>(ctl, U0, U1, kr, em, partial, nc, nsp, rtol, atol, clamp);       \
   }
-RS_ATTEMPT(rs_jit_attempt_r0, false, false)
-RS_ATTEMPT(rs_jit_attempt_r1, true, false)
+RS_ATTEMPT(rs_jit_attempt_r0, false, false, 1)
+RS_ATTEMPT(rs_jit_attempt_r1, true, false, 1)
+RS_ATTEMPT(rs_jit_attempt_q0, false, false, 2)
+RS_ATTEMPT(rs_jit_attempt_q1, true, false, 2)
 )";
   if (with_smem)
-    o << "RS_ATTEMPT(rs_jit_attempt_s0, false, true)\nRS_ATTEMPT(rs_jit_attempt_s1, true, true)\n";
+    o << "RS_ATTEMPT(rs_jit_attempt_s0, false, true, 1)\nRS_ATTEMPT(rs_jit_attempt_s1, true, true, 1)\n";
   o << R"(
 #define RS_PER_CELL(NAME, HE)                                                                \
   extern "C" __global__ void __launch_bounds__(256) NAME(int nc, int nsp,                   \
@@ -429,6 +450,13 @@ RS_ATTEMPT(rs_jit_attempt_r1, true, false)
   }
 RS_PER_CELL(rs_jit_per_cell_0, false)
 RS_PER_CELL(rs_jit_per_cell_1, true)
+
+// the production reciprocal applied elementwise (accuracy check against IEEE division)
+extern "C" __global__ void rs_jit_rcp(const double* __restrict__ x, double* __restrict__ r,
+                                      int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) r[i] = rcp_nr(x[i]);
+}
 )";
   return o.str();
 }
@@ -506,6 +534,8 @@ bool compile_and_load(const std::string& src, bool strict, Compiled* out, std::s
 
 }  // namespace
 
+const char* const kJitVariantNames[kJitVariants] = {"regs", "smem", "regs2"};
+
 bool jit_chem_eligible(const MechTables& T) {
   return T.ns >= 1 && T.ns <= 32 && T.nlu <= 256 && T.nr <= 160 && T.npart <= 320;
 }
@@ -546,7 +576,9 @@ std::shared_ptr<JitChem> jit_chem_build(const MechTables& T, double ros_d, doubl
     return e == cudaSuccess;
   };
   bool ok = get(&J->attempt[0][0], "rs_jit_attempt_r0") && get(&J->attempt[0][1], "rs_jit_attempt_r1") &&
-            get(&J->per_cell[0], "rs_jit_per_cell_0") && get(&J->per_cell[1], "rs_jit_per_cell_1");
+            get(&J->attempt[2][0], "rs_jit_attempt_q0") && get(&J->attempt[2][1], "rs_jit_attempt_q1") &&
+            get(&J->per_cell[0], "rs_jit_per_cell_0") && get(&J->per_cell[1], "rs_jit_per_cell_1") &&
+            get(&J->rcp, "rs_jit_rcp");
   if (!ok) return nullptr;
   if (with_smem && get(&J->attempt[1][0], "rs_jit_attempt_s0") &&
       get(&J->attempt[1][1], "rs_jit_attempt_s1")) {
@@ -563,7 +595,7 @@ std::shared_ptr<JitChem> jit_chem_build(const MechTables& T, double ros_d, doubl
       }
     }
   }
-  for (int v = 0; v < 2; ++v) {
+  for (int v = 0; v < kJitVariants; ++v) {
     cudaFuncAttributes fa{};
     if (J->attempt[v][0] && cudaFuncGetAttributes(&fa, (const void*)J->attempt[v][0]) == cudaSuccess)
       J->regs[v] = fa.numRegs;
@@ -577,12 +609,18 @@ std::shared_ptr<JitChem> jit_chem_build(const MechTables& T, double ros_d, doubl
 void jit_launch_attempt(const JitChem& J, cudaStream_t st, int nc, int nsp, const Ctl* ctl,
                         double* U0, double* U1, const double* kr, const double* em,
                         double* part, double rtol, double atol, int clamp) {
-  const int sm = (J.use_smem && J.attempt[1][0]) ? 1 : 0;
-  cudaKernel_t k = J.attempt[sm][em ? 1 : 0];
+  const int v = J.attempt[J.variant][0] ? J.variant : 0;
+  const int sm = v == 1;
+  cudaKernel_t k = J.attempt[v][em ? 1 : 0];
   const unsigned char* c = reinterpret_cast<const unsigned char*>(ctl);
   void* args[] = {&c, &U0, &U1, &kr, &em, &part, &nc, &nsp, &rtol, &atol, &clamp};
   int nb = (nc + kBlock - 1) / kBlock;
   cudaLaunchKernel((const void*)k, dim3(nb), dim3(kBlock), args, sm ? J.attempt_smem : 0, st);
+}
+
+void jit_launch_rcp(const JitChem& J, cudaStream_t st, const double* x, double* r, int n) {
+  void* args[] = {&x, &r, &n};
+  cudaLaunchKernel((const void*)J.rcp, dim3((n + 255) / 256), dim3(256), args, 0, st);
 }
 
 void jit_launch_per_cell(const JitChem& J, cudaStream_t st, int nc, int nsp, int nblocks,

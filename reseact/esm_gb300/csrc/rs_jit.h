@@ -21,13 +21,21 @@ namespace rs {
 
 struct PerCellArgs;
 
+// Variants of the global-dt attempt kernel (the autotuner picks one by timing):
+//   0 "regs"   W in registers (spilled by ptxas where needed), one 256-thread block per SM
+//   1 "smem"   W in dynamic shared memory, [slot][thread] so a warp's accesses are contiguous
+//   2 "regs2"  as 0 but capped at 128 registers for two blocks per SM
+constexpr int kJitVariants = 3;
+extern const char* const kJitVariantNames[kJitVariants];
+
 struct JitChem {
-  cudaKernel_t attempt[2][2] = {};  // [W in shared memory][has emission]; null: not built
-  cudaKernel_t per_cell[2] = {};    // [has emission]
-  size_t attempt_smem = 0;          // dynamic shared bytes of the shared-memory variant
-  int use_smem = 0;                 // variant used for global-dt attempts
-  double compile_ms = 0;            // NVRTC time (0 when the compiled image came from cache)
-  int regs[2] = {0, 0};             // registers per thread of the two attempt variants
+  cudaKernel_t attempt[kJitVariants][2] = {};  // [variant][has emission]; null: not built
+  cudaKernel_t per_cell[2] = {};               // [has emission]
+  cudaKernel_t rcp = nullptr;                  // elementwise production reciprocal
+  size_t attempt_smem = 0;  // dynamic shared bytes of the shared-memory variant
+  int variant = 0;          // variant used for global-dt attempts
+  double compile_ms = 0;    // NVRTC time (0 when the compiled image came from cache)
+  int regs[kJitVariants] = {0, 0, 0};  // registers per thread of each attempt variant
 };
 
 // True when the mechanism is small enough for straight-line code (all work arrays of one
@@ -51,6 +59,7 @@ bool jit_compile(const std::string& src, bool strict, bool verbose, std::vector<
 void jit_launch_attempt(const JitChem& J, cudaStream_t st, int nc, int nsp, const Ctl* ctl,
                         double* U0, double* U1, const double* kr, const double* em,
                         double* part, double rtol, double atol, int clamp);
+void jit_launch_rcp(const JitChem& J, cudaStream_t st, const double* x, double* r, int n);
 void jit_launch_per_cell(const JitChem& J, cudaStream_t st, int nc, int nsp, int nblocks,
                          int threads, double* U, const double* kr, const double* em,
                          double* dtc, double* steps, unsigned long long* queue, int* status,

@@ -12,7 +12,8 @@ struct MechTables {
       rhs_ptr, rhs_r,               // RHS terms of species s: reactions ascending
       part_r, part_q, part_e,       // partial p = d v_{part_r} / d x_{part_q}
       jac_ptr, jac_slot, jac_diag, jac_part,  // Jacobian entries (row-major) and their terms
-      lu_diag,                      // LU slot of (i,i)
+      lu_diag,                      // LU slot of pivot k (elimination position)
+      ord,                          // species eliminated at position k
       elim_ptr, elim_lik, upd_ptr, upd_dst, upd_src,  // natural-order elimination schedule
       low_ptr, low_row, low_slot,   // forward solve, column k: rows i>k
       up_ptr, up_col, up_slot,      // backward solve, row i: columns j>i ascending

@@ -208,8 +208,37 @@ class Mechanism:
             upper_ptr=i32(upper_ptr), upper_col=i32(upper_col), upper_slot=i32(upper_slot),
         )
 
-    def flop_counts(self):
-        """FP64 operation counts per cell for one ROS23 attempt (sparse, as executed)."""
+    def lu_counts(self, order=None):
+        """(LU slots, multipliers, updates, lower entries, upper entries) of the pivot-free
+        elimination of W = I - gamma h J in the given species order (natural if None)."""
+        t = self.tables()
+        if order is None:
+            return (int(t["n_lu"]), len(t["elim_lik"]), len(t["upd_dst"]),
+                    len(t["lower_slot"]), len(t["upper_slot"]))
+        ns = self.ns
+        net = self.net_stoich()
+        pos = {int(s): k for k, s in enumerate(order)}
+        fill = {(k, k) for k in range(ns)}
+        for r, rx in enumerate(self.reactions):
+            for q, _nu in rx.reactants:
+                for s in range(ns):
+                    if net[r, s] != 0.0:
+                        fill.add((pos[s], pos[q]))
+        mults = upds = 0
+        for k in range(ns):
+            rows = [i for i in range(k + 1, ns) if (i, k) in fill]
+            cols = [j for j in range(k + 1, ns) if (k, j) in fill]
+            mults += len(rows)
+            upds += len(rows) * len(cols)
+            for i in rows:
+                for j in cols:
+                    fill.add((i, j))
+        low = sum(1 for (i, j) in fill if i > j)
+        return len(fill), mults, upds, low, sum(1 for (i, j) in fill if i < j)
+
+    def flop_counts(self, order=None):
+        """FP64 operation counts per cell for one ROS23 attempt (sparse, as executed) with the
+        LU eliminated in the given species order (natural, as the reference, if None)."""
         t = self.tables()
         nr, ns = self.nr, self.ns
         n_react = int(t["react_ptr"][-1])
@@ -218,9 +247,10 @@ class Mechanism:
         rhs = rate + 2 * len(t["rhs_reaction"])  # mul + add per term
         part = int(t["n_partials"]) * max(1, n_react // max(1, nr))  # ~products per partial
         jac = part + 2 * len(t["jac_part"])
-        wbuild = int(t["n_lu"]) + ns  # scale + diagonal add
-        lu = ns + len(t["elim_lik"]) + 2 * len(t["upd_dst"])  # piv, multipliers, updates
-        solve = 2 * len(t["lower_slot"]) + 2 * len(t["upper_slot"]) + ns
+        n_lu, n_mult, n_upd, n_low, n_up = self.lu_counts(order)
+        wbuild = n_lu + ns  # scale + diagonal add
+        lu = ns + n_mult + 2 * n_upd  # piv, multipliers, updates
+        solve = 2 * n_low + 2 * n_up + ns
         stage = 3 * 3 * ns + 6 * ns  # stage combos k2, unew, b3, utilde
         eest = 8 * ns
         total = 3 * rhs + jac + wbuild + lu + 3 * solve + stage + eest

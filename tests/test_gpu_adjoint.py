@@ -39,6 +39,7 @@ def test_adjoint_sweep_matches_oracle(oracle_mod, do_T, do_C):
     f = w.forcing_abi()
     s.set_forcing(f)
     o = oracle_mod.Oracle(cfg, f, mabi)
+    o.set_lu_order(s.lu_order())
     o.set_rates(s.rates())
     s.set_state(w.u0_cellmajor())
     s.record(True)

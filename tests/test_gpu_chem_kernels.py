@@ -76,6 +76,7 @@ def test_attempt_specialised_vs_oracle(oracle_mod, strict):
     s.set_forcing(f)
     assert s.chem_kernel()[0] == CHEM_KERNEL_SPECIALIZED
     o = oracle_mod.Oracle(cfg, f, mabi)
+    o.set_lu_order(s.lu_order())
     o.set_rates(s.rates())
     un_o, e_o = o.single_step(abi.RS_OP_CHEMISTRY, w.u0, 0.0, 30.0)
     un_g, e_g = s.single_step(abi.RS_OP_CHEMISTRY, w.u0_cellmajor(), 0.0, 30.0)
@@ -140,7 +141,8 @@ def test_autotuned_chemistry_variant_is_bitwise_neutral():
         s.set_state(w.u0_cellmajor())
         rep = s.autotune() if tune else None
         if tune:
-            assert rep["chem_choice"] in ("regs", "smem") and len(rep["chem_attempt"]) == 2
+            assert rep["chem_choice"] in ("regs", "smem", "regs2")
+            assert len(rep["chem_attempt"]) == 3
         t, a, b = 0.0, 15.0, 0.5
         for _ in range(2):
             _, a, b, _ = s.macro_step(t, t + 600.0, a, b)
@@ -148,3 +150,18 @@ def test_autotuned_chemistry_variant_is_bitwise_neutral():
         res.append(s.get_state())
         s.close()
     assert np.array_equal(res[0], res[1])
+
+
+def test_production_reciprocal_within_two_ulp():
+    """The Newton-Raphson reciprocal that replaces IEEE division in the production build's
+    specialised kernels, against the correctly rounded 1/x, over the magnitudes the kernels
+    divide by (LU pivots near 1, error-norm denominators from atol upwards)."""
+    rng = np.random.default_rng(7)
+    x = np.concatenate([10.0 ** rng.uniform(-30, 30, 200000), 1.0 + rng.uniform(0, 1e3, 50000),
+                        np.array([1.0, 2.0, 3.0, 1e-9, 1.0 + 2.0 ** -52, 1.5, 7.0])])
+    s = Solver.for_workload(workloads.c1())
+    r = s.chem_kernel_reciprocal(x)
+    ref = 1.0 / x
+    ulp = np.abs(r - ref) / np.spacing(ref)
+    assert ulp.max() <= 2.0, ulp.max()
+    assert np.mean(r == ref) > 0.5  # mostly the correctly rounded value

@@ -12,6 +12,8 @@ import pytest
 from reseact.esm_gb300 import Solver, abi, workloads
 from reseact.esm_gb300._lib import RsError
 
+from parity_util import per_cell_agreement
+
 pytestmark = pytest.mark.gpu
 
 REL = 1e-10  # spec FP64 parity tolerance
@@ -40,6 +42,7 @@ def make_pair(w, oracle_mod, strict=False, **kw):
     f = w.forcing_abi()
     s.set_forcing(f)
     o = oracle_mod.Oracle(cfg, f, mabi)
+    o.set_lu_order(s.lu_order())  # the elimination order of this build
     return s, o
 
 
@@ -188,6 +191,7 @@ def _c3_pair(oracle_mod, strict, ncells=2048, **kw):
     f = w.forcing_abi()
     s.set_forcing(f)
     o = oracle_mod.Oracle(cfg, f, mabi)
+    o.set_lu_order(s.lu_order())
     o.set_rates(s.rates())
     s.set_state(w.u0_cellmajor())
     return w, cfg, s, o
@@ -214,22 +218,19 @@ def test_per_cell_single_attempt(oracle_mod, strict):
 @pytest.mark.parametrize("strict", [False, True])
 def test_per_cell_mode_matches_oracle(oracle_mod, strict):
     """Per-cell adaptive chemistry (persistent work-queue kernel) against the oracle's per-cell
-    loop over a whole 600 s window, uneven step counts.  This problem is sensitive at the
-    solver's absolute tolerance: the ORACLE ITSELF moves by ~1e-9 absolute when dt0 changes
-    by one ulp (values below atol are uncontrolled and clamped at 0), so the bound is the
-    integration tolerance, rtol*|u| + atol, not roundoff."""
+    loop over a whole 600 s window, uneven step counts, on the stiff synthetic mechanism
+    (stiffness ratio ~1e8).  The solution of this problem is only determined to the
+    integration tolerance: the oracle itself moves by up to ~1 x (rtol |u| + atol) when dt0
+    changes by one ulp, and a cell whose accept/reject sequence flips on roundoff ends at a
+    different valid point (checked by per_cell_agreement)."""
     w, cfg, s, o = _c3_pair(oracle_mod, strict)
     u = np.ascontiguousarray(w.u0.copy())
     rc, _, _, st = s.macro_step(0.0, 600.0, 1.0, 1e-3)
     orc, _, steps = o.chem_per_cell(u, 0.0, 600.0, 1e-3)
     assert rc == 0 and orc == 0
     assert steps.min() >= 1 and steps.max() > 2 * steps.min()  # uneven per-cell work
-    got, ref = s.get_state(), cm(w, u)
-    bound = cfg.rtol_C * np.abs(ref) + cfg.atol_C
-    assert np.all(np.abs(got - ref) <= 2.0 * bound), np.max(np.abs(got - ref) / bound)
-    # most of the state agrees far more tightly than the bound
-    rel = np.abs(got - ref) / np.maximum(np.abs(ref), cfg.atol_C)
-    assert np.median(rel) < 1e-9
+    per_cell_agreement(s.get_state(), cm(w, u), cfg, w.nsp)
+
 
 def test_maxiters_is_reported_and_handle_stays_usable(oracle_mod):
     w = small_c2()
