@@ -52,6 +52,8 @@ def parse():
     p.add_argument("--c3-cells", type=int, default=1 << 20)
     p.add_argument("--c3-skip-global", action="store_true", help="time only the per-cell form")
     p.add_argument("--small", action="store_true", help="small grid (profiling/debug)")
+    p.add_argument("--c5", type=int, default=0, metavar="STEPS",
+                   help="also time STEPS macro steps of the full-scale C5 forms (several minutes)")
     return p.parse_args()
 
 
@@ -296,6 +298,7 @@ def run_gb300(args):
     adjoint = None if args.no_adjoint else measure_adjoint(args, local, barrier)
     batched_c3 = None if args.no_c3 else measure_c3(local, barrier, args.c3_cells,
                                                     args.c3_skip_global)
+    full_c5 = measure_c5(local, barrier, args.c5) if args.c5 > 0 else None
 
     # ------------------------------------------------------------------ roofline pass
     t, dtT, dtC = t_end, dtT_end, dtC_end
@@ -357,7 +360,7 @@ def run_gb300(args):
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": "256 MiB flush between timed steps"},
             "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "forms": forms,
-            "adjoint": adjoint, "batched_c3": batched_c3,
+            "adjoint": adjoint, "batched_c3": batched_c3, "full_c5": full_c5,
             "autotune": {k: v for k, v in tuning.items() if k.endswith("choice")},
             "transport": transport, "kernels": kernels, "dominant": dom,
             "attempts_per_step": {"naT": float(np.mean([c[0] for c in counts])),
@@ -450,6 +453,75 @@ def measure_c3(local, barrier, ncells=1 << 20, skip_global=False):
         s.close()
     if not skip_global:
         out["per_cell_speedup"] = round(out["global_dt"]["ms"] / out["per_cell"]["ms"], 3)
+    return out
+
+
+def measure_c5(local, barrier, steps=1):
+    """Full scale: 360x181x72 (4.69M cells), the synthetic 30-species / 60-reaction mechanism
+    plus air mass, dt = 300 s, deformational winds.  From the same seeded state, `steps` macro
+    steps of (a) plain FP64 with the reference's global-dt chemistry, (b) mixed-precision
+    transport with global-dt chemistry, (c) the batched mixed form (mixed transport, per-cell
+    chemistry work queue).  (b) against (a) isolates the precision change; (c) against (a)
+    also changes the chemistry step sequence, so its difference is stated in units of the
+    integration tolerance."""
+    import torch
+    from reseact.esm_gb300 import Solver, abi, workloads
+    w = workloads.c5(precision=abi.RS_PREC_FP64)
+    u0 = w.u0_cellmajor()
+    out = {"workload": "C5 360x181x72 (4,691,520 cells) synthetic 30x60 + air mass, dt=300 s, "
+                       "%d macro step(s) from t=0" % steps}
+    ends = {}
+    forms = (("fp64", dict(precision=abi.RS_PREC_FP64)),
+             ("mixed", dict(precision=abi.RS_PREC_MIXED)),
+             ("batched_mixed", dict(precision=abi.RS_PREC_MIXED, chem_mode=abi.RS_CHEM_PER_CELL)),
+             ("batched_fp64", dict(precision=abi.RS_PREC_FP64, chem_mode=abi.RS_CHEM_PER_CELL)),
+             ("transport_fp64", dict(precision=abi.RS_PREC_FP64, do_chemistry=False)),
+             ("transport_mixed", dict(precision=abi.RS_PREC_MIXED, do_chemistry=False)))
+    for name, kw in forms:
+        t_form = time.perf_counter()
+        # maxiters bounds a pathological form to minutes instead of the reference's 2e4 attempts
+        s = Solver.for_workload(w, device=local, maxiters=5000, **kw)
+        s.set_state(u0)
+        tune = s.autotune()
+        stream = torch.cuda.ExternalStream(s.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t, a, b = 0.0, w.dt0_T, w.dt0_C
+        counts = []
+        barrier()
+        e0.record(stream)
+        for _ in range(steps):
+            rc, a, b, st = s.macro_step(t, t + w.dt_macro, a, b)
+            counts.append([st.naT, st.nrT, st.naC, st.nrC, st.chem_cell_steps])
+            t += w.dt_macro
+        e1.record(stream)
+        barrier()
+        ms = e0.elapsed_time(e1)
+        ends[name] = s.get_state()
+        print("c5 %s: %.1f ms/step, %.1f s wall, attempts %s" % (name, ms / steps,
+              time.perf_counter() - t_form, counts), file=sys.stderr, flush=True)
+        out[name] = {"ms_per_step": round(ms / steps, 2),
+                     "value": round(w.ncells * steps / (ms * 1e-3), 2), "status": rc,
+                     "attempts": counts, "chem_kernel": s.chem_kernel()[1].get("kind"),
+                     "tune": {k: tune[k] for k in ("chem_choice", "per_cell_choice",
+                                                   "transport_choice") if k in tune}}
+        s.close()
+    def diff(a, b):
+        d = np.abs(ends[a] - ends[b])
+        r = d / np.maximum(np.abs(ends[b]), 1e-30)
+        rc = r.reshape(-1, w.nsp).max(axis=1)  # worst species per cell
+        return {"max_rel_err": float((d / np.maximum(np.abs(ends[b]), 1e-9)).max()),
+                "median_rel_err": float(np.median(r)),
+                "cells_within_1e-6_rel": float(np.mean(rc <= 1e-6)),
+                "max_err_in_tolerance_units": float((d / (1e-4 * np.abs(ends[b]) + 1e-9)).max())}
+    for name in ("mixed", "batched_mixed", "batched_fp64"):
+        out[name]["speedup_vs_fp64"] = round(out["fp64"]["ms_per_step"] / out[name]["ms_per_step"], 3)
+    # precision alone: same method, FP32 reconstruction vs FP64
+    out["errors"] = {"transport_mixed_vs_transport_fp64": diff("transport_mixed", "transport_fp64"),
+                     "batched_mixed_vs_batched_fp64": diff("batched_mixed", "batched_fp64"),
+                     "mixed_vs_fp64": diff("mixed", "fp64"),
+                     # method change too: per-cell vs global error control over 145M states
+                     "batched_mixed_vs_fp64": diff("batched_mixed", "fp64"),
+                     "batched_fp64_vs_fp64": diff("batched_fp64", "fp64")}
     return out
 
 

@@ -106,8 +106,14 @@ def winds_solid_body(g, dp, u0=20.0):
     return mx, my, mz
 
 
-def winds_deformational(g, dp, u0=40.0, w0=0.05, seed=7):
-    """u = U0 sin^2(lon_face) sin(2 lat), v = 0, Mz = +-w0 (seeded sign per column)."""
+def winds_deformational(g, dp, u0=40.0, w0=0.05, seed=7, w_shape="constant"):
+    """u = U0 sin^2(lon_face) sin(2 lat), v = 0, Mz = +-w0 (seeded sign per column).
+
+    w_shape "constant": Mz = +-w0 at every interior interface (zero at the surface and the
+    model top).  "sine": Mz = +-w0 sin(pi p / p_s) at interface pressure p, which vanishes
+    towards the model top and the surface, so that thin layers (the 1 Pa top layer of the
+    72-level hybrid grid) are not emptied: with the constant shape that layer loses its
+    whole mass in 20 s."""
     nlon, nlat, nlev = g["nlon"], g["nlat"], g["nlev"]
     latc = g["lat0_deg"] + np.arange(nlat) * g["dlat_deg"]
     lonf = g["lon0_deg"] + (np.arange(nlon + 1) - 0.5) * g["dlon_deg"]
@@ -118,7 +124,12 @@ def winds_deformational(g, dp, u0=40.0, w0=0.05, seed=7):
     sign = rng.choice([-1.0, 1.0], size=(nlat, nlon))
     mz = np.zeros((nlev + 1, nlat, nlon))
     if nlev > 1:
-        mz[1:nlev] = w0 * sign[None, :, :]
+        if w_shape == "sine":
+            p_int = np.concatenate([[0.0], np.cumsum(dp[::-1])])[::-1]  # interface k, k=0 surface
+            shape = np.sin(np.pi * p_int[1:nlev] / p_int[0])
+            mz[1:nlev] = w0 * shape[:, None, None] * sign[None, :, :]
+        else:
+            mz[1:nlev] = w0 * sign[None, :, :]
     return np.ascontiguousarray(mx), my, mz
 
 
@@ -236,7 +247,7 @@ def c5(seed=5, mech=None, precision=abi.RS_PREC_MIXED):
     g = latlon_grid(360, 181, 72, lon0=0.0, dlon=1.0)
     dp, pm = hybrid72()
     dp3, p3, t3 = _column_fields(g, dp, pm)
-    mx, my, mz = winds_deformational(g, dp, seed=seed + 100)
+    mx, my, mz = winds_deformational(g, dp, seed=seed + 100, w_shape="sine")
     rng = np.random.default_rng(seed)
     shape = (g["nlev"], g["nlat"], g["nlon"])
     planes = [10.0 ** rng.uniform(-12.0, -6.0, size=shape) for _ in mech.species]
