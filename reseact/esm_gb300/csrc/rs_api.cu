@@ -347,6 +347,7 @@ struct rs_handle {
   } tune;
   // mechanism-specialised chemistry kernels (null: not built) and the kind in use
   std::shared_ptr<rs::JitChem> jit;
+  DevBuf<double> fsal[2];  // f(U[b]) planes [ns][nc] for the specialised global-dt attempts
   std::string jit_why;
   int chem_kernel = RS_CHEM_KERNEL_AUTO;
 };
@@ -603,7 +604,7 @@ void chem_attempt(rs_handle* h, Ctl* c) {
     Scope s(h, "ros23_attempt");
     rs::launch_ros23_attempt(h->lc, c, h->U[0].p, h->U[1].p, h->krates.p,
                              h->have_emis ? h->emis.p : nullptr, h->partial.p, h->cfg.rtol_C,
-                             h->cfg.atol_C, h->cfg.clamp_nonneg);
+                             h->cfg.atol_C, h->cfg.clamp_nonneg, h->fsal[0].p, h->fsal[1].p);
   }
   Scope s(h, "finalize");
   rs::launch_finalize(h->st, c, h->partial.p, (int)((h->nc + 255) / 256));
@@ -655,7 +656,7 @@ void build_loop_graph(rs_handle* h, int slot) {
     lc.stream = h->cap;
     rs::launch_ros23_attempt(lc, c, h->U[0].p, h->U[1].p, h->krates.p,
                              h->have_emis ? h->emis.p : nullptr, h->partial.p, h->cfg.rtol_C,
-                             h->cfg.atol_C, h->cfg.clamp_nonneg);
+                             h->cfg.atol_C, h->cfg.clamp_nonneg, h->fsal[0].p, h->fsal[1].p);
   }
   rs::launch_finalize_graph(h->cap, c, h->partial.p, nparts, cond);
   cudaGraph_t captured = nullptr;
@@ -764,6 +765,10 @@ rs_status rs_create(const rs_config* cfg, rs_handle** out) {
     h->lc = rs::LaunchCtx{h->st, h->dm, (int)h->nc, h->nsp, cls};
     h->jit = rs::jit_chem_build(h->mt, h->dm.ros_d, h->dm.ros_c32, RS_STRICT != 0, &h->jit_why);
     h->lc.jit = h->jit.get();
+    if (h->jit && cfg->do_chemistry && cfg->chem_mode == RS_CHEM_GLOBAL_DT) {
+      h->fsal[0].alloc((size_t)T.ns * h->nc);
+      h->fsal[1].alloc((size_t)T.ns * h->nc);
+    }
     size_t n = h->nc * h->nsp;
     h->U[0].alloc(n); h->U[1].alloc(n);
     h->U[0].zero(h->st); h->U[1].zero(h->st);
@@ -827,7 +832,7 @@ void rs_destroy(rs_handle* h) {
                             &h->partial, &h->krates, &h->T, &h->P, &h->emis, &h->io, &h->io2,
                             &h->mx, &h->my, &h->mz, &h->qw, &h->qe, &h->qs, &h->qn, &h->gx,
                             &h->gylo, &h->gyhi, &h->vsA, &h->vsB, &h->veAB, &h->veC, &h->veD,
-                            &h->dtcell, &h->stepcell, &h->totals};
+                            &h->dtcell, &h->stepcell, &h->totals, &h->fsal[0], &h->fsal[1]};
   for (auto* b : bufs) b->release();
   h->slot_row.release();
   h->slot_col.release();

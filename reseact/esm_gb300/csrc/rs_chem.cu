@@ -304,10 +304,10 @@ void launch_rates(const LaunchCtx& L, const double* T, const double* P, double* 
 }
 void launch_ros23_attempt(const LaunchCtx& L, const Ctl* ctl, double* U0, double* U1,
                           const double* kr, const double* em, double* part, double rtol,
-                          double atol, int clamp) {
+                          double atol, int clamp, double* F0, double* F1) {
   if (L.jit) {
     jit_launch_attempt(*L.jit, L.stream, L.nc, L.nsp, ctl, U0, U1, kr, em, part, rtol, atol,
-                       clamp);
+                       clamp, F0, F1);
     return;
   }
   if (L.size_class == 0) Small::attempt(L, ctl, U0, U1, kr, em, part, rtol, atol, clamp);

@@ -120,9 +120,12 @@ struct Gen {
       else if (c == -1.0) e << "-" << term;
       else e << lit(c) << "*" << term;
     } else {
-      if (c == 1.0) e << " + " << term;
-      else if (c == -1.0) e << " - " << term;
-      else e << " + " << lit(c) << "*" << term;
+      // fold into the running sum: e is rebuilt around the previous expression
+      std::string prev = e.str();
+      e.str("");
+      if (c == 1.0) e << prev << " + " << term;
+      else if (c == -1.0) e << prev << " - " << term;
+      else e << "RS_FMA(" << lit(c) << ", " << term << ", " << prev << ")";
     }
   }
   void rhs(const char* f) {
@@ -170,7 +173,7 @@ struct Gen {
         first = false;
       }
       std::string a = first ? std::string("0.0") : acc.str();
-      w[T.jac_slot[e]] = T.jac_diag[e] ? "1.0 - dtg*(" + a + ")" : "-(dtg*(" + a + "))";
+      w[T.jac_slot[e]] = T.jac_diag[e] ? "RS_FMA(-dtg, (" + a + "), 1.0)" : "-(dtg*(" + a + "))";
     }
     for (int e = 0; e < T.nlu; ++e) o << "  WV(" << e << ") = " << w[e] << ";\n";
   }
@@ -185,8 +188,8 @@ struct Gen {
         int sl = T.elim_lik[ii];
         o << "  { const double mu_ = WV(" << sl << ") * pv[" << k << "];\n";
         for (int u = T.upd_ptr[m]; u < T.upd_ptr[m + 1]; ++u)
-          o << "    WV(" << T.upd_dst[u] << ") = WV(" << T.upd_dst[u] << ") - mu_ * WV("
-            << T.upd_src[u] << ");\n";
+          o << "    WV(" << T.upd_dst[u] << ") = RS_FMA(-mu_, WV(" << T.upd_src[u] << "), WV("
+            << T.upd_dst[u] << "));\n";
         o << "    WV(" << sl << ") = mu_; }\n";
       }
     }
@@ -195,18 +198,18 @@ struct Gen {
   void lu_solve(const char* b) {
     for (int k = 0; k < T.ns; ++k)
       for (int e = T.low_ptr[k]; e < T.low_ptr[k + 1]; ++e)
-        o << "  " << b << "[" << T.low_row[e] << "] = " << b << "[" << T.low_row[e] << "] - WV("
-          << T.low_slot[e] << ") * " << b << "[" << T.ord[k] << "];\n";
+        o << "  " << b << "[" << T.low_row[e] << "] = RS_FMA(-WV(" << T.low_slot[e] << "), " << b
+          << "[" << T.ord[k] << "], " << b << "[" << T.low_row[e] << "]);\n";
     for (int i = T.ns - 1; i >= 0; --i) {
       const int si = T.ord[i];
-      std::ostringstream acc;
-      acc << b << "[" << si << "]";
+      std::string acc = std::string(b) + "[" + std::to_string(si) + "]";
       for (int e = T.up_ptr[i]; e < T.up_ptr[i + 1]; ++e)
-        acc << " - WV(" << T.up_slot[e] << ") * " << b << "[" << T.up_col[e] << "]";
+        acc = "RS_FMA(-WV(" + std::to_string(T.up_slot[e]) + "), " + b + "[" +
+              std::to_string(T.up_col[e]) + "], " + acc + ")";
       if (strict)
-        o << "  " << b << "[" << si << "] = (" << acc.str() << ") / WV(" << T.lu_diag[i] << ");\n";
+        o << "  " << b << "[" << si << "] = (" << acc << ") / WV(" << T.lu_diag[i] << ");\n";
       else
-        o << "  " << b << "[" << si << "] = (" << acc.str() << ") * pv[" << i << "];\n";
+        o << "  " << b << "[" << si << "] = (" << acc << ") * pv[" << i << "];\n";
     }
   }
 };
@@ -267,52 +270,82 @@ std::string generate(const MechTables& T, double ros_d, double ros_c32, bool str
   o << "#define OFF_DONE " << offsetof(Ctl, done) << "\n#define OFF_CUR " << offsetof(Ctl, cur)
     << "\n#define OFF_DTC " << offsetof(Ctl, dtc) << "\n#define OFF_DTO2 "
     << offsetof(Ctl, dto2) << "\n#define OFF_DTO6 " << offsetof(Ctl, dto6)
-    << "\n#define OFF_DTG " << offsetof(Ctl, dtgamma) << "\n";
+    << "\n#define OFF_DTG " << offsetof(Ctl, dtgamma) << "\n#define OFF_ITERS "
+    << offsetof(Ctl, iters) << "\n";
   o << kPrelude;
-  o << (strict ? "#define RS_QUOT(a, b) ((a) / (b))\n" : "#define RS_QUOT(a, b) ((a) * rcp_nr(b))\n");
-  // one ROS23 attempt of one cell: xn (unclamped) and the cell's sum of squared scaled errors
+  // Every multiply-add is written out: RS_FMA fuses in the production build and keeps the
+  // multiply and the add separate in the strict build; both builds compile with --fmad=false,
+  // so no compiler contraction decides anything and all variants compute the same bits.
+  o << (strict ? "#define RS_QUOT(a, b) ((a) / (b))\n#define RS_FMA(a, b, c) ((a) * (b) + (c))\n"
+               : "#define RS_QUOT(a, b) ((a) * rcp_nr(b))\n#define RS_FMA(a, b, c) fma((a), (b), (c))\n");
+  // One ROS23 attempt of one cell: xn (unclamped) and the cell's sum of squared scaled errors.
+  // f0 = f(x) is computed here unless the caller already holds it (have_f0): after an
+  // accepted attempt whose clamp left the state bit for bit unchanged, f(x_new) is exactly
+  // the third RHS evaluation f2 of that attempt.  fout (global layout, may be null) receives
+  // f2 when the clamp leaves xn unchanged and a NaN marker in plane 0 otherwise; with KEEP
+  // the caller also gets f2 in registers.
   o << R"(
-template <bool HE, int WS>
+template <bool HE, int WS, bool KEEP>
 __device__ __forceinline__ double ros23_cell(const double* __restrict__ kr,
     const double* __restrict__ em, u64 N, int c, const double* x, double* xn, double* W,
+    double* f0, bool have_f0, double* __restrict__ fout, int clamp, double* f2,
     double dt, double dto2, double dto6, double dtg, double rtol, double atol) {
 #define K(r) __ldg(kr + (u64)(r) * N + c)
 #define EM(s) __ldg(em + (u64)(s) * N + c)
 #define WV(e) W[(e) * WS]
-  double v[NRA], P[NPA], f0[NS], k1[NS], f1[NS], k2[NS], b[NS], pv[NS];
+  double v[NRA], P[NPA], k1[NS], f1[NS], k2[NS], b[NS], pv[NS];
+  if (!have_f0) {
 )";
   g.vel("x");
   g.rhs("f0");
+  o << "  }\n";
   g.partials();
   g.build_w();
   g.lu_factor();
   o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) k1[s] = f0[s];\n";
   g.lu_solve("k1");
-  o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) xn[s] = x[s] + dto2 * k1[s];\n";
+  o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) xn[s] = RS_FMA(dto2, k1[s], x[s]);\n";
   g.vel("xn");
   g.rhs("f1");
   o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) k2[s] = f1[s] - k1[s];\n";
   g.lu_solve("k2");
   o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) k2[s] = k2[s] + k1[s];\n";
-  o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) xn[s] = x[s] + dt * k2[s];\n";
+  o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) xn[s] = RS_FMA(dt, k2[s], x[s]);\n";
   g.vel("xn");
   g.rhs("b");
-  o << R"(#pragma unroll
+  o << R"(  if (fout) {
+    bool same = true;
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+      const double cl = clamp ? fmax(xn[s], 0.0) : xn[s];
+      same = same && (__double_as_longlong(cl) == __double_as_longlong(xn[s]));
+    }
+    if (same) {
+#pragma unroll
+      for (int s = 0; s < NS; ++s) fout[(u64)s * N + c] = b[s];
+    } else {
+      fout[c] = __longlong_as_double(0x7ff8000000000000LL);
+    }
+  }
+  if constexpr (KEEP) {
+#pragma unroll
+    for (int s = 0; s < NS; ++s) f2[s] = b[s];
+  }
+#pragma unroll
   for (int s = 0; s < NS; ++s) {
-    const double a = ROS_C32 * (k2[s] - f1[s]);
     const double cc = 2.0 * (k1[s] - f0[s]);
-    b[s] = (b[s] - a) - cc;
+    b[s] = RS_FMA(-ROS_C32, (k2[s] - f1[s]), b[s]) - cc;
   }
 )";
   g.lu_solve("b");
   o << R"(  double acc = 0.0;
 #pragma unroll
   for (int s = 0; s < NS; ++s) {
-    const double ut = dto6 * ((k1[s] - 2.0 * k2[s]) + b[s]);
+    const double ut = dto6 * (RS_FMA(-2.0, k2[s], k1[s]) + b[s]);
     const double am = fmax(fabs(x[s]), fabs(xn[s]));
-    const double den = am * rtol + atol;
+    const double den = RS_FMA(am, rtol, atol);
     const double at = RS_QUOT(ut, den);
-    acc = acc + at * at;
+    acc = RS_FMA(at, at, acc);
   }
   return acc;
 #undef K
@@ -320,12 +353,15 @@ __device__ __forceinline__ double ros23_cell(const double* __restrict__ kr,
 #undef WV
 }
 
-// global-dt attempt: every cell steps with the controller's dtc; 256-cell block partials
+// global-dt attempt: every cell steps with the controller's dtc; 256-cell block partials.
+// F0/F1 (may be null) pair with U0/U1: F[cur] holds f(U[cur]) per cell (NaN in plane 0 where
+// unknown); from the second attempt of a solve on, a cell reuses it instead of evaluating
+// f(x) again (the first attempt of a solve starts from a state written elsewhere).
 template <bool HE, bool SMEM>
 __device__ __forceinline__ void attempt_body(const unsigned char* __restrict__ ctl,
     double* __restrict__ U0, double* __restrict__ U1, const double* __restrict__ kr,
     const double* __restrict__ em, double* __restrict__ partial, int nc, int nsp,
-    double rtol, double atol, int clamp) {
+    double rtol, double atol, int clamp, double* __restrict__ F0, double* __restrict__ F1) {
   __shared__ double red[256];
   if (*(const int*)(ctl + OFF_DONE)) return;
   const double dt = *(const double*)(ctl + OFF_DTC);
@@ -333,22 +369,37 @@ __device__ __forceinline__ void attempt_body(const unsigned char* __restrict__ c
   const double dto6 = *(const double*)(ctl + OFF_DTO6);
   const double dtg = *(const double*)(ctl + OFF_DTG);
   const int cur = *(const int*)(ctl + OFF_CUR);
+  const double iters = *(const double*)(ctl + OFF_ITERS);
   const double* __restrict__ U = cur ? U1 : U0;
   double* __restrict__ Un = cur ? U0 : U1;
+  double* __restrict__ Fin = cur ? F1 : F0;
+  double* __restrict__ Fout = cur ? F0 : F1;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   const u64 N = (u64)nc;
   double e = 0.0;
   if (c < nc) {
-    double x[NS], xn[NS];
+    double x[NS], xn[NS], f0[NS];
 #pragma unroll
     for (int s = 0; s < NS; ++s) x[s] = U[(u64)s * N + c];
+    bool have = false;
+    if (F0 && iters > 0.0) {
+#pragma unroll
+      for (int s = 0; s < NS; ++s) f0[s] = Fin[(u64)s * N + c];
+      have = f0[0] == f0[0];
+    }
     if constexpr (SMEM) {
       extern __shared__ double wsm[];
-      e = ros23_cell<HE, 256>(kr, em, N, c, x, xn, wsm + threadIdx.x, dt, dto2, dto6, dtg,
-                              rtol, atol);
+      e = ros23_cell<HE, 256, false>(kr, em, N, c, x, xn, wsm + threadIdx.x, f0, have,
+                                     F0 ? Fout : nullptr, clamp, nullptr, dt, dto2, dto6, dtg,
+                                     rtol, atol);
     } else {
       double W[NLU];
-      e = ros23_cell<HE, 1>(kr, em, N, c, x, xn, W, dt, dto2, dto6, dtg, rtol, atol);
+      e = ros23_cell<HE, 1, false>(kr, em, N, c, x, xn, W, f0, have, F0 ? Fout : nullptr,
+                                   clamp, nullptr, dt, dto2, dto6, dtg, rtol, atol);
+    }
+    if (F0 && !have) {  // keep f(x) for a retry of this state after a rejection
+#pragma unroll
+      for (int s = 0; s < NS; ++s) Fin[(u64)s * N + c] = f0[s];
     }
 #pragma unroll
     for (int s = 0; s < NS; ++s) Un[(u64)s * N + c] = clamp ? fmax(xn[s], 0.0) : xn[s];
@@ -368,7 +419,8 @@ __device__ __forceinline__ void per_cell_body(int nc, int nsp, double* __restric
     const double* __restrict__ kr, const double* __restrict__ em,
     double* __restrict__ dt_cell, double* __restrict__ steps_cell,
     unsigned long long* __restrict__ queue, int* __restrict__ status, PCA a) {
-  double x[NS], xn[NS], W[NLU];
+  double x[NS], xn[NS], W[NLU], f0[NS], f2[NS];
+  bool have = false;  // f0 == f(x) for the current cell
   double my_steps = 0.0, my_attempts = 0.0;
   double t = 0, dt = 0, qold = 0, iters = 0, nacc = 0;
   int c = -1;
@@ -381,6 +433,7 @@ __device__ __forceinline__ void per_cell_body(int nc, int nsp, double* __restric
       c = (int)nxt;
 #pragma unroll
       for (int s = 0; s < NS; ++s) x[s] = U[(u64)s * N + c];
+      have = false;
       t = a.t0;
       dt = dt_cell[c] > 0.0 ? dt_cell[c] : a.dt0;
       qold = a.qoldinit;
@@ -389,16 +442,28 @@ __device__ __forceinline__ void per_cell_body(int nc, int nsp, double* __restric
     }
     if ((t < tlim) && (iters < a.maxiters)) {
       const double dtc = fmin(dt, a.t1 - t);
-      const double sse = ros23_cell<HE, 1>(kr, em, N, c, x, xn, W, dtc, dtc / 2, dtc / 6,
-                                           dtc * ROS_D, a.rtol, a.atol);
+      const double sse = ros23_cell<HE, 1, true>(kr, em, N, c, x, xn, W, f0, have, nullptr,
+                                                 a.clamp, f2, dtc, dtc / 2, dtc / 6,
+                                                 dtc * ROS_D, a.rtol, a.atol);
+      have = true;  // f0 == f(x) after the call; replaced below if x moves
       double EEst = sqrt(sse / (double)nsp);
       if (EEst != EEst) EEst = 1.0e10;
       const double q11 = pow(fmax(EEst, 1.0e-35), a.beta1);
       double q = q11 / pow(qold, a.beta2);
       q = fmax(a.invqmax, fmin(a.invqmin, q / a.gamma));
       if (EEst <= 1.0) {
+        bool same = true;
 #pragma unroll
-        for (int s = 0; s < NS; ++s) x[s] = a.clamp ? fmax(xn[s], 0.0) : xn[s];
+        for (int s = 0; s < NS; ++s) {
+          const double xs = a.clamp ? fmax(xn[s], 0.0) : xn[s];
+          same = same && (__double_as_longlong(xs) == __double_as_longlong(xn[s]));
+          x[s] = xs;
+        }
+        if (same) {
+#pragma unroll
+          for (int s = 0; s < NS; ++s) f0[s] = f2[s];
+        }
+        have = same;
         t = t + dtc;
         const bool insteady = (a.qsmin <= q) && (q <= a.qsmax);
         dt = dtc / (insteady ? 1.0 : q);
@@ -430,8 +495,10 @@ __device__ __forceinline__ void per_cell_body(int nc, int nsp, double* __restric
       const unsigned char* __restrict__ ctl, double* __restrict__ U0,                       \
       double* __restrict__ U1, const double* __restrict__ kr,                               \
       const double* __restrict__ em, double* __restrict__ partial, int nc, int nsp,         \
-      double rtol, double atol, int clamp) {                                                \
-    attempt_body<HE, SMEM>(ctl, U0, U1, kr, em, partial, nc, nsp, rtol, atol, clamp);       \
+      double rtol, double atol, int clamp, double* __restrict__ F0,                         \
+      double* __restrict__ F1) {                                                            \
+    attempt_body<HE, SMEM>(ctl, U0, U1, kr, em, partial, nc, nsp, rtol, atol, clamp, F0,    \
+                           F1);                                                             \
   }
 RS_ATTEMPT(rs_jit_attempt_r0, false, false, 1)
 RS_ATTEMPT(rs_jit_attempt_r1, true, false, 1)
@@ -486,8 +553,8 @@ bool jit_compile(const std::string& src, bool strict, bool verbose, std::vector<
     *log = std::string("nvrtcCreateProgram: ") + N.err(r);
     return false;
   }
-  std::vector<const char*> opts = {"-arch=sm_103a", "-std=c++17",
-                                   strict ? "--fmad=false" : "--fmad=true"};
+  (void)strict;  // the source itself differs between the builds (RS_FMA, RS_QUOT)
+  std::vector<const char*> opts = {"-arch=sm_103a", "-std=c++17", "--fmad=false"};
   if (verbose) opts.push_back("--ptxas-options=-v");
   r = N.compile(prog, (int)opts.size(), opts.data());
   size_t n = 0;
@@ -608,12 +675,14 @@ std::shared_ptr<JitChem> jit_chem_build(const MechTables& T, double ros_d, doubl
 
 void jit_launch_attempt(const JitChem& J, cudaStream_t st, int nc, int nsp, const Ctl* ctl,
                         double* U0, double* U1, const double* kr, const double* em,
-                        double* part, double rtol, double atol, int clamp) {
+                        double* part, double rtol, double atol, int clamp, double* F0,
+                        double* F1) {
   const int v = J.attempt[J.variant][0] ? J.variant : 0;
   const int sm = v == 1;
   cudaKernel_t k = J.attempt[v][em ? 1 : 0];
   const unsigned char* c = reinterpret_cast<const unsigned char*>(ctl);
-  void* args[] = {&c, &U0, &U1, &kr, &em, &part, &nc, &nsp, &rtol, &atol, &clamp};
+  if (!F0 || !F1) F0 = F1 = nullptr;
+  void* args[] = {&c, &U0, &U1, &kr, &em, &part, &nc, &nsp, &rtol, &atol, &clamp, &F0, &F1};
   int nb = (nc + kBlock - 1) / kBlock;
   cudaLaunchKernel((const void*)k, dim3(nb), dim3(kBlock), args, sm ? J.attempt_smem : 0, st);
 }

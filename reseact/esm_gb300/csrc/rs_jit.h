@@ -58,7 +58,8 @@ bool jit_compile(const std::string& src, bool strict, bool verbose, std::vector<
 // Same contracts as launch_ros23_attempt / launch_chem_per_cell in rs_kernels.h.
 void jit_launch_attempt(const JitChem& J, cudaStream_t st, int nc, int nsp, const Ctl* ctl,
                         double* U0, double* U1, const double* kr, const double* em,
-                        double* part, double rtol, double atol, int clamp);
+                        double* part, double rtol, double atol, int clamp, double* F0,
+                        double* F1);
 void jit_launch_rcp(const JitChem& J, cudaStream_t st, const double* x, double* r, int n);
 void jit_launch_per_cell(const JitChem& J, cudaStream_t st, int nc, int nsp, int nblocks,
                          int threads, double* U, const double* kr, const double* em,

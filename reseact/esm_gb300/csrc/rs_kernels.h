@@ -73,9 +73,11 @@ struct DevTransport {
 
 // chemistry (rs_chem.cu)
 void launch_rates(const LaunchCtx& L, const double* T, const double* P, double* kr);
+// F0/F1 (optional, the specialised kernels only): per-cell f(U0)/f(U1) planes [ns][nc] that
+// let an attempt reuse the previous accepted attempt's last RHS evaluation.
 void launch_ros23_attempt(const LaunchCtx& L, const Ctl* ctl, double* U0, double* U1,
                           const double* kr, const double* em, double* part, double rtol,
-                          double atol, int clamp);
+                          double atol, int clamp, double* F0 = nullptr, double* F1 = nullptr);
 void launch_chem_rhs(const LaunchCtx& L, const double* U, const double* kr, const double* em,
                      double* dU);
 void launch_block_jac(const LaunchCtx& L, const double* U, const double* kr, const int* srow,

@@ -23,11 +23,12 @@ namespace rs {
 constexpr double kOneSixth = 1.0 / 6.0;
 constexpr int kFluxThreads = 256;
 
+// (the limit 2 min(|d0|, |d1|) equals min(2|d0|, 2|d1|) exactly: scaling by 2 is exact)
 __device__ __forceinline__ double slope_u(double am, double a, double ap) {
   double d0 = a - am, d1 = ap - a;
   if (d1 * d0 > 0.0) {
     double da = 0.5 * (ap - am);
-    double lim = fmin(2.0 * fabs(d0), 2.0 * fabs(d1));
+    double lim = 2.0 * fmin(fabs(d0), fabs(d1));
     return copysign(fmin(fabs(da), lim), da);
   }
   return 0.0;
@@ -36,7 +37,7 @@ __device__ __forceinline__ double slope_n(double am, double a, double ap, double
   double d0 = a - am, d1 = ap - a;
   if (d1 * d0 > 0.0) {
     double da = sA * d1 + sB * d0;
-    double lim = fmin(2.0 * fabs(d0), 2.0 * fabs(d1));
+    double lim = 2.0 * fmin(fabs(d0), fabs(d1));
     return copysign(fmin(fabs(da), lim), da);
   }
   return 0.0;
@@ -364,10 +365,12 @@ __global__ void __launch_bounds__(256) k_flux_x_fused(DevTransport<double> T, St
   double* V = smx;           // V[p+3], p in [-3, n+2]
   double* D = smx + L;       // D[p+3], slopes p in [-2, n+1]
   double* E = smx + 2 * L;   // E[f+3], edge between f-1 and f, f in [-1, n+1]
+  double* Mf = smx + 3 * L;  // Mf[f], the face's air-mass flux g*mx (shared by all tracers)
   const int row = blockIdx.x;  // (k, j)
   const int j = row % T.nlat, k = row / T.nlat;
   const size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
   const size_t rbase = ((size_t)k * T.nlat + j) * n;
+  for (int f = threadIdx.x; f <= n; f += blockDim.x) Mf[f] = g * T.mx[((size_t)k * T.nlat + j) * nf + f];
   for (int s = 0; s < T.ntr; ++s) {
     const double* q = Q + (size_t)s * nc + rbase;
     for (int p = threadIdx.x - 3; p <= n + 2; p += blockDim.x) {
@@ -388,8 +391,8 @@ __global__ void __launch_bounds__(256) k_flux_x_fused(DevTransport<double> T, St
       E[f + 3] = V[f + 2] + 0.5 * (V[f + 3] - V[f + 2]) - (D[f + 3] - D[f + 2]) * kOneSixth;
     __syncthreads();
     for (int f = threadIdx.x; f <= n; f += blockDim.x) {
-      double M = g * T.mx[((size_t)k * T.nlat + j) * nf + f];
-      bool right = M > 0.0;
+      const double M = Mf[f];
+      const bool right = __double_as_longlong(M) > 0;  // M > 0 for every non-NaN M
       int up = right ? f - 1 : f;
       double aL = E[up + 3], aR = E[up + 4];
       limit(V[up + 3], aL, aR);
@@ -410,6 +413,7 @@ __global__ void __launch_bounds__(512) k_flux_y_fused(DevTransport<double> T, St
   double* V = smy;                    // [L][kPencil]
   double* D = smy + L * kPencil;
   double* E = smy + 2 * L * kPencil;
+  double* Mf = smy + 3 * L * kPencil;  // [n+1][kPencil] face air-mass fluxes g*my
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int ntile = (T.nlon + kPencil - 1) / kPencil;
   const int k = blockIdx.x / ntile;
@@ -418,6 +422,9 @@ __global__ void __launch_bounds__(512) k_flux_y_fused(DevTransport<double> T, St
   const size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
   const size_t fplane = (size_t)T.nlev * nfj * T.nlon;
   const bool open = T.lat_bc == 1;
+  if (live)
+    for (int f = ty; f <= n; f += blockDim.y)
+      Mf[f * kPencil + tx] = g * T.my[((size_t)k * nfj + f) * T.nlon + i];
   for (int s = 0; s < T.ntr; ++s) {
     const double* q = Q + (size_t)s * nc + (size_t)k * T.nlat * T.nlon;
     for (int p = (int)ty - 3; p <= n + 2; p += blockDim.y) {
@@ -450,8 +457,8 @@ __global__ void __launch_bounds__(512) k_flux_y_fused(DevTransport<double> T, St
           T.fy[(size_t)s * fplane + fb] = 0.0;
           continue;
         }
-        double M = g * T.my[fb];
-        bool right = M > 0.0;
+        const double M = Mf[f * kPencil + tx];
+        const bool right = __double_as_longlong(M) > 0;
         int up = right ? f - 1 : f;
         double aL = E[(up + 3) * kPencil + tx], aR = E[(up + 4) * kPencil + tx];
         limit(V[(up + 3) * kPencil + tx], aL, aR);
@@ -473,12 +480,15 @@ __global__ void __launch_bounds__(512) k_flux_z_fused(DevTransport<double> T, St
   double* V = smz;
   double* D = smz + L * kPencil;
   double* E = smz + 2 * L * kPencil;
+  double* Mf = smz + 3 * L * kPencil;  // [n+1][kPencil] face air-mass fluxes g*mz
   const int tx = threadIdx.x, ty = threadIdx.y;
   const size_t ncol = (size_t)T.nlon * T.nlat;
   const size_t col = (size_t)blockIdx.x * kPencil + tx;
   const bool live = col < ncol;
   const size_t nc = ncol * n;
   const size_t fplane = ncol * (n + 1);
+  if (live)
+    for (int kf = ty; kf <= n; kf += blockDim.y) Mf[kf * kPencil + tx] = g * T.mz[(size_t)kf * ncol + col];
   for (int s = 0; s < T.ntr; ++s) {
     const double* q = Q + (size_t)s * nc;
     for (int p = (int)ty - 3; p <= n + 2; p += blockDim.y) {
@@ -508,8 +518,8 @@ __global__ void __launch_bounds__(512) k_flux_z_fused(DevTransport<double> T, St
           T.fz[(size_t)s * fplane + (size_t)kf * ncol + col] = 0.0;
           continue;
         }
-        double M = g * T.mz[(size_t)kf * ncol + col];
-        bool right = M > 0.0;
+        const double M = Mf[kf * kPencil + tx];
+        const bool right = __double_as_longlong(M) > 0;
         int up = right ? kf - 1 : kf;
         double aL = E[(up + 3) * kPencil + tx], aR = E[(up + 4) * kPencil + tx];
         limit(V[(up + 3) * kPencil + tx], aL, aR);
@@ -700,16 +710,76 @@ __global__ void __launch_bounds__(kRedThreads) k_rhs_eval(DevTransport<double> T
 }
 
 // allow > 48 KB of dynamic shared memory for long pencils (once per process)
+constexpr int kPencilSmemCap = 200 * 1024;
 static void allow_big_smem() {
   static bool done = false;
   if (done) return;
-  const int cap = 200 * 1024;
+  const int cap = kPencilSmemCap;
   cudaFuncSetAttribute(k_flux_x_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
   cudaFuncSetAttribute(k_flux_y_fused<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
   cudaFuncSetAttribute(k_flux_y_fused<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
   cudaFuncSetAttribute(k_flux_z_fused<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
   cudaFuncSetAttribute(k_flux_z_fused<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
   done = true;
+}
+
+// Launch shape of the fused pencil kernels: V, D, E rows (n+6 each) plus the n+1 face fluxes,
+// per pencil.  The tuned pencil width drops to 16 where 32 does not fit; a direction whose
+// pencils do not fit even at 16 uses the per-face FP64 kernel (the same fluxes, bit for bit).
+struct FluxShape {
+  int pw, rows, xt;
+  size_t shx, shy, shz;
+  bool fx, fy, fz;  // fused kernel used for x / y / z
+};
+static size_t pencil_bytes(int n, int pw) { return (size_t)(3 * (n + 6) + (n + 1)) * pw * sizeof(double); }
+static FluxShape flux_shape(const DevTransport<double>& T) {
+  FluxShape f;
+  f.pw = T.pencil == 16 ? 16 : 32;
+  if (pencil_bytes(T.nlat, f.pw) > (size_t)kPencilSmemCap ||
+      pencil_bytes(T.nlev, f.pw) > (size_t)kPencilSmemCap)
+    f.pw = 16;
+  f.rows = (T.rows == 4 || T.rows == 16) ? T.rows : 8;
+  f.xt = (T.xthreads == 64 || T.xthreads == 256) ? T.xthreads : 128;
+  f.shx = pencil_bytes(T.nlon, 1);
+  f.shy = pencil_bytes(T.nlat, f.pw);
+  f.shz = pencil_bytes(T.nlev, f.pw);
+  f.fx = f.shx <= (size_t)kPencilSmemCap;
+  f.fy = f.shy <= (size_t)kPencilSmemCap;
+  f.fz = f.shz <= (size_t)kPencilSmemCap;
+  return f;
+}
+
+static void launch_flux_one(cudaStream_t st, const DevTransport<double>& T, const StageSel& sel,
+                            const FluxShape& f, int dir) {
+  size_t ncol = (size_t)T.nlon * T.nlat;
+  if (dir == 0) {
+    if (f.fx) {
+      k_flux_x_fused<<<(unsigned)(T.nlat * T.nlev), f.xt, f.shx, st>>>(T, sel);
+    } else {
+      long long nx = (long long)(T.nlon + 1) * T.nlat * T.nlev;
+      k_flux_x<<<(unsigned)((nx + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);
+    }
+  } else if (dir == 1) {
+    if (f.fy) {
+      unsigned ntile = (unsigned)((T.nlon + f.pw - 1) / f.pw);
+      if (f.pw == 16)
+        k_flux_y_fused<16><<<ntile * (unsigned)T.nlev, dim3(16, f.rows), f.shy, st>>>(T, sel);
+      else
+        k_flux_y_fused<32><<<ntile * (unsigned)T.nlev, dim3(32, f.rows), f.shy, st>>>(T, sel);
+    } else {
+      long long ny = (long long)T.nlon * (T.nlat + 1) * T.nlev;
+      k_flux_y<<<(unsigned)((ny + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);
+    }
+  } else {
+    if (f.fz) {
+      unsigned nzb = (unsigned)((ncol + f.pw - 1) / f.pw);
+      if (f.pw == 16) k_flux_z_fused<16><<<nzb, dim3(16, f.rows), f.shz, st>>>(T, sel);
+      else k_flux_z_fused<32><<<nzb, dim3(32, f.rows), f.shz, st>>>(T, sel);
+    } else {
+      long long nz = (long long)T.nlon * T.nlat * (T.nlev + 1);
+      k_flux_z<<<(unsigned)((nz + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);
+    }
+  }
 }
 
 static void launch_fluxes(cudaStream_t st, const DevTransport<double>& T, const StageSel& sel) {
@@ -722,24 +792,9 @@ static void launch_fluxes(cudaStream_t st, const DevTransport<double>& T, const 
     k_flux_z<<<(unsigned)((nz + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);
     return;
   }
-  size_t shx = 3 * (size_t)(T.nlon + 6) * sizeof(double);
   allow_big_smem();
-  const int pw = T.pencil == 16 ? 16 : 32;
-  const int rows = (T.rows == 4 || T.rows == 16) ? T.rows : 8;
-  const int xt = (T.xthreads == 64 || T.xthreads == 256) ? T.xthreads : 128;
-  size_t shy = 3 * (size_t)(T.nlat + 6) * pw * sizeof(double);
-  size_t shz = 3 * (size_t)(T.nlev + 6) * pw * sizeof(double);
-  unsigned ntile = (unsigned)((T.nlon + pw - 1) / pw);
-  size_t ncol = (size_t)T.nlon * T.nlat;
-  unsigned nzb = (unsigned)((ncol + pw - 1) / pw);
-  k_flux_x_fused<<<(unsigned)(T.nlat * T.nlev), xt, shx, st>>>(T, sel);
-  if (pw == 16) {
-    k_flux_y_fused<16><<<ntile * (unsigned)T.nlev, dim3(16, rows), shy, st>>>(T, sel);
-    k_flux_z_fused<16><<<nzb, dim3(16, rows), shz, st>>>(T, sel);
-  } else {
-    k_flux_y_fused<32><<<ntile * (unsigned)T.nlev, dim3(32, rows), shy, st>>>(T, sel);
-    k_flux_z_fused<32><<<nzb, dim3(32, rows), shz, st>>>(T, sel);
-  }
+  const FluxShape f = flux_shape(T);
+  for (int dir = 0; dir < 3; ++dir) launch_flux_one(st, T, sel, f, dir);
 }
 
 // one direction of the flux computation on a given field (used by the autotuner)
@@ -748,24 +803,7 @@ void launch_flux_dir(cudaStream_t st, const DevTransport<double>& T, const doubl
   DevTransport<double> T1 = T;
   T1.mixed = 0;
   allow_big_smem();
-  const int pw = T.pencil == 16 ? 16 : 32;
-  const int rows = (T.rows == 4 || T.rows == 16) ? T.rows : 8;
-  const int xt = (T.xthreads == 64 || T.xthreads == 256) ? T.xthreads : 128;
-  size_t ncol = (size_t)T.nlon * T.nlat;
-  if (dir == 0) {
-    size_t shx = 3 * (size_t)(T.nlon + 6) * sizeof(double);
-    k_flux_x_fused<<<(unsigned)(T.nlat * T.nlev), xt, shx, st>>>(T1, sel);
-  } else if (dir == 1) {
-    size_t shy = 3 * (size_t)(T.nlat + 6) * pw * sizeof(double);
-    unsigned ntile = (unsigned)((T.nlon + pw - 1) / pw);
-    if (pw == 16) k_flux_y_fused<16><<<ntile * (unsigned)T.nlev, dim3(16, rows), shy, st>>>(T1, sel);
-    else k_flux_y_fused<32><<<ntile * (unsigned)T.nlev, dim3(32, rows), shy, st>>>(T1, sel);
-  } else {
-    size_t shz = 3 * (size_t)(T.nlev + 6) * pw * sizeof(double);
-    unsigned nzb = (unsigned)((ncol + pw - 1) / pw);
-    if (pw == 16) k_flux_z_fused<16><<<nzb, dim3(16, rows), shz, st>>>(T1, sel);
-    else k_flux_z_fused<32><<<nzb, dim3(32, rows), shz, st>>>(T1, sel);
-  }
+  launch_flux_one(st, T1, sel, flux_shape(T1), dir);
 }
 
 void launch_ssprk43_attempt(cudaStream_t st, const DevTransport<double>& T, const Ctl* ctl,
