@@ -152,6 +152,19 @@ typedef struct rs_forcing {
   const double* temperature; /* [nlev][nlat][nlon] K */
   const double* pressure;    /* [nlev][nlat][nlon] Pa */
   const double* emission;    /* [n_species][nlev][nlat][nlon] source added to d(species)/dt */
+  /* GEOS-Chem-style full PBL mixing, a transport-half term (reseact.esm Transport3D equations
+   * p_pbl_top, pbl_f, pbl_wt, pbl_sum_*, pbl_mean_*; tracer tendency
+   * pbl_f*(pbl_mean - q)/tau_pblmix).  p_pbl_top = PS*exp(-PBLH*g/(Rd*T_surface)) with
+   * g = 9.80665, Rd = 287.05 and T_surface the temperature of level 0; pbl_f is the clamped
+   * overlap of each layer's pressure interval with [p_pbl_top, PS] over dp; the mean is
+   * sum_k (dp*pbl_f)_k q_k / max(sum_k (dp*pbl_f)_k, 1 Pa).  Active once pblh, ps, hyb_a,
+   * hyb_b and the temperature have been given and tau_pblmix > 0; tau_pblmix is taken from a
+   * call that passes pblh.  Exactly mass-conserving: sum_k dp_k * tendency_k = 0. */
+  const double* pblh;        /* [nlat][nlon] PBL height (m) */
+  const double* ps;          /* [nlat][nlon] surface pressure (Pa) */
+  const double* hyb_a;       /* [nlev+1] interface pressure coefficient A (Pa), 0 = surface */
+  const double* hyb_b;       /* [nlev+1] interface coefficient B: p_k = A_k + B_k * PS */
+  double tau_pblmix;         /* relaxation time (s); the reference's default is 900 */
 } rs_forcing;
 
 /* Per-macro-step statistics (op_split.jl:159-163 return tuple plus the carried dts). */

@@ -47,6 +47,8 @@ struct RsForcing
     dp::Ptr{Float64}; qbc_w::Ptr{Float64}; qbc_e::Ptr{Float64}; qbc_s::Ptr{Float64}
     qbc_n::Ptr{Float64}; temperature::Ptr{Float64}; pressure::Ptr{Float64}
     emission::Ptr{Float64}
+    pblh::Ptr{Float64}; ps::Ptr{Float64}; hyb_a::Ptr{Float64}; hyb_b::Ptr{Float64}
+    tau_pblmix::Float64
 end
 
 mutable struct RsStats

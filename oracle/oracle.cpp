@@ -285,6 +285,11 @@ Grid make_grid(const rs_grid* g) {
 struct Forcing {
   std::vector<double> mx, my, mz, dp, qw, qe, qs, qn, T, P, emis;
   double omega = 0.0;
+  // full PBL mixing (reseact.esm Transport3D p_pbl_top, pbl_f, pbl_wt, pbl_mean_*): inputs,
+  // and per layer the fraction f and weight w = dp f, per column den = max(sum w, 1 Pa)
+  std::vector<double> pblh, ps, hyb_a, hyb_b, pbl_f, pbl_w, pbl_den;
+  double tau_pbl = 0.0;
+  bool pbl = false;
   // vertical PPM coefficients per column: slope (sA,sB) for cells -1..nlev, edge (eAB,eC,eD)
   // for edges 0..nlev (edge e lies between cells e-1 and e)
   std::vector<double> vs, ve;
@@ -484,6 +489,34 @@ inline double qz(const Model& md, const double* q, int i, int j, int k) {
 }
 
 // face fluxes of tracer s at cell (i,j,k): west/east, south/north, bottom/top
+// PBL fraction and weights of every layer, as the reseact.esm Transport3D equations define them:
+// p_top = PS exp(-(PBLH g)/(Rd T_surface)); f_k = max(0, min(1, (min(PS, p_k) - max(p_top,
+// p_k+1))/dp_k)) with interface p_k = A_k + B_k PS (k = 0 at the surface); den = max(sum w, 1).
+void build_pbl(const Grid& G, Forcing& F) {
+  size_t ncol = (size_t)G.nlon * G.nlat;
+  F.pbl = F.tau_pbl > 0.0 && F.pblh.size() == ncol && F.ps.size() == ncol && !F.T.empty() &&
+          F.hyb_a.size() == (size_t)G.nlev + 1 && F.hyb_b.size() == (size_t)G.nlev + 1;
+  if (!F.pbl) return;
+  const double g_acc = 9.80665, rd_air = 287.05;
+  F.pbl_f.assign(G.nc, 0.0);
+  F.pbl_w.assign(G.nc, 0.0);
+  F.pbl_den.assign(ncol, 0.0);
+  for (size_t col = 0; col < ncol; ++col) {
+    double PS = F.ps[col];
+    double ptop = PS * std::exp(-1.0 * ((F.pblh[col] * g_acc) / (rd_air * F.T[col])));
+    double wt = 0.0;
+    for (int k = 0; k < G.nlev; ++k) {
+      size_t c = (size_t)k * ncol + col;
+      double lo = F.hyb_a[k] + F.hyb_b[k] * PS, up = F.hyb_a[k + 1] + F.hyb_b[k + 1] * PS;
+      double f = std::max(0.0, std::min(1.0, (std::min(PS, lo) - std::max(ptop, up)) / F.dp[c]));
+      F.pbl_f[c] = f;
+      F.pbl_w[c] = F.dp[c] * f;
+      wt = wt + F.pbl_w[c];
+    }
+    F.pbl_den[col] = std::max(wt, 1.0);
+  }
+}
+
 double xflux(const Model& md, const double* q, int s, int i, int j, int k, double g) {
   const Grid& G = md.G;
   double M = g * md.F.mx[((size_t)k * G.nlat + j) * (G.nlon + 1) + i];
@@ -526,12 +559,26 @@ double zflux(const Model& md, const double* q, int i, int j, int kf, double g) {
 }
 
 // Transport RHS (CWC mixing-ratio form, reseact.esm:2083; continuity reseact.esm:1535).
-void transport_rhs(const Model& md, const double* u, double t, double* du) {
+// with_pbl = false gives the advective tendency alone (the adjoint's air-mass derivative)
+void transport_rhs(const Model& md, const double* u, double t, double* du, bool with_pbl = true) {
   const Grid& G = md.G;
   double g = md.F.omega != 0.0 ? std::cos(md.F.omega * t) : 1.0;
   size_t nc = G.nc;
   int ntr = md.has_m ? md.nsp - 1 : md.nsp;
   const double* m = md.has_m ? u + (size_t)(md.nsp - 1) * nc : nullptr;
+  const bool pbl = with_pbl && md.F.pbl;
+  const size_t ncol0 = (size_t)G.nlon * G.nlat;
+  std::vector<double> qbar;
+  if (pbl) {  // PBL mean of every tracer and column, summed from the surface up
+    qbar.assign((size_t)ntr * ncol0, 0.0);
+    for (int s = 0; s < ntr; ++s)
+      for (size_t col = 0; col < ncol0; ++col) {
+        double acc = 0.0;
+        for (int k = 0; k < G.nlev; ++k)
+          acc = acc + md.F.pbl_w[(size_t)k * ncol0 + col] * u[(size_t)s * nc + (size_t)k * ncol0 + col];
+        qbar[(size_t)s * ncol0 + col] = acc / md.F.pbl_den[col];
+      }
+  }
 #pragma omp parallel for collapse(2) schedule(static)
   for (int k = 0; k < G.nlev; ++k)
     for (int j = 0; j < G.nlat; ++j)
@@ -560,7 +607,10 @@ void transport_rhs(const Model& md, const double* u, double t, double* du) {
           double Dz = ft - fb;
           double a = -((Dx + Dy) + Dz);
           double b = q[c] * divM;
-          du[(size_t)s * nc + c] = m ? (a + b) / m[c] : a + b;
+          double adv = m ? (a + b) / m[c] : a + b;
+          if (pbl)  // full PBL mixing: pbl_f * (pbl_mean - q) / tau_pblmix
+            adv = adv + (md.F.pbl_f[c] * (qbar[(size_t)s * ncol0 + col] - q[c])) / md.F.tau_pbl;
+          du[(size_t)s * nc + c] = adv;
         }
         if (md.has_m) du[(size_t)(md.nsp - 1) * nc + c] = -divM;
       }
@@ -770,8 +820,25 @@ void transport_rhs_vjp(const Model& md, const double* u, double t, const double*
   int ntr = md.nsp - 1;
   const double* m = u + (size_t)ntr * nc;
   std::vector<double> f((size_t)md.nsp * nc);
-  transport_rhs(md, u, t, f.data());
+  transport_rhs(md, u, t, f.data(), false);  // advective part: the air mass enters only there
   std::fill(ubar, ubar + (size_t)md.nsp * nc, 0.0);
+  if (md.F.pbl) {  // PBL mixing: ubar_j += (w_j/den) (sum_k fbar_k f_k)/tau - fbar_j f_j/tau
+    size_t ncol0 = (size_t)G.nlon * G.nlat;
+    for (int s = 0; s < ntr; ++s)
+      for (size_t col = 0; col < ncol0; ++col) {
+        double a = 0.0;
+        for (int k = 0; k < G.nlev; ++k) {
+          size_t x = (size_t)k * ncol0 + col;
+          a = a + fbar[(size_t)s * nc + x] * md.F.pbl_f[x];
+        }
+        double at = a / md.F.tau_pbl, den = md.F.pbl_den[col];
+        for (int k = 0; k < G.nlev; ++k) {
+          size_t x = (size_t)k * ncol0 + col;
+          ubar[(size_t)s * nc + x] += (md.F.pbl_w[x] / den) * at -
+                                      (fbar[(size_t)s * nc + x] * md.F.pbl_f[x]) / md.F.tau_pbl;
+        }
+      }
+  }
   std::vector<double> gq((size_t)ntr * nc);
   size_t ncol = (size_t)G.nlon * G.nlat;
   for (int k = 0; k < G.nlev; ++k)
@@ -1086,6 +1153,15 @@ int or_set_forcing(or_model* h, const rs_forcing* f) {
   if (f->pressure) md.F.P.assign(f->pressure, f->pressure + nc);
   if (f->emission) md.F.emis.assign(f->emission, f->emission + (size_t)ns * nc);
   vertical_coefs(G, md.F);
+  size_t ncol = (size_t)G.nlon * G.nlat;
+  if (f->pblh) {
+    md.F.pblh.assign(f->pblh, f->pblh + ncol);
+    md.F.tau_pbl = f->tau_pblmix;
+  }
+  if (f->ps) md.F.ps.assign(f->ps, f->ps + ncol);
+  if (f->hyb_a) md.F.hyb_a.assign(f->hyb_a, f->hyb_a + G.nlev + 1);
+  if (f->hyb_b) md.F.hyb_b.assign(f->hyb_b, f->hyb_b + G.nlev + 1);
+  if (md.cfg.do_transport) build_pbl(G, md.F);
   if (tp) compute_rates(md);
   return 0;
 }

@@ -60,7 +60,8 @@ class rs_forcing(C.Structure):
     _fields_ = [("mx", _f64p), ("my", _f64p), ("mz", _f64p), ("flux_omega", C.c_double),
                 ("dp", _f64p), ("qbc_w", _f64p), ("qbc_e", _f64p), ("qbc_s", _f64p),
                 ("qbc_n", _f64p), ("temperature", _f64p), ("pressure", _f64p),
-                ("emission", _f64p)]
+                ("emission", _f64p), ("pblh", _f64p), ("ps", _f64p), ("hyb_a", _f64p),
+                ("hyb_b", _f64p), ("tau_pblmix", C.c_double)]
 
 
 class rs_stats(C.Structure):
@@ -129,9 +130,9 @@ class ForcingABI:
     """Keeps forcing arrays alive (contiguous float64) behind an rs_forcing struct."""
 
     NAMES = ("mx", "my", "mz", "dp", "qbc_w", "qbc_e", "qbc_s", "qbc_n", "temperature",
-             "pressure", "emission")
+             "pressure", "emission", "pblh", "ps", "hyb_a", "hyb_b")
 
-    def __init__(self, flux_omega=0.0, **arrays):
+    def __init__(self, flux_omega=0.0, tau_pblmix=0.0, **arrays):
         self.arrays = {k: (None if arrays.get(k) is None else
                            np.ascontiguousarray(arrays[k], dtype=np.float64))
                        for k in self.NAMES}
@@ -143,4 +144,7 @@ class ForcingABI:
                                  _ptr(a["qbc_n"], C.c_double),
                                  _ptr(a["temperature"], C.c_double),
                                  _ptr(a["pressure"], C.c_double),
-                                 _ptr(a["emission"], C.c_double))
+                                 _ptr(a["emission"], C.c_double),
+                                 _ptr(a["pblh"], C.c_double), _ptr(a["ps"], C.c_double),
+                                 _ptr(a["hyb_a"], C.c_double), _ptr(a["hyb_b"], C.c_double),
+                                 float(tau_pblmix))

@@ -453,6 +453,26 @@ __global__ void __launch_bounds__(256) k_adj_gather(DevTransport<double> T, cons
 }
 
 // ubar = (d f_T / du)^T fbar at stage state U (whose RHS value is F), time factor g
+// VJP of the PBL mixing term t_k = f_k (qbar - q_k) / tau with qbar = sum_j w_j q_j / den:
+// ubar_j += (w_j / den) * (sum_k fbar_k f_k) / tau - fbar_j f_j / tau, per tracer and column
+// (the term does not depend on the air mass).
+__global__ void k_pbl_vjp(DevTransport<double> T, const double* __restrict__ fbar,
+                          double* __restrict__ ubar) {
+  const size_t ncol = (size_t)T.nlon * T.nlat, nc = ncol * T.nlev;
+  const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= (size_t)T.ntr * ncol) return;
+  const size_t s = id / ncol, col = id % ncol;
+  const double* fb = fbar + s * nc + col;
+  double* ub = ubar + s * nc + col;
+  double a = 0.0;
+  for (int k = 0; k < T.nlev; ++k) a = a + fb[(size_t)k * ncol] * T.pbl_f[(size_t)k * ncol + col];
+  const double at = a / T.pbl_tau, den = T.pbl_den[col];
+  for (int k = 0; k < T.nlev; ++k) {
+    const size_t x = (size_t)k * ncol + col;
+    ub[(size_t)k * ncol] += (T.pbl_w[x] / den) * at - (fb[(size_t)k * ncol] * T.pbl_f[x]) / T.pbl_tau;
+  }
+}
+
 void launch_transport_rhs_vjp(cudaStream_t st, const DevTransport<double>& T, const double* U,
                               const double* F, const double* fbar, double* ubar, double* G,
                               double* Cf, double g) {
@@ -468,6 +488,10 @@ void launch_transport_rhs_vjp(cudaStream_t st, const DevTransport<double>& T, co
   k_adj_gather<1><<<nb, 256, 0, st>>>(T, U, Cf, ubar, g);
   k_adj_face<2><<<(unsigned)((nz + 255) / 256), 256, 0, st>>>(T, U, G, Cf, g);
   k_adj_gather<2><<<nb, 256, 0, st>>>(T, U, Cf, ubar, g);
+  if (T.pbl) {
+    size_t n = (size_t)T.ntr * T.nlon * T.nlat;
+    k_pbl_vjp<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(T, fbar, ubar);
+  }
 }
 
 // out = a*x + b*y + c*z over n elements (null operands skipped)

@@ -346,6 +346,12 @@ struct rs_handle {
     int pencil = 32, rows = 8, xthreads = 128;        // transport pencil kernels
   } tune;
   // mechanism-specialised chemistry kernels (null: not built) and the kind in use
+  // full PBL mixing: host inputs, and the derived per-layer fraction / weight and column
+  // normaliser on the device (recomputed when an input changes)
+  std::vector<double> pblh_host, ps_host, hyb_a_host, hyb_b_host, tsfc_host;
+  double tau_pbl = 0.0;
+  bool pbl_on = false;
+  DevBuf<double> pbl_f, pbl_w, pbl_den, pbl_qbar;
   std::shared_ptr<rs::JitChem> jit;
   DevBuf<double> fsal[2];  // f(U[b]) planes [ns][nc] for the specialised global-dt attempts
   std::string jit_why;
@@ -541,6 +547,46 @@ void refresh_dt(rs_handle* h) {
   T.pencil = h->tune.pencil;
   T.rows = h->tune.rows;
   T.xthreads = h->tune.xthreads;
+  T.pbl = h->pbl_on;
+  T.pbl_f = h->pbl_f.p; T.pbl_w = h->pbl_w.p; T.pbl_den = h->pbl_den.p; T.pbl_qbar = h->pbl_qbar.p;
+  T.pbl_tau = h->tau_pbl;
+  T.pbl_rtau = h->tau_pbl > 0.0 ? 1.0 / h->tau_pbl : 0.0;
+}
+
+// PBL fraction and weights of every layer (reseact.esm Transport3D p_pbl_top, pbl_f, pbl_wt):
+//   p_top = PS exp(-(PBLH g) / (Rd T_surface)),  p_k = A_k + B_k PS (interface k, 0 = surface)
+//   f_k = max(0, min(1, (min(PS, p_k) - max(p_top, p_k+1)) / dp_k)),  w_k = dp_k f_k,
+//   den = max(sum_k w_k, 1 Pa), summed from the surface up.
+void build_pbl(rs_handle* h) {
+  const rs_grid& g = h->cfg.grid;
+  const size_t ncol = (size_t)g.nlon * g.nlat;
+  h->pbl_on = h->cfg.do_transport && h->tau_pbl > 0.0 && h->pblh_host.size() == ncol &&
+              h->ps_host.size() == ncol && h->tsfc_host.size() == ncol &&
+              h->hyb_a_host.size() == (size_t)g.nlev + 1 && h->hyb_b_host.size() == (size_t)g.nlev + 1;
+  if (!h->pbl_on) return;
+  const double g_acc = 9.80665, rd_air = 287.05;
+  std::vector<double> F(h->nc), W(h->nc), D(ncol);
+  const double* dp = h->dp_host.data();
+  const double* A = h->hyb_a_host.data();
+  const double* B = h->hyb_b_host.data();
+  for (size_t col = 0; col < ncol; ++col) {
+    const double PS = h->ps_host[col];
+    const double ptop = PS * std::exp(-1.0 * ((h->pblh_host[col] * g_acc) / (rd_air * h->tsfc_host[col])));
+    double wt = 0.0;
+    for (int k = 0; k < g.nlev; ++k) {
+      const size_t c = (size_t)k * ncol + col;
+      const double lo = A[k] + B[k] * PS, up = A[k + 1] + B[k + 1] * PS;
+      const double f = std::max(0.0, std::min(1.0, (std::min(PS, lo) - std::max(ptop, up)) / dp[c]));
+      F[c] = f;
+      W[c] = dp[c] * f;
+      wt = wt + W[c];
+    }
+    D[col] = std::max(wt, 1.0);
+  }
+  h->pbl_f.upload(F.data(), F.size(), h->st);
+  h->pbl_w.upload(W.data(), W.size(), h->st);
+  h->pbl_den.upload(D.data(), D.size(), h->st);
+  h->pbl_qbar.alloc((size_t)h->ntr * ncol);
 }
 
 Ctl make_ctl(rs_handle* h, double t0, double t1, double dt0, const rs_controller& c,
@@ -832,7 +878,8 @@ void rs_destroy(rs_handle* h) {
                             &h->partial, &h->krates, &h->T, &h->P, &h->emis, &h->io, &h->io2,
                             &h->mx, &h->my, &h->mz, &h->qw, &h->qe, &h->qs, &h->qn, &h->gx,
                             &h->gylo, &h->gyhi, &h->vsA, &h->vsB, &h->veAB, &h->veC, &h->veD,
-                            &h->dtcell, &h->stepcell, &h->totals, &h->fsal[0], &h->fsal[1]};
+                            &h->dtcell, &h->stepcell, &h->totals, &h->fsal[0], &h->fsal[1],
+                            &h->pbl_f, &h->pbl_w, &h->pbl_den, &h->pbl_qbar};
   for (auto* b : bufs) b->release();
   h->slot_row.release();
   h->slot_col.release();
@@ -916,6 +963,24 @@ rs_status rs_set_forcing(rs_handle* h, const rs_forcing* f) {
         build_vertical(h);
       }
       if (f->mx || f->my || f->mz) h->omega = f->flux_omega;
+      const size_t ncol = (size_t)g.nlon * g.nlat;
+      bool pbl_inputs = f->dp != nullptr || f->temperature != nullptr;
+      if (f->pblh) {
+        if (!(f->tau_pblmix >= 0.0)) throw RsError(RS_ERR_INVALID, "tau_pblmix must be >= 0");
+        h->pblh_host.assign(f->pblh, f->pblh + ncol);
+        h->tau_pbl = f->tau_pblmix;
+        pbl_inputs = true;
+      }
+      if (f->ps) {
+        for (size_t c = 0; c < ncol; ++c)
+          if (!(f->ps[c] > 0.0)) throw RsError(RS_ERR_INVALID, "ps must be positive");
+        h->ps_host.assign(f->ps, f->ps + ncol);
+        pbl_inputs = true;
+      }
+      if (f->hyb_a) { h->hyb_a_host.assign(f->hyb_a, f->hyb_a + g.nlev + 1); pbl_inputs = true; }
+      if (f->hyb_b) { h->hyb_b_host.assign(f->hyb_b, f->hyb_b + g.nlev + 1); pbl_inputs = true; }
+      if (f->temperature) h->tsfc_host.assign(f->temperature, f->temperature + ncol);
+      if (pbl_inputs) build_pbl(h);
     }
     if (f->temperature) {
       h->T.upload(f->temperature, nc, st);
@@ -1256,35 +1321,40 @@ void transport_step_vjp(rs_handle* h, const double* u, double t, double dt, cons
   double* A = h->adj.p + 7 * n;
   double* B = h->adj.p + 8 * n;
   double* Wb = h->adj.p + 9 * n;
+  // the air-mass derivative of the VJP takes the advective tendency alone (PBL mixing does not
+  // depend on the air mass): with PBL mixing it is kept in four more slabs
+  double* Fa[4] = {F0, F1, F2, F3};
+  if (h->pbl_on)
+    for (int q = 0; q < 4; ++q) Fa[q] = h->adj.p + (11 + q) * n;
   rs::DevTransport<double> T = h->dt;
   T.mixed = 0;  // the adjoint differentiates the FP64 scheme
   auto gf = [&](double tt) { return h->omega != 0.0 ? std::cos(h->omega * tt) : 1.0; };
   double h2 = dt / 2;
   cudaStream_t st = h->st;
-  rs::launch_transport_rhs(st, T, u, gf(t), F0);
+  rs::launch_transport_rhs(st, T, u, gf(t), F0, h->pbl_on ? Fa[0] : nullptr);
   rs::launch_lincomb(st, n, V1, 1.0, u, h2, F0, 0.0, nullptr);
-  rs::launch_transport_rhs(st, T, V1, gf(t + 0.5 * dt), F1);
+  rs::launch_transport_rhs(st, T, V1, gf(t + 0.5 * dt), F1, h->pbl_on ? Fa[1] : nullptr);
   rs::launch_lincomb(st, n, V2, 1.0, V1, h2, F1, 0.0, nullptr);
-  rs::launch_transport_rhs(st, T, V2, gf(t + 1.0 * dt), F2);
+  rs::launch_transport_rhs(st, T, V2, gf(t + 1.0 * dt), F2, h->pbl_on ? Fa[2] : nullptr);
   rs::launch_lincomb(st, n, V4, 1.0, V2, h2, F2, 0.0, nullptr);        // u3
   rs::launch_lincomb(st, n, V4, 2.0 / 3.0, u, 1.0 / 3.0, V4, 0.0, nullptr);  // u4
-  rs::launch_transport_rhs(st, T, V4, gf(t + h2), F3);
+  rs::launch_transport_rhs(st, T, V4, gf(t + h2), F3, h->pbl_on ? Fa[3] : nullptr);
   auto vjp = [&](const double* Us, const double* Fs, double g, const double* fbar, double* ub) {
     rs::launch_transport_rhs_vjp(st, T, Us, Fs, fbar, ub, h->G.p, h->Cf.p, g);
   };
   rs::launch_lincomb(st, n, Wb, h2, lam, 0.0, nullptr, 0.0, nullptr);
-  vjp(V4, F3, gf(t + h2), Wb, A);
+  vjp(V4, Fa[3], gf(t + h2), Wb, A);
   rs::launch_lincomb(st, n, A, 1.0, A, 1.0, lam, 0.0, nullptr);           // ubar4
   rs::launch_lincomb(st, n, out, 2.0 / 3.0, A, 0.0, nullptr, 0.0, nullptr);
   rs::launch_lincomb(st, n, B, 1.0 / 3.0, A, 0.0, nullptr, 0.0, nullptr);  // ubar3 = ubar2
   rs::launch_lincomb(st, n, Wb, h2, B, 0.0, nullptr, 0.0, nullptr);
-  vjp(V2, F2, gf(t + 1.0 * dt), Wb, A);
+  vjp(V2, Fa[2], gf(t + 1.0 * dt), Wb, A);
   rs::launch_lincomb(st, n, B, 1.0, B, 1.0, A, 0.0, nullptr);             // ubar2 -> ubar1
   rs::launch_lincomb(st, n, Wb, h2, B, 0.0, nullptr, 0.0, nullptr);
-  vjp(V1, F1, gf(t + 0.5 * dt), Wb, A);
+  vjp(V1, Fa[1], gf(t + 0.5 * dt), Wb, A);
   rs::launch_lincomb(st, n, B, 1.0, B, 1.0, A, 0.0, nullptr);             // ubar1 -> ubar0
   rs::launch_lincomb(st, n, Wb, h2, B, 0.0, nullptr, 0.0, nullptr);
-  vjp(u, F0, gf(t), Wb, A);
+  vjp(u, Fa[0], gf(t), Wb, A);
   rs::launch_lincomb(st, n, out, 1.0, out, 1.0, B, 1.0, A);
 }
 
@@ -1297,7 +1367,7 @@ void ensure_adjoint_buffers(rs_handle* h) {
     h->ebar.zero(h->st);
   }
   if (h->cfg.do_transport) {
-    h->adj.alloc(11 * n);
+    h->adj.alloc((h->pbl_on ? 15 : 11) * n);  // + 4 advection-only tendencies with PBL mixing
     h->G.alloc((size_t)h->ntr * h->nc);
     const rs_grid& g = h->cfg.grid;
     size_t fx = (size_t)(g.nlon + 1) * g.nlat * g.nlev, fy = (size_t)g.nlon * (g.nlat + 1) * g.nlev,

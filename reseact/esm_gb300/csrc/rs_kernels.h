@@ -65,6 +65,14 @@ struct DevTransport {
   const float* veC32;
   const float* veD32;
   int mixed;
+  // full PBL mixing (transport half): per-layer fraction f and weight w = dp*f, the column
+  // normaliser max(sum_k w, 1 Pa), scratch for the per-tracer column means, 1/tau
+  int pbl;
+  const double* pbl_f;     // [nlev][nlat][nlon]
+  const double* pbl_w;     // [nlev][nlat][nlon]
+  const double* pbl_den;   // [nlat][nlon]
+  double* pbl_qbar;        // [ntr][nlat][nlon]
+  double pbl_tau, pbl_rtau;
   // launch shape of the FP64 pencil flux kernels (chosen by rs_autotune)
   int pencil;    // pencils per block in the lat / vertical kernels: 16 or 32
   int rows;      // threads along the pencil (blockDim.y): 4, 8 or 16
@@ -99,8 +107,10 @@ struct TransportBufs {
 void launch_ssprk43_attempt(cudaStream_t st, const DevTransport<double>& T, const Ctl* ctl,
                             const TransportBufs& B, double rtol, double atol, int clamp);
 // du = f_transport(u) with flux time factor g for a grid-SoA state (single evaluation hook)
+// dUadv (optional): the same tendency without the PBL mixing term (the adjoint's air-mass
+// derivative uses the advective part only)
 void launch_transport_rhs(cudaStream_t st, const DevTransport<double>& T, const double* U,
-                          double g, double* dU);
+                          double g, double* dU, double* dUadv = nullptr);
 
 void launch_flux_dir(cudaStream_t st, const DevTransport<double>& T, const double* Q, int dir);
 

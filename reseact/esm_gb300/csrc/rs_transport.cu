@@ -576,6 +576,38 @@ __device__ __forceinline__ double div_m(const DevTransport<double>& T, int i, in
   return (DxM + DyM) + DzM;
 }
 
+// Full PBL mixing (reseact.esm Transport3D pbl_sum_* / pbl_mean_*): per tracer and column the
+// PBL mean qbar = sum_k w_k q_k / den, summed from the surface up as the reference's column
+// aggregate; the stage kernels add pbl_f * (qbar - q) / tau to each tracer tendency.
+__global__ void __launch_bounds__(kRedThreads) k_pbl_mean(DevTransport<double> T, StageSel sel) {
+  const double* Q;
+  double g;
+  if (!resolve_stage(sel, Q, g)) return;
+  const size_t ncol = (size_t)T.nlon * T.nlat, nc = ncol * T.nlev;
+  const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= (size_t)T.ntr * ncol) return;
+  const size_t s = id / ncol, col = id % ncol;
+  const double* q = Q + s * nc + col;
+  double acc = 0.0;
+  for (int k = 0; k < T.nlev; ++k) acc = acc + T.pbl_w[(size_t)k * ncol + col] * q[(size_t)k * ncol];
+  T.pbl_qbar[id] = acc / T.pbl_den[col];
+}
+
+__device__ __forceinline__ double pbl_term(const DevTransport<double>& T, size_t c, size_t col,
+                                           int s, double q) {
+  const double pb = T.pbl_f[c] * (T.pbl_qbar[(size_t)s * T.nlon * T.nlat + col] - q);
+#if RS_STRICT
+  return pb / T.pbl_tau;
+#else
+  return pb * T.pbl_rtau;
+#endif
+}
+
+static void launch_pbl_mean(cudaStream_t st, const DevTransport<double>& T, const StageSel& sel) {
+  size_t n = (size_t)T.ntr * T.nlon * T.nlat;
+  k_pbl_mean<<<(unsigned)((n + kRedThreads - 1) / kRedThreads), kRedThreads, 0, st>>>(T, sel);
+}
+
 // stage in 1..4.  Qin: the field whose fluxes were computed (RHS argument).
 //   1: S1 = U + dt/2 f(U)           2: S2 = S1 + dt/2 f(S1)
 //   3: S1 = u3 = S2 + dt/2 f(S2), S3 = u4 = 2/3 U + 1/3 u3
@@ -632,6 +664,7 @@ __global__ void __launch_bounds__(kRedThreads) k_stage(DevTransport<double> T,
 #else
         du = (a + b) * rm;
 #endif
+        if (T.pbl) du = du + pbl_term(T, c, col, s, q);
       } else {
         du = -divM;
       }
@@ -673,7 +706,8 @@ __global__ void __launch_bounds__(kRedThreads) k_stage(DevTransport<double> T,
 // Plain RHS evaluation for the rs_rhs_transport hook: du = f(U) at time factor g.
 __global__ void __launch_bounds__(kRedThreads) k_rhs_eval(DevTransport<double> T,
                                                           const double* __restrict__ Qin,
-                                                          double* __restrict__ dU, double g) {
+                                                          double* __restrict__ dU, double g,
+                                                          double* __restrict__ dUadv) {
   const size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
   size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
@@ -702,9 +736,12 @@ __global__ void __launch_bounds__(kRedThreads) k_rhs_eval(DevTransport<double> T
       double Dz = ft - fb;
       double a = -((Dx + Dy) + Dz);
       double b = Qin[x] * divM;
-      dU[x] = has_m ? (a + b) / m : a + b;
+      const double adv = has_m ? (a + b) / m : a + b;
+      dU[x] = T.pbl ? adv + pbl_term(T, c, col, s, Qin[x]) : adv;
+      if (dUadv) dUadv[x] = adv;
     } else {
       dU[x] = -divM;
+      if (dUadv) dUadv[x] = -divM;
     }
   }
 }
@@ -817,20 +854,24 @@ void launch_ssprk43_attempt(cudaStream_t st, const DevTransport<double>& T, cons
         T, ctl, B.U0, B.U1, nullptr);
   }
   launch_fluxes(st, T, sel);
+  if (T.pbl) launch_pbl_mean(st, T, sel);
   k_stage<1><<<nb, kRedThreads, 0, st>>>(T, ctl, B, rtol, atol, clamp);
   sel.stage = 2;
   launch_fluxes(st, T, sel);
+  if (T.pbl) launch_pbl_mean(st, T, sel);
   k_stage<2><<<nb, kRedThreads, 0, st>>>(T, ctl, B, rtol, atol, clamp);
   sel.stage = 3;
   launch_fluxes(st, T, sel);
+  if (T.pbl) launch_pbl_mean(st, T, sel);
   k_stage<3><<<nb, kRedThreads, 0, st>>>(T, ctl, B, rtol, atol, clamp);
   sel.stage = 4;
   launch_fluxes(st, T, sel);
+  if (T.pbl) launch_pbl_mean(st, T, sel);
   k_stage<4><<<nb, kRedThreads, 0, st>>>(T, ctl, B, rtol, atol, clamp);
 }
 
 void launch_transport_rhs(cudaStream_t st, const DevTransport<double>& T, const double* U,
-                          double g, double* dU) {
+                          double g, double* dU, double* dUadv) {
   StageSel sel{nullptr, 0, nullptr, nullptr, nullptr, nullptr, nullptr, U, g};
   size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
   if (T.mixed) {
@@ -839,7 +880,9 @@ void launch_transport_rhs(cudaStream_t st, const DevTransport<double>& T, const 
         T, nullptr, nullptr, nullptr, U);
   }
   launch_fluxes(st, T, sel);
-  k_rhs_eval<<<(unsigned)((nc + kRedThreads - 1) / kRedThreads), kRedThreads, 0, st>>>(T, U, dU, g);
+  if (T.pbl) launch_pbl_mean(st, T, sel);
+  k_rhs_eval<<<(unsigned)((nc + kRedThreads - 1) / kRedThreads), kRedThreads, 0, st>>>(T, U, dU, g,
+                                                                                     dUadv);
 }
 
 }  // namespace rs

@@ -176,7 +176,8 @@ class Workload:
     def forcing_abi(self):
         f = dict(self.forcing)
         om = f.pop("flux_omega", 0.0)
-        return abi.ForcingABI(flux_omega=om, **f)
+        tau = f.pop("tau_pblmix", 0.0)
+        return abi.ForcingABI(flux_omega=om, tau_pblmix=tau, **f)
 
     def u0_cellmajor(self):
         g = self.grid
@@ -188,6 +189,28 @@ def _column_fields(g, dp, pmid):
     dp3 = np.broadcast_to(dp[:, None, None], shape).copy()
     p3 = np.broadcast_to(pmid[:, None, None], shape).copy()
     return dp3, p3, standard_temperature(p3)
+
+
+def with_pbl(w, tau=900.0, pblh_median=1000.0, sigma=0.5, seed=11):
+    """Switch on the full PBL mixing term of the transport half: a seeded lognormal PBL height
+    per column (median pblh_median m), the workload's own interface pressures as hybrid
+    coefficients (A = p_interface, B = 0; surface pressure is uniform in these grids) and the
+    relaxation time tau (the reference's default is 900 s)."""
+    g = w.grid
+    dp = np.asarray(w.forcing["dp"])[:, 0, 0]
+    pmid = np.asarray(w.forcing["pressure"])[:, 0, 0]
+    p_int = np.empty(g["nlev"] + 1)
+    p_int[0] = pmid[0] + 0.5 * dp[0]
+    for k in range(g["nlev"]):
+        p_int[k + 1] = p_int[k] - dp[k]
+    rng = np.random.default_rng(seed)
+    w.forcing["pblh"] = pblh_median * np.exp(sigma * rng.standard_normal((g["nlat"], g["nlon"])))
+    w.forcing["ps"] = np.full((g["nlat"], g["nlon"]), p_int[0])
+    w.forcing["hyb_a"] = p_int
+    w.forcing["hyb_b"] = np.zeros(g["nlev"] + 1)
+    w.forcing["tau_pblmix"] = float(tau)
+    w.name += " + PBL mixing"
+    return w
 
 
 def c1(seed=1, mech=None):
