@@ -165,6 +165,14 @@ typedef struct rs_forcing {
   const double* hyb_a;       /* [nlev+1] interface pressure coefficient A (Pa), 0 = surface */
   const double* hyb_b;       /* [nlev+1] interface coefficient B: p_k = A_k + B_k * PS */
   double tau_pblmix;         /* relaxation time (s); the reference's default is 900 */
+  /* Pressure fixer with diagnosed vertical mass flux (reseact.esm Transport3D divh, divh_col,
+   * dp_col, divh_fix, Mz, dm/dt): with dps_dt and hyb_b given, the horizontal divergence is
+   * corrected to the surface-pressure tendency, divh_fix = divh + (-dPSdt - sum_k divh_k) *
+   * dp_k / sum_k dp_k; Mz is diagnosed as sum over the layers below of -(dB_k dPSdt +
+   * divh_fix_k) (the mz field is then ignored); the air mass obeys dm/dt = -(divh_fix + D(Mz))
+   * = dB_k dPSdt; tracers keep the raw horizontal fluxes with the diagnosed Mz.  Needs steady
+   * fluxes (flux_omega = 0). */
+  const double* dps_dt;      /* [nlat][nlon] surface-pressure tendency (Pa/s) */
 } rs_forcing;
 
 /* Per-macro-step statistics (op_split.jl:159-163 return tuple plus the carried dts). */
@@ -256,6 +264,11 @@ rs_status rs_get_chem_kernel(rs_handle* h, int32_t* kind, char* info, size_t inf
 rs_status rs_lu_order(rs_handle* h, int32_t* ord, int32_t n);
 rs_status rs_mechanism_lu_order(const rs_mechanism* mech, int32_t natural, int32_t* ord,
                                 int32_t n);
+/* Air-mass continuity drift (run_reseact.jl:297-324): r = (m - dp(PS)) / dp(PS) per cell with
+ * dp(PS) = dA_k + dB_k PS from the hybrid coefficients and the caller's surface pressure ps
+ * [nlat][nlon] at the state's time; out[0] = RMS over interior cells, out[1] = RMS over the
+ * lateral wall cells, out[2] = the interior value of largest magnitude. */
+rs_status rs_continuity_drift(rs_handle* h, const double* ps, double* out3);
 /* The reciprocal the production build's specialised kernels use in place of IEEE division
  * (Newton-Raphson from the hardware approximation; the strict build divides), applied to n
  * host values on the handle's device: a numerics check, r[i] ~ 1/x[i] within a few ulp. */

@@ -49,6 +49,7 @@ struct RsForcing
     emission::Ptr{Float64}
     pblh::Ptr{Float64}; ps::Ptr{Float64}; hyb_a::Ptr{Float64}; hyb_b::Ptr{Float64}
     tau_pblmix::Float64
+    dps_dt::Ptr{Float64}
 end
 
 mutable struct RsStats

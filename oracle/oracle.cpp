@@ -290,6 +290,9 @@ struct Forcing {
   std::vector<double> pblh, ps, hyb_a, hyb_b, pbl_f, pbl_w, pbl_den;
   double tau_pbl = 0.0;
   bool pbl = false;
+  // pressure fixer (reseact.esm Transport3D divh_fix / diagnosed Mz): dPS/dt per column and
+  // the per-cell correction of the horizontal divergence in the air-mass equation
+  std::vector<double> dpsdt, mcorr;
   // vertical PPM coefficients per column: slope (sA,sB) for cells -1..nlev, edge (eAB,eC,eD)
   // for edges 0..nlev (edge e lies between cells e-1 and e)
   std::vector<double> vs, ve;
@@ -517,6 +520,47 @@ void build_pbl(const Grid& G, Forcing& F) {
   }
 }
 
+// Pressure fixer, per column with sums from the surface up (reseact.esm Transport3D divh,
+// divh_col, dp_col, divh_fix, Mz): corr_k = (-dPSdt - sum_k divh_k) * (dp_k / sum_k dp_k),
+// Mz_{k+1} = Mz_k + -(dB_k dPSdt + (divh_k + corr_k)) with Mz_0 = 0; Mz replaces the given mz.
+void build_fixer(const Grid& G, Forcing& F) {
+  size_t ncol = (size_t)G.nlon * G.nlat, nf = (size_t)G.nlon + 1;
+  F.mcorr.clear();
+  if (F.dpsdt.size() != ncol || F.hyb_b.size() != (size_t)G.nlev + 1 || F.mx.empty() ||
+      F.my.empty())
+    return;
+  bool open_lat = G.lat_bc == RS_BC_OPEN;
+  std::vector<double> divh(G.nc);
+  F.mcorr.assign(G.nc, 0.0);
+  F.mz.assign((size_t)(G.nlev + 1) * ncol, 0.0);
+  for (int j = 0; j < G.nlat; ++j)
+    for (int i = 0; i < G.nlon; ++i) {
+      size_t col = (size_t)j * G.nlon + i;
+      double hcol = 0.0, dcol = 0.0;
+      for (int k = 0; k < G.nlev; ++k) {
+        size_t c = (size_t)k * ncol + col;
+        double mxw = F.mx[((size_t)k * G.nlat + j) * nf + i];
+        double mxe = F.mx[((size_t)k * G.nlat + j) * nf + i + 1];
+        double mys = (!open_lat && j == 0) ? 0.0 : F.my[((size_t)k * (G.nlat + 1) + j) * G.nlon + i];
+        double myn = (!open_lat && j + 1 == G.nlat) ? 0.0
+                   : F.my[((size_t)k * (G.nlat + 1) + j + 1) * G.nlon + i];
+        double DxM = (mxe - mxw) * G.gx[j];
+        double DyM = myn * G.gyhi[j] - mys * G.gylo[j];
+        divh[c] = DxM + DyM;
+        hcol = hcol + divh[c];
+        dcol = dcol + F.dp[c];
+      }
+      double dps = F.dpsdt[col], acc = 0.0;
+      for (int k = 0; k < G.nlev; ++k) {
+        size_t c = (size_t)k * ncol + col;
+        F.mcorr[c] = (-dps - hcol) * (F.dp[c] / dcol);
+        double fix = divh[c] + F.mcorr[c];
+        acc = acc + -((F.hyb_b[k] - F.hyb_b[k + 1]) * dps + fix);
+        F.mz[(size_t)(k + 1) * ncol + col] = acc;
+      }
+    }
+}
+
 double xflux(const Model& md, const double* q, int s, int i, int j, int k, double g) {
   const Grid& G = md.G;
   double M = g * md.F.mx[((size_t)k * G.nlat + j) * (G.nlon + 1) + i];
@@ -612,7 +656,9 @@ void transport_rhs(const Model& md, const double* u, double t, double* du, bool 
             adv = adv + (md.F.pbl_f[c] * (qbar[(size_t)s * ncol0 + col] - q[c])) / md.F.tau_pbl;
           du[(size_t)s * nc + c] = adv;
         }
-        if (md.has_m) du[(size_t)(md.nsp - 1) * nc + c] = -divM;
+        if (md.has_m)  // with the pressure fixer: -((divh + corr) + DzM)
+          du[(size_t)(md.nsp - 1) * nc + c] =
+              md.F.mcorr.empty() ? -divM : -(((DxM + DyM) + md.F.mcorr[c]) + DzM);
       }
 }
 
@@ -1162,6 +1208,9 @@ int or_set_forcing(or_model* h, const rs_forcing* f) {
   if (f->hyb_a) md.F.hyb_a.assign(f->hyb_a, f->hyb_a + G.nlev + 1);
   if (f->hyb_b) md.F.hyb_b.assign(f->hyb_b, f->hyb_b + G.nlev + 1);
   if (md.cfg.do_transport) build_pbl(G, md.F);
+  if (f->dps_dt) md.F.dpsdt.assign(f->dps_dt, f->dps_dt + ncol);
+  if (md.cfg.do_transport && (f->dps_dt || f->hyb_b || f->mx || f->my || f->mz || f->dp))
+    build_fixer(G, md.F);
   if (tp) compute_rates(md);
   return 0;
 }

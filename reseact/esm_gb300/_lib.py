@@ -21,7 +21,7 @@ SYMBOLS = [
     "rs_backward_macro_step", "rs_adjoint_get_grad_emission", "rs_adjoint_reset_grad",
     "rs_autotune", "rs_set_chem_kernel", "rs_get_chem_kernel", "rs_chem_kernel_source",
     "rs_chem_kernel_compile", "rs_chem_kernel_reciprocal", "rs_lu_order",
-    "rs_mechanism_lu_order",
+    "rs_mechanism_lu_order", "rs_continuity_drift",
 ]
 
 CHEM_KERNEL_AUTO, CHEM_KERNEL_TABLE, CHEM_KERNEL_SPECIALIZED = 0, 1, 2
@@ -97,6 +97,8 @@ def _declare(L):
     L.rs_chem_kernel_source.restype = C.c_int
     L.rs_chem_kernel_compile.argtypes = [C.POINTER(abi.rs_mechanism), i32, C.c_char_p, sz]
     L.rs_chem_kernel_compile.restype = C.c_int
+    L.rs_continuity_drift.argtypes = [vp, dp, dp]
+    L.rs_continuity_drift.restype = C.c_int
     L.rs_lu_order.argtypes = [vp, C.POINTER(i32), i32]
     L.rs_lu_order.restype = C.c_int
     L.rs_mechanism_lu_order.argtypes = [C.POINTER(abi.rs_mechanism), i32, C.POINTER(i32), i32]
@@ -297,6 +299,13 @@ class Solver:
         buf = C.create_string_buffer(1024)
         self._check(self.L.rs_get_chem_kernel(self.h, C.byref(k), buf, 1024))
         return k.value, json.loads(buf.value.decode())
+
+    def continuity_drift(self, ps):
+        """(rms over interior cells, rms over wall cells, worst interior) of (m - dp(PS))/dp(PS)."""
+        ps = np.ascontiguousarray(ps, dtype=np.float64)
+        out = np.zeros(3)
+        self._check(self.L.rs_continuity_drift(self.h, _p(ps), _p(out)))
+        return tuple(out)
 
     def lu_order(self):
         """Species eliminated at each pivot of this handle's LU (natural in the strict build)."""

@@ -61,7 +61,7 @@ class rs_forcing(C.Structure):
                 ("dp", _f64p), ("qbc_w", _f64p), ("qbc_e", _f64p), ("qbc_s", _f64p),
                 ("qbc_n", _f64p), ("temperature", _f64p), ("pressure", _f64p),
                 ("emission", _f64p), ("pblh", _f64p), ("ps", _f64p), ("hyb_a", _f64p),
-                ("hyb_b", _f64p), ("tau_pblmix", C.c_double)]
+                ("hyb_b", _f64p), ("tau_pblmix", C.c_double), ("dps_dt", _f64p)]
 
 
 class rs_stats(C.Structure):
@@ -130,7 +130,7 @@ class ForcingABI:
     """Keeps forcing arrays alive (contiguous float64) behind an rs_forcing struct."""
 
     NAMES = ("mx", "my", "mz", "dp", "qbc_w", "qbc_e", "qbc_s", "qbc_n", "temperature",
-             "pressure", "emission", "pblh", "ps", "hyb_a", "hyb_b")
+             "pressure", "emission", "pblh", "ps", "hyb_a", "hyb_b", "dps_dt")
 
     def __init__(self, flux_omega=0.0, tau_pblmix=0.0, **arrays):
         self.arrays = {k: (None if arrays.get(k) is None else
@@ -147,4 +147,4 @@ class ForcingABI:
                                  _ptr(a["emission"], C.c_double),
                                  _ptr(a["pblh"], C.c_double), _ptr(a["ps"], C.c_double),
                                  _ptr(a["hyb_a"], C.c_double), _ptr(a["hyb_b"], C.c_double),
-                                 float(tau_pblmix))
+                                 float(tau_pblmix), _ptr(a["dps_dt"], C.c_double))

@@ -352,6 +352,11 @@ struct rs_handle {
   double tau_pbl = 0.0;
   bool pbl_on = false;
   DevBuf<double> pbl_f, pbl_w, pbl_den, pbl_qbar;
+  // pressure fixer: host inputs (horizontal fluxes, geometry, dPS/dt) and the air-mass
+  // divergence correction on the device; the diagnosed Mz replaces the mz field
+  std::vector<double> mx_host, my_host, gx_host, gylo_host, gyhi_host, dpsdt_host;
+  bool fixer_on = false;
+  DevBuf<double> mcorr;
   std::shared_ptr<rs::JitChem> jit;
   DevBuf<double> fsal[2];  // f(U[b]) planes [ns][nc] for the specialised global-dt attempts
   std::string jit_why;
@@ -480,6 +485,9 @@ void build_geometry(rs_handle* h) {
   h->gx.upload(gx.data(), gx.size(), h->st);
   h->gylo.upload(gl.data(), gl.size(), h->st);
   h->gyhi.upload(gh.data(), gh.size(), h->st);
+  h->gx_host = gx;
+  h->gylo_host = gl;
+  h->gyhi_host = gh;
 }
 
 // CW84 nonuniform coefficients from dp (eqs. 1.6-1.7), mirror ghosts at the no-flux walls.
@@ -551,6 +559,57 @@ void refresh_dt(rs_handle* h) {
   T.pbl_f = h->pbl_f.p; T.pbl_w = h->pbl_w.p; T.pbl_den = h->pbl_den.p; T.pbl_qbar = h->pbl_qbar.p;
   T.pbl_tau = h->tau_pbl;
   T.pbl_rtau = h->tau_pbl > 0.0 ? 1.0 / h->tau_pbl : 0.0;
+  T.mcorr = h->fixer_on ? h->mcorr.p : nullptr;
+}
+
+// Pressure fixer (reseact.esm Transport3D divh, divh_col, dp_col, divh_fix, Mz), per column:
+//   divh_k = DxM + DyM (the kernels' expressions, steady fluxes), corr_k = (-dPSdt - sum divh)
+//   * (dp_k / sum dp), Mz_0 = 0, Mz_{k+1} = Mz_k + -(dB_k dPSdt + (divh_k + corr_k)),
+// sums from the surface up; corr goes to the air-mass equation, Mz replaces the mz field.
+void build_fixer(rs_handle* h) {
+  const rs_grid& g = h->cfg.grid;
+  const size_t ncol = (size_t)g.nlon * g.nlat, nf = (size_t)g.nlon + 1;
+  h->fixer_on = h->cfg.do_transport && h->dpsdt_host.size() == ncol &&
+                h->hyb_b_host.size() == (size_t)g.nlev + 1 &&
+                h->mx_host.size() == (size_t)g.nlev * g.nlat * nf &&
+                h->my_host.size() == (size_t)g.nlev * (g.nlat + 1) * g.nlon;
+  if (!h->fixer_on) return;
+  if (h->omega != 0.0)
+    throw RsError(RS_ERR_UNSUPPORTED, "the pressure fixer needs steady fluxes (flux_omega = 0)");
+  const bool open_lat = g.lat_bc == RS_BC_OPEN;
+  const double* dp = h->dp_host.data();
+  const double* B = h->hyb_b_host.data();
+  std::vector<double> divh(h->nc), corr(h->nc), mz((size_t)(g.nlev + 1) * ncol, 0.0);
+  for (int j = 0; j < g.nlat; ++j)
+    for (int i = 0; i < g.nlon; ++i) {
+      const size_t col = (size_t)j * g.nlon + i;
+      double hcol = 0.0, dcol = 0.0;
+      for (int k = 0; k < g.nlev; ++k) {
+        const size_t c = (size_t)k * ncol + col;
+        const double mxw = h->mx_host[((size_t)k * g.nlat + j) * nf + i];
+        const double mxe = h->mx_host[((size_t)k * g.nlat + j) * nf + i + 1];
+        const double mys = (!open_lat && j == 0) ? 0.0
+                         : h->my_host[((size_t)k * (g.nlat + 1) + j) * g.nlon + i];
+        const double myn = (!open_lat && j + 1 == g.nlat) ? 0.0
+                         : h->my_host[((size_t)k * (g.nlat + 1) + j + 1) * g.nlon + i];
+        const double DxM = (mxe - mxw) * h->gx_host[j];
+        const double DyM = myn * h->gyhi_host[j] - mys * h->gylo_host[j];
+        divh[c] = DxM + DyM;
+        hcol = hcol + divh[c];
+        dcol = dcol + dp[c];
+      }
+      const double dps = h->dpsdt_host[col];
+      double acc = 0.0;
+      for (int k = 0; k < g.nlev; ++k) {
+        const size_t c = (size_t)k * ncol + col;
+        corr[c] = (-dps - hcol) * (dp[c] / dcol);
+        const double fix = divh[c] + corr[c];
+        acc = acc + -((B[k] - B[k + 1]) * dps + fix);
+        mz[(size_t)(k + 1) * ncol + col] = acc;
+      }
+    }
+  h->mz.upload(mz.data(), mz.size(), h->st);
+  h->mcorr.upload(corr.data(), corr.size(), h->st);
 }
 
 // PBL fraction and weights of every layer (reseact.esm Transport3D p_pbl_top, pbl_f, pbl_wt):
@@ -879,7 +938,7 @@ void rs_destroy(rs_handle* h) {
                             &h->mx, &h->my, &h->mz, &h->qw, &h->qe, &h->qs, &h->qn, &h->gx,
                             &h->gylo, &h->gyhi, &h->vsA, &h->vsB, &h->veAB, &h->veC, &h->veD,
                             &h->dtcell, &h->stepcell, &h->totals, &h->fsal[0], &h->fsal[1],
-                            &h->pbl_f, &h->pbl_w, &h->pbl_den, &h->pbl_qbar};
+                            &h->pbl_f, &h->pbl_w, &h->pbl_den, &h->pbl_qbar, &h->mcorr};
   for (auto* b : bufs) b->release();
   h->slot_row.release();
   h->slot_col.release();
@@ -949,8 +1008,14 @@ rs_status rs_set_forcing(rs_handle* h, const rs_forcing* f) {
     cudaStream_t st = h->st;
     size_t nc = h->nc;
     if (h->cfg.do_transport) {
-      if (f->mx) h->mx.upload(f->mx, (size_t)g.nlev * g.nlat * (g.nlon + 1), st);
-      if (f->my) h->my.upload(f->my, (size_t)g.nlev * (g.nlat + 1) * g.nlon, st);
+      if (f->mx) {
+        h->mx.upload(f->mx, (size_t)g.nlev * g.nlat * (g.nlon + 1), st);
+        h->mx_host.assign(f->mx, f->mx + (size_t)g.nlev * g.nlat * (g.nlon + 1));
+      }
+      if (f->my) {
+        h->my.upload(f->my, (size_t)g.nlev * (g.nlat + 1) * g.nlon, st);
+        h->my_host.assign(f->my, f->my + (size_t)g.nlev * (g.nlat + 1) * g.nlon);
+      }
       if (f->mz) h->mz.upload(f->mz, (size_t)(g.nlev + 1) * g.nlat * g.nlon, st);
       if (f->qbc_w) h->qw.upload(f->qbc_w, (size_t)h->ntr * g.nlev * g.nlat, st);
       if (f->qbc_e) h->qe.upload(f->qbc_e, (size_t)h->ntr * g.nlev * g.nlat, st);
@@ -981,6 +1046,8 @@ rs_status rs_set_forcing(rs_handle* h, const rs_forcing* f) {
       if (f->hyb_b) { h->hyb_b_host.assign(f->hyb_b, f->hyb_b + g.nlev + 1); pbl_inputs = true; }
       if (f->temperature) h->tsfc_host.assign(f->temperature, f->temperature + ncol);
       if (pbl_inputs) build_pbl(h);
+      if (f->dps_dt) h->dpsdt_host.assign(f->dps_dt, f->dps_dt + ncol);
+      if (f->dps_dt || f->hyb_b || f->mx || f->my || f->mz || f->dp) build_fixer(h);
     }
     if (f->temperature) {
       h->T.upload(f->temperature, nc, st);
@@ -1570,6 +1637,43 @@ extern "C" rs_status rs_lu_order(rs_handle* h, int32_t* ord, int32_t n) {
   return guard(h, [&] {
     if (n < h->mt.ns) throw RsError(RS_ERR_INVALID, "ord holds fewer entries than species");
     for (int k = 0; k < h->mt.ns; ++k) ord[k] = h->mt.ord[k];
+  });
+}
+
+extern "C" rs_status rs_continuity_drift(rs_handle* h, const double* ps, double* out3) {
+  if (!h || !ps || !out3) return RS_ERR_INVALID;
+  return guard(h, [&] {
+    const rs_grid& g = h->cfg.grid;
+    if (!h->cfg.has_air_mass) throw RsError(RS_ERR_INVALID, "the state carries no air mass");
+    if (h->hyb_a_host.size() != (size_t)g.nlev + 1 || h->hyb_b_host.size() != (size_t)g.nlev + 1)
+      throw RsError(RS_ERR_STATE, "hybrid coefficients not given (rs_forcing hyb_a, hyb_b)");
+    const size_t ncol = (size_t)g.nlon * g.nlat;
+    std::vector<double> m(h->nc);
+    CK(cudaMemcpyAsync(m.data(), h->U[h->cur].p + (size_t)(h->nsp - 1) * h->nc,
+                       h->nc * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    const double* A = h->hyb_a_host.data();
+    const double* B = h->hyb_b_host.data();
+    double s2i = 0.0, s2w = 0.0, worst = 0.0;
+    size_t ni = 0, nw = 0;
+    for (int k = 0; k < g.nlev; ++k)
+      for (int j = 0; j < g.nlat; ++j)
+        for (int i = 0; i < g.nlon; ++i) {
+          const size_t col = (size_t)j * g.nlon + i;
+          const double dpk = (A[k] - A[k + 1]) + (B[k] - B[k + 1]) * ps[col];
+          const double r = (m[(size_t)k * ncol + col] - dpk) / dpk;
+          if (i == 0 || i == g.nlon - 1 || j == 0 || j == g.nlat - 1) {
+            s2w += r * r;
+            ++nw;
+          } else {
+            s2i += r * r;
+            ++ni;
+            if (std::fabs(r) > std::fabs(worst)) worst = r;
+          }
+        }
+    out3[0] = std::sqrt(s2i / (double)std::max<size_t>(ni, 1));
+    out3[1] = std::sqrt(s2w / (double)std::max<size_t>(nw, 1));
+    out3[2] = worst;
   });
 }
 

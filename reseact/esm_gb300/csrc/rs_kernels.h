@@ -73,6 +73,9 @@ struct DevTransport {
   const double* pbl_den;   // [nlat][nlon]
   double* pbl_qbar;        // [ntr][nlat][nlon]
   double pbl_tau, pbl_rtau;
+  // pressure fixer: per-cell correction of the horizontal divergence in the air-mass equation,
+  // dm/dt = -(((DxM + DyM) + mcorr) + DzM); null when off
+  const double* mcorr;     // [nlev][nlat][nlon]
   // launch shape of the FP64 pencil flux kernels (chosen by rs_autotune)
   int pencil;    // pencils per block in the lat / vertical kernels: 16 or 32
   int rows;      // threads along the pencil (blockDim.y): 4, 8 or 16

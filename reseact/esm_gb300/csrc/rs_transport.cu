@@ -558,8 +558,9 @@ __global__ void __launch_bounds__(kRedThreads) k_split_input(DevTransport<double
 struct CellGeo {
   double gx, gylo, gyhi;
 };
-__device__ __forceinline__ double div_m(const DevTransport<double>& T, int i, int j, int k,
-                                        double g, const CellGeo& G) {
+// horizontal (DxM + DyM) and vertical (DzM) parts of the air-mass flux divergence
+__device__ __forceinline__ void div_parts(const DevTransport<double>& T, int i, int j, int k,
+                                          double g, const CellGeo& G, double& hz, double& vz) {
   const int nf = T.nlon + 1;
   const size_t ncol = (size_t)T.nlon * T.nlat, col = (size_t)j * T.nlon + i;
   double mxw = g * T.mx[((size_t)k * T.nlat + j) * nf + i];
@@ -572,8 +573,21 @@ __device__ __forceinline__ double div_m(const DevTransport<double>& T, int i, in
   double mzt = (k + 1 == T.nlev) ? 0.0 : g * T.mz[(size_t)(k + 1) * ncol + col];
   double DxM = (mxe - mxw) * G.gx;
   double DyM = myn * G.gyhi - mys * G.gylo;
-  double DzM = mzt - mzb;
-  return (DxM + DyM) + DzM;
+  hz = DxM + DyM;
+  vz = mzt - mzb;
+}
+__device__ __forceinline__ double div_m(const DevTransport<double>& T, int i, int j, int k,
+                                        double g, const CellGeo& G) {
+  double hz, vz;
+  div_parts(T, i, j, k, g, G, hz, vz);
+  return hz + vz;
+}
+// air-mass tendency: -divM, or with the pressure fixer -((divh + corr) + DzM)
+__device__ __forceinline__ double dm_dt(const DevTransport<double>& T, int i, int j, int k,
+                                        double g, const CellGeo& G, size_t c) {
+  double hz, vz;
+  div_parts(T, i, j, k, g, G, hz, vz);
+  return T.mcorr ? -((hz + T.mcorr[c]) + vz) : -(hz + vz);
 }
 
 // Full PBL mixing (reseact.esm Transport3D pbl_sum_* / pbl_mean_*): per tracer and column the
@@ -666,7 +680,7 @@ __global__ void __launch_bounds__(kRedThreads) k_stage(DevTransport<double> T,
 #endif
         if (T.pbl) du = du + pbl_term(T, c, col, s, q);
       } else {
-        du = -divM;
+        du = dm_dt(T, i, j, k, g, G, c);
       }
       if (STAGE == 1) {
         double nx = q + dt_2 * du;
@@ -740,8 +754,9 @@ __global__ void __launch_bounds__(kRedThreads) k_rhs_eval(DevTransport<double> T
       dU[x] = T.pbl ? adv + pbl_term(T, c, col, s, Qin[x]) : adv;
       if (dUadv) dUadv[x] = adv;
     } else {
-      dU[x] = -divM;
-      if (dUadv) dUadv[x] = -divM;
+      const double dm = dm_dt(T, i, j, k, g, G, c);
+      dU[x] = dm;
+      if (dUadv) dUadv[x] = dm;
     }
   }
 }

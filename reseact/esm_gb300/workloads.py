@@ -213,6 +213,30 @@ def with_pbl(w, tau=900.0, pblh_median=1000.0, sigma=0.5, seed=11):
     return w
 
 
+def with_pressure_fixer(w, dps_amp=2e-3, seed=12):
+    """Switch on the pressure fixer with diagnosed vertical mass flux: steady fluxes, hybrid
+    coefficients of the workload's own levels that reach B = 0 at the lid (B_k = (p_k - p_top)
+    / (PS - p_top), A_k = p_top (1 - B_k), so that dm_k/dt = dB_k dPS/dt is exercised and the
+    diagnosed Mz closes at the top) and a seeded surface-pressure tendency field of amplitude
+    dps_amp (Pa/s).  The given mz is ignored once the fixer is on."""
+    g = w.grid
+    dp = np.asarray(w.forcing["dp"])[:, 0, 0]
+    pmid = np.asarray(w.forcing["pressure"])[:, 0, 0]
+    p_int = np.empty(g["nlev"] + 1)
+    p_int[0] = pmid[0] + 0.5 * dp[0]
+    for k in range(g["nlev"]):
+        p_int[k + 1] = p_int[k] - dp[k]
+    rng = np.random.default_rng(seed)
+    w.forcing["flux_omega"] = 0.0
+    b = (p_int - p_int[-1]) / (p_int[0] - p_int[-1])
+    w.forcing["hyb_a"] = p_int[-1] * (1.0 - b)
+    w.forcing["hyb_b"] = b
+    w.forcing["ps"] = np.full((g["nlat"], g["nlon"]), p_int[0])
+    w.forcing["dps_dt"] = dps_amp * rng.standard_normal((g["nlat"], g["nlon"]))
+    w.name += " + pressure fixer"
+    return w
+
+
 def c1(seed=1, mech=None):
     mech = mech or mechmod.superfast()
     g = latlon_grid(36, 18, 10)
