@@ -264,6 +264,38 @@ rs_status rs_get_chem_kernel(rs_handle* h, int32_t* kind, char* info, size_t inf
 rs_status rs_lu_order(rs_handle* h, int32_t* ord, int32_t n);
 rs_status rs_mechanism_lu_order(const rs_mechanism* mech, int32_t natural, int32_t* ord,
                                 int32_t n);
+/* Lie-Trotter window solve inside the library (op_split.jl:100-164 lie_trotter_solve and
+ * :219-241 lie_trotter_solve_bisect): the stop grid is the macro-dt lattice joined with the
+ * forcing cadence boundaries in the half-open interval (t0, t1] and t1 itself; each stop
+ * interval is one rs_macro_step; refresh(user, t) fires after a stop that lands on a cadence
+ * boundary (the callback may call rs_set_forcing); with min_macro_dt > 0 a failed window
+ * restarts from its initial state (kept on the device) as two halves, down to min_macro_dt,
+ * calling on_bisect(user, t0, t1) first.  Works on the device-resident state (rs_set_state /
+ * rs_get_state around it); *dtT / *dtC carry the inner step sizes in and out.  The counts in
+ * the result are summed over the windows that succeeded (a failed window's attempts are not
+ * counted, as in the reference). */
+typedef void (*rs_refresh_fn)(void* user, double t);
+typedef void (*rs_bisect_fn)(void* user, double t0, double t1);
+typedef struct rs_solve_opts {
+  double macro_dt;              /* > 0 */
+  double min_macro_dt;          /* bisection floor (reference default 9 s); <= 0: no bisection */
+  const double* forcing_tstops; /* cadence boundaries (may be NULL) */
+  size_t n_tstops;
+  rs_refresh_fn refresh;        /* may be NULL */
+  rs_bisect_fn on_bisect;       /* may be NULL */
+  void* user;
+} rs_solve_opts;
+typedef struct rs_solve_result {
+  double naT, nrT, naC, nrC;    /* accepted / rejected inner attempts */
+  double nmacro;                /* macro steps taken */
+  double nbisect;               /* windows split */
+  double nrefresh;              /* refresh calls */
+  int32_t status;               /* RS_OK or the status of the window that failed */
+  int32_t pad;
+} rs_solve_result;
+rs_status rs_lie_trotter_solve(rs_handle* h, double t0, double t1, double* dtT, double* dtC,
+                               const rs_solve_opts* opts, rs_solve_result* out);
+
 /* Air-mass continuity drift (run_reseact.jl:297-324): r = (m - dp(PS)) / dp(PS) per cell with
  * dp(PS) = dA_k + dB_k PS from the hybrid coefficients and the caller's surface pressure ps
  * [nlat][nlon] at the state's time; out[0] = RMS over interior cells, out[1] = RMS over the

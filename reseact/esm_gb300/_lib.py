@@ -21,7 +21,7 @@ SYMBOLS = [
     "rs_backward_macro_step", "rs_adjoint_get_grad_emission", "rs_adjoint_reset_grad",
     "rs_autotune", "rs_set_chem_kernel", "rs_get_chem_kernel", "rs_chem_kernel_source",
     "rs_chem_kernel_compile", "rs_chem_kernel_reciprocal", "rs_lu_order",
-    "rs_mechanism_lu_order", "rs_continuity_drift",
+    "rs_mechanism_lu_order", "rs_continuity_drift", "rs_lie_trotter_solve",
 ]
 
 CHEM_KERNEL_AUTO, CHEM_KERNEL_TABLE, CHEM_KERNEL_SPECIALIZED = 0, 1, 2
@@ -97,6 +97,9 @@ def _declare(L):
     L.rs_chem_kernel_source.restype = C.c_int
     L.rs_chem_kernel_compile.argtypes = [C.POINTER(abi.rs_mechanism), i32, C.c_char_p, sz]
     L.rs_chem_kernel_compile.restype = C.c_int
+    L.rs_lie_trotter_solve.argtypes = [vp, C.c_double, C.c_double, dp, dp,
+                                       C.POINTER(abi.rs_solve_opts), C.POINTER(abi.rs_solve_result)]
+    L.rs_lie_trotter_solve.restype = C.c_int
     L.rs_continuity_drift.argtypes = [vp, dp, dp]
     L.rs_continuity_drift.restype = C.c_int
     L.rs_lu_order.argtypes = [vp, C.POINTER(i32), i32]
@@ -299,6 +302,22 @@ class Solver:
         buf = C.create_string_buffer(1024)
         self._check(self.L.rs_get_chem_kernel(self.h, C.byref(k), buf, 1024))
         return k.value, json.loads(buf.value.decode())
+
+    def lie_trotter_solve(self, t0, t1, dtT, dtC, *, macro_dt, min_macro_dt=0.0,
+                          forcing_tstops=(), refresh=None, on_bisect=None):
+        """One window through the library's own stop grid and bisection (rs_lie_trotter_solve)
+        on the device-resident state.  Returns (status, dtT, dtC, result struct)."""
+        ts = np.ascontiguousarray(np.asarray(forcing_tstops, dtype=np.float64))
+        rf = abi.REFRESH_FN((lambda u, t: refresh(t)) if refresh else 0)
+        bf = abi.BISECT_FN((lambda u, a, b: on_bisect(a, b)) if on_bisect else 0)
+        o = abi.rs_solve_opts(float(macro_dt), float(min_macro_dt),
+                              ts.ctypes.data_as(C.POINTER(C.c_double)) if ts.size else None,
+                              ts.size, rf, bf, None)
+        a, b = C.c_double(dtT), C.c_double(dtC)
+        r = abi.rs_solve_result()
+        rc = self.L.rs_lie_trotter_solve(self.h, float(t0), float(t1), C.byref(a), C.byref(b),
+                                         C.byref(o), C.byref(r))
+        return rc, a.value, b.value, r
 
     def continuity_drift(self, ps):
         """(rms over interior cells, rms over wall cells, worst interior) of (m - dp(PS))/dp(PS)."""

@@ -72,6 +72,22 @@ class rs_stats(C.Structure):
                 ("status", C.c_int32)]
 
 
+REFRESH_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_double)
+BISECT_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_double, C.c_double)
+
+
+class rs_solve_opts(C.Structure):
+    _fields_ = [("macro_dt", C.c_double), ("min_macro_dt", C.c_double),
+                ("forcing_tstops", _f64p), ("n_tstops", C.c_size_t),
+                ("refresh", REFRESH_FN), ("on_bisect", BISECT_FN), ("user", C.c_void_p)]
+
+
+class rs_solve_result(C.Structure):
+    _fields_ = [("naT", C.c_double), ("nrT", C.c_double), ("naC", C.c_double),
+                ("nrC", C.c_double), ("nmacro", C.c_double), ("nbisect", C.c_double),
+                ("nrefresh", C.c_double), ("status", C.c_int32), ("pad", C.c_int32)]
+
+
 def pictrl_ros23():
     return rs_controller(7 / 20, 1 / 5, 1 / 5, 10.0, 9 / 10, 1.0, 6 / 5, 1e-4)
 

@@ -1677,6 +1677,101 @@ extern "C" rs_status rs_continuity_drift(rs_handle* h, const double* ps, double*
   });
 }
 
+// ====================================================================== window solve
+namespace {
+
+double round6(double t) { return std::round(t * 1.0e6) / 1.0e6; }
+
+struct WindowSolve {
+  rs_handle* h;
+  const rs_solve_opts& o;
+  rs_solve_result r{};
+  std::vector<DevBuf<double>> ck;  // window start states, one per bisection depth
+
+  // one window with the reference's stop grid; counts of a failed window are dropped
+  rs_status plain(double t0, double tf, double macro_dt, double& dtT, double& dtC) {
+    std::vector<double> stops;
+    std::set<double> fstops;
+    for (size_t q = 0; q < o.n_tstops; ++q) {
+      const double t = o.forcing_tstops[q];
+      if (t0 + 1e-6 < t && t <= tf + 1e-6) fstops.insert(round6(t));
+    }
+    for (long i = 1;; ++i) {
+      const double x = t0 + macro_dt * (double)i;
+      if (x > tf - 1e-9) break;
+      stops.push_back(x);
+    }
+    for (double t : fstops) stops.push_back(t);
+    stops.push_back(tf);
+    std::sort(stops.begin(), stops.end());
+    stops.erase(std::unique(stops.begin(), stops.end()), stops.end());
+    rs_solve_result part{};
+    double tcur = t0;
+    for (double tnext : stops) {
+      if (tnext <= tcur + 1e-9) continue;
+      rs_stats st{};
+      rs_status rc = rs_macro_step(h, tcur, tnext, &dtT, &dtC, &st);
+      if (rc != RS_OK) return rc;
+      part.naT += st.naT; part.nrT += st.nrT; part.naC += st.naC; part.nrC += st.nrC;
+      part.nmacro += 1.0;
+      tcur = tnext;
+      if (fstops.count(round6(tcur))) {
+        part.nrefresh += 1.0;
+        if (o.refresh) o.refresh(o.user, tcur);
+      }
+    }
+    r.naT += part.naT; r.nrT += part.nrT; r.naC += part.naC; r.nrC += part.nrC;
+    r.nmacro += part.nmacro;
+    r.nrefresh += part.nrefresh;
+    return RS_OK;
+  }
+
+  rs_status bisect(double t0, double tf, double macro_dt, double& dtT, double& dtC, int depth) {
+    const bool can_split = o.min_macro_dt > 0.0 && (tf - t0) > o.min_macro_dt + 1e-9;
+    const size_t n = h->nc * h->nsp;
+    if (can_split) {  // the window's start state, for a restart
+      if ((int)ck.size() <= depth) ck.resize(depth + 1);
+      ck[depth].alloc(n);
+      CK(cudaMemcpyAsync(ck[depth].p, h->U[h->cur].p, n * sizeof(double),
+                         cudaMemcpyDeviceToDevice, h->st));
+    }
+    const double dtT0 = dtT, dtC0 = dtC;
+    rs_status rc = plain(t0, tf, macro_dt, dtT, dtC);
+    if (rc == RS_OK || !can_split) return rc;
+    CK(cudaMemcpyAsync(h->U[h->cur].p, ck[depth].p, n * sizeof(double),
+                       cudaMemcpyDeviceToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    const double tm = 0.5 * (t0 + tf);
+    r.nbisect += 1.0;
+    if (o.on_bisect) o.on_bisect(o.user, t0, tf);
+    dtT = dtT0;
+    dtC = dtC0;
+    rc = bisect(t0, tm, std::min(macro_dt, tm - t0), dtT, dtC, depth + 1);
+    if (rc != RS_OK) return rc;
+    return bisect(tm, tf, std::min(macro_dt, tf - tm), dtT, dtC, depth + 1);
+  }
+};
+
+}  // namespace
+
+extern "C" rs_status rs_lie_trotter_solve(rs_handle* h, double t0, double t1, double* dtT,
+                                          double* dtC, const rs_solve_opts* opts,
+                                          rs_solve_result* out) {
+  if (!h || !dtT || !dtC || !opts) return RS_ERR_INVALID;
+  WindowSolve ws{h, *opts};
+  rs_status rc = guard(h, [&] {
+    if (!(t1 > t0)) throw RsError(RS_ERR_INVALID, "t1 must exceed t0");
+    if (!(opts->macro_dt > 0.0)) throw RsError(RS_ERR_INVALID, "macro_dt must be positive");
+    if (opts->n_tstops && !opts->forcing_tstops) throw RsError(RS_ERR_INVALID, "forcing_tstops");
+    rs_status w = ws.bisect(t0, t1, opts->macro_dt, *dtT, *dtC, 0);
+    if (w != RS_OK) throw RsError(w, std::string("window failed: ") + h->err);
+  });
+  for (auto& b : ws.ck) b.release();
+  ws.r.status = rc;
+  if (out) *out = ws.r;
+  return rc;
+}
+
 // Source and compile check of the specialised kernels for a mechanism (no device needed).
 namespace {
 rs_status nohandle(const std::function<void()>& fn) {
