@@ -153,4 +153,116 @@ function lie_trotter_solve_bisect(h::Handle, u0, tspan; macro_dt, min_macro_dt::
             dtT = r2.dtT, dtC = r2.dtC)
 end
 
+# ---------------------------------------------------------------- the window solve in the library
+struct RsSolveOpts
+    macro_dt::Float64; min_macro_dt::Float64
+    forcing_tstops::Ptr{Float64}; n_tstops::Csize_t
+    refresh::Ptr{Cvoid}; on_bisect::Ptr{Cvoid}; user::Ptr{Cvoid}
+end
+
+mutable struct RsSolveResult
+    naT::Float64; nrT::Float64; naC::Float64; nrC::Float64
+    nmacro::Float64; nbisect::Float64; nrefresh::Float64; status::Int32; pad::Int32
+end
+RsSolveResult() = RsSolveResult(0, 0, 0, 0, 0, 0, 0, 0, 0)
+
+# callbacks: the library passes back the `user` pointer, here the Julia context object
+mutable struct SolveCtx
+    refresh::Any
+    on_bisect::Any
+end
+_refresh_tramp(user::Ptr{Cvoid}, t::Float64) =
+    ((unsafe_pointer_to_objref(user)::SolveCtx).refresh(t); nothing)
+_bisect_tramp(user::Ptr{Cvoid}, t0::Float64, t1::Float64) =
+    ((unsafe_pointer_to_objref(user)::SolveCtx).on_bisect(t0, t1); nothing)
+
+"""
+    solve_window!(h, t0, t1; macro_dt, min_macro_dt=9.0, forcing_tstops, refresh, on_bisect,
+                  dtT=15.0, dtC=0.5)
+
+lie_trotter_solve_bisect done inside the library (rs_lie_trotter_solve) on the device-resident
+state: the same stop grid, refresh rule and bisection, with the window's start state kept on
+the GPU for a restart.  Returns (; retcode, naT, nrT, naC, nrC, nmacro, nbisect, dtT, dtC).
+"""
+function solve_window!(h::Handle, t0, t1; macro_dt, min_macro_dt::Real = 9.0,
+                       forcing_tstops = Float64[], refresh = (_t -> nothing),
+                       on_bisect = (_a, _b) -> nothing, dtT = 15.0, dtC = 0.5)
+    ctx = SolveCtx(refresh, on_bisect)
+    ts = collect(Float64, forcing_tstops)
+    rf = @cfunction(_refresh_tramp, Cvoid, (Ptr{Cvoid}, Float64))
+    bf = @cfunction(_bisect_tramp, Cvoid, (Ptr{Cvoid}, Float64, Float64))
+    a = Ref(Float64(dtT)); b = Ref(Float64(dtC)); r = RsSolveResult()
+    rc = GC.@preserve ctx ts begin
+        opts = RsSolveOpts(Float64(macro_dt), Float64(min_macro_dt),
+                           isempty(ts) ? C_NULL : pointer(ts), length(ts), rf, bf,
+                           pointer_from_objref(ctx))
+        ccall((:rs_lie_trotter_solve, LIB[]), Int32,
+              (Ptr{Cvoid}, Float64, Float64, Ref{Float64}, Ref{Float64}, Ref{RsSolveOpts},
+               Ref{RsSolveResult}), h.ptr, Float64(t0), Float64(t1), a, b, opts, r)
+    end
+    return (; retcode = rc == RS_OK ? :Success : :Failure, naT = Int(r.naT), nrT = Int(r.nrT),
+            naC = Int(r.naC), nrC = Int(r.nrC), nmacro = Int(r.nmacro),
+            nbisect = Int(r.nbisect), dtT = a[], dtC = b[])
+end
+
+# ---------------------------------------------------------------- discrete adjoint
+record!(h::Handle, on::Bool) =
+    check(h, ccall((:rs_record, LIB[]), Int32, (Ptr{Cvoid}, Int32), h.ptr, Int32(on)))
+record_count(h::Handle) = Int(ccall((:rs_record_count, LIB[]), Int32, (Ptr{Cvoid},), h.ptr))
+set_lambda!(h::Handle, lam::Vector{Float64}) =
+    check(h, ccall((:rs_adjoint_set_lambda, LIB[]), Int32, (Ptr{Cvoid}, Ptr{Float64}, Csize_t),
+                   h.ptr, lam, length(lam)))
+function get_lambda!(h::Handle, lam::Vector{Float64})
+    check(h, ccall((:rs_adjoint_get_lambda, LIB[]), Int32, (Ptr{Cvoid}, Ptr{Float64}, Csize_t),
+                   h.ptr, lam, length(lam)))
+    return lam
+end
+backward_macro_step!(h::Handle, k::Integer) =
+    check(h, ccall((:rs_backward_macro_step, LIB[]), Int32, (Ptr{Cvoid}, Int32), h.ptr, Int32(k)))
+function grad_emission!(h::Handle, g::Vector{Float64})
+    check(h, ccall((:rs_adjoint_get_grad_emission, LIB[]), Int32,
+                   (Ptr{Cvoid}, Ptr{Float64}, Csize_t), h.ptr, g, length(g)))
+    return g
+end
+reset_grad!(h::Handle) = check(h, ccall((:rs_adjoint_reset_grad, LIB[]), Int32, (Ptr{Cvoid},), h.ptr))
+
+"""
+    forward_with_pullback(h, u0, tspan; macro_dt, kwargs...)
+
+The windowed forward (lie_trotter_solve without bisection) recorded for the discrete adjoint,
+and its pullback: ū_end -> (ū_0, ē) with ē the gradient w.r.t. the emission forcing, by the
+library's backward sweep over the recorded macro steps (checkpoint + recomputation per step).
+This is what the ChainRulesCore rrule of the package extension returns.
+"""
+function forward_with_pullback(h::Handle, u0, tspan; kwargs...)
+    record!(h, true)
+    r = lie_trotter_solve(h, u0, tspan; kwargs...)
+    record!(h, false)
+    r.retcode == :Success || error("forward window failed; nothing to differentiate")
+    nrec = record_count(h)
+    function pullback(ubar_end::AbstractVector)
+        reset_grad!(h)
+        set_lambda!(h, collect(Float64, ubar_end))
+        for k in (nrec - 1):-1:0
+            backward_macro_step!(h, k)
+        end
+        ubar0 = get_lambda!(h, similar(collect(Float64, ubar_end)))
+        return ubar0
+    end
+    return r, pullback
+end
+
+# ---------------------------------------------------------------- kernel selection
+const RS_CHEM_KERNEL_AUTO = Int32(0)
+const RS_CHEM_KERNEL_TABLE = Int32(1)
+const RS_CHEM_KERNEL_SPECIALIZED = Int32(2)
+set_chem_kernel!(h::Handle, kind::Integer) =
+    check(h, ccall((:rs_set_chem_kernel, LIB[]), Int32, (Ptr{Cvoid}, Int32), h.ptr, Int32(kind)))
+function autotune!(h::Handle)
+    buf = Vector{UInt8}(undef, 16384)
+    check(h, ccall((:rs_autotune, LIB[]), Int32, (Ptr{Cvoid}, Ptr{UInt8}, Csize_t),
+                   h.ptr, buf, length(buf)))
+    return unsafe_string(pointer(buf))
+end
+
 end # module

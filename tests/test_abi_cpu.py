@@ -57,3 +57,34 @@ def test_null_arguments_rejected():
     assert L.rs_create(None, None) == abi.RS_ERR_INVALID
     assert L.rs_macro_step(None, 0.0, 1.0, None, None, None) == abi.RS_ERR_INVALID
     assert L.rs_state_size(None) == 0
+
+
+def test_ctypes_mirrors_match_the_header_layout(tmp_path):
+    """Every ctypes mirror of a header struct has the header's size and field offsets
+    (a small C program built with the host compiler prints them)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = {"rs_grid": abi.rs_grid, "rs_controller": abi.rs_controller,
+               "rs_mechanism": abi.rs_mechanism, "rs_config": abi.rs_config,
+               "rs_forcing": abi.rs_forcing, "rs_stats": abi.rs_stats,
+               "rs_solve_opts": abi.rs_solve_opts, "rs_solve_result": abi.rs_solve_result}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "reseact_gb300.h"',
+             'int main(void) {']
+    for name, cls in structs.items():
+        lines.append('  printf("%s %%zu\\n", sizeof(%s));' % (name, name))
+        for f in cls._fields_:
+            lines.append('  printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (name, f[0], name, f[0]))
+    lines.append('  return 0; }')
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = dict(l.split() for l in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                  check=True).stdout.splitlines())
+    for name, cls in structs.items():
+        assert int(out[name]) == C.sizeof(cls), name
+        for f in cls._fields_:
+            assert int(out["%s.%s" % (name, f[0])]) == getattr(cls, f[0]).offset, (name, f[0])
