@@ -212,10 +212,15 @@ class Solver:
         u = np.ascontiguousarray(u_cellmajor, dtype=np.float64)
         self._check(self.L.rs_set_state(self.h, _p(u), u.size))
 
-    def get_state(self):
-        u = np.empty(self.n)
-        self._check(self.L.rs_get_state(self.h, _p(u), u.size))
-        return u
+    def get_state(self, out=None):
+        """The cell-major state; into `out` (float64, C-contiguous, size n) when given, e.g. a
+        pinned host buffer, which the device then writes directly."""
+        if out is None:
+            out = np.empty(self.n)
+        elif out.dtype != np.float64 or not out.flags.c_contiguous or out.size != self.n:
+            raise ValueError("out must be a C-contiguous float64 array of size %d" % self.n)
+        self._check(self.L.rs_get_state(self.h, _p(out), out.size))
+        return out
 
     def rates(self):
         k = np.empty(self.nr * self.nc)

@@ -7,11 +7,12 @@
 // from J(u); for mass action that Hessian is exact and sparse (only reactant pairs of one
 // reaction), which is what replaces the reference's Enzyme second derivative.  PPM limiter
 // branches are frozen at the primal: the face value is then linear in its five stencil values
-// and its weights come from a forward-mode pass (Lin5) through the same reconstruction.
+// and its weights are assembled from the linear forms of the same reconstruction.
 // Sums are gathered per cell in a fixed order (no atomics): results are deterministic.
 #include <cuda_runtime.h>
 
 #include "rs_device.cuh"
+#include "rs_jit.h"
 #include "rs_kernels.h"
 
 namespace rs {
@@ -175,6 +176,10 @@ __global__ void __launch_bounds__(128) k_ros23_vjp(
 void launch_ros23_vjp(const LaunchCtx& L, const double* U, const double* Uout, const double* lam,
                       double* lam_out, const double* kr, const double* em, double* ebar,
                       double dt, int clamp) {
+  if (L.jit) {
+    jit_launch_vjp(*L.jit, L.stream, L.nc, L.nsp, U, Uout, lam, lam_out, kr, em, ebar, dt, clamp);
+    return;
+  }
   int nb = (L.nc + 127) / 128;
   if (L.size_class == 0)
     k_ros23_vjp<kSmallMS, kSmallMR, kSmallMLU, kSmallMP><<<nb, 128, 0, L.stream>>>(
@@ -185,87 +190,95 @@ void launch_ros23_vjp(const LaunchCtx& L, const double* U, const double* Uout, c
 }
 
 // ------------------------------------------------------------------ transport (K4)
-struct Lin5 {
-  double v, g[5];
-};
-__device__ __forceinline__ Lin5 l5(double v) {
-  Lin5 r;
-  r.v = v;
-  for (int o = 0; o < 5; ++o) r.g[o] = 0.0;
-  return r;
-}
-__device__ __forceinline__ Lin5 ladd(const Lin5& a, const Lin5& b) {
-  Lin5 r;
-  r.v = a.v + b.v;
-  for (int o = 0; o < 5; ++o) r.g[o] = a.g[o] + b.g[o];
-  return r;
-}
-__device__ __forceinline__ Lin5 lsub(const Lin5& a, const Lin5& b) {
-  Lin5 r;
-  r.v = a.v - b.v;
-  for (int o = 0; o < 5; ++o) r.g[o] = a.g[o] - b.g[o];
-  return r;
-}
-__device__ __forceinline__ Lin5 lscale(double c, const Lin5& a) {
-  Lin5 r;
-  r.v = c * a.v;
-  for (int o = 0; o < 5; ++o) r.g[o] = c * a.g[o];
-  return r;
-}
-__device__ __forceinline__ Lin5 labs5(const Lin5& a) { return a.v < 0.0 ? lscale(-1.0, a) : a; }
-__device__ __forceinline__ Lin5 lmin5(const Lin5& a, const Lin5& b) { return (b.v < a.v) ? b : a; }
-__device__ __forceinline__ Lin5 lcopysign5(const Lin5& mag, const Lin5& sgn) {
-  return (signbit(sgn.v) == signbit(mag.v)) ? mag : lscale(-1.0, mag);
-}
-__device__ __forceinline__ Lin5 lslope(const Lin5& am, const Lin5& a, const Lin5& ap, double sA,
-                                       double sB, bool uniform) {
-  Lin5 d0 = lsub(a, am), d1 = lsub(ap, a);
-  if (d1.v * d0.v > 0.0) {
-    Lin5 da = uniform ? lscale(0.5, lsub(ap, am)) : ladd(lscale(sA, d1), lscale(sB, d0));
-    Lin5 lim = lmin5(lscale(2.0, labs5(d0)), lscale(2.0, labs5(d1)));
-    return lcopysign5(lmin5(labs5(da), lim), da);
-  }
-  return l5(0.0);
-}
-__device__ __forceinline__ void llimit(const Lin5& a, Lin5& aL, Lin5& aR) {
-  if ((aR.v - a.v) * (a.v - aL.v) <= 0.0) {
-    aL = a;
-    aR = a;
-  } else {
-    double dA = aR.v - aL.v;
-    double a6 = 6.0 * (a.v - 0.5 * (aL.v + aR.v));
-    if (dA * a6 > dA * dA) aL = lsub(lscale(3.0, a), lscale(2.0, aR));
-    else if (-(dA * dA) > dA * a6) aR = lsub(lscale(3.0, a), lscale(2.0, aL));
-  }
-}
-// weights of the upwind face value w.r.t. the five stencil values; uniform (horizontal) or
-// dp-weighted (vertical: slope coefficients sA/sB of cells up-1..up+1, edge coefficients)
-__device__ __forceinline__ void face_weights(const double* v, bool right, bool uniform,
-                                             const double* sA, const double* sB,
-                                             const double* eL, const double* eR, double* w) {
-  Lin5 x[5];
-  for (int o = 0; o < 5; ++o) {
-    x[o] = l5(v[o]);
-    x[o].g[o] = 1.0;
-  }
-  const double k6 = 1.0 / 6.0;
-  Lin5 dm1 = lslope(x[0], x[1], x[2], sA[0], sB[0], uniform);
-  Lin5 d0 = lslope(x[1], x[2], x[3], sA[1], sB[1], uniform);
-  Lin5 dp1 = lslope(x[2], x[3], x[4], sA[2], sB[2], uniform);
-  Lin5 aL, aR;
+// Weights of the upwind face value w.r.t. the five stencil values (uniform horizontally,
+// dp-weighted vertically).  With the branch decisions frozen at the forward state, every
+// quantity of the reconstruction is a linear form in the five stencil values: a limited slope
+// is 0 (extremum) or exactly one of da, +-2 d0, +-2 d1 (the smallest, with da's sign); the
+// edges and the CW84 limiter combine those.  The value-level decisions use the forward
+// kernels' expressions; only the coefficients are carried, about a quarter of the FP64 work of
+// a forward-mode pass with five tangents (the oracle's restatement, which the tests compare).
+__device__ __forceinline__ void slope_form(double am, double a, double ap, double sA, double sB,
+                                           bool uniform, double& val, double c[3]) {
+  c[0] = c[1] = c[2] = 0.0;
+  val = 0.0;
+  const double d0 = a - am, d1 = ap - a;
+  if (!(d1 * d0 > 0.0)) return;
+  double da, f[3];
   if (uniform) {
-    aL = lsub(ladd(x[1], lscale(0.5, lsub(x[2], x[1]))), lscale(k6, lsub(d0, dm1)));
-    aR = lsub(ladd(x[2], lscale(0.5, lsub(x[3], x[2]))), lscale(k6, lsub(dp1, d0)));
+    da = 0.5 * (ap - am);
+    f[0] = -0.5; f[1] = 0.0; f[2] = 0.5;
   } else {
-    aL = ladd(ladd(ladd(x[1], lscale(eL[0], lsub(x[2], x[1]))), lscale(eL[1], d0)),
-              lscale(eL[2], dm1));
-    aR = ladd(ladd(ladd(x[2], lscale(eR[0], lsub(x[3], x[2]))), lscale(eR[1], dp1)),
-              lscale(eR[2], d0));
+    da = sA * d1 + sB * d0;
+    f[0] = -sB; f[1] = sB - sA; f[2] = sA;
   }
-  llimit(x[2], aL, aR);
-  const Lin5& r = right ? aR : aL;
-  for (int o = 0; o < 5; ++o) w[o] = r.g[o];
+  const double a0 = d0 < 0.0 ? -d0 : d0, a1 = d1 < 0.0 ? -d1 : d1, ada = da < 0.0 ? -da : da;
+  const double l0 = 2.0 * a0, l1 = 2.0 * a1;
+  const bool pick1 = l1 < l0;                    // lim = min(2|d0|, 2|d1|) as lmin5
+  const double lim = pick1 ? l1 : l0;
+  const double sg = signbit(da) ? -1.0 : 1.0;     // copysign onto da
+  if (lim < ada) {                                // the limit binds
+    if (pick1) {
+      const double m = (d1 < 0.0 ? -2.0 : 2.0) * sg;
+      c[1] = -m; c[2] = m;
+    } else {
+      const double m = (d0 < 0.0 ? -2.0 : 2.0) * sg;
+      c[0] = -m; c[1] = m;
+    }
+    val = sg * lim;
+  } else {
+    const double m = (da < 0.0 ? -1.0 : 1.0) * sg;  // |da| carried back onto da's sign
+    c[0] = m * f[0]; c[1] = m * f[1]; c[2] = m * f[2];
+    val = sg * ada;
+  }
 }
+__device__ __forceinline__ void face_weights_lin(const double* v, bool right, bool uniform,
+                                                 const double* sA, const double* sB,
+                                                 const double* eL, const double* eR, double* w) {
+  double vm1, vd0, vp1, cm1[3], c0[3], cp1[3];
+  slope_form(v[0], v[1], v[2], sA[0], sB[0], uniform, vm1, cm1);  // cell up-1: positions 0..2
+  slope_form(v[1], v[2], v[3], sA[1], sB[1], uniform, vd0, c0);   // cell up:   positions 1..3
+  slope_form(v[2], v[3], v[4], sA[2], sB[2], uniform, vp1, cp1);  // cell up+1: positions 2..4
+  const double k6 = 1.0 / 6.0;
+  double L[5] = {0, 0, 0, 0, 0}, R[5] = {0, 0, 0, 0, 0}, aLv, aRv;
+  if (uniform) {
+    aLv = (v[1] + 0.5 * (v[2] - v[1])) - k6 * (vd0 - vm1);
+    aRv = (v[2] + 0.5 * (v[3] - v[2])) - k6 * (vp1 - vd0);
+    L[1] = 0.5; L[2] = 0.5;
+    R[2] = 0.5; R[3] = 0.5;
+    for (int o = 0; o < 3; ++o) {
+      L[1 + o] -= k6 * c0[o];
+      L[o] += k6 * cm1[o];
+      R[2 + o] -= k6 * cp1[o];
+      R[1 + o] += k6 * c0[o];
+    }
+  } else {
+    aLv = ((v[1] + eL[0] * (v[2] - v[1])) + eL[1] * vd0) + eL[2] * vm1;
+    aRv = ((v[2] + eR[0] * (v[3] - v[2])) + eR[1] * vp1) + eR[2] * vd0;
+    L[1] = 1.0 - eL[0]; L[2] = eL[0];
+    R[2] = 1.0 - eR[0]; R[3] = eR[0];
+    for (int o = 0; o < 3; ++o) {
+      L[1 + o] += eL[1] * c0[o];
+      L[o] += eL[2] * cm1[o];
+      R[2 + o] += eR[1] * cp1[o];
+      R[1 + o] += eR[2] * c0[o];
+    }
+  }
+  const double a = v[2];
+  if ((aRv - a) * (a - aLv) <= 0.0) {  // extremum: flat at the cell value
+    for (int o = 0; o < 5; ++o) w[o] = o == 2 ? 1.0 : 0.0;
+    return;
+  }
+  const double dA = aRv - aLv;
+  const double a6 = 6.0 * (a - 0.5 * (aLv + aRv));
+  if (dA * a6 > dA * dA) {             // aL = 3a - 2aR
+    for (int o = 0; o < 5; ++o) L[o] = (o == 2 ? 3.0 : 0.0) - 2.0 * R[o];
+  } else if (-(dA * dA) > dA * a6) {   // aR = 3a - 2aL
+    for (int o = 0; o < 5; ++o) R[o] = (o == 2 ? 3.0 : 0.0) - 2.0 * L[o];
+  }
+  const double* r = right ? R : L;
+  for (int o = 0; o < 5; ++o) w[o] = r[o];
+}
+
 
 // index maps of a stencil position p along a direction -> position in range, or -1 (open ghost)
 __device__ __forceinline__ int map_pos(int p, int n, int bc) {
@@ -386,7 +399,7 @@ __global__ void __launch_bounds__(256) k_adj_face(DevTransport<double> T, const 
         else v[o] = (p < 0 ? T.qs : T.qn)[((size_t)s * T.nlev + k) * T.nlon + i];
       }
     }
-    face_weights(v, right, DIR != 2, sA, sB, eL, eR, w);
+    face_weights_lin(v, right, DIR != 2, sA, sB, eL, eR, w);
     double Fb = 0.0;
     if (cb >= 0) Fb = Fb - G[(size_t)s * nc + cb] * cbw;
     if (ca >= 0) Fb = Fb + G[(size_t)s * nc + ca] * caw;

@@ -1519,14 +1519,19 @@ rs_status rs_backward_macro_step(rs_handle* h, int32_t k) {
     const auto& r = h->recs[k];
     size_t n = h->nc * h->nsp;
     int nT = (int)(r.seqT.size() / 2), nC = (int)(r.seqC.size() / 2);
-    h->tape.alloc((size_t)(nT + nC + 2) * n);
+    // one tape for the largest recorded macro step (no reallocation during a sweep)
+    size_t most = 0;
+    for (const auto& q : h->recs) most = std::max(most, (q.seqT.size() + q.seqC.size()) / 2);
+    h->tape.alloc((most + 2) * n);
     double* tape = h->tape.p;
     double* R[2] = {tape + (size_t)(nT + nC) * n, tape + (size_t)(nT + nC + 1) * n};
     cudaStream_t st = h->st;
     const int clamp = h->cfg.clamp_nonneg;
     // ---- fixed-sequence replay from the checkpoint, keeping every step's input
-    CK(cudaMemcpyAsync(R[0], r.ck.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
     int cur = 0;
+    {
+    Scope sc_replay(h, "adj_replay");
+    CK(cudaMemcpyAsync(R[0], r.ck.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
     Ctl* c = h->ctl.p + 2;
     double ntot = (double)n;
     for (int j = 0; j < nT + nC; ++j) {
@@ -1550,12 +1555,14 @@ rs_status rs_backward_macro_step(rs_handle* h, int32_t k) {
       rs::launch_replay_accept(st, c);
       cur ^= 1;
     }
+    }
     // the final replayed state closes the tape (output of the last step)
     double* fin = R[cur];
     auto out_of = [&](int j) -> const double* {
       return (j + 1 < nT + nC) ? tape + (size_t)(j + 1) * n : fin;
     };
     // ---- chemistry steps in reverse, then transport steps in reverse
+    { Scope sc_vjp(h, "adj_chem_vjp");
     for (int j = nC - 1; j >= 0; --j) {
       int jj = nT + j;
       rs::launch_ros23_vjp(h->lc, tape + (size_t)jj * n, clamp ? out_of(jj) : nullptr, h->lam.p,
@@ -1563,6 +1570,8 @@ rs_status rs_backward_macro_step(rs_handle* h, int32_t k) {
                            h->ebar.p, r.seqC[2 * j + 1], clamp);
       std::swap(h->lam.p, h->lam2.p);
     }
+    }
+    Scope sc_tvjp(h, "adj_transport_vjp");
     for (int j = nT - 1; j >= 0; --j) {
       if (clamp) rs::launch_clamp_mask(st, n, h->lam.p, out_of(j));
       transport_step_vjp(h, tape + (size_t)j * n, r.seqT[2 * j], r.seqT[2 * j + 1], h->lam.p,

@@ -141,7 +141,7 @@ struct Gen {
         << ") : a_; }\n";
     }
   }
-  void partials() {
+  void partials(const char* xa = "x", const char* Pa = "P") {
     for (int p = 0; p < T.npart; ++p) {
       int r = T.part_r[p], qs = T.part_q[p];
       std::ostringstream d;
@@ -152,14 +152,14 @@ struct Gen {
           if (nu >= 2) {
             std::ostringstream f;
             f << lit((double)nu);
-            for (int t = 1; t < nu; ++t) f << "*x[" << s << "]";
+            for (int t = 1; t < nu; ++t) f << "*" << xa << "[" << s << "]";
             d << "*(" << f.str() << ")";
           }
         } else {
-          for (int t = 0; t < nu; ++t) d << "*x[" << s << "]";
+          for (int t = 0; t < nu; ++t) d << "*" << xa << "[" << s << "]";
         }
       }
-      o << "  P[" << p << "] = " << d.str() << ";\n";
+      o << "  " << Pa << "[" << p << "] = " << d.str() << ";\n";
     }
   }
   void build_w() {
@@ -194,6 +194,88 @@ struct Gen {
       }
     }
   }
+  // W^T x = b in place with the same factors: U^T then L^T (the table kernels' lu_solve_T)
+  void lu_solve_T(const char* b) {
+    for (int j = 0; j < T.ns; ++j) {
+      const int sj = T.ord[j];
+      if (strict)
+        o << "  { const double tj = " << b << "[" << sj << "] / WV(" << T.lu_diag[j] << ");\n";
+      else
+        o << "  { const double tj = " << b << "[" << sj << "] * pv[" << j << "];\n";
+      o << "    " << b << "[" << sj << "] = tj;\n";
+      for (int e = T.up_ptr[j]; e < T.up_ptr[j + 1]; ++e)
+        o << "    " << b << "[" << T.up_col[e] << "] = RS_FMA(-WV(" << T.up_slot[e] << "), tj, " << b
+          << "[" << T.up_col[e] << "]);\n";
+      o << "  }\n";
+    }
+    for (int k = T.ns - 1; k >= 0; --k) {
+      const int sk = T.ord[k];
+      std::string acc = std::string(b) + "[" + std::to_string(sk) + "]";
+      for (int e = T.low_ptr[k]; e < T.low_ptr[k + 1]; ++e)
+        acc = "RS_FMA(-WV(" + std::to_string(T.low_slot[e]) + "), " + b + "[" +
+              std::to_string(T.low_row[e]) + "], " + acc + ")";
+      o << "  " << b << "[" << sk << "] = " << acc << ";\n";
+    }
+  }
+  // a_r = sum_s net[r,s] y_s, species ascending within each reaction (the tables' order)
+  void reaction_sums(const char* y, const char* a) {
+    std::vector<std::vector<std::pair<int, double>>> per(T.nr);
+    for (int sp = 0; sp < T.ns; ++sp)
+      for (int t = T.rhs_ptr[sp]; t < T.rhs_ptr[sp + 1]; ++t)
+        per[T.rhs_r[t]].push_back({sp, T.rhs_c[t]});
+    for (int r = 0; r < T.nr; ++r) {
+      std::ostringstream e;
+      bool first = true;
+      for (auto& tc : per[r]) {
+        sum_terms(e, first, tc.second, std::string(y) + "[" + std::to_string(tc.first) + "]");
+        first = false;
+      }
+      o << "  " << a << "[" << r << "] = " << (first ? std::string("0.0") : e.str()) << ";\n";
+    }
+  }
+  // out += J^T y from the partials Pa (a: scratch for the reaction sums)
+  void jt_apply(const char* Pa, const char* y, const char* a, const char* out) {
+    reaction_sums(y, a);
+    for (int p = 0; p < T.npart; ++p)
+      o << "  " << out << "[" << T.part_q[p] << "] = RS_FMA(" << a << "[" << T.part_r[p] << "], "
+        << Pa << "[" << p << "], " << out << "[" << T.part_q[p] << "]);\n";
+  }
+  // exact mass-action Hessian term of the ROS23 VJP: for every reaction r and reactant entries
+  // j, q: ub_q += dtg (a1_r z2_j + a0_r k1_j) d2v_r/dx_j dx_q (structural zeros skipped)
+  void hessian() {
+    for (int r = 0; r < T.nr; ++r)
+      for (int ea = T.rptr[r]; ea < T.rptr[r + 1]; ++ea) {
+        const int j = T.rsp[ea];
+        bool any = false;
+        std::ostringstream body;
+        for (int eb = T.rptr[r]; eb < T.rptr[r + 1]; ++eb) {
+          const int q = T.rsp[eb];
+          std::ostringstream d;
+          d << "K(" << r << ")";
+          bool zero = false;
+          for (int e = T.rptr[r]; e < T.rptr[r + 1]; ++e) {
+            const int sp = T.rsp[e], nu = T.rnu[e];
+            const int order = (sp == j) + (sp == q);
+            if (order > nu) { zero = true; break; }
+            double cst = 1.0;
+            for (int t = 0; t < order; ++t) cst *= (double)(nu - t);
+            const int m = nu - order;
+            if (cst == 1.0 && m == 0) continue;
+            std::ostringstream c;
+            if (cst != 1.0) c << lit(cst);
+            for (int t = 0; t < m; ++t) c << ((cst != 1.0 || t > 0) ? "*" : "") << "x[" << sp << "]";
+            d << "*(" << c.str() << ")";
+          }
+          if (zero) continue;
+          any = true;
+          body << "    ub[" << q << "] = RS_FMA(gj, " << d.str() << ", ub[" << q << "]);\n";
+        }
+        if (!any) continue;
+        o << "  { const double gj = dtg * RS_FMA(a0[" << r << "], k1[" << j << "], a1[" << r
+          << "] * z2[" << j << "]);\n" << body.str() << "  }\n";
+      }
+  }
+
   // pivots in elimination order, vector entries by species index (T.ord maps the two)
   void lu_solve(const char* b) {
     for (int k = 0; k < T.ns; ++k)
@@ -518,6 +600,99 @@ RS_ATTEMPT(rs_jit_attempt_q1, true, false, 2)
 RS_PER_CELL(rs_jit_per_cell_0, false)
 RS_PER_CELL(rs_jit_per_cell_1, true)
 
+// VJP of one ROS23 step at a recorded dt (the table kernel k_ros23_vjp, specialised): forward
+// recompute of the live stages, then lam_out = (d unew / d u)^T lam and ebar += d J / d emission
+template <bool HE>
+__device__ __forceinline__ void vjp_body(int nc, int nsp, const double* __restrict__ U,
+    const double* __restrict__ Uout, const double* __restrict__ lam,
+    double* __restrict__ lam_out, const double* __restrict__ kr,
+    const double* __restrict__ em, double* __restrict__ ebar, double dt, int clamp) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  const u64 N = (u64)nc;
+  const double dto2 = dt / 2, dtg = dt * ROS_D;
+#define K(r) __ldg(kr + (u64)(r) * N + c)
+#define EM(s) __ldg(em + (u64)(s) * N + c)
+#define WV(e) W[(e)]
+  double x[NS], f0[NS], k1[NS], u1[NS], f1[NS], z2[NS], bb[NS], f0b[NS], f1b[NS], ub[NS], pv[NS];
+  double v[NRA], a0[NRA], a1[NRA], P[NPA], P1[NPA], W[NLU];
+#pragma unroll
+  for (int s = 0; s < NS; ++s) x[s] = U[(u64)s * N + c];
+)";
+  o << "  {\n";
+  g.vel("x");
+  g.rhs("f0");
+  o << "  }\n";
+  g.partials("x", "P");
+  g.build_w();
+  g.lu_factor();
+  o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) k1[s] = f0[s];\n";
+  g.lu_solve("k1");
+  o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) u1[s] = RS_FMA(dto2, k1[s], x[s]);\n";
+  o << "  {\n";
+  g.vel("u1");
+  g.rhs("f1");
+  o << "  }\n";
+  g.partials("u1", "P1");
+  o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) z2[s] = f1[s] - k1[s];\n";
+  g.lu_solve("z2");
+  o << R"(#pragma unroll
+  for (int s = 0; s < NS; ++s) {
+    double l = lam[(u64)s * N + c];
+    if (clamp && Uout && !(Uout[(u64)s * N + c] > 0.0)) l = 0.0;
+    ub[s] = l;
+    bb[s] = dt * l;
+  }
+)";
+  g.lu_solve_T("bb");
+  o << R"(#pragma unroll
+  for (int s = 0; s < NS; ++s) {
+    f1b[s] = bb[s];
+    f0b[s] = RS_FMA(dt, ub[s], -bb[s]);
+  }
+  {
+    double u1b[NS];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) u1b[s] = 0.0;
+)";
+  g.jt_apply("P1", "f1b", "a0", "u1b");
+  o << R"(#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+      ub[s] = ub[s] + u1b[s];
+      f0b[s] = RS_FMA(dto2, u1b[s], f0b[s]);
+    }
+  }
+)";
+  g.lu_solve_T("f0b");
+  g.jt_apply("P", "f0b", "a0", "ub");
+  g.reaction_sums("bb", "a1");
+  g.reaction_sums("f0b", "a0");
+  g.hessian();
+  o << R"(#pragma unroll
+  for (int s = 0; s < NS; ++s) {
+    lam_out[(u64)s * N + c] = ub[s];
+    if (ebar) ebar[(u64)s * N + c] += f0b[s] + f1b[s];
+  }
+  for (int s = NS; s < nsp; ++s) {
+    double l = lam[(u64)s * N + c];
+    if (clamp && Uout && !(Uout[(u64)s * N + c] > 0.0)) l = 0.0;
+    lam_out[(u64)s * N + c] = l;
+  }
+#undef K
+#undef EM
+#undef WV
+}
+#define RS_VJP(NAME, HE)                                                                     \
+  extern "C" __global__ void __launch_bounds__(128) NAME(int nc, int nsp,                   \
+      const double* __restrict__ U, const double* __restrict__ Uout,                        \
+      const double* __restrict__ lam, double* __restrict__ lam_out,                         \
+      const double* __restrict__ kr, const double* __restrict__ em,                         \
+      double* __restrict__ ebar, double dt, int clamp) {                                     \
+    vjp_body<HE>(nc, nsp, U, Uout, lam, lam_out, kr, em, ebar, dt, clamp);                   \
+  }
+RS_VJP(rs_jit_vjp_0, false)
+RS_VJP(rs_jit_vjp_1, true)
+
 // the production reciprocal applied elementwise (accuracy check against IEEE division)
 extern "C" __global__ void rs_jit_rcp(const double* __restrict__ x, double* __restrict__ r,
                                       int n) {
@@ -645,7 +820,8 @@ std::shared_ptr<JitChem> jit_chem_build(const MechTables& T, double ros_d, doubl
   bool ok = get(&J->attempt[0][0], "rs_jit_attempt_r0") && get(&J->attempt[0][1], "rs_jit_attempt_r1") &&
             get(&J->attempt[2][0], "rs_jit_attempt_q0") && get(&J->attempt[2][1], "rs_jit_attempt_q1") &&
             get(&J->per_cell[0], "rs_jit_per_cell_0") && get(&J->per_cell[1], "rs_jit_per_cell_1") &&
-            get(&J->rcp, "rs_jit_rcp");
+            get(&J->rcp, "rs_jit_rcp") && get(&J->vjp[0], "rs_jit_vjp_0") &&
+            get(&J->vjp[1], "rs_jit_vjp_1");
   if (!ok) return nullptr;
   if (with_smem && get(&J->attempt[1][0], "rs_jit_attempt_s0") &&
       get(&J->attempt[1][1], "rs_jit_attempt_s1")) {
@@ -690,6 +866,14 @@ void jit_launch_attempt(const JitChem& J, cudaStream_t st, int nc, int nsp, cons
 void jit_launch_rcp(const JitChem& J, cudaStream_t st, const double* x, double* r, int n) {
   void* args[] = {&x, &r, &n};
   cudaLaunchKernel((const void*)J.rcp, dim3((n + 255) / 256), dim3(256), args, 0, st);
+}
+
+void jit_launch_vjp(const JitChem& J, cudaStream_t st, int nc, int nsp, const double* U,
+                    const double* Uout, const double* lam, double* lam_out, const double* kr,
+                    const double* em, double* ebar, double dt, int clamp) {
+  cudaKernel_t k = J.vjp[em ? 1 : 0];
+  void* args[] = {&nc, &nsp, &U, &Uout, &lam, &lam_out, &kr, &em, &ebar, &dt, &clamp};
+  cudaLaunchKernel((const void*)k, dim3((nc + 127) / 128), dim3(128), args, 0, st);
 }
 
 void jit_launch_per_cell(const JitChem& J, cudaStream_t st, int nc, int nsp, int nblocks,

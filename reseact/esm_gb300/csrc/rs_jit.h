@@ -32,6 +32,7 @@ struct JitChem {
   cudaKernel_t attempt[kJitVariants][2] = {};  // [variant][has emission]; null: not built
   cudaKernel_t per_cell[2] = {};               // [has emission]
   cudaKernel_t rcp = nullptr;                  // elementwise production reciprocal
+  cudaKernel_t vjp[2] = {};                    // ROS23 step VJP [has emission]
   size_t attempt_smem = 0;  // dynamic shared bytes of the shared-memory variant
   int variant = 0;          // variant used for global-dt attempts
   double compile_ms = 0;    // NVRTC time (0 when the compiled image came from cache)
@@ -61,6 +62,10 @@ void jit_launch_attempt(const JitChem& J, cudaStream_t st, int nc, int nsp, cons
                         double* part, double rtol, double atol, int clamp, double* F0,
                         double* F1);
 void jit_launch_rcp(const JitChem& J, cudaStream_t st, const double* x, double* r, int n);
+// same contract as launch_ros23_vjp in rs_kernels.h
+void jit_launch_vjp(const JitChem& J, cudaStream_t st, int nc, int nsp, const double* U,
+                    const double* Uout, const double* lam, double* lam_out, const double* kr,
+                    const double* em, double* ebar, double dt, int clamp);
 void jit_launch_per_cell(const JitChem& J, cudaStream_t st, int nc, int nsp, int nblocks,
                          int threads, double* U, const double* kr, const double* em,
                          double* dtc, double* steps, unsigned long long* queue, int* status,

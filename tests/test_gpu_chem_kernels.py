@@ -165,3 +165,33 @@ def test_production_reciprocal_within_two_ulp():
     ulp = np.abs(r - ref) / np.spacing(ref)
     assert ulp.max() <= 2.0, ulp.max()
     assert np.mean(r == ref) > 0.5  # mostly the correctly rounded value
+
+
+@pytest.mark.parametrize("strict", [False, True])
+def test_adjoint_specialised_vs_table(strict):
+    """The specialised ROS23 step VJP (forward recompute, W^T solves, J^T products, the exact
+    mass-action Hessian) against the table kernel over a recorded sweep: the strict build
+    identical bits, the production build to roundoff."""
+    w = _small_c2(emission=True)
+    g = w.grid
+    out = []
+    for kind in (CHEM_KERNEL_TABLE, CHEM_KERNEL_SPECIALIZED):
+        s = Solver.for_workload(w, strict=strict, do_transport=False)
+        s.set_chem_kernel(kind)
+        s.set_state(w.u0_cellmajor())
+        s.record(True)
+        t, a, b = 0.0, 15.0, 0.5
+        for _ in range(2):
+            _, a, b, _ = s.macro_step(t, t + 600.0, a, b)
+            t += 600.0
+        s.record(False)
+        lam = np.zeros(s.n)
+        lam[w.mech.species.index("O3")::w.nsp] = 1.0
+        out.append(s.adjoint_backward(lam))
+        s.close()
+    (la, ea), (lb, eb) = out
+    if strict:
+        assert np.array_equal(la, lb) and np.array_equal(ea, eb)
+    else:
+        assert np.abs(lb - la).max() <= 1e-10 * np.abs(la).max()
+        assert np.abs(eb - ea).max() <= 1e-10 * np.abs(ea).max()
