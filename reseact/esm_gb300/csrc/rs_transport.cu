@@ -530,6 +530,237 @@ __global__ void __launch_bounds__(512) k_flux_z_fused(DevTransport<double> T, St
   }
 }
 
+// ------------------------------------------------------------------ mixed-precision pencils
+// FP32 reconstruction once per cell (instead of per face): a pencil stages the split state
+// (hi, lo planes) in shared memory, forms the neighbour differences
+//   dl_p = (hi_{p+1} - hi_p) + (lo_{p+1} - lo_p)          (exact hi differences of nearby values)
+// and each cell's monotone slope from them; a face then needs only the upwind cell's two edge
+// DEVIATIONS (translation invariance of PPM: the value of the upwind cell is 0)
+//   uniform:  aL = -dl_{up-1}/2 - (S_up - S_{up-1})/6,  aR = dl_up/2 - (S_{up+1} - S_up)/6
+//   dp-weighted (edge e between cells e-1, e with coefficients ab, c, d):
+//             aL = (ab_up - 1) dl_{up-1} + c_up S_up + d_up S_{up-1}
+//             aR = ab_{up+1} dl_up + c_{up+1} S_{up+1} + d_{up+1} S_up
+// the CW84 limiter on (0, aL, aR), and the face value a_up + dev in FP64.  q == 1 gives dl = 0,
+// S = 0, dev = 0 and a face of exactly 1 (the freestream stays exact).
+__device__ __forceinline__ float slope_from_diff(float d0, float d1) {
+  if (d1 * d0 > 0.0f) {
+    const float da = 0.5f * (d0 + d1);
+    const float lim = 2.0f * fminf(fabsf(d0), fabsf(d1));
+    return copysignf(fminf(fabsf(da), lim), da);
+  }
+  return 0.0f;
+}
+__device__ __forceinline__ float slope_from_diff_n(float d0, float d1, float sA, float sB) {
+  if (d1 * d0 > 0.0f) {
+    const float da = sA * d1 + sB * d0;
+    const float lim = 2.0f * fminf(fabsf(d0), fabsf(d1));
+    return copysignf(fminf(fabsf(da), lim), da);
+  }
+  return 0.0f;
+}
+
+__global__ void __launch_bounds__(256) k_flux_x_mixed(DevTransport<double> T, StageSel sel) {
+  const double* Q;
+  double g;
+  if (!resolve_stage(sel, Q, g)) return;
+  extern __shared__ double smm[];
+  const int n = T.nlon, nf = n + 1, L = n + 6;
+  double* Mf = smm;                                   // [n+1] face air-mass flux
+  float* H = reinterpret_cast<float*>(smm + nf);      // H[p+3], p in [-3, n+2]
+  float* Lo = H + L;
+  float* Dl = Lo + L;                                  // Dl[p+3] = v(p+1) - v(p), p in [-3, n+1]
+  float* S = Dl + L;                                   // S[p+3], slopes of cells p in [-2, n+1]
+  const int row = blockIdx.x;
+  const int j = row % T.nlat, k = row / T.nlat;
+  const size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
+  const size_t rbase = ((size_t)k * T.nlat + j) * n;
+  const bool periodic = T.lon_bc == 0;
+  for (int f = threadIdx.x; f <= n; f += blockDim.x) Mf[f] = g * T.mx[((size_t)k * T.nlat + j) * nf + f];
+  for (int s = 0; s < T.ntr; ++s) {
+    const size_t pb = (size_t)s * nc + rbase;
+    for (int p = threadIdx.x - 3; p <= n + 2; p += blockDim.x) {
+      float h, l;
+      if (p < 0 || p >= n) {
+        if (periodic) {
+          const int q = ((p % n) + n) % n;
+          h = T.qhi[pb + q];
+          l = T.qlo[pb + q];
+        } else {
+          split_d((p < 0 ? T.qw : T.qe)[((size_t)s * T.nlev + k) * T.nlat + j], h, l);
+        }
+      } else {
+        h = T.qhi[pb + p];
+        l = T.qlo[pb + p];
+      }
+      H[p + 3] = h;
+      Lo[p + 3] = l;
+    }
+    __syncthreads();
+    for (int p = threadIdx.x - 3; p <= n + 1; p += blockDim.x)
+      Dl[p + 3] = (H[p + 4] - H[p + 3]) + (Lo[p + 4] - Lo[p + 3]);
+    __syncthreads();
+    for (int p = threadIdx.x - 2; p <= n + 1; p += blockDim.x) S[p + 3] = slope_from_diff(Dl[p + 2], Dl[p + 3]);
+    __syncthreads();
+    for (int f = threadIdx.x; f <= n; f += blockDim.x) {
+      const double M = Mf[f];
+      const bool right = __double_as_longlong(M) > 0;
+      const int up = right ? f - 1 : f;
+      float aL = -0.5f * Dl[up + 2] - (S[up + 3] - S[up + 2]) * (1.0f / 6.0f);
+      float aR = 0.5f * Dl[up + 3] - (S[up + 4] - S[up + 3]) * (1.0f / 6.0f);
+      limitf(0.0f, aL, aR);
+      double a2;
+      if (up >= 0 && up < n) a2 = Q[pb + up];
+      else if (periodic) a2 = Q[pb + (up < 0 ? n - 1 : 0)];
+      else a2 = (double)H[up + 3] + (double)Lo[up + 3];
+      T.fx[((size_t)s * T.nlev * T.nlat + (size_t)k * T.nlat + j) * nf + f] =
+          M * (a2 + (double)(right ? aR : aL));
+    }
+    __syncthreads();
+  }
+}
+
+template <int kPencil>
+__global__ void __launch_bounds__(512) k_flux_y_mixed(DevTransport<double> T, StageSel sel) {
+  const double* Q;
+  double g;
+  if (!resolve_stage(sel, Q, g)) return;
+  extern __shared__ double smym[];
+  const int n = T.nlat, nfj = n + 1, L = n + 6;
+  double* Mf = smym;                                         // [n+1][kPencil]
+  float* H = reinterpret_cast<float*>(smym + nfj * kPencil);  // [L][kPencil]
+  float* Lo = H + L * kPencil;
+  float* Dl = Lo + L * kPencil;
+  float* S = Dl + L * kPencil;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int ntile = (T.nlon + kPencil - 1) / kPencil;
+  const int k = blockIdx.x / ntile;
+  const int i = (blockIdx.x % ntile) * kPencil + tx;
+  const bool live = i < T.nlon;
+  const size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
+  const size_t fplane = (size_t)T.nlev * nfj * T.nlon;
+  const bool open = T.lat_bc == 1;
+  if (live)
+    for (int f = ty; f <= n; f += blockDim.y)
+      Mf[f * kPencil + tx] = g * T.my[((size_t)k * nfj + f) * T.nlon + i];
+  for (int s = 0; s < T.ntr; ++s) {
+    const size_t pb = (size_t)s * nc + (size_t)k * T.nlat * T.nlon;
+    for (int p = (int)ty - 3; p <= n + 2; p += blockDim.y) {
+      float h = 0.0f, l = 0.0f;
+      if (live) {
+        if (p < 0 || p >= n) {
+          if (open) {
+            split_d((p < 0 ? T.qs : T.qn)[((size_t)s * T.nlev + k) * T.nlon + i], h, l);
+          } else {
+            const size_t q = (size_t)(p < 0 ? -1 - p : 2 * n - 1 - p) * T.nlon + i;
+            h = T.qhi[pb + q];
+            l = T.qlo[pb + q];
+          }
+        } else {
+          h = T.qhi[pb + (size_t)p * T.nlon + i];
+          l = T.qlo[pb + (size_t)p * T.nlon + i];
+        }
+      }
+      H[(p + 3) * kPencil + tx] = h;
+      Lo[(p + 3) * kPencil + tx] = l;
+    }
+    __syncthreads();
+    for (int p = (int)ty - 3; p <= n + 1; p += blockDim.y)
+      Dl[(p + 3) * kPencil + tx] = (H[(p + 4) * kPencil + tx] - H[(p + 3) * kPencil + tx]) +
+                                   (Lo[(p + 4) * kPencil + tx] - Lo[(p + 3) * kPencil + tx]);
+    __syncthreads();
+    for (int p = (int)ty - 2; p <= n + 1; p += blockDim.y)
+      S[(p + 3) * kPencil + tx] = slope_from_diff(Dl[(p + 2) * kPencil + tx], Dl[(p + 3) * kPencil + tx]);
+    __syncthreads();
+    if (live) {
+      for (int f = ty; f <= n; f += blockDim.y) {
+        const size_t fb = ((size_t)k * nfj + f) * T.nlon + i;
+        if (!open && (f == 0 || f == n)) {
+          T.fy[(size_t)s * fplane + fb] = 0.0;
+          continue;
+        }
+        const double M = Mf[f * kPencil + tx];
+        const bool right = __double_as_longlong(M) > 0;
+        const int up = right ? f - 1 : f;
+        float aL = -0.5f * Dl[(up + 2) * kPencil + tx] -
+                   (S[(up + 3) * kPencil + tx] - S[(up + 2) * kPencil + tx]) * (1.0f / 6.0f);
+        float aR = 0.5f * Dl[(up + 3) * kPencil + tx] -
+                   (S[(up + 4) * kPencil + tx] - S[(up + 3) * kPencil + tx]) * (1.0f / 6.0f);
+        limitf(0.0f, aL, aR);
+        const double a2 = (up >= 0 && up < n) ? Q[pb + (size_t)up * T.nlon + i]
+                        : (double)H[(up + 3) * kPencil + tx] + (double)Lo[(up + 3) * kPencil + tx];
+        T.fy[(size_t)s * fplane + fb] = M * (a2 + (double)(right ? aR : aL));
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <int kPencil>
+__global__ void __launch_bounds__(512) k_flux_z_mixed(DevTransport<double> T, StageSel sel) {
+  const double* Q;
+  double g;
+  if (!resolve_stage(sel, Q, g)) return;
+  extern __shared__ double smzm[];
+  const int n = T.nlev, L = n + 6;
+  double* Mf = smzm;                                          // [n+1][kPencil]
+  float* H = reinterpret_cast<float*>(smzm + (n + 1) * kPencil);
+  float* Lo = H + L * kPencil;
+  float* Dl = Lo + L * kPencil;
+  float* S = Dl + L * kPencil;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const size_t ncol = (size_t)T.nlon * T.nlat;
+  const size_t col = (size_t)blockIdx.x * kPencil + tx;
+  const bool live = col < ncol;
+  const size_t nc = ncol * n;
+  const size_t fplane = ncol * (n + 1);
+  if (live)
+    for (int kf = ty; kf <= n; kf += blockDim.y) Mf[kf * kPencil + tx] = g * T.mz[(size_t)kf * ncol + col];
+  for (int s = 0; s < T.ntr; ++s) {
+    const size_t pb = (size_t)s * nc + col;
+    for (int p = (int)ty - 3; p <= n + 2; p += blockDim.y) {
+      const int pp = p < 0 ? -1 - p : (p >= n ? 2 * n - 1 - p : p);
+      H[(p + 3) * kPencil + tx] = live ? T.qhi[pb + (size_t)pp * ncol] : 0.0f;
+      Lo[(p + 3) * kPencil + tx] = live ? T.qlo[pb + (size_t)pp * ncol] : 0.0f;
+    }
+    __syncthreads();
+    for (int p = (int)ty - 3; p <= n + 1; p += blockDim.y)
+      Dl[(p + 3) * kPencil + tx] = (H[(p + 4) * kPencil + tx] - H[(p + 3) * kPencil + tx]) +
+                                   (Lo[(p + 4) * kPencil + tx] - Lo[(p + 3) * kPencil + tx]);
+    __syncthreads();
+    for (int p = (int)ty - 1; p <= n; p += blockDim.y) {  // slopes of cells -1..n (coefficient row p+1)
+      const float sA = live ? T.vsA32[(size_t)(p + 1) * ncol + col] : 0.0f;
+      const float sB = live ? T.vsB32[(size_t)(p + 1) * ncol + col] : 0.0f;
+      S[(p + 3) * kPencil + tx] =
+          slope_from_diff_n(Dl[(p + 2) * kPencil + tx], Dl[(p + 3) * kPencil + tx], sA, sB);
+    }
+    __syncthreads();
+    if (live) {
+      for (int kf = ty; kf <= n; kf += blockDim.y) {
+        if (kf == 0 || kf == n) {
+          T.fz[(size_t)s * fplane + (size_t)kf * ncol + col] = 0.0;
+          continue;
+        }
+        const double M = Mf[kf * kPencil + tx];
+        const bool right = __double_as_longlong(M) > 0;
+        const int up = right ? kf - 1 : kf;
+        const float lab = T.veAB32[(size_t)up * ncol + col], lc = T.veC32[(size_t)up * ncol + col],
+                    ld = T.veD32[(size_t)up * ncol + col];
+        const float rab = T.veAB32[(size_t)(up + 1) * ncol + col],
+                    rc = T.veC32[(size_t)(up + 1) * ncol + col],
+                    rd = T.veD32[(size_t)(up + 1) * ncol + col];
+        float aL = (lab - 1.0f) * Dl[(up + 2) * kPencil + tx] + lc * S[(up + 3) * kPencil + tx] +
+                   ld * S[(up + 2) * kPencil + tx];
+        float aR = rab * Dl[(up + 3) * kPencil + tx] + rc * S[(up + 4) * kPencil + tx] +
+                   rd * S[(up + 3) * kPencil + tx];
+        limitf(0.0f, aL, aR);
+        const double a2 = Q[pb + (size_t)up * ncol];
+        T.fz[(size_t)s * fplane + (size_t)kf * ncol + col] = M * (a2 + (double)(right ? aR : aL));
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // ------------------------------------------------------------------ stage kernel
 __device__ __forceinline__ void split_store(const DevTransport<double>& T, size_t x, double v) {
   float hi = (float)v;
@@ -772,6 +1003,11 @@ static void allow_big_smem() {
   cudaFuncSetAttribute(k_flux_y_fused<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
   cudaFuncSetAttribute(k_flux_z_fused<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
   cudaFuncSetAttribute(k_flux_z_fused<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_flux_x_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_flux_y_mixed<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_flux_y_mixed<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_flux_z_mixed<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_flux_z_mixed<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
   done = true;
 }
 
@@ -834,17 +1070,51 @@ static void launch_flux_one(cudaStream_t st, const DevTransport<double>& T, cons
   }
 }
 
-static void launch_fluxes(cudaStream_t st, const DevTransport<double>& T, const StageSel& sel) {
-  if (T.mixed) {  // FP32 deviation-form reconstruction, one thread per face
+// Mixed-precision pencils: the n+1 FP64 face fluxes plus four FP32 rows (hi, lo, neighbour
+// differences, slopes; n+6 each) per pencil.  A direction that does not fit uses the per-face
+// FP32 kernel (the same deviation-form reconstruction, evaluated per face).
+static size_t mixed_pencil_bytes(int n, int pw) {
+  return ((size_t)(n + 1) * sizeof(double) + (size_t)4 * (n + 6) * sizeof(float)) * pw;
+}
+static void launch_fluxes_mixed(cudaStream_t st, const DevTransport<double>& T, const StageSel& sel) {
+  const FluxShape f = flux_shape(T);
+  int pw = f.pw;
+  if (mixed_pencil_bytes(T.nlat, pw) > (size_t)kPencilSmemCap ||
+      mixed_pencil_bytes(T.nlev, pw) > (size_t)kPencilSmemCap)
+    pw = 16;
+  const size_t ncol = (size_t)T.nlon * T.nlat;
+  const size_t shx = mixed_pencil_bytes(T.nlon, 1), shy = mixed_pencil_bytes(T.nlat, pw),
+               shz = mixed_pencil_bytes(T.nlev, pw);
+  if (shx <= (size_t)kPencilSmemCap) {
+    k_flux_x_mixed<<<(unsigned)(T.nlat * T.nlev), f.xt, shx, st>>>(T, sel);
+  } else {
     long long nx = (long long)(T.nlon + 1) * T.nlat * T.nlev;
-    long long ny = (long long)T.nlon * (T.nlat + 1) * T.nlev;
-    long long nz = (long long)T.nlon * T.nlat * (T.nlev + 1);
     k_flux_x<<<(unsigned)((nx + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);
+  }
+  if (shy <= (size_t)kPencilSmemCap) {
+    unsigned ntile = (unsigned)((T.nlon + pw - 1) / pw);
+    if (pw == 16) k_flux_y_mixed<16><<<ntile * (unsigned)T.nlev, dim3(16, f.rows), shy, st>>>(T, sel);
+    else k_flux_y_mixed<32><<<ntile * (unsigned)T.nlev, dim3(32, f.rows), shy, st>>>(T, sel);
+  } else {
+    long long ny = (long long)T.nlon * (T.nlat + 1) * T.nlev;
     k_flux_y<<<(unsigned)((ny + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);
+  }
+  if (shz <= (size_t)kPencilSmemCap) {
+    unsigned nzb = (unsigned)((ncol + pw - 1) / pw);
+    if (pw == 16) k_flux_z_mixed<16><<<nzb, dim3(16, f.rows), shz, st>>>(T, sel);
+    else k_flux_z_mixed<32><<<nzb, dim3(32, f.rows), shz, st>>>(T, sel);
+  } else {
+    long long nz = (long long)T.nlon * T.nlat * (T.nlev + 1);
     k_flux_z<<<(unsigned)((nz + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);
+  }
+}
+
+static void launch_fluxes(cudaStream_t st, const DevTransport<double>& T, const StageSel& sel) {
+  allow_big_smem();
+  if (T.mixed) {
+    launch_fluxes_mixed(st, T, sel);
     return;
   }
-  allow_big_smem();
   const FluxShape f = flux_shape(T);
   for (int dir = 0; dir < 3; ++dir) launch_flux_one(st, T, sel, f, dir);
 }
