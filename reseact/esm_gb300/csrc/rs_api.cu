@@ -344,6 +344,8 @@ struct rs_handle {
   struct Tune {
     int pc_threads = 128, pc_blocks_per_sm = 4;      // per-cell chemistry kernel
     int pencil = 32, rows = 8, xthreads = 128;        // transport pencil kernels
+    int mpencil = 16, mrows = 16, mxthreads = 128;    // mixed-precision pencil kernels
+    int msper_x = 1 << 20, msper_yz = 1;             // tracers per block (clamped to ntr)
   } tune;
   // mechanism-specialised chemistry kernels (null: not built) and the kind in use
   // full PBL mixing: host inputs, and the derived per-layer fraction / weight and column
@@ -555,6 +557,11 @@ void refresh_dt(rs_handle* h) {
   T.pencil = h->tune.pencil;
   T.rows = h->tune.rows;
   T.xthreads = h->tune.xthreads;
+  T.mpencil = h->tune.mpencil;
+  T.mrows = h->tune.mrows;
+  T.mxthreads = h->tune.mxthreads;
+  T.msper_x = h->tune.msper_x;
+  T.msper_yz = h->tune.msper_yz;
   T.pbl = h->pbl_on;
   T.pbl_f = h->pbl_f.p; T.pbl_w = h->pbl_w.p; T.pbl_den = h->pbl_den.p; T.pbl_qbar = h->pbl_qbar.p;
   T.pbl_tau = h->tau_pbl;
@@ -1991,6 +1998,62 @@ extern "C" rs_status rs_autotune(rs_handle* h, char* buf, size_t buf_len) {
                     "], \"transport_choice\": {\"xthreads\": %d, \"pencil\": %d, \"rows\": %d}",
                     h->tune.xthreads, h->tune.pencil, h->tune.rows);
       rep += line;
+      if (h->cfg.precision == RS_PREC_MIXED) {
+        // the FP32 deviation-form pencils: threads per lon row and tracers per block for x,
+        // pencil width, rows and tracers per block for y and z (one split of Q, then timings)
+        const int ntr = h->dt.ntr;
+        std::vector<int> spers{1, 2, ntr};
+        rs::launch_flux_dir_mixed(h->st, T, Q, -1, true);
+        rep += ", \"mixed_lon_rows\": [";
+        first = true;
+        float bmx = 1e30f;
+        for (int xt : {64, 128, 256})
+          for (int sp : spers) {
+            T.mxthreads = xt;
+            T.msper_x = sp;
+            float ms = time_min(h->st, 3, [&] { rs::launch_flux_dir_mixed(h->st, T, Q, 0, false); });
+            std::snprintf(line, sizeof line, "%s{\"threads\": %d, \"tracers\": %d, \"ms\": %.4f}",
+                          first ? "" : ", ", xt, sp, ms);
+            rep += line;
+            first = false;
+            if (ms < bmx) {
+              bmx = ms;
+              h->tune.mxthreads = xt;
+              h->tune.msper_x = sp;
+            }
+          }
+        rep += "], \"mixed_pencils\": [";
+        first = true;
+        float bmyz = 1e30f;
+        for (int pw : {16, 32})
+          for (int rows : {4, 8, 16})
+            for (int sp : spers) {
+              T.mpencil = pw;
+              T.mrows = rows;
+              T.msper_yz = sp;
+              float ms = time_min(h->st, 3, [&] {
+                rs::launch_flux_dir_mixed(h->st, T, Q, 1, false);
+                rs::launch_flux_dir_mixed(h->st, T, Q, 2, false);
+              });
+              std::snprintf(line, sizeof line,
+                            "%s{\"pencil\": %d, \"rows\": %d, \"tracers\": %d, \"ms\": %.4f}",
+                            first ? "" : ", ", pw, rows, sp, ms);
+              rep += line;
+              first = false;
+              if (ms < bmyz) {
+                bmyz = ms;
+                h->tune.mpencil = pw;
+                h->tune.mrows = rows;
+                h->tune.msper_yz = sp;
+              }
+            }
+        std::snprintf(line, sizeof line,
+                      "], \"mixed_choice\": {\"xthreads\": %d, \"x_tracers\": %d, \"pencil\": %d, "
+                      "\"rows\": %d, \"yz_tracers\": %d}",
+                      h->tune.mxthreads, std::min(h->tune.msper_x, ntr), h->tune.mpencil,
+                      h->tune.mrows, h->tune.msper_yz);
+        rep += line;
+      }
       refresh_dt(h);
       invalidate_graphs(h);
     }

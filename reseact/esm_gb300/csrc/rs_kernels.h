@@ -80,6 +80,9 @@ struct DevTransport {
   int pencil;    // pencils per block in the lat / vertical kernels: 16 or 32
   int rows;      // threads along the pencil (blockDim.y): 4, 8 or 16
   int xthreads;  // threads per lon row: 64, 128 or 256
+  // launch shape of the mixed-precision pencil kernels (chosen by rs_autotune)
+  int mpencil, mrows, mxthreads;
+  int msper_x, msper_yz;  // tracers per block (blockIdx.y selects the group)
 };
 
 // chemistry (rs_chem.cu)
@@ -116,6 +119,8 @@ void launch_transport_rhs(cudaStream_t st, const DevTransport<double>& T, const 
                           double g, double* dU, double* dUadv = nullptr);
 
 void launch_flux_dir(cudaStream_t st, const DevTransport<double>& T, const double* Q, int dir);
+void launch_flux_dir_mixed(cudaStream_t st, const DevTransport<double>& T, const double* Q, int dir,
+                           bool split);
 
 // control (rs_control.cu)
 void launch_ctl_init(cudaStream_t st, Ctl* ctl, const Ctl& init);

@@ -15,6 +15,8 @@
 // fixed-tree partial sums of the hairer norm.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "rs_device.cuh"
 #include "rs_kernels.h"
 
@@ -541,7 +543,8 @@ __global__ void __launch_bounds__(512) k_flux_z_fused(DevTransport<double> T, St
 //             aL = (ab_up - 1) dl_{up-1} + c_up S_up + d_up S_{up-1}
 //             aR = ab_{up+1} dl_up + c_{up+1} S_{up+1} + d_{up+1} S_up
 // the CW84 limiter on (0, aL, aR), and the face value a_up + dev in FP64.  q == 1 gives dl = 0,
-// S = 0, dev = 0 and a face of exactly 1 (the freestream stays exact).
+// S = 0, dev = 0 and a face of exactly 1 (the freestream stays exact).  blockIdx.y selects a
+// group of sper tracers, so short pencil grids still fill the 152 SMs.
 __device__ __forceinline__ float slope_from_diff(float d0, float d1) {
   if (d1 * d0 > 0.0f) {
     const float da = 0.5f * (d0 + d1);
@@ -559,10 +562,11 @@ __device__ __forceinline__ float slope_from_diff_n(float d0, float d1, float sA,
   return 0.0f;
 }
 
-__global__ void __launch_bounds__(256) k_flux_x_mixed(DevTransport<double> T, StageSel sel) {
+__global__ void __launch_bounds__(256) k_flux_x_mixed(DevTransport<double> T, StageSel sel, int sper) {
   const double* Q;
   double g;
   if (!resolve_stage(sel, Q, g)) return;
+  const int s0 = blockIdx.y * sper, s1 = min(T.ntr, s0 + sper);  // this block's tracers
   extern __shared__ double smm[];
   const int n = T.nlon, nf = n + 1, L = n + 6;
   double* Mf = smm;                                   // [n+1] face air-mass flux
@@ -576,7 +580,7 @@ __global__ void __launch_bounds__(256) k_flux_x_mixed(DevTransport<double> T, St
   const size_t rbase = ((size_t)k * T.nlat + j) * n;
   const bool periodic = T.lon_bc == 0;
   for (int f = threadIdx.x; f <= n; f += blockDim.x) Mf[f] = g * T.mx[((size_t)k * T.nlat + j) * nf + f];
-  for (int s = 0; s < T.ntr; ++s) {
+  for (int s = s0; s < s1; ++s) {
     const size_t pb = (size_t)s * nc + rbase;
     for (int p = threadIdx.x - 3; p <= n + 2; p += blockDim.x) {
       float h, l;
@@ -620,10 +624,11 @@ __global__ void __launch_bounds__(256) k_flux_x_mixed(DevTransport<double> T, St
 }
 
 template <int kPencil>
-__global__ void __launch_bounds__(512) k_flux_y_mixed(DevTransport<double> T, StageSel sel) {
+__global__ void __launch_bounds__(512) k_flux_y_mixed(DevTransport<double> T, StageSel sel, int sper) {
   const double* Q;
   double g;
   if (!resolve_stage(sel, Q, g)) return;
+  const int s0 = blockIdx.y * sper, s1 = min(T.ntr, s0 + sper);  // this block's tracers
   extern __shared__ double smym[];
   const int n = T.nlat, nfj = n + 1, L = n + 6;
   double* Mf = smym;                                         // [n+1][kPencil]
@@ -642,7 +647,7 @@ __global__ void __launch_bounds__(512) k_flux_y_mixed(DevTransport<double> T, St
   if (live)
     for (int f = ty; f <= n; f += blockDim.y)
       Mf[f * kPencil + tx] = g * T.my[((size_t)k * nfj + f) * T.nlon + i];
-  for (int s = 0; s < T.ntr; ++s) {
+  for (int s = s0; s < s1; ++s) {
     const size_t pb = (size_t)s * nc + (size_t)k * T.nlat * T.nlon;
     for (int p = (int)ty - 3; p <= n + 2; p += blockDim.y) {
       float h = 0.0f, l = 0.0f;
@@ -696,10 +701,11 @@ __global__ void __launch_bounds__(512) k_flux_y_mixed(DevTransport<double> T, St
 }
 
 template <int kPencil>
-__global__ void __launch_bounds__(512) k_flux_z_mixed(DevTransport<double> T, StageSel sel) {
+__global__ void __launch_bounds__(512) k_flux_z_mixed(DevTransport<double> T, StageSel sel, int sper) {
   const double* Q;
   double g;
   if (!resolve_stage(sel, Q, g)) return;
+  const int s0 = blockIdx.y * sper, s1 = min(T.ntr, s0 + sper);  // this block's tracers
   extern __shared__ double smzm[];
   const int n = T.nlev, L = n + 6;
   double* Mf = smzm;                                          // [n+1][kPencil]
@@ -715,7 +721,7 @@ __global__ void __launch_bounds__(512) k_flux_z_mixed(DevTransport<double> T, St
   const size_t fplane = ncol * (n + 1);
   if (live)
     for (int kf = ty; kf <= n; kf += blockDim.y) Mf[kf * kPencil + tx] = g * T.mz[(size_t)kf * ncol + col];
-  for (int s = 0; s < T.ntr; ++s) {
+  for (int s = s0; s < s1; ++s) {
     const size_t pb = (size_t)s * nc + col;
     for (int p = (int)ty - 3; p <= n + 2; p += blockDim.y) {
       const int pp = p < 0 ? -1 - p : (p >= n ? 2 * n - 1 - p : p);
@@ -1076,36 +1082,46 @@ static void launch_flux_one(cudaStream_t st, const DevTransport<double>& T, cons
 static size_t mixed_pencil_bytes(int n, int pw) {
   return ((size_t)(n + 1) * sizeof(double) + (size_t)4 * (n + 6) * sizeof(float)) * pw;
 }
-static void launch_fluxes_mixed(cudaStream_t st, const DevTransport<double>& T, const StageSel& sel) {
-  const FluxShape f = flux_shape(T);
-  int pw = f.pw;
+static void launch_fluxes_mixed(cudaStream_t st, const DevTransport<double>& T, const StageSel& sel,
+                                int only_dir = -1) {
+  int pw = T.mpencil == 16 ? 16 : 32;
   if (mixed_pencil_bytes(T.nlat, pw) > (size_t)kPencilSmemCap ||
       mixed_pencil_bytes(T.nlev, pw) > (size_t)kPencilSmemCap)
     pw = 16;
+  const int rows = (T.mrows == 4 || T.mrows == 16) ? T.mrows : 8;
+  const int xt = (T.mxthreads == 64 || T.mxthreads == 256) ? T.mxthreads : 128;
+  auto groups = [&](int sper) { return (unsigned)((T.ntr + sper - 1) / sper); };
+  const int sx = std::max(1, std::min(T.ntr, T.msper_x)), syz = std::max(1, std::min(T.ntr, T.msper_yz));
   const size_t ncol = (size_t)T.nlon * T.nlat;
   const size_t shx = mixed_pencil_bytes(T.nlon, 1), shy = mixed_pencil_bytes(T.nlat, pw),
                shz = mixed_pencil_bytes(T.nlev, pw);
-  if (shx <= (size_t)kPencilSmemCap) {
-    k_flux_x_mixed<<<(unsigned)(T.nlat * T.nlev), f.xt, shx, st>>>(T, sel);
-  } else {
-    long long nx = (long long)(T.nlon + 1) * T.nlat * T.nlev;
-    k_flux_x<<<(unsigned)((nx + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);
+  if (only_dir < 0 || only_dir == 0) {
+    if (shx <= (size_t)kPencilSmemCap) {
+      k_flux_x_mixed<<<dim3((unsigned)(T.nlat * T.nlev), groups(sx)), xt, shx, st>>>(T, sel, sx);
+    } else {
+      long long nx = (long long)(T.nlon + 1) * T.nlat * T.nlev;
+      k_flux_x<<<(unsigned)((nx + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);
+    }
   }
-  if (shy <= (size_t)kPencilSmemCap) {
-    unsigned ntile = (unsigned)((T.nlon + pw - 1) / pw);
-    if (pw == 16) k_flux_y_mixed<16><<<ntile * (unsigned)T.nlev, dim3(16, f.rows), shy, st>>>(T, sel);
-    else k_flux_y_mixed<32><<<ntile * (unsigned)T.nlev, dim3(32, f.rows), shy, st>>>(T, sel);
-  } else {
-    long long ny = (long long)T.nlon * (T.nlat + 1) * T.nlev;
-    k_flux_y<<<(unsigned)((ny + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);
+  if (only_dir < 0 || only_dir == 1) {
+    if (shy <= (size_t)kPencilSmemCap) {
+      dim3 grid((unsigned)((T.nlon + pw - 1) / pw) * (unsigned)T.nlev, groups(syz));
+      if (pw == 16) k_flux_y_mixed<16><<<grid, dim3(16, rows), shy, st>>>(T, sel, syz);
+      else k_flux_y_mixed<32><<<grid, dim3(32, rows), shy, st>>>(T, sel, syz);
+    } else {
+      long long ny = (long long)T.nlon * (T.nlat + 1) * T.nlev;
+      k_flux_y<<<(unsigned)((ny + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);
+    }
   }
-  if (shz <= (size_t)kPencilSmemCap) {
-    unsigned nzb = (unsigned)((ncol + pw - 1) / pw);
-    if (pw == 16) k_flux_z_mixed<16><<<nzb, dim3(16, f.rows), shz, st>>>(T, sel);
-    else k_flux_z_mixed<32><<<nzb, dim3(32, f.rows), shz, st>>>(T, sel);
-  } else {
-    long long nz = (long long)T.nlon * T.nlat * (T.nlev + 1);
-    k_flux_z<<<(unsigned)((nz + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);
+  if (only_dir < 0 || only_dir == 2) {
+    if (shz <= (size_t)kPencilSmemCap) {
+      dim3 grid((unsigned)((ncol + pw - 1) / pw), groups(syz));
+      if (pw == 16) k_flux_z_mixed<16><<<grid, dim3(16, rows), shz, st>>>(T, sel, syz);
+      else k_flux_z_mixed<32><<<grid, dim3(32, rows), shz, st>>>(T, sel, syz);
+    } else {
+      long long nz = (long long)T.nlon * T.nlat * (T.nlev + 1);
+      k_flux_z<<<(unsigned)((nz + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);
+    }
   }
 }
 
@@ -1117,6 +1133,20 @@ static void launch_fluxes(cudaStream_t st, const DevTransport<double>& T, const 
   }
   const FluxShape f = flux_shape(T);
   for (int dir = 0; dir < 3; ++dir) launch_flux_one(st, T, sel, f, dir);
+}
+
+// one direction of the mixed-precision flux computation on a given field (used by the
+// autotuner); the hi/lo planes of Q are split first
+void launch_flux_dir_mixed(cudaStream_t st, const DevTransport<double>& T, const double* Q, int dir,
+                           bool split) {
+  StageSel sel{nullptr, 0, nullptr, nullptr, nullptr, nullptr, nullptr, Q, 1.0};
+  allow_big_smem();
+  if (split) {
+    size_t n = (size_t)T.ntr * T.nlon * T.nlat * T.nlev;
+    k_split_input<<<(unsigned)((n + kRedThreads - 1) / kRedThreads), kRedThreads, 0, st>>>(
+        T, nullptr, nullptr, nullptr, Q);
+  }
+  launch_fluxes_mixed(st, T, sel, dir);
 }
 
 // one direction of the flux computation on a given field (used by the autotuner)
