@@ -240,6 +240,14 @@ void* rs_stream(rs_handle* h);
  * the fastest for this handle and writes a JSON report of every candidate into buf. */
 rs_status rs_autotune(rs_handle* h, char* buf, size_t buf_len);
 
+/* Set one launch shape that rs_autotune would choose, e.g. to replay an earlier tuning without
+ * timing again (no reference counterpart).  Keys: "xthreads", "pencil", "rows" (FP64 pencils);
+ * "mixed_xthreads", "mixed_x_tracers", "mixed_pencil", "mixed_rows", "mixed_yz_tracers",
+ * "mixed_x_bulk", "mixed_yz_bulk" (mixed pencils); "per_cell_threads",
+ * "per_cell_blocks_per_sm" (per-cell chemistry).  Values outside a key's candidates are
+ * RS_ERR_INVALID.  Every shape gives bit-identical results. */
+rs_status rs_set_launch_shape(rs_handle* h, const char* key, int32_t value);
+
 /* Chemistry kernel selection (no reference counterpart; the reference compiles its RHS and
  * Jacobian from the .esm system into native code, which the SPECIALIZED kernels mirror).
  * SPECIALIZED: the mechanism's rate products, RHS, Jacobian, LU and solves are generated as
@@ -253,6 +261,19 @@ enum { RS_CHEM_KERNEL_AUTO = 0, RS_CHEM_KERNEL_TABLE = 1, RS_CHEM_KERNEL_SPECIAL
 rs_status rs_set_chem_kernel(rs_handle* h, int32_t kind);
 /* The kernel kind in use (TABLE or SPECIALIZED) and a one-line JSON description of it. */
 rs_status rs_get_chem_kernel(rs_handle* h, int32_t* kind, char* info, size_t info_len);
+/* Staging of the mixed-precision transport pencils (no reference counterpart).
+ * BULK: the interior of every lat / vertical pencil is copied into shared memory by one
+ *   tensor-map bulk copy (TMA) per split plane and every lon row by a 1-D bulk copy, double
+ *   buffered across tracers; the ghost cells are loaded by the threads.  Used where the grid
+ *   meets the copy engine's rules (nlon % 4 == 0, nlat and nlev <= 256 for the pencils);
+ * PLAIN: the threads load every cell;
+ * AUTO (the default): BULK where available (rs_autotune may pick PLAIN when it is faster).
+ * Both give bit-identical fluxes.  A bulk-copy wait that runs out stops the solve with
+ * RS_ERR_CUDA.  rs_get_transport_staging reports the mode in use and a one-line JSON of the
+ * directions that can use bulk copies. */
+enum { RS_STAGING_AUTO = 0, RS_STAGING_PLAIN = 1, RS_STAGING_BULK = 2 };
+rs_status rs_set_transport_staging(rs_handle* h, int32_t mode);
+rs_status rs_get_transport_staging(rs_handle* h, int32_t* mode, char* info, size_t info_len);
 /* The generated CUDA source of a mechanism's specialised kernels, and an NVRTC compile of it
  * for sm_103a with ptxas's resource report in log; neither needs a device.  *len_out (may be
  * NULL) receives the source length + 1; buf may be NULL to query it. */

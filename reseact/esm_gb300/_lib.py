@@ -22,9 +22,11 @@ SYMBOLS = [
     "rs_autotune", "rs_set_chem_kernel", "rs_get_chem_kernel", "rs_chem_kernel_source",
     "rs_chem_kernel_compile", "rs_chem_kernel_reciprocal", "rs_lu_order",
     "rs_mechanism_lu_order", "rs_continuity_drift", "rs_lie_trotter_solve",
+    "rs_set_transport_staging", "rs_get_transport_staging", "rs_set_launch_shape",
 ]
 
 CHEM_KERNEL_AUTO, CHEM_KERNEL_TABLE, CHEM_KERNEL_SPECIALIZED = 0, 1, 2
+STAGING_AUTO, STAGING_PLAIN, STAGING_BULK = 0, 1, 2
 
 
 class RsError(RuntimeError):
@@ -92,6 +94,12 @@ def _declare(L):
     L.rs_set_chem_kernel.restype = C.c_int
     L.rs_get_chem_kernel.argtypes = [vp, C.POINTER(i32), C.c_char_p, sz]
     L.rs_get_chem_kernel.restype = C.c_int
+    L.rs_set_launch_shape.argtypes = [vp, C.c_char_p, i32]
+    L.rs_set_launch_shape.restype = C.c_int
+    L.rs_set_transport_staging.argtypes = [vp, i32]
+    L.rs_set_transport_staging.restype = C.c_int
+    L.rs_get_transport_staging.argtypes = [vp, C.POINTER(i32), C.c_char_p, sz]
+    L.rs_get_transport_staging.restype = C.c_int
     L.rs_chem_kernel_source.argtypes = [C.POINTER(abi.rs_mechanism), i32, C.c_char_p, sz,
                                         C.POINTER(sz)]
     L.rs_chem_kernel_source.restype = C.c_int
@@ -306,6 +314,24 @@ class Solver:
         k = C.c_int32(0)
         buf = C.create_string_buffer(1024)
         self._check(self.L.rs_get_chem_kernel(self.h, C.byref(k), buf, 1024))
+        return k.value, json.loads(buf.value.decode())
+
+    def set_launch_shape(self, **shape):
+        """Pin launch shapes by key (the keys rs_autotune reports), e.g. mixed_yz_tracers=3."""
+        for k, v in shape.items():
+            self._check(self.L.rs_set_launch_shape(self.h, k.encode(), int(v)))
+
+    def set_transport_staging(self, mode):
+        """STAGING_AUTO / _PLAIN / _BULK for the mixed-precision pencils (raises if BULK is
+        unavailable on this grid or precision)."""
+        self._check(self.L.rs_set_transport_staging(self.h, int(mode)))
+
+    def transport_staging(self):
+        """(mode in use, per-direction description dict) of the mixed pencils' staging."""
+        import json
+        k = C.c_int32(0)
+        buf = C.create_string_buffer(512)
+        self._check(self.L.rs_get_transport_staging(self.h, C.byref(k), buf, 512))
         return k.value, json.loads(buf.value.decode())
 
     def lie_trotter_solve(self, t0, t1, dtT, dtC, *, macro_dt, min_macro_dt=0.0,

@@ -307,6 +307,10 @@ struct rs_handle {
   DevBuf<double> mx, my, mz, qw, qe, qs, qn, gx, gylo, gyhi, vsA, vsB, veAB, veC, veD, dtcell,
       stepcell, totals;
   DevBuf<float> qhi, qlo, vsA32, vsB32, veAB32, veC32, veD32;  // mixed-precision transport
+  rs::MixedTmaps* tmaps = nullptr;  // bulk-copy staging of the mixed pencils (null: unavailable)
+  std::string tmaps_why;
+  int staging = RS_STAGING_AUTO;
+  DevBuf<int> tma_err;              // set by a pencil kernel whose staging wait ran out
   DevBuf<Ctl> ctl;  // [0] transport, [1] chemistry, [2] single-step scratch
   DevBuf<int> flag;
   DevBuf<unsigned long long> queue;
@@ -346,6 +350,7 @@ struct rs_handle {
     int pencil = 32, rows = 8, xthreads = 128;        // transport pencil kernels
     int mpencil = 16, mrows = 16, mxthreads = 128;    // mixed-precision pencil kernels
     int msper_x = 1 << 20, msper_yz = 1;             // tracers per block (clamped to ntr)
+    int mbulk_x = 1, mbulk_yz = 1;                    // bulk-copy staging per direction
   } tune;
   // mechanism-specialised chemistry kernels (null: not built) and the kind in use
   // full PBL mixing: host inputs, and the derived per-layer fraction / weight and column
@@ -562,6 +567,10 @@ void refresh_dt(rs_handle* h) {
   T.mxthreads = h->tune.mxthreads;
   T.msper_x = h->tune.msper_x;
   T.msper_yz = h->tune.msper_yz;
+  T.tma = (h->staging != RS_STAGING_PLAIN) ? h->tmaps : nullptr;
+  T.tma_err = h->tma_err.p;
+  T.mbulk_x = h->staging == RS_STAGING_BULK ? 1 : h->tune.mbulk_x;
+  T.mbulk_yz = h->staging == RS_STAGING_BULK ? 1 : h->tune.mbulk_yz;
   T.pbl = h->pbl_on;
   T.pbl_f = h->pbl_f.p; T.pbl_w = h->pbl_w.p; T.pbl_den = h->pbl_den.p; T.pbl_qbar = h->pbl_qbar.p;
   T.pbl_tau = h->tau_pbl;
@@ -914,11 +923,19 @@ rs_status rs_create(const rs_config* cfg, rs_handle** out) {
         h->qhi.alloc((size_t)h->ntr * h->nc);
         h->qlo.alloc((size_t)h->ntr * h->nc);
       }
+      h->tma_err.alloc(1);
+      h->tma_err.zero(h->st);
       build_geometry(h);
       h->dp_host.assign(h->nc, 1.0);
       build_vertical(h);
     }
     refresh_dt(h);
+    if (cfg->do_transport && cfg->precision == RS_PREC_MIXED) {
+      const char* why = nullptr;
+      h->tmaps = rs::mixed_tmaps_create(h->dt, &why);
+      if (!h->tmaps) h->tmaps_why = why ? why : "";
+      refresh_dt(h);
+    }
     CK(cudaStreamSynchronize(h->st));
   });
   if (st != RS_OK) {
@@ -955,6 +972,8 @@ void rs_destroy(rs_handle* h) {
                              &h->Cf};
   for (auto* b : abufs) b->release();
   h->nseq.release();
+  h->tma_err.release();
+  rs::mixed_tmaps_destroy(h->tmaps);
   h->ctl.release();
   h->flag.release();
   h->queue.release();
@@ -1099,6 +1118,19 @@ rs_status rs_set_rate_constants(rs_handle* h, const double* k, size_t n) {
   });
 }
 
+// A mixed pencil kernel whose bulk-copy wait ran out sets tma_err and stops the solve.
+static void check_staging(rs_handle* h) {
+  if (!h->tma_err.p) return;
+  int e = 0;
+  CK(cudaMemcpyAsync(h->hflag, h->tma_err.p, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  e = *h->hflag;
+  if (e) {
+    CK(cudaMemsetAsync(h->tma_err.p, 0, sizeof(int), h->st));
+    throw RsError(RS_ERR_CUDA, "a transport pencil's bulk-copy wait timed out; solve stopped");
+  }
+}
+
 rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double* dtC,
                         rs_stats* out) {
   if (!h || !dtT || !dtC) return RS_ERR_INVALID;
@@ -1221,7 +1253,10 @@ rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double*
         CK(cudaMemcpy(r.seqC.data(), h->seqbuf.p + (size_t)2 * seqcap,
                       r.seqC.size() * sizeof(double), cudaMemcpyDeviceToHost));
     }
-    if (!okT || !okC) throw RsError(RS_ERR_MAXITERS, "adaptive solve stopped before t1 (maxiters)");
+    if (!okT || !okC) {
+      check_staging(h);
+      throw RsError(RS_ERR_MAXITERS, "adaptive solve stopped before t1 (maxiters)");
+    }
     CK(cudaMemsetAsync(h->flag.p, 0, sizeof(int), h->st));
     rs::launch_nonfinite(h->st, h->U[h->cur].p, h->nc * h->nsp, h->flag.p);
     h->launches += 1;
@@ -1249,6 +1284,7 @@ rs_status rs_rhs_transport(rs_handle* h, double t, const double* u, double* du, 
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(du, h->io2.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
+    if (h->tmaps) check_staging(h);
   });
 }
 
@@ -1632,6 +1668,83 @@ extern "C" rs_status rs_get_chem_kernel(rs_handle* h, int32_t* kind, char* info,
   });
 }
 
+// ====================================================================== launch shapes
+extern "C" rs_status rs_set_launch_shape(rs_handle* h, const char* key, int32_t value) {
+  if (!h || !key) return RS_ERR_INVALID;
+  return guard(h, [&] {
+    const std::string k(key);
+    auto in = [&](std::initializer_list<int> c) {
+      for (int v : c)
+        if (v == value) return true;
+      return false;
+    };
+    auto& t = h->tune;
+    const int ntr = std::max(1, h->dt.ntr);
+    bool ok = true;
+    if (k == "xthreads") ok = in({64, 128, 256}) && (t.xthreads = value, true);
+    else if (k == "pencil") ok = in({16, 32}) && (t.pencil = value, true);
+    else if (k == "rows") ok = in({4, 8, 16}) && (t.rows = value, true);
+    else if (k == "mixed_xthreads") ok = in({64, 128, 256}) && (t.mxthreads = value, true);
+    else if (k == "mixed_x_tracers") ok = value >= 1 && value <= ntr && (t.msper_x = value, true);
+    else if (k == "mixed_pencil") ok = in({16, 32}) && (t.mpencil = value, true);
+    else if (k == "mixed_rows") ok = in({4, 8, 16}) && (t.mrows = value, true);
+    else if (k == "mixed_yz_tracers") ok = value >= 1 && value <= ntr && (t.msper_yz = value, true);
+    else if (k == "mixed_x_bulk") ok = in({0, 1}) && (t.mbulk_x = value, true);
+    else if (k == "mixed_yz_bulk") ok = in({0, 1}) && (t.mbulk_yz = value, true);
+    else if (k == "per_cell_threads") ok = in({64, 128, 256}) && (t.pc_threads = value, true);
+    else if (k == "per_cell_blocks_per_sm") ok = in({1, 2, 4, 8}) && (t.pc_blocks_per_sm = value, true);
+    else throw RsError(RS_ERR_INVALID, "unknown launch-shape key: " + k);
+    if (!ok) throw RsError(RS_ERR_INVALID, "value out of range for " + k);
+    refresh_dt(h);
+    invalidate_graphs(h);
+  });
+}
+
+// ====================================================================== transport staging
+extern "C" rs_status rs_set_transport_staging(rs_handle* h, int32_t mode) {
+  if (!h) return RS_ERR_INVALID;
+  return guard(h, [&] {
+    if (mode != RS_STAGING_AUTO && mode != RS_STAGING_PLAIN && mode != RS_STAGING_BULK)
+      throw RsError(RS_ERR_INVALID, "unknown staging mode");
+    if (mode == RS_STAGING_BULK && !h->tmaps)
+      throw RsError(RS_ERR_UNSUPPORTED,
+                    "bulk-copy staging unavailable: " +
+                        (h->tmaps_why.empty() ? std::string("mixed-precision transport only")
+                                              : h->tmaps_why));
+    h->staging = mode;
+    refresh_dt(h);
+    invalidate_graphs(h);
+  });
+}
+
+extern "C" rs_status rs_get_transport_staging(rs_handle* h, int32_t* mode, char* info,
+                                              size_t info_len) {
+  if (!h) return RS_ERR_INVALID;
+  return guard(h, [&] {
+    const bool bulk = h->tmaps && h->staging != RS_STAGING_PLAIN &&
+                      (h->staging == RS_STAGING_BULK || h->tune.mbulk_x || h->tune.mbulk_yz);
+    if (mode) *mode = bulk ? RS_STAGING_BULK : RS_STAGING_PLAIN;
+    if (info && info_len) {
+      char line[256];
+      const rs::DevTransport<double>& T = h->dt;
+      auto use = [&](int d) {
+        if (!rs::mixed_tmaps_dir_ok(h->tmaps, d)) return "unavailable";
+        return (T.tma && (d == 0 ? T.mbulk_x : T.mbulk_yz)) ? "bulk" : "plain";
+      };
+      if (h->tmaps)
+        std::snprintf(line, sizeof line,
+                      "{\"mode\": \"%s\", \"lon_rows\": \"%s\", \"lat_pencils\": \"%s\", "
+                      "\"vertical_pencils\": \"%s\"}",
+                      bulk ? "bulk" : "plain", use(0), use(1), use(2));
+      else
+        std::snprintf(line, sizeof line, "{\"mode\": \"plain\", \"why\": \"%.180s\"}",
+                      h->tmaps_why.c_str());
+      std::strncpy(info, line, info_len - 1);
+      info[info_len - 1] = 0;
+    }
+  });
+}
+
 extern "C" rs_status rs_chem_kernel_reciprocal(rs_handle* h, const double* x, double* r,
                                                size_t n) {
   if (!h || (n && (!x || !r))) return RS_ERR_INVALID;
@@ -2000,58 +2113,78 @@ extern "C" rs_status rs_autotune(rs_handle* h, char* buf, size_t buf_len) {
       rep += line;
       if (h->cfg.precision == RS_PREC_MIXED) {
         // the FP32 deviation-form pencils: threads per lon row and tracers per block for x,
-        // pencil width, rows and tracers per block for y and z (one split of Q, then timings)
+        // pencil width, rows and tracers per block for y and z, each with bulk-copy and with
+        // plain-load staging when the mode is AUTO (one split of Q, then timings)
         const int ntr = h->dt.ntr;
         std::vector<int> spers{1, 2, ntr};
+        std::vector<int> modes;
+        if (h->tmaps && h->staging != RS_STAGING_PLAIN) modes.push_back(RS_STAGING_BULK);
+        if (!h->tmaps || h->staging != RS_STAGING_BULK) modes.push_back(RS_STAGING_PLAIN);
         rs::launch_flux_dir_mixed(h->st, T, Q, -1, true);
         rep += ", \"mixed_lon_rows\": [";
         first = true;
-        float bmx = 1e30f;
-        for (int xt : {64, 128, 256})
-          for (int sp : spers) {
-            T.mxthreads = xt;
-            T.msper_x = sp;
-            float ms = time_min(h->st, 3, [&] { rs::launch_flux_dir_mixed(h->st, T, Q, 0, false); });
-            std::snprintf(line, sizeof line, "%s{\"threads\": %d, \"tracers\": %d, \"ms\": %.4f}",
-                          first ? "" : ", ", xt, sp, ms);
-            rep += line;
-            first = false;
-            if (ms < bmx) {
-              bmx = ms;
-              h->tune.mxthreads = xt;
-              h->tune.msper_x = sp;
-            }
-          }
-        rep += "], \"mixed_pencils\": [";
-        first = true;
-        float bmyz = 1e30f;
-        for (int pw : {16, 32})
-          for (int rows : {4, 8, 16})
+        float bmx = 1e30f, bmyz = 1e30f;
+        int mode_x = modes[0], mode_yz = modes[0];
+        T.tma = h->tmaps;
+        for (int md : modes) {
+          T.mbulk_x = md == RS_STAGING_BULK;
+          for (int xt : {64, 128, 256})
             for (int sp : spers) {
-              T.mpencil = pw;
-              T.mrows = rows;
-              T.msper_yz = sp;
-              float ms = time_min(h->st, 3, [&] {
-                rs::launch_flux_dir_mixed(h->st, T, Q, 1, false);
-                rs::launch_flux_dir_mixed(h->st, T, Q, 2, false);
-              });
+              T.mxthreads = xt;
+              T.msper_x = sp;
+              float ms = time_min(h->st, 3, [&] { rs::launch_flux_dir_mixed(h->st, T, Q, 0, false); });
               std::snprintf(line, sizeof line,
-                            "%s{\"pencil\": %d, \"rows\": %d, \"tracers\": %d, \"ms\": %.4f}",
-                            first ? "" : ", ", pw, rows, sp, ms);
+                            "%s{\"staging\": \"%s\", \"threads\": %d, \"tracers\": %d, \"ms\": %.4f}",
+                            first ? "" : ", ", md == RS_STAGING_BULK ? "bulk" : "plain", xt, sp, ms);
               rep += line;
               first = false;
-              if (ms < bmyz) {
-                bmyz = ms;
-                h->tune.mpencil = pw;
-                h->tune.mrows = rows;
-                h->tune.msper_yz = sp;
+              if (ms < bmx) {
+                bmx = ms;
+                mode_x = md;
+                h->tune.mxthreads = xt;
+                h->tune.msper_x = sp;
               }
             }
+        }
+        rep += "], \"mixed_pencils\": [";
+        first = true;
+        for (int md : modes) {
+          T.mbulk_yz = md == RS_STAGING_BULK;
+          for (int pw : {16, 32})
+            for (int rows : {4, 8, 16})
+              for (int sp : spers) {
+                T.mpencil = pw;
+                T.mrows = rows;
+                T.msper_yz = sp;
+                float ms = time_min(h->st, 3, [&] {
+                  rs::launch_flux_dir_mixed(h->st, T, Q, 1, false);
+                  rs::launch_flux_dir_mixed(h->st, T, Q, 2, false);
+                });
+                std::snprintf(line, sizeof line,
+                              "%s{\"staging\": \"%s\", \"pencil\": %d, \"rows\": %d, "
+                              "\"tracers\": %d, \"ms\": %.4f}",
+                              first ? "" : ", ", md == RS_STAGING_BULK ? "bulk" : "plain", pw, rows,
+                              sp, ms);
+                rep += line;
+                first = false;
+                if (ms < bmyz) {
+                  bmyz = ms;
+                  mode_yz = md;
+                  h->tune.mpencil = pw;
+                  h->tune.mrows = rows;
+                  h->tune.msper_yz = sp;
+                }
+              }
+        }
+        h->tune.mbulk_x = mode_x == RS_STAGING_BULK;
+        h->tune.mbulk_yz = mode_yz == RS_STAGING_BULK;
         std::snprintf(line, sizeof line,
-                      "], \"mixed_choice\": {\"xthreads\": %d, \"x_tracers\": %d, \"pencil\": %d, "
-                      "\"rows\": %d, \"yz_tracers\": %d}",
-                      h->tune.mxthreads, std::min(h->tune.msper_x, ntr), h->tune.mpencil,
-                      h->tune.mrows, h->tune.msper_yz);
+                      "], \"mixed_choice\": {\"xthreads\": %d, \"x_tracers\": %d, \"x_staging\": "
+                      "\"%s\", \"pencil\": %d, \"rows\": %d, \"yz_tracers\": %d, "
+                      "\"yz_staging\": \"%s\"}",
+                      h->tune.mxthreads, std::min(h->tune.msper_x, ntr),
+                      mode_x == RS_STAGING_BULK ? "bulk" : "plain", h->tune.mpencil, h->tune.mrows,
+                      h->tune.msper_yz, mode_yz == RS_STAGING_BULK ? "bulk" : "plain");
         rep += line;
       }
       refresh_dt(h);

@@ -200,6 +200,18 @@ __device__ __forceinline__ void lu_solve(const DevMech& M, const double* W, cons
   }
 }
 
+// Reciprocal by Newton-Raphson iteration r <- r + r (1 - d r) from the hardware approximation
+// (PTX rcp.approx.ftz.f64); each step squares the relative error, two steps reach ~1 ulp.
+// The production build uses it where d > 0 and normal (error-norm denominators >= atol).
+__device__ __forceinline__ double rcp_nr(double d) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(d));
+  double e = fma(-d, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-d, r, 1.0);
+  return fma(r, e, r);
+}
+
 // ------------------------------------------------------------------ fixed-tree reductions
 // Pairwise tree over 256 lanes: v[t] += v[t+s] for s = 128 ... 1 (identical to the CPU
 // restatement's tree256).  Returns the total in thread 0.

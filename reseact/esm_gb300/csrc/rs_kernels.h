@@ -15,6 +15,7 @@ constexpr int kLargeMS = 64, kLargeMR = 128, kLargeMLU = 1600, kLargeMP = 256;
 constexpr int kMaxProgStack = 32;
 
 struct JitChem;
+struct MixedTmaps;  // tensor maps of the mixed-precision split planes (rs_transport.cu)
 
 struct LaunchCtx {
   cudaStream_t stream;
@@ -83,6 +84,11 @@ struct DevTransport {
   // launch shape of the mixed-precision pencil kernels (chosen by rs_autotune)
   int mpencil, mrows, mxthreads;
   int msper_x, msper_yz;  // tracers per block (blockIdx.y selects the group)
+  // bulk-copy staging of the mixed pencils: host-side tensor maps (null: plain loads) and the
+  // device word a pencil kernel sets when a staging wait runs out (1) -- the solve then stops
+  const MixedTmaps* tma;
+  int* tma_err;
+  int mbulk_x, mbulk_yz;  // use the bulk copies for lon rows / lat and vertical pencils
 };
 
 // chemistry (rs_chem.cu)
@@ -118,6 +124,11 @@ void launch_ssprk43_attempt(cudaStream_t st, const DevTransport<double>& T, cons
 void launch_transport_rhs(cudaStream_t st, const DevTransport<double>& T, const double* U,
                           double g, double* dU, double* dUadv = nullptr);
 
+// Tensor maps for the bulk-copy staging of the mixed pencils over T.qhi / T.qlo; null (and the
+// reason in *why) where the grid does not meet the copy engine's alignment and size rules.
+MixedTmaps* mixed_tmaps_create(const DevTransport<double>& T, const char** why);
+void mixed_tmaps_destroy(MixedTmaps* m);
+bool mixed_tmaps_dir_ok(const MixedTmaps* m, int dir);  // dir 0 lon rows, 1 lat, 2 vertical
 void launch_flux_dir(cudaStream_t st, const DevTransport<double>& T, const double* Q, int dir);
 void launch_flux_dir_mixed(cudaStream_t st, const DevTransport<double>& T, const double* Q, int dir,
                            bool split);

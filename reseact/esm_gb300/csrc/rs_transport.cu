@@ -13,9 +13,12 @@
 // SSPRK43 attempt (rx_traced_integrator.jl:362-400): 4 stages, each = 3 face-flux kernels
 // (x, y, z) + 1 stage kernel; the 4th stage kernel also forms the embedded error and the
 // fixed-tree partial sums of the hairer norm.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
 
 #include "rs_device.cuh"
 #include "rs_kernels.h"
@@ -562,182 +565,445 @@ __device__ __forceinline__ float slope_from_diff_n(float d0, float d1, float sA,
   return 0.0f;
 }
 
+// Shared-memory layout of the mixed pencils (floats first, 128-byte aligned rows so that bulk
+// copies can land in them): the H, Lo rows (two sets when staged by bulk copies, so the next
+// tracer's copy overlaps this tracer's work), then Dl, S rows of L entries (interior cell p at
+// row p + kHo), then the face air-mass flux as float and as double.
+constexpr int kHoX = 32;  // lon rows: interior starts 128 bytes into each row
+constexpr int kHoP = 8;   // lat / vertical pencils: interior starts 8 pencil rows in
+__host__ __device__ inline int mixed_rows_x(int n) { return (n + kHoX + 3 + 31) / 32 * 32; }
+__host__ __device__ inline int mixed_rows_p(int n) { return (n + kHoP + 3 + 1) / 2 * 2; }
+
+// The face flux is M a2 + M dev: a2 the upwind cell's FP64 value, the deviation product in FP32
+// (one FMA in FP64); q == 1 gives exactly M.
+__device__ __forceinline__ double mixed_flux(double M, float Mf, double a2, float dev) {
+  return fma(M, a2, (double)(Mf * dev));
+}
+
+// ---- bulk-copy staging (TMA): mbarrier with a transaction count, one elected issuing thread.
+// Every wait is bounded: after kSpinLimit polls the block records the failure, stops the
+// adaptive solve it belongs to, waits (bounded again) for its own copies and returns.
+struct MixedTmaps {
+  CUtensorMap yh[2], yl[2];  // lat pencils over qhi / qlo, box {pw, nlat, 1}; [0]: pw 16, [1]: 32
+  CUtensorMap zh[2], zl[2];  // vertical pencils, box {pw, nlev, 1}
+  bool x_ok, y_ok, z_ok;
+};
+constexpr int kSpinLimit = 1 << 24;
+constexpr size_t kSmemAlignPad = 128;  // the launch adds this so the layout can start 128-aligned
+
+__device__ __forceinline__ float* align128(unsigned char* p) {
+  return reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(p) + 127) & ~(uintptr_t)127);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* b) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(b)) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* b, uint32_t parity) {
+  for (int i = 0; i < kSpinLimit; ++i) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(b)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* m, int c0, int c1, int c2,
+                                            unsigned long long* b) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(m)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(b))
+      : "memory");
+}
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes,
+                                          unsigned long long* b) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(b))
+      : "memory");
+}
+// A staging wait ran out: flag it, stop the solve (every later kernel of the attempt returns on
+// `done` and the controller ends the loop), then give this block's copies a bounded chance to
+// land before the block's shared memory is released.
+__device__ __noinline__ void staging_abort(int* err, const Ctl* ctl, unsigned long long* bar,
+                                           int uses0, int uses1) {
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    atomicOr(err, 1);
+    if (ctl) atomicExch(const_cast<int*>(&ctl->done), 1);
+    if (uses0 > 0) mbar_wait_bounded(bar, (uint32_t)((uses0 - 1) & 1));
+    if (uses1 > 0) mbar_wait_bounded(bar + 1, (uint32_t)((uses1 - 1) & 1));
+  }
+}
+
+template <bool kTma>
 __global__ void __launch_bounds__(256) k_flux_x_mixed(DevTransport<double> T, StageSel sel, int sper) {
   const double* Q;
   double g;
   if (!resolve_stage(sel, Q, g)) return;
   const int s0 = blockIdx.y * sper, s1 = min(T.ntr, s0 + sper);  // this block's tracers
-  extern __shared__ double smm[];
-  const int n = T.nlon, nf = n + 1, L = n + 6;
-  double* Mf = smm;                                   // [n+1] face air-mass flux
-  float* H = reinterpret_cast<float*>(smm + nf);      // H[p+3], p in [-3, n+2]
-  float* Lo = H + L;
-  float* Dl = Lo + L;                                  // Dl[p+3] = v(p+1) - v(p), p in [-3, n+1]
-  float* S = Dl + L;                                   // S[p+3], slopes of cells p in [-2, n+1]
+  extern __shared__ __align__(16) unsigned char smx32_raw[];
+  float* smx32 = align128(smx32_raw);
+  __shared__ __align__(8) unsigned long long bar[2];
+  const int n = T.nlon, nf = n + 1, L = mixed_rows_x(n);
+  float* const H0 = smx32;  // H[p + kHoX], p in [-3, n+2]
+  float* const L0 = smx32 + L;
+  float* const H1 = smx32 + (kTma ? 2 * L : 0);
+  float* const L1 = smx32 + (kTma ? 3 * L : L);
+  float* Dl = smx32 + (kTma ? 4 : 2) * L;  // Dl[p + kHoX] = v(p+1) - v(p), p in [-3, n+1]
+  float* S = Dl + L;                       // S[p + kHoX], slopes of cells p in [-2, n+1]
+  float* Mf32 = S + L;                     // [n+1]
+  double* Mf = reinterpret_cast<double*>(Mf32 + (nf + 1) / 2 * 2);  // [n+1]
   const int row = blockIdx.x;
   const int j = row % T.nlat, k = row / T.nlat;
   const size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
   const size_t rbase = ((size_t)k * T.nlat + j) * n;
   const bool periodic = T.lon_bc == 0;
-  for (int f = threadIdx.x; f <= n; f += blockDim.x) Mf[f] = g * T.mx[((size_t)k * T.nlat + j) * nf + f];
-  for (int s = s0; s < s1; ++s) {
+  const int tid = threadIdx.x;
+  int uses0 = 0, uses1 = 0;  // copies issued per buffer
+  auto issue = [&](int s, int b) {  // one tracer's interior hi / lo rows (n floats each)
     const size_t pb = (size_t)s * nc + rbase;
-    for (int p = threadIdx.x - 3; p <= n + 2; p += blockDim.x) {
-      float h, l;
-      if (p < 0 || p >= n) {
+    fence_proxy_async();
+    mbar_expect_tx(bar + b, (uint32_t)(2 * n * sizeof(float)));
+    bulk_load((b ? H1 : H0) + kHoX, T.qhi + pb, (uint32_t)(n * sizeof(float)), bar + b);
+    bulk_load((b ? L1 : L0) + kHoX, T.qlo + pb, (uint32_t)(n * sizeof(float)), bar + b);
+  };
+  if (kTma) {
+    if (tid == 0) {
+      mbar_init(bar);
+      mbar_init(bar + 1);
+      fence_mbar_init();
+    }
+    __syncthreads();
+    if (tid == 0 && s0 < s1) issue(s0, 0);
+    uses0 = s0 < s1;
+  }
+  for (int f = tid; f <= n; f += blockDim.x) {
+    const double M = g * T.mx[((size_t)k * T.nlat + j) * nf + f];
+    Mf[f] = M;
+    Mf32[f] = (float)M;
+  }
+  for (int s = s0; s < s1; ++s) {
+    const int it = s - s0, b = kTma ? (it & 1) : 0;
+    float* H = b ? H1 : H0;
+    float* Lo = b ? L1 : L0;
+    const size_t pb = (size_t)s * nc + rbase;
+    if (kTma) {
+      if (s + 1 < s1) {
+        if (tid == 0) issue(s + 1, b ^ 1);
+        if (b) uses0 += 1;
+        else uses1 += 1;
+      }
+      if (tid < 6) {  // the three ghost cells on each side
+        const int p = tid < 3 ? tid - 3 : n + tid - 3;
+        float h, l;
         if (periodic) {
-          const int q = ((p % n) + n) % n;
+          const int q = p < 0 ? p + n : p - n;
           h = T.qhi[pb + q];
           l = T.qlo[pb + q];
         } else {
           split_d((p < 0 ? T.qw : T.qe)[((size_t)s * T.nlev + k) * T.nlat + j], h, l);
         }
-      } else {
-        h = T.qhi[pb + p];
-        l = T.qlo[pb + p];
+        H[p + kHoX] = h;
+        Lo[p + kHoX] = l;
       }
-      H[p + 3] = h;
-      Lo[p + 3] = l;
+      const bool ok = mbar_wait_bounded(bar + b, (uint32_t)(((it >> 1)) & 1));
+      if (__syncthreads_or(!ok)) {
+        staging_abort(T.tma_err, sel.ctl, bar, uses0, uses1);
+        return;
+      }
+    } else {
+      for (int p = tid - 3; p <= n + 2; p += blockDim.x) {
+        float h, l;
+        if (p < 0 || p >= n) {
+          if (periodic) {
+            const int q = ((p % n) + n) % n;
+            h = T.qhi[pb + q];
+            l = T.qlo[pb + q];
+          } else {
+            split_d((p < 0 ? T.qw : T.qe)[((size_t)s * T.nlev + k) * T.nlat + j], h, l);
+          }
+        } else {
+          h = T.qhi[pb + p];
+          l = T.qlo[pb + p];
+        }
+        H[p + kHoX] = h;
+        Lo[p + kHoX] = l;
+      }
+      __syncthreads();
     }
+    for (int p = tid - 3; p <= n + 1; p += blockDim.x)
+      Dl[p + kHoX] = (H[p + kHoX + 1] - H[p + kHoX]) + (Lo[p + kHoX + 1] - Lo[p + kHoX]);
     __syncthreads();
-    for (int p = threadIdx.x - 3; p <= n + 1; p += blockDim.x)
-      Dl[p + 3] = (H[p + 4] - H[p + 3]) + (Lo[p + 4] - Lo[p + 3]);
+    for (int p = tid - 2; p <= n + 1; p += blockDim.x)
+      S[p + kHoX] = slope_from_diff(Dl[p + kHoX - 1], Dl[p + kHoX]);
     __syncthreads();
-    for (int p = threadIdx.x - 2; p <= n + 1; p += blockDim.x) S[p + 3] = slope_from_diff(Dl[p + 2], Dl[p + 3]);
-    __syncthreads();
-    for (int f = threadIdx.x; f <= n; f += blockDim.x) {
+    auto face = [&](int f, bool ghosts) {
       const double M = Mf[f];
       const bool right = __double_as_longlong(M) > 0;
       const int up = right ? f - 1 : f;
-      float aL = -0.5f * Dl[up + 2] - (S[up + 3] - S[up + 2]) * (1.0f / 6.0f);
-      float aR = 0.5f * Dl[up + 3] - (S[up + 4] - S[up + 3]) * (1.0f / 6.0f);
+      const int u = up + kHoX;
+      float aL = -0.5f * Dl[u - 1] - (S[u] - S[u - 1]) * (1.0f / 6.0f);
+      float aR = 0.5f * Dl[u] - (S[u + 1] - S[u]) * (1.0f / 6.0f);
       limitf(0.0f, aL, aR);
       double a2;
-      if (up >= 0 && up < n) a2 = Q[pb + up];
-      else if (periodic) a2 = Q[pb + (up < 0 ? n - 1 : 0)];
-      else a2 = (double)H[up + 3] + (double)Lo[up + 3];
+      if (!ghosts) a2 = Q[pb + (up < 0 ? n - 1 : (up >= n ? 0 : up))];
+      else if (up >= 0 && up < n) a2 = Q[pb + up];
+      else a2 = (double)H[u] + (double)Lo[u];
       T.fx[((size_t)s * T.nlev * T.nlat + (size_t)k * T.nlat + j) * nf + f] =
-          M * (a2 + (double)(right ? aR : aL));
-    }
+          mixed_flux(M, Mf32[f], a2, right ? aR : aL);
+    };
+    if (periodic)
+      for (int f = tid; f <= n; f += blockDim.x) face(f, false);
+    else
+      for (int f = tid; f <= n; f += blockDim.x) face(f, true);
     __syncthreads();
   }
 }
 
-template <int kPencil>
-__global__ void __launch_bounds__(512) k_flux_y_mixed(DevTransport<double> T, StageSel sel, int sper) {
+template <int kPencil, bool kTma>
+__global__ void __launch_bounds__(512) k_flux_y_mixed(DevTransport<double> T, StageSel sel, int sper,
+                                                      const __grid_constant__ CUtensorMap mh,
+                                                      const __grid_constant__ CUtensorMap ml) {
   const double* Q;
   double g;
   if (!resolve_stage(sel, Q, g)) return;
   const int s0 = blockIdx.y * sper, s1 = min(T.ntr, s0 + sper);  // this block's tracers
-  extern __shared__ double smym[];
-  const int n = T.nlat, nfj = n + 1, L = n + 6;
-  double* Mf = smym;                                         // [n+1][kPencil]
-  float* H = reinterpret_cast<float*>(smym + nfj * kPencil);  // [L][kPencil]
-  float* Lo = H + L * kPencil;
-  float* Dl = Lo + L * kPencil;
-  float* S = Dl + L * kPencil;
+  extern __shared__ __align__(16) unsigned char smy32_raw[];
+  float* smy32 = align128(smy32_raw);
+  __shared__ __align__(8) unsigned long long bar[2];
+  const int n = T.nlat, nfj = n + 1, L = mixed_rows_p(n);
+  const int R = L * kPencil;  // one row set [L][kPencil], cell p at row p + kHoP
+  float* const H0 = smy32;
+  float* const L0 = smy32 + R;
+  float* const H1 = smy32 + (kTma ? 2 * R : 0);
+  float* const L1 = smy32 + (kTma ? 3 * R : R);
+  float* Dl = smy32 + (kTma ? 4 : 2) * R;
+  float* S = Dl + R;
+  float* Mf32 = S + R;  // [n+1][kPencil]
+  double* Mf = reinterpret_cast<double*>(Mf32 + nfj * kPencil);
   const int tx = threadIdx.x, ty = threadIdx.y;
+  const bool lead = tx == 0 && ty == 0;
   const int ntile = (T.nlon + kPencil - 1) / kPencil;
   const int k = blockIdx.x / ntile;
-  const int i = (blockIdx.x % ntile) * kPencil + tx;
+  const int i0 = (blockIdx.x % ntile) * kPencil;
+  const int i = i0 + tx;
   const bool live = i < T.nlon;
   const size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
   const size_t fplane = (size_t)T.nlev * nfj * T.nlon;
   const bool open = T.lat_bc == 1;
-  if (live)
-    for (int f = ty; f <= n; f += blockDim.y)
-      Mf[f * kPencil + tx] = g * T.my[((size_t)k * nfj + f) * T.nlon + i];
-  for (int s = s0; s < s1; ++s) {
-    const size_t pb = (size_t)s * nc + (size_t)k * T.nlat * T.nlon;
-    for (int p = (int)ty - 3; p <= n + 2; p += blockDim.y) {
-      float h = 0.0f, l = 0.0f;
-      if (live) {
-        if (p < 0 || p >= n) {
-          if (open) {
-            split_d((p < 0 ? T.qs : T.qn)[((size_t)s * T.nlev + k) * T.nlon + i], h, l);
-          } else {
-            const size_t q = (size_t)(p < 0 ? -1 - p : 2 * n - 1 - p) * T.nlon + i;
-            h = T.qhi[pb + q];
-            l = T.qlo[pb + q];
-          }
-        } else {
-          h = T.qhi[pb + (size_t)p * T.nlon + i];
-          l = T.qlo[pb + (size_t)p * T.nlon + i];
-        }
-      }
-      H[(p + 3) * kPencil + tx] = h;
-      Lo[(p + 3) * kPencil + tx] = l;
+  int uses0 = 0, uses1 = 0;  // copies issued per buffer
+  auto issue = [&](int s, int b) {  // interior rows 0..n-1 of (i0.., k, s): box {kPencil, n, 1}
+    fence_proxy_async();
+    mbar_expect_tx(bar + b, (uint32_t)(2 * n * kPencil * sizeof(float)));
+    tma_load_3d((b ? H1 : H0) + kHoP * kPencil, &mh, i0, 0, k + s * T.nlev, bar + b);
+    tma_load_3d((b ? L1 : L0) + kHoP * kPencil, &ml, i0, 0, k + s * T.nlev, bar + b);
+  };
+  if (kTma) {
+    if (lead) {
+      mbar_init(bar);
+      mbar_init(bar + 1);
+      fence_mbar_init();
     }
     __syncthreads();
+    if (lead && s0 < s1) issue(s0, 0);
+    uses0 = s0 < s1;
+  }
+  if (live)
+    for (int f = ty; f <= n; f += blockDim.y) {
+      const double M = g * T.my[((size_t)k * nfj + f) * T.nlon + i];
+      Mf[f * kPencil + tx] = M;
+      Mf32[f * kPencil + tx] = (float)M;
+    }
+#define RS_Y(a, p) a[((p) + kHoP) * kPencil + tx]
+  for (int s = s0; s < s1; ++s) {
+    const int it = s - s0, b = kTma ? (it & 1) : 0;
+    float* H = b ? H1 : H0;
+    float* Lo = b ? L1 : L0;
+    const size_t pb = (size_t)s * nc + (size_t)k * T.nlat * T.nlon;
+    auto cell = [&](int p, float& h, float& l) {  // a ghost (p outside 0..n-1) or interior cell
+      h = 0.0f;
+      l = 0.0f;
+      if (!live) return;
+      if (p < 0 || p >= n) {
+        if (open) {
+          split_d((p < 0 ? T.qs : T.qn)[((size_t)s * T.nlev + k) * T.nlon + i], h, l);
+          return;
+        }
+        p = p < 0 ? -1 - p : 2 * n - 1 - p;
+      }
+      h = T.qhi[pb + (size_t)p * T.nlon + i];
+      l = T.qlo[pb + (size_t)p * T.nlon + i];
+    };
+    if (kTma) {
+      if (s + 1 < s1) {
+        if (lead) issue(s + 1, b ^ 1);
+        if (b) uses0 += 1;
+        else uses1 += 1;
+      }
+      for (int r = ty; r < 6; r += blockDim.y) {
+        const int p = r < 3 ? r - 3 : n + r - 3;
+        float h, l;
+        cell(p, h, l);
+        RS_Y(H, p) = h;
+        RS_Y(Lo, p) = l;
+      }
+      const bool ok = mbar_wait_bounded(bar + b, (uint32_t)((it >> 1) & 1));
+      if (__syncthreads_or(!ok)) {
+        staging_abort(T.tma_err, sel.ctl, bar, uses0, uses1);
+        return;
+      }
+    } else {
+      for (int p = (int)ty - 3; p <= n + 2; p += blockDim.y) {
+        float h, l;
+        cell(p, h, l);
+        RS_Y(H, p) = h;
+        RS_Y(Lo, p) = l;
+      }
+      __syncthreads();
+    }
     for (int p = (int)ty - 3; p <= n + 1; p += blockDim.y)
-      Dl[(p + 3) * kPencil + tx] = (H[(p + 4) * kPencil + tx] - H[(p + 3) * kPencil + tx]) +
-                                   (Lo[(p + 4) * kPencil + tx] - Lo[(p + 3) * kPencil + tx]);
+      RS_Y(Dl, p) = (RS_Y(H, p + 1) - RS_Y(H, p)) + (RS_Y(Lo, p + 1) - RS_Y(Lo, p));
     __syncthreads();
     for (int p = (int)ty - 2; p <= n + 1; p += blockDim.y)
-      S[(p + 3) * kPencil + tx] = slope_from_diff(Dl[(p + 2) * kPencil + tx], Dl[(p + 3) * kPencil + tx]);
+      RS_Y(S, p) = slope_from_diff(RS_Y(Dl, p - 1), RS_Y(Dl, p));
     __syncthreads();
+    auto face = [&](int f, bool ghosts) {
+      const size_t fb = ((size_t)k * nfj + f) * T.nlon + i;
+      const double M = Mf[f * kPencil + tx];
+      const bool right = __double_as_longlong(M) > 0;
+      const int up = right ? f - 1 : f;
+      float aL = -0.5f * RS_Y(Dl, up - 1) - (RS_Y(S, up) - RS_Y(S, up - 1)) * (1.0f / 6.0f);
+      float aR = 0.5f * RS_Y(Dl, up) - (RS_Y(S, up + 1) - RS_Y(S, up)) * (1.0f / 6.0f);
+      limitf(0.0f, aL, aR);
+      double a2;
+      if (!ghosts || (up >= 0 && up < n)) a2 = Q[pb + (size_t)up * T.nlon + i];
+      else a2 = (double)RS_Y(H, up) + (double)RS_Y(Lo, up);
+      T.fy[(size_t)s * fplane + fb] = mixed_flux(M, Mf32[f * kPencil + tx], a2, right ? aR : aL);
+    };
     if (live) {
-      for (int f = ty; f <= n; f += blockDim.y) {
-        const size_t fb = ((size_t)k * nfj + f) * T.nlon + i;
-        if (!open && (f == 0 || f == n)) {
-          T.fy[(size_t)s * fplane + fb] = 0.0;
-          continue;
+      if (open) {
+        for (int f = ty; f <= n; f += blockDim.y) face(f, true);
+      } else {  // walls: zero flux on the two boundary faces, interior faces have no ghosts
+        for (int f = ty; f <= n; f += blockDim.y) {
+          if (f == 0 || f == n) T.fy[(size_t)s * fplane + ((size_t)k * nfj + f) * T.nlon + i] = 0.0;
+          else face(f, false);
         }
-        const double M = Mf[f * kPencil + tx];
-        const bool right = __double_as_longlong(M) > 0;
-        const int up = right ? f - 1 : f;
-        float aL = -0.5f * Dl[(up + 2) * kPencil + tx] -
-                   (S[(up + 3) * kPencil + tx] - S[(up + 2) * kPencil + tx]) * (1.0f / 6.0f);
-        float aR = 0.5f * Dl[(up + 3) * kPencil + tx] -
-                   (S[(up + 4) * kPencil + tx] - S[(up + 3) * kPencil + tx]) * (1.0f / 6.0f);
-        limitf(0.0f, aL, aR);
-        const double a2 = (up >= 0 && up < n) ? Q[pb + (size_t)up * T.nlon + i]
-                        : (double)H[(up + 3) * kPencil + tx] + (double)Lo[(up + 3) * kPencil + tx];
-        T.fy[(size_t)s * fplane + fb] = M * (a2 + (double)(right ? aR : aL));
       }
     }
     __syncthreads();
   }
+#undef RS_Y
 }
 
-template <int kPencil>
-__global__ void __launch_bounds__(512) k_flux_z_mixed(DevTransport<double> T, StageSel sel, int sper) {
+template <int kPencil, bool kTma>
+__global__ void __launch_bounds__(512) k_flux_z_mixed(DevTransport<double> T, StageSel sel, int sper,
+                                                      const __grid_constant__ CUtensorMap mh,
+                                                      const __grid_constant__ CUtensorMap ml) {
   const double* Q;
   double g;
   if (!resolve_stage(sel, Q, g)) return;
   const int s0 = blockIdx.y * sper, s1 = min(T.ntr, s0 + sper);  // this block's tracers
-  extern __shared__ double smzm[];
-  const int n = T.nlev, L = n + 6;
-  double* Mf = smzm;                                          // [n+1][kPencil]
-  float* H = reinterpret_cast<float*>(smzm + (n + 1) * kPencil);
-  float* Lo = H + L * kPencil;
-  float* Dl = Lo + L * kPencil;
-  float* S = Dl + L * kPencil;
+  extern __shared__ __align__(16) unsigned char smz32_raw[];
+  float* smz32 = align128(smz32_raw);
+  __shared__ __align__(8) unsigned long long bar[2];
+  const int n = T.nlev, L = mixed_rows_p(n);
+  const int R = L * kPencil;
+  float* const H0 = smz32;
+  float* const L0 = smz32 + R;
+  float* const H1 = smz32 + (kTma ? 2 * R : 0);
+  float* const L1 = smz32 + (kTma ? 3 * R : R);
+  float* Dl = smz32 + (kTma ? 4 : 2) * R;
+  float* S = Dl + R;
+  float* Mf32 = S + R;  // [n+1][kPencil]
+  double* Mf = reinterpret_cast<double*>(Mf32 + (n + 1) * kPencil);
   const int tx = threadIdx.x, ty = threadIdx.y;
+  const bool lead = tx == 0 && ty == 0;
   const size_t ncol = (size_t)T.nlon * T.nlat;
-  const size_t col = (size_t)blockIdx.x * kPencil + tx;
+  const size_t col0 = (size_t)blockIdx.x * kPencil;
+  const size_t col = col0 + tx;
   const bool live = col < ncol;
   const size_t nc = ncol * n;
   const size_t fplane = ncol * (n + 1);
-  if (live)
-    for (int kf = ty; kf <= n; kf += blockDim.y) Mf[kf * kPencil + tx] = g * T.mz[(size_t)kf * ncol + col];
-  for (int s = s0; s < s1; ++s) {
-    const size_t pb = (size_t)s * nc + col;
-    for (int p = (int)ty - 3; p <= n + 2; p += blockDim.y) {
-      const int pp = p < 0 ? -1 - p : (p >= n ? 2 * n - 1 - p : p);
-      H[(p + 3) * kPencil + tx] = live ? T.qhi[pb + (size_t)pp * ncol] : 0.0f;
-      Lo[(p + 3) * kPencil + tx] = live ? T.qlo[pb + (size_t)pp * ncol] : 0.0f;
+  int uses0 = 0, uses1 = 0;  // copies issued per buffer
+  auto issue = [&](int s, int b) {  // levels 0..n-1 of columns col0..: box {kPencil, n, 1}
+    fence_proxy_async();
+    mbar_expect_tx(bar + b, (uint32_t)(2 * n * kPencil * sizeof(float)));
+    tma_load_3d((b ? H1 : H0) + kHoP * kPencil, &mh, (int)col0, 0, s, bar + b);
+    tma_load_3d((b ? L1 : L0) + kHoP * kPencil, &ml, (int)col0, 0, s, bar + b);
+  };
+  if (kTma) {
+    if (lead) {
+      mbar_init(bar);
+      mbar_init(bar + 1);
+      fence_mbar_init();
     }
     __syncthreads();
+    if (lead && s0 < s1) issue(s0, 0);
+    uses0 = s0 < s1;
+  }
+  if (live)
+    for (int kf = ty; kf <= n; kf += blockDim.y) {
+      const double M = g * T.mz[(size_t)kf * ncol + col];
+      Mf[kf * kPencil + tx] = M;
+      Mf32[kf * kPencil + tx] = (float)M;
+    }
+#define RS_Z(a, p) a[((p) + kHoP) * kPencil + tx]
+  for (int s = s0; s < s1; ++s) {
+    const int it = s - s0, b = kTma ? (it & 1) : 0;
+    float* H = b ? H1 : H0;
+    float* Lo = b ? L1 : L0;
+    const size_t pb = (size_t)s * nc + col;
+    if (kTma) {
+      if (s + 1 < s1) {
+        if (lead) issue(s + 1, b ^ 1);
+        if (b) uses0 += 1;
+        else uses1 += 1;
+      }
+      for (int r = ty; r < 6; r += blockDim.y) {  // mirrored ghost levels
+        const int p = r < 3 ? r - 3 : n + r - 3;
+        const int pp = p < 0 ? -1 - p : 2 * n - 1 - p;
+        RS_Z(H, p) = live ? T.qhi[pb + (size_t)pp * ncol] : 0.0f;
+        RS_Z(Lo, p) = live ? T.qlo[pb + (size_t)pp * ncol] : 0.0f;
+      }
+      const bool ok = mbar_wait_bounded(bar + b, (uint32_t)((it >> 1) & 1));
+      if (__syncthreads_or(!ok)) {
+        staging_abort(T.tma_err, sel.ctl, bar, uses0, uses1);
+        return;
+      }
+    } else {
+      for (int p = (int)ty - 3; p <= n + 2; p += blockDim.y) {
+        const int pp = p < 0 ? -1 - p : (p >= n ? 2 * n - 1 - p : p);
+        RS_Z(H, p) = live ? T.qhi[pb + (size_t)pp * ncol] : 0.0f;
+        RS_Z(Lo, p) = live ? T.qlo[pb + (size_t)pp * ncol] : 0.0f;
+      }
+      __syncthreads();
+    }
     for (int p = (int)ty - 3; p <= n + 1; p += blockDim.y)
-      Dl[(p + 3) * kPencil + tx] = (H[(p + 4) * kPencil + tx] - H[(p + 3) * kPencil + tx]) +
-                                   (Lo[(p + 4) * kPencil + tx] - Lo[(p + 3) * kPencil + tx]);
+      RS_Z(Dl, p) = (RS_Z(H, p + 1) - RS_Z(H, p)) + (RS_Z(Lo, p + 1) - RS_Z(Lo, p));
     __syncthreads();
     for (int p = (int)ty - 1; p <= n; p += blockDim.y) {  // slopes of cells -1..n (coefficient row p+1)
       const float sA = live ? T.vsA32[(size_t)(p + 1) * ncol + col] : 0.0f;
       const float sB = live ? T.vsB32[(size_t)(p + 1) * ncol + col] : 0.0f;
-      S[(p + 3) * kPencil + tx] =
-          slope_from_diff_n(Dl[(p + 2) * kPencil + tx], Dl[(p + 3) * kPencil + tx], sA, sB);
+      RS_Z(S, p) = slope_from_diff_n(RS_Z(Dl, p - 1), RS_Z(Dl, p), sA, sB);
     }
     __syncthreads();
     if (live) {
@@ -754,17 +1020,17 @@ __global__ void __launch_bounds__(512) k_flux_z_mixed(DevTransport<double> T, St
         const float rab = T.veAB32[(size_t)(up + 1) * ncol + col],
                     rc = T.veC32[(size_t)(up + 1) * ncol + col],
                     rd = T.veD32[(size_t)(up + 1) * ncol + col];
-        float aL = (lab - 1.0f) * Dl[(up + 2) * kPencil + tx] + lc * S[(up + 3) * kPencil + tx] +
-                   ld * S[(up + 2) * kPencil + tx];
-        float aR = rab * Dl[(up + 3) * kPencil + tx] + rc * S[(up + 4) * kPencil + tx] +
-                   rd * S[(up + 3) * kPencil + tx];
+        float aL = (lab - 1.0f) * RS_Z(Dl, up - 1) + lc * RS_Z(S, up) + ld * RS_Z(S, up - 1);
+        float aR = rab * RS_Z(Dl, up) + rc * RS_Z(S, up + 1) + rd * RS_Z(S, up);
         limitf(0.0f, aL, aR);
         const double a2 = Q[pb + (size_t)up * ncol];
-        T.fz[(size_t)s * fplane + (size_t)kf * ncol + col] = M * (a2 + (double)(right ? aR : aL));
+        T.fz[(size_t)s * fplane + (size_t)kf * ncol + col] =
+            mixed_flux(M, Mf32[kf * kPencil + tx], a2, right ? aR : aL);
       }
     }
     __syncthreads();
   }
+#undef RS_Z
 }
 
 // ------------------------------------------------------------------ stage kernel
@@ -897,10 +1163,16 @@ __global__ void __launch_bounds__(kRedThreads) k_stage(DevTransport<double> T,
     const size_t fxi = ((size_t)k * T.nlat + j) * nfx + i;
     const size_t fyi = ((size_t)k * nfy + j) * T.nlon + i;
     const size_t fzi = (size_t)k * ncol + col;
+#if !RS_STRICT
+    const double sc = dt_2 * rm;  // the tracer increment is (a + q divM) * sc without PBL mixing
+#endif
     for (int s = 0; s < T.nsp; ++s) {
       size_t x = (size_t)s * nc + c;
       double q = Qin[x];
-      double du;
+      // the stage's new value is q + dt/2 * f: nx = q + dt_2 * du (strict: the oracle's
+      // expression order); the production build forms it as fma(du, scale, q), folding 1/m
+      // into the scale when no PBL term is added
+      double du, scale = dt_2;
       if (s < T.ntr) {
         double fw = T.fx[s * fxp + fxi], fe = T.fx[s * fxp + fxi + 1];
         double fs = T.fy[s * fyp + fyi], fn = T.fy[s * fyp + fyi + T.nlon];
@@ -909,26 +1181,35 @@ __global__ void __launch_bounds__(kRedThreads) k_stage(DevTransport<double> T,
         double Dy = fn * G.gyhi - fs * G.gylo;
         double Dz = ft - fb;
         double a = -((Dx + Dy) + Dz);
-        double b = q * divM;
 #if RS_STRICT
+        double b = q * divM;
         du = (a + b) / m;
-#else
-        du = (a + b) * rm;
-#endif
         if (T.pbl) du = du + pbl_term(T, c, col, s, q);
+#else
+        const double ab = fma(q, divM, a);
+        if (T.pbl) {
+          du = fma(ab, rm, pbl_term(T, c, col, s, q));
+        } else {
+          du = ab;
+          scale = sc;
+        }
+#endif
       } else {
         du = dm_dt(T, i, j, k, g, G, c);
       }
+#if RS_STRICT
+      const double nx = q + dt_2 * du;
+#else
+      const double nx = fma(du, scale, q);
+#endif
       if (STAGE == 1) {
-        double nx = q + dt_2 * du;
         B.S1[x] = nx;
         if (T.mixed && s < T.ntr) split_store(T, x, nx);
       } else if (STAGE == 2) {
-        double nx = q + dt_2 * du;
         B.S2[x] = nx;
         if (T.mixed && s < T.ntr) split_store(T, x, nx);
       } else if (STAGE == 3) {
-        double u3 = q + dt_2 * du;
+        double u3 = nx;
         double u0 = U[x];
         B.S1[x] = u3;
         double u4 = (2.0 / 3.0) * u0 + (1.0 / 3.0) * u3;
@@ -938,11 +1219,15 @@ __global__ void __launch_bounds__(kRedThreads) k_stage(DevTransport<double> T,
         double u0 = U[x];
         double u3 = B.S1[x];
         double ut = (1.0 / 3.0) * u0 + (2.0 / 3.0) * u3;
-        double un = q + dt_2 * du;
+        double un = nx;
         double err = 0.5 * (ut - un);
         double am = fmax(fabs(u0), fabs(un));
         double den = am * rtol + atol;
+#if RS_STRICT
         double at = err / den;
+#else
+        double at = err * rcp_nr(den);  // den >= atol > 0
+#endif
         e = e + at * at;
         Un[x] = clamp ? fmax(un, 0.0) : un;
       }
@@ -1009,11 +1294,16 @@ static void allow_big_smem() {
   cudaFuncSetAttribute(k_flux_y_fused<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
   cudaFuncSetAttribute(k_flux_z_fused<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
   cudaFuncSetAttribute(k_flux_z_fused<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
-  cudaFuncSetAttribute(k_flux_x_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
-  cudaFuncSetAttribute(k_flux_y_mixed<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
-  cudaFuncSetAttribute(k_flux_y_mixed<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
-  cudaFuncSetAttribute(k_flux_z_mixed<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
-  cudaFuncSetAttribute(k_flux_z_mixed<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_flux_x_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_flux_x_mixed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_flux_y_mixed<16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_flux_y_mixed<32, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_flux_y_mixed<16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_flux_y_mixed<32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_flux_z_mixed<16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_flux_z_mixed<32, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_flux_z_mixed<16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_flux_z_mixed<32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
   done = true;
 }
 
@@ -1076,28 +1366,114 @@ static void launch_flux_one(cudaStream_t st, const DevTransport<double>& T, cons
   }
 }
 
-// Mixed-precision pencils: the n+1 FP64 face fluxes plus four FP32 rows (hi, lo, neighbour
-// differences, slopes; n+6 each) per pencil.  A direction that does not fit uses the per-face
-// FP32 kernel (the same deviation-form reconstruction, evaluated per face).
-static size_t mixed_pencil_bytes(int n, int pw) {
-  return ((size_t)(n + 1) * sizeof(double) + (size_t)4 * (n + 6) * sizeof(float)) * pw;
+// Mixed-precision pencils: four FP32 rows (hi, lo, neighbour differences, slopes; six with the
+// second hi / lo set of the bulk-copy staging) plus the n+1 face fluxes as float and double, per
+// pencil.  A direction that does not fit uses the per-face FP32 kernel (the same deviation-form
+// reconstruction, evaluated per face).
+static size_t mixed_pencil_bytes(int n, int pw, bool tma) {
+  const int rows = tma ? 6 : 4;
+  if (pw == 1) {
+    const int L = mixed_rows_x(n);
+    return (size_t)rows * L * sizeof(float) + (size_t)((n + 2) / 2 * 2) * sizeof(float) +
+           (size_t)(n + 1) * sizeof(double) + kSmemAlignPad;
+  }
+  const int L = mixed_rows_p(n);
+  return ((size_t)rows * L * sizeof(float) + (size_t)(n + 1) * (sizeof(float) + sizeof(double))) * pw +
+         kSmemAlignPad;
 }
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link to the driver
+// library); null when the entry point is unavailable.
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    else
+      cudaGetLastError();
+  }
+  return fn;
+}
+
+// 3-D FP32 tensor {d0, d1, d2} (d0 contiguous) with box {b0, b1, 1}; false if rejected.
+static bool encode_f32_3d(CUtensorMap* m, float* base, uint64_t d0, uint64_t d1, uint64_t d2,
+                          uint32_t b0, uint32_t b1) {
+  auto enc = tensor_map_encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[3] = {d0, d1, d2};
+  const cuuint64_t strides[2] = {d0 * sizeof(float), d0 * d1 * sizeof(float)};
+  const cuuint32_t box[3] = {b0, b1, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+MixedTmaps* mixed_tmaps_create(const DevTransport<double>& T, const char** why) {
+  *why = nullptr;
+  if (!T.qhi || !T.qlo) {
+    *why = "no split planes (FP64 transport)";
+    return nullptr;
+  }
+  auto* m = new MixedTmaps();
+  const uint64_t ncol = (uint64_t)T.nlon * T.nlat;
+  // 1-D bulk copies of lon rows: 16-byte aligned starts and sizes need nlon % 4 == 0
+  m->x_ok = T.nlon % 4 == 0;
+  // tensor strides must be multiples of 16 bytes; boxes at most 256 rows
+  m->y_ok = T.nlon % 4 == 0 && T.nlat <= 256;
+  m->z_ok = ncol % 4 == 0 && T.nlev <= 256;
+  for (int w = 0; w < 2 && m->y_ok; ++w) {
+    const uint32_t pw = w ? 32 : 16;
+    m->y_ok = encode_f32_3d(&m->yh[w], T.qhi, T.nlon, T.nlat, (uint64_t)T.nlev * T.ntr, pw, T.nlat) &&
+              encode_f32_3d(&m->yl[w], T.qlo, T.nlon, T.nlat, (uint64_t)T.nlev * T.ntr, pw, T.nlat);
+  }
+  for (int w = 0; w < 2 && m->z_ok; ++w) {
+    const uint32_t pw = w ? 32 : 16;
+    m->z_ok = encode_f32_3d(&m->zh[w], T.qhi, ncol, T.nlev, T.ntr, pw, T.nlev) &&
+              encode_f32_3d(&m->zl[w], T.qlo, ncol, T.nlev, T.ntr, pw, T.nlev);
+  }
+  if (!m->x_ok && !m->y_ok && !m->z_ok) {
+    *why = "grid does not meet the bulk-copy alignment rules";
+    delete m;
+    return nullptr;
+  }
+  return m;
+}
+
+void mixed_tmaps_destroy(MixedTmaps* m) { delete m; }
+bool mixed_tmaps_dir_ok(const MixedTmaps* m, int dir) {
+  return m && (dir == 0 ? m->x_ok : (dir == 1 ? m->y_ok : m->z_ok));
+}
+
 static void launch_fluxes_mixed(cudaStream_t st, const DevTransport<double>& T, const StageSel& sel,
                                 int only_dir = -1) {
   int pw = T.mpencil == 16 ? 16 : 32;
-  if (mixed_pencil_bytes(T.nlat, pw) > (size_t)kPencilSmemCap ||
-      mixed_pencil_bytes(T.nlev, pw) > (size_t)kPencilSmemCap)
+  const MixedTmaps* tm = T.tma;
+  const bool tx = tm && tm->x_ok && T.mbulk_x, ty = tm && tm->y_ok && T.mbulk_yz,
+             tz = tm && tm->z_ok && T.mbulk_yz;
+  if (mixed_pencil_bytes(T.nlat, pw, ty) > (size_t)kPencilSmemCap ||
+      mixed_pencil_bytes(T.nlev, pw, tz) > (size_t)kPencilSmemCap)
     pw = 16;
+  const int w = pw == 32;
   const int rows = (T.mrows == 4 || T.mrows == 16) ? T.mrows : 8;
   const int xt = (T.mxthreads == 64 || T.mxthreads == 256) ? T.mxthreads : 128;
   auto groups = [&](int sper) { return (unsigned)((T.ntr + sper - 1) / sper); };
   const int sx = std::max(1, std::min(T.ntr, T.msper_x)), syz = std::max(1, std::min(T.ntr, T.msper_yz));
   const size_t ncol = (size_t)T.nlon * T.nlat;
-  const size_t shx = mixed_pencil_bytes(T.nlon, 1), shy = mixed_pencil_bytes(T.nlat, pw),
-               shz = mixed_pencil_bytes(T.nlev, pw);
+  const size_t shx = mixed_pencil_bytes(T.nlon, 1, tx), shy = mixed_pencil_bytes(T.nlat, pw, ty),
+               shz = mixed_pencil_bytes(T.nlev, pw, tz);
+  static const CUtensorMap kNoMap{};  // placeholder argument of the plain-load variants
   if (only_dir < 0 || only_dir == 0) {
     if (shx <= (size_t)kPencilSmemCap) {
-      k_flux_x_mixed<<<dim3((unsigned)(T.nlat * T.nlev), groups(sx)), xt, shx, st>>>(T, sel, sx);
+      dim3 grid((unsigned)(T.nlat * T.nlev), groups(sx));
+      if (tx) k_flux_x_mixed<true><<<grid, xt, shx, st>>>(T, sel, sx);
+      else k_flux_x_mixed<false><<<grid, xt, shx, st>>>(T, sel, sx);
     } else {
       long long nx = (long long)(T.nlon + 1) * T.nlat * T.nlev;
       k_flux_x<<<(unsigned)((nx + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);
@@ -1106,8 +1482,15 @@ static void launch_fluxes_mixed(cudaStream_t st, const DevTransport<double>& T, 
   if (only_dir < 0 || only_dir == 1) {
     if (shy <= (size_t)kPencilSmemCap) {
       dim3 grid((unsigned)((T.nlon + pw - 1) / pw) * (unsigned)T.nlev, groups(syz));
-      if (pw == 16) k_flux_y_mixed<16><<<grid, dim3(16, rows), shy, st>>>(T, sel, syz);
-      else k_flux_y_mixed<32><<<grid, dim3(32, rows), shy, st>>>(T, sel, syz);
+      const CUtensorMap& mh = ty ? tm->yh[w] : kNoMap;
+      const CUtensorMap& ml = ty ? tm->yl[w] : kNoMap;
+      if (pw == 16) {
+        if (ty) k_flux_y_mixed<16, true><<<grid, dim3(16, rows), shy, st>>>(T, sel, syz, mh, ml);
+        else k_flux_y_mixed<16, false><<<grid, dim3(16, rows), shy, st>>>(T, sel, syz, mh, ml);
+      } else {
+        if (ty) k_flux_y_mixed<32, true><<<grid, dim3(32, rows), shy, st>>>(T, sel, syz, mh, ml);
+        else k_flux_y_mixed<32, false><<<grid, dim3(32, rows), shy, st>>>(T, sel, syz, mh, ml);
+      }
     } else {
       long long ny = (long long)T.nlon * (T.nlat + 1) * T.nlev;
       k_flux_y<<<(unsigned)((ny + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);
@@ -1116,8 +1499,15 @@ static void launch_fluxes_mixed(cudaStream_t st, const DevTransport<double>& T, 
   if (only_dir < 0 || only_dir == 2) {
     if (shz <= (size_t)kPencilSmemCap) {
       dim3 grid((unsigned)((ncol + pw - 1) / pw), groups(syz));
-      if (pw == 16) k_flux_z_mixed<16><<<grid, dim3(16, rows), shz, st>>>(T, sel, syz);
-      else k_flux_z_mixed<32><<<grid, dim3(32, rows), shz, st>>>(T, sel, syz);
+      const CUtensorMap& mh = tz ? tm->zh[w] : kNoMap;
+      const CUtensorMap& ml = tz ? tm->zl[w] : kNoMap;
+      if (pw == 16) {
+        if (tz) k_flux_z_mixed<16, true><<<grid, dim3(16, rows), shz, st>>>(T, sel, syz, mh, ml);
+        else k_flux_z_mixed<16, false><<<grid, dim3(16, rows), shz, st>>>(T, sel, syz, mh, ml);
+      } else {
+        if (tz) k_flux_z_mixed<32, true><<<grid, dim3(32, rows), shz, st>>>(T, sel, syz, mh, ml);
+        else k_flux_z_mixed<32, false><<<grid, dim3(32, rows), shz, st>>>(T, sel, syz, mh, ml);
+      }
     } else {
       long long nz = (long long)T.nlon * T.nlat * (T.nlev + 1);
       k_flux_z<<<(unsigned)((nz + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);

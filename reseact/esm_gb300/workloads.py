@@ -327,4 +327,6 @@ def regional_freestream(n=7):
     dA = np.array([Ap[k] - Ap[k + 1] for k in range(7)])
     dB = np.array([Bp[k] - Bp[k + 1] for k in range(7)])
     dp = dA + dB * 101325.0
+    if n != 7:  # other sizes: the 7 layer thicknesses interpolated onto n layers
+        dp = np.interp(np.linspace(0.0, 6.0, n), np.arange(7.0), dp)
     return g, np.ascontiguousarray(mx), np.ascontiguousarray(my), mz, dp
