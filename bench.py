@@ -52,6 +52,8 @@ def parse():
     p.add_argument("--c3-cells", type=int, default=1 << 20)
     p.add_argument("--c3-skip-global", action="store_true", help="time only the per-cell form")
     p.add_argument("--small", action="store_true", help="small grid (profiling/debug)")
+    p.add_argument("--form", default="fp64", choices=["fp64", "mixed", "batched_mixed"],
+                   help="what the main timed loop runs (default: the plain FP64 method)")
     p.add_argument("--c5", type=int, default=0, metavar="STEPS",
                    help="also time STEPS macro steps of the full-scale C5 forms (several minutes)")
     return p.parse_args()
@@ -196,7 +198,13 @@ def run_gb300(args):
     from reseact.esm_gb300 import Solver, workloads
 
     w = workload(args.small)
-    solver = Solver.for_workload(w, device=local)
+    from reseact.esm_gb300 import abi as _abi0
+    form_kw = {"fp64": {}, "mixed": dict(precision=_abi0.RS_PREC_MIXED),
+               "batched_mixed": dict(precision=_abi0.RS_PREC_MIXED,
+                                     chem_mode=_abi0.RS_CHEM_PER_CELL)}[args.form]
+    solver = Solver.for_workload(w, device=local, **form_kw)
+    if args.form != "fp64":
+        args.no_forms = True  # the forms are compared against the plain FP64 main loop
     stream = torch.cuda.ExternalStream(solver.stream())
     nc = w.ncells
     u0 = w.u0_cellmajor()
@@ -315,11 +323,13 @@ def run_gb300(args):
 
     # ------------------------------------------------------------------ roofline pass
     t, dtT, dtC = t_end, dtT_end, dtC_end
-    solver.set_profiling(True)
+    solver.set_profiling(True)  # eager launches: the steps below are visible to a profiler
     solver.reset_profile()
+    torch.cuda.nvtx.range_push("profiled_steps")
     for _ in range(2):
         _, dtT, dtC, st = solver.macro_step(t, t + dtm, dtT, dtC)
         t += dtm
+    torch.cuda.nvtx.range_pop()
     prof = solver.profile()
     solver.set_profiling(False)
     peaks = fp64_peak() if rank == 0 else {}
@@ -373,9 +383,11 @@ def run_gb300(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (analytic deformational winds, seeded lognormal fields; GEOS-FP/NEI unavailable offline)",
-            "config": {"workload": WORKLOAD if not args.small else "C2-small 48x31x16",
+            "config": {"workload": (WORKLOAD if not args.small else "C2-small 48x31x16")
+                       + ("" if args.form == "fp64" else ", form " + args.form),
                        "cells": nc, "species_per_cell": w.nsp, "macro_dt_s": dtm,
-                       "chem_mode": "global dt (reference)", "precision": "FP64",
+                       "chem_mode": "per-cell dt" if args.form == "batched_mixed" else "global dt (reference)",
+                       "precision": "FP64" if args.form == "fp64" else "mixed (FP32 reconstruction)",
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": "256 MiB flush between timed steps"},
             "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "forms": forms,

@@ -264,5 +264,25 @@ function autotune!(h::Handle)
                    h.ptr, buf, length(buf)))
     return unsafe_string(pointer(buf))
 end
+# replay launch shapes reported by an earlier autotune!, e.g. set_launch_shape!(h; mixed_yz_tracers=2)
+function set_launch_shape!(h::Handle; shapes...)
+    for (k, v) in shapes
+        check(h, ccall((:rs_set_launch_shape, LIB[]), Int32, (Ptr{Cvoid}, Cstring, Int32),
+                       h.ptr, String(k), Int32(v)))
+    end
+    return h
+end
+const RS_STAGING_AUTO = Int32(0)
+const RS_STAGING_PLAIN = Int32(1)
+const RS_STAGING_BULK = Int32(2)
+set_transport_staging!(h::Handle, mode::Integer) =
+    check(h, ccall((:rs_set_transport_staging, LIB[]), Int32, (Ptr{Cvoid}, Int32), h.ptr, Int32(mode)))
+function transport_staging(h::Handle)
+    mode = Ref{Int32}(0)
+    buf = Vector{UInt8}(undef, 512)
+    check(h, ccall((:rs_get_transport_staging, LIB[]), Int32,
+                   (Ptr{Cvoid}, Ref{Int32}, Ptr{UInt8}, Csize_t), h.ptr, mode, buf, length(buf)))
+    return mode[], unsafe_string(pointer(buf))
+end
 
 end # module

@@ -58,13 +58,90 @@ __device__ __forceinline__ void limit(double a, double& aL, double& aR) {
     else if (-(dA * dA) > dA * a6) aR = 3.0 * a - 2.0 * aL;
   }
 }
+// ---- production-build forms of slope_u / slope_n / limit.  The same slopes, edges and limiter
+// decisions, with the sign tests and the exact power-of-two scalings done on the sign and
+// exponent bits in the integer pipes (FP64 issues at ~2 lanes per SM per clock on this GPU):
+//   d1*d0 > 0            <=>  d0, d1 nonzero with equal signs       (unless the product underflows)
+//   0.5*s, 2*m           =    exponent field -1 / +1                 (normal operands)
+//   fmin of magnitudes   =    integer min of the magnitude bits
+// so slopes and the extremum test are bit-identical to the FP forms for normal operands.  The
+// steepening tests dA*a6 > dA*dA and -(dA*dA) > dA*a6 become sign tests of dA and a6 -+ dA,
+// which can differ from the FP forms only where a6 = +-dA to roundoff -- where the limiter is
+// continuous (the steepened edge equals the unsteepened one), so a face moves by roundoff only.
+__device__ __forceinline__ bool sgn_same_nz(double a, double b) {
+  const int ha = __double2hiint(a), hb = __double2hiint(b);
+  const bool nza = ((ha & 0x7fffffff) | __double2loint(a)) != 0;
+  const bool nzb = ((hb & 0x7fffffff) | __double2loint(b)) != 0;
+  return ((ha ^ hb) >= 0) & nza & nzb;
+}
+__device__ __forceinline__ bool sgn_opp_nz(double a, double b) {
+  const int ha = __double2hiint(a), hb = __double2hiint(b);
+  const bool nza = ((ha & 0x7fffffff) | __double2loint(a)) != 0;
+  const bool nzb = ((hb & 0x7fffffff) | __double2loint(b)) != 0;
+  return ((ha ^ hb) < 0) & nza & nzb;
+}
+constexpr long long kMagMask = 0x7fffffffffffffffLL, kSignBit = (long long)0x8000000000000000ULL,
+                    kExpOne = 1LL << 52;
+// copysign(min(|da|, 2 min(|d0|, |d1|)), da) from |da| and da's sign as bits
+__device__ __forceinline__ double slope_pick(long long abs_da, long long sign_da, double d0, double d1) {
+  const long long m0 = __double_as_longlong(d0) & kMagMask, m1 = __double_as_longlong(d1) & kMagMask;
+  const long long lim = (m0 < m1 ? m0 : m1) + kExpOne;
+  return __longlong_as_double((abs_da < lim ? abs_da : lim) | sign_da);
+}
+__device__ __forceinline__ double slope_u_fast(double am, double a, double ap) {
+  const double d0 = a - am, d1 = ap - a;
+  if (!sgn_same_nz(d0, d1)) return 0.0;
+  const long long sb = __double_as_longlong(ap - am);  // nonzero here; |da| = |ap - am| / 2
+  return slope_pick((sb & kMagMask) - kExpOne, sb & kSignBit, d0, d1);
+}
+__device__ __forceinline__ double slope_n_fast(double am, double a, double ap, double sA, double sB) {
+  const double d0 = a - am, d1 = ap - a;
+  if (!sgn_same_nz(d0, d1)) return 0.0;
+  const long long db = __double_as_longlong(sA * d1 + sB * d0);
+  return slope_pick(db & kMagMask, db & kSignBit, d0, d1);
+}
+__device__ __forceinline__ void limit_fast(double a, double& aL, double& aR) {
+  if (!sgn_same_nz(aR - a, a - aL)) {
+    aL = a;
+    aR = a;
+    return;
+  }
+  const double dA = aR - aL;
+  const double a6 = 6.0 * (a - 0.5 * (aL + aR));
+  if (sgn_same_nz(dA, a6 - dA)) aL = 3.0 * a - 2.0 * aR;
+  else if (sgn_opp_nz(dA, a6 + dA)) aR = 3.0 * a - 2.0 * aL;
+}
+// the forms the transport kernels use: the oracle's in the strict build, the integer-pipe forms
+// in the production build
+__device__ __forceinline__ double slope_u_p(double am, double a, double ap) {
+#if RS_STRICT
+  return slope_u(am, a, ap);
+#else
+  return slope_u_fast(am, a, ap);
+#endif
+}
+__device__ __forceinline__ double slope_n_p(double am, double a, double ap, double sA, double sB) {
+#if RS_STRICT
+  return slope_n(am, a, ap, sA, sB);
+#else
+  return slope_n_fast(am, a, ap, sA, sB);
+#endif
+}
+__device__ __forceinline__ void limit_p(double a, double& aL, double& aR) {
+#if RS_STRICT
+  limit(a, aL, aR);
+#else
+  limit_fast(a, aL, aR);
+#endif
+}
+
 __device__ __forceinline__ double ppm_face_u(const double* v, bool right) {
-  double dm1 = slope_u(v[0], v[1], v[2]);
-  double d0 = slope_u(v[1], v[2], v[3]);
-  double dp1 = slope_u(v[2], v[3], v[4]);
+  double dm1 = slope_u_p(v[0], v[1], v[2]);
+  double d0 = slope_u_p(v[1], v[2], v[3]);
+  double dp1 = slope_u_p(v[2], v[3], v[4]);
   double aL = v[1] + 0.5 * (v[2] - v[1]) - (d0 - dm1) * kOneSixth;
   double aR = v[2] + 0.5 * (v[3] - v[2]) - (dp1 - d0) * kOneSixth;
-  limit(v[2], aL, aR);
+  limit_p(v[2], aL, aR);
   return right ? aR : aL;
 }
 
@@ -344,12 +421,12 @@ __global__ void __launch_bounds__(kFluxThreads) k_flux_z(DevTransport<double> T,
     const double* q = Q + (size_t)s * nc + col;
     double v[5];
     for (int o = 0; o < 5; ++o) v[o] = q[(size_t)kk[o] * ncol];
-    double dm1 = slope_n(v[0], v[1], v[2], sA0, sB0);
-    double d0 = slope_n(v[1], v[2], v[3], sA1, sB1);
-    double dp1 = slope_n(v[2], v[3], v[4], sA2, sB2);
+    double dm1 = slope_n_p(v[0], v[1], v[2], sA0, sB0);
+    double d0 = slope_n_p(v[1], v[2], v[3], sA1, sB1);
+    double dp1 = slope_n_p(v[2], v[3], v[4], sA2, sB2);
     double aL = v[1] + eLab * (v[2] - v[1]) + eLc * d0 + eLd * dm1;
     double aR = v[2] + eRab * (v[3] - v[2]) + eRc * dp1 + eRd * d0;
-    limit(v[2], aL, aR);
+    limit_p(v[2], aL, aR);
     T.fz[(size_t)s * fplane + (size_t)kf * ncol + col] = M * (right ? aR : aL);
   }
 }
@@ -390,7 +467,7 @@ __global__ void __launch_bounds__(256) k_flux_x_fused(DevTransport<double> T, St
     }
     __syncthreads();
     for (int p = threadIdx.x - 2; p <= n + 1; p += blockDim.x)
-      D[p + 3] = slope_u(V[p + 2], V[p + 3], V[p + 4]);
+      D[p + 3] = slope_u_p(V[p + 2], V[p + 3], V[p + 4]);
     __syncthreads();
     for (int f = threadIdx.x - 1; f <= n + 1; f += blockDim.x)
       E[f + 3] = V[f + 2] + 0.5 * (V[f + 3] - V[f + 2]) - (D[f + 3] - D[f + 2]) * kOneSixth;
@@ -400,7 +477,7 @@ __global__ void __launch_bounds__(256) k_flux_x_fused(DevTransport<double> T, St
       const bool right = __double_as_longlong(M) > 0;  // M > 0 for every non-NaN M
       int up = right ? f - 1 : f;
       double aL = E[up + 3], aR = E[up + 4];
-      limit(V[up + 3], aL, aR);
+      limit_p(V[up + 3], aL, aR);
       T.fx[((size_t)s * T.nlev * T.nlat + (size_t)k * T.nlat + j) * nf + f] = M * (right ? aR : aL);
     }
     __syncthreads();
@@ -446,7 +523,7 @@ __global__ void __launch_bounds__(512) k_flux_y_fused(DevTransport<double> T, St
     }
     __syncthreads();
     for (int p = (int)ty - 2; p <= n + 1; p += blockDim.y)
-      D[(p + 3) * kPencil + tx] = slope_u(V[(p + 2) * kPencil + tx], V[(p + 3) * kPencil + tx],
+      D[(p + 3) * kPencil + tx] = slope_u_p(V[(p + 2) * kPencil + tx], V[(p + 3) * kPencil + tx],
                                           V[(p + 4) * kPencil + tx]);
     __syncthreads();
     for (int f = (int)ty - 1; f <= n + 1; f += blockDim.y) {
@@ -466,7 +543,7 @@ __global__ void __launch_bounds__(512) k_flux_y_fused(DevTransport<double> T, St
         const bool right = __double_as_longlong(M) > 0;
         int up = right ? f - 1 : f;
         double aL = E[(up + 3) * kPencil + tx], aR = E[(up + 4) * kPencil + tx];
-        limit(V[(up + 3) * kPencil + tx], aL, aR);
+        limit_p(V[(up + 3) * kPencil + tx], aL, aR);
         T.fy[(size_t)s * fplane + fb] = M * (right ? aR : aL);
       }
     }
@@ -504,7 +581,7 @@ __global__ void __launch_bounds__(512) k_flux_z_fused(DevTransport<double> T, St
     for (int p = (int)ty - 1; p <= n; p += blockDim.y) {  // slopes of cells -1..n
       double sA = live ? T.vsA[(size_t)(p + 1) * ncol + col] : 0.0;
       double sB = live ? T.vsB[(size_t)(p + 1) * ncol + col] : 0.0;
-      D[(p + 3) * kPencil + tx] = slope_n(V[(p + 2) * kPencil + tx], V[(p + 3) * kPencil + tx],
+      D[(p + 3) * kPencil + tx] = slope_n_p(V[(p + 2) * kPencil + tx], V[(p + 3) * kPencil + tx],
                                           V[(p + 4) * kPencil + tx], sA, sB);
     }
     __syncthreads();
@@ -527,7 +604,7 @@ __global__ void __launch_bounds__(512) k_flux_z_fused(DevTransport<double> T, St
         const bool right = __double_as_longlong(M) > 0;
         int up = right ? kf - 1 : kf;
         double aL = E[(up + 3) * kPencil + tx], aR = E[(up + 4) * kPencil + tx];
-        limit(V[(up + 3) * kPencil + tx], aL, aR);
+        limit_p(V[(up + 3) * kPencil + tx], aL, aR);
         T.fz[(size_t)s * fplane + (size_t)kf * ncol + col] = M * (right ? aR : aL);
       }
     }
@@ -1172,7 +1249,10 @@ __global__ void __launch_bounds__(kRedThreads) k_stage(DevTransport<double> T,
       // the stage's new value is q + dt/2 * f: nx = q + dt_2 * du (strict: the oracle's
       // expression order); the production build forms it as fma(du, scale, q), folding 1/m
       // into the scale when no PBL term is added
-      double du, scale = dt_2;
+      double du;
+#if !RS_STRICT
+      double scale = dt_2;
+#endif
       if (s < T.ntr) {
         double fw = T.fx[s * fxp + fxi], fe = T.fx[s * fxp + fxi + 1];
         double fs = T.fy[s * fyp + fyi], fn = T.fy[s * fyp + fyi + T.nlon];
