@@ -212,6 +212,19 @@ __device__ __forceinline__ double rcp_nr(double d) {
   return fma(r, e, r);
 }
 
+// One Newton step (relative error ~1e-12 or better) and max(|a|, |b|) on the magnitude bits:
+// the production build's forms for error-norm terms, whose only use is the step-size controller.
+__device__ __forceinline__ double rcp_nr1(double d) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(d));
+  return fma(r, fma(-d, r, 1.0), r);
+}
+__device__ __forceinline__ double amax_bits(double a, double b) {
+  const long long ma = __double_as_longlong(a) & 0x7fffffffffffffffLL;
+  const long long mb = __double_as_longlong(b) & 0x7fffffffffffffffLL;
+  return __longlong_as_double(ma > mb ? ma : mb);
+}
+
 // ------------------------------------------------------------------ fixed-tree reductions
 // Pairwise tree over 256 lanes: v[t] += v[t+s] for s = 128 ... 1 (identical to the CPU
 // restatement's tree256).  Returns the total in thread 0.

@@ -318,6 +318,19 @@ __device__ __forceinline__ double rcp_nr(double d) {
   e = fma(-d, r, 1.0);
   return fma(r, e, r);
 }
+// one Newton step: relative error ~1e-12 or better -- enough for error-norm denominators, whose
+// only use is the step-size controller
+__device__ __forceinline__ double rcp_nr1(double d) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(d));
+  return fma(r, fma(-d, r, 1.0), r);
+}
+// max(|a|, |b|) as the larger magnitude bit pattern (integer pipe; NaN stays NaN)
+__device__ __forceinline__ double amax_bits(double a, double b) {
+  const long long ma = __double_as_longlong(a) & 0x7fffffffffffffffLL;
+  const long long mb = __double_as_longlong(b) & 0x7fffffffffffffffLL;
+  return __longlong_as_double(ma > mb ? ma : mb);
+}
 
 // pairwise tree over 256 lanes, v[t] += v[t+s] for s = 128 ... 1; total in thread 0
 __device__ __forceinline__ double tree256(double v, double* sm) {
@@ -358,8 +371,12 @@ std::string generate(const MechTables& T, double ros_d, double ros_c32, bool str
   // Every multiply-add is written out: RS_FMA fuses in the production build and keeps the
   // multiply and the add separate in the strict build; both builds compile with --fmad=false,
   // so no compiler contraction decides anything and all variants compute the same bits.
+  // RS_NQUOT / RS_AMAX serve the error norm only (its value steers the controller and nothing
+  // else): a one-step reciprocal and an integer magnitude max in the production build.
   o << (strict ? "#define RS_QUOT(a, b) ((a) / (b))\n#define RS_FMA(a, b, c) ((a) * (b) + (c))\n"
-               : "#define RS_QUOT(a, b) ((a) * rcp_nr(b))\n#define RS_FMA(a, b, c) fma((a), (b), (c))\n");
+                 "#define RS_NQUOT(a, b) ((a) / (b))\n#define RS_AMAX(a, b) fmax(fabs(a), fabs(b))\n"
+               : "#define RS_QUOT(a, b) ((a) * rcp_nr(b))\n#define RS_FMA(a, b, c) fma((a), (b), (c))\n"
+                 "#define RS_NQUOT(a, b) ((a) * rcp_nr1(b))\n#define RS_AMAX(a, b) amax_bits((a), (b))\n");
   // One ROS23 attempt of one cell: xn (unclamped) and the cell's sum of squared scaled errors.
   // f0 = f(x) is computed here unless the caller already holds it (have_f0): after an
   // accepted attempt whose clamp left the state bit for bit unchanged, f(x_new) is exactly
@@ -424,9 +441,9 @@ __device__ __forceinline__ double ros23_cell(const double* __restrict__ kr,
 #pragma unroll
   for (int s = 0; s < NS; ++s) {
     const double ut = dto6 * (RS_FMA(-2.0, k2[s], k1[s]) + b[s]);
-    const double am = fmax(fabs(x[s]), fabs(xn[s]));
+    const double am = RS_AMAX(x[s], xn[s]);
     const double den = RS_FMA(am, rtol, atol);
-    const double at = RS_QUOT(ut, den);
+    const double at = RS_NQUOT(ut, den);
     acc = RS_FMA(at, at, acc);
   }
   return acc;

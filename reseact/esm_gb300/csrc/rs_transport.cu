@@ -135,6 +135,37 @@ __device__ __forceinline__ void limit_p(double a, double& aL, double& aR) {
 #endif
 }
 
+// slopes from the neighbour differences d0 = a - am, d1 = ap - a (computed once per cell by the
+// pencil kernels) -- the same operations as slope_u / slope_n, so bit-identical to them
+__device__ __forceinline__ double slope_ud(double d0, double d1, double am, double ap) {
+#if RS_STRICT
+  if (d1 * d0 > 0.0) {
+    double da = 0.5 * (ap - am);
+    double lim = 2.0 * fmin(fabs(d0), fabs(d1));
+    return copysign(fmin(fabs(da), lim), da);
+  }
+  return 0.0;
+#else
+  if (!sgn_same_nz(d0, d1)) return 0.0;
+  const long long sb = __double_as_longlong(ap - am);
+  return slope_pick((sb & kMagMask) - kExpOne, sb & kSignBit, d0, d1);
+#endif
+}
+__device__ __forceinline__ double slope_nd(double d0, double d1, double sA, double sB) {
+#if RS_STRICT
+  if (d1 * d0 > 0.0) {
+    double da = sA * d1 + sB * d0;
+    double lim = 2.0 * fmin(fabs(d0), fabs(d1));
+    return copysign(fmin(fabs(da), lim), da);
+  }
+  return 0.0;
+#else
+  if (!sgn_same_nz(d0, d1)) return 0.0;
+  const long long db = __double_as_longlong(sA * d1 + sB * d0);
+  return slope_pick(db & kMagMask, db & kSignBit, d0, d1);
+#endif
+}
+
 __device__ __forceinline__ double ppm_face_u(const double* v, bool right) {
   double dm1 = slope_u_p(v[0], v[1], v[2]);
   double d0 = slope_u_p(v[1], v[2], v[3]);
@@ -444,10 +475,11 @@ __global__ void __launch_bounds__(256) k_flux_x_fused(DevTransport<double> T, St
   if (!resolve_stage(sel, Q, g)) return;
   extern __shared__ double smx[];
   const int n = T.nlon, nf = n + 1, L = n + 6;
-  double* V = smx;           // V[p+3], p in [-3, n+2]
-  double* D = smx + L;       // D[p+3], slopes p in [-2, n+1]
-  double* E = smx + 2 * L;   // E[f+3], edge between f-1 and f, f in [-1, n+1]
-  double* Mf = smx + 3 * L;  // Mf[f], the face's air-mass flux g*mx (shared by all tracers)
+  double* V = smx;            // V[p+3], p in [-3, n+2]
+  double* Dd = smx + L;       // Dd[p+3] = v(p+1) - v(p), p in [-3, n+1]
+  double* D = smx + 2 * L;    // D[p+3], slopes p in [-2, n+1]
+  double* E = smx + 3 * L;    // E[f+3], edge between f-1 and f, f in [-1, n+1]
+  double* Mf = smx + 4 * L;   // Mf[f], the face's air-mass flux g*mx (shared by all tracers)
   const int row = blockIdx.x;  // (k, j)
   const int j = row % T.nlat, k = row / T.nlat;
   const size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
@@ -455,22 +487,24 @@ __global__ void __launch_bounds__(256) k_flux_x_fused(DevTransport<double> T, St
   for (int f = threadIdx.x; f <= n; f += blockDim.x) Mf[f] = g * T.mx[((size_t)k * T.nlat + j) * nf + f];
   for (int s = 0; s < T.ntr; ++s) {
     const double* q = Q + (size_t)s * nc + rbase;
-    for (int p = threadIdx.x - 3; p <= n + 2; p += blockDim.x) {
-      double v;
+    auto val = [&](int p) -> double {
       if (p < 0 || p >= n) {
-        if (T.lon_bc == 0) v = q[((p % n) + n) % n];
-        else v = (p < 0 ? T.qw : T.qe)[((size_t)s * T.nlev + k) * T.nlat + j];
-      } else {
-        v = q[p];
+        if (T.lon_bc == 0) return q[((p % n) + n) % n];
+        return (p < 0 ? T.qw : T.qe)[((size_t)s * T.nlev + k) * T.nlat + j];
       }
+      return q[p];
+    };
+    for (int p = threadIdx.x - 3; p <= n + 2; p += blockDim.x) {
+      const double v = val(p);
       V[p + 3] = v;
+      if (p <= n + 1) Dd[p + 3] = val(p + 1) - v;
     }
     __syncthreads();
     for (int p = threadIdx.x - 2; p <= n + 1; p += blockDim.x)
-      D[p + 3] = slope_u_p(V[p + 2], V[p + 3], V[p + 4]);
+      D[p + 3] = slope_ud(Dd[p + 2], Dd[p + 3], V[p + 2], V[p + 4]);
     __syncthreads();
     for (int f = threadIdx.x - 1; f <= n + 1; f += blockDim.x)
-      E[f + 3] = V[f + 2] + 0.5 * (V[f + 3] - V[f + 2]) - (D[f + 3] - D[f + 2]) * kOneSixth;
+      E[f + 3] = V[f + 2] + 0.5 * Dd[f + 2] - (D[f + 3] - D[f + 2]) * kOneSixth;
     __syncthreads();
     for (int f = threadIdx.x; f <= n; f += blockDim.x) {
       const double M = Mf[f];
@@ -493,9 +527,10 @@ __global__ void __launch_bounds__(512) k_flux_y_fused(DevTransport<double> T, St
   extern __shared__ double smy[];
   const int n = T.nlat, nfj = n + 1, L = n + 6;
   double* V = smy;                    // [L][kPencil]
-  double* D = smy + L * kPencil;
-  double* E = smy + 2 * L * kPencil;
-  double* Mf = smy + 3 * L * kPencil;  // [n+1][kPencil] face air-mass fluxes g*my
+  double* Dd = smy + L * kPencil;     // neighbour differences v(p+1) - v(p)
+  double* D = smy + 2 * L * kPencil;
+  double* E = smy + 3 * L * kPencil;
+  double* Mf = smy + 4 * L * kPencil;  // [n+1][kPencil] face air-mass fluxes g*my
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int ntile = (T.nlon + kPencil - 1) / kPencil;
   const int k = blockIdx.x / ntile;
@@ -507,30 +542,28 @@ __global__ void __launch_bounds__(512) k_flux_y_fused(DevTransport<double> T, St
   if (live)
     for (int f = ty; f <= n; f += blockDim.y)
       Mf[f * kPencil + tx] = g * T.my[((size_t)k * nfj + f) * T.nlon + i];
+#define RS_P(a, p) a[((p) + 3) * kPencil + tx]
   for (int s = 0; s < T.ntr; ++s) {
     const double* q = Q + (size_t)s * nc + (size_t)k * T.nlat * T.nlon;
-    for (int p = (int)ty - 3; p <= n + 2; p += blockDim.y) {
-      double v = 0.0;
-      if (live) {
-        if (p < 0 || p >= n) {
-          if (open) v = (p < 0 ? T.qs : T.qn)[((size_t)s * T.nlev + k) * T.nlon + i];
-          else v = q[(size_t)(p < 0 ? -1 - p : 2 * n - 1 - p) * T.nlon + i];
-        } else {
-          v = q[(size_t)p * T.nlon + i];
-        }
+    auto val = [&](int p) -> double {
+      if (!live) return 0.0;
+      if (p < 0 || p >= n) {
+        if (open) return (p < 0 ? T.qs : T.qn)[((size_t)s * T.nlev + k) * T.nlon + i];
+        return q[(size_t)(p < 0 ? -1 - p : 2 * n - 1 - p) * T.nlon + i];
       }
-      V[(p + 3) * kPencil + tx] = v;
+      return q[(size_t)p * T.nlon + i];
+    };
+    for (int p = (int)ty - 3; p <= n + 2; p += blockDim.y) {
+      const double v = val(p);
+      RS_P(V, p) = v;
+      if (p <= n + 1) RS_P(Dd, p) = val(p + 1) - v;
     }
     __syncthreads();
     for (int p = (int)ty - 2; p <= n + 1; p += blockDim.y)
-      D[(p + 3) * kPencil + tx] = slope_u_p(V[(p + 2) * kPencil + tx], V[(p + 3) * kPencil + tx],
-                                          V[(p + 4) * kPencil + tx]);
+      RS_P(D, p) = slope_ud(RS_P(Dd, p - 1), RS_P(Dd, p), RS_P(V, p - 1), RS_P(V, p + 1));
     __syncthreads();
-    for (int f = (int)ty - 1; f <= n + 1; f += blockDim.y) {
-      double vl = V[(f + 2) * kPencil + tx], vr = V[(f + 3) * kPencil + tx];
-      E[(f + 3) * kPencil + tx] =
-          vl + 0.5 * (vr - vl) - (D[(f + 3) * kPencil + tx] - D[(f + 2) * kPencil + tx]) * kOneSixth;
-    }
+    for (int f = (int)ty - 1; f <= n + 1; f += blockDim.y)
+      RS_P(E, f) = RS_P(V, f - 1) + 0.5 * RS_P(Dd, f - 1) - (RS_P(D, f) - RS_P(D, f - 1)) * kOneSixth;
     __syncthreads();
     if (live) {
       for (int f = ty; f <= n; f += blockDim.y) {
@@ -542,8 +575,8 @@ __global__ void __launch_bounds__(512) k_flux_y_fused(DevTransport<double> T, St
         const double M = Mf[f * kPencil + tx];
         const bool right = __double_as_longlong(M) > 0;
         int up = right ? f - 1 : f;
-        double aL = E[(up + 3) * kPencil + tx], aR = E[(up + 4) * kPencil + tx];
-        limit_p(V[(up + 3) * kPencil + tx], aL, aR);
+        double aL = RS_P(E, up), aR = RS_P(E, up + 1);
+        limit_p(RS_P(V, up), aL, aR);
         T.fy[(size_t)s * fplane + fb] = M * (right ? aR : aL);
       }
     }
@@ -560,9 +593,10 @@ __global__ void __launch_bounds__(512) k_flux_z_fused(DevTransport<double> T, St
   extern __shared__ double smz[];
   const int n = T.nlev, L = n + 6;
   double* V = smz;
-  double* D = smz + L * kPencil;
-  double* E = smz + 2 * L * kPencil;
-  double* Mf = smz + 3 * L * kPencil;  // [n+1][kPencil] face air-mass fluxes g*mz
+  double* Dd = smz + L * kPencil;
+  double* D = smz + 2 * L * kPencil;
+  double* E = smz + 3 * L * kPencil;
+  double* Mf = smz + 4 * L * kPencil;  // [n+1][kPencil] face air-mass fluxes g*mz
   const int tx = threadIdx.x, ty = threadIdx.y;
   const size_t ncol = (size_t)T.nlon * T.nlat;
   const size_t col = (size_t)blockIdx.x * kPencil + tx;
@@ -573,25 +607,27 @@ __global__ void __launch_bounds__(512) k_flux_z_fused(DevTransport<double> T, St
     for (int kf = ty; kf <= n; kf += blockDim.y) Mf[kf * kPencil + tx] = g * T.mz[(size_t)kf * ncol + col];
   for (int s = 0; s < T.ntr; ++s) {
     const double* q = Q + (size_t)s * nc;
+    auto val = [&](int p) -> double {
+      const int pp = p < 0 ? -1 - p : (p >= n ? 2 * n - 1 - p : p);
+      return live ? q[(size_t)pp * ncol + col] : 0.0;
+    };
     for (int p = (int)ty - 3; p <= n + 2; p += blockDim.y) {
-      int pp = p < 0 ? -1 - p : (p >= n ? 2 * n - 1 - p : p);
-      V[(p + 3) * kPencil + tx] = live ? q[(size_t)pp * ncol + col] : 0.0;
+      const double v = val(p);
+      RS_P(V, p) = v;
+      if (p <= n + 1) RS_P(Dd, p) = val(p + 1) - v;
     }
     __syncthreads();
     for (int p = (int)ty - 1; p <= n; p += blockDim.y) {  // slopes of cells -1..n
       double sA = live ? T.vsA[(size_t)(p + 1) * ncol + col] : 0.0;
       double sB = live ? T.vsB[(size_t)(p + 1) * ncol + col] : 0.0;
-      D[(p + 3) * kPencil + tx] = slope_n_p(V[(p + 2) * kPencil + tx], V[(p + 3) * kPencil + tx],
-                                          V[(p + 4) * kPencil + tx], sA, sB);
+      RS_P(D, p) = slope_nd(RS_P(Dd, p - 1), RS_P(Dd, p), sA, sB);
     }
     __syncthreads();
     for (int e = ty; e <= n; e += blockDim.y) {  // edges 0..n (cells e-1 | e)
       double eab = live ? T.veAB[(size_t)e * ncol + col] : 0.0;
       double ec = live ? T.veC[(size_t)e * ncol + col] : 0.0;
       double ed = live ? T.veD[(size_t)e * ncol + col] : 0.0;
-      double vl = V[(e + 2) * kPencil + tx], vr = V[(e + 3) * kPencil + tx];
-      E[(e + 3) * kPencil + tx] =
-          vl + eab * (vr - vl) + ec * D[(e + 3) * kPencil + tx] + ed * D[(e + 2) * kPencil + tx];
+      RS_P(E, e) = RS_P(V, e - 1) + eab * RS_P(Dd, e - 1) + ec * RS_P(D, e) + ed * RS_P(D, e - 1);
     }
     __syncthreads();
     if (live) {
@@ -603,13 +639,14 @@ __global__ void __launch_bounds__(512) k_flux_z_fused(DevTransport<double> T, St
         const double M = Mf[kf * kPencil + tx];
         const bool right = __double_as_longlong(M) > 0;
         int up = right ? kf - 1 : kf;
-        double aL = E[(up + 3) * kPencil + tx], aR = E[(up + 4) * kPencil + tx];
-        limit_p(V[(up + 3) * kPencil + tx], aL, aR);
+        double aL = RS_P(E, up), aR = RS_P(E, up + 1);
+        limit_p(RS_P(V, up), aL, aR);
         T.fz[(size_t)s * fplane + (size_t)kf * ncol + col] = M * (right ? aR : aL);
       }
     }
     __syncthreads();
   }
+#undef RS_P
 }
 
 // ------------------------------------------------------------------ mixed-precision pencils
@@ -1301,12 +1338,13 @@ __global__ void __launch_bounds__(kRedThreads) k_stage(DevTransport<double> T,
         double ut = (1.0 / 3.0) * u0 + (2.0 / 3.0) * u3;
         double un = nx;
         double err = 0.5 * (ut - un);
+#if RS_STRICT
         double am = fmax(fabs(u0), fabs(un));
         double den = am * rtol + atol;
-#if RS_STRICT
         double at = err / den;
 #else
-        double at = err * rcp_nr(den);  // den >= atol > 0
+        double den = fma(amax_bits(u0, un), rtol, atol);
+        double at = err * rcp_nr1(den);  // den >= atol > 0
 #endif
         e = e + at * at;
         Un[x] = clamp ? fmax(un, 0.0) : un;
@@ -1387,7 +1425,7 @@ static void allow_big_smem() {
   done = true;
 }
 
-// Launch shape of the fused pencil kernels: V, D, E rows (n+6 each) plus the n+1 face fluxes,
+// Launch shape of the fused pencil kernels: V, Dd, D, E rows (n+6 each) plus the n+1 face fluxes,
 // per pencil.  The tuned pencil width drops to 16 where 32 does not fit; a direction whose
 // pencils do not fit even at 16 uses the per-face FP64 kernel (the same fluxes, bit for bit).
 struct FluxShape {
@@ -1395,7 +1433,7 @@ struct FluxShape {
   size_t shx, shy, shz;
   bool fx, fy, fz;  // fused kernel used for x / y / z
 };
-static size_t pencil_bytes(int n, int pw) { return (size_t)(3 * (n + 6) + (n + 1)) * pw * sizeof(double); }
+static size_t pencil_bytes(int n, int pw) { return (size_t)(4 * (n + 6) + (n + 1)) * pw * sizeof(double); }
 static FluxShape flux_shape(const DevTransport<double>& T) {
   FluxShape f;
   f.pw = T.pencil == 16 ? 16 : 32;
