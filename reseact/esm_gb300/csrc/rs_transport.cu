@@ -74,12 +74,6 @@ __device__ __forceinline__ bool sgn_same_nz(double a, double b) {
   const bool nzb = ((hb & 0x7fffffff) | __double2loint(b)) != 0;
   return ((ha ^ hb) >= 0) & nza & nzb;
 }
-__device__ __forceinline__ bool sgn_opp_nz(double a, double b) {
-  const int ha = __double2hiint(a), hb = __double2hiint(b);
-  const bool nza = ((ha & 0x7fffffff) | __double2loint(a)) != 0;
-  const bool nzb = ((hb & 0x7fffffff) | __double2loint(b)) != 0;
-  return ((ha ^ hb) < 0) & nza & nzb;
-}
 constexpr long long kMagMask = 0x7fffffffffffffffLL, kSignBit = (long long)0x8000000000000000ULL,
                     kExpOne = 1LL << 52;
 // copysign(min(|da|, 2 min(|d0|, |d1|)), da) from |da| and da's sign as bits
@@ -90,26 +84,44 @@ __device__ __forceinline__ double slope_pick(long long abs_da, long long sign_da
 }
 __device__ __forceinline__ double slope_u_fast(double am, double a, double ap) {
   const double d0 = a - am, d1 = ap - a;
-  if (!sgn_same_nz(d0, d1)) return 0.0;
-  const long long sb = __double_as_longlong(ap - am);  // nonzero here; |da| = |ap - am| / 2
-  return slope_pick((sb & kMagMask) - kExpOne, sb & kSignBit, d0, d1);
+  const long long sb = __double_as_longlong(ap - am);  // nonzero where used; |da| = |ap - am| / 2
+  const double v = slope_pick((sb & kMagMask) - kExpOne, sb & kSignBit, d0, d1);
+  return __longlong_as_double(sgn_same_nz(d0, d1) ? __double_as_longlong(v) : 0LL);
 }
 __device__ __forceinline__ double slope_n_fast(double am, double a, double ap, double sA, double sB) {
   const double d0 = a - am, d1 = ap - a;
-  if (!sgn_same_nz(d0, d1)) return 0.0;
   const long long db = __double_as_longlong(sA * d1 + sB * d0);
-  return slope_pick(db & kMagMask, db & kSignBit, d0, d1);
+  const double v = slope_pick(db & kMagMask, db & kSignBit, d0, d1);
+  return __longlong_as_double(sgn_same_nz(d0, d1) ? __double_as_longlong(v) : 0LL);
+}
+// Branch-free: every lane issues the same ten FP64 instructions and picks its result with
+// integer selects -- with the limiter's data-dependent branches, a warp issued both sides and
+// the FP64 pipe (16 cycles per warp instruction) ran with about half its lanes idle.
+__device__ __forceinline__ double sel_d(bool c, double x, double y) {
+  return __longlong_as_double(c ? __double_as_longlong(x) : __double_as_longlong(y));
+}
+// Order-preserving integer key of a finite double (-0 and +0 both map to 0, key(-x) = -key(x)):
+// the sign of the rounded difference x - y is the sign of key(x) - key(y) (gradual underflow
+// makes x - y == 0 exactly when x == y), so the limiter's sign tests need no subtraction.
+__device__ __forceinline__ long long ord_key(double x) {
+  const long long b = __double_as_longlong(x);
+  const long long sgn = b >> 63;  // 0 or -1
+  return (b ^ (sgn & kMagMask)) - sgn;
 }
 __device__ __forceinline__ void limit_fast(double a, double& aL, double& aR) {
-  if (!sgn_same_nz(aR - a, a - aL)) {
-    aL = a;
-    aR = a;
-    return;
-  }
+  const long long ka = ord_key(a), kl = ord_key(aL), kr = ord_key(aR);
+  // extremum: (aR - a)(a - aL) <= 0
+  const bool flat = !((kr > ka && ka > kl) || (kr < ka && ka < kl));
   const double dA = aR - aL;
   const double a6 = 6.0 * (a - 0.5 * (aL + aR));
-  if (sgn_same_nz(dA, a6 - dA)) aL = 3.0 * a - 2.0 * aR;
-  else if (sgn_opp_nz(dA, a6 + dA)) aR = 3.0 * a - 2.0 * aL;
+  const long long kd = ord_key(dA), k6 = ord_key(a6);
+  // dA (a6 - dA) > 0 and dA (a6 + dA) < 0 as comparisons of a6 with +-dA
+  const bool stl = (kd > 0 && k6 > kd) || (kd < 0 && k6 < kd);             // aL <- 3a - 2aR
+  const bool str = !stl && ((kd > 0 && k6 < -kd) || (kd < 0 && k6 > -kd));  // aR <- 3a - 2aL
+  const double st = fma(-2.0, sel_d(stl, aR, aL), 3.0 * a);
+  const double nL = sel_d(stl, st, aL), nR = sel_d(str, st, aR);
+  aL = sel_d(flat, a, nL);
+  aR = sel_d(flat, a, nR);
 }
 // the forms the transport kernels use: the oracle's in the strict build, the integer-pipe forms
 // in the production build
@@ -146,9 +158,9 @@ __device__ __forceinline__ double slope_ud(double d0, double d1, double am, doub
   }
   return 0.0;
 #else
-  if (!sgn_same_nz(d0, d1)) return 0.0;
   const long long sb = __double_as_longlong(ap - am);
-  return slope_pick((sb & kMagMask) - kExpOne, sb & kSignBit, d0, d1);
+  const double v = slope_pick((sb & kMagMask) - kExpOne, sb & kSignBit, d0, d1);
+  return __longlong_as_double(sgn_same_nz(d0, d1) ? __double_as_longlong(v) : 0LL);
 #endif
 }
 __device__ __forceinline__ double slope_nd(double d0, double d1, double sA, double sB) {
@@ -160,9 +172,9 @@ __device__ __forceinline__ double slope_nd(double d0, double d1, double sA, doub
   }
   return 0.0;
 #else
-  if (!sgn_same_nz(d0, d1)) return 0.0;
   const long long db = __double_as_longlong(sA * d1 + sB * d0);
-  return slope_pick(db & kMagMask, db & kSignBit, d0, d1);
+  const double v = slope_pick(db & kMagMask, db & kSignBit, d0, d1);
+  return __longlong_as_double(sgn_same_nz(d0, d1) ? __double_as_longlong(v) : 0LL);
 #endif
 }
 
@@ -690,8 +702,22 @@ __host__ __device__ inline int mixed_rows_p(int n) { return (n + kHoP + 3 + 1) /
 
 // The face flux is M a2 + M dev: a2 the upwind cell's FP64 value, the deviation product in FP32
 // (one FMA in FP64); q == 1 gives exactly M.
+// float -> double by re-biasing the exponent in the integer pipes (exact; zero kept, subnormal,
+// inf and NaN convert)
+__device__ __forceinline__ double f2d_bits(float x) {
+  const unsigned u = __float_as_uint(x);
+  const unsigned fe = (u >> 23) & 0xffu;
+  if ((u << 1) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+  if (fe == 0u || fe == 255u) return (double)x;
+  return __hiloint2double((int)((u & 0x80000000u) | ((fe + 896u) << 20) | ((u & 0x7fffffu) >> 3)),
+                          (int)(u << 29));
+}
 __device__ __forceinline__ double mixed_flux(double M, float Mf, double a2, float dev) {
+#if RS_STRICT
   return fma(M, a2, (double)(Mf * dev));
+#else
+  return fma(M, a2, f2d_bits(Mf * dev));
+#endif
 }
 
 // ---- bulk-copy staging (TMA): mbarrier with a transaction count, one elected issuing thread.
@@ -1148,10 +1174,40 @@ __global__ void __launch_bounds__(512) k_flux_z_mixed(DevTransport<double> T, St
 }
 
 // ------------------------------------------------------------------ stage kernel
+#if !RS_STRICT
+// hi + lo split without FP64-pipe conversions (production build): hi = v truncated to 24
+// significant bits, lo = the next 24 bits of the remainder, truncated -- hi + lo = v to 2^-47
+// relative.  Values outside [2^-74, 2^127) (zero, subnormals, inf, NaN included) convert.
+__device__ __forceinline__ void split_bits(double v, float& hi, float& lo) {
+  const unsigned h = (unsigned)__double2hiint(v), l = (unsigned)__double2loint(v);
+  const int e = (int)((h >> 20) & 0x7ff);
+  if (e < 949 || e > 1150) {
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
+    return;
+  }
+  const unsigned sign = h & 0x80000000u;
+  hi = __uint_as_float(sign | ((unsigned)(e - 896) << 23) | ((h & 0xfffffu) << 3) | (l >> 29));
+  const unsigned r = l & 0x1fffffffu;  // the 29 mantissa bits below hi
+  if (r == 0) {
+    lo = 0.0f;
+    return;
+  }
+  const int t = 31 - __clz((int)r);  // leading bit of r, 0..28
+  const unsigned mant = t >= 23 ? (r >> (t - 23)) : (r << (23 - t));
+  lo = __uint_as_float(sign | ((unsigned)(e - 948 + t) << 23) | (mant & 0x7fffffu));
+}
+#endif
 __device__ __forceinline__ void split_store(const DevTransport<double>& T, size_t x, double v) {
-  float hi = (float)v;
+  float hi, lo;
+#if RS_STRICT
+  hi = (float)v;
+  lo = (float)(v - (double)hi);
+#else
+  split_bits(v, hi, lo);
+#endif
   T.qhi[x] = hi;
-  T.qlo[x] = (float)(v - (double)hi);
+  T.qlo[x] = lo;
 }
 
 // split the attempt's input state U[cur] (stage 1's RHS argument) into hi/lo planes
