@@ -144,9 +144,10 @@ def workload(small=False):
 
 
 def ros23_flops_per_cell(mech, order=None):
-    """FP64 operations one ROS23 attempt executes per cell (the chemistry attempt kernel) with
-    the LU eliminated in `order` (natural, as the reference, if None): +,-,*,/ each counted
-    once, an FMA as two; comparisons, abs and max not counted."""
+    """FP64 operations of one ROS23 attempt per cell as the table-walking kernel executes it
+    (every stoichiometric term a multiply-add, no folding of unit coefficients) with the LU
+    eliminated in `order` (natural, as the reference, if None): +,-,*,/ each counted once, an
+    FMA as two; comparisons, abs and max not counted."""
     t = mech.tables()
     n_lu, n_mult, n_upd, n_low, n_up = mech.lu_counts(order)
     n = mech.ns
@@ -166,6 +167,55 @@ def ros23_flops_per_cell(mech, order=None):
     return 3 * (vel + rhs) + part + buildw + lu + 3 * solve + stage + err
 
 
+def ros23_exec_counts(mech, order, evals, emissions=False):
+    """(FP64 flops, FP64 instructions) per cell of one attempt of the mechanism-specialised ROS23
+    kernel as generated (production build): the generator folds +-1 stoichiometric
+    coefficients into adds, writes every other multiply-add as one FMA (2 flops, 1
+    instruction), forms the pivot reciprocals with two Newton steps and the error-norm ones
+    with one.  `evals` = 3 RHS evaluations, or 2 when the attempt reuses f(x).  Checked against
+    ncu's DADD/DMUL/DFMA counts of the kernel (1,553 flops counted here, 1,570 measured, for a
+    3-evaluation attempt of SuperFast in the minimum-fill order)."""
+    t = mech.tables()
+    ns = mech.ns
+
+    def terms(coefs):  # (instructions, flops) of a folded sum of c_t * a_t
+        i = f = 0
+        for k, c in enumerate(coefs):
+            if abs(c) == 1.0:
+                i, f = (i, f) if k == 0 else (i + 1, f + 1)
+            else:
+                i, f = (i + 1, f + 1) if k == 0 else (i + 1, f + 2)
+        return i, f
+
+    rp, rs, rn = t["react_ptr"], t["react_species"], t["react_nu"]
+    vel = int(sum(rn))
+    ri = rf = 0
+    for sp in range(ns):
+        a, b = terms(t["rhs_coef"][t["rhs_ptr"][sp]:t["rhs_ptr"][sp + 1]])
+        ri, rf = ri + a, rf + b
+    if emissions:
+        ri, rf = ri + ns, rf + ns
+    part = 0
+    for pr, q in zip(t["part_reaction"], t["part_species"]):
+        for e in range(rp[pr], rp[pr + 1]):
+            nu = int(rn[e])
+            part += nu if rs[e] != q else (nu if nu >= 2 else 0)
+    diag = set(int(x) for x in t["lu_diag"])
+    wi = wf = 0
+    for e in range(t["n_jac"]):
+        a, b = terms(t["jac_coef"][t["jac_ptr"][e]:t["jac_ptr"][e + 1]])
+        d = int(t["jac_slot"][e]) in diag
+        wi, wf = wi + a + 1, wf + b + (2 if d else 1)
+    _, n_mult, n_upd, n_low, n_up = mech.lu_counts(order)
+    lu_i, lu_f = 4 * ns + n_mult + n_upd, 8 * ns + n_mult + 2 * n_upd
+    sv_i, sv_f = n_low + n_up + ns, 2 * (n_low + n_up) + ns
+    stage_i, stage_f = 9 * ns, 12 * ns
+    norm_i, norm_f = 8 * ns, 13 * ns
+    inst = evals * (vel + ri) + part + wi + lu_i + 3 * sv_i + stage_i + norm_i
+    flops = evals * (vel + rf) + part + wf + lu_f + 3 * sv_f + stage_f + norm_f
+    return flops, inst
+
+
 def ros23_rhs_flops_per_cell(mech):
     """FP64 operations of one RHS evaluation f(x) per cell (rate products and the stoichiometric
     sums); an attempt that reuses f(x) from the previous attempt skips one of its three."""
@@ -174,11 +224,17 @@ def ros23_rhs_flops_per_cell(mech):
 
 
 def transport_flops_per_cell(nsp):
-    """FP64 operations of one SSPRK43 attempt per cell (4 stages): per tracer and stage, three
-    face reconstructions (~48 each: 3 slopes, 2 edges, limiter, flux) and the divergence and
-    stage update (~14); the air-mass row ~12."""
-    per_stage = (nsp - 1) * (3 * 48 + 14) + 12
-    return 4 * per_stage + 6 * nsp
+    """FP64 flops of one SSPRK43 attempt per cell as the production kernels execute them
+    (counted from their source, FMA = 2): per stage and tracer the x and y pencils 16 each
+    (neighbour difference, slope span, edge, branch-free limiter, flux) and the dp-weighted
+    vertical pencil 19; the stage kernels 12 per tracer in stages 1-2, 15 in stage 3 and 26 in
+    stage 4 (embedded error and norm), plus ~35 per cell and stage for the air-mass divergence
+    and row.  ncu measures 19 / 19 / 22 per face for the pencils (halo cells and the
+    compiler's choice of DMUL+DADD over DFMA), so this is the lower figure."""
+    ntr = nsp - 1
+    pencils = 4 * ntr * (16 + 16 + 19)
+    stages = ntr * (12 + 12 + 15 + 26) + 4 * 35
+    return pencils + stages
 
 
 def transport_bytes_per_cell(nsp):
@@ -345,20 +401,35 @@ def run_gb300(args):
     roofline = None
     if "ros23_attempt" in fams and rank == 0:
         n_l, tot = fams["ros23_attempt"]
-        # every attempt after the first of a solve reuses f(x) (the previous attempt's last RHS
-        # evaluation, kept per cell): count its flops as skipped in all of them (a lower bound
-        # on the executed work; cells whose state the clamp moved do evaluate it)
-        n_solves = 2
-        f_exec = f_ros - ros23_rhs_flops_per_cell(w.mech) * max(0.0, n_l - n_solves) / n_l
-        achieved = f_exec * nc / (tot / n_l * 1e-3) / 1e12
-        peak = peaks.get("fp64_tflops")
         kind, kinfo = solver.chem_kernel()
+        emis = "emis" in w.forcing
+        # every attempt after the first of a solve reuses f(x) (the previous attempt's last RHS
+        # evaluation, kept per cell): count it as skipped in all of them (a lower bound on the
+        # executed work; cells whose state the clamp moved do evaluate it)
+        n_solves = 2
+        reuse = max(0.0, n_l - n_solves) / n_l
+        if kinfo.get("kind") == "specialized":
+            f3, i3 = ros23_exec_counts(w.mech, solver.lu_order(), 3, emis)
+            f2, i2 = ros23_exec_counts(w.mech, solver.lu_order(), 2, emis)
+            f_exec = f3 + (f2 - f3) * reuse
+            i_exec = i3 + (i2 - i3) * reuse
+        else:  # table kernel: the algorithmic count (no folding of unit coefficients)
+            f_exec = f_ros - ros23_rhs_flops_per_cell(w.mech) * reuse
+            i_exec = None
+        sec = tot / n_l * 1e-3
+        achieved = f_exec * nc / sec / 1e12
+        peak = peaks.get("fp64_tflops")
         roofline = {"kernel": "ros23 attempt (%s, %s)" % (kinfo.get("kind"), kinfo.get("variant", "-")),
                     "bound": "fp64", "achieved": round(achieved, 4),
                     "peak": peak, "unit": "TFLOP/s", "frac": round(achieved / peak, 4) if peak else None,
                     "traffic": None, "flops_per_cell_attempt": round(f_exec, 1),
-                    "flops_per_cell_attempt_without_reuse": f_ros,
-                    "flops_per_cell_attempt_natural_order": f_ros_ref,
+                    # FP64 issue: instructions / (peak flops / 2 per FMA instruction); the flop
+                    # fraction is capped below 1 by the kernel's share of non-FMA instructions
+                    "fp64_issue_frac": (round(i_exec * nc / sec / (peak * 1e12 / 2), 4)
+                                        if (peak and i_exec) else None),
+                    "fp64_instructions_per_cell_attempt": round(i_exec, 1) if i_exec else None,
+                    "flops_table_kernel_count": f_ros,
+                    "flops_table_kernel_natural_order": f_ros_ref,
                     "peak_source": "own FMA-chain probe (csrc/peak_probe.cu), FP64 has no entry in MEASURED_PEAKS.json"}
     transport = None
     if "ssprk43_stages" in fams and rank == 0:
