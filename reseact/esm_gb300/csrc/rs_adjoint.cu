@@ -11,6 +11,8 @@
 // Sums are gathered per cell in a fixed order (no atomics): results are deterministic.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "rs_device.cuh"
 #include "rs_jit.h"
 #include "rs_kernels.h"
@@ -465,6 +467,236 @@ __global__ void __launch_bounds__(256) k_adj_gather(DevTransport<double> T, cons
   }
 }
 
+// ------------------------------------------------------------------ fused adjoint pencils
+// One block per pencil (a lon row; or PW adjacent lat lines / vertical columns), looping over
+// the tracers.  The same arithmetic as face_weights_lin + the per-cell gather, reorganised:
+//   1. the tracer values (3-cell halo) and the cell adjoints g = fbar / m go to shared memory;
+//   2. each cell's linearised slope (value + 3 coefficients) once per cell;
+//   3. each edge's value and weights over its 4 stencil positions once per edge -- the aL of
+//      the cell right of the edge and the aR of the cell left of it are the same expression;
+//   4. per face: the frozen-branch limiter on (a, aL, aR) with those weights, the face
+//      adjoint Fbar (from the two adjacent cells' g) and the contributions Fbar M w_o;
+//   5. per cell: the contributions of every face whose stencil covers it, faces ascending and
+//      positions ascending (the fixed order of the per-cell gather), added to ubar.
+// Per face the old path evaluated three slope forms and both edges' weights and went through
+// a global slab; here each is done once and stays on chip.  Bit-identical to that path.
+template <int DIR>
+__device__ __forceinline__ void adj_pencil_geometry(const DevTransport<double>& T, int& n, int& bc) {
+  n = DIR == 0 ? T.nlon : (DIR == 1 ? T.nlat : T.nlev);
+  bc = DIR == 0 ? T.lon_bc : (DIR == 1 ? (T.lat_bc == 1 ? 1 : 2) : 2);
+}
+// doubles of shared memory per pencil (and the int upwind indices) for a direction of length n
+__host__ __device__ inline int adj_pencil_doubles(int n) {
+  return (n + 6) + n + 4 * (n + 4) + 5 * (n + 3) + 5 * (n + 1) + (n + 1);
+}
+
+template <int DIR, int PW>
+__global__ void __launch_bounds__(256) k_adj_pencil(DevTransport<double> T,
+                                                    const double* __restrict__ U,
+                                                    const double* __restrict__ G,
+                                                    double* __restrict__ ubar, double g) {
+  const int s_blk = blockIdx.y;  // one tracer per block row of the grid
+  int n, bc;
+  adj_pencil_geometry<DIR>(T, n, bc);
+  extern __shared__ double sma[];
+  const int tx = threadIdx.x, ty = threadIdx.y, ny = blockDim.y;
+  // per-pencil arrays, [index][PW] with the pencil's lane fastest
+  double* V = sma;                           // [n+6]: stencil positions -3 .. n+2
+  double* Gc = V + (n + 6) * PW;             // [n]:   cell adjoints 0 .. n-1
+  double* SV = Gc + n * PW;                  // [n+4]: slope values of cells -2 .. n+1
+  double* SC = SV + (n + 4) * PW;            // [3][n+4]: slope coefficients
+  double* EV = SC + 3 * (n + 4) * PW;        // [n+3]: edge values, edges -1 .. n+1
+  double* EW = EV + (n + 3) * PW;            // [4][n+3]: edge weights on positions e-2 .. e+1
+  double* C = EW + 4 * (n + 3) * PW;         // [5][n+1]: face contributions
+  double* Mf = C + 5 * (n + 1) * PW;         // [n+1]: face air-mass flux (0 on walls)
+  int* upf = reinterpret_cast<int*>(Mf + (n + 1) * PW);  // [n+1]
+  const int ln = DIR == 0 ? 0 : tx;  // lane of this thread's pencil in the [index][PW] arrays
+#define AV(a, i) a[(i) * PW + ln]
+  const size_t ncol = (size_t)T.nlon * T.nlat, nc = ncol * T.nlev;
+  // the pencil: fixed (j, k) for x; (i, k) for y; (i, j) for z
+  int i = 0, j = 0, k = 0;
+  bool live = true;
+  if (DIR == 0) {
+    j = blockIdx.x % T.nlat;
+    k = blockIdx.x / T.nlat;
+  } else if (DIR == 1) {
+    const int ntile = (T.nlon + PW - 1) / PW;
+    k = blockIdx.x / ntile;
+    i = (blockIdx.x % ntile) * PW + tx;
+    live = i < T.nlon;
+  } else {
+    const size_t col = (size_t)blockIdx.x * PW + tx;
+    live = col < ncol;
+    i = live ? (int)(col % T.nlon) : 0;
+    j = live ? (int)(col / T.nlon) : 0;
+  }
+  auto cell = [&](int q) -> size_t {  // flat cell index of position q (0 <= q < n)
+    if (DIR == 0) return ((size_t)k * T.nlat + j) * T.nlon + q;
+    if (DIR == 1) return ((size_t)k * T.nlat + q) * T.nlon + i;
+    return (size_t)q * ncol + (size_t)j * T.nlon + i;
+  };
+  const size_t colz = (size_t)j * T.nlon + i;
+  // x rows: one lane per position (PW == 1); y / z: one lane per pencil, ty strides positions
+  const int lane0 = DIR == 0 ? threadIdx.x : ty;
+  const int lstride = DIR == 0 ? blockDim.x : ny;
+  for (int f = lane0; f <= n; f += lstride) {
+    const bool wall = (DIR == 1 && T.lat_bc != 1 && (f == 0 || f == n)) || (DIR == 2 && (f == 0 || f == n));
+    double M = 0.0;
+    if (live && !wall) {
+      if (DIR == 0) M = g * T.mx[((size_t)k * T.nlat + j) * (T.nlon + 1) + f];
+      else if (DIR == 1) M = g * T.my[((size_t)k * (T.nlat + 1) + f) * T.nlon + i];
+      else M = g * T.mz[(size_t)f * ncol + colz];
+    }
+    AV(Mf, f) = M;
+    AV(upf, f) = (M > 0.0) ? f - 1 : f;
+  }
+  {
+    const int s = s_blk;
+    const double* q = U + (size_t)s * nc;
+    // 1. values and cell adjoints
+    for (int p = lane0 - 3; p <= n + 2; p += lstride) {
+      double v = 0.0;
+      if (live) {
+        const int qq = map_pos(p, n, bc);
+        if (qq >= 0) {
+          v = q[cell(qq)];
+        } else if (DIR == 0) {
+          v = (p < 0 ? T.qw : T.qe)[((size_t)s * T.nlev + k) * T.nlat + j];
+        } else {
+          v = (p < 0 ? T.qs : T.qn)[((size_t)s * T.nlev + k) * T.nlon + i];
+        }
+      }
+      AV(V, p + 3) = v;
+      if (p >= 0 && p < n) AV(Gc, p) = live ? G[(size_t)s * nc + cell(p)] : 0.0;
+    }
+    __syncthreads();
+    // 2. slopes of cells -2 .. n+1 (vertical coefficient rows p+1, as the forward kernels)
+    for (int p = lane0 - 2; p <= n + 1; p += lstride) {
+      double sA = 0.0, sB = 0.0;
+      if (DIR == 2 && live && p >= -1 && p <= n) {
+        sA = T.vsA[(size_t)(p + 1) * ncol + colz];
+        sB = T.vsB[(size_t)(p + 1) * ncol + colz];
+      }
+      double val, c[3];
+      slope_form(AV(V, p + 2), AV(V, p + 3), AV(V, p + 4), sA, sB, DIR != 2, val, c);
+      AV(SV, p + 2) = val;
+      for (int o = 0; o < 3; ++o) AV(SC, o * (n + 4) + p + 2) = c[o];
+    }
+    __syncthreads();
+    // 3. edges -1 .. n+1 between cells e-1 and e: value and weights on positions e-2 .. e+1,
+    //    built in face_weights_lin's order (the aL of cell e, the aR of cell e-1)
+    for (int e = lane0 - 1; e <= n + 1; e += lstride) {
+      const double vm = AV(V, e + 2), vc = AV(V, e + 3);  // cells e-1, e
+      const double sm_ = AV(SV, e + 1), sc_ = AV(SV, e + 2);  // slopes of cells e-1, e
+      double w[4] = {0.0, 0.0, 0.0, 0.0}, ev;
+      if (DIR != 2) {
+        const double k6 = 1.0 / 6.0;
+        ev = (vm + 0.5 * (vc - vm)) - k6 * (sc_ - sm_);
+        w[1] = 0.5; w[2] = 0.5;
+        for (int o = 0; o < 3; ++o) {
+          w[1 + o] -= k6 * AV(SC, o * (n + 4) + e + 2);
+          w[o] += k6 * AV(SC, o * (n + 4) + e + 1);
+        }
+      } else {
+        double eab = 0.0, ec = 0.0, ed = 0.0;
+        if (live && e >= 0 && e <= n) {
+          eab = T.veAB[(size_t)e * ncol + colz];
+          ec = T.veC[(size_t)e * ncol + colz];
+          ed = T.veD[(size_t)e * ncol + colz];
+        }
+        ev = ((vm + eab * (vc - vm)) + ec * sc_) + ed * sm_;
+        w[1] = 1.0 - eab; w[2] = eab;
+        for (int o = 0; o < 3; ++o) {
+          w[1 + o] += ec * AV(SC, o * (n + 4) + e + 2);
+          w[o] += ed * AV(SC, o * (n + 4) + e + 1);
+        }
+      }
+      AV(EV, e + 1) = ev;
+      for (int o = 0; o < 4; ++o) AV(EW, o * (n + 3) + e + 1) = w[o];
+    }
+    __syncthreads();
+    // 4. faces: limiter with frozen branches, face adjoint, contributions
+    for (int f = lane0; f <= n; f += lstride) {
+      const double M = AV(Mf, f);
+      double* out = &AV(C, f);  // C[o][f] at out[o * (n+1) * PW]
+      const size_t cstr = (size_t)(n + 1) * PW;
+      const bool wall = (DIR == 1 && T.lat_bc != 1 && (f == 0 || f == n)) || (DIR == 2 && (f == 0 || f == n));
+      if (wall) {
+        for (int o = 0; o < 5; ++o) out[o * cstr] = 0.0;
+        continue;
+      }
+      const int up = AV(upf, f);
+      const bool right = M > 0.0;
+      double L[5], R[5];
+      L[4] = 0.0; R[0] = 0.0;
+      for (int o = 0; o < 4; ++o) {
+        L[o] = AV(EW, o * (n + 3) + up + 1);      // edge up: positions up-2 .. up+1
+        R[1 + o] = AV(EW, o * (n + 3) + up + 2);  // edge up+1: positions up-1 .. up+2
+      }
+      const double aLv = AV(EV, up + 1), aRv = AV(EV, up + 2), a = AV(V, up + 3);
+      double w[5];
+      if ((aRv - a) * (a - aLv) <= 0.0) {
+        for (int o = 0; o < 5; ++o) w[o] = o == 2 ? 1.0 : 0.0;
+      } else {
+        const double dA = aRv - aLv;
+        const double a6 = 6.0 * (a - 0.5 * (aLv + aRv));
+        if (dA * a6 > dA * dA) {
+          for (int o = 0; o < 5; ++o) L[o] = (o == 2 ? 3.0 : 0.0) - 2.0 * R[o];
+        } else if (-(dA * dA) > dA * a6) {
+          for (int o = 0; o < 5; ++o) R[o] = (o == 2 ? 3.0 : 0.0) - 2.0 * L[o];
+        }
+        for (int o = 0; o < 5; ++o) w[o] = right ? R[o] : L[o];
+      }
+      double cbw, caw;
+      if (DIR == 0) cbw = caw = T.gx[j];
+      else if (DIR == 1) {
+        cbw = f >= 1 ? T.gyhi[f - 1] : 0.0;
+        caw = f < n ? T.gylo[f] : 0.0;
+      } else cbw = caw = 1.0;
+      double Fb = 0.0;
+      if (f >= 1) Fb = Fb - AV(Gc, f - 1) * cbw;
+      if (f < n) Fb = Fb + AV(Gc, f) * caw;
+      for (int o = 0; o < 5; ++o) out[o * cstr] = Fb * M * w[o];
+    }
+    __syncthreads();
+    // 5. gather (faces ascending, positions ascending; periodic seam windows as before).  A cell
+    //    at least 3 positions from either end is reached only by faces pos-2 .. pos+3, each
+    //    through exactly one in-range stencil position: the same faces in the same order.
+    for (int pos = lane0; pos < n; pos += lstride) {
+      if (!live) break;
+      if (pos >= 3 && pos <= n - 4) {
+        double acc = 0.0;
+        for (int f = pos - 2; f <= pos + 3; ++f) {
+          const int o = pos - AV(upf, f) + 2;
+          if (o >= 0 && o <= 4) acc = acc + AV(C, o * (n + 1) + f);
+        }
+        ubar[(size_t)s * nc + cell(pos)] += acc;
+        continue;
+      }
+      int lo[3], hi[3], nw = 0;
+      if (bc == 0) { lo[nw] = pos - n - 5; hi[nw] = pos - n + 5; ++nw; }
+      lo[nw] = pos - 5; hi[nw] = pos + 5; ++nw;
+      if (bc == 0) { lo[nw] = pos + n - 5; hi[nw] = pos + n + 5; ++nw; }
+      double acc = 0.0;
+      int last = -1;
+      for (int wdw = 0; wdw < nw; ++wdw) {
+        const int a0 = lo[wdw] < 0 ? 0 : lo[wdw];
+        const int b0 = hi[wdw] > n ? n : hi[wdw];
+        for (int f = a0; f <= b0; ++f) {
+          if (f <= last) continue;
+          last = f;
+          const int up = AV(upf, f);
+          for (int o = 0; o < 5; ++o)
+            if (map_pos(up - 2 + o, n, bc) == pos) acc = acc + AV(C, o * (n + 1) + f);
+        }
+      }
+      ubar[(size_t)s * nc + cell(pos)] += acc;
+    }
+    __syncthreads();
+  }
+#undef AV
+}
+
 // ubar = (d f_T / du)^T fbar at stage state U (whose RHS value is F), time factor g
 // VJP of the PBL mixing term t_k = f_k (qbar - q_k) / tau with qbar = sum_j w_j q_j / den:
 // ubar_j += (w_j / den) * (sum_k fbar_k f_k) / tau - fbar_j f_j / tau, per tracer and column
@@ -486,21 +718,87 @@ __global__ void k_pbl_vjp(DevTransport<double> T, const double* __restrict__ fba
   }
 }
 
+// The fused adjoint pencils for all three directions, or false (nothing launched) when a
+// direction's pencils do not fit in shared memory -- the caller then uses the face + gather
+// kernels, which compute the same bits.
+constexpr size_t kAdjSmemCap = 110 * 1024;  // two blocks per SM
+static size_t adj_pencil_bytes(int n, int pw) {
+  return ((size_t)adj_pencil_doubles(n) * sizeof(double) + (size_t)(n + 1) * sizeof(int)) * pw;
+}
+template <int DIR, int PW>
+static void adj_pencil_launch(cudaStream_t st, const DevTransport<double>& T, const double* U,
+                              const double* G, double* ubar, double g, size_t smem) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_adj_pencil<DIR, PW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kAdjSmemCap);
+    attr = true;
+  }
+  const size_t ncol = (size_t)T.nlon * T.nlat;
+  if constexpr (DIR == 0) {
+    const int thr = std::min(256, (T.nlon + 6 + 31) / 32 * 32);
+    k_adj_pencil<0, 1><<<dim3((unsigned)(T.nlat * T.nlev), (unsigned)T.ntr), thr, smem, st>>>(T, U, G, ubar, g);
+  } else if constexpr (DIR == 1) {
+    const unsigned ntile = (unsigned)((T.nlon + PW - 1) / PW);
+    k_adj_pencil<1, PW><<<dim3(ntile * (unsigned)T.nlev, (unsigned)T.ntr), dim3(PW, 256 / PW), smem, st>>>(T, U, G, ubar, g);
+  } else {
+    k_adj_pencil<2, PW><<<dim3((unsigned)((ncol + PW - 1) / PW), (unsigned)T.ntr), dim3(PW, 256 / PW), smem, st>>>(T, U, G, ubar, g);
+  }
+}
+template <int DIR>
+static bool adj_pencil_dir(cudaStream_t st, const DevTransport<double>& T, const double* U,
+                           const double* G, double* ubar, double g, bool dry) {
+  const int n = DIR == 0 ? T.nlon : (DIR == 1 ? T.nlat : T.nlev);
+  if constexpr (DIR == 0) {
+    const size_t b = adj_pencil_bytes(n, 1);
+    if (b > kAdjSmemCap) return false;
+    if (!dry) adj_pencil_launch<0, 1>(st, T, U, G, ubar, g, b);
+    return true;
+  } else {
+    // the widest pencil tile that leaves room for four blocks per SM, else for two
+    int pick = 0;
+    for (int pw : {16, 8, 4})
+      if (!pick && adj_pencil_bytes(n, pw) <= kAdjSmemCap / 2) pick = pw;
+    for (int pw : {16, 8, 4})
+      if (!pick && adj_pencil_bytes(n, pw) <= kAdjSmemCap) pick = pw;
+    if (!pick) return false;
+    const size_t b = adj_pencil_bytes(n, pick);
+    if (!dry) {
+      if (pick == 16) adj_pencil_launch<DIR, 16>(st, T, U, G, ubar, g, b);
+      else if (pick == 8) adj_pencil_launch<DIR, 8>(st, T, U, G, ubar, g, b);
+      else adj_pencil_launch<DIR, 4>(st, T, U, G, ubar, g, b);
+    }
+    return true;
+  }
+}
+static bool launch_adj_pencils(cudaStream_t st, const DevTransport<double>& T, const double* U,
+                               const double* G, double* ubar, double g) {
+  if (!adj_pencil_dir<0>(st, T, U, G, ubar, g, true) || !adj_pencil_dir<1>(st, T, U, G, ubar, g, true) ||
+      !adj_pencil_dir<2>(st, T, U, G, ubar, g, true))
+    return false;
+  adj_pencil_dir<0>(st, T, U, G, ubar, g, false);
+  adj_pencil_dir<1>(st, T, U, G, ubar, g, false);
+  adj_pencil_dir<2>(st, T, U, G, ubar, g, false);
+  return true;
+}
+
 void launch_transport_rhs_vjp(cudaStream_t st, const DevTransport<double>& T, const double* U,
                               const double* F, const double* fbar, double* ubar, double* G,
                               double* Cf, double g) {
   size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
   unsigned nb = (unsigned)((nc + 255) / 256);
   k_adj_cell<<<nb, 256, 0, st>>>(T, U, F, fbar, ubar, G, g);
-  long long nx = (long long)(T.nlon + 1) * T.nlat * T.nlev;
-  long long ny = (long long)T.nlon * (T.nlat + 1) * T.nlev;
-  long long nz = (long long)T.nlon * T.nlat * (T.nlev + 1);
-  k_adj_face<0><<<(unsigned)((nx + 255) / 256), 256, 0, st>>>(T, U, G, Cf, g);
-  k_adj_gather<0><<<nb, 256, 0, st>>>(T, U, Cf, ubar, g);
-  k_adj_face<1><<<(unsigned)((ny + 255) / 256), 256, 0, st>>>(T, U, G, Cf, g);
-  k_adj_gather<1><<<nb, 256, 0, st>>>(T, U, Cf, ubar, g);
-  k_adj_face<2><<<(unsigned)((nz + 255) / 256), 256, 0, st>>>(T, U, G, Cf, g);
-  k_adj_gather<2><<<nb, 256, 0, st>>>(T, U, Cf, ubar, g);
+  if (!launch_adj_pencils(st, T, U, G, ubar, g)) {  // pencils too long for shared memory
+    long long nx = (long long)(T.nlon + 1) * T.nlat * T.nlev;
+    long long ny = (long long)T.nlon * (T.nlat + 1) * T.nlev;
+    long long nz = (long long)T.nlon * T.nlat * (T.nlev + 1);
+    k_adj_face<0><<<(unsigned)((nx + 255) / 256), 256, 0, st>>>(T, U, G, Cf, g);
+    k_adj_gather<0><<<nb, 256, 0, st>>>(T, U, Cf, ubar, g);
+    k_adj_face<1><<<(unsigned)((ny + 255) / 256), 256, 0, st>>>(T, U, G, Cf, g);
+    k_adj_gather<1><<<nb, 256, 0, st>>>(T, U, Cf, ubar, g);
+    k_adj_face<2><<<(unsigned)((nz + 255) / 256), 256, 0, st>>>(T, U, G, Cf, g);
+    k_adj_gather<2><<<nb, 256, 0, st>>>(T, U, Cf, ubar, g);
+  }
   if (T.pbl) {
     size_t n = (size_t)T.ntr * T.nlon * T.nlat;
     k_pbl_vjp<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(T, fbar, ubar);
