@@ -285,7 +285,7 @@ __device__ __forceinline__ void face_weights_lin(const double* v, bool right, bo
 // index maps of a stencil position p along a direction -> position in range, or -1 (open ghost)
 __device__ __forceinline__ int map_pos(int p, int n, int bc) {
   if (p >= 0 && p < n) return p;
-  if (bc == 0) return ((p % n) + n) % n;  // periodic
+  if (bc == 0) return p < 0 ? p + n : p - n;  // periodic (stencil positions lie in [-3, n+2])
   if (bc == 1) return -1;                  // open: boundary data, no state
   return p < 0 ? -1 - p : 2 * n - 1 - p;   // mirror (closed walls, vertical)
 }

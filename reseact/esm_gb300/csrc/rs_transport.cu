@@ -1321,10 +1321,13 @@ __global__ void __launch_bounds__(kRedThreads) k_stage(DevTransport<double> T,
     int j = (int)((c / T.nlon) % T.nlat);
     int k = (int)(c / ((size_t)T.nlon * T.nlat));
     CellGeo G{T.gx[j], T.gylo[j], T.gyhi[j]};
-    double divM = div_m(T, i, j, k, g, G);
+    double hz, vz;  // the air-mass divergence, once per cell: tracers and the air-mass row
+    div_parts(T, i, j, k, g, G, hz, vz);
+    const double divM = hz + vz;
+    const double dmdt = T.mcorr ? -((hz + T.mcorr[c]) + vz) : -(hz + vz);  // = dm_dt(...)
     double m = Qin[(size_t)(T.nsp - 1) * nc + c];
 #if !RS_STRICT
-    double rm = 1.0 / m;
+    double rm = rcp_nr(m);  // m > 0
 #endif
     const int nfx = T.nlon + 1, nfy = T.nlat + 1;
     const size_t ncol = (size_t)T.nlon * T.nlat, col = (size_t)j * T.nlon + i;
@@ -1368,7 +1371,7 @@ __global__ void __launch_bounds__(kRedThreads) k_stage(DevTransport<double> T,
         }
 #endif
       } else {
-        du = dm_dt(T, i, j, k, g, G, c);
+        du = dmdt;
       }
 #if RS_STRICT
       const double nx = q + dt_2 * du;
