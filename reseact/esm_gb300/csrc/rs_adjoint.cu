@@ -233,6 +233,47 @@ __device__ __forceinline__ void slope_form(double am, double a, double ap, doubl
     val = sg * ada;
   }
 }
+// slope_form without branches: the same value and coefficients for every input.  Each
+// coefficient of a limited slope is an exact constant (0, +-1/2, +-2) or a sign flip of a
+// vertical coefficient, so the frozen branch is picked by integer compares of the magnitude
+// bits (2|d| = |d| with the exponent field + 1 for the nonzero d of a live slope) and selects;
+// the fused adjoint pencils' lanes then issue the same 4-5 FP64 instructions whatever branch
+// their cell took.
+__device__ __forceinline__ void slope_form_bf(double am, double a, double ap, double sA, double sB,
+                                              bool uniform, double& val, double c[3]) {
+  const double d0 = a - am, d1 = ap - a;
+#if RS_STRICT
+  const bool live = d1 * d0 > 0.0;
+#else
+  const bool live = sgn_same_nz(d0, d1);  // the forward kernels' test
+#endif
+  const double da = uniform ? 0.5 * (ap - am) : sA * d1 + sB * d0;
+  const long long b0 = __double_as_longlong(d0), b1 = __double_as_longlong(d1),
+                  bd = __double_as_longlong(da);
+  const long long m0 = b0 & kMagMask, m1 = b1 & kMagMask, mda = bd & kMagMask;
+  const bool pick1 = m1 < m0;                          // 2|d1| < 2|d0|
+  const long long limb = (pick1 ? m1 : m0) + kExpOne;  // 2 min(|d0|, |d1|)
+  const bool binds = limb < mda;                       // the limit binds
+  const bool dneg = bd < 0;                            // signbit(da)
+  val = live ? __longlong_as_double((binds ? limb : mda) | (bd & kSignBit)) : 0.0;
+  // limited: c = (0, -m, m) or (-m, m, 0) with m = (d < 0 ? -2 : 2) * sg, d the picked difference
+  const bool mneg = (pick1 ? (b1 < 0) : (b0 < 0)) != dneg;
+  const double m = mneg ? -2.0 : 2.0;
+  // unlimited: c = (da < 0 ? -1 : 1) * sg * f, which is -f only for da == -0
+  double f0 = -0.5, f1 = 0.0, f2 = 0.5;
+  if (!uniform) {
+    f0 = -sB;
+    f1 = sB - sA;
+    f2 = sA;
+  }
+  const bool flip = bd == kSignBit;
+  const double u0 = flip ? -f0 : f0, u1 = flip ? -f1 : f1, u2 = flip ? -f2 : f2;
+  const double l0 = pick1 ? 0.0 : -m, l1 = pick1 ? -m : m, l2 = pick1 ? m : 0.0;
+  c[0] = live ? sel_d(binds, l0, u0) : 0.0;
+  c[1] = live ? sel_d(binds, l1, u1) : 0.0;
+  c[2] = live ? sel_d(binds, l2, u2) : 0.0;
+}
+
 __device__ __forceinline__ void face_weights_lin(const double* v, bool right, bool uniform,
                                                  const double* sA, const double* sB,
                                                  const double* eL, const double* eR, double* w) {
@@ -578,7 +619,7 @@ __global__ void __launch_bounds__(256) k_adj_pencil(DevTransport<double> T,
         sB = T.vsB[(size_t)(p + 1) * ncol + colz];
       }
       double val, c[3];
-      slope_form(AV(V, p + 2), AV(V, p + 3), AV(V, p + 4), sA, sB, DIR != 2, val, c);
+      slope_form_bf(AV(V, p + 2), AV(V, p + 3), AV(V, p + 4), sA, sB, DIR != 2, val, c);
       AV(SV, p + 2) = val;
       for (int o = 0; o < 3; ++o) AV(SC, o * (n + 4) + p + 2) = c[o];
     }
@@ -634,18 +675,27 @@ __global__ void __launch_bounds__(256) k_adj_pencil(DevTransport<double> T,
         R[1 + o] = AV(EW, o * (n + 3) + up + 2);  // edge up+1: positions up-1 .. up+2
       }
       const double aLv = AV(EV, up + 1), aRv = AV(EV, up + 2), a = AV(V, up + 3);
+      // the limiter's decisions as the forward kernels take them, then one set of weights
+      // per lane by selects: flat -> e_2; steepened side -> 3 e_2 - 2 (other side); else the side
+      const double dA = aRv - aLv;
+      const double a6 = 6.0 * (a - 0.5 * (aLv + aRv));
+#if RS_STRICT
+      const bool flat = (aRv - a) * (a - aLv) <= 0.0;
+      const bool stl = dA * a6 > dA * dA;                      // aL <- 3a - 2aR
+      const bool str = !stl && (-(dA * dA) > dA * a6);         // aR <- 3a - 2aL
+#else
+      const long long ka = ord_key(a), kl = ord_key(aLv), kr = ord_key(aRv);
+      const bool flat = !((kr > ka && ka > kl) || (kr < ka && ka < kl));
+      const long long kd = ord_key(dA), k6 = ord_key(a6);
+      const bool stl = (kd > 0 && k6 > kd) || (kd < 0 && k6 < kd);
+      const bool str = !stl && ((kd > 0 && k6 < -kd) || (kd < 0 && k6 > -kd));
+#endif
+      const bool need = (stl && !right) || (str && right);
       double w[5];
-      if ((aRv - a) * (a - aLv) <= 0.0) {
-        for (int o = 0; o < 5; ++o) w[o] = o == 2 ? 1.0 : 0.0;
-      } else {
-        const double dA = aRv - aLv;
-        const double a6 = 6.0 * (a - 0.5 * (aLv + aRv));
-        if (dA * a6 > dA * dA) {
-          for (int o = 0; o < 5; ++o) L[o] = (o == 2 ? 3.0 : 0.0) - 2.0 * R[o];
-        } else if (-(dA * dA) > dA * a6) {
-          for (int o = 0; o < 5; ++o) R[o] = (o == 2 ? 3.0 : 0.0) - 2.0 * L[o];
-        }
-        for (int o = 0; o < 5; ++o) w[o] = right ? R[o] : L[o];
+      for (int o = 0; o < 5; ++o) {
+        const double st = (o == 2 ? 3.0 : 0.0) - 2.0 * sel_d(stl, R[o], L[o]);
+        const double side = sel_d(right, R[o], L[o]);
+        w[o] = sel_d(flat, o == 2 ? 1.0 : 0.0, sel_d(need, st, side));
       }
       double cbw, caw;
       if (DIR == 0) cbw = caw = T.gx[j];

@@ -225,6 +225,30 @@ __device__ __forceinline__ double amax_bits(double a, double b) {
   return __longlong_as_double(ma > mb ? ma : mb);
 }
 
+// ------------------------------------------------------------------ integer-pipe FP64 helpers
+// Sign tests, magnitude compares and selects of doubles on their bit patterns (the integer
+// pipes; FP64 issues at ~2 lanes per SM per clock on this GPU).
+// d0, d1 nonzero with equal signs: d1*d0 > 0 unless the product underflows
+__device__ __forceinline__ bool sgn_same_nz(double a, double b) {
+  const int ha = __double2hiint(a), hb = __double2hiint(b);
+  const bool nza = ((ha & 0x7fffffff) | __double2loint(a)) != 0;
+  const bool nzb = ((hb & 0x7fffffff) | __double2loint(b)) != 0;
+  return ((ha ^ hb) >= 0) & nza & nzb;
+}
+constexpr long long kMagMask = 0x7fffffffffffffffLL, kSignBit = (long long)0x8000000000000000ULL,
+                    kExpOne = 1LL << 52;
+__device__ __forceinline__ double sel_d(bool c, double x, double y) {
+  return __longlong_as_double(c ? __double_as_longlong(x) : __double_as_longlong(y));
+}
+// Order-preserving integer key of a finite double (-0 and +0 both map to 0, key(-x) = -key(x)):
+// the sign of the rounded difference x - y is the sign of key(x) - key(y) (gradual underflow
+// makes x - y == 0 exactly when x == y), so the limiter's sign tests need no subtraction.
+__device__ __forceinline__ long long ord_key(double x) {
+  const long long b = __double_as_longlong(x);
+  const long long sgn = b >> 63;  // 0 or -1
+  return (b ^ (sgn & kMagMask)) - sgn;
+}
+
 // ------------------------------------------------------------------ fixed-tree reductions
 // Pairwise tree over 256 lanes: v[t] += v[t+s] for s = 128 ... 1 (identical to the CPU
 // restatement's tree256).  Returns the total in thread 0.

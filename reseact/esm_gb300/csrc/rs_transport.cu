@@ -68,14 +68,6 @@ __device__ __forceinline__ void limit(double a, double& aL, double& aR) {
 // steepening tests dA*a6 > dA*dA and -(dA*dA) > dA*a6 become sign tests of dA and a6 -+ dA,
 // which can differ from the FP forms only where a6 = +-dA to roundoff -- where the limiter is
 // continuous (the steepened edge equals the unsteepened one), so a face moves by roundoff only.
-__device__ __forceinline__ bool sgn_same_nz(double a, double b) {
-  const int ha = __double2hiint(a), hb = __double2hiint(b);
-  const bool nza = ((ha & 0x7fffffff) | __double2loint(a)) != 0;
-  const bool nzb = ((hb & 0x7fffffff) | __double2loint(b)) != 0;
-  return ((ha ^ hb) >= 0) & nza & nzb;
-}
-constexpr long long kMagMask = 0x7fffffffffffffffLL, kSignBit = (long long)0x8000000000000000ULL,
-                    kExpOne = 1LL << 52;
 // copysign(min(|da|, 2 min(|d0|, |d1|)), da) from |da| and da's sign as bits
 __device__ __forceinline__ double slope_pick(long long abs_da, long long sign_da, double d0, double d1) {
   const long long m0 = __double_as_longlong(d0) & kMagMask, m1 = __double_as_longlong(d1) & kMagMask;
@@ -94,20 +86,10 @@ __device__ __forceinline__ double slope_n_fast(double am, double a, double ap, d
   const double v = slope_pick(db & kMagMask, db & kSignBit, d0, d1);
   return __longlong_as_double(sgn_same_nz(d0, d1) ? __double_as_longlong(v) : 0LL);
 }
-// Branch-free: every lane issues the same ten FP64 instructions and picks its result with
-// integer selects -- with the limiter's data-dependent branches, a warp issued both sides and
-// the FP64 pipe (16 cycles per warp instruction) ran with about half its lanes idle.
-__device__ __forceinline__ double sel_d(bool c, double x, double y) {
-  return __longlong_as_double(c ? __double_as_longlong(x) : __double_as_longlong(y));
-}
-// Order-preserving integer key of a finite double (-0 and +0 both map to 0, key(-x) = -key(x)):
-// the sign of the rounded difference x - y is the sign of key(x) - key(y) (gradual underflow
-// makes x - y == 0 exactly when x == y), so the limiter's sign tests need no subtraction.
-__device__ __forceinline__ long long ord_key(double x) {
-  const long long b = __double_as_longlong(x);
-  const long long sgn = b >> 63;  // 0 or -1
-  return (b ^ (sgn & kMagMask)) - sgn;
-}
+// Branch-free: every lane issues the same six FP64 instructions (dA, a6, one steepened edge) and
+// picks its result with integer selects -- with the limiter's data-dependent branches, a warp
+// issued both sides and the FP64 pipe (16 cycles per warp instruction) ran with about half its
+// lanes idle.
 __device__ __forceinline__ void limit_fast(double a, double& aL, double& aR) {
   const long long ka = ord_key(a), kl = ord_key(aL), kr = ord_key(aR);
   // extremum: (aR - a)(a - aL) <= 0
