@@ -422,7 +422,13 @@ def run_gb300(args):
         roofline = {"kernel": "ros23 attempt (%s, %s)" % (kinfo.get("kind"), kinfo.get("variant", "-")),
                     "bound": "fp64", "achieved": round(achieved, 4),
                     "peak": peak, "unit": "TFLOP/s", "frac": round(achieved / peak, 4) if peak else None,
-                    "traffic": None, "flops_per_cell_attempt": round(f_exec, 1),
+                    # DRAM bytes per launch from one ncu capture of this kernel on this
+                    # workload (dram__bytes_read.sum + dram__bytes_write.sum: 296.8 MB + 996.1 MB,
+                    # mostly the 128-register variant's spill stores); null for other kernels
+                    "traffic": (1292.9e6 if (kinfo.get("kind") == "specialized" and not args.small
+                                             and kinfo.get("variant") == "regs2") else None),
+                    "traffic_source": "ncu capture summarised in profiles/rs_jit_attempt_c2_144x91x47.md",
+                    "flops_per_cell_attempt": round(f_exec, 1),
                     # FP64 issue: instructions / (peak flops / 2 per FMA instruction); the flop
                     # fraction is capped below 1 by the kernel's share of non-FMA instructions
                     "fp64_issue_frac": (round(i_exec * nc / sec / (peak * 1e12 / 2), 4)
