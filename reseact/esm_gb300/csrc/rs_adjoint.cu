@@ -242,6 +242,10 @@ __device__ __forceinline__ void slope_form(double am, double a, double ap, doubl
 __device__ __forceinline__ void slope_form_bf(double am, double a, double ap, double sA, double sB,
                                               bool uniform, double& val, double c[3]) {
   const double d0 = a - am, d1 = ap - a;
+  if (prod_may_underflow(d0, d1)) {  // tiny or subnormal differences: the FP form, as forward
+    slope_form(am, a, ap, sA, sB, uniform, val, c);
+    return;
+  }
 #if RS_STRICT
   const bool live = d1 * d0 > 0.0;
 #else
@@ -679,17 +683,21 @@ __global__ void __launch_bounds__(256) k_adj_pencil(DevTransport<double> T,
       // per lane by selects: flat -> e_2; steepened side -> 3 e_2 - 2 (other side); else the side
       const double dA = aRv - aLv;
       const double a6 = 6.0 * (a - 0.5 * (aLv + aRv));
-#if RS_STRICT
-      const bool flat = (aRv - a) * (a - aLv) <= 0.0;
-      const bool stl = dA * a6 > dA * dA;                      // aL <- 3a - 2aR
-      const bool str = !stl && (-(dA * dA) > dA * a6);         // aR <- 3a - 2aL
-#else
-      const long long ka = ord_key(a), kl = ord_key(aLv), kr = ord_key(aRv);
-      const bool flat = !((kr > ka && ka > kl) || (kr < ka && ka < kl));
-      const long long kd = ord_key(dA), k6 = ord_key(a6);
-      const bool stl = (kd > 0 && k6 > kd) || (kd < 0 && k6 < kd);
-      const bool str = !stl && ((kd > 0 && k6 < -kd) || (kd < 0 && k6 > -kd));
+      bool flat, stl, str;
+#if !RS_STRICT
+      if (!(tiny_operand(a) || tiny_operand(aLv) || tiny_operand(aRv))) {
+        const long long ka = ord_key(a), kl = ord_key(aLv), kr = ord_key(aRv);
+        flat = !((kr > ka && ka > kl) || (kr < ka && ka < kl));
+        const long long kd = ord_key(dA), k6 = ord_key(a6);
+        stl = (kd > 0 && k6 > kd) || (kd < 0 && k6 < kd);
+        str = !stl && ((kd > 0 && k6 < -kd) || (kd < 0 && k6 > -kd));
+      } else
 #endif
+      {
+        flat = (aRv - a) * (a - aLv) <= 0.0;
+        stl = dA * a6 > dA * dA;                      // aL <- 3a - 2aR
+        str = !stl && (-(dA * dA) > dA * a6);         // aR <- 3a - 2aL
+      }
       const bool need = (stl && !right) || (str && right);
       double w[5];
       for (int o = 0; o < 5; ++o) {

@@ -240,6 +240,24 @@ constexpr long long kMagMask = 0x7fffffffffffffffLL, kSignBit = (long long)0x800
 __device__ __forceinline__ double sel_d(bool c, double x, double y) {
   return __longlong_as_double(c ? __double_as_longlong(x) : __double_as_longlong(y));
 }
+// Biased exponent field of x (0 for zero and subnormals).
+__device__ __forceinline__ int bexp(double x) { return (__double2hiint(x) >> 20) & 0x7ff; }
+__device__ __forceinline__ bool is_zero_d(double x) {
+  return ((__double2hiint(x) & 0x7fffffff) | __double2loint(x)) == 0;
+}
+// The integer forms reproduce the FP forms' products d0*d1 only while those cannot underflow:
+// for nonzero normal d0, d1 the product is >= 2^(e0 + e1 - 2046), nonzero when e0 + e1 >= 972.
+// Where a product could underflow (or an operand is subnormal) the FP form decides instead.
+__device__ __forceinline__ bool prod_may_underflow(double d0, double d1) {
+  if (is_zero_d(d0) || is_zero_d(d1)) return false;  // exact zero either way
+  const int e0 = bexp(d0), e1 = bexp(d1);
+  return e0 == 0 || e1 == 0 || e0 + e1 < 980;
+}
+// Any nonzero difference of doubles >= 2^-484 in magnitude (or zero) is >= 2^-537, so
+// products of two such differences do not underflow; tiny operands use the FP form.
+__device__ __forceinline__ bool tiny_operand(double x) {
+  return !is_zero_d(x) && bexp(x) < 539;
+}
 // Order-preserving integer key of a finite double (-0 and +0 both map to 0, key(-x) = -key(x)):
 // the sign of the rounded difference x - y is the sign of key(x) - key(y) (gradual underflow
 // makes x - y == 0 exactly when x == y), so the limiter's sign tests need no subtraction.

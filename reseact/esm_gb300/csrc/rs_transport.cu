@@ -64,7 +64,8 @@ __device__ __forceinline__ void limit(double a, double& aL, double& aR) {
 //   d1*d0 > 0            <=>  d0, d1 nonzero with equal signs       (unless the product underflows)
 //   0.5*s, 2*m           =    exponent field -1 / +1                 (normal operands)
 //   fmin of magnitudes   =    integer min of the magnitude bits
-// so slopes and the extremum test are bit-identical to the FP forms for normal operands.  The
+// so slopes and the extremum test are bit-identical to the FP forms for normal operands (where a
+// product of differences could underflow, or an operand is subnormal, the FP form decides).  The
 // steepening tests dA*a6 > dA*dA and -(dA*dA) > dA*a6 become sign tests of dA and a6 -+ dA,
 // which can differ from the FP forms only where a6 = +-dA to roundoff -- where the limiter is
 // continuous (the steepened edge equals the unsteepened one), so a face moves by roundoff only.
@@ -76,12 +77,14 @@ __device__ __forceinline__ double slope_pick(long long abs_da, long long sign_da
 }
 __device__ __forceinline__ double slope_u_fast(double am, double a, double ap) {
   const double d0 = a - am, d1 = ap - a;
+  if (prod_may_underflow(d0, d1)) return slope_u(am, a, ap);
   const long long sb = __double_as_longlong(ap - am);  // nonzero where used; |da| = |ap - am| / 2
   const double v = slope_pick((sb & kMagMask) - kExpOne, sb & kSignBit, d0, d1);
   return __longlong_as_double(sgn_same_nz(d0, d1) ? __double_as_longlong(v) : 0LL);
 }
 __device__ __forceinline__ double slope_n_fast(double am, double a, double ap, double sA, double sB) {
   const double d0 = a - am, d1 = ap - a;
+  if (prod_may_underflow(d0, d1)) return slope_n(am, a, ap, sA, sB);
   const long long db = __double_as_longlong(sA * d1 + sB * d0);
   const double v = slope_pick(db & kMagMask, db & kSignBit, d0, d1);
   return __longlong_as_double(sgn_same_nz(d0, d1) ? __double_as_longlong(v) : 0LL);
@@ -91,6 +94,10 @@ __device__ __forceinline__ double slope_n_fast(double am, double a, double ap, d
 // issued both sides and the FP64 pipe (16 cycles per warp instruction) ran with about half its
 // lanes idle.
 __device__ __forceinline__ void limit_fast(double a, double& aL, double& aR) {
+  if (tiny_operand(a) || tiny_operand(aL) || tiny_operand(aR)) {
+    limit(a, aL, aR);
+    return;
+  }
   const long long ka = ord_key(a), kl = ord_key(aL), kr = ord_key(aR);
   // extremum: (aR - a)(a - aL) <= 0
   const bool flat = !((kr > ka && ka > kl) || (kr < ka && ka < kl));
@@ -140,6 +147,14 @@ __device__ __forceinline__ double slope_ud(double d0, double d1, double am, doub
   }
   return 0.0;
 #else
+  if (prod_may_underflow(d0, d1)) {
+    if (d1 * d0 > 0.0) {
+      double da = 0.5 * (ap - am);
+      double lim = 2.0 * fmin(fabs(d0), fabs(d1));
+      return copysign(fmin(fabs(da), lim), da);
+    }
+    return 0.0;
+  }
   const long long sb = __double_as_longlong(ap - am);
   const double v = slope_pick((sb & kMagMask) - kExpOne, sb & kSignBit, d0, d1);
   return __longlong_as_double(sgn_same_nz(d0, d1) ? __double_as_longlong(v) : 0LL);
@@ -154,6 +169,14 @@ __device__ __forceinline__ double slope_nd(double d0, double d1, double sA, doub
   }
   return 0.0;
 #else
+  if (prod_may_underflow(d0, d1)) {
+    if (d1 * d0 > 0.0) {
+      double da = sA * d1 + sB * d0;
+      double lim = 2.0 * fmin(fabs(d0), fabs(d1));
+      return copysign(fmin(fabs(da), lim), da);
+    }
+    return 0.0;
+  }
   const long long db = __double_as_longlong(sA * d1 + sB * d0);
   const double v = slope_pick(db & kMagMask, db & kSignBit, d0, d1);
   return __longlong_as_double(sgn_same_nz(d0, d1) ? __double_as_longlong(v) : 0LL);
