@@ -252,16 +252,19 @@ __device__ __forceinline__ void slope_form_bf(double am, double a, double ap, do
   const bool live = sgn_same_nz(d0, d1);  // the forward kernels' test
 #endif
   const double da = uniform ? 0.5 * (ap - am) : sA * d1 + sB * d0;
-  const long long b0 = __double_as_longlong(d0), b1 = __double_as_longlong(d1),
-                  bd = __double_as_longlong(da);
-  const long long m0 = b0 & kMagMask, m1 = b1 & kMagMask, mda = bd & kMagMask;
-  const bool pick1 = m1 < m0;                          // 2|d1| < 2|d0|
-  const long long limb = (pick1 ? m1 : m0) + kExpOne;  // 2 min(|d0|, |d1|)
-  const bool binds = limb < mda;                       // the limit binds
-  const bool dneg = bd < 0;                            // signbit(da)
-  val = live ? __longlong_as_double((binds ? limb : mda) | (bd & kSignBit)) : 0.0;
+  const int s0 = __double2hiint(d0), s1 = __double2hiint(d1), sd = __double2hiint(da);
+  const unsigned h0 = (unsigned)s0 & 0x7fffffffu, l0 = (unsigned)__double2loint(d0);
+  const unsigned h1 = (unsigned)s1 & 0x7fffffffu, l1 = (unsigned)__double2loint(d1);
+  const unsigned hd = (unsigned)sd & 0x7fffffffu, ld = (unsigned)__double2loint(da);
+  const bool pick1 = mag_lt(h1, l1, h0, l0);                              // 2|d1| < 2|d0|
+  const unsigned hm = (pick1 ? h1 : h0) + (1u << 20), lm = pick1 ? l1 : l0;  // 2 min(|d0|, |d1|)
+  const bool binds = mag_lt(hm, lm, hd, ld);                              // the limit binds
+  const bool dneg = sd < 0;                                               // signbit(da)
+  val = live ? __hiloint2double((int)((binds ? hm : hd) | ((unsigned)sd & 0x80000000u)),
+                                (int)(binds ? lm : ld))
+             : 0.0;
   // limited: c = (0, -m, m) or (-m, m, 0) with m = (d < 0 ? -2 : 2) * sg, d the picked difference
-  const bool mneg = (pick1 ? (b1 < 0) : (b0 < 0)) != dneg;
+  const bool mneg = (pick1 ? (s1 < 0) : (s0 < 0)) != dneg;
   const double m = mneg ? -2.0 : 2.0;
   // unlimited: c = (da < 0 ? -1 : 1) * sg * f, which is -f only for da == -0
   double f0 = -0.5, f1 = 0.0, f2 = 0.5;
@@ -270,12 +273,12 @@ __device__ __forceinline__ void slope_form_bf(double am, double a, double ap, do
     f1 = sB - sA;
     f2 = sA;
   }
-  const bool flip = bd == kSignBit;
+  const bool flip = (unsigned)sd == 0x80000000u && ld == 0u;  // da == -0.0
   const double u0 = flip ? -f0 : f0, u1 = flip ? -f1 : f1, u2 = flip ? -f2 : f2;
-  const double l0 = pick1 ? 0.0 : -m, l1 = pick1 ? -m : m, l2 = pick1 ? m : 0.0;
-  c[0] = live ? sel_d(binds, l0, u0) : 0.0;
-  c[1] = live ? sel_d(binds, l1, u1) : 0.0;
-  c[2] = live ? sel_d(binds, l2, u2) : 0.0;
+  const double q0 = pick1 ? 0.0 : -m, q1 = pick1 ? -m : m, q2 = pick1 ? m : 0.0;
+  c[0] = live ? sel_d(binds, q0, u0) : 0.0;
+  c[1] = live ? sel_d(binds, q1, u1) : 0.0;
+  c[2] = live ? sel_d(binds, q2, u2) : 0.0;
 }
 
 __device__ __forceinline__ void face_weights_lin(const double* v, bool right, bool uniform,

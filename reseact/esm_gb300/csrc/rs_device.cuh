@@ -219,10 +219,11 @@ __device__ __forceinline__ double rcp_nr1(double d) {
   asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(d));
   return fma(r, fma(-d, r, 1.0), r);
 }
-__device__ __forceinline__ double amax_bits(double a, double b) {
-  const long long ma = __double_as_longlong(a) & 0x7fffffffffffffffLL;
-  const long long mb = __double_as_longlong(b) & 0x7fffffffffffffffLL;
-  return __longlong_as_double(ma > mb ? ma : mb);
+__device__ __forceinline__ double amax_bits(double a, double b) {  // on 32-bit halves
+  const unsigned ha = (unsigned)__double2hiint(a) & 0x7fffffffu, la = (unsigned)__double2loint(a);
+  const unsigned hb = (unsigned)__double2hiint(b) & 0x7fffffffu, lb = (unsigned)__double2loint(b);
+  const bool bl = ha < hb || (ha == hb && la < lb);
+  return __hiloint2double((int)(bl ? hb : ha), (int)(bl ? lb : la));
 }
 
 // ------------------------------------------------------------------ integer-pipe FP64 helpers
@@ -239,6 +240,12 @@ constexpr long long kMagMask = 0x7fffffffffffffffLL, kSignBit = (long long)0x800
                     kExpOne = 1LL << 52;
 __device__ __forceinline__ double sel_d(bool c, double x, double y) {
   return __longlong_as_double(c ? __double_as_longlong(x) : __double_as_longlong(y));
+}
+// |x| < |y| for magnitude bit patterns given as (hi & 0x7fffffff, lo) halves.  The integer
+// helpers work on 32-bit halves: 64-bit masks of reinterpreted doubles were partly emitted as
+// FP64 instructions.
+__device__ __forceinline__ bool mag_lt(unsigned h0, unsigned l0, unsigned h1, unsigned l1) {
+  return h0 < h1 || (h0 == h1 && l0 < l1);
 }
 // Biased exponent field of x (0 for zero and subnormals).
 __device__ __forceinline__ int bexp(double x) { return (__double2hiint(x) >> 20) & 0x7ff; }

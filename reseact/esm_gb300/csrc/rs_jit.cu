@@ -325,11 +325,13 @@ __device__ __forceinline__ double rcp_nr1(double d) {
   asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(d));
   return fma(r, fma(-d, r, 1.0), r);
 }
-// max(|a|, |b|) as the larger magnitude bit pattern (integer pipe; NaN stays NaN)
+// max(|a|, |b|) as the larger magnitude bit pattern, on 32-bit halves (integer pipe; NaN stays
+// NaN)
 __device__ __forceinline__ double amax_bits(double a, double b) {
-  const long long ma = __double_as_longlong(a) & 0x7fffffffffffffffLL;
-  const long long mb = __double_as_longlong(b) & 0x7fffffffffffffffLL;
-  return __longlong_as_double(ma > mb ? ma : mb);
+  const unsigned ha = (unsigned)__double2hiint(a) & 0x7fffffffu, la = (unsigned)__double2loint(a);
+  const unsigned hb = (unsigned)__double2hiint(b) & 0x7fffffffu, lb = (unsigned)__double2loint(b);
+  const bool bl = ha < hb || (ha == hb && la < lb);
+  return __hiloint2double((int)(bl ? hb : ha), (int)(bl ? lb : la));
 }
 
 // pairwise tree over 256 lanes, v[t] += v[t+s] for s = 128 ... 1; total in thread 0

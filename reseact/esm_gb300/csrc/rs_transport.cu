@@ -69,25 +69,32 @@ __device__ __forceinline__ void limit(double a, double& aL, double& aR) {
 // steepening tests dA*a6 > dA*dA and -(dA*dA) > dA*a6 become sign tests of dA and a6 -+ dA,
 // which can differ from the FP forms only where a6 = +-dA to roundoff -- where the limiter is
 // continuous (the steepened edge equals the unsteepened one), so a face moves by roundoff only.
-// copysign(min(|da|, 2 min(|d0|, |d1|)), da) from |da| and da's sign as bits
-__device__ __forceinline__ double slope_pick(long long abs_da, long long sign_da, double d0, double d1) {
-  const long long m0 = __double_as_longlong(d0) & kMagMask, m1 = __double_as_longlong(d1) & kMagMask;
-  const long long lim = (m0 < m1 ? m0 : m1) + kExpOne;
-  return __longlong_as_double((abs_da < lim ? abs_da : lim) | sign_da);
+// copysign(min(|da|, 2 min(|d0|, |d1|)), da), or 0 where d0, d1 are not nonzero with equal
+// signs, on the 32-bit halves of the bit patterns.  (Written on 64-bit masks of reinterpreted
+// doubles, the same arithmetic was partly emitted as FP64 adds -- three per slope, measured with
+// ncu -- so everything here stays in 32-bit integer operations.)  `half`: |da| = |span| / 2.
+__device__ __forceinline__ double slope_pick32(double d0, double d1, double da, bool half) {
+  const unsigned hs = (unsigned)__double2hiint(da);
+  const unsigned hd = (hs & 0x7fffffffu) - (half ? (1u << 20) : 0u), ld = (unsigned)__double2loint(da);
+  const unsigned h0 = (unsigned)__double2hiint(d0) & 0x7fffffffu, l0 = (unsigned)__double2loint(d0);
+  const unsigned h1 = (unsigned)__double2hiint(d1) & 0x7fffffffu, l1 = (unsigned)__double2loint(d1);
+  const bool p1 = mag_lt(h1, l1, h0, l0);
+  const unsigned hm = (p1 ? h1 : h0) + (1u << 20), lm = p1 ? l1 : l0;  // 2 min(|d0|, |d1|)
+  const bool binds = mag_lt(hm, lm, hd, ld);
+  const unsigned hr = (binds ? hm : hd) | (hs & 0x80000000u), lr = binds ? lm : ld;
+  const bool live = ((__double2hiint(d0) ^ __double2hiint(d1)) >= 0) & ((h0 | l0) != 0u) &
+                    ((h1 | l1) != 0u);
+  return __hiloint2double(live ? (int)hr : 0, live ? (int)lr : 0);
 }
 __device__ __forceinline__ double slope_u_fast(double am, double a, double ap) {
   const double d0 = a - am, d1 = ap - a;
   if (prod_may_underflow(d0, d1)) return slope_u(am, a, ap);
-  const long long sb = __double_as_longlong(ap - am);  // nonzero where used; |da| = |ap - am| / 2
-  const double v = slope_pick((sb & kMagMask) - kExpOne, sb & kSignBit, d0, d1);
-  return __longlong_as_double(sgn_same_nz(d0, d1) ? __double_as_longlong(v) : 0LL);
+  return slope_pick32(d0, d1, ap - am, true);  // nonzero span where live; |da| = |ap - am| / 2
 }
 __device__ __forceinline__ double slope_n_fast(double am, double a, double ap, double sA, double sB) {
   const double d0 = a - am, d1 = ap - a;
   if (prod_may_underflow(d0, d1)) return slope_n(am, a, ap, sA, sB);
-  const long long db = __double_as_longlong(sA * d1 + sB * d0);
-  const double v = slope_pick(db & kMagMask, db & kSignBit, d0, d1);
-  return __longlong_as_double(sgn_same_nz(d0, d1) ? __double_as_longlong(v) : 0LL);
+  return slope_pick32(d0, d1, sA * d1 + sB * d0, false);
 }
 // Branch-free: every lane issues the same six FP64 instructions (dA, a6, one steepened edge) and
 // picks its result with integer selects -- with the limiter's data-dependent branches, a warp
@@ -155,9 +162,7 @@ __device__ __forceinline__ double slope_ud(double d0, double d1, double am, doub
     }
     return 0.0;
   }
-  const long long sb = __double_as_longlong(ap - am);
-  const double v = slope_pick((sb & kMagMask) - kExpOne, sb & kSignBit, d0, d1);
-  return __longlong_as_double(sgn_same_nz(d0, d1) ? __double_as_longlong(v) : 0LL);
+  return slope_pick32(d0, d1, ap - am, true);
 #endif
 }
 __device__ __forceinline__ double slope_nd(double d0, double d1, double sA, double sB) {
@@ -177,9 +182,7 @@ __device__ __forceinline__ double slope_nd(double d0, double d1, double sA, doub
     }
     return 0.0;
   }
-  const long long db = __double_as_longlong(sA * d1 + sB * d0);
-  const double v = slope_pick(db & kMagMask, db & kSignBit, d0, d1);
-  return __longlong_as_double(sgn_same_nz(d0, d1) ? __double_as_longlong(v) : 0LL);
+  return slope_pick32(d0, d1, sA * d1 + sB * d0, false);
 #endif
 }
 
