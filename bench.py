@@ -243,6 +243,22 @@ def transport_bytes_per_cell(nsp):
     return 2 * nsp * 8 + 3 * 8
 
 
+def max_over_ranks(x, world, device):
+    """The largest of a per-rank value over all ranks (the value itself on one rank)."""
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(cells, steps, world, ms):
+    """Whole-job cell-steps/s over `ms` (the slowest rank's time): each rank is a replica
+    of the full grid (weak scaling), so the job does world x cells x steps."""
+    return cells * steps * world / (ms * 1e-3)
+
+
 # ---------------------------------------------------------------------------- GB300 arm
 def run_gb300(args):
     import torch
@@ -299,12 +315,8 @@ def run_gb300(args):
             counts.append((st.naT, st.nrT, st.naC, st.nrC))
         barrier()
     ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
-    ms_t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-    if world > 1:
-        import torch.distributed as dist
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-    ms_max = float(ms_t.item())
-    value = nc * args.steps * world / (ms_max * 1e-3)
+    ms_max = max_over_ranks(ms, world, "cuda")
+    value = job_throughput(nc, args.steps, world, ms_max)
 
     # ------------------------------------------------------------------ e2e through the ABI
     e2e = None
@@ -323,11 +335,8 @@ def run_gb300(args):
             t += dtm
         barrier()
         wall = time.perf_counter() - t0
-        wt = torch.tensor([wall], device="cuda", dtype=torch.float64)
-        if world > 1:
-            import torch.distributed as dist
-            dist.all_reduce(wt, op=dist.ReduceOp.MAX)
-        e2e = {"value": nc * args.steps * world / float(wt.item()), "unit": UNIT,
+        wall_max = max_over_ranks(wall, world, "cuda")
+        e2e = {"value": job_throughput(nc, args.steps, world, wall_max * 1e3), "unit": UNIT,
                "h2d_bytes_per_step": int(solver.n * 8), "d2h_bytes_per_step": int(solver.n * 8)}
 
     # ------------------------------------------------------------------ other forms, same steps
