@@ -169,12 +169,20 @@ def ros23_flops_per_cell(mech, order=None):
 
 def ros23_exec_counts(mech, order, evals, emissions=False):
     """(FP64 flops, FP64 instructions) per cell of one attempt of the mechanism-specialised ROS23
-    kernel as generated (production build): the generator folds +-1 stoichiometric
-    coefficients into adds, writes every other multiply-add as one FMA (2 flops, 1
-    instruction), forms the pivot reciprocals with two Newton steps and the error-norm ones
-    with one.  `evals` = 3 RHS evaluations, or 2 when the attempt reuses f(x).  Checked against
-    ncu's DADD/DMUL/DFMA counts of the kernel (1,553 flops counted here, 1,570 measured, for a
-    3-evaluation attempt of SuperFast in the minimum-fill order)."""
+    kernel as generated (production build).  `evals` = 3 RHS evaluations, or 2 when the attempt
+    reuses f(x).
+
+    Flops are the algorithm's: each rate product once per reaction and one multiply-add per
+    stoichiometric term (+-1 coefficients folded into adds), FMA = 2; the LU with two Newton
+    steps per pivot reciprocal, the solves, the stage algebra and the error norm with one
+    Newton step per reciprocal.  Instructions follow the fused RHS the generator emits: per
+    reaction one head u_r = K_r * (all factors but the last), each +-1 term one FMA of u_r with
+    the last factor (a multiply for a sum's first term), terms with other coefficients sharing
+    one product u_r * last.  The FMAs re-multiply u_r * last per term, so the executed flops
+    exceed these by the products that the rate-once form shares.  W = I - dtg*J is formed from
+    partials of kd_r = -dtg*K_r, and the error norm takes dto6^2 out of its sum.  Checked
+    against ncu's DADD/DMUL/DFMA counts of the kernel (3-evaluation attempt of SuperFast in the
+    minimum-fill order: 1,049 instructions counted here, 1,010.5 measured)."""
     t = mech.tables()
     ns = mech.ns
 
@@ -188,11 +196,23 @@ def ros23_exec_counts(mech, order, evals, emissions=False):
         return i, f
 
     rp, rs, rn = t["react_ptr"], t["react_species"], t["react_nu"]
-    vel = int(sum(rn))
-    ri = rf = 0
+    nfac = [int(sum(rn[rp[r]:rp[r + 1]])) for r in range(len(rp) - 1)]
+    rf = int(sum(rn))  # the rate products
     for sp in range(ns):
-        a, b = terms(t["rhs_coef"][t["rhs_ptr"][sp]:t["rhs_ptr"][sp + 1]])
-        ri, rf = ri + a, rf + b
+        rf += terms(t["rhs_coef"][t["rhs_ptr"][sp]:t["rhs_ptr"][sp + 1]])[1]
+    ri = sum(max(n - 1, 0) for n in nfac)  # the heads
+    shared = set()  # reactions whose product u_r * last is formed once for non-unit terms
+    for sp in range(ns):
+        lo, hi = t["rhs_ptr"][sp], t["rhs_ptr"][sp + 1]
+        for k, (r, c) in enumerate(zip(t["rhs_reaction"][lo:hi], t["rhs_coef"][lo:hi])):
+            r = int(r)
+            if nfac[r] == 0:  # u_r is the rate itself
+                ri += terms([c])[0] if k == 0 else 1
+            else:
+                ri += 1
+                if abs(c) != 1.0:
+                    shared.add(r)
+    ri += len(shared)
     if emissions:
         ri, rf = ri + ns, rf + ns
     part = 0
@@ -200,19 +220,21 @@ def ros23_exec_counts(mech, order, evals, emissions=False):
         for e in range(rp[pr], rp[pr + 1]):
             nu = int(rn[e])
             part += nu if rs[e] != q else (nu if nu >= 2 else 0)
+    # W = I - dtg*J from partials of the scaled rate constants kd_r = -dtg*K_r: one multiply
+    # per reaction with partials, each entry its folded sum, plus 1 on the diagonal
     diag = set(int(x) for x in t["lu_diag"])
-    wi = wf = 0
+    wi = wf = len(set(int(r) for r in t["part_reaction"]))
     for e in range(t["n_jac"]):
         a, b = terms(t["jac_coef"][t["jac_ptr"][e]:t["jac_ptr"][e + 1]])
         d = int(t["jac_slot"][e]) in diag
-        wi, wf = wi + a + 1, wf + b + (2 if d else 1)
+        wi, wf = wi + a + d, wf + b + d
     _, n_mult, n_upd, n_low, n_up = mech.lu_counts(order)
     lu_i, lu_f = 4 * ns + n_mult + n_upd, 8 * ns + n_mult + 2 * n_upd
     sv_i, sv_f = n_low + n_up + ns, 2 * (n_low + n_up) + ns
-    stage_i, stage_f = 9 * ns, 12 * ns
-    norm_i, norm_f = 8 * ns, 13 * ns
-    inst = evals * (vel + ri) + part + wi + lu_i + 3 * sv_i + stage_i + norm_i
-    flops = evals * (vel + rf) + part + wf + lu_f + 3 * sv_f + stage_f + norm_f
+    stage_i, stage_f = 8 * ns, 12 * ns
+    norm_i, norm_f = 7 * ns + 2, 12 * ns + 2  # dto6^2 applied once to the sum
+    inst = evals * ri + part + wi + lu_i + 3 * sv_i + stage_i + norm_i
+    flops = evals * rf + part + wf + lu_f + 3 * sv_f + stage_f + norm_f
     return flops, inst
 
 
@@ -432,9 +454,9 @@ def run_gb300(args):
                     "bound": "fp64", "achieved": round(achieved, 4),
                     "peak": peak, "unit": "TFLOP/s", "frac": round(achieved / peak, 4) if peak else None,
                     # DRAM bytes per launch from one ncu capture of this kernel on this
-                    # workload (dram__bytes_read.sum + dram__bytes_write.sum: 296.8 MB + 996.1 MB,
+                    # workload (dram__bytes_read.sum + dram__bytes_write.sum: 303.6 MB + 1050.6 MB,
                     # mostly the 128-register variant's spill stores); null for other kernels
-                    "traffic": (1292.9e6 if (kinfo.get("kind") == "specialized" and not args.small
+                    "traffic": (1354.2e6 if (kinfo.get("kind") == "specialized" and not args.small
                                              and kinfo.get("variant") == "regs2") else None),
                     "traffic_source": "ncu capture summarised in profiles/rs_jit_attempt_c2_144x91x47.md",
                     "flops_per_cell_attempt": round(f_exec, 1),

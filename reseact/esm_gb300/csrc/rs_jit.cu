@@ -141,11 +141,65 @@ struct Gen {
         << ") : a_; }\n";
     }
   }
-  void partials(const char* xa = "x", const char* Pa = "P") {
+  // f = RHS at state x.  Strict build: the rates v_r, then each species' sum of c * v_r (the
+  // oracle's order).  Production build: per reaction the head u_r = K_r * (all factors but
+  // the last) once, and each term as one FMA of u_r with the last factor into the species'
+  // sum -- one instruction fewer per reaction than a rate product followed by adds.
+  void rates_rhs(const char* x, const char* f) {
+    if (strict) {
+      vel(x);
+      rhs(f);
+      return;
+    }
+    o << "  {\n";  // the heads are local to this evaluation
+    std::vector<std::string> last(T.nr);
+    for (int r = 0; r < T.nr; ++r) {
+      std::vector<int> fac;
+      for (int q = T.rptr[r]; q < T.rptr[r + 1]; ++q)
+        for (int t = 0; t < T.rnu[q]; ++t) fac.push_back(T.rsp[q]);
+      std::ostringstream h;
+      h << "K(" << r << ")";
+      for (size_t i = 0; i + 1 < fac.size(); ++i) h << "*" << x << "[" << fac[i] << "]";
+      o << "  const double u" << r << "_ = " << h.str() << ";\n";
+      last[r] = fac.empty() ? std::string() : std::string(x) + "[" + std::to_string(fac.back()) + "]";
+    }
+    for (int sp = 0; sp < T.ns; ++sp) {
+      std::string acc;
+      for (int t = T.rhs_ptr[sp]; t < T.rhs_ptr[sp + 1]; ++t) {
+        const int r = T.rhs_r[t];
+        const double cf = T.rhs_c[t];
+        const std::string u = "u" + std::to_string(r) + "_";
+        std::string term;  // the product c * v_r, for a first term
+        if (last[r].empty()) term = cf == 1.0 ? u : (cf == -1.0 ? "(-" + u + ")" : lit(cf) + "*" + u);
+        else if (cf == 1.0) term = u + "*" + last[r];
+        else if (cf == -1.0) term = "(-" + u + ")*" + last[r];
+        else term = lit(cf) + "*(" + u + "*" + last[r] + ")";
+        if (acc.empty()) {
+          acc = term;
+        } else if (last[r].empty()) {
+          acc = cf == 1.0 ? acc + " + " + u : (cf == -1.0 ? acc + " - " + u : "RS_FMA(" + lit(cf) + ", " + u + ", " + acc + ")");
+        } else if (cf == 1.0) {
+          acc = "RS_FMA(" + u + ", " + last[r] + ", " + acc + ")";
+        } else if (cf == -1.0) {
+          acc = "RS_FMA(-" + u + ", " + last[r] + ", " + acc + ")";
+        } else {
+          acc = "RS_FMA(" + lit(cf) + ", " + u + "*" + last[r] + ", " + acc + ")";
+        }
+      }
+      if (acc.empty()) acc = "0.0";
+      o << "  { const double a_ = " << acc << "; " << f << "[" << sp << "] = HE ? a_ + EM(" << sp
+        << ") : a_; }\n";
+    }
+    o << "  }\n";
+  }
+  // Partial derivatives dv_r/dx_q of the rates at xa; `scaled` forms them from kd<r>_ =
+  // -dtg * K_r (declared by build_w_scaled) instead of K_r.
+  void partials(const char* xa = "x", const char* Pa = "P", bool scaled = false) {
     for (int p = 0; p < T.npart; ++p) {
       int r = T.part_r[p], qs = T.part_q[p];
       std::ostringstream d;
-      d << "K(" << r << ")";
+      if (scaled) d << "kd" << r << "_";
+      else d << "K(" << r << ")";
       for (int q = T.rptr[r]; q < T.rptr[r + 1]; ++q) {
         int s = T.rsp[q], nu = T.rnu[q];
         if (s == qs) {
@@ -176,6 +230,32 @@ struct Gen {
       w[T.jac_slot[e]] = T.jac_diag[e] ? "RS_FMA(-dtg, (" + a + "), 1.0)" : "-(dtg*(" + a + "))";
     }
     for (int e = 0; e < T.nlu; ++e) o << "  WV(" << e << ") = " << w[e] << ";\n";
+  }
+  // Production attempt: W = I - dtg*J with -dtg folded once into each reaction's rate
+  // constant (kd_r = -dtg * K_r) before the partials at x are formed, so each Jacobian entry of
+  // W is its plain sum of scaled partials (plus 1 on the diagonal): one multiply per reaction
+  // instead of one per entry.
+  void build_w_scaled() {
+    std::vector<char> used(T.nr, 0);
+    for (int p = 0; p < T.npart; ++p) used[T.part_r[p]] = 1;
+    o << "  {\n";
+    for (int r = 0; r < T.nr; ++r)
+      if (used[r]) o << "  const double kd" << r << "_ = -dtg * K(" << r << ");\n";
+    partials("x", "P", true);
+    std::vector<std::string> w(T.nlu, "0.0");
+    for (int i = 0; i < T.ns; ++i) w[T.lu_diag[i]] = "1.0";
+    for (int e = 0; e < T.njac; ++e) {
+      std::ostringstream acc;
+      bool first = true;
+      for (int t = T.jac_ptr[e]; t < T.jac_ptr[e + 1]; ++t) {
+        sum_terms(acc, first, T.jac_coef[t], "P[" + std::to_string(T.jac_part[t]) + "]");
+        first = false;
+      }
+      if (first) continue;
+      w[T.jac_slot[e]] = T.jac_diag[e] ? "1.0 + (" + acc.str() + ")" : acc.str();
+    }
+    for (int e = 0; e < T.nlu; ++e) o << "  WV(" << e << ") = " << w[e] << ";\n";
+    o << "  }\n";
   }
   void lu_factor() {
     int m = 0;
@@ -397,23 +477,24 @@ __device__ __forceinline__ double ros23_cell(const double* __restrict__ kr,
   double v[NRA], P[NPA], k1[NS], f1[NS], k2[NS], b[NS], pv[NS];
   if (!have_f0) {
 )";
-  g.vel("x");
-  g.rhs("f0");
+  g.rates_rhs("x", "f0");
   o << "  }\n";
-  g.partials();
-  g.build_w();
+  if (g.strict) {
+    g.partials();
+    g.build_w();
+  } else {
+    g.build_w_scaled();
+  }
   g.lu_factor();
   o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) k1[s] = f0[s];\n";
   g.lu_solve("k1");
   o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) xn[s] = RS_FMA(dto2, k1[s], x[s]);\n";
-  g.vel("xn");
-  g.rhs("f1");
+  g.rates_rhs("xn", "f1");
   o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) k2[s] = f1[s] - k1[s];\n";
   g.lu_solve("k2");
   o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) k2[s] = k2[s] + k1[s];\n";
   o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) xn[s] = RS_FMA(dt, k2[s], x[s]);\n";
-  g.vel("xn");
-  g.rhs("b");
+  g.rates_rhs("xn", "b");
   o << R"(  if (fout) {
     bool same = true;
 #pragma unroll
@@ -433,23 +514,24 @@ __device__ __forceinline__ double ros23_cell(const double* __restrict__ kr,
     for (int s = 0; s < NS; ++s) f2[s] = b[s];
   }
 #pragma unroll
-  for (int s = 0; s < NS; ++s) {
-    const double cc = 2.0 * (k1[s] - f0[s]);
-    b[s] = RS_FMA(-ROS_C32, (k2[s] - f1[s]), b[s]) - cc;
-  }
+  for (int s = 0; s < NS; ++s)  // y - 2d as fma(-2, d, y): exact doubling, one rounding either way
+    b[s] = RS_FMA(-2.0, k1[s] - f0[s], RS_FMA(-ROS_C32, (k2[s] - f1[s]), b[s]));
 )";
   g.lu_solve("b");
+  // error norm sum_s (dto6 * e_s / den_s)^2; the production build takes dto6^2 out of the sum
+  const char* ut = g.strict ? "dto6 * (RS_FMA(-2.0, k2[s], k1[s]) + b[s])" : "RS_FMA(-2.0, k2[s], k1[s]) + b[s]";
   o << R"(  double acc = 0.0;
 #pragma unroll
   for (int s = 0; s < NS; ++s) {
-    const double ut = dto6 * (RS_FMA(-2.0, k2[s], k1[s]) + b[s]);
+    const double ut = )" << ut << R"(;
     const double am = RS_AMAX(x[s], xn[s]);
     const double den = RS_FMA(am, rtol, atol);
     const double at = RS_NQUOT(ut, den);
     acc = RS_FMA(at, at, acc);
   }
-  return acc;
-#undef K
+)";
+  o << (g.strict ? "  return acc;\n" : "  return acc * (dto6 * dto6);\n");
+  o << R"(#undef K
 #undef EM
 #undef WV
 }
@@ -639,8 +721,7 @@ __device__ __forceinline__ void vjp_body(int nc, int nsp, const double* __restri
   for (int s = 0; s < NS; ++s) x[s] = U[(u64)s * N + c];
 )";
   o << "  {\n";
-  g.vel("x");
-  g.rhs("f0");
+  g.rates_rhs("x", "f0");
   o << "  }\n";
   g.partials("x", "P");
   g.build_w();
@@ -649,8 +730,7 @@ __device__ __forceinline__ void vjp_body(int nc, int nsp, const double* __restri
   g.lu_solve("k1");
   o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) u1[s] = RS_FMA(dto2, k1[s], x[s]);\n";
   o << "  {\n";
-  g.vel("u1");
-  g.rhs("f1");
+  g.rates_rhs("u1", "f1");
   o << "  }\n";
   g.partials("u1", "P1");
   o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) z2[s] = f1[s] - k1[s];\n";
