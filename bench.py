@@ -173,16 +173,17 @@ def ros23_exec_counts(mech, order, evals, emissions=False):
     reuses f(x).
 
     Flops are the algorithm's: each rate product once per reaction and one multiply-add per
-    stoichiometric term (+-1 coefficients folded into adds), FMA = 2; the LU with two Newton
-    steps per pivot reciprocal, the solves, the stage algebra and the error norm with one
-    Newton step per reciprocal.  Instructions follow the fused RHS the generator emits: per
+    stoichiometric term (+-1 coefficients folded into adds), FMA = 2; the LU with a
+    third-order refined reciprocal per pivot (three FMAs), the solves, the stage algebra and
+    the error norm with one Newton step per reciprocal.  Instructions follow the fused RHS the generator emits: per
     reaction one head u_r = K_r * (all factors but the last), each +-1 term one FMA of u_r with
     the last factor (a multiply for a sum's first term), terms with other coefficients sharing
     one product u_r * last.  The FMAs re-multiply u_r * last per term, so the executed flops
     exceed these by the products that the rate-once form shares.  W = I - dtg*J is formed from
     partials of kd_r = -dtg*K_r, and the error norm takes dto6^2 out of its sum.  Checked
     against ncu's DADD/DMUL/DFMA counts of the kernel (3-evaluation attempt of SuperFast in the
-    minimum-fill order: 1,049 instructions counted here, 1,010.5 measured)."""
+    minimum-fill order: 1,037 instructions counted here; ncu measures 1,010.5 with two Newton
+    steps per pivot, 1,049 counted for that form)."""
     t = mech.tables()
     ns = mech.ns
 
@@ -229,7 +230,7 @@ def ros23_exec_counts(mech, order, evals, emissions=False):
         d = int(t["jac_slot"][e]) in diag
         wi, wf = wi + a + d, wf + b + d
     _, n_mult, n_upd, n_low, n_up = mech.lu_counts(order)
-    lu_i, lu_f = 4 * ns + n_mult + n_upd, 8 * ns + n_mult + 2 * n_upd
+    lu_i, lu_f = 3 * ns + n_mult + n_upd, 6 * ns + n_mult + 2 * n_upd
     sv_i, sv_f = n_low + n_up + ns, 2 * (n_low + n_up) + ns
     stage_i, stage_f = 8 * ns, 12 * ns
     norm_i, norm_f = 7 * ns + 2, 12 * ns + 2  # dto6^2 applied once to the sum

@@ -200,16 +200,16 @@ __device__ __forceinline__ void lu_solve(const DevMech& M, const double* W, cons
   }
 }
 
-// Reciprocal by Newton-Raphson iteration r <- r + r (1 - d r) from the hardware approximation
-// (PTX rcp.approx.ftz.f64); each step squares the relative error, two steps reach ~1 ulp.
-// The production build uses it where d > 0 and normal (error-norm denominators >= atol).
+// Reciprocal from the hardware approximation r (PTX rcp.approx.ftz.f64) by one third-order
+// correction: with e = 1 - d r, 1/d = r / (1 - e) = r (1 + e + e^2 + ...), so r (1 + e + e^2)
+// leaves e^3 -- below an ulp for the approximation's |e| -- in three FMAs (two Newton steps
+// take four).  The production build uses it where d > 0 and normal (LU pivots, m, error-norm
+// denominators >= atol).
 __device__ __forceinline__ double rcp_nr(double d) {
   double r;
   asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(d));
-  double e = fma(-d, r, 1.0);
-  r = fma(r, e, r);
-  e = fma(-d, r, 1.0);
-  return fma(r, e, r);
+  const double e = fma(-d, r, 1.0);
+  return fma(r, fma(e, e, e), r);
 }
 
 // One Newton step (relative error ~1e-12 or better) and max(|a|, |b|) on the magnitude bits:

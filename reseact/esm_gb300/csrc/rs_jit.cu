@@ -386,17 +386,16 @@ struct PCA {
 };
 static_assert(sizeof(PCA) == 128, "PerCellArgs layout");
 
-// Reciprocal by Newton-Raphson iteration r <- r + r (1 - d r) from the hardware approximation
-// (PTX rcp.approx.ftz.f64); each step squares the relative error, two steps reach ~1 ulp.
-// Used by the production build in place of IEEE division; d > 0 and normal on every call site
-// (LU pivots 1 - dtgamma*J_ii, error-norm denominators >= atol).
+// Reciprocal from the hardware approximation r (PTX rcp.approx.ftz.f64) by one third-order
+// correction: with e = 1 - d r, 1/d = r / (1 - e) = r (1 + e + e^2 + ...), so r (1 + e + e^2)
+// leaves e^3 -- below an ulp for the approximation's |e| -- in three FMAs.  Used by the
+// production build in place of IEEE division; d > 0 and normal on every call site (LU pivots
+// 1 - dtgamma*J_ii, error-norm denominators >= atol).
 __device__ __forceinline__ double rcp_nr(double d) {
   double r;
   asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(d));
-  double e = fma(-d, r, 1.0);
-  r = fma(r, e, r);
-  e = fma(-d, r, 1.0);
-  return fma(r, e, r);
+  const double e = fma(-d, r, 1.0);
+  return fma(r, fma(e, e, e), r);
 }
 // one Newton step: relative error ~1e-12 or better -- enough for error-norm denominators, whose
 // only use is the step-size controller

@@ -1239,23 +1239,43 @@ __global__ void __launch_bounds__(kRedThreads) k_split_input(DevTransport<double
 struct CellGeo {
   double gx, gylo, gyhi;
 };
-// horizontal (DxM + DyM) and vertical (DzM) parts of the air-mass flux divergence
-__device__ __forceinline__ void div_parts(const DevTransport<double>& T, int i, int j, int k,
-                                          double g, const CellGeo& G, double& hz, double& vz) {
+// The six air-mass face fluxes of cell (i,j,k) at time factor g, zero through closed walls.
+struct MassFluxes {
+  double w, e, s, n, b, t;
+};
+__device__ __forceinline__ MassFluxes mass_fluxes(const DevTransport<double>& T, int i, int j,
+                                                  int k, double g) {
   const int nf = T.nlon + 1;
   const size_t ncol = (size_t)T.nlon * T.nlat, col = (size_t)j * T.nlon + i;
-  double mxw = g * T.mx[((size_t)k * T.nlat + j) * nf + i];
-  double mxe = g * T.mx[((size_t)k * T.nlat + j) * nf + i + 1];
-  double mys = (T.lat_bc != 1 && j == 0) ? 0.0
-             : g * T.my[((size_t)k * (T.nlat + 1) + j) * T.nlon + i];
-  double myn = (T.lat_bc != 1 && j + 1 == T.nlat) ? 0.0
-             : g * T.my[((size_t)k * (T.nlat + 1) + j + 1) * T.nlon + i];
-  double mzb = (k == 0) ? 0.0 : g * T.mz[(size_t)k * ncol + col];
-  double mzt = (k + 1 == T.nlev) ? 0.0 : g * T.mz[(size_t)(k + 1) * ncol + col];
-  double DxM = (mxe - mxw) * G.gx;
-  double DyM = myn * G.gyhi - mys * G.gylo;
+  MassFluxes F;
+  F.w = g * T.mx[((size_t)k * T.nlat + j) * nf + i];
+  F.e = g * T.mx[((size_t)k * T.nlat + j) * nf + i + 1];
+  F.s = (T.lat_bc != 1 && j == 0) ? 0.0 : g * T.my[((size_t)k * (T.nlat + 1) + j) * T.nlon + i];
+  F.n = (T.lat_bc != 1 && j + 1 == T.nlat) ? 0.0
+      : g * T.my[((size_t)k * (T.nlat + 1) + j + 1) * T.nlon + i];
+  F.b = (k == 0) ? 0.0 : g * T.mz[(size_t)k * ncol + col];
+  F.t = (k + 1 == T.nlev) ? 0.0 : g * T.mz[(size_t)(k + 1) * ncol + col];
+  return F;
+}
+// horizontal (DxM + DyM) and vertical (DzM) parts of the air-mass flux divergence
+__device__ __forceinline__ void div_parts(const MassFluxes& F, const CellGeo& G, double& hz,
+                                          double& vz) {
+  double DxM = (F.e - F.w) * G.gx;
+  double DyM = F.n * G.gyhi - F.s * G.gylo;
   hz = DxM + DyM;
-  vz = mzt - mzb;
+  vz = F.t - F.b;
+}
+__device__ __forceinline__ void div_parts(const DevTransport<double>& T, int i, int j, int k,
+                                          double g, const CellGeo& G, double& hz, double& vz) {
+  div_parts(mass_fluxes(T, i, j, k, g), G, hz, vz);
+}
+// Production form of a flux divergence, (e - w) gx + n gyhi - s gylo + (t - b), as one FMA
+// chain (five FP64 operations).  k_stage applies it to the air-mass fluxes and to every tracer's
+// fluxes alike, so a tracer whose fluxes equal the air-mass fluxes bit for bit (a uniform
+// field) still cancels exactly.
+__device__ __forceinline__ double div_chain(double w, double e, double s, double n, double b,
+                                            double t, const CellGeo& G) {
+  return fma(e - w, G.gx, fma(n, G.gyhi, fma(-s, G.gylo, t - b)));
 }
 __device__ __forceinline__ double div_m(const DevTransport<double>& T, int i, int j, int k,
                                         double g, const CellGeo& G) {
@@ -1329,10 +1349,22 @@ __global__ void __launch_bounds__(kRedThreads) k_stage(DevTransport<double> T,
     int j = (int)((c / T.nlon) % T.nlat);
     int k = (int)(c / ((size_t)T.nlon * T.nlat));
     CellGeo G{T.gx[j], T.gylo[j], T.gyhi[j]};
-    double hz, vz;  // the air-mass divergence, once per cell: tracers and the air-mass row
-    div_parts(T, i, j, k, g, G, hz, vz);
+    // the air-mass divergence, once per cell: tracers and the air-mass row
+    const MassFluxes F = mass_fluxes(T, i, j, k, g);
+#if RS_STRICT
+    double hz, vz;
+    div_parts(F, G, hz, vz);
     const double divM = hz + vz;
     const double dmdt = T.mcorr ? -((hz + T.mcorr[c]) + vz) : -(hz + vz);  // = dm_dt(...)
+#else
+    const double divM = div_chain(F.w, F.e, F.s, F.n, F.b, F.t, G);  // the tracers' own chain
+    double dmdt = -divM;
+    if (T.mcorr) {  // the pressure fixer's -((divh + corr) + DzM)
+      double hz, vz;
+      div_parts(F, G, hz, vz);
+      dmdt = -((hz + T.mcorr[c]) + vz);
+    }
+#endif
     double m = Qin[(size_t)(T.nsp - 1) * nc + c];
 #if !RS_STRICT
     double rm = rcp_nr(m);  // m > 0
@@ -1361,16 +1393,16 @@ __global__ void __launch_bounds__(kRedThreads) k_stage(DevTransport<double> T,
         double fw = T.fx[s * fxp + fxi], fe = T.fx[s * fxp + fxi + 1];
         double fs = T.fy[s * fyp + fyi], fn = T.fy[s * fyp + fyi + T.nlon];
         double fb = T.fz[s * fzp + fzi], ft = T.fz[s * fzp + fzi + ncol];
+#if RS_STRICT
         double Dx = (fe - fw) * G.gx;
         double Dy = fn * G.gyhi - fs * G.gylo;
         double Dz = ft - fb;
         double a = -((Dx + Dy) + Dz);
-#if RS_STRICT
         double b = q * divM;
         du = (a + b) / m;
         if (T.pbl) du = du + pbl_term(T, c, col, s, q);
 #else
-        const double ab = fma(q, divM, a);
+        const double ab = fma(q, divM, -div_chain(fw, fe, fs, fn, fb, ft, G));
         if (T.pbl) {
           du = fma(ab, rm, pbl_term(T, c, col, s, q));
         } else {
@@ -1402,22 +1434,31 @@ __global__ void __launch_bounds__(kRedThreads) k_stage(DevTransport<double> T,
       } else {
         double u0 = U[x];
         double u3 = B.S1[x];
-        double ut = (1.0 / 3.0) * u0 + (2.0 / 3.0) * u3;
         double un = nx;
-        double err = 0.5 * (ut - un);
 #if RS_STRICT
+        double ut = (1.0 / 3.0) * u0 + (2.0 / 3.0) * u3;
+        double err = 0.5 * (ut - un);
         double am = fmax(fabs(u0), fabs(un));
         double den = am * rtol + atol;
         double at = err / den;
-#else
-        double den = fma(amax_bits(u0, un), rtol, atol);
-        double at = err * rcp_nr1(den);  // den >= atol > 0
-#endif
         e = e + at * at;
         Un[x] = clamp ? fmax(un, 0.0) : un;
+#else
+        // (1/3 u0 + 2/3 u3) - un in two FMAs; the factor 1/2 of the error goes onto the
+        // cell's sum as an exact 1/4
+        const double err = fma(2.0 / 3.0, u3, fma(1.0 / 3.0, u0, -un));
+        const double den = fma(amax_bits(u0, un), rtol, atol);
+        const double at = err * rcp_nr1(den);  // den >= atol > 0
+        e = fma(at, at, e);
+        // clamp at 0 on the sign bit (integer pipe); a NaN candidate fails the norm anyway
+        Un[x] = (clamp && __double2hiint(un) < 0) ? 0.0 : un;
+#endif
       }
     }
   }
+#if !RS_STRICT
+  if (STAGE == 4) e = 0.25 * e;
+#endif
   if (STAGE == 4) {
     double tot = block_tree256(e, sm);
     if (threadIdx.x == 0) B.partial[blockIdx.x] = tot;
