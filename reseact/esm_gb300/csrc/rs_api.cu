@@ -1681,9 +1681,9 @@ extern "C" rs_status rs_set_launch_shape(rs_handle* h, const char* key, int32_t 
     auto& t = h->tune;
     const int ntr = std::max(1, h->dt.ntr);
     bool ok = true;
-    if (k == "xthreads") ok = in({64, 128, 256}) && (t.xthreads = value, true);
-    else if (k == "pencil") ok = in({16, 32}) && (t.pencil = value, true);
-    else if (k == "rows") ok = in({4, 8, 16}) && (t.rows = value, true);
+    if (k == "xthreads") ok = in({64, 96, 128, 160, 192, 224, 256}) && (t.xthreads = value, true);
+    else if (k == "pencil") ok = in({8, 16, 32}) && (t.pencil = value, true);
+    else if (k == "rows") ok = in({4, 8, 16, 32}) && (t.rows = value, true);
     else if (k == "mixed_xthreads") ok = in({64, 128, 256}) && (t.mxthreads = value, true);
     else if (k == "mixed_x_tracers") ok = value >= 1 && value <= ntr && (t.msper_x = value, true);
     else if (k == "mixed_pencil") ok = in({16, 32}) && (t.mpencil = value, true);
@@ -2074,7 +2074,11 @@ extern "C" rs_status rs_autotune(rs_handle* h, char* buf, size_t buf_len) {
       float bx = 1e30f;
       rep += std::string(rep.size() > 1 ? ", " : "") + "\"lon_rows\": [";
       bool first = true;
-      for (int xt : {64, 128, 256}) {
+      // the row (n + 6 cells) in one pass of whole warps, and the fixed sizes around it
+      const int fit = (h->nlon + 6 + 31) / 32 * 32;
+      std::vector<int> xts{64, 128, 256};
+      if (fit > 128 && fit < 256) xts.push_back(fit);
+      for (int xt : xts) {
         T.xthreads = xt;
         float ms = time_min(h->st, 3, [&] { rs::launch_flux_dir(h->st, T, Q, 0); });
         std::snprintf(line, sizeof line, "%s{\"threads\": %d, \"ms\": %.4f}", first ? "" : ", ", xt, ms);
@@ -2089,8 +2093,9 @@ extern "C" rs_status rs_autotune(rs_handle* h, char* buf, size_t buf_len) {
       first = true;
       float byz = 1e30f;
       T.xthreads = h->tune.xthreads;
-      for (int pw : {16, 32})
-        for (int rows : {4, 8, 16}) {
+      for (int pw : {8, 16, 32})
+        for (int rows : {4, 8, 16, 32}) {
+          if (pw * rows < 64 || pw * rows > 512) continue;
           T.pencil = pw;
           T.rows = rows;
           float ms = time_min(h->st, 3, [&] {

@@ -1516,8 +1516,10 @@ static void allow_big_smem() {
   if (done) return;
   const int cap = kPencilSmemCap;
   cudaFuncSetAttribute(k_flux_x_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_flux_y_fused<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
   cudaFuncSetAttribute(k_flux_y_fused<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
   cudaFuncSetAttribute(k_flux_y_fused<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_flux_z_fused<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
   cudaFuncSetAttribute(k_flux_z_fused<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
   cudaFuncSetAttribute(k_flux_z_fused<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
   cudaFuncSetAttribute(k_flux_x_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
@@ -1534,8 +1536,10 @@ static void allow_big_smem() {
 }
 
 // Launch shape of the fused pencil kernels: V, Dd, D, E rows (n+6 each) plus the n+1 face fluxes,
-// per pencil.  The tuned pencil width drops to 16 where 32 does not fit; a direction whose
-// pencils do not fit even at 16 uses the per-face FP64 kernel (the same fluxes, bit for bit).
+// per pencil.  Lat / vertical blocks are (pencil width 8, 16 or 32) x rows threads, at most 512;
+// the tuned width drops to 16 where 32 does not fit; a direction whose pencils do not fit even
+// at 16 uses the per-face FP64 kernel (the same fluxes, bit for bit).  Lon rows take 64..256
+// threads in steps of 32.
 struct FluxShape {
   int pw, rows, xt;
   size_t shx, shy, shz;
@@ -1544,12 +1548,13 @@ struct FluxShape {
 static size_t pencil_bytes(int n, int pw) { return (size_t)(4 * (n + 6) + (n + 1)) * pw * sizeof(double); }
 static FluxShape flux_shape(const DevTransport<double>& T) {
   FluxShape f;
-  f.pw = T.pencil == 16 ? 16 : 32;
-  if (pencil_bytes(T.nlat, f.pw) > (size_t)kPencilSmemCap ||
-      pencil_bytes(T.nlev, f.pw) > (size_t)kPencilSmemCap)
+  f.pw = (T.pencil == 8 || T.pencil == 16) ? T.pencil : 32;
+  if (f.pw == 32 && (pencil_bytes(T.nlat, f.pw) > (size_t)kPencilSmemCap ||
+                     pencil_bytes(T.nlev, f.pw) > (size_t)kPencilSmemCap))
     f.pw = 16;
-  f.rows = (T.rows == 4 || T.rows == 16) ? T.rows : 8;
-  f.xt = (T.xthreads == 64 || T.xthreads == 256) ? T.xthreads : 128;
+  f.rows = (T.rows == 4 || T.rows == 16 || T.rows == 32) ? T.rows : 8;
+  if (f.pw * f.rows > 512) f.rows = 512 / f.pw;
+  f.xt = (T.xthreads >= 64 && T.xthreads <= 256 && T.xthreads % 32 == 0) ? T.xthreads : 128;
   f.shx = pencil_bytes(T.nlon, 1);
   f.shy = pencil_bytes(T.nlat, f.pw);
   f.shz = pencil_bytes(T.nlev, f.pw);
@@ -1572,7 +1577,9 @@ static void launch_flux_one(cudaStream_t st, const DevTransport<double>& T, cons
   } else if (dir == 1) {
     if (f.fy) {
       unsigned ntile = (unsigned)((T.nlon + f.pw - 1) / f.pw);
-      if (f.pw == 16)
+      if (f.pw == 8)
+        k_flux_y_fused<8><<<ntile * (unsigned)T.nlev, dim3(8, f.rows), f.shy, st>>>(T, sel);
+      else if (f.pw == 16)
         k_flux_y_fused<16><<<ntile * (unsigned)T.nlev, dim3(16, f.rows), f.shy, st>>>(T, sel);
       else
         k_flux_y_fused<32><<<ntile * (unsigned)T.nlev, dim3(32, f.rows), f.shy, st>>>(T, sel);
@@ -1583,7 +1590,8 @@ static void launch_flux_one(cudaStream_t st, const DevTransport<double>& T, cons
   } else {
     if (f.fz) {
       unsigned nzb = (unsigned)((ncol + f.pw - 1) / f.pw);
-      if (f.pw == 16) k_flux_z_fused<16><<<nzb, dim3(16, f.rows), f.shz, st>>>(T, sel);
+      if (f.pw == 8) k_flux_z_fused<8><<<nzb, dim3(8, f.rows), f.shz, st>>>(T, sel);
+      else if (f.pw == 16) k_flux_z_fused<16><<<nzb, dim3(16, f.rows), f.shz, st>>>(T, sel);
       else k_flux_z_fused<32><<<nzb, dim3(32, f.rows), f.shz, st>>>(T, sel);
     } else {
       long long nz = (long long)T.nlon * T.nlat * (T.nlev + 1);

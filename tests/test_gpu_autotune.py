@@ -25,7 +25,28 @@ def test_autotune_transport_is_bitwise_neutral():
     w = workloads.c2(nlon=48, nlat=31, nlev=16)
     ref, _ = _run(w, False)
     got, rep = _run(w, True)
-    assert "transport_choice" in rep and len(rep["pencils"]) == 6
+    # pencil widths 8 / 16 / 32 x rows 4..32 with 64..512 threads per block
+    assert "transport_choice" in rep and len(rep["pencils"]) == 10
+    assert np.array_equal(ref, got)
+
+
+@pytest.mark.parametrize("shape", [dict(pencil=8, rows=8), dict(pencil=8, rows=32),
+                                   dict(pencil=16, rows=32), dict(xthreads=96),
+                                   dict(xthreads=160), dict(xthreads=192)])
+def test_transport_launch_shapes_are_bitwise_neutral(shape):
+    """Every FP64 pencil shape (lat/vertical pencil width x rows, threads per lon row) gives
+    the same state bit for bit after adaptive macro steps."""
+    w = workloads.c2(nlon=48, nlat=31, nlev=16)
+    ref, _ = _run(w, False)
+    s = Solver.for_workload(w)
+    s.set_launch_shape(**shape)
+    s.set_state(w.u0_cellmajor())
+    t, a, b = 0.0, w.dt0_T, w.dt0_C
+    for _ in range(2):
+        _, a, b, _ = s.macro_step(t, t + w.dt_macro, a, b)
+        t += w.dt_macro
+    got = s.get_state()
+    s.close()
     assert np.array_equal(ref, got)
 
 
