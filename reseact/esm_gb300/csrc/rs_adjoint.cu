@@ -720,16 +720,27 @@ __global__ void __launch_bounds__(256) k_adj_pencil(DevTransport<double> T,
       for (int o = 0; o < 5; ++o) out[o * cstr] = Fb * M * w[o];
     }
     __syncthreads();
-    // 5. gather (faces ascending, positions ascending; periodic seam windows as before).  A cell
-    //    at least 3 positions from either end is reached only by faces pos-2 .. pos+3, each
-    //    through exactly one in-range stencil position: the same faces in the same order.
+    // 5. gather (faces ascending, positions ascending; periodic seam windows as before).  The
+    //    stencil positions that map to cell pos are pos itself and, on a periodic seam, its
+    //    images pos -+ n (open walls map ghosts to the boundary values, not to cells).  Face f
+    //    covers positions f-3 .. f+2, so each image p is reached only by faces p-2 .. p+3; for
+    //    n >= 6 these face ranges are disjoint and ascending with the images, and each face
+    //    reaches pos through exactly one position -- the same faces in the same order as the
+    //    general loop below, without its divergent window scan at the row ends.  Mirror walls
+    //    (a face can reach a cell next to the wall twice) and short pencils take that loop.
     for (int pos = lane0; pos < n; pos += lstride) {
       if (!live) break;
-      if (pos >= 3 && pos <= n - 4) {
+      const bool end = pos < 3 || pos > n - 4;
+      if (!end || (bc != 2 && n >= 6)) {
+        const int nimg = (bc == 0 && end) ? 3 : 1;
         double acc = 0.0;
-        for (int f = pos - 2; f <= pos + 3; ++f) {
-          const int o = pos - AV(upf, f) + 2;
-          if (o >= 0 && o <= 4) acc = acc + AV(C, o * (n + 1) + f);
+        for (int m = 0; m < nimg; ++m) {
+          const int img = nimg == 3 ? pos + (m - 1) * n : pos;
+          const int fa = img - 2 < 0 ? 0 : img - 2, fb = img + 3 > n ? n : img + 3;
+          for (int f = fa; f <= fb; ++f) {
+            const int o = img - AV(upf, f) + 2;
+            if (o >= 0 && o <= 4) acc = acc + AV(C, o * (n + 1) + f);
+          }
         }
         ubar[(size_t)s * nc + cell(pos)] += acc;
         continue;
