@@ -1591,9 +1591,9 @@ rs_status rs_backward_macro_step(rs_handle* h, int32_t k) {
         rs::TransportBufs B{R[0], R[1], h->S1.p, h->S2.p, h->S3.p, h->partial.p};
         rs::launch_ssprk43_attempt(st, h->dt, c, B, h->cfg.rtol_T, h->cfg.atol_T, clamp);
       } else {
-        rs::launch_ros23_attempt(h->lc, c, R[0], R[1], h->krates.p,
-                                 h->have_emis ? h->emis.p : nullptr, h->partial.p,
-                                 h->cfg.rtol_C, h->cfg.atol_C, clamp);
+        rs::launch_ros23_step(h->lc, c, R[0], R[1], h->krates.p,
+                              h->have_emis ? h->emis.p : nullptr, h->partial.p,
+                              h->cfg.rtol_C, h->cfg.atol_C, clamp);
       }
       rs::launch_replay_accept(st, c);
       cur ^= 1;

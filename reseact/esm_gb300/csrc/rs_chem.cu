@@ -313,6 +313,15 @@ void launch_ros23_attempt(const LaunchCtx& L, const Ctl* ctl, double* U0, double
   if (L.size_class == 0) Small::attempt(L, ctl, U0, U1, kr, em, part, rtol, atol, clamp);
   else Large::attempt(L, ctl, U0, U1, kr, em, part, rtol, atol, clamp);
 }
+void launch_ros23_step(const LaunchCtx& L, const Ctl* ctl, double* U0, double* U1,
+                       const double* kr, const double* em, double* part, double rtol,
+                       double atol, int clamp) {
+  if (L.jit && L.jit->step[em ? 1 : 0]) {
+    jit_launch_step(*L.jit, L.stream, L.nc, L.nsp, ctl, U0, U1, kr, em, clamp);
+    return;
+  }
+  launch_ros23_attempt(L, ctl, U0, U1, kr, em, part, rtol, atol, clamp);
+}
 void launch_chem_rhs(const LaunchCtx& L, const double* U, const double* kr, const double* em,
                      double* dU) {
   if (L.size_class == 0) Small::rhs(L, U, kr, em, dU);

@@ -456,8 +456,10 @@ std::string generate(const MechTables& T, double ros_d, double ros_c32, bool str
   // else): a one-step reciprocal and an integer magnitude max in the production build.
   o << (strict ? "#define RS_QUOT(a, b) ((a) / (b))\n#define RS_FMA(a, b, c) ((a) * (b) + (c))\n"
                  "#define RS_NQUOT(a, b) ((a) / (b))\n#define RS_AMAX(a, b) fmax(fabs(a), fabs(b))\n"
+                 "#define RS_VDECL double v[NRA];  // the rates of the oracle-order RHS\n"
                : "#define RS_QUOT(a, b) ((a) * rcp_nr(b))\n#define RS_FMA(a, b, c) fma((a), (b), (c))\n"
-                 "#define RS_NQUOT(a, b) ((a) * rcp_nr1(b))\n#define RS_AMAX(a, b) amax_bits((a), (b))\n");
+                 "#define RS_NQUOT(a, b) ((a) * rcp_nr1(b))\n#define RS_AMAX(a, b) amax_bits((a), (b))\n"
+                 "#define RS_VDECL  // the fused RHS keeps no rate array\n");
   // One ROS23 attempt of one cell: xn (unclamped) and the cell's sum of squared scaled errors.
   // f0 = f(x) is computed here unless the caller already holds it (have_f0): after an
   // accepted attempt whose clamp left the state bit for bit unchanged, f(x_new) is exactly
@@ -465,7 +467,8 @@ std::string generate(const MechTables& T, double ros_d, double ros_c32, bool str
   // f2 when the clamp leaves xn unchanged and a NaN marker in plane 0 otherwise; with KEEP
   // the caller also gets f2 in registers.
   o << R"(
-template <bool HE, int WS, bool KEEP>
+// SOL: the step's solution only (a replay along recorded accepted steps needs no error norm)
+template <bool HE, int WS, bool KEEP, bool SOL = false>
 __device__ __forceinline__ double ros23_cell(const double* __restrict__ kr,
     const double* __restrict__ em, u64 N, int c, const double* x, double* xn, double* W,
     double* f0, bool have_f0, double* __restrict__ fout, int clamp, double* f2,
@@ -473,7 +476,8 @@ __device__ __forceinline__ double ros23_cell(const double* __restrict__ kr,
 #define K(r) __ldg(kr + (u64)(r) * N + c)
 #define EM(s) __ldg(em + (u64)(s) * N + c)
 #define WV(e) W[(e) * WS]
-  double v[NRA], P[NPA], k1[NS], f1[NS], k2[NS], b[NS], pv[NS];
+  RS_VDECL
+  double P[NPA], k1[NS], f1[NS], k2[NS], b[NS], pv[NS];
   if (!have_f0) {
 )";
   g.rates_rhs("x", "f0");
@@ -493,6 +497,7 @@ __device__ __forceinline__ double ros23_cell(const double* __restrict__ kr,
   g.lu_solve("k2");
   o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) k2[s] = k2[s] + k1[s];\n";
   o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) xn[s] = RS_FMA(dt, k2[s], x[s]);\n";
+  o << "  if constexpr (SOL) return 0.0;\n";
   g.rates_rhs("xn", "b");
   o << R"(  if (fout) {
     bool same = true;
@@ -686,6 +691,45 @@ RS_ATTEMPT(rs_jit_attempt_r0, false, false, 1)
 RS_ATTEMPT(rs_jit_attempt_r1, true, false, 1)
 RS_ATTEMPT(rs_jit_attempt_q0, false, false, 2)
 RS_ATTEMPT(rs_jit_attempt_q1, true, false, 2)
+
+// one accepted step at the controller's dtc without the error estimate: the attempt's own
+// arithmetic up to the new state (the same bits), for the fixed-sequence replay of a recorded
+// macro step
+template <bool HE>
+__device__ __forceinline__ void step_body(const unsigned char* __restrict__ ctl,
+    double* __restrict__ U0, double* __restrict__ U1, const double* __restrict__ kr,
+    const double* __restrict__ em, int nc, int nsp, int clamp) {
+  if (*(const int*)(ctl + OFF_DONE)) return;
+  const double dt = *(const double*)(ctl + OFF_DTC);
+  const double dto2 = *(const double*)(ctl + OFF_DTO2);
+  const double dtg = *(const double*)(ctl + OFF_DTG);
+  const int cur = *(const int*)(ctl + OFF_CUR);
+  const double* __restrict__ U = cur ? U1 : U0;
+  double* __restrict__ Un = cur ? U0 : U1;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  const u64 N = (u64)nc;
+  double x[NS], xn[NS], f0[NS], W[NLU];
+#pragma unroll
+  for (int s = 0; s < NS; ++s) x[s] = U[(u64)s * N + c];
+  ros23_cell<HE, 1, false, true>(kr, em, N, c, x, xn, W, f0, false, nullptr, clamp, nullptr,
+                                 dt, dto2, 0.0, dtg, 0.0, 0.0);
+#pragma unroll
+  for (int s = 0; s < NS; ++s) Un[(u64)s * N + c] = clamp ? fmax(xn[s], 0.0) : xn[s];
+  for (int s = NS; s < nsp; ++s) {
+    const double xv = U[(u64)s * N + c];
+    Un[(u64)s * N + c] = clamp ? fmax(xv, 0.0) : xv;
+  }
+}
+#define RS_STEP(NAME, HE)                                                                   \
+  extern "C" __global__ void __launch_bounds__(256, 2) NAME(                                \
+      const unsigned char* __restrict__ ctl, double* __restrict__ U0,                       \
+      double* __restrict__ U1, const double* __restrict__ kr,                               \
+      const double* __restrict__ em, int nc, int nsp, int clamp) {                          \
+    step_body<HE>(ctl, U0, U1, kr, em, nc, nsp, clamp);                                     \
+  }
+RS_STEP(rs_jit_step_0, false)
+RS_STEP(rs_jit_step_1, true)
 )";
   if (with_smem)
     o << "RS_ATTEMPT(rs_jit_attempt_s0, false, true, 1)\nRS_ATTEMPT(rs_jit_attempt_s1, true, true, 1)\n";
@@ -715,7 +759,8 @@ __device__ __forceinline__ void vjp_body(int nc, int nsp, const double* __restri
 #define EM(s) __ldg(em + (u64)(s) * N + c)
 #define WV(e) W[(e)]
   double x[NS], f0[NS], k1[NS], u1[NS], f1[NS], z2[NS], bb[NS], f0b[NS], f1b[NS], ub[NS], pv[NS];
-  double v[NRA], a0[NRA], a1[NRA], P[NPA], P1[NPA], W[NLU];
+  RS_VDECL
+  double a0[NRA], a1[NRA], P[NPA], P1[NPA], W[NLU];
 #pragma unroll
   for (int s = 0; s < NS; ++s) x[s] = U[(u64)s * N + c];
 )";
@@ -919,7 +964,8 @@ std::shared_ptr<JitChem> jit_chem_build(const MechTables& T, double ros_d, doubl
             get(&J->attempt[2][0], "rs_jit_attempt_q0") && get(&J->attempt[2][1], "rs_jit_attempt_q1") &&
             get(&J->per_cell[0], "rs_jit_per_cell_0") && get(&J->per_cell[1], "rs_jit_per_cell_1") &&
             get(&J->rcp, "rs_jit_rcp") && get(&J->vjp[0], "rs_jit_vjp_0") &&
-            get(&J->vjp[1], "rs_jit_vjp_1");
+            get(&J->vjp[1], "rs_jit_vjp_1") && get(&J->step[0], "rs_jit_step_0") &&
+            get(&J->step[1], "rs_jit_step_1");
   if (!ok) return nullptr;
   if (with_smem && get(&J->attempt[1][0], "rs_jit_attempt_s0") &&
       get(&J->attempt[1][1], "rs_jit_attempt_s1")) {
@@ -959,6 +1005,14 @@ void jit_launch_attempt(const JitChem& J, cudaStream_t st, int nc, int nsp, cons
   void* args[] = {&c, &U0, &U1, &kr, &em, &part, &nc, &nsp, &rtol, &atol, &clamp, &F0, &F1};
   int nb = (nc + kBlock - 1) / kBlock;
   cudaLaunchKernel((const void*)k, dim3(nb), dim3(kBlock), args, sm ? J.attempt_smem : 0, st);
+}
+
+void jit_launch_step(const JitChem& J, cudaStream_t st, int nc, int nsp, const Ctl* ctl,
+                     double* U0, double* U1, const double* kr, const double* em, int clamp) {
+  cudaKernel_t k = J.step[em ? 1 : 0];
+  const unsigned char* c = reinterpret_cast<const unsigned char*>(ctl);
+  void* args[] = {&c, &U0, &U1, &kr, &em, &nc, &nsp, &clamp};
+  cudaLaunchKernel((const void*)k, dim3((nc + kBlock - 1) / kBlock), dim3(kBlock), args, 0, st);
 }
 
 void jit_launch_rcp(const JitChem& J, cudaStream_t st, const double* x, double* r, int n) {

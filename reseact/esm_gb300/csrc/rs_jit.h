@@ -33,6 +33,7 @@ struct JitChem {
   cudaKernel_t per_cell[2] = {};               // [has emission]
   cudaKernel_t rcp = nullptr;                  // elementwise production reciprocal
   cudaKernel_t vjp[2] = {};                    // ROS23 step VJP [has emission]
+  cudaKernel_t step[2] = {};                   // accepted step, no error estimate [has emission]
   size_t attempt_smem = 0;  // dynamic shared bytes of the shared-memory variant
   int variant = 0;          // variant used for global-dt attempts
   double compile_ms = 0;    // NVRTC time (0 when the compiled image came from cache)
@@ -61,6 +62,9 @@ void jit_launch_attempt(const JitChem& J, cudaStream_t st, int nc, int nsp, cons
                         double* U0, double* U1, const double* kr, const double* em,
                         double* part, double rtol, double atol, int clamp, double* F0,
                         double* F1);
+// same contract as launch_ros23_step in rs_kernels.h
+void jit_launch_step(const JitChem& J, cudaStream_t st, int nc, int nsp, const Ctl* ctl,
+                     double* U0, double* U1, const double* kr, const double* em, int clamp);
 void jit_launch_rcp(const JitChem& J, cudaStream_t st, const double* x, double* r, int n);
 // same contract as launch_ros23_vjp in rs_kernels.h
 void jit_launch_vjp(const JitChem& J, cudaStream_t st, int nc, int nsp, const double* U,

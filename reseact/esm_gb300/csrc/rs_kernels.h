@@ -98,6 +98,12 @@ void launch_rates(const LaunchCtx& L, const double* T, const double* P, double* 
 void launch_ros23_attempt(const LaunchCtx& L, const Ctl* ctl, double* U0, double* U1,
                           const double* kr, const double* em, double* part, double rtol,
                           double atol, int clamp, double* F0 = nullptr, double* F1 = nullptr);
+// One step at the controller's dtc that is accepted whatever its error (the replay of a
+// recorded step): the specialised kernels skip the error estimate; the table kernels run the
+// full attempt (part: its block partials, unused).  Same new state as launch_ros23_attempt.
+void launch_ros23_step(const LaunchCtx& L, const Ctl* ctl, double* U0, double* U1,
+                       const double* kr, const double* em, double* part, double rtol,
+                       double atol, int clamp);
 void launch_chem_rhs(const LaunchCtx& L, const double* U, const double* kr, const double* em,
                      double* dU);
 void launch_block_jac(const LaunchCtx& L, const double* U, const double* kr, const int* srow,
