@@ -241,7 +241,8 @@ void* rs_stream(rs_handle* h);
 rs_status rs_autotune(rs_handle* h, char* buf, size_t buf_len);
 
 /* Set one launch shape that rs_autotune would choose, e.g. to replay an earlier tuning without
- * timing again (no reference counterpart).  Keys: "xthreads", "pencil", "rows" (FP64 pencils);
+ * timing again (no reference counterpart).  Keys: "xthreads", "pencil", "rows",
+ * "x_tracer_groups", "yz_tracer_groups" (FP64 pencils);
  * "mixed_xthreads", "mixed_x_tracers", "mixed_pencil", "mixed_rows", "mixed_yz_tracers",
  * "mixed_x_bulk", "mixed_yz_bulk" (mixed pencils); "per_cell_threads",
  * "per_cell_blocks_per_sm" (per-cell chemistry).  Values outside a key's candidates are

@@ -348,6 +348,7 @@ struct rs_handle {
   struct Tune {
     int pc_threads = 128, pc_blocks_per_sm = 4;      // per-cell chemistry kernel
     int pencil = 32, rows = 8, xthreads = 128;        // transport pencil kernels
+    int xgroups = 1, yzgroups = 1;                    // their tracer groups
     int mpencil = 16, mrows = 16, mxthreads = 128;    // mixed-precision pencil kernels
     int msper_x = 1 << 20, msper_yz = 1;             // tracers per block (clamped to ntr)
     int mbulk_x = 1, mbulk_yz = 1;                    // bulk-copy staging per direction
@@ -562,6 +563,8 @@ void refresh_dt(rs_handle* h) {
   T.pencil = h->tune.pencil;
   T.rows = h->tune.rows;
   T.xthreads = h->tune.xthreads;
+  T.xgroups = h->tune.xgroups;
+  T.yzgroups = h->tune.yzgroups;
   T.mpencil = h->tune.mpencil;
   T.mrows = h->tune.mrows;
   T.mxthreads = h->tune.mxthreads;
@@ -1684,6 +1687,8 @@ extern "C" rs_status rs_set_launch_shape(rs_handle* h, const char* key, int32_t 
     if (k == "xthreads") ok = in({64, 96, 128, 160, 192, 224, 256}) && (t.xthreads = value, true);
     else if (k == "pencil") ok = in({8, 16, 32}) && (t.pencil = value, true);
     else if (k == "rows") ok = in({4, 8, 16, 32}) && (t.rows = value, true);
+    else if (k == "x_tracer_groups") ok = value >= 1 && value <= ntr && (t.xgroups = value, true);
+    else if (k == "yz_tracer_groups") ok = value >= 1 && value <= ntr && (t.yzgroups = value, true);
     else if (k == "mixed_xthreads") ok = in({64, 128, 256}) && (t.mxthreads = value, true);
     else if (k == "mixed_x_tracers") ok = value >= 1 && value <= ntr && (t.msper_x = value, true);
     else if (k == "mixed_pencil") ok = in({16, 32}) && (t.mpencil = value, true);
@@ -2112,9 +2117,39 @@ extern "C" rs_status rs_autotune(rs_handle* h, char* buf, size_t buf_len) {
             h->tune.rows = rows;
           }
         }
+      T.pencil = h->tune.pencil;
+      T.rows = h->tune.rows;
+      // tracer groups per launch (grid y): more, shorter blocks fill the last wave of the grid
+      auto sweep_groups = [&](const char* key, int& best_g, int& Tg, std::function<void()> run) {
+        rep += std::string("], \"") + key + "\": [";
+        bool first_g = true;
+        float bg = 1e30f;
+        for (int gsz : {1, 2, 3, 4, 6}) {
+          if (gsz > std::max(1, h->dt.ntr)) continue;
+          Tg = gsz;
+          float ms = time_min(h->st, 3, run);
+          std::snprintf(line, sizeof line, "%s{\"groups\": %d, \"ms\": %.4f}",
+                        first_g ? "" : ", ", gsz, ms);
+          rep += line;
+          first_g = false;
+          if (ms < bg) {
+            bg = ms;
+            best_g = gsz;
+          }
+        }
+        Tg = best_g;
+      };
+      sweep_groups("x_tracer_groups", h->tune.xgroups, T.xgroups,
+                   [&] { rs::launch_flux_dir(h->st, T, Q, 0); });
+      sweep_groups("yz_tracer_groups", h->tune.yzgroups, T.yzgroups, [&] {
+        rs::launch_flux_dir(h->st, T, Q, 1);
+        rs::launch_flux_dir(h->st, T, Q, 2);
+      });
       std::snprintf(line, sizeof line,
-                    "], \"transport_choice\": {\"xthreads\": %d, \"pencil\": %d, \"rows\": %d}",
-                    h->tune.xthreads, h->tune.pencil, h->tune.rows);
+                    "], \"transport_choice\": {\"xthreads\": %d, \"pencil\": %d, \"rows\": %d, "
+                    "\"x_tracer_groups\": %d, \"yz_tracer_groups\": %d}",
+                    h->tune.xthreads, h->tune.pencil, h->tune.rows, h->tune.xgroups,
+                    h->tune.yzgroups);
       rep += line;
       if (h->cfg.precision == RS_PREC_MIXED) {
         // the FP32 deviation-form pencils: threads per lon row and tracers per block for x,

@@ -78,9 +78,10 @@ struct DevTransport {
   // dm/dt = -(((DxM + DyM) + mcorr) + DzM); null when off
   const double* mcorr;     // [nlev][nlat][nlon]
   // launch shape of the FP64 pencil flux kernels (chosen by rs_autotune)
-  int pencil;    // pencils per block in the lat / vertical kernels: 16 or 32
-  int rows;      // threads along the pencil (blockDim.y): 4, 8 or 16
-  int xthreads;  // threads per lon row: 64, 128 or 256
+  int pencil;    // pencils per block in the lat / vertical kernels: 8, 16 or 32
+  int rows;      // threads along the pencil (blockDim.y): 4 .. 32
+  int xthreads;  // threads per lon row: 64 .. 256 in steps of 32
+  int xgroups, yzgroups;  // tracer groups (blockIdx.y) of the lon / lat and vertical pencils
   // launch shape of the mixed-precision pencil kernels (chosen by rs_autotune)
   int mpencil, mrows, mxthreads;
   int msper_x, msper_yz;  // tracers per block (blockIdx.y selects the group)

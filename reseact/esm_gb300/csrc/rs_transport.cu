@@ -505,7 +505,9 @@ __global__ void __launch_bounds__(256) k_flux_x_fused(DevTransport<double> T, St
   const size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
   const size_t rbase = ((size_t)k * T.nlat + j) * n;
   for (int f = threadIdx.x; f <= n; f += blockDim.x) Mf[f] = g * T.mx[((size_t)k * T.nlat + j) * nf + f];
-  for (int s = 0; s < T.ntr; ++s) {
+  const int s0 = (int)((long long)blockIdx.y * T.ntr / gridDim.y);  // this block's tracers
+  const int s1 = (int)((long long)(blockIdx.y + 1) * T.ntr / gridDim.y);
+  for (int s = s0; s < s1; ++s) {
     const double* q = Q + (size_t)s * nc + rbase;
     auto val = [&](int p) -> double {
       if (p < 0 || p >= n) {
@@ -563,7 +565,9 @@ __global__ void __launch_bounds__(512) k_flux_y_fused(DevTransport<double> T, St
     for (int f = ty; f <= n; f += blockDim.y)
       Mf[f * kPencil + tx] = g * T.my[((size_t)k * nfj + f) * T.nlon + i];
 #define RS_P(a, p) a[((p) + 3) * kPencil + tx]
-  for (int s = 0; s < T.ntr; ++s) {
+  const int s0 = (int)((long long)blockIdx.y * T.ntr / gridDim.y);  // this block's tracers
+  const int s1 = (int)((long long)(blockIdx.y + 1) * T.ntr / gridDim.y);
+  for (int s = s0; s < s1; ++s) {
     const double* q = Q + (size_t)s * nc + (size_t)k * T.nlat * T.nlon;
     auto val = [&](int p) -> double {
       if (!live) return 0.0;
@@ -625,7 +629,9 @@ __global__ void __launch_bounds__(512) k_flux_z_fused(DevTransport<double> T, St
   const size_t fplane = ncol * (n + 1);
   if (live)
     for (int kf = ty; kf <= n; kf += blockDim.y) Mf[kf * kPencil + tx] = g * T.mz[(size_t)kf * ncol + col];
-  for (int s = 0; s < T.ntr; ++s) {
+  const int s0 = (int)((long long)blockIdx.y * T.ntr / gridDim.y);  // this block's tracers
+  const int s1 = (int)((long long)(blockIdx.y + 1) * T.ntr / gridDim.y);
+  for (int s = s0; s < s1; ++s) {
     const double* q = Q + (size_t)s * nc;
     auto val = [&](int p) -> double {
       const int pp = p < 0 ? -1 - p : (p >= n ? 2 * n - 1 - p : p);
@@ -1542,6 +1548,7 @@ static void allow_big_smem() {
 // threads in steps of 32.
 struct FluxShape {
   int pw, rows, xt;
+  int gx, gyz;  // tracer groups (grid y) of the lon and of the lat / vertical pencils
   size_t shx, shy, shz;
   bool fx, fy, fz;  // fused kernel used for x / y / z
 };
@@ -1555,6 +1562,9 @@ static FluxShape flux_shape(const DevTransport<double>& T) {
   f.rows = (T.rows == 4 || T.rows == 16 || T.rows == 32) ? T.rows : 8;
   if (f.pw * f.rows > 512) f.rows = 512 / f.pw;
   f.xt = (T.xthreads >= 64 && T.xthreads <= 256 && T.xthreads % 32 == 0) ? T.xthreads : 128;
+  const int ntr = T.ntr > 0 ? T.ntr : 1;
+  f.gx = T.xgroups < 1 ? 1 : (T.xgroups > ntr ? ntr : T.xgroups);
+  f.gyz = T.yzgroups < 1 ? 1 : (T.yzgroups > ntr ? ntr : T.yzgroups);
   f.shx = pencil_bytes(T.nlon, 1);
   f.shy = pencil_bytes(T.nlat, f.pw);
   f.shz = pencil_bytes(T.nlev, f.pw);
@@ -1569,7 +1579,7 @@ static void launch_flux_one(cudaStream_t st, const DevTransport<double>& T, cons
   size_t ncol = (size_t)T.nlon * T.nlat;
   if (dir == 0) {
     if (f.fx) {
-      k_flux_x_fused<<<(unsigned)(T.nlat * T.nlev), f.xt, f.shx, st>>>(T, sel);
+      k_flux_x_fused<<<dim3((unsigned)(T.nlat * T.nlev), (unsigned)f.gx), f.xt, f.shx, st>>>(T, sel);
     } else {
       long long nx = (long long)(T.nlon + 1) * T.nlat * T.nlev;
       k_flux_x<<<(unsigned)((nx + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);
@@ -1577,22 +1587,20 @@ static void launch_flux_one(cudaStream_t st, const DevTransport<double>& T, cons
   } else if (dir == 1) {
     if (f.fy) {
       unsigned ntile = (unsigned)((T.nlon + f.pw - 1) / f.pw);
-      if (f.pw == 8)
-        k_flux_y_fused<8><<<ntile * (unsigned)T.nlev, dim3(8, f.rows), f.shy, st>>>(T, sel);
-      else if (f.pw == 16)
-        k_flux_y_fused<16><<<ntile * (unsigned)T.nlev, dim3(16, f.rows), f.shy, st>>>(T, sel);
-      else
-        k_flux_y_fused<32><<<ntile * (unsigned)T.nlev, dim3(32, f.rows), f.shy, st>>>(T, sel);
+      const dim3 grid(ntile * (unsigned)T.nlev, (unsigned)f.gyz);
+      if (f.pw == 8) k_flux_y_fused<8><<<grid, dim3(8, f.rows), f.shy, st>>>(T, sel);
+      else if (f.pw == 16) k_flux_y_fused<16><<<grid, dim3(16, f.rows), f.shy, st>>>(T, sel);
+      else k_flux_y_fused<32><<<grid, dim3(32, f.rows), f.shy, st>>>(T, sel);
     } else {
       long long ny = (long long)T.nlon * (T.nlat + 1) * T.nlev;
       k_flux_y<<<(unsigned)((ny + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);
     }
   } else {
     if (f.fz) {
-      unsigned nzb = (unsigned)((ncol + f.pw - 1) / f.pw);
-      if (f.pw == 8) k_flux_z_fused<8><<<nzb, dim3(8, f.rows), f.shz, st>>>(T, sel);
-      else if (f.pw == 16) k_flux_z_fused<16><<<nzb, dim3(16, f.rows), f.shz, st>>>(T, sel);
-      else k_flux_z_fused<32><<<nzb, dim3(32, f.rows), f.shz, st>>>(T, sel);
+      const dim3 grid((unsigned)((ncol + f.pw - 1) / f.pw), (unsigned)f.gyz);
+      if (f.pw == 8) k_flux_z_fused<8><<<grid, dim3(8, f.rows), f.shz, st>>>(T, sel);
+      else if (f.pw == 16) k_flux_z_fused<16><<<grid, dim3(16, f.rows), f.shz, st>>>(T, sel);
+      else k_flux_z_fused<32><<<grid, dim3(32, f.rows), f.shz, st>>>(T, sel);
     } else {
       long long nz = (long long)T.nlon * T.nlat * (T.nlev + 1);
       k_flux_z<<<(unsigned)((nz + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);

@@ -32,10 +32,13 @@ def test_autotune_transport_is_bitwise_neutral():
 
 @pytest.mark.parametrize("shape", [dict(pencil=8, rows=8), dict(pencil=8, rows=32),
                                    dict(pencil=16, rows=32), dict(xthreads=96),
-                                   dict(xthreads=160), dict(xthreads=192)])
+                                   dict(xthreads=160), dict(xthreads=192),
+                                   dict(x_tracer_groups=3, yz_tracer_groups=4),
+                                   dict(x_tracer_groups=5, yz_tracer_groups=2, pencil=8)])
 def test_transport_launch_shapes_are_bitwise_neutral(shape):
-    """Every FP64 pencil shape (lat/vertical pencil width x rows, threads per lon row) gives
-    the same state bit for bit after adaptive macro steps."""
+    """Every FP64 pencil shape (lat/vertical pencil width x rows, threads per lon row, tracer
+    groups per launch, including uneven groups) gives the same state bit for bit after
+    adaptive macro steps."""
     w = workloads.c2(nlon=48, nlat=31, nlev=16)
     ref, _ = _run(w, False)
     s = Solver.for_workload(w)
