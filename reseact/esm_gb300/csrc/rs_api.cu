@@ -2124,7 +2124,7 @@ extern "C" rs_status rs_autotune(rs_handle* h, char* buf, size_t buf_len) {
         rep += std::string("], \"") + key + "\": [";
         bool first_g = true;
         float bg = 1e30f;
-        for (int gsz : {1, 2, 3, 4, 6}) {
+        for (int gsz : {1, 2, 3, 4, 6, 8, 12}) {
           if (gsz > std::max(1, h->dt.ntr)) continue;
           Tg = gsz;
           float ms = time_min(h->st, 3, run);
