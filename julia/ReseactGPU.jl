@@ -264,7 +264,8 @@ function autotune!(h::Handle)
                    h.ptr, buf, length(buf)))
     return unsafe_string(pointer(buf))
 end
-# replay launch shapes reported by an earlier autotune!, e.g. set_launch_shape!(h; mixed_yz_tracers=2)
+# replay launch shapes reported by an earlier autotune!, e.g.
+# set_launch_shape!(h; xthreads=160, pencil=8, rows=32, yz_tracer_groups=6)
 function set_launch_shape!(h::Handle; shapes...)
     for (k, v) in shapes
         check(h, ccall((:rs_set_launch_shape, LIB[]), Int32, (Ptr{Cvoid}, Cstring, Int32),
