@@ -209,6 +209,11 @@ end
 record!(h::Handle, on::Bool) =
     check(h, ccall((:rs_record, LIB[]), Int32, (Ptr{Cvoid}, Int32), h.ptr, Int32(on)))
 record_count(h::Handle) = Int(ccall((:rs_record_count, LIB[]), Int32, (Ptr{Cvoid},), h.ptr))
+# device tape of the next recording: bytes, -1 = a quarter of free device memory, 0 = replay only
+set_adjoint_tape!(h::Handle, budget_bytes::Integer) =
+    check(h, ccall((:rs_set_adjoint_tape, LIB[]), Int32, (Ptr{Cvoid}, Int64), h.ptr,
+                   Int64(budget_bytes)))
+record_taped(h::Handle) = Int(ccall((:rs_record_taped, LIB[]), Int32, (Ptr{Cvoid},), h.ptr))
 set_lambda!(h::Handle, lam::Vector{Float64}) =
     check(h, ccall((:rs_adjoint_set_lambda, LIB[]), Int32, (Ptr{Cvoid}, Ptr{Float64}, Csize_t),
                    h.ptr, lam, length(lam)))

@@ -17,7 +17,8 @@ SYMBOLS = [
     "rs_get_rate_constants", "rs_set_rate_constants", "rs_macro_step", "rs_rhs_transport",
     "rs_rhs_chem", "rs_block_jac", "rs_single_step", "rs_state_device_ptr", "rs_stream",
     "rs_set_profiling", "rs_get_profile", "rs_reset_profile", "rs_ros23_attempt_noalloc",
-    "rs_record", "rs_record_count", "rs_adjoint_set_lambda", "rs_adjoint_get_lambda",
+    "rs_record", "rs_record_count", "rs_set_adjoint_tape", "rs_record_taped",
+    "rs_adjoint_set_lambda", "rs_adjoint_get_lambda",
     "rs_backward_macro_step", "rs_adjoint_get_grad_emission", "rs_adjoint_reset_grad",
     "rs_autotune", "rs_set_chem_kernel", "rs_get_chem_kernel", "rs_chem_kernel_source",
     "rs_chem_kernel_compile", "rs_chem_kernel_reciprocal", "rs_lu_order",
@@ -81,6 +82,10 @@ def _declare(L):
     L.rs_record.restype = C.c_int
     L.rs_record_count.argtypes = [vp]
     L.rs_record_count.restype = i32
+    L.rs_set_adjoint_tape.argtypes = [vp, C.c_int64]
+    L.rs_set_adjoint_tape.restype = C.c_int
+    L.rs_record_taped.argtypes = [vp]
+    L.rs_record_taped.restype = i32
     for f in ("rs_adjoint_set_lambda", "rs_adjoint_get_lambda", "rs_adjoint_get_grad_emission"):
         getattr(L, f).argtypes = [vp, dp, sz]
         getattr(L, f).restype = C.c_int
@@ -278,6 +283,15 @@ class Solver:
 
     def record_count(self):
         return self.L.rs_record_count(self.h)
+
+    def set_adjoint_tape(self, budget_bytes=-1):
+        """Device-tape budget of the next recording: bytes, -1 for a quarter of the free device
+        memory (the default), 0 to replay every recorded macro step from its checkpoint."""
+        self._check(self.L.rs_set_adjoint_tape(self.h, int(budget_bytes)))
+
+    def record_taped(self):
+        """Recorded macro steps whose device tape is complete (swept back without replay)."""
+        return self.L.rs_record_taped(self.h)
 
     def adjoint_backward(self, lam_end_cellmajor, steps=None, on_step=None):
         """Backward sweep over the recorded macro steps (newest first).  Returns

@@ -328,8 +328,20 @@ struct rs_handle {
     DevBuf<double> ck;
     double t0 = 0, t1 = 0;
     std::vector<double> seqT, seqC;  // flattened (t, dt) pairs
+    // device tape: the state before every accepted step, then the end state, at
+    // tape_arena + tape_off (complete: the backward needs no replay)
+    size_t tape_off = 0;
+    size_t tape_cap = 0;  // states available to this macro step
+    bool tape_ok = false;
   };
   bool rec_on = false;
+  // tape budget in bytes (-1: a quarter of the free device memory when recording starts,
+  // 0: always replay), the arena reserved for it and the doubles the recorded steps use
+  long long tape_budget = -1;
+  DevBuf<double> tape_arena;
+  size_t tape_limit = 0, tape_used = 0;
+  DevBuf<int> ntape;  // per half: states stored, slot overflow
+  bool tape_live = false;  // the attempts of the running half store the tape
   std::vector<Rec> recs;
   std::vector<DevBuf<double>> ck_pool;  // checkpoint buffers kept for reuse across recordings
   DevBuf<double> seqbuf, lam, lam2, ebar, tape, adj, G, Cf;
@@ -340,6 +352,7 @@ struct rs_handle {
     cudaGraph_t g = nullptr;
     cudaGraphExec_t ex = nullptr;
     bool valid = false;
+    bool with_tape = false;  // body stores the adjoint tape after the controller
   };
   LoopGraph loops[2];
   cudaStream_t cap = nullptr;
@@ -720,6 +733,7 @@ void transport_attempt(rs_handle* h, Ctl* c) {
   }
   Scope s(h, "finalize");
   rs::launch_finalize(h->st, c, h->partial.p, (int)((h->nc + 255) / 256));
+  if (h->tape_live) rs::launch_tape_store(h->st, c, h->U[0].p, h->U[1].p, h->nc * h->nsp);
   h->launches += h->cfg.precision == RS_PREC_MIXED ? 18 : 17;
 }
 
@@ -732,6 +746,7 @@ void chem_attempt(rs_handle* h, Ctl* c) {
   }
   Scope s(h, "finalize");
   rs::launch_finalize(h->st, c, h->partial.p, (int)((h->nc + 255) / 256));
+  if (h->tape_live) rs::launch_tape_store(h->st, c, h->U[0].p, h->U[1].p, h->nc * h->nsp);
   h->launches += 2;
 }
 
@@ -783,6 +798,8 @@ void build_loop_graph(rs_handle* h, int slot) {
                              h->cfg.atol_C, h->cfg.clamp_nonneg, h->fsal[0].p, h->fsal[1].p);
   }
   rs::launch_finalize_graph(h->cap, c, h->partial.p, nparts, cond);
+  if (h->tape_live) rs::launch_tape_store(h->cap, c, h->U[0].p, h->U[1].p, h->nc * h->nsp);
+  L.with_tape = h->tape_live;
   cudaGraph_t captured = nullptr;
   CK(cudaStreamEndCapture(h->cap, &captured));
   CK(cudaGraphInstantiate(&L.ex, L.g, 0));
@@ -793,7 +810,7 @@ void build_loop_graph(rs_handle* h, int slot) {
 // controller once at the end.
 void run_adaptive_graph(rs_handle* h, int slot) {
   auto& L = h->loops[slot];
-  if (!L.valid) build_loop_graph(h, slot);
+  if (!L.valid || L.with_tape != h->tape_live) build_loop_graph(h, slot);
   CK(cudaGraphLaunch(L.ex, h->st));
   CK(cudaMemcpyAsync(&h->hctl[slot], h->ctl.p + slot, sizeof(Ctl), cudaMemcpyDeviceToHost,
                      h->st));
@@ -972,9 +989,10 @@ void rs_destroy(rs_handle* h) {
   for (auto& r : h->recs) r.ck.release();
   for (auto& b : h->ck_pool) b.release();
   DevBuf<double>* abufs[] = {&h->seqbuf, &h->lam, &h->lam2, &h->ebar, &h->tape, &h->adj, &h->G,
-                             &h->Cf};
+                             &h->Cf, &h->tape_arena};
   for (auto* b : abufs) b->release();
   h->nseq.release();
+  h->ntape.release();
   h->tma_err.release();
   rs::mixed_tmaps_destroy(h->tmaps);
   h->ctl.release();
@@ -1142,6 +1160,7 @@ rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double*
     if (!(t1 > t0)) throw RsError(RS_ERR_INVALID, "t1 must exceed t0");
     if (!(*dtT > 0.0) || !(*dtC > 0.0)) throw RsError(RS_ERR_INVALID, "dt must be positive");
     h->launches = 0;
+    h->tape_live = false;
     if (h->rates_dirty && !h->rates_override) h->launches += 1;
     ensure_rates(h);
     double ntot = (double)h->nc * h->nsp;
@@ -1169,7 +1188,24 @@ rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double*
       h->seqbuf.alloc((size_t)4 * seqcap);
       h->nseq.alloc(2);
       CK(cudaMemsetAsync(h->nseq.p, 0, 2 * sizeof(int), h->st));
+      r.tape_off = h->tape_used;
+      r.tape_cap = h->tape_limit > h->tape_used ? (h->tape_limit - h->tape_used) / n : 0;
+      h->ntape.alloc(4);
+      CK(cudaMemsetAsync(h->ntape.p, 0, 4 * sizeof(int), h->st));
     }
+    // slots of the device tape for the half about to run (before, the half's first state is
+    // `first`; one slot stays for the end state)
+    auto tape_half = [&](Ctl& init, size_t first, int half) {
+      h->tape_live = false;
+      if (!h->rec_on) return;
+      const auto& r = h->recs.back();
+      const size_t n = h->nc * h->nsp;
+      if (r.tape_cap < first + 2) return;
+      init.tape = h->tape_arena.p + r.tape_off + first * n;
+      init.ntape = h->ntape.p + 2 * half;
+      init.tapecap = (int)std::min<size_t>(r.tape_cap - 1 - first, 1u << 30);
+      h->tape_live = true;
+    };
     if (h->cfg.do_transport) {
       Ctl init = make_ctl(h, t0, t1, *dtT, h->cfg.ctrl_T, ntot);
       init.cur = h->cur;
@@ -1178,6 +1214,7 @@ rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double*
         init.nseq = h->nseq.p;
         init.seqcap = seqcap;
       }
+      tape_half(init, 0, 0);
       rs::launch_ctl_init(h->st, h->ctl.p + 0, init);
       h->launches += 1;
       if (h->use_graphs && !h->prof.on) run_adaptive_graph(h, 0);
@@ -1197,6 +1234,7 @@ rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double*
           init.nseq = h->nseq.p + 1;
           init.seqcap = seqcap;
         }
+        tape_half(init, h->cfg.do_transport ? (size_t)stats.naT : 0, 1);
         rs::launch_ctl_init(h->st, h->ctl.p + 1, init);
         h->launches += 1;
         if (h->use_graphs && !h->prof.on) run_adaptive_graph(h, 1);
@@ -1255,7 +1293,21 @@ rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double*
       if (ns_h[1])
         CK(cudaMemcpy(r.seqC.data(), h->seqbuf.p + (size_t)2 * seqcap,
                       r.seqC.size() * sizeof(double), cudaMemcpyDeviceToHost));
+      // the tape is complete when both halves stored every accepted step's input (a half
+      // that did not run stored none); the end state closes it
+      int nt[4] = {0, 0, 0, 0};
+      CK(cudaMemcpy(nt, h->ntape.p, sizeof(nt), cudaMemcpyDeviceToHost));
+      const size_t n = h->nc * h->nsp, used = (size_t)ns_h[0] + ns_h[1] + 1;
+      r.tape_ok = h->tape_limit > 0 && nt[1] == 0 && nt[3] == 0 && nt[0] == ns_h[0] &&
+                  nt[2] == ns_h[1] && used <= r.tape_cap &&
+                  (ns_h[0] == 0 || h->cfg.do_transport) && (ns_h[1] == 0 || h->cfg.do_chemistry);
+      if (r.tape_ok) {
+        CK(cudaMemcpyAsync(h->tape_arena.p + r.tape_off + (used - 1) * n, h->U[h->cur].p,
+                           n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+        h->tape_used += used * n;
+      }
     }
+    h->tape_live = false;
     if (!okT || !okC) {
       check_staging(h);
       throw RsError(RS_ERR_MAXITERS, "adaptive solve stopped before t1 (maxiters)");
@@ -1505,12 +1557,42 @@ rs_status rs_record(rs_handle* h, int32_t on) {
         r.ck.n = 0;
       }
       h->recs.clear();
+      // the device tape's arena, reserved here so that recorded macro steps allocate nothing
+      size_t want = 0;
+      if (h->tape_budget < 0) {
+        size_t fr = 0, tot = 0;
+        CK(cudaMemGetInfo(&fr, &tot));
+        want = (fr + h->tape_arena.n * sizeof(double)) / 4;
+      } else {
+        want = (size_t)h->tape_budget;
+      }
+      h->tape_limit = want / sizeof(double);
+      if (h->tape_limit > h->tape_arena.n) {
+        h->tape_arena.release();
+        h->tape_arena.alloc(h->tape_limit);
+      }
+      h->tape_used = 0;
     }
     h->rec_on = on != 0;
   });
 }
 
 int32_t rs_record_count(const rs_handle* h) { return h ? (int32_t)h->recs.size() : 0; }
+
+rs_status rs_set_adjoint_tape(rs_handle* h, int64_t budget_bytes) {
+  if (!h) return RS_ERR_INVALID;
+  return guard(h, [&] {
+    if (budget_bytes < -1) throw RsError(RS_ERR_INVALID, "tape budget must be >= -1");
+    h->tape_budget = budget_bytes;
+  });
+}
+
+int32_t rs_record_taped(const rs_handle* h) {
+  if (!h) return 0;
+  int32_t k = 0;
+  for (const auto& r : h->recs) k += r.tape_ok ? 1 : 0;
+  return k;
+}
 
 rs_status rs_adjoint_set_lambda(rs_handle* h, const double* lam, size_t n) {
   if (!h || !lam) return RS_ERR_INVALID;
@@ -1565,14 +1647,20 @@ rs_status rs_backward_macro_step(rs_handle* h, int32_t k) {
     const auto& r = h->recs[k];
     size_t n = h->nc * h->nsp;
     int nT = (int)(r.seqT.size() / 2), nC = (int)(r.seqC.size() / 2);
+    cudaStream_t st = h->st;
+    const int clamp = h->cfg.clamp_nonneg;
+    double* tape = nullptr;
+    double* fin = nullptr;
+    if (r.tape_ok) {  // the forward stored every step's input and the end state
+      tape = h->tape_arena.p + r.tape_off;
+      fin = tape + (size_t)(nT + nC) * n;
+    } else {
     // one tape for the largest recorded macro step (no reallocation during a sweep)
     size_t most = 0;
     for (const auto& q : h->recs) most = std::max(most, (q.seqT.size() + q.seqC.size()) / 2);
     h->tape.alloc((most + 2) * n);
-    double* tape = h->tape.p;
+    tape = h->tape.p;
     double* R[2] = {tape + (size_t)(nT + nC) * n, tape + (size_t)(nT + nC + 1) * n};
-    cudaStream_t st = h->st;
-    const int clamp = h->cfg.clamp_nonneg;
     // ---- fixed-sequence replay from the checkpoint, keeping every step's input
     int cur = 0;
     {
@@ -1603,7 +1691,8 @@ rs_status rs_backward_macro_step(rs_handle* h, int32_t k) {
     }
     }
     // the final replayed state closes the tape (output of the last step)
-    double* fin = R[cur];
+    fin = R[cur];
+    }
     auto out_of = [&](int j) -> const double* {
       return (j + 1 < nT + nC) ? tape + (size_t)(j + 1) * n : fin;
     };

@@ -137,6 +137,33 @@ __global__ void k_to_cellmajor(const double* __restrict__ soa, double* __restric
   cm[y] = soa[(size_t)s * nc + ((size_t)k * nlat + j) * nlon + i];
 }
 
+// Adjoint tape, one attempt's close-out after the controller's: when the attempt was accepted
+// (the accepted count passed the stored count) the state before the step -- the buffer the
+// accepted candidate did not go to -- is copied to its slot; k_tape_bump then records it.
+__global__ void k_tape_store(const Ctl* __restrict__ c, const double* __restrict__ U0,
+                             const double* __restrict__ U1, size_t n) {
+  if (!c->tape) return;
+  const int k = (int)c->nacc - 1;
+  if (k < c->ntape[0] || k >= c->tapecap) return;
+  const double* __restrict__ src = c->cur ? U0 : U1;
+  double* __restrict__ dst = c->tape + (size_t)k * n;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x)
+    dst[e] = src[e];
+}
+__global__ void k_tape_bump(const Ctl* __restrict__ c) {
+  if (!c->tape) return;
+  const int k = (int)c->nacc;
+  if (k <= c->ntape[0]) return;
+  if (k > c->tapecap) c->ntape[1] = 1;
+  else c->ntape[0] = k;
+}
+void launch_tape_store(cudaStream_t st, const Ctl* ctl, const double* U0, const double* U1,
+                       size_t n) {
+  k_tape_store<<<1024, 256, 0, st>>>(ctl, U0, U1, n);  // grid-stride copy
+  k_tape_bump<<<1, 1, 0, st>>>(ctl);
+}
+
 // fixed-sequence replay: accept the attempt unconditionally (tools/adjoint_gradient.jl:647-669)
 __global__ void k_replay_accept(Ctl* __restrict__ c) {
   c->cur ^= 1;

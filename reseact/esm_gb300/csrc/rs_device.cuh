@@ -78,6 +78,13 @@ struct Ctl {
   int done;
   int accept;
   int pad;
+  // if set: the state before each accepted step is copied to tape + k * n, k the accepted
+  // count, while k < tapecap (adjoint tape); ntape[0] counts stored states, ntape[1] is raised
+  // when a step found no slot
+  double* tape;
+  int* ntape;
+  int tapecap;
+  int pad2;
 };
 
 __device__ __forceinline__ double ld(const double* p) { return __ldg(p); }

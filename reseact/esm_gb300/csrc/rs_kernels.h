@@ -143,6 +143,10 @@ void launch_flux_dir_mixed(cudaStream_t st, const DevTransport<double>& T, const
 // control (rs_control.cu)
 void launch_ctl_init(cudaStream_t st, Ctl* ctl, const Ctl& init);
 void launch_replay_accept(cudaStream_t st, Ctl* ctl);
+// adjoint tape: after an attempt's controller, store the pre-step state of an accepted step
+// (two launches; no-ops unless the controller carries a tape)
+void launch_tape_store(cudaStream_t st, const Ctl* ctl, const double* U0, const double* U1,
+                       size_t n);
 void launch_clamp_mask(cudaStream_t st, size_t n, double* lam, const double* out);
 
 // discrete adjoint (rs_adjoint.cu)
