@@ -554,12 +554,20 @@ def measure_adjoint(args, local, barrier):
     e2.record(stream)
     barrier()
     fwd, bwd = e0.elapsed_time(e1), e1b.elapsed_time(e2)
+    # the backward's split by kernel family, from a second sweep over the same records with the
+    # library's per-scope CUDA-event timing (outside the timed region)
+    s.set_profiling(True)
+    s.reset_profile()
+    s.adjoint_backward(lam_cm)
+    split = {k: round(v[1], 3) for k, v in s.profile().items() if k.startswith("adj_")}
+    s.set_profiling(False)
     iNO = w.mech.species.index("NO")
     out = {"workload": "C4 72x46x47 SuperFast FP64, J = sum_surface (O3_end - O3_obs)^2, "
                        "gradient w.r.t. surface NO emission",
            "macro_steps": args.steps, "forward_ms": round(fwd, 3), "backward_ms": round(bwd, 3),
            "adjoint_over_forward": round(bwd / fwd, 3),
            "grad_norm": float(np.linalg.norm(grad[iNO, 0])),
+           "backward_split_ms": split, "taped_macro_steps": s.record_taped(),
            "reference_adjoint_over_forward": 2.51}
     s.close()
     return out
