@@ -341,7 +341,6 @@ struct rs_handle {
   DevBuf<double> tape_arena;
   size_t tape_limit = 0, tape_used = 0;
   DevBuf<int> ntape;  // per half: states stored, slot overflow
-  bool tape_live = false;  // the attempts of the running half store the tape
   std::vector<Rec> recs;
   std::vector<DevBuf<double>> ck_pool;  // checkpoint buffers kept for reuse across recordings
   DevBuf<double> seqbuf, lam, lam2, ebar, tape, adj, G, Cf;
@@ -352,7 +351,7 @@ struct rs_handle {
     cudaGraph_t g = nullptr;
     cudaGraphExec_t ex = nullptr;
     bool valid = false;
-    bool with_tape = false;  // body stores the adjoint tape after the controller
+    bool with_tape = false;  // body stores the adjoint tape after the controller (recording)
   };
   LoopGraph loops[2];
   cudaStream_t cap = nullptr;
@@ -733,7 +732,7 @@ void transport_attempt(rs_handle* h, Ctl* c) {
   }
   Scope s(h, "finalize");
   rs::launch_finalize(h->st, c, h->partial.p, (int)((h->nc + 255) / 256));
-  if (h->tape_live) rs::launch_tape_store(h->st, c, h->U[0].p, h->U[1].p, h->nc * h->nsp);
+  if (h->rec_on) rs::launch_tape_store(h->st, c, h->U[0].p, h->U[1].p, h->nc * h->nsp);
   h->launches += h->cfg.precision == RS_PREC_MIXED ? 18 : 17;
 }
 
@@ -746,7 +745,7 @@ void chem_attempt(rs_handle* h, Ctl* c) {
   }
   Scope s(h, "finalize");
   rs::launch_finalize(h->st, c, h->partial.p, (int)((h->nc + 255) / 256));
-  if (h->tape_live) rs::launch_tape_store(h->st, c, h->U[0].p, h->U[1].p, h->nc * h->nsp);
+  if (h->rec_on) rs::launch_tape_store(h->st, c, h->U[0].p, h->U[1].p, h->nc * h->nsp);
   h->launches += 2;
 }
 
@@ -798,8 +797,10 @@ void build_loop_graph(rs_handle* h, int slot) {
                              h->cfg.atol_C, h->cfg.clamp_nonneg, h->fsal[0].p, h->fsal[1].p);
   }
   rs::launch_finalize_graph(h->cap, c, h->partial.p, nparts, cond);
-  if (h->tape_live) rs::launch_tape_store(h->cap, c, h->U[0].p, h->U[1].p, h->nc * h->nsp);
-  L.with_tape = h->tape_live;
+  // while recording, the tape kernels follow the controller (no-ops for a controller without
+  // a tape: a macro step the arena has no room for)
+  if (h->rec_on) rs::launch_tape_store(h->cap, c, h->U[0].p, h->U[1].p, h->nc * h->nsp);
+  L.with_tape = h->rec_on;
   cudaGraph_t captured = nullptr;
   CK(cudaStreamEndCapture(h->cap, &captured));
   CK(cudaGraphInstantiate(&L.ex, L.g, 0));
@@ -810,7 +811,7 @@ void build_loop_graph(rs_handle* h, int slot) {
 // controller once at the end.
 void run_adaptive_graph(rs_handle* h, int slot) {
   auto& L = h->loops[slot];
-  if (!L.valid || L.with_tape != h->tape_live) build_loop_graph(h, slot);
+  if (!L.valid || L.with_tape != h->rec_on) build_loop_graph(h, slot);
   CK(cudaGraphLaunch(L.ex, h->st));
   CK(cudaMemcpyAsync(&h->hctl[slot], h->ctl.p + slot, sizeof(Ctl), cudaMemcpyDeviceToHost,
                      h->st));
@@ -1160,7 +1161,6 @@ rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double*
     if (!(t1 > t0)) throw RsError(RS_ERR_INVALID, "t1 must exceed t0");
     if (!(*dtT > 0.0) || !(*dtC > 0.0)) throw RsError(RS_ERR_INVALID, "dt must be positive");
     h->launches = 0;
-    h->tape_live = false;
     if (h->rates_dirty && !h->rates_override) h->launches += 1;
     ensure_rates(h);
     double ntot = (double)h->nc * h->nsp;
@@ -1196,7 +1196,6 @@ rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double*
     // slots of the device tape for the half about to run (before, the half's first state is
     // `first`; one slot stays for the end state)
     auto tape_half = [&](Ctl& init, size_t first, int half) {
-      h->tape_live = false;
       if (!h->rec_on) return;
       const auto& r = h->recs.back();
       const size_t n = h->nc * h->nsp;
@@ -1204,7 +1203,6 @@ rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double*
       init.tape = h->tape_arena.p + r.tape_off + first * n;
       init.ntape = h->ntape.p + 2 * half;
       init.tapecap = (int)std::min<size_t>(r.tape_cap - 1 - first, 1u << 30);
-      h->tape_live = true;
     };
     if (h->cfg.do_transport) {
       Ctl init = make_ctl(h, t0, t1, *dtT, h->cfg.ctrl_T, ntot);
@@ -1307,7 +1305,6 @@ rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double*
         h->tape_used += used * n;
       }
     }
-    h->tape_live = false;
     if (!okT || !okC) {
       check_staging(h);
       throw RsError(RS_ERR_MAXITERS, "adaptive solve stopped before t1 (maxiters)");
@@ -1574,6 +1571,12 @@ rs_status rs_record(rs_handle* h, int32_t on) {
       h->tape_used = 0;
     }
     h->rec_on = on != 0;
+    // the device loops with the tape kernels, built now rather than in the first recorded
+    // macro step
+    if (h->rec_on && h->use_graphs) {
+      if (h->cfg.do_transport) build_loop_graph(h, 0);
+      if (h->cfg.do_chemistry && h->cfg.chem_mode == RS_CHEM_GLOBAL_DT) build_loop_graph(h, 1);
+    }
   });
 }
 
