@@ -16,7 +16,7 @@ copied host->device before and device->host after every step (pinned host buffer
 reference; the Julia reference itself cannot run without julia and its un-vendored stack) on
 all host threads, on a bounded sample: the same physics on a 36 x 23 x 47 sub-grid.
 
-Multi-GPU: the path does not shard in this build; N ranks run N independent replicas
+Multi-GPU: the operator-split step does not shard; N ranks run N independent replicas
 (scaling "weak", no collective in the data path; NCCL only for the barrier and the max).
 """
 import argparse

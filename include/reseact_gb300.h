@@ -58,7 +58,7 @@ typedef enum rs_status {
   RS_ERR_NONFINITE = 4,   /* non-finite state after a macro step */
   RS_ERR_NOMEM = 5,       /* device allocation failed */
   RS_ERR_STATE = 6,       /* call out of order (e.g. no forcing set) */
-  RS_ERR_UNSUPPORTED = 7  /* feature not available in this build */
+  RS_ERR_UNSUPPORTED = 7  /* feature not available (library, device or configuration) */
 } rs_status;
 
 /* lateral boundary kinds */

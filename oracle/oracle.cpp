@@ -1,6 +1,6 @@
 // ORACLE -- CPU FP64 restatement of ReSEACT's operator-split step.  TEST INFRASTRUCTURE ONLY:
 // only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load this library,
-// and only as the checker / the timed CPU baseline.  The product (libreseact_gb300.so) never
+// and only as the parity reference / the timed CPU baseline.  The product (libreseact_gb300.so) never
 // links, loads or calls it.
 //
 // The reference is Julia and cannot run here (no julia, un-vendored EarthSciAST /

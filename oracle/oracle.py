@@ -1,7 +1,7 @@
 """ctypes wrapper of the CPU oracle (oracle.cpp).  TEST INFRASTRUCTURE ONLY.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may use this module,
-and only as the checker or the timed CPU baseline.  Build with ``make -C oracle`` (or
+and only as the parity reference or the timed CPU baseline.  Build with ``make -C oracle`` (or
 ``build()`` below).  Arrays are grid SoA [species][nlev][nlat][nlon] float64.
 """
 import ctypes as C

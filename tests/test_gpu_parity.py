@@ -42,7 +42,7 @@ def make_pair(w, oracle_mod, strict=False, **kw):
     f = w.forcing_abi()
     s.set_forcing(f)
     o = oracle_mod.Oracle(cfg, f, mabi)
-    o.set_lu_order(s.lu_order())  # the elimination order of this build
+    o.set_lu_order(s.lu_order())  # the handle's elimination order
     return s, o
 
 
