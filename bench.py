@@ -182,8 +182,7 @@ def ros23_exec_counts(mech, order, evals, emissions=False):
     exceed these by the products that the rate-once form shares.  W = I - dtg*J is formed from
     partials of kd_r = -dtg*K_r, and the error norm takes dto6^2 out of its sum.  Checked
     against ncu's DADD/DMUL/DFMA counts of the kernel (3-evaluation attempt of SuperFast in the
-    minimum-fill order: 1,037 instructions counted here; ncu measures 1,010.5 with two Newton
-    steps per pivot, 1,049 counted for that form)."""
+    minimum-fill order: 1,037 instructions counted here, 997.5 measured)."""
     t = mech.tables()
     ns = mech.ns
 
@@ -455,9 +454,9 @@ def run_gb300(args):
                     "bound": "fp64", "achieved": round(achieved, 4),
                     "peak": peak, "unit": "TFLOP/s", "frac": round(achieved / peak, 4) if peak else None,
                     # DRAM bytes per launch from one ncu capture of this kernel on this
-                    # workload (dram__bytes_read.sum + dram__bytes_write.sum: 303.6 MB + 1050.6 MB,
+                    # workload (dram__bytes_read.sum + dram__bytes_write.sum: 302.1 MB + 1055.1 MB,
                     # mostly the 128-register variant's spill stores); null for other kernels
-                    "traffic": (1354.2e6 if (kinfo.get("kind") == "specialized" and not args.small
+                    "traffic": (1357.2e6 if (kinfo.get("kind") == "specialized" and not args.small
                                              and kinfo.get("variant") == "regs2") else None),
                     "traffic_source": "ncu capture summarised in profiles/rs_jit_attempt_c2_144x91x47.md",
                     "flops_per_cell_attempt": round(f_exec, 1),
