@@ -88,3 +88,22 @@ def test_ctypes_mirrors_match_the_header_layout(tmp_path):
         assert int(out[name]) == C.sizeof(cls), name
         for f in cls._fields_:
             assert int(out["%s.%s" % (name, f[0])]) == getattr(cls, f[0]).offset, (name, f[0])
+
+
+@pytest.mark.parametrize("dims", [(2, 9, 6), (16, 2, 6), (16, 9, 2)])
+def test_transport_grid_below_the_stencil_is_rejected(dims):
+    """A transport grid with fewer than 3 cells along any direction cannot hold the PPM
+    stencil (three cells each side, mirrored or wrapped): rs_create refuses it before any
+    device call, so this holds without a GPU."""
+    nlon, nlat, nlev = dims
+    w = workloads.c2(nlon=nlon, nlat=nlat, nlev=nlev, steps=1)
+    with pytest.raises(_lib.RsError) as ei:
+        _lib.Solver.for_workload(w)
+    assert ei.value.status == abi.RS_ERR_INVALID
+    assert "nlon, nlat, nlev >= 3" in str(ei.value)
+
+
+def test_adjoint_tape_budget_rejects_negative_values():
+    L = _lib.load()
+    assert L.rs_set_adjoint_tape(None, -1) == abi.RS_ERR_INVALID  # no handle
+    assert L.rs_record_taped(None) == 0

@@ -312,3 +312,29 @@ def test_mixed_precision_full_step_within_1e6(oracle_mod):
     got, ref = s.get_state(), cm(w, u)
     err = np.abs(got - ref) / np.maximum(np.abs(ref), 1e-9)
     assert err.max() < 1e-6, err.max()
+
+
+@pytest.mark.parametrize("strict", [False, True])
+def test_minimum_grid_matches_oracle(oracle_mod, strict):
+    """The smallest transport grid, 3 x 3 x 3 (every ghost position a wrapped or mirrored
+    cell), through adaptive macro steps of transport and chemistry against the oracle, in
+    both builds, with the same accept/reject counts."""
+    w = workloads.c2(nlon=3, nlat=3, nlev=3, steps=1)
+    mabi = abi.MechanismABI(w.mech)
+    cfg = w.config(mabi)
+    s = Solver(cfg, mabi, strict=strict)
+    f = w.forcing_abi()
+    s.set_forcing(f)
+    o = oracle_mod.Oracle(cfg, f, mabi)
+    o.set_lu_order(s.lu_order())
+    o.set_rates(s.rates())
+    s.set_state(w.u0_cellmajor())
+    u = np.ascontiguousarray(w.u0.copy())
+    t, a, b, ao, bo = 0.0, 15.0, 0.5, 15.0, 0.5
+    for _ in range(2):
+        _, a, b, st = s.macro_step(t, t + 600.0, a, b)
+        _, ao, bo, ost = o.macro_step(u, t, t + 600.0, ao, bo)
+        assert (st.naT, st.nrT, st.naC, st.nrC) == tuple(ost[:4])
+        t += 600.0
+    ok, worst = close(s.get_state(), workloads.soa_to_cellmajor(u, 3, 3, 3), rel=REL, floor=1e-9)
+    assert ok, worst
