@@ -177,9 +177,10 @@ __global__ void __launch_bounds__(128) k_ros23_vjp(
 
 void launch_ros23_vjp(const LaunchCtx& L, const double* U, const double* Uout, const double* lam,
                       double* lam_out, const double* kr, const double* em, double* ebar,
-                      double dt, int clamp) {
+                      double dt, int clamp, const double* kz) {
   if (L.jit) {
-    jit_launch_vjp(*L.jit, L.stream, L.nc, L.nsp, U, Uout, lam, lam_out, kr, em, ebar, dt, clamp);
+    jit_launch_vjp(*L.jit, L.stream, L.nc, L.nsp, U, Uout, lam, lam_out, kr, em, ebar, dt, clamp,
+                   kz);
     return;
   }
   int nb = (L.nc + 127) / 128;

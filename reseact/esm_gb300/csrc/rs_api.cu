@@ -333,6 +333,8 @@ struct rs_handle {
     size_t tape_off = 0;
     size_t tape_cap = 0;  // states available to this macro step
     bool tape_ok = false;
+    size_t kz_off = 0, kz_cap = 0;  // its chemistry stage slots (k1, z2 per accepted step)
+    bool kz_ok = false;             // the forward wrote every chemistry step's stages
   };
   bool rec_on = false;
   // tape budget in bytes (-1: a quarter of the free device memory when recording starts,
@@ -341,6 +343,11 @@ struct rs_handle {
   DevBuf<double> tape_arena;
   size_t tape_limit = 0, tape_used = 0;
   DevBuf<int> ntape;  // per half: states stored, slot overflow
+  // the stage tape (specialised chemistry kernels): k1 and z2 of every accepted chemistry
+  // step, [2][ns][nc] doubles each, in its own arena (its share of the tape budget), and the
+  // replay's scratch of the same layout
+  DevBuf<double> kz_arena, kzs;
+  size_t kz_limit = 0, kz_used = 0;
   std::vector<Rec> recs;
   std::vector<DevBuf<double>> ck_pool;  // checkpoint buffers kept for reuse across recordings
   DevBuf<double> seqbuf, lam, lam2, ebar, tape, adj, G, Cf;
@@ -990,7 +997,7 @@ void rs_destroy(rs_handle* h) {
   for (auto& r : h->recs) r.ck.release();
   for (auto& b : h->ck_pool) b.release();
   DevBuf<double>* abufs[] = {&h->seqbuf, &h->lam, &h->lam2, &h->ebar, &h->tape, &h->adj, &h->G,
-                             &h->Cf, &h->tape_arena};
+                             &h->Cf, &h->tape_arena, &h->kz_arena, &h->kzs};
   for (auto* b : abufs) b->release();
   h->nseq.release();
   h->ntape.release();
@@ -1190,6 +1197,9 @@ rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double*
       CK(cudaMemsetAsync(h->nseq.p, 0, 2 * sizeof(int), h->st));
       r.tape_off = h->tape_used;
       r.tape_cap = h->tape_limit > h->tape_used ? (h->tape_limit - h->tape_used) / n : 0;
+      const size_t nkz = (size_t)2 * h->mt.ns * h->nc;
+      r.kz_off = h->kz_used;
+      r.kz_cap = h->kz_limit > h->kz_used ? (h->kz_limit - h->kz_used) / nkz : 0;
       h->ntape.alloc(4);
       CK(cudaMemsetAsync(h->ntape.p, 0, 4 * sizeof(int), h->st));
     }
@@ -1233,6 +1243,10 @@ rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double*
           init.seqcap = seqcap;
         }
         tape_half(init, h->cfg.do_transport ? (size_t)stats.naT : 0, 1);
+        if (h->rec_on && h->lc.jit && h->recs.back().kz_cap > 0) {  // the stage tape
+          init.kz = h->kz_arena.p + h->recs.back().kz_off;
+          init.kzcap = (int)std::min<size_t>(h->recs.back().kz_cap, 1u << 30);
+        }
         rs::launch_ctl_init(h->st, h->ctl.p + 1, init);
         h->launches += 1;
         if (h->use_graphs && !h->prof.on) run_adaptive_graph(h, 1);
@@ -1296,13 +1310,19 @@ rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double*
       int nt[4] = {0, 0, 0, 0};
       CK(cudaMemcpy(nt, h->ntape.p, sizeof(nt), cudaMemcpyDeviceToHost));
       const size_t n = h->nc * h->nsp, used = (size_t)ns_h[0] + ns_h[1] + 1;
+      // with the specialised kernels the chemistry stages must be complete too, so that every
+      // step VJP reads its k1, z2 from a forward pass (the tape's or the replay's)
+      const bool need_kz = h->lc.jit && ns_h[1] > 0;
       r.tape_ok = h->tape_limit > 0 && nt[1] == 0 && nt[3] == 0 && nt[0] == ns_h[0] &&
                   nt[2] == ns_h[1] && used <= r.tape_cap &&
-                  (ns_h[0] == 0 || h->cfg.do_transport) && (ns_h[1] == 0 || h->cfg.do_chemistry);
+                  (ns_h[0] == 0 || h->cfg.do_transport) && (ns_h[1] == 0 || h->cfg.do_chemistry) &&
+                  (!need_kz || (size_t)ns_h[1] <= r.kz_cap);
       if (r.tape_ok) {
         CK(cudaMemcpyAsync(h->tape_arena.p + r.tape_off + (used - 1) * n, h->U[h->cur].p,
                            n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
         h->tape_used += used * n;
+        if (need_kz) h->kz_used += (size_t)ns_h[1] * 2 * h->mt.ns * h->nc;
+        r.kz_ok = need_kz;
       }
     }
     if (!okT || !okC) {
@@ -1559,16 +1579,26 @@ rs_status rs_record(rs_handle* h, int32_t on) {
       if (h->tape_budget < 0) {
         size_t fr = 0, tot = 0;
         CK(cudaMemGetInfo(&fr, &tot));
-        want = (fr + h->tape_arena.n * sizeof(double)) / 4;
+        want = (fr + (h->tape_arena.n + h->kz_arena.n) * sizeof(double)) / 4;
       } else {
         want = (size_t)h->tape_budget;
       }
-      h->tape_limit = want / sizeof(double);
+      // states and chemistry stages share the budget in proportion to their sizes per step
+      // (the stages only with the specialised kernels, the only ones that write them)
+      const double nst = (double)h->nsp, nkz = h->lc.jit ? 2.0 * h->mt.ns : 0.0;
+      const size_t want_kz = (size_t)((double)want * nkz / (nst + nkz));
+      h->tape_limit = (want - want_kz) / sizeof(double);
+      h->kz_limit = want_kz / sizeof(double);
       if (h->tape_limit > h->tape_arena.n) {
         h->tape_arena.release();
         h->tape_arena.alloc(h->tape_limit);
       }
+      if (h->kz_limit > h->kz_arena.n) {
+        h->kz_arena.release();
+        h->kz_arena.alloc(h->kz_limit);
+      }
       h->tape_used = 0;
+      h->kz_used = 0;
     }
     h->rec_on = on != 0;
     // the device loops with the tape kernels, built now rather than in the first recorded
@@ -1654,10 +1684,22 @@ rs_status rs_backward_macro_step(rs_handle* h, int32_t k) {
     const int clamp = h->cfg.clamp_nonneg;
     double* tape = nullptr;
     double* fin = nullptr;
+    // k1, z2 of every chemistry step (specialised kernels): the forward's stage tape, or the
+    // replay's scratch; the step VJPs read them instead of recomputing both stages
+    const size_t nkz = (size_t)2 * h->mt.ns * h->nc;
+    const bool use_kz = h->lc.jit != nullptr && nC > 0;
+    double* kzb = nullptr;
     if (r.tape_ok) {  // the forward stored every step's input and the end state
       tape = h->tape_arena.p + r.tape_off;
       fin = tape + (size_t)(nT + nC) * n;
+      if (use_kz && r.kz_ok) kzb = h->kz_arena.p + r.kz_off;
     } else {
+    if (use_kz) {
+      size_t mostC = 0;
+      for (const auto& q : h->recs) mostC = std::max(mostC, q.seqC.size() / 2);
+      h->kzs.alloc(mostC * nkz);
+      kzb = h->kzs.p;
+    }
     // one tape for the largest recorded macro step (no reallocation during a sweep)
     size_t most = 0;
     for (const auto& q : h->recs) most = std::max(most, (q.seqT.size() + q.seqC.size()) / 2);
@@ -1680,6 +1722,10 @@ rs_status rs_backward_macro_step(rs_handle* h, int32_t k) {
       // tend well past t + dt so that dtc = min(dt, tend - t) is the recorded dt exactly
       Ctl init = make_ctl(h, tj, tj + 4.0 * dj + 1.0, dj, tr ? h->cfg.ctrl_T : h->cfg.ctrl_C, ntot);
       init.cur = cur;
+      if (!tr && kzb) {  // the step writes its k1, z2 to its own slot (accepted count 0)
+        init.kz = kzb + (size_t)(j - nT) * nkz;
+        init.kzcap = 1;
+      }
       rs::launch_ctl_init(st, c, init);
       if (tr) {
         rs::TransportBufs B{R[0], R[1], h->S1.p, h->S2.p, h->S3.p, h->partial.p};
@@ -1705,7 +1751,8 @@ rs_status rs_backward_macro_step(rs_handle* h, int32_t k) {
       int jj = nT + j;
       rs::launch_ros23_vjp(h->lc, tape + (size_t)jj * n, clamp ? out_of(jj) : nullptr, h->lam.p,
                            h->lam2.p, h->krates.p, h->have_emis ? h->emis.p : nullptr,
-                           h->ebar.p, r.seqC[2 * j + 1], clamp);
+                           h->ebar.p, r.seqC[2 * j + 1], clamp,
+                           kzb ? kzb + (size_t)j * nkz : nullptr);
       std::swap(h->lam.p, h->lam2.p);
     }
     }

@@ -85,6 +85,12 @@ struct Ctl {
   int* ntape;
   int tapecap;
   int pad2;
+  // if set (specialised chemistry kernels): every attempt writes its stage vectors k1 and z2
+  // (the second solve's result before k1 is added), [2][ns][n] doubles, to kz + slot * 2 ns n
+  // with slot = the accepted count, while slot < kzcap -- the adjoint's stage tape
+  double* kz;
+  int kzcap;
+  int pad3;
 };
 
 __device__ __forceinline__ double ld(const double* p) { return __ldg(p); }

@@ -447,7 +447,9 @@ std::string generate(const MechTables& T, double ros_d, double ros_c32, bool str
     << "\n#define OFF_DTC " << offsetof(Ctl, dtc) << "\n#define OFF_DTO2 "
     << offsetof(Ctl, dto2) << "\n#define OFF_DTO6 " << offsetof(Ctl, dto6)
     << "\n#define OFF_DTG " << offsetof(Ctl, dtgamma) << "\n#define OFF_ITERS "
-    << offsetof(Ctl, iters) << "\n";
+    << offsetof(Ctl, iters) << "\n#define OFF_NACC " << offsetof(Ctl, nacc)
+    << "\n#define OFF_KZ " << offsetof(Ctl, kz) << "\n#define OFF_KZCAP "
+    << offsetof(Ctl, kzcap) << "\n";
   o << kPrelude;
   // Every multiply-add is written out: RS_FMA fuses in the production build and keeps the
   // multiply and the add separate in the strict build; both builds compile with --fmad=false,
@@ -467,12 +469,21 @@ std::string generate(const MechTables& T, double ros_d, double ros_c32, bool str
   // f2 when the clamp leaves xn unchanged and a NaN marker in plane 0 otherwise; with KEEP
   // the caller also gets f2 in registers.
   o << R"(
+// the stage-tape slot of the attempt a controller is running (null when it keeps no tape):
+// slot = the accepted count, [2][NS][N] doubles per slot, slots below the controller's kzcap
+__device__ __forceinline__ double* stage_slot(const unsigned char* __restrict__ ctl, u64 N) {
+  double* kz = *(double* const*)(ctl + OFF_KZ);
+  const int cap = *(const int*)(ctl + OFF_KZCAP);
+  const int slot = (int)*(const double*)(ctl + OFF_NACC);
+  return (kz && slot >= 0 && slot < cap) ? kz + (u64)slot * 2 * NS * N : nullptr;
+}
 // SOL: the step's solution only (a replay along recorded accepted steps needs no error norm)
 template <bool HE, int WS, bool KEEP, bool SOL = false>
 __device__ __forceinline__ double ros23_cell(const double* __restrict__ kr,
     const double* __restrict__ em, u64 N, int c, const double* x, double* xn, double* W,
     double* f0, bool have_f0, double* __restrict__ fout, int clamp, double* f2,
-    double dt, double dto2, double dto6, double dtg, double rtol, double atol) {
+    double dt, double dto2, double dto6, double dtg, double rtol, double atol,
+    double* __restrict__ kzo) {
 #define K(r) __ldg(kr + (u64)(r) * N + c)
 #define EM(s) __ldg(em + (u64)(s) * N + c)
 #define WV(e) W[(e) * WS]
@@ -491,10 +502,14 @@ __device__ __forceinline__ double ros23_cell(const double* __restrict__ kr,
   g.lu_factor();
   o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) k1[s] = f0[s];\n";
   g.lu_solve("k1");
+  o << "  if (kzo) {  // stage tape: k1\n#pragma unroll\n    for (int s = 0; s < NS; ++s) "
+       "kzo[(u64)s * N + c] = k1[s];\n  }\n";
   o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) xn[s] = RS_FMA(dto2, k1[s], x[s]);\n";
   g.rates_rhs("xn", "f1");
   o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) k2[s] = f1[s] - k1[s];\n";
   g.lu_solve("k2");
+  o << "  if (kzo) {  // stage tape: z2, the solve's result before k1 is added\n#pragma unroll\n"
+       "    for (int s = 0; s < NS; ++s) kzo[(u64)(NS + s) * N + c] = k2[s];\n  }\n";
   o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) k2[s] = k2[s] + k1[s];\n";
   o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) xn[s] = RS_FMA(dt, k2[s], x[s]);\n";
   o << "  if constexpr (SOL) return 0.0;\n";
@@ -561,6 +576,7 @@ __device__ __forceinline__ void attempt_body(const unsigned char* __restrict__ c
   double* __restrict__ Un = cur ? U0 : U1;
   double* __restrict__ Fin = cur ? F1 : F0;
   double* __restrict__ Fout = cur ? F0 : F1;
+  double* __restrict__ kzo = stage_slot(ctl, (u64)nc);
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   const u64 N = (u64)nc;
   double e = 0.0;
@@ -578,11 +594,11 @@ __device__ __forceinline__ void attempt_body(const unsigned char* __restrict__ c
       extern __shared__ double wsm[];
       e = ros23_cell<HE, 256, false>(kr, em, N, c, x, xn, wsm + threadIdx.x, f0, have,
                                      F0 ? Fout : nullptr, clamp, nullptr, dt, dto2, dto6, dtg,
-                                     rtol, atol);
+                                     rtol, atol, kzo);
     } else {
       double W[NLU];
       e = ros23_cell<HE, 1, false>(kr, em, N, c, x, xn, W, f0, have, F0 ? Fout : nullptr,
-                                   clamp, nullptr, dt, dto2, dto6, dtg, rtol, atol);
+                                   clamp, nullptr, dt, dto2, dto6, dtg, rtol, atol, kzo);
     }
     if (F0 && !have) {  // keep f(x) for a retry of this state after a rejection
 #pragma unroll
@@ -631,7 +647,7 @@ __device__ __forceinline__ void per_cell_body(int nc, int nsp, double* __restric
       const double dtc = fmin(dt, a.t1 - t);
       const double sse = ros23_cell<HE, 1, true>(kr, em, N, c, x, xn, W, f0, have, nullptr,
                                                  a.clamp, f2, dtc, dtc / 2, dtc / 6,
-                                                 dtc * ROS_D, a.rtol, a.atol);
+                                                 dtc * ROS_D, a.rtol, a.atol, nullptr);
       have = true;  // f0 == f(x) after the call; replaced below if x moves
       double EEst = sqrt(sse / (double)nsp);
       if (EEst != EEst) EEst = 1.0e10;
@@ -713,7 +729,7 @@ __device__ __forceinline__ void step_body(const unsigned char* __restrict__ ctl,
 #pragma unroll
   for (int s = 0; s < NS; ++s) x[s] = U[(u64)s * N + c];
   ros23_cell<HE, 1, false, true>(kr, em, N, c, x, xn, W, f0, false, nullptr, clamp, nullptr,
-                                 dt, dto2, 0.0, dtg, 0.0, 0.0);
+                                 dt, dto2, 0.0, dtg, 0.0, 0.0, stage_slot(ctl, N));
 #pragma unroll
   for (int s = 0; s < NS; ++s) Un[(u64)s * N + c] = clamp ? fmax(xn[s], 0.0) : xn[s];
   for (int s = NS; s < nsp; ++s) {
@@ -745,12 +761,16 @@ RS_PER_CELL(rs_jit_per_cell_0, false)
 RS_PER_CELL(rs_jit_per_cell_1, true)
 
 // VJP of one ROS23 step at a recorded dt (the table kernel k_ros23_vjp, specialised): forward
-// recompute of the live stages, then lam_out = (d unew / d u)^T lam and ebar += d J / d emission
-template <bool HE>
+// recompute of the live stages, then lam_out = (d unew / d u)^T lam and ebar += d J / d emission.
+// KZ: k1 and z2 come from the stage tape (kzi, [2][NS][nc]) written by the step's forward, so
+// the two RHS evaluations and forward solves are skipped; the partials, W and its LU are
+// recomputed either way.
+template <bool HE, bool KZ>
 __device__ __forceinline__ void vjp_body(int nc, int nsp, const double* __restrict__ U,
     const double* __restrict__ Uout, const double* __restrict__ lam,
     double* __restrict__ lam_out, const double* __restrict__ kr,
-    const double* __restrict__ em, double* __restrict__ ebar, double dt, int clamp) {
+    const double* __restrict__ em, double* __restrict__ ebar, double dt, int clamp,
+    const double* __restrict__ kzi) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
   const u64 N = (u64)nc;
@@ -764,21 +784,27 @@ __device__ __forceinline__ void vjp_body(int nc, int nsp, const double* __restri
 #pragma unroll
   for (int s = 0; s < NS; ++s) x[s] = U[(u64)s * N + c];
 )";
-  o << "  {\n";
+  o << "  if constexpr (!KZ) {\n";
   g.rates_rhs("x", "f0");
   o << "  }\n";
   g.partials("x", "P");
   g.build_w();
   g.lu_factor();
+  o << "  if constexpr (KZ) {\n#pragma unroll\n    for (int s = 0; s < NS; ++s) k1[s] = "
+       "kzi[(u64)s * N + c];\n  } else {\n";
   o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) k1[s] = f0[s];\n";
   g.lu_solve("k1");
+  o << "  }\n";
   o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) u1[s] = RS_FMA(dto2, k1[s], x[s]);\n";
-  o << "  {\n";
+  o << "  if constexpr (!KZ) {\n";
   g.rates_rhs("u1", "f1");
   o << "  }\n";
   g.partials("u1", "P1");
+  o << "  if constexpr (KZ) {\n#pragma unroll\n    for (int s = 0; s < NS; ++s) z2[s] = "
+       "kzi[(u64)(NS + s) * N + c];\n  } else {\n";
   o << "#pragma unroll\n  for (int s = 0; s < NS; ++s) z2[s] = f1[s] - k1[s];\n";
   g.lu_solve("z2");
+  o << "  }\n";
   o << R"(#pragma unroll
   for (int s = 0; s < NS; ++s) {
     double l = lam[(u64)s * N + c];
@@ -825,16 +851,18 @@ __device__ __forceinline__ void vjp_body(int nc, int nsp, const double* __restri
 #undef EM
 #undef WV
 }
-#define RS_VJP(NAME, HE)                                                                     \
+#define RS_VJP(NAME, HE, KZ)                                                                 \
   extern "C" __global__ void __launch_bounds__(128) NAME(int nc, int nsp,                   \
       const double* __restrict__ U, const double* __restrict__ Uout,                        \
       const double* __restrict__ lam, double* __restrict__ lam_out,                         \
       const double* __restrict__ kr, const double* __restrict__ em,                         \
-      double* __restrict__ ebar, double dt, int clamp) {                                     \
-    vjp_body<HE>(nc, nsp, U, Uout, lam, lam_out, kr, em, ebar, dt, clamp);                   \
+      double* __restrict__ ebar, double dt, int clamp, const double* __restrict__ kzi) {     \
+    vjp_body<HE, KZ>(nc, nsp, U, Uout, lam, lam_out, kr, em, ebar, dt, clamp, kzi);          \
   }
-RS_VJP(rs_jit_vjp_0, false)
-RS_VJP(rs_jit_vjp_1, true)
+RS_VJP(rs_jit_vjp_0, false, false)
+RS_VJP(rs_jit_vjp_1, true, false)
+RS_VJP(rs_jit_vjpk_0, false, true)
+RS_VJP(rs_jit_vjpk_1, true, true)
 
 // the production reciprocal applied elementwise (accuracy check against IEEE division)
 extern "C" __global__ void rs_jit_rcp(const double* __restrict__ x, double* __restrict__ r,
@@ -965,7 +993,8 @@ std::shared_ptr<JitChem> jit_chem_build(const MechTables& T, double ros_d, doubl
             get(&J->per_cell[0], "rs_jit_per_cell_0") && get(&J->per_cell[1], "rs_jit_per_cell_1") &&
             get(&J->rcp, "rs_jit_rcp") && get(&J->vjp[0], "rs_jit_vjp_0") &&
             get(&J->vjp[1], "rs_jit_vjp_1") && get(&J->step[0], "rs_jit_step_0") &&
-            get(&J->step[1], "rs_jit_step_1");
+            get(&J->step[1], "rs_jit_step_1") && get(&J->vjpk[0], "rs_jit_vjpk_0") &&
+            get(&J->vjpk[1], "rs_jit_vjpk_1");
   if (!ok) return nullptr;
   if (with_smem && get(&J->attempt[1][0], "rs_jit_attempt_s0") &&
       get(&J->attempt[1][1], "rs_jit_attempt_s1")) {
@@ -1022,9 +1051,9 @@ void jit_launch_rcp(const JitChem& J, cudaStream_t st, const double* x, double* 
 
 void jit_launch_vjp(const JitChem& J, cudaStream_t st, int nc, int nsp, const double* U,
                     const double* Uout, const double* lam, double* lam_out, const double* kr,
-                    const double* em, double* ebar, double dt, int clamp) {
-  cudaKernel_t k = J.vjp[em ? 1 : 0];
-  void* args[] = {&nc, &nsp, &U, &Uout, &lam, &lam_out, &kr, &em, &ebar, &dt, &clamp};
+                    const double* em, double* ebar, double dt, int clamp, const double* kz) {
+  cudaKernel_t k = kz ? J.vjpk[em ? 1 : 0] : J.vjp[em ? 1 : 0];
+  void* args[] = {&nc, &nsp, &U, &Uout, &lam, &lam_out, &kr, &em, &ebar, &dt, &clamp, &kz};
   cudaLaunchKernel((const void*)k, dim3((nc + 127) / 128), dim3(128), args, 0, st);
 }
 

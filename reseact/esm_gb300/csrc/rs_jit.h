@@ -34,6 +34,7 @@ struct JitChem {
   cudaKernel_t rcp = nullptr;                  // elementwise production reciprocal
   cudaKernel_t vjp[2] = {};                    // ROS23 step VJP [has emission]
   cudaKernel_t step[2] = {};                   // accepted step, no error estimate [has emission]
+  cudaKernel_t vjpk[2] = {};                   // step VJP reading k1, z2 from the stage tape
   size_t attempt_smem = 0;  // dynamic shared bytes of the shared-memory variant
   int variant = 0;          // variant used for global-dt attempts
   double compile_ms = 0;    // NVRTC time (0 when the compiled image came from cache)
@@ -69,7 +70,8 @@ void jit_launch_rcp(const JitChem& J, cudaStream_t st, const double* x, double* 
 // same contract as launch_ros23_vjp in rs_kernels.h
 void jit_launch_vjp(const JitChem& J, cudaStream_t st, int nc, int nsp, const double* U,
                     const double* Uout, const double* lam, double* lam_out, const double* kr,
-                    const double* em, double* ebar, double dt, int clamp);
+                    const double* em, double* ebar, double dt, int clamp,
+                    const double* kz = nullptr);
 void jit_launch_per_cell(const JitChem& J, cudaStream_t st, int nc, int nsp, int nblocks,
                          int threads, double* U, const double* kr, const double* em,
                          double* dtc, double* steps, unsigned long long* queue, int* status,

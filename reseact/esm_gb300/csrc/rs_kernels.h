@@ -150,9 +150,10 @@ void launch_tape_store(cudaStream_t st, const Ctl* ctl, const double* U0, const 
 void launch_clamp_mask(cudaStream_t st, size_t n, double* lam, const double* out);
 
 // discrete adjoint (rs_adjoint.cu)
+// kz (optional, the specialised kernels only): the step's k1 and z2 from the stage tape
 void launch_ros23_vjp(const LaunchCtx& L, const double* U, const double* Uout, const double* lam,
                       double* lam_out, const double* kr, const double* em, double* ebar,
-                      double dt, int clamp);
+                      double dt, int clamp, const double* kz = nullptr);
 void launch_transport_rhs_vjp(cudaStream_t st, const DevTransport<double>& T, const double* U,
                               const double* F, const double* fbar, double* ubar, double* G,
                               double* Cf, double g);

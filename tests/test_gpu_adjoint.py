@@ -100,23 +100,27 @@ def _sweep(w, iO3, obs, kw, budget):
 
 
 def test_device_tape_equals_replay_bitwise():
-    """The forward's device tape (every accepted step's input kept in HBM) and the replay from
-    checkpoints give the same gradients bit for bit -- the replay reproduces the forward's
-    states exactly -- whether all, none or only the first recorded macro steps fit the tape."""
+    """The forward's device tape (every accepted step's input and chemistry stages kept in
+    HBM) and the replay from checkpoints give the same gradients bit for bit -- the replay
+    reproduces the forward's states and stages exactly -- whether all, none or only the first
+    recorded macro steps fit the tape."""
     w, iNO, iO3, obs, kw = _case()
     lg, eg, taped = _sweep(w, iO3, obs, kw, -1)
     assert taped == 3
     lr, er, taped0 = _sweep(w, iO3, obs, kw, 0)
     assert taped0 == 0
     assert np.array_equal(lg, lr) and np.array_equal(eg, er)
-    # room for a little more than one macro step's states: the first is taped, the rest replay
-    n = w.grid["nlon"] * w.grid["nlat"] * w.grid["nlev"] * w.nsp
+    # room for one macro step and one slot more: the first is taped, the rest replay.  The
+    # budget is shared by the states (nsp doubles per cell) and the chemistry stages k1, z2
+    # (2 ns doubles per cell) in proportion to their sizes
+    nc = w.grid["nlon"] * w.grid["nlat"] * w.grid["nlev"]
     s = Solver.for_workload(w, **kw)
     s.set_state(w.u0_cellmajor())
     s.record(True)
     st = s.macro_step(0.0, 600.0, 15.0, 0.5)[3]
     s.close()
     per_step = int(st.naT + st.naC + 1)
-    lp, ep, tapedp = _sweep(w, iO3, obs, kw, (per_step + 2) * n * 8)
+    budget = (per_step + 1) * (w.nsp + 2 * w.mech.ns) * nc * 8
+    lp, ep, tapedp = _sweep(w, iO3, obs, kw, budget)
     assert tapedp == 1
     assert np.array_equal(lg, lp) and np.array_equal(eg, ep)
