@@ -335,6 +335,8 @@ struct rs_handle {
     bool tape_ok = false;
     size_t kz_off = 0, kz_cap = 0;  // its chemistry stage slots (k1, z2 per accepted step)
     bool kz_ok = false;             // the forward wrote every chemistry step's stages
+    size_t f_off = 0, f_cap = 0;    // its transport stage slots (F0..F3, V1, V2, V4)
+    bool f_set = false, f_ok = false;
   };
   bool rec_on = false;
   // tape budget in bytes (-1: a quarter of the free device memory when recording starts,
@@ -348,6 +350,11 @@ struct rs_handle {
   // replay's scratch of the same layout
   DevBuf<double> kz_arena, kzs;
   size_t kz_limit = 0, kz_used = 0;
+  // the transport stage tape (FP64 scheme without PBL mixing): per accepted transport step
+  // the stage tendencies F0..F3 and stage states V1, V2, V4, [7][nsp][nc] doubles; its arena,
+  // and the replay's scratch of the same layout
+  DevBuf<double> f_arena, fs;
+  size_t f_limit = 0, f_used = 0;
   std::vector<Rec> recs;
   std::vector<DevBuf<double>> ck_pool;  // checkpoint buffers kept for reuse across recordings
   DevBuf<double> seqbuf, lam, lam2, ebar, tape, adj, G, Cf;
@@ -686,6 +693,12 @@ void build_pbl(rs_handle* h) {
   h->pbl_qbar.alloc((size_t)h->ntr * ncol);
 }
 
+// The transport stage tape applies to the FP64 scheme the adjoint differentiates, without PBL
+// mixing (whose VJP needs the advective tendency on its own).
+bool transport_stage_tape(const rs_handle* h) {
+  return h->cfg.do_transport && !h->pbl_on && h->cfg.precision == RS_PREC_FP64;
+}
+
 Ctl make_ctl(rs_handle* h, double t0, double t1, double dt0, const rs_controller& c,
              double ntot) {
   Ctl k{};
@@ -997,7 +1010,8 @@ void rs_destroy(rs_handle* h) {
   for (auto& r : h->recs) r.ck.release();
   for (auto& b : h->ck_pool) b.release();
   DevBuf<double>* abufs[] = {&h->seqbuf, &h->lam, &h->lam2, &h->ebar, &h->tape, &h->adj, &h->G,
-                             &h->Cf, &h->tape_arena, &h->kz_arena, &h->kzs};
+                             &h->Cf, &h->tape_arena, &h->kz_arena, &h->kzs, &h->f_arena,
+                             &h->fs};
   for (auto* b : abufs) b->release();
   h->nseq.release();
   h->ntape.release();
@@ -1200,6 +1214,8 @@ rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double*
       const size_t nkz = (size_t)2 * h->mt.ns * h->nc;
       r.kz_off = h->kz_used;
       r.kz_cap = h->kz_limit > h->kz_used ? (h->kz_limit - h->kz_used) / nkz : 0;
+      r.f_off = h->f_used;
+      r.f_cap = h->f_limit > h->f_used ? (h->f_limit - h->f_used) / (7 * n) : 0;
       h->ntape.alloc(4);
       CK(cudaMemsetAsync(h->ntape.p, 0, 4 * sizeof(int), h->st));
     }
@@ -1223,6 +1239,11 @@ rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double*
         init.seqcap = seqcap;
       }
       tape_half(init, 0, 0);
+      if (h->rec_on && transport_stage_tape(h) && h->recs.back().f_cap > 0) {
+        init.ftape = h->f_arena.p + h->recs.back().f_off;
+        init.fcap = (int)std::min<size_t>(h->recs.back().f_cap, 1u << 30);
+        h->recs.back().f_set = true;
+      }
       rs::launch_ctl_init(h->st, h->ctl.p + 0, init);
       h->launches += 1;
       if (h->use_graphs && !h->prof.on) run_adaptive_graph(h, 0);
@@ -1313,16 +1334,20 @@ rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double*
       // with the specialised kernels the chemistry stages must be complete too, so that every
       // step VJP reads its k1, z2 from a forward pass (the tape's or the replay's)
       const bool need_kz = h->lc.jit && ns_h[1] > 0;
+      const bool need_f = r.f_set && ns_h[0] > 0;
       r.tape_ok = h->tape_limit > 0 && nt[1] == 0 && nt[3] == 0 && nt[0] == ns_h[0] &&
                   nt[2] == ns_h[1] && used <= r.tape_cap &&
                   (ns_h[0] == 0 || h->cfg.do_transport) && (ns_h[1] == 0 || h->cfg.do_chemistry) &&
-                  (!need_kz || (size_t)ns_h[1] <= r.kz_cap);
+                  (!need_kz || (size_t)ns_h[1] <= r.kz_cap) &&
+                  (!need_f || (size_t)ns_h[0] <= r.f_cap);
       if (r.tape_ok) {
         CK(cudaMemcpyAsync(h->tape_arena.p + r.tape_off + (used - 1) * n, h->U[h->cur].p,
                            n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
         h->tape_used += used * n;
         if (need_kz) h->kz_used += (size_t)ns_h[1] * 2 * h->mt.ns * h->nc;
         r.kz_ok = need_kz;
+        if (need_f) h->f_used += (size_t)ns_h[0] * 7 * n;
+        r.f_ok = need_f;
       }
     }
     if (!okT || !okC) {
@@ -1490,8 +1515,10 @@ namespace {
 
 // SSPRK43 step VJP at fixed (t, dt): recompute the stage states, then walk the stages back
 // (the transpose of rx_traced_integrator.jl:404-437).  Buffers: adj = 11 state-sized slabs.
+// rec (optional): the step's transport stage record from the forward or the replay --
+// F0..F3 and V1, V2, V4, [7][n] -- in place of recomputing the stages here
 void transport_step_vjp(rs_handle* h, const double* u, double t, double dt, const double* lam,
-                        double* out) {
+                        double* out, const double* rec = nullptr) {
   size_t n = h->nc * h->nsp;
   double* V1 = h->adj.p + 0 * n;
   double* V2 = h->adj.p + 1 * n;
@@ -1513,30 +1540,37 @@ void transport_step_vjp(rs_handle* h, const double* u, double t, double dt, cons
   auto gf = [&](double tt) { return h->omega != 0.0 ? std::cos(h->omega * tt) : 1.0; };
   double h2 = dt / 2;
   cudaStream_t st = h->st;
-  rs::launch_transport_rhs(st, T, u, gf(t), F0, h->pbl_on ? Fa[0] : nullptr);
-  rs::launch_lincomb(st, n, V1, 1.0, u, h2, F0, 0.0, nullptr);
-  rs::launch_transport_rhs(st, T, V1, gf(t + 0.5 * dt), F1, h->pbl_on ? Fa[1] : nullptr);
-  rs::launch_lincomb(st, n, V2, 1.0, V1, h2, F1, 0.0, nullptr);
-  rs::launch_transport_rhs(st, T, V2, gf(t + 1.0 * dt), F2, h->pbl_on ? Fa[2] : nullptr);
-  rs::launch_lincomb(st, n, V4, 1.0, V2, h2, F2, 0.0, nullptr);        // u3
-  rs::launch_lincomb(st, n, V4, 2.0 / 3.0, u, 1.0 / 3.0, V4, 0.0, nullptr);  // u4
-  rs::launch_transport_rhs(st, T, V4, gf(t + h2), F3, h->pbl_on ? Fa[3] : nullptr);
+  const double* Fr[4] = {Fa[0], Fa[1], Fa[2], Fa[3]};
+  const double* Vr[3] = {V1, V2, V4};
+  if (rec) {
+    for (int q = 0; q < 4; ++q) Fr[q] = rec + (size_t)q * n;
+    for (int q = 0; q < 3; ++q) Vr[q] = rec + (size_t)(4 + q) * n;
+  } else {
+    rs::launch_transport_rhs(st, T, u, gf(t), F0, h->pbl_on ? Fa[0] : nullptr);
+    rs::launch_lincomb(st, n, V1, 1.0, u, h2, F0, 0.0, nullptr);
+    rs::launch_transport_rhs(st, T, V1, gf(t + 0.5 * dt), F1, h->pbl_on ? Fa[1] : nullptr);
+    rs::launch_lincomb(st, n, V2, 1.0, V1, h2, F1, 0.0, nullptr);
+    rs::launch_transport_rhs(st, T, V2, gf(t + 1.0 * dt), F2, h->pbl_on ? Fa[2] : nullptr);
+    rs::launch_lincomb(st, n, V4, 1.0, V2, h2, F2, 0.0, nullptr);        // u3
+    rs::launch_lincomb(st, n, V4, 2.0 / 3.0, u, 1.0 / 3.0, V4, 0.0, nullptr);  // u4
+    rs::launch_transport_rhs(st, T, V4, gf(t + h2), F3, h->pbl_on ? Fa[3] : nullptr);
+  }
   auto vjp = [&](const double* Us, const double* Fs, double g, const double* fbar, double* ub) {
     rs::launch_transport_rhs_vjp(st, T, Us, Fs, fbar, ub, h->G.p, h->Cf.p, g);
   };
   rs::launch_lincomb(st, n, Wb, h2, lam, 0.0, nullptr, 0.0, nullptr);
-  vjp(V4, Fa[3], gf(t + h2), Wb, A);
+  vjp(Vr[2], Fr[3], gf(t + h2), Wb, A);
   rs::launch_lincomb(st, n, A, 1.0, A, 1.0, lam, 0.0, nullptr);           // ubar4
   rs::launch_lincomb(st, n, out, 2.0 / 3.0, A, 0.0, nullptr, 0.0, nullptr);
   rs::launch_lincomb(st, n, B, 1.0 / 3.0, A, 0.0, nullptr, 0.0, nullptr);  // ubar3 = ubar2
   rs::launch_lincomb(st, n, Wb, h2, B, 0.0, nullptr, 0.0, nullptr);
-  vjp(V2, Fa[2], gf(t + 1.0 * dt), Wb, A);
+  vjp(Vr[1], Fr[2], gf(t + 1.0 * dt), Wb, A);
   rs::launch_lincomb(st, n, B, 1.0, B, 1.0, A, 0.0, nullptr);             // ubar2 -> ubar1
   rs::launch_lincomb(st, n, Wb, h2, B, 0.0, nullptr, 0.0, nullptr);
-  vjp(V1, Fa[1], gf(t + 0.5 * dt), Wb, A);
+  vjp(Vr[0], Fr[1], gf(t + 0.5 * dt), Wb, A);
   rs::launch_lincomb(st, n, B, 1.0, B, 1.0, A, 0.0, nullptr);             // ubar1 -> ubar0
   rs::launch_lincomb(st, n, Wb, h2, B, 0.0, nullptr, 0.0, nullptr);
-  vjp(u, Fa[0], gf(t), Wb, A);
+  vjp(u, Fr[0], gf(t), Wb, A);
   rs::launch_lincomb(st, n, out, 1.0, out, 1.0, B, 1.0, A);
 }
 
@@ -1579,16 +1613,27 @@ rs_status rs_record(rs_handle* h, int32_t on) {
       if (h->tape_budget < 0) {
         size_t fr = 0, tot = 0;
         CK(cudaMemGetInfo(&fr, &tot));
-        want = (fr + (h->tape_arena.n + h->kz_arena.n) * sizeof(double)) / 4;
+        want = (fr + (h->tape_arena.n + h->kz_arena.n + h->f_arena.n) * sizeof(double)) / 4;
       } else {
         want = (size_t)h->tape_budget;
       }
-      // states and chemistry stages share the budget in proportion to their sizes per step
-      // (the stages only with the specialised kernels, the only ones that write them)
-      const double nst = (double)h->nsp, nkz = h->lc.jit ? 2.0 * h->mt.ns : 0.0;
-      const size_t want_kz = (size_t)((double)want * nkz / (nst + nkz));
-      h->tape_limit = (want - want_kz) / sizeof(double);
+      // states, chemistry stages and transport stages share the budget in fixed proportions:
+      // their sizes per step, weighted for six chemistry steps per transport step (states:
+      // one per step, 7 per transport step; the chemistry stages only with the specialised
+      // kernels, the only ones that write them; the transport stages only for the FP64
+      // scheme without PBL mixing).  A macro step that overruns any of them is replayed.
+      const double ws = 7.0 * h->nsp;
+      const double wk = (h->lc.jit && h->cfg.do_chemistry) ? 12.0 * h->mt.ns : 0.0;
+      const double wf = transport_stage_tape(h) ? 7.0 * h->nsp : 0.0;
+      const size_t want_kz = (size_t)((double)want * wk / (ws + wk + wf));
+      const size_t want_f = (size_t)((double)want * wf / (ws + wk + wf));
+      h->tape_limit = (want - want_kz - want_f) / sizeof(double);
       h->kz_limit = want_kz / sizeof(double);
+      h->f_limit = want_f / sizeof(double);
+      if (h->f_limit > h->f_arena.n) {
+        h->f_arena.release();
+        h->f_arena.alloc(h->f_limit);
+      }
       if (h->tape_limit > h->tape_arena.n) {
         h->tape_arena.release();
         h->tape_arena.alloc(h->tape_limit);
@@ -1599,6 +1644,7 @@ rs_status rs_record(rs_handle* h, int32_t on) {
       }
       h->tape_used = 0;
       h->kz_used = 0;
+      h->f_used = 0;
     }
     h->rec_on = on != 0;
     // the device loops with the tape kernels, built now rather than in the first recorded
@@ -1689,16 +1735,26 @@ rs_status rs_backward_macro_step(rs_handle* h, int32_t k) {
     const size_t nkz = (size_t)2 * h->mt.ns * h->nc;
     const bool use_kz = h->lc.jit != nullptr && nC > 0;
     double* kzb = nullptr;
+    // F0..F3, V1, V2, V4 of every transport step: the forward's stage tape, or the replay's
+    const bool use_f = transport_stage_tape(h) && nT > 0;
+    double* fb = nullptr;
     if (r.tape_ok) {  // the forward stored every step's input and the end state
       tape = h->tape_arena.p + r.tape_off;
       fin = tape + (size_t)(nT + nC) * n;
       if (use_kz && r.kz_ok) kzb = h->kz_arena.p + r.kz_off;
+      if (use_f && r.f_ok) fb = h->f_arena.p + r.f_off;
     } else {
     if (use_kz) {
       size_t mostC = 0;
       for (const auto& q : h->recs) mostC = std::max(mostC, q.seqC.size() / 2);
       h->kzs.alloc(mostC * nkz);
       kzb = h->kzs.p;
+    }
+    if (use_f) {
+      size_t mostT = 0;
+      for (const auto& q : h->recs) mostT = std::max(mostT, q.seqT.size() / 2);
+      h->fs.alloc(mostT * 7 * n);
+      fb = h->fs.p;
     }
     // one tape for the largest recorded macro step (no reallocation during a sweep)
     size_t most = 0;
@@ -1725,6 +1781,10 @@ rs_status rs_backward_macro_step(rs_handle* h, int32_t k) {
       if (!tr && kzb) {  // the step writes its k1, z2 to its own slot (accepted count 0)
         init.kz = kzb + (size_t)(j - nT) * nkz;
         init.kzcap = 1;
+      }
+      if (tr && fb) {  // the step writes its stage record to its own slot
+        init.ftape = fb + (size_t)j * 7 * n;
+        init.fcap = 1;
       }
       rs::launch_ctl_init(st, c, init);
       if (tr) {
@@ -1760,7 +1820,7 @@ rs_status rs_backward_macro_step(rs_handle* h, int32_t k) {
     for (int j = nT - 1; j >= 0; --j) {
       if (clamp) rs::launch_clamp_mask(st, n, h->lam.p, out_of(j));
       transport_step_vjp(h, tape + (size_t)j * n, r.seqT[2 * j], r.seqT[2 * j + 1], h->lam.p,
-                         h->lam2.p);
+                         h->lam2.p, fb ? fb + (size_t)j * 7 * n : nullptr);
       std::swap(h->lam.p, h->lam2.p);
     }
     CK(cudaGetLastError());

@@ -91,6 +91,13 @@ struct Ctl {
   double* kz;
   int kzcap;
   int pad3;
+  // if set (transport, FP64 scheme without PBL mixing): every attempt's stage kernels write
+  // the stage tendencies F0..F3 and the stage states V1, V2, V4 ([7][nsp][nc] doubles) to
+  // ftape + slot * 7 nsp nc, slot = the accepted count, while slot < fcap -- the transport
+  // stage tape
+  double* ftape;
+  int fcap;
+  int pad4;
 };
 
 __device__ __forceinline__ double ld(const double* p) { return __ldg(p); }

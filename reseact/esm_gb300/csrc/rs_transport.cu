@@ -1349,6 +1349,19 @@ __global__ void __launch_bounds__(kRedThreads) k_stage(DevTransport<double> T,
   const double* Qin = STAGE == 1 ? U : (STAGE == 2 ? B.S1 : (STAGE == 3 ? B.S2 : B.S3));
   const size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
   size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  // transport stage tape (recording): this stage's tendency at Fo, its output state (stages
+  // 1-3: V1, V2, V4) at Vo, in the slot of the accepted count
+  double* Fo = nullptr;
+  double* Vo = nullptr;
+  if (ctl->ftape) {
+    const int slot = (int)ctl->nacc;
+    if (slot >= 0 && slot < ctl->fcap) {
+      const size_t nst = nc * (size_t)T.nsp;
+      double* rec = ctl->ftape + (size_t)slot * 7 * nst;
+      Fo = rec + (size_t)(STAGE - 1) * nst;
+      if (STAGE < 4) Vo = rec + (size_t)(3 + STAGE) * nst;
+    }
+  }
   double e = 0.0;
   if (c < nc) {
     int i = (int)(c % T.nlon);
@@ -1394,6 +1407,7 @@ __global__ void __launch_bounds__(kRedThreads) k_stage(DevTransport<double> T,
       double du;
 #if !RS_STRICT
       double scale = dt_2;
+      bool per_m = false;  // du is the tendency times m (1/m folded into the scale)
 #endif
       if (s < T.ntr) {
         double fw = T.fx[s * fxp + fxi], fe = T.fx[s * fxp + fxi + 1];
@@ -1414,6 +1428,7 @@ __global__ void __launch_bounds__(kRedThreads) k_stage(DevTransport<double> T,
         } else {
           du = ab;
           scale = sc;
+          per_m = true;
         }
 #endif
       } else {
@@ -1421,14 +1436,18 @@ __global__ void __launch_bounds__(kRedThreads) k_stage(DevTransport<double> T,
       }
 #if RS_STRICT
       const double nx = q + dt_2 * du;
+      if (Fo) Fo[x] = du;
 #else
       const double nx = fma(du, scale, q);
+      if (Fo) Fo[x] = per_m ? du * rm : du;
 #endif
       if (STAGE == 1) {
         B.S1[x] = nx;
+        if (Vo) Vo[x] = nx;
         if (T.mixed && s < T.ntr) split_store(T, x, nx);
       } else if (STAGE == 2) {
         B.S2[x] = nx;
+        if (Vo) Vo[x] = nx;
         if (T.mixed && s < T.ntr) split_store(T, x, nx);
       } else if (STAGE == 3) {
         double u3 = nx;
@@ -1436,6 +1455,7 @@ __global__ void __launch_bounds__(kRedThreads) k_stage(DevTransport<double> T,
         B.S1[x] = u3;
         double u4 = (2.0 / 3.0) * u0 + (1.0 / 3.0) * u3;
         B.S3[x] = u4;
+        if (Vo) Vo[x] = u4;
         if (T.mixed && s < T.ntr) split_store(T, x, u4);
       } else {
         double u0 = U[x];

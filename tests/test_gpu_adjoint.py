@@ -100,27 +100,29 @@ def _sweep(w, iO3, obs, kw, budget):
 
 
 def test_device_tape_equals_replay_bitwise():
-    """The forward's device tape (every accepted step's input and chemistry stages kept in
-    HBM) and the replay from checkpoints give the same gradients bit for bit -- the replay
-    reproduces the forward's states and stages exactly -- whether all, none or only the first
-    recorded macro steps fit the tape."""
+    """The forward's device tape (every accepted step's input, chemistry stages and transport
+    stage records kept in HBM) and the replay from checkpoints give the same gradients bit for
+    bit -- the replay reproduces the forward's states and stages exactly -- whether all, none
+    or only the first recorded macro steps fit the tape."""
     w, iNO, iO3, obs, kw = _case()
     lg, eg, taped = _sweep(w, iO3, obs, kw, -1)
     assert taped == 3
     lr, er, taped0 = _sweep(w, iO3, obs, kw, 0)
     assert taped0 == 0
     assert np.array_equal(lg, lr) and np.array_equal(eg, er)
-    # room for one macro step and one slot more: the first is taped, the rest replay.  The
-    # budget is shared by the states (nsp doubles per cell) and the chemistry stages k1, z2
-    # (2 ns doubles per cell) in proportion to their sizes
+    # room for the first macro step and half of another: the first is taped, the rest replay.
+    # A macro step needs its states (nsp doubles per cell, one per step and the end state), the
+    # chemistry stages k1, z2 (2 ns per cell and chemistry step) and the transport stage
+    # records (7 nsp per cell and transport step); the three share the budget in fixed
+    # proportions close to these
     nc = w.grid["nlon"] * w.grid["nlat"] * w.grid["nlev"]
     s = Solver.for_workload(w, **kw)
     s.set_state(w.u0_cellmajor())
     s.record(True)
     st = s.macro_step(0.0, 600.0, 15.0, 0.5)[3]
     s.close()
-    per_step = int(st.naT + st.naC + 1)
-    budget = (per_step + 1) * (w.nsp + 2 * w.mech.ns) * nc * 8
-    lp, ep, tapedp = _sweep(w, iO3, obs, kw, budget)
+    nT, nC = int(st.naT), int(st.naC)
+    need = ((nT + nC + 1) * w.nsp + nC * 2 * w.mech.ns + nT * 7 * w.nsp) * nc * 8
+    lp, ep, tapedp = _sweep(w, iO3, obs, kw, int(1.5 * need))
     assert tapedp == 1
     assert np.array_equal(lg, lp) and np.array_equal(eg, ep)
