@@ -345,11 +345,12 @@ rs_status rs_record(rs_handle* h, int32_t on);
 int32_t rs_record_count(const rs_handle* h);
 /* Device tape of the recording (no reference counterpart; the reference replays from its
  * checkpoints).  While recording, the forward also stores the state before every accepted
- * step and each macro step's end state, and -- with the specialised chemistry kernels -- the
- * stage vectors k1, z2 of every accepted chemistry step, which the step VJPs then read instead
- * of recomputing.  States and stages share budget_bytes of device memory in proportion to
- * their sizes, in arenas reserved by rs_record(h, 1): -1 (the default) for a quarter of the
- * free device memory, 0 for none.  A recorded macro step whose tape is complete is swept back
+ * step and each macro step's end state; with the specialised chemistry kernels the stage
+ * vectors k1, z2 of every accepted chemistry step; and for the FP64 scheme without PBL
+ * mixing the stage tendencies and states of every accepted transport step.  The step VJPs
+ * read the stages instead of recomputing them.  The three share budget_bytes of device
+ * memory in fixed proportions, in arenas reserved by rs_record(h, 1): -1 (the default) for a
+ * quarter of the free device memory, 0 for none.  A recorded macro step whose tape is complete is swept back
  * without the replay -- the same bits, since the replay reproduces the forward's states and
  * stages exactly; one that did not fit (or any step, with budget 0) is replayed from its
  * checkpoint.  Takes effect at the next rs_record(h, 1).  rs_record_taped counts the recorded
