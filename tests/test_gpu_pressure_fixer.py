@@ -100,3 +100,38 @@ def test_fixer_needs_steady_fluxes():
     with pytest.raises(RsError) as e:
         Solver.for_workload(w)
     assert e.value.status == abi.RS_ERR_UNSUPPORTED
+
+
+def test_adjoint_with_fixer_matches_oracle_taped_or_replayed(oracle_mod):
+    """The discrete adjoint with the pressure fixer (its correction enters the air-mass
+    tendency but not the state derivative) against the oracle, with the device tape and with
+    the replay -- the transport stage records carry the corrected air-mass tendency."""
+    w = _w()
+    g = w.grid
+    iO3 = w.mech.species.index("O3")
+    grads = []
+    for budget in (-1, 0):
+        s, o = _pair(w, oracle_mod)
+        s.set_adjoint_tape(budget)
+        s.set_state(w.u0_cellmajor())
+        s.record(True)
+        u = np.ascontiguousarray(w.u0.copy())
+        t, a, b, ao, bo = 0.0, 15.0, 0.5, 15.0, 0.5
+        for _ in range(2):
+            _, a, b, st = s.macro_step(t, t + 600.0, a, b)
+            orc, ao, bo, ost = o.record_macro_step(u, t, t + 600.0, ao, bo)
+            assert (st.naT, st.naC) == (ost[0], ost[2])
+            t += 600.0
+        s.record(False)
+        assert s.record_taped() == (2 if budget else 0)
+        uend = workloads.cellmajor_to_soa(s.get_state(), w.nsp, g["nlon"], g["nlat"], g["nlev"])
+        lam = np.zeros_like(uend)
+        lam[iO3, 0] = 2 * uend[iO3, 0]
+        lg, _ = s.adjoint_backward(cm(w, lam))
+        lo, _ = o.adjoint_backward(lam)
+        lo = cm(w, lo)
+        scale = np.abs(lo).max()
+        assert np.abs(lg - lo).max() <= 1e-8 * scale, np.abs(lg - lo).max() / scale
+        grads.append(lg)
+        s.close()
+    assert np.array_equal(grads[0], grads[1])
