@@ -1219,8 +1219,8 @@ rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double*
       h->ntape.alloc(4);
       CK(cudaMemsetAsync(h->ntape.p, 0, 4 * sizeof(int), h->st));
     }
-    // slots of the device tape for the half about to run (before, the half's first state is
-    // `first`; one slot stays for the end state)
+    // device-tape slots for the half about to run: its steps' inputs from slot `first` on
+    // (the transport half's steps come first), one slot kept for the macro step's end state
     auto tape_half = [&](Ctl& init, size_t first, int half) {
       if (!h->rec_on) return;
       const auto& r = h->recs.back();
