@@ -727,8 +727,9 @@ __global__ void __launch_bounds__(256) k_adj_pencil(DevTransport<double> T,
     //    covers positions f-3 .. f+2, so each image p is reached only by faces p-2 .. p+3; for
     //    n >= 6 these face ranges are disjoint and ascending with the images, and each face
     //    reaches pos through exactly one position -- the same faces in the same order as the
-    //    general loop below, without its divergent window scan at the row ends.  Mirror walls
-    //    (a face can reach a cell next to the wall twice) and short pencils take that loop.
+    //    general loop below, without its divergent window scan at the row ends.  Next to a
+    //    mirror wall a face can reach the cell twice (itself and its reflection); those cells
+    //    scan the faces that reach either, and short pencils take the general loop.
     for (int pos = lane0; pos < n; pos += lstride) {
       if (!live) break;
       const bool end = pos < 3 || pos > n - 4;
@@ -742,6 +743,24 @@ __global__ void __launch_bounds__(256) k_adj_pencil(DevTransport<double> T,
             const int o = img - AV(upf, f) + 2;
             if (o >= 0 && o <= 4) acc = acc + AV(C, o * (n + 1) + f);
           }
+        }
+        ubar[(size_t)s * nc + cell(pos)] += acc;
+        continue;
+      }
+      if (bc == 2 && n >= 6) {
+        // mirror walls: positions pos and its reflection r (-1-pos below, 2n-1-pos above) map
+        // to this cell.  Faces ascending over those that can reach either, and per face the
+        // two candidate positions ascending (r < pos below the wall, pos < r above): the
+        // general loop's terms in its order.
+        const int r = pos < 3 ? -1 - pos : 2 * n - 1 - pos;
+        const int p0 = r < pos ? r : pos, p1 = r < pos ? pos : r;
+        const int fa = p0 - 2 < 0 ? 0 : p0 - 2, fb = p1 + 3 > n ? n : p1 + 3;
+        double acc = 0.0;
+        for (int f = fa; f <= fb; ++f) {
+          const int up = AV(upf, f);
+          const int o0 = p0 - up + 2, o1 = p1 - up + 2;
+          if (o0 >= 0 && o0 <= 4) acc = acc + AV(C, o0 * (n + 1) + f);
+          if (o1 >= 0 && o1 <= 4) acc = acc + AV(C, o1 * (n + 1) + f);
         }
         ubar[(size_t)s * nc + cell(pos)] += acc;
         continue;
