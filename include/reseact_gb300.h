@@ -63,7 +63,9 @@ typedef enum rs_status {
 
 /* lateral boundary kinds */
 enum { RS_BC_PERIODIC = 0, RS_BC_OPEN = 1, RS_BC_CLOSED = 2 };
-/* arithmetic of the transport half */
+/* arithmetic of the transport half: FP64, or MIXED = compensated FP32 (the PPM reconstruction
+ * and face terms in double-float pairs on the FP32 pipe, about 48 significant bits; the state,
+ * air mass, stage updates and error norm in FP64) */
 enum { RS_PREC_FP64 = 0, RS_PREC_MIXED = 1 };
 /* chemistry step-size control: one global dt (reference) or per-cell adaptive substeps */
 enum { RS_CHEM_GLOBAL_DT = 0, RS_CHEM_PER_CELL = 1 };

@@ -124,12 +124,15 @@ def _declare(L):
     return L
 
 
-def load(strict=False, build_if_missing=True):
-    """Load (building in-tree if needed) the production or strict-arithmetic library."""
-    key = bool(strict)
+def load(strict=False, build_if_missing=True, check=False):
+    """Load (building in-tree if needed) the production or strict-arithmetic library, or the
+    bounds-check build of the production arithmetic (check=True, built on first use)."""
+    key = "check" if check else bool(strict)
     if key in _LIBS:
         return _LIBS[key]
-    path = build.lib_path(strict)
+    path = build.lib_path(strict, check)
+    if check and build_if_missing:
+        build.build(only=[build.CHECK_LIB])
     if not os.path.exists(path):
         if not build_if_missing:
             raise RuntimeError("CUDA library %s is missing; run build()" % path)
@@ -179,8 +182,8 @@ def chem_kernel_compile(mech_abi, strict=False):
 class Solver:
     """One rs_handle: a grid + mechanism + forcing resident on the GPU."""
 
-    def __init__(self, config, mech_abi, strict=False):
-        self.L = load(strict)
+    def __init__(self, config, mech_abi, strict=False, check=False):
+        self.L = load(strict, check=check)
         self._keep = [mech_abi]
         self.cfg = config
         h = C.c_void_p()
@@ -196,9 +199,9 @@ class Solver:
         self.nr = config.mech.n_reactions
 
     @classmethod
-    def for_workload(cls, w, strict=False, **cfg_kw):
+    def for_workload(cls, w, strict=False, check=False, **cfg_kw):
         mabi = abi.MechanismABI(w.mech)
-        s = cls(w.config(mabi, **cfg_kw), mabi, strict=strict)
+        s = cls(w.config(mabi, **cfg_kw), mabi, strict=strict, check=check)
         s.set_forcing(w.forcing_abi())
         return s
 

@@ -5,6 +5,8 @@ Two builds of the same sources:
   _build/libreseact_gb300_strict.so  --fmad=false and -DRS_STRICT=1: divides where the
                                      reference divides, no contraction; bit-compatible with
                                      the CPU restatement given identical rate constants.
+and on demand a third, _build/libreseact_gb300_check.so (-DRS_BOUNDS_CHECK=1), the production
+arithmetic with index checks in the transport pencils.
 Host code is compiled with -ffp-contract=off so the geometry and PPM coefficient tables are
 identical on x86_64 and aarch64.  Translation units compile in parallel.
 """
@@ -22,6 +24,11 @@ SOURCES = ["rs_api.cu", "rs_chem.cu", "rs_transport.cu", "rs_control.cu", "rs_ad
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 LIBS = {"libreseact_gb300.so": ["--fmad=true", "-DRS_STRICT=0"],
         "libreseact_gb300_strict.so": ["--fmad=false", "-DRS_STRICT=1"]}
+# Bounds-check build of the production arithmetic: the transport pencils check every
+# shared-memory row, halo load and bulk-copy box start and report a failed check as a status
+# (no trap).  Built on demand by the tests that use it (build(only=[CHECK_LIB])).
+CHECK_LIB = "libreseact_gb300_check.so"
+CHECK_FLAGS = ["--fmad=true", "-DRS_STRICT=0", "-DRS_BOUNDS_CHECK=1"]
 
 
 def nvcc():
@@ -41,7 +48,9 @@ def _compile(args):
     return obj, r.stderr
 
 
-def lib_path(strict=False):
+def lib_path(strict=False, check=False):
+    if check:
+        return os.path.join(OUT, CHECK_LIB)
     return os.path.join(OUT, "libreseact_gb300_strict.so" if strict else "libreseact_gb300.so")
 
 
@@ -58,7 +67,10 @@ def up_to_date(lib):
 def build(force=False, verbose=False, only=None):
     os.makedirs(OUT, exist_ok=True)
     jobs, links = [], []
-    for lib, flags in LIBS.items():
+    libs = dict(LIBS)
+    if only and CHECK_LIB in only:
+        libs[CHECK_LIB] = CHECK_FLAGS
+    for lib, flags in libs.items():
         if only and lib not in only:
             continue
         path = os.path.join(OUT, lib)

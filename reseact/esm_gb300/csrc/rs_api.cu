@@ -306,7 +306,8 @@ struct rs_handle {
   DevBuf<double> U[2], S1, S2, S3, fx, fy, fz, partial, krates, T, P, emis, io, io2;
   DevBuf<double> mx, my, mz, qw, qe, qs, qn, gx, gylo, gyhi, vsA, vsB, veAB, veC, veD, dtcell,
       stepcell, totals;
-  DevBuf<float> qhi, qlo, vsA32, vsB32, veAB32, veC32, veD32;  // mixed-precision transport
+  DevBuf<float> qhi, qlo;  // mixed-precision transport: split planes
+  DevBuf<float> gx2, gylo2, gyhi2, vsA2, vsB2, veAB2, veC2, veD2;  // (hi, lo) pairs
   rs::MixedTmaps* tmaps = nullptr;  // bulk-copy staging of the mixed pencils (null: unavailable)
   std::string tmaps_why;
   int staging = RS_STAGING_AUTO;
@@ -497,6 +498,19 @@ void build_device_mech(rs_handle* h) {
   h->slot_col.upload(T.slot_col.data(), T.slot_col.size(), h->st);
 }
 
+// (hi, lo) float pairs of a double array for the compensated FP32 transport:
+// hi = fl32(v), lo = fl32(v - hi); hi + lo = v to about 2^-48 relative
+void upload_pairs(const std::vector<double>& v, DevBuf<float>& d, cudaStream_t st) {
+  std::vector<float> w(2 * v.size());
+  for (size_t i = 0; i < v.size(); ++i) {
+    const float hi = (float)v[i];
+    w[2 * i] = hi;
+    w[2 * i + 1] = (float)(v[i] - (double)hi);
+  }
+  d.upload(w.data(), w.size(), st);
+  CK(cudaStreamSynchronize(st));  // w is a temporary
+}
+
 // Lat-lon geometry on the unit sphere (same formulas and order as the CPU restatement).
 void build_geometry(rs_handle* h) {
   const rs_grid& g = h->cfg.grid;
@@ -522,6 +536,11 @@ void build_geometry(rs_handle* h) {
   h->gx_host = gx;
   h->gylo_host = gl;
   h->gyhi_host = gh;
+  if (h->cfg.precision == RS_PREC_MIXED) {
+    upload_pairs(gx, h->gx2, h->st);
+    upload_pairs(gl, h->gylo2, h->st);
+    upload_pairs(gh, h->gyhi2, h->st);
+  }
 }
 
 // CW84 nonuniform coefficients from dp (eqs. 1.6-1.7), mirror ghosts at the no-flux walls.
@@ -561,12 +580,11 @@ void build_vertical(rs_handle* h) {
   h->veC.upload(eC.data(), eC.size(), h->st);
   h->veD.upload(eD.data(), eD.size(), h->st);
   if (h->cfg.precision == RS_PREC_MIXED) {
-    auto f32 = [&](const std::vector<double>& v, DevBuf<float>& d) {
-      std::vector<float> w(v.begin(), v.end());
-      d.upload(w.data(), w.size(), h->st);
-      CK(cudaStreamSynchronize(h->st));  // w is a temporary
-    };
-    f32(sA, h->vsA32); f32(sB, h->vsB32); f32(eAB, h->veAB32); f32(eC, h->veC32); f32(eD, h->veD32);
+    upload_pairs(sA, h->vsA2, h->st);
+    upload_pairs(sB, h->vsB2, h->st);
+    upload_pairs(eAB, h->veAB2, h->st);
+    upload_pairs(eC, h->veC2, h->st);
+    upload_pairs(eD, h->veD2, h->st);
   }
   CK(cudaStreamSynchronize(h->st));  // the host vectors above are temporaries
 }
@@ -584,8 +602,11 @@ void refresh_dt(rs_handle* h) {
   T.fx = h->fx.p; T.fy = h->fy.p; T.fz = h->fz.p;
   T.mixed = h->cfg.precision == RS_PREC_MIXED;
   T.qhi = h->qhi.p; T.qlo = h->qlo.p;
-  T.vsA32 = h->vsA32.p; T.vsB32 = h->vsB32.p; T.veAB32 = h->veAB32.p; T.veC32 = h->veC32.p;
-  T.veD32 = h->veD32.p;
+  auto f2 = [](const DevBuf<float>& b) { return reinterpret_cast<const float2*>(b.p); };
+  T.gx2 = f2(h->gx2); T.gylo2 = f2(h->gylo2); T.gyhi2 = f2(h->gyhi2);
+  T.vsA2 = f2(h->vsA2); T.vsB2 = f2(h->vsB2); T.veAB2 = f2(h->veAB2); T.veC2 = f2(h->veC2);
+  T.veD2 = f2(h->veD2);
+  T.acc = T.mixed ? reinterpret_cast<float2*>(h->fx.p) : nullptr;  // ntr*nc pairs fit in fx
   T.pencil = h->tune.pencil;
   T.rows = h->tune.rows;
   T.xthreads = h->tune.xthreads;
@@ -904,6 +925,15 @@ rs_status rs_create(const rs_config* cfg, rs_handle** out) {
         throw RsError(RS_ERR_INVALID, "transport needs nlon, nlat, nlev >= 3");
       if (cfg->precision != RS_PREC_FP64 && cfg->precision != RS_PREC_MIXED)
         throw RsError(RS_ERR_INVALID, "precision");
+      // the compensated FP32 pencils keep a whole lon row / 16 lat or vertical pencils in
+      // shared memory
+      if (cfg->precision == RS_PREC_MIXED &&
+          (rs::mixed_pencil_bytes(g.nlon, 1, false) > rs::mixed_pencil_cap() ||
+           rs::mixed_pencil_bytes(g.nlat, 16, false) > rs::mixed_pencil_cap() ||
+           rs::mixed_pencil_bytes(g.nlev, 16, false) > rs::mixed_pencil_cap()))
+        throw RsError(RS_ERR_UNSUPPORTED,
+                      "mixed precision needs lon rows and 16-wide lat / vertical pencils that fit "
+                      "in shared memory (nlon <= 6365, nlat and nlev <= 391)");
     }
     if (cfg->maxiters < 1) throw RsError(RS_ERR_INVALID, "maxiters");
     CK(cudaSetDevice(cfg->device));
@@ -995,8 +1025,8 @@ void rs_destroy(rs_handle* h) {
   if (h->cap) cudaStreamDestroy(h->cap);
   for (auto& b : h->itabs) b.release();
   for (auto& b : h->dtabs) b.release();
-  DevBuf<float>* fbufs[] = {&h->qhi, &h->qlo, &h->vsA32, &h->vsB32, &h->veAB32, &h->veC32,
-                            &h->veD32};
+  DevBuf<float>* fbufs[] = {&h->qhi, &h->qlo, &h->gx2, &h->gylo2, &h->gyhi2, &h->vsA2,
+                            &h->vsB2, &h->veAB2, &h->veC2, &h->veD2};
   for (auto* b : fbufs) b->release();
   DevBuf<double>* bufs[] = {&h->U[0], &h->U[1], &h->S1, &h->S2, &h->S3, &h->fx, &h->fy, &h->fz,
                             &h->partial, &h->krates, &h->T, &h->P, &h->emis, &h->io, &h->io2,
@@ -1161,7 +1191,11 @@ rs_status rs_set_rate_constants(rs_handle* h, const double* k, size_t n) {
   });
 }
 
-// A mixed pencil kernel whose bulk-copy wait ran out sets tma_err and stops the solve.
+#ifndef RS_BOUNDS_CHECK
+#define RS_BOUNDS_CHECK 0
+#endif
+// A mixed pencil kernel whose bulk-copy wait ran out sets bit 1 of tma_err and stops the
+// solve; in the bounds-check build a pencil kernel whose index check failed sets bit 2.
 static void check_staging(rs_handle* h) {
   if (!h->tma_err.p) return;
   int e = 0;
@@ -1170,6 +1204,8 @@ static void check_staging(rs_handle* h) {
   e = *h->hflag;
   if (e) {
     CK(cudaMemsetAsync(h->tma_err.p, 0, sizeof(int), h->st));
+    if (e & 2)
+      throw RsError(RS_ERR_INVALID, "a transport kernel's index check failed (bounds-check build)");
     throw RsError(RS_ERR_CUDA, "a transport pencil's bulk-copy wait timed out; solve stopped");
   }
 }
@@ -1360,6 +1396,7 @@ rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double*
     CK(cudaMemcpyAsync(h->hflag, h->flag.p, sizeof(int), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
     if (*h->hflag) throw RsError(RS_ERR_NONFINITE, "non-finite state after the macro step");
+    if (RS_BOUNDS_CHECK) check_staging(h);
   });
   stats.status = rc;
   stats.kernel_launches = h->launches;
@@ -1381,7 +1418,7 @@ rs_status rs_rhs_transport(rs_handle* h, double t, const double* u, double* du, 
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(du, h->io2.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
-    if (h->tmaps) check_staging(h);
+    if (h->tmaps || RS_BOUNDS_CHECK) check_staging(h);
   });
 }
 

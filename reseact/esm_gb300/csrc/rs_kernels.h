@@ -56,15 +56,20 @@ struct DevTransport {
   R* fx;               // [ntr][nlev][nlat][nlon+1]
   R* fy;               // [ntr][nlev][nlat+1][nlon]
   R* fz;               // [ntr][nlev+1][nlat][nlon]
-  // mixed precision: the RHS input split into hi = fl(q), lo = fl(q - hi) planes [ntr][nc],
-  // and FP32 copies of the vertical coefficients
+  // mixed precision (compensated FP32): the RHS input split into hi, lo planes [ntr][nc]
+  // (hi + lo = q to 2^-47), the metric factors and vertical coefficients as (hi, lo) pairs, and
+  // the per-cell accumulator of m dq/dt as pairs [ntr][nc] (in the memory of fx)
   float* qhi;
   float* qlo;
-  const float* vsA32;
-  const float* vsB32;
-  const float* veAB32;
-  const float* veC32;
-  const float* veD32;
+  const float2* gx2;    // [nlat]
+  const float2* gylo2;  // [nlat]
+  const float2* gyhi2;  // [nlat]
+  const float2* vsA2;   // as vsA / vsB / veAB / veC / veD
+  const float2* vsB2;
+  const float2* veAB2;
+  const float2* veC2;
+  const float2* veD2;
+  float2* acc;
   int mixed;
   // full PBL mixing (transport half): per-layer fraction f and weight w = dp*f, the column
   // normaliser max(sum_k w, 1 Pa), scratch for the per-tracer column means, 1/tau
@@ -134,6 +139,9 @@ void launch_transport_rhs(cudaStream_t st, const DevTransport<double>& T, const 
 // Tensor maps for the bulk-copy staging of the mixed pencils over T.qhi / T.qlo; null (and the
 // reason in *why) where the grid does not meet the copy engine's alignment and size rules.
 MixedTmaps* mixed_tmaps_create(const DevTransport<double>& T, const char** why);
+// Dynamic shared memory of a mixed-precision pencil block (pw = 1: a lon row) and the cap.
+size_t mixed_pencil_bytes(int n, int pw, bool tma);
+size_t mixed_pencil_cap();
 void mixed_tmaps_destroy(MixedTmaps* m);
 bool mixed_tmaps_dir_ok(const MixedTmaps* m, int dir);  // dir 0 lon rows, 1 lat, 2 vertical
 void launch_flux_dir(cudaStream_t st, const DevTransport<double>& T, const double* Q, int dir);

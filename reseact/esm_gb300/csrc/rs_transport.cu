@@ -196,54 +196,28 @@ __device__ __forceinline__ double ppm_face_u(const double* v, bool right) {
   return right ? aR : aL;
 }
 
-// ---- mixed precision: the same reconstruction in FP32 on deviations from the upwind cell.
-// PPM is translation-equivariant (slopes, edges and limiter tests use differences only), so
-// subtracting the upwind value a2 from the stencil changes nothing in exact arithmetic; the
-// deviations d_o = (hi_o - hi_2) + (lo_o - lo_2) come from the split (hi, lo) state planes
-// without any FP64 instruction, FP32 then carries ~1e-7 relative error of the DEVIATION (not
-// of q), and the face value is a2 + dev in FP64.  q == 1 gives d == 0 and a face of exactly 1.
-__device__ __forceinline__ float slope_uf(float am, float a, float ap) {
-  float d0 = a - am, d1 = ap - a;
-  if (d1 * d0 > 0.0f) {
-    float da = 0.5f * (ap - am);
-    float lim = fminf(2.0f * fabsf(d0), 2.0f * fabsf(d1));
-    return copysignf(fminf(fabsf(da), lim), da);
-  }
-  return 0.0f;
-}
-__device__ __forceinline__ float slope_nf(float am, float a, float ap, float sA, float sB) {
-  float d0 = a - am, d1 = ap - a;
-  if (d1 * d0 > 0.0f) {
-    float da = sA * d1 + sB * d0;
-    float lim = fminf(2.0f * fabsf(d0), 2.0f * fabsf(d1));
-    return copysignf(fminf(fabsf(da), lim), da);
-  }
-  return 0.0f;
-}
-__device__ __forceinline__ void limitf(float a, float& aL, float& aR) {
-  if ((aR - a) * (a - aL) <= 0.0f) {
-    aL = a;
-    aR = a;
-  } else {
-    float dA = aR - aL;
-    float a6 = 6.0f * (a - 0.5f * (aL + aR));
-    if (dA * a6 > dA * dA) aL = 3.0f * a - 2.0f * aR;
-    else if (-(dA * dA) > dA * a6) aR = 3.0f * a - 2.0f * aL;
-  }
-}
-__device__ __forceinline__ float ppm_face_uf(const float* v, bool right) {
-  float dm1 = slope_uf(v[0], v[1], v[2]);
-  float d0 = slope_uf(v[1], v[2], v[3]);
-  float dp1 = slope_uf(v[2], v[3], v[4]);
-  float aL = v[1] + 0.5f * (v[2] - v[1]) - (d0 - dm1) * (1.0f / 6.0f);
-  float aR = v[2] + 0.5f * (v[3] - v[2]) - (dp1 - d0) * (1.0f / 6.0f);
-  limitf(v[2], aL, aR);
-  return right ? aR : aL;
-}
 // split a double into hi + lo floats (used only for boundary ghosts in the flux kernels)
 __device__ __forceinline__ void split_d(double x, float& hi, float& lo) {
   hi = (float)x;
   lo = (float)(x - (double)hi);
+}
+
+// Bounds-check build (-DRS_BOUNDS_CHECK=1): the pencil kernels check every shared-memory row
+// index, every halo / ghost load and every bulk-copy box start against its array.  An index
+// outside [0, n) sets bit 2 of the handle's staging word (T.tma_err) and is replaced by 0, so
+// the access stays inside the array; the host reports RS_ERR_INVALID after the step.  The
+// other builds compile the checks away.
+#ifndef RS_BOUNDS_CHECK
+#define RS_BOUNDS_CHECK 0
+#endif
+__device__ __forceinline__ long long bck(const DevTransport<double>& T, long long i, long long n) {
+#if RS_BOUNDS_CHECK
+  if (i < 0 || i >= n) {
+    if (T.tma_err) atomicOr(T.tma_err, 2);
+    return 0;
+  }
+#endif
+  return i;
 }
 
 // Stage input selection: inside an adaptive attempt the field and the time factor come from
@@ -302,27 +276,6 @@ __global__ void __launch_bounds__(kFluxThreads) k_flux_x(DevTransport<double> T,
     }
     ii[o] = q;
   }
-  if (T.mixed) {
-    for (int s = 0; s < T.ntr; ++s) {
-      const size_t pb = (size_t)s * nc + row;
-      float hi[5], lo[5];
-      for (int o = 0; o < 5; ++o) {
-        if (ghost[o]) {
-          const double* b = ii[o] < 0 ? T.qw : T.qe;
-          split_d(b[((size_t)s * T.nlev + k) * T.nlat + j], hi[o], lo[o]);
-        } else {
-          hi[o] = T.qhi[pb + ii[o]];
-          lo[o] = T.qlo[pb + ii[o]];
-        }
-      }
-      float d[5];
-      for (int o = 0; o < 5; ++o) d[o] = (hi[o] - hi[2]) + (lo[o] - lo[2]);
-      double a2 = ghost[2] ? (double)hi[2] + (double)lo[2] : Q[pb + ii[2]];
-      T.fx[((size_t)s * T.nlev * T.nlat + (size_t)k * T.nlat + j) * nf + i] =
-          M * (a2 + (double)ppm_face_uf(d, right));
-    }
-    return;
-  }
   for (int s = 0; s < T.ntr; ++s) {
     const double* q = Q + (size_t)s * nc + row;
     double v[5];
@@ -370,26 +323,6 @@ __global__ void __launch_bounds__(kFluxThreads) k_flux_y(DevTransport<double> T,
       else q = q < 0 ? -1 - q : 2 * T.nlat - 1 - q;
     }
     jj[o] = q;
-  }
-  if (T.mixed) {
-    for (int s = 0; s < T.ntr; ++s) {
-      const size_t pb = (size_t)s * nc + (size_t)k * T.nlat * T.nlon + i;
-      float hi[5], lo[5];
-      for (int o = 0; o < 5; ++o) {
-        if (ghost[o]) {
-          const double* b = jj[o] < 0 ? T.qs : T.qn;
-          split_d(b[((size_t)s * T.nlev + k) * T.nlon + i], hi[o], lo[o]);
-        } else {
-          hi[o] = T.qhi[pb + (size_t)jj[o] * T.nlon];
-          lo[o] = T.qlo[pb + (size_t)jj[o] * T.nlon];
-        }
-      }
-      float d[5];
-      for (int o = 0; o < 5; ++o) d[o] = (hi[o] - hi[2]) + (lo[o] - lo[2]);
-      double a2 = ghost[2] ? (double)hi[2] + (double)lo[2] : Q[pb + (size_t)jj[2] * T.nlon];
-      T.fy[(size_t)s * fplane + fbase] = M * (a2 + (double)ppm_face_uf(d, right));
-    }
-    return;
   }
   for (int s = 0; s < T.ntr; ++s) {
     const double* q = Q + (size_t)s * nc + (size_t)k * T.nlat * T.nlon + i;
@@ -440,34 +373,6 @@ __global__ void __launch_bounds__(kFluxThreads) k_flux_z(DevTransport<double> T,
          eLd = T.veD[(size_t)up * ncol + col];
   double eRab = T.veAB[(size_t)(up + 1) * ncol + col], eRc = T.veC[(size_t)(up + 1) * ncol + col],
          eRd = T.veD[(size_t)(up + 1) * ncol + col];
-  if (T.mixed) {
-    float fA0 = T.vsA32[(size_t)(up) * ncol + col], fB0 = T.vsB32[(size_t)(up) * ncol + col];
-    float fA1 = T.vsA32[(size_t)(up + 1) * ncol + col], fB1 = T.vsB32[(size_t)(up + 1) * ncol + col];
-    float fA2 = T.vsA32[(size_t)(up + 2) * ncol + col], fB2 = T.vsB32[(size_t)(up + 2) * ncol + col];
-    float fLab = T.veAB32[(size_t)up * ncol + col], fLc = T.veC32[(size_t)up * ncol + col],
-          fLd = T.veD32[(size_t)up * ncol + col];
-    float fRab = T.veAB32[(size_t)(up + 1) * ncol + col],
-          fRc = T.veC32[(size_t)(up + 1) * ncol + col], fRd = T.veD32[(size_t)(up + 1) * ncol + col];
-    for (int s = 0; s < T.ntr; ++s) {
-      const size_t pb = (size_t)s * nc + col;
-      float hi[5], lo[5];
-      for (int o = 0; o < 5; ++o) {
-        hi[o] = T.qhi[pb + (size_t)kk[o] * ncol];
-        lo[o] = T.qlo[pb + (size_t)kk[o] * ncol];
-      }
-      float d[5];
-      for (int o = 0; o < 5; ++o) d[o] = (hi[o] - hi[2]) + (lo[o] - lo[2]);
-      float dm1 = slope_nf(d[0], d[1], d[2], fA0, fB0);
-      float d0 = slope_nf(d[1], d[2], d[3], fA1, fB1);
-      float dp1 = slope_nf(d[2], d[3], d[4], fA2, fB2);
-      float aL = d[1] + fLab * (d[2] - d[1]) + fLc * d0 + fLd * dm1;
-      float aR = d[2] + fRab * (d[3] - d[2]) + fRc * dp1 + fRd * d0;
-      limitf(d[2], aL, aR);
-      double a2 = Q[pb + (size_t)kk[2] * ncol];
-      T.fz[(size_t)s * fplane + (size_t)kf * ncol + col] = M * (a2 + (double)(right ? aR : aL));
-    }
-    return;
-  }
   for (int s = 0; s < T.ntr; ++s) {
     const double* q = Q + (size_t)s * nc + col;
     double v[5];
@@ -504,36 +409,36 @@ __global__ void __launch_bounds__(256) k_flux_x_fused(DevTransport<double> T, St
   const int j = row % T.nlat, k = row / T.nlat;
   const size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
   const size_t rbase = ((size_t)k * T.nlat + j) * n;
-  for (int f = threadIdx.x; f <= n; f += blockDim.x) Mf[f] = g * T.mx[((size_t)k * T.nlat + j) * nf + f];
+  for (int f = threadIdx.x; f <= n; f += blockDim.x) Mf[bck(T, f, nf)] = g * T.mx[((size_t)k * T.nlat + j) * nf + f];
   const int s0 = (int)((long long)blockIdx.y * T.ntr / gridDim.y);  // this block's tracers
   const int s1 = (int)((long long)(blockIdx.y + 1) * T.ntr / gridDim.y);
   for (int s = s0; s < s1; ++s) {
     const double* q = Q + (size_t)s * nc + rbase;
     auto val = [&](int p) -> double {
       if (p < 0 || p >= n) {
-        if (T.lon_bc == 0) return q[((p % n) + n) % n];
-        return (p < 0 ? T.qw : T.qe)[((size_t)s * T.nlev + k) * T.nlat + j];
+        if (T.lon_bc == 0) return q[bck(T, ((p % n) + n) % n, n)];
+        return (p < 0 ? T.qw : T.qe)[bck(T, ((size_t)s * T.nlev + k) * T.nlat + j, (long long)T.ntr * T.nlev * T.nlat)];
       }
-      return q[p];
+      return q[bck(T, p, n)];
     };
     for (int p = threadIdx.x - 3; p <= n + 2; p += blockDim.x) {
       const double v = val(p);
-      V[p + 3] = v;
-      if (p <= n + 1) Dd[p + 3] = val(p + 1) - v;
+      V[bck(T, p + 3, L)] = v;
+      if (p <= n + 1) Dd[bck(T, p + 3, L)] = val(p + 1) - v;
     }
     __syncthreads();
     for (int p = threadIdx.x - 2; p <= n + 1; p += blockDim.x)
-      D[p + 3] = slope_ud(Dd[p + 2], Dd[p + 3], V[p + 2], V[p + 4]);
+      D[bck(T, p + 3, L)] = slope_ud(Dd[bck(T, p + 2, L)], Dd[bck(T, p + 3, L)], V[bck(T, p + 2, L)], V[bck(T, p + 4, L)]);
     __syncthreads();
     for (int f = threadIdx.x - 1; f <= n + 1; f += blockDim.x)
-      E[f + 3] = V[f + 2] + 0.5 * Dd[f + 2] - (D[f + 3] - D[f + 2]) * kOneSixth;
+      E[bck(T, f + 3, L)] = V[bck(T, f + 2, L)] + 0.5 * Dd[bck(T, f + 2, L)] - (D[bck(T, f + 3, L)] - D[bck(T, f + 2, L)]) * kOneSixth;
     __syncthreads();
     for (int f = threadIdx.x; f <= n; f += blockDim.x) {
-      const double M = Mf[f];
+      const double M = Mf[bck(T, f, nf)];
       const bool right = __double_as_longlong(M) > 0;  // M > 0 for every non-NaN M
       int up = right ? f - 1 : f;
-      double aL = E[up + 3], aR = E[up + 4];
-      limit_p(V[up + 3], aL, aR);
+      double aL = E[bck(T, up + 3, L)], aR = E[bck(T, up + 4, L)];
+      limit_p(V[bck(T, up + 3, L)], aL, aR);
       T.fx[((size_t)s * T.nlev * T.nlat + (size_t)k * T.nlat + j) * nf + f] = M * (right ? aR : aL);
     }
     __syncthreads();
@@ -563,8 +468,8 @@ __global__ void __launch_bounds__(512) k_flux_y_fused(DevTransport<double> T, St
   const bool open = T.lat_bc == 1;
   if (live)
     for (int f = ty; f <= n; f += blockDim.y)
-      Mf[f * kPencil + tx] = g * T.my[((size_t)k * nfj + f) * T.nlon + i];
-#define RS_P(a, p) a[((p) + 3) * kPencil + tx]
+      Mf[bck(T, f * kPencil + tx, (long long)(n + 1) * kPencil)] = g * T.my[((size_t)k * nfj + f) * T.nlon + i];
+#define RS_P(a, p) a[bck(T, ((p) + 3) * kPencil + tx, (long long)L * kPencil)]
   const int s0 = (int)((long long)blockIdx.y * T.ntr / gridDim.y);  // this block's tracers
   const int s1 = (int)((long long)(blockIdx.y + 1) * T.ntr / gridDim.y);
   for (int s = s0; s < s1; ++s) {
@@ -572,10 +477,10 @@ __global__ void __launch_bounds__(512) k_flux_y_fused(DevTransport<double> T, St
     auto val = [&](int p) -> double {
       if (!live) return 0.0;
       if (p < 0 || p >= n) {
-        if (open) return (p < 0 ? T.qs : T.qn)[((size_t)s * T.nlev + k) * T.nlon + i];
-        return q[(size_t)(p < 0 ? -1 - p : 2 * n - 1 - p) * T.nlon + i];
+        if (open) return (p < 0 ? T.qs : T.qn)[bck(T, ((size_t)s * T.nlev + k) * T.nlon + i, (long long)T.ntr * T.nlev * T.nlon)];
+        return q[bck(T, (size_t)(p < 0 ? -1 - p : 2 * n - 1 - p) * T.nlon + i, (long long)T.nlat * T.nlon)];
       }
-      return q[(size_t)p * T.nlon + i];
+      return q[bck(T, (size_t)p * T.nlon + i, (long long)T.nlat * T.nlon)];
     };
     for (int p = (int)ty - 3; p <= n + 2; p += blockDim.y) {
       const double v = val(p);
@@ -596,7 +501,7 @@ __global__ void __launch_bounds__(512) k_flux_y_fused(DevTransport<double> T, St
           T.fy[(size_t)s * fplane + fb] = 0.0;
           continue;
         }
-        const double M = Mf[f * kPencil + tx];
+        const double M = Mf[bck(T, f * kPencil + tx, (long long)(n + 1) * kPencil)];
         const bool right = __double_as_longlong(M) > 0;
         int up = right ? f - 1 : f;
         double aL = RS_P(E, up), aR = RS_P(E, up + 1);
@@ -628,14 +533,14 @@ __global__ void __launch_bounds__(512) k_flux_z_fused(DevTransport<double> T, St
   const size_t nc = ncol * n;
   const size_t fplane = ncol * (n + 1);
   if (live)
-    for (int kf = ty; kf <= n; kf += blockDim.y) Mf[kf * kPencil + tx] = g * T.mz[(size_t)kf * ncol + col];
+    for (int kf = ty; kf <= n; kf += blockDim.y) Mf[bck(T, kf * kPencil + tx, (long long)(n + 1) * kPencil)] = g * T.mz[(size_t)kf * ncol + col];
   const int s0 = (int)((long long)blockIdx.y * T.ntr / gridDim.y);  // this block's tracers
   const int s1 = (int)((long long)(blockIdx.y + 1) * T.ntr / gridDim.y);
   for (int s = s0; s < s1; ++s) {
     const double* q = Q + (size_t)s * nc;
     auto val = [&](int p) -> double {
       const int pp = p < 0 ? -1 - p : (p >= n ? 2 * n - 1 - p : p);
-      return live ? q[(size_t)pp * ncol + col] : 0.0;
+      return live ? q[bck(T, (size_t)pp * ncol + col, (long long)nc)] : 0.0;
     };
     for (int p = (int)ty - 3; p <= n + 2; p += blockDim.y) {
       const double v = val(p);
@@ -644,15 +549,15 @@ __global__ void __launch_bounds__(512) k_flux_z_fused(DevTransport<double> T, St
     }
     __syncthreads();
     for (int p = (int)ty - 1; p <= n; p += blockDim.y) {  // slopes of cells -1..n
-      double sA = live ? T.vsA[(size_t)(p + 1) * ncol + col] : 0.0;
-      double sB = live ? T.vsB[(size_t)(p + 1) * ncol + col] : 0.0;
+      double sA = live ? T.vsA[bck(T, (size_t)(p + 1) * ncol + col, (long long)(n + 2) * ncol)] : 0.0;
+      double sB = live ? T.vsB[bck(T, (size_t)(p + 1) * ncol + col, (long long)(n + 2) * ncol)] : 0.0;
       RS_P(D, p) = slope_nd(RS_P(Dd, p - 1), RS_P(Dd, p), sA, sB);
     }
     __syncthreads();
     for (int e = ty; e <= n; e += blockDim.y) {  // edges 0..n (cells e-1 | e)
-      double eab = live ? T.veAB[(size_t)e * ncol + col] : 0.0;
-      double ec = live ? T.veC[(size_t)e * ncol + col] : 0.0;
-      double ed = live ? T.veD[(size_t)e * ncol + col] : 0.0;
+      double eab = live ? T.veAB[bck(T, (size_t)e * ncol + col, (long long)(n + 1) * ncol)] : 0.0;
+      double ec = live ? T.veC[bck(T, (size_t)e * ncol + col, (long long)(n + 1) * ncol)] : 0.0;
+      double ed = live ? T.veD[bck(T, (size_t)e * ncol + col, (long long)(n + 1) * ncol)] : 0.0;
       RS_P(E, e) = RS_P(V, e - 1) + eab * RS_P(Dd, e - 1) + ec * RS_P(D, e) + ed * RS_P(D, e - 1);
     }
     __syncthreads();
@@ -662,7 +567,7 @@ __global__ void __launch_bounds__(512) k_flux_z_fused(DevTransport<double> T, St
           T.fz[(size_t)s * fplane + (size_t)kf * ncol + col] = 0.0;
           continue;
         }
-        const double M = Mf[kf * kPencil + tx];
+        const double M = Mf[bck(T, kf * kPencil + tx, (long long)(n + 1) * kPencil)];
         const bool right = __double_as_longlong(M) > 0;
         int up = right ? kf - 1 : kf;
         double aL = RS_P(E, up), aR = RS_P(E, up + 1);
@@ -675,47 +580,126 @@ __global__ void __launch_bounds__(512) k_flux_z_fused(DevTransport<double> T, St
 #undef RS_P
 }
 
-// ------------------------------------------------------------------ mixed-precision pencils
-// FP32 reconstruction once per cell (instead of per face): a pencil stages the split state
-// (hi, lo planes) in shared memory, forms the neighbour differences
-//   dl_p = (hi_{p+1} - hi_p) + (lo_{p+1} - lo_p)          (exact hi differences of nearby values)
-// and each cell's monotone slope from them; a face then needs only the upwind cell's two edge
-// DEVIATIONS (translation invariance of PPM: the value of the upwind cell is 0)
-//   uniform:  aL = -dl_{up-1}/2 - (S_up - S_{up-1})/6,  aR = dl_up/2 - (S_{up+1} - S_up)/6
-//   dp-weighted (edge e between cells e-1, e with coefficients ab, c, d):
-//             aL = (ab_up - 1) dl_{up-1} + c_up S_up + d_up S_{up-1}
-//             aR = ab_{up+1} dl_up + c_{up+1} S_{up+1} + d_{up+1} S_up
-// the CW84 limiter on (0, aL, aR), and the face value a_up + dev in FP64.  q == 1 gives dl = 0,
-// S = 0, dev = 0 and a face of exactly 1 (the freestream stays exact).  blockIdx.y selects a
-// group of sper tracers, so short pencil grids still fill the 152 SMs.
-__device__ __forceinline__ float slope_from_diff(float d0, float d1) {
-  if (d1 * d0 > 0.0f) {
-    const float da = 0.5f * (d0 + d1);
-    const float lim = 2.0f * fminf(fabsf(d0), fabsf(d1));
-    return copysignf(fminf(fabsf(da), lim), da);
-  }
-  return 0.0f;
+// ------------------------------------------------------------------ mixed precision
+// Compensated FP32 transport.  Every transport value is carried as a double-float pair
+// (value = h + l, |l| <= ulp(h)/2: two FP32 numbers, about 48 significant bits) and combined
+// with error-free transformations (Knuth's TwoSum for sums, FMA-based TwoProduct for products),
+// so the reconstruction runs on the FP32 pipe at FP64-class accuracy.  The face terms are written
+// in advective form: for cell c and face f with air-mass flux M_f, the CWC tendency
+//   m dq/dt = -div(M q) + q div(M) = sum_f sigma_f G_f M_f (q_c - q_f)
+// (sigma_f = +1 on the east / north / top face, -1 on the west / south / bottom face, G_f the
+// face's metric factor) needs only differences: q_c - q_f is minus the edge deviation when c is
+// upwind, or minus (neighbour difference + edge deviation) when it is not.  With
+//   Phi_f = M_f (q_f - q_L),  Psi_f = M_f (q_R - q_f)      (L / R: the cells below / above f)
+// a cell's tendency is -G (Phi_e + Psi_w) along x, -(G_n Phi_n + G_s Psi_s) along y and
+// -(Phi_t + Psi_b) vertically.  No term is of the size of q itself, so a value far smaller
+// than its neighbours keeps its relative accuracy (an FP32 reconstruction of deviations does
+// not: its error scales with the neighbour difference).  q == const gives exactly zero.
+//
+// Each direction's pencil adds its part of m dq/dt into a per-cell double-float accumulator
+// (x writes it, y and z add), and the stage kernel turns it into the stage update in FP64.
+// The state, the air mass, the stage combinations and the error norm stay FP64.
+struct df {
+  float h, l;
+};
+__device__ __forceinline__ df df_two_sum(float a, float b) {  // a + b = s + e exactly
+  const float s = a + b, bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
 }
-__device__ __forceinline__ float slope_from_diff_n(float d0, float d1, float sA, float sB) {
-  if (d1 * d0 > 0.0f) {
-    const float da = sA * d1 + sB * d0;
-    const float lim = 2.0f * fminf(fabsf(d0), fabsf(d1));
-    return copysignf(fminf(fabsf(da), lim), da);
-  }
-  return 0.0f;
+__device__ __forceinline__ df df_add(df a, df b) {
+  const df s = df_two_sum(a.h, b.h);
+  return df_two_sum(s.h, s.l + (a.l + b.l));
 }
+__device__ __forceinline__ df df_neg(df a) { return {-a.h, -a.l}; }
+__device__ __forceinline__ df df_sub(df a, df b) { return df_add(a, df_neg(b)); }
+__device__ __forceinline__ df df_mul(df a, df b) {
+  const float p = a.h * b.h;
+  const float e = fmaf(a.h, b.l, fmaf(a.l, b.h, fmaf(a.h, b.h, -p)));
+  const float s = p + e;
+  return {s, e - (s - p)};
+}
+__device__ __forceinline__ df df_scale(df a, float pow2) { return {a.h * pow2, a.l * pow2}; }
+__device__ __forceinline__ df df_ld(const float* H, const float* L, long long x) {
+  return {H[x], L[x]};
+}
+__device__ __forceinline__ df df_ld2(const float2* p, size_t x) {
+  const float2 v = p[x];
+  return {v.x, v.y};
+}
+// 1/6 as a pair (hi = fl(1/6), lo = fl(1/6 - hi))
+constexpr float kSixthH = (float)(1.0 / 6.0);
+constexpr float kSixthL = (float)(1.0 / 6.0 - (double)(float)(1.0 / 6.0));
 
-// Shared-memory layout of the mixed pencils (floats first, 128-byte aligned rows so that bulk
-// copies can land in them): the H, Lo rows (two sets when staged by bulk copies, so the next
-// tracer's copy overlaps this tracer's work), then Dl, S rows of L entries (interior cell p at
-// row p + kHo), then the face air-mass flux as float and as double.
-constexpr int kHoX = 32;  // lon rows: interior starts 128 bytes into each row
-constexpr int kHoP = 8;   // lat / vertical pencils: interior starts 8 pencil rows in
-__host__ __device__ inline int mixed_rows_x(int n) { return (n + kHoX + 3 + 31) / 32 * 32; }
-__host__ __device__ inline int mixed_rows_p(int n) { return (n + kHoP + 3 + 1) / 2 * 2; }
-
-// The face flux is M a2 + M dev: a2 the upwind cell's FP64 value, the deviation product in FP32
-// (one FMA in FP64); q == 1 gives exactly M.
+// |a| < |b| for pairs of the same sign (sg = +1 or -1 their sign)
+__device__ __forceinline__ bool df_absless(df a, df b, float sg) {
+  return (fabsf(a.h) < fabsf(b.h)) || (a.h == b.h && sg * a.l < sg * b.l);
+}
+// CW84 eq. 1.8 monotonised slope from the neighbour differences d0 (left) and d1 (right):
+// 0 unless they have the same strict sign, else the smallest in magnitude of the centred
+// slope da and 2 d0, 2 d1 (all three share that sign)
+__device__ __forceinline__ df mc_pick(df d0, df d1, df da) {
+  const bool same = (d0.h > 0.0f && d1.h > 0.0f) || (d0.h < 0.0f && d1.h < 0.0f);
+  const float sg = d0.h > 0.0f ? 1.0f : -1.0f;
+  df m = da;
+  const df t0 = df_scale(d0, 2.0f), t1 = df_scale(d1, 2.0f);
+  if (df_absless(t0, m, sg)) m = t0;
+  if (df_absless(t1, m, sg)) m = t1;
+  return same ? m : df{0.0f, 0.0f};
+}
+__device__ __forceinline__ df mc_slope(df d0, df d1) {
+  return mc_pick(d0, d1, df_scale(df_add(d0, d1), 0.5f));
+}
+__device__ __forceinline__ df mc_slope_n(df d0, df d1, df sA, df sB) {  // dp-weighted centre
+  return mc_pick(d0, d1, df_add(df_mul(sA, d1), df_mul(sB, d0)));
+}
+// CW84 eq. 1.10 limiter on the upwind cell's edge deviations (aL, aR) from its own value
+// (a = 0): flatten unless aL and aR have strictly opposite signs, else steepen where the
+// parabola overshoots; the tests dA a6 > dA^2 and -dA^2 > dA a6 of the FP64 form become sign
+// tests of aL + 2 aR and 2 aL + aR.  Returns the limited right (M > 0) or left edge.
+__device__ __forceinline__ df lim_pick(df aL, df aR, bool right) {
+  const bool opp = (aR.h > 0.0f && aL.h < 0.0f) || (aR.h < 0.0f && aL.h > 0.0f);
+  const float sR = aR.h > 0.0f ? 1.0f : -1.0f;
+  const df t1 = df_add(aL, df_scale(aR, 2.0f));
+  const df t2 = df_add(df_scale(aL, 2.0f), aR);
+  const bool c1 = sR * t1.h < 0.0f;
+  const bool c2 = !c1 && sR * t2.h > 0.0f;
+  df r = right ? (c2 ? df_scale(aL, -2.0f) : aR) : (c1 ? df_scale(aR, -2.0f) : aL);
+  return opp ? r : df{0.0f, 0.0f};
+}
+// Edge term E_p of cell p (the deviation of edge p+1/2 from cell p, unlimited), uniform grid:
+// E_p = D_p / 2 - (S_{p+1} - S_p) / 6; the left edge of cell p is E_{p-1} - D_{p-1}.
+__device__ __forceinline__ df edge_u(df Dp, df Sp, df Sp1) {
+  return df_sub(df_scale(Dp, 0.5f), df_mul(df_sub(Sp1, Sp), df{kSixthH, kSixthL}));
+}
+// dp-weighted: E_p = ab D_p + c S_{p+1} + d S_p with the coefficients of edge p+1
+__device__ __forceinline__ df edge_n(df Dp, df Sp, df Sp1, df ab, df c, df d) {
+  return df_add(df_add(df_mul(ab, Dp), df_mul(c, Sp1)), df_mul(d, Sp));
+}
+// A cell's two faces along one direction: w (below, flux Mw) and e (above, flux Me).
+// E(o), D(o) give E_{p+o}, D_{p+o}.  Returns {Psi_w, Phi_e}; a face with M == 0 (a wall)
+// contributes exactly 0.
+template <class FE, class FD>
+__device__ __forceinline__ void cell_faces(df Mw, df Me, FE E, FD D, df& psi, df& phi) {
+  psi = df{0.0f, 0.0f};
+  phi = df{0.0f, 0.0f};
+  if (Mw.h > 0.0f) {  // upwind p-1: its right edge
+    const df dev = lim_pick(df_sub(E(-2), D(-2)), E(-1), true);
+    psi = df_mul(Mw, df_sub(D(-1), dev));
+  } else if (Mw.h < 0.0f) {  // upwind p: its left edge
+    const df dev = lim_pick(df_sub(E(-1), D(-1)), E(0), false);
+    psi = df_mul(Mw, df_neg(dev));
+  }
+  if (Me.h > 0.0f) {  // upwind p: its right edge
+    const df dev = lim_pick(df_sub(E(-1), D(-1)), E(0), true);
+    phi = df_mul(Me, dev);
+  } else if (Me.h < 0.0f) {  // upwind p+1: its left edge
+    const df dev = lim_pick(df_sub(E(0), D(0)), E(1), false);
+    phi = df_mul(Me, df_add(D(0), dev));
+  }
+}
+// split a double into a pair: production build with integer operations (split_bits below,
+// truncating: hi + lo = v to 2^-47), strict build with conversions
+__device__ __forceinline__ df split_df(double v);
 // float -> double by re-biasing the exponent in the integer pipes (exact; zero kept, subnormal,
 // inf and NaN convert)
 __device__ __forceinline__ double f2d_bits(float x) {
@@ -726,11 +710,11 @@ __device__ __forceinline__ double f2d_bits(float x) {
   return __hiloint2double((int)((u & 0x80000000u) | ((fe + 896u) << 20) | ((u & 0x7fffffu) >> 3)),
                           (int)(u << 29));
 }
-__device__ __forceinline__ double mixed_flux(double M, float Mf, double a2, float dev) {
+__device__ __forceinline__ double df_to_d(float2 v) {
 #if RS_STRICT
-  return fma(M, a2, (double)(Mf * dev));
+  return (double)v.x + (double)v.y;
 #else
-  return fma(M, a2, f2d_bits(Mf * dev));
+  return f2d_bits(v.x) + f2d_bits(v.y);
 #endif
 }
 
@@ -808,8 +792,20 @@ __device__ __noinline__ void staging_abort(int* err, const Ctl* ctl, unsigned lo
   }
 }
 
+// Shared-memory layout of the mixed pencils (floats, 128-byte aligned rows so that bulk copies
+// can land in them): the staged hi / lo rows (two sets with bulk copies, so the next tracer's
+// copy overlaps this tracer's work), then the pair rows of the neighbour differences D and the
+// slopes S (interior cell p at row p + kHo), then the face air-mass fluxes as pairs.  After the
+// differences are formed the current hi / lo rows hold the edge terms E.
+constexpr int kHoX = 32;  // lon rows: interior starts 128 bytes into each row
+constexpr int kHoP = 8;   // lat / vertical pencils: interior starts 8 pencil rows in
+__host__ __device__ inline int mixed_rows_x(int n) { return (n + kHoX + 3 + 31) / 32 * 32; }
+__host__ __device__ inline int mixed_rows_p(int n) { return (n + kHoP + 3 + 1) / 2 * 2; }
+__host__ __device__ inline int mixed_frows(int n) { return (n + 1 + 31) / 32 * 32; }
+
+// Lon rows: one block per (lat, level) row, blockIdx.y a group of sper tracers.
 template <bool kTma>
-__global__ void __launch_bounds__(256) k_flux_x_mixed(DevTransport<double> T, StageSel sel, int sper) {
+__global__ void __launch_bounds__(256) k_adv_x_mixed(DevTransport<double> T, StageSel sel, int sper) {
   const double* Q;
   double g;
   if (!resolve_stage(sel, Q, g)) return;
@@ -822,19 +818,24 @@ __global__ void __launch_bounds__(256) k_flux_x_mixed(DevTransport<double> T, St
   float* const L0 = smx32 + L;
   float* const H1 = smx32 + (kTma ? 2 * L : 0);
   float* const L1 = smx32 + (kTma ? 3 * L : L);
-  float* Dl = smx32 + (kTma ? 4 : 2) * L;  // Dl[p + kHoX] = v(p+1) - v(p), p in [-3, n+1]
-  float* S = Dl + L;                       // S[p + kHoX], slopes of cells p in [-2, n+1]
-  float* Mf32 = S + L;                     // [n+1]
-  double* Mf = reinterpret_cast<double*>(Mf32 + (nf + 1) / 2 * 2);  // [n+1]
+  float* const Dh = smx32 + (kTma ? 4 : 2) * L;  // D[p] = q(p+1) - q(p), p in [-3, n+1]
+  float* const Dl = Dh + L;
+  float* const Sh = Dl + L;  // slopes of cells [-2, n+1]
+  float* const Sl = Sh + L;
+  float* const Mh = Sl + L;  // face fluxes [0, n] as pairs
+  float* const Ml = Mh + mixed_frows(n);
   const int row = blockIdx.x;
   const int j = row % T.nlat, k = row / T.nlat;
   const size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
+  const long long nall = (long long)T.ntr * nc;
   const size_t rbase = ((size_t)k * T.nlat + j) * n;
   const bool periodic = T.lon_bc == 0;
   const int tid = threadIdx.x;
+  const df G = df_ld2(T.gx2, j);
+  auto X = [&](int p) { return bck(T, p + kHoX, L); };  // row index of cell p
   int uses0 = 0, uses1 = 0;  // copies issued per buffer
   auto issue = [&](int s, int b) {  // one tracer's interior hi / lo rows (n floats each)
-    const size_t pb = (size_t)s * nc + rbase;
+    const size_t pb = (size_t)bck(T, (size_t)s * nc + rbase, nall - n + 1);
     fence_proxy_async();
     mbar_expect_tx(bar + b, (uint32_t)(2 * n * sizeof(float)));
     bulk_load((b ? H1 : H0) + kHoX, T.qhi + pb, (uint32_t)(n * sizeof(float)), bar + b);
@@ -851,15 +852,25 @@ __global__ void __launch_bounds__(256) k_flux_x_mixed(DevTransport<double> T, St
     uses0 = s0 < s1;
   }
   for (int f = tid; f <= n; f += blockDim.x) {
-    const double M = g * T.mx[((size_t)k * T.nlat + j) * nf + f];
-    Mf[f] = M;
-    Mf32[f] = (float)M;
+    const df M = split_df(g * T.mx[((size_t)k * T.nlat + j) * nf + f]);
+    Mh[bck(T, f, mixed_frows(n))] = M.h;
+    Ml[bck(T, f, mixed_frows(n))] = M.l;
   }
   for (int s = s0; s < s1; ++s) {
     const int it = s - s0, b = kTma ? (it & 1) : 0;
     float* H = b ? H1 : H0;
     float* Lo = b ? L1 : L0;
     const size_t pb = (size_t)s * nc + rbase;
+    auto ghost = [&](int p, float& h, float& l) {  // p outside 0..n-1
+      if (periodic) {
+        const int q = ((p % n) + n) % n;
+        h = T.qhi[bck(T, pb + q, nall)];
+        l = T.qlo[bck(T, pb + q, nall)];
+      } else {
+        split_d((p < 0 ? T.qw : T.qe)[bck(T, ((size_t)s * T.nlev + k) * T.nlat + j,
+                                          (long long)T.ntr * T.nlev * T.nlat)], h, l);
+      }
+    };
     if (kTma) {
       if (s + 1 < s1) {
         if (tid == 0) issue(s + 1, b ^ 1);
@@ -869,15 +880,9 @@ __global__ void __launch_bounds__(256) k_flux_x_mixed(DevTransport<double> T, St
       if (tid < 6) {  // the three ghost cells on each side
         const int p = tid < 3 ? tid - 3 : n + tid - 3;
         float h, l;
-        if (periodic) {
-          const int q = p < 0 ? p + n : p - n;
-          h = T.qhi[pb + q];
-          l = T.qlo[pb + q];
-        } else {
-          split_d((p < 0 ? T.qw : T.qe)[((size_t)s * T.nlev + k) * T.nlat + j], h, l);
-        }
-        H[p + kHoX] = h;
-        Lo[p + kHoX] = l;
+        ghost(p, h, l);
+        H[X(p)] = h;
+        Lo[X(p)] = l;
       }
       const bool ok = mbar_wait_bounded(bar + b, (uint32_t)(((it >> 1)) & 1));
       if (__syncthreads_or(!ok)) {
@@ -888,88 +893,106 @@ __global__ void __launch_bounds__(256) k_flux_x_mixed(DevTransport<double> T, St
       for (int p = tid - 3; p <= n + 2; p += blockDim.x) {
         float h, l;
         if (p < 0 || p >= n) {
-          if (periodic) {
-            const int q = ((p % n) + n) % n;
-            h = T.qhi[pb + q];
-            l = T.qlo[pb + q];
-          } else {
-            split_d((p < 0 ? T.qw : T.qe)[((size_t)s * T.nlev + k) * T.nlat + j], h, l);
-          }
+          ghost(p, h, l);
         } else {
-          h = T.qhi[pb + p];
-          l = T.qlo[pb + p];
+          h = T.qhi[bck(T, pb + p, nall)];
+          l = T.qlo[bck(T, pb + p, nall)];
         }
-        H[p + kHoX] = h;
-        Lo[p + kHoX] = l;
+        H[X(p)] = h;
+        Lo[X(p)] = l;
       }
       __syncthreads();
     }
-    for (int p = tid - 3; p <= n + 1; p += blockDim.x)
-      Dl[p + kHoX] = (H[p + kHoX + 1] - H[p + kHoX]) + (Lo[p + kHoX + 1] - Lo[p + kHoX]);
+    for (int p = tid - 3; p <= n + 1; p += blockDim.x) {
+      const df d = df_sub(df_ld(H, Lo, X(p + 1)), df_ld(H, Lo, X(p)));
+      Dh[X(p)] = d.h;
+      Dl[X(p)] = d.l;
+    }
     __syncthreads();
-    for (int p = tid - 2; p <= n + 1; p += blockDim.x)
-      S[p + kHoX] = slope_from_diff(Dl[p + kHoX - 1], Dl[p + kHoX]);
+    for (int p = tid - 2; p <= n + 1; p += blockDim.x) {
+      const df sl = mc_slope(df_ld(Dh, Dl, X(p - 1)), df_ld(Dh, Dl, X(p)));
+      Sh[X(p)] = sl.h;
+      Sl[X(p)] = sl.l;
+    }
     __syncthreads();
-    auto face = [&](int f, bool ghosts) {
-      const double M = Mf[f];
-      const bool right = __double_as_longlong(M) > 0;
-      const int up = right ? f - 1 : f;
-      const int u = up + kHoX;
-      float aL = -0.5f * Dl[u - 1] - (S[u] - S[u - 1]) * (1.0f / 6.0f);
-      float aR = 0.5f * Dl[u] - (S[u + 1] - S[u]) * (1.0f / 6.0f);
-      limitf(0.0f, aL, aR);
-      double a2;
-      if (!ghosts) a2 = Q[pb + (up < 0 ? n - 1 : (up >= n ? 0 : up))];
-      else if (up >= 0 && up < n) a2 = Q[pb + up];
-      else a2 = (double)H[u] + (double)Lo[u];
-      T.fx[((size_t)s * T.nlev * T.nlat + (size_t)k * T.nlat + j) * nf + f] =
-          mixed_flux(M, Mf32[f], a2, right ? aR : aL);
-    };
-    if (periodic)
-      for (int f = tid; f <= n; f += blockDim.x) face(f, false);
-    else
-      for (int f = tid; f <= n; f += blockDim.x) face(f, true);
+    for (int p = tid - 2; p <= n; p += blockDim.x) {  // edge terms over the staged values
+      const df e = edge_u(df_ld(Dh, Dl, X(p)), df_ld(Sh, Sl, X(p)), df_ld(Sh, Sl, X(p + 1)));
+      H[X(p)] = e.h;
+      Lo[X(p)] = e.l;
+    }
+    __syncthreads();
+    for (int p = tid; p < n; p += blockDim.x) {
+      df psi, phi;
+      cell_faces(df{Mh[bck(T, p, nf)], Ml[bck(T, p, nf)]},
+                 df{Mh[bck(T, p + 1, nf)], Ml[bck(T, p + 1, nf)]},
+                 [&](int o) { return df_ld(H, Lo, X(p + o)); },
+                 [&](int o) { return df_ld(Dh, Dl, X(p + o)); }, psi, phi);
+      const df a = df_neg(df_mul(G, df_add(phi, psi)));
+      T.acc[bck(T, pb + p, nall)] = make_float2(a.h, a.l);
+    }
     __syncthreads();
   }
 }
 
-template <int kPencil, bool kTma>
-__global__ void __launch_bounds__(512) k_flux_y_mixed(DevTransport<double> T, StageSel sel, int sper,
+// Lat (DIR 1) and vertical (DIR 2) pencils: kPencil columns per block (threadIdx.x), the
+// pencil's cells along threadIdx.y; rows [L][kPencil].  The lat pencils use the uniform
+// reconstruction with the metric factors of the south and north faces, the vertical ones the
+// dp-weighted coefficients; both add their part into the accumulator.
+template <int DIR, int kPencil, bool kTma>
+__global__ void __launch_bounds__(512) k_adv_yz_mixed(DevTransport<double> T, StageSel sel, int sper,
                                                       const __grid_constant__ CUtensorMap mh,
                                                       const __grid_constant__ CUtensorMap ml) {
   const double* Q;
   double g;
   if (!resolve_stage(sel, Q, g)) return;
   const int s0 = blockIdx.y * sper, s1 = min(T.ntr, s0 + sper);  // this block's tracers
-  extern __shared__ __align__(16) unsigned char smy32_raw[];
-  float* smy32 = align128(smy32_raw);
+  extern __shared__ __align__(16) unsigned char smp32_raw[];
+  float* smp32 = align128(smp32_raw);
   __shared__ __align__(8) unsigned long long bar[2];
-  const int n = T.nlat, nfj = n + 1, L = mixed_rows_p(n);
+  const int n = DIR == 1 ? T.nlat : T.nlev, L = mixed_rows_p(n);
   const int R = L * kPencil;  // one row set [L][kPencil], cell p at row p + kHoP
-  float* const H0 = smy32;
-  float* const L0 = smy32 + R;
-  float* const H1 = smy32 + (kTma ? 2 * R : 0);
-  float* const L1 = smy32 + (kTma ? 3 * R : R);
-  float* Dl = smy32 + (kTma ? 4 : 2) * R;
-  float* S = Dl + R;
-  float* Mf32 = S + R;  // [n+1][kPencil]
-  double* Mf = reinterpret_cast<double*>(Mf32 + nfj * kPencil);
+  float* const H0 = smp32;
+  float* const L0 = smp32 + R;
+  float* const H1 = smp32 + (kTma ? 2 * R : 0);
+  float* const L1 = smp32 + (kTma ? 3 * R : R);
+  float* const Dh = smp32 + (kTma ? 4 : 2) * R;
+  float* const Dl = Dh + R;
+  float* const Sh = Dl + R;
+  float* const Sl = Sh + R;
+  float* const Mh = Sl + R;  // [n+1][kPencil]
+  float* const Ml = Mh + (n + 1) * kPencil;
   const int tx = threadIdx.x, ty = threadIdx.y;
   const bool lead = tx == 0 && ty == 0;
+  const size_t ncol = (size_t)T.nlon * T.nlat;
+  const size_t nc = ncol * T.nlev;
+  const long long nall = (long long)T.ntr * nc;
+  const long long mb = (long long)(n + 1) * kPencil;
+  // DIR 1: blockIdx.x = (lon tile, level); DIR 2: blockIdx.x = column tile
   const int ntile = (T.nlon + kPencil - 1) / kPencil;
-  const int k = blockIdx.x / ntile;
-  const int i0 = (blockIdx.x % ntile) * kPencil;
+  const int k = DIR == 1 ? (int)(blockIdx.x / ntile) : 0;
+  const int i0 = DIR == 1 ? (int)(blockIdx.x % ntile) * kPencil : 0;
+  const size_t col0 = DIR == 2 ? (size_t)blockIdx.x * kPencil : 0;
   const int i = i0 + tx;
-  const bool live = i < T.nlon;
-  const size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
-  const size_t fplane = (size_t)T.nlev * nfj * T.nlon;
-  const bool open = T.lat_bc == 1;
+  const size_t col = col0 + tx;
+  const bool live = DIR == 1 ? i < T.nlon : col < ncol;
+  const size_t stride = DIR == 1 ? (size_t)T.nlon : ncol;  // cell p to p+1
+  const size_t cbase = DIR == 1 ? (size_t)k * ncol + i : col;  // cell 0 of the pencil
+  const bool open = DIR == 1 && T.lat_bc == 1;
   int uses0 = 0, uses1 = 0;  // copies issued per buffer
-  auto issue = [&](int s, int b) {  // interior rows 0..n-1 of (i0.., k, s): box {kPencil, n, 1}
+  auto issue = [&](int s, int b) {  // interior rows 0..n-1: box {kPencil, n, 1}
+    if (RS_BOUNDS_CHECK) {  // box starts inside the tensor
+      bck(T, DIR == 1 ? i0 : (long long)col0, DIR == 1 ? T.nlon : (long long)ncol);
+      bck(T, DIR == 1 ? k + s * T.nlev : s, DIR == 1 ? (long long)T.nlev * T.ntr : T.ntr);
+    }
     fence_proxy_async();
     mbar_expect_tx(bar + b, (uint32_t)(2 * n * kPencil * sizeof(float)));
-    tma_load_3d((b ? H1 : H0) + kHoP * kPencil, &mh, i0, 0, k + s * T.nlev, bar + b);
-    tma_load_3d((b ? L1 : L0) + kHoP * kPencil, &ml, i0, 0, k + s * T.nlev, bar + b);
+    if (DIR == 1) {
+      tma_load_3d((b ? H1 : H0) + kHoP * kPencil, &mh, i0, 0, k + s * T.nlev, bar + b);
+      tma_load_3d((b ? L1 : L0) + kHoP * kPencil, &ml, i0, 0, k + s * T.nlev, bar + b);
+    } else {
+      tma_load_3d((b ? H1 : H0) + kHoP * kPencil, &mh, (int)col0, 0, s, bar + b);
+      tma_load_3d((b ? L1 : L0) + kHoP * kPencil, &ml, (int)col0, 0, s, bar + b);
+    }
   };
   if (kTma) {
     if (lead) {
@@ -981,31 +1004,38 @@ __global__ void __launch_bounds__(512) k_flux_y_mixed(DevTransport<double> T, St
     if (lead && s0 < s1) issue(s0, 0);
     uses0 = s0 < s1;
   }
+#define RS_P(a, p) a[bck(T, ((p) + kHoP) * kPencil + tx, R)]
   if (live)
     for (int f = ty; f <= n; f += blockDim.y) {
-      const double M = g * T.my[((size_t)k * nfj + f) * T.nlon + i];
-      Mf[f * kPencil + tx] = M;
-      Mf32[f * kPencil + tx] = (float)M;
+      df M{0.0f, 0.0f};
+      if (DIR == 1) {
+        if (open || (f > 0 && f < n))  // closed walls: no flux through the poles
+          M = split_df(g * T.my[((size_t)k * (n + 1) + f) * T.nlon + i]);
+      } else if (f > 0 && f < n) {  // no flux through the surface and the model top
+        M = split_df(g * T.mz[(size_t)f * ncol + col]);
+      }
+      Mh[bck(T, f * kPencil + tx, mb)] = M.h;
+      Ml[bck(T, f * kPencil + tx, mb)] = M.l;
     }
-#define RS_Y(a, p) a[((p) + kHoP) * kPencil + tx]
   for (int s = s0; s < s1; ++s) {
     const int it = s - s0, b = kTma ? (it & 1) : 0;
     float* H = b ? H1 : H0;
     float* Lo = b ? L1 : L0;
-    const size_t pb = (size_t)s * nc + (size_t)k * T.nlat * T.nlon;
+    const size_t pb = (size_t)s * nc + cbase;
     auto cell = [&](int p, float& h, float& l) {  // a ghost (p outside 0..n-1) or interior cell
       h = 0.0f;
       l = 0.0f;
       if (!live) return;
       if (p < 0 || p >= n) {
         if (open) {
-          split_d((p < 0 ? T.qs : T.qn)[((size_t)s * T.nlev + k) * T.nlon + i], h, l);
+          split_d((p < 0 ? T.qs : T.qn)[bck(T, ((size_t)s * T.nlev + k) * T.nlon + i,
+                                            (long long)T.ntr * T.nlev * T.nlon)], h, l);
           return;
         }
-        p = p < 0 ? -1 - p : 2 * n - 1 - p;
+        p = p < 0 ? -1 - p : 2 * n - 1 - p;  // mirror ghosts at the walls
       }
-      h = T.qhi[pb + (size_t)p * T.nlon + i];
-      l = T.qlo[pb + (size_t)p * T.nlon + i];
+      h = T.qhi[bck(T, pb + (size_t)p * stride, nall)];
+      l = T.qlo[bck(T, pb + (size_t)p * stride, nall)];
     };
     if (kTma) {
       if (s + 1 < s1) {
@@ -1017,8 +1047,8 @@ __global__ void __launch_bounds__(512) k_flux_y_mixed(DevTransport<double> T, St
         const int p = r < 3 ? r - 3 : n + r - 3;
         float h, l;
         cell(p, h, l);
-        RS_Y(H, p) = h;
-        RS_Y(Lo, p) = l;
+        RS_P(H, p) = h;
+        RS_P(Lo, p) = l;
       }
       const bool ok = mbar_wait_bounded(bar + b, (uint32_t)((it >> 1) & 1));
       if (__syncthreads_or(!ok)) {
@@ -1029,162 +1059,67 @@ __global__ void __launch_bounds__(512) k_flux_y_mixed(DevTransport<double> T, St
       for (int p = (int)ty - 3; p <= n + 2; p += blockDim.y) {
         float h, l;
         cell(p, h, l);
-        RS_Y(H, p) = h;
-        RS_Y(Lo, p) = l;
+        RS_P(H, p) = h;
+        RS_P(Lo, p) = l;
       }
       __syncthreads();
     }
-    for (int p = (int)ty - 3; p <= n + 1; p += blockDim.y)
-      RS_Y(Dl, p) = (RS_Y(H, p + 1) - RS_Y(H, p)) + (RS_Y(Lo, p + 1) - RS_Y(Lo, p));
-    __syncthreads();
-    for (int p = (int)ty - 2; p <= n + 1; p += blockDim.y)
-      RS_Y(S, p) = slope_from_diff(RS_Y(Dl, p - 1), RS_Y(Dl, p));
-    __syncthreads();
-    auto face = [&](int f, bool ghosts) {
-      const size_t fb = ((size_t)k * nfj + f) * T.nlon + i;
-      const double M = Mf[f * kPencil + tx];
-      const bool right = __double_as_longlong(M) > 0;
-      const int up = right ? f - 1 : f;
-      float aL = -0.5f * RS_Y(Dl, up - 1) - (RS_Y(S, up) - RS_Y(S, up - 1)) * (1.0f / 6.0f);
-      float aR = 0.5f * RS_Y(Dl, up) - (RS_Y(S, up + 1) - RS_Y(S, up)) * (1.0f / 6.0f);
-      limitf(0.0f, aL, aR);
-      double a2;
-      if (!ghosts || (up >= 0 && up < n)) a2 = Q[pb + (size_t)up * T.nlon + i];
-      else a2 = (double)RS_Y(H, up) + (double)RS_Y(Lo, up);
-      T.fy[(size_t)s * fplane + fb] = mixed_flux(M, Mf32[f * kPencil + tx], a2, right ? aR : aL);
-    };
-    if (live) {
-      if (open) {
-        for (int f = ty; f <= n; f += blockDim.y) face(f, true);
-      } else {  // walls: zero flux on the two boundary faces, interior faces have no ghosts
-        for (int f = ty; f <= n; f += blockDim.y) {
-          if (f == 0 || f == n) T.fy[(size_t)s * fplane + ((size_t)k * nfj + f) * T.nlon + i] = 0.0;
-          else face(f, false);
-        }
-      }
+    for (int p = (int)ty - 3; p <= n + 1; p += blockDim.y) {
+      const df d = df_sub(df{RS_P(H, p + 1), RS_P(Lo, p + 1)}, df{RS_P(H, p), RS_P(Lo, p)});
+      RS_P(Dh, p) = d.h;
+      RS_P(Dl, p) = d.l;
     }
     __syncthreads();
-  }
-#undef RS_Y
-}
-
-template <int kPencil, bool kTma>
-__global__ void __launch_bounds__(512) k_flux_z_mixed(DevTransport<double> T, StageSel sel, int sper,
-                                                      const __grid_constant__ CUtensorMap mh,
-                                                      const __grid_constant__ CUtensorMap ml) {
-  const double* Q;
-  double g;
-  if (!resolve_stage(sel, Q, g)) return;
-  const int s0 = blockIdx.y * sper, s1 = min(T.ntr, s0 + sper);  // this block's tracers
-  extern __shared__ __align__(16) unsigned char smz32_raw[];
-  float* smz32 = align128(smz32_raw);
-  __shared__ __align__(8) unsigned long long bar[2];
-  const int n = T.nlev, L = mixed_rows_p(n);
-  const int R = L * kPencil;
-  float* const H0 = smz32;
-  float* const L0 = smz32 + R;
-  float* const H1 = smz32 + (kTma ? 2 * R : 0);
-  float* const L1 = smz32 + (kTma ? 3 * R : R);
-  float* Dl = smz32 + (kTma ? 4 : 2) * R;
-  float* S = Dl + R;
-  float* Mf32 = S + R;  // [n+1][kPencil]
-  double* Mf = reinterpret_cast<double*>(Mf32 + (n + 1) * kPencil);
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  const bool lead = tx == 0 && ty == 0;
-  const size_t ncol = (size_t)T.nlon * T.nlat;
-  const size_t col0 = (size_t)blockIdx.x * kPencil;
-  const size_t col = col0 + tx;
-  const bool live = col < ncol;
-  const size_t nc = ncol * n;
-  const size_t fplane = ncol * (n + 1);
-  int uses0 = 0, uses1 = 0;  // copies issued per buffer
-  auto issue = [&](int s, int b) {  // levels 0..n-1 of columns col0..: box {kPencil, n, 1}
-    fence_proxy_async();
-    mbar_expect_tx(bar + b, (uint32_t)(2 * n * kPencil * sizeof(float)));
-    tma_load_3d((b ? H1 : H0) + kHoP * kPencil, &mh, (int)col0, 0, s, bar + b);
-    tma_load_3d((b ? L1 : L0) + kHoP * kPencil, &ml, (int)col0, 0, s, bar + b);
-  };
-  if (kTma) {
-    if (lead) {
-      mbar_init(bar);
-      mbar_init(bar + 1);
-      fence_mbar_init();
+    for (int p = (int)ty - 2; p <= n + 1; p += blockDim.y) {
+      const df d0{RS_P(Dh, p - 1), RS_P(Dl, p - 1)}, d1{RS_P(Dh, p), RS_P(Dl, p)};
+      df sl{0.0f, 0.0f};
+      if (DIR == 1) {
+        sl = mc_slope(d0, d1);
+      } else if (p >= -1 && p <= n && live) {  // slopes of cells -1..n (coefficient row p+1)
+        const size_t x = bck(T, (size_t)(p + 1) * ncol + col, (long long)(n + 2) * ncol);
+        sl = mc_slope_n(d0, d1, df_ld2(T.vsA2, x), df_ld2(T.vsB2, x));
+      }
+      RS_P(Sh, p) = sl.h;
+      RS_P(Sl, p) = sl.l;
     }
     __syncthreads();
-    if (lead && s0 < s1) issue(s0, 0);
-    uses0 = s0 < s1;
-  }
-  if (live)
-    for (int kf = ty; kf <= n; kf += blockDim.y) {
-      const double M = g * T.mz[(size_t)kf * ncol + col];
-      Mf[kf * kPencil + tx] = M;
-      Mf32[kf * kPencil + tx] = (float)M;
-    }
-#define RS_Z(a, p) a[((p) + kHoP) * kPencil + tx]
-  for (int s = s0; s < s1; ++s) {
-    const int it = s - s0, b = kTma ? (it & 1) : 0;
-    float* H = b ? H1 : H0;
-    float* Lo = b ? L1 : L0;
-    const size_t pb = (size_t)s * nc + col;
-    if (kTma) {
-      if (s + 1 < s1) {
-        if (lead) issue(s + 1, b ^ 1);
-        if (b) uses0 += 1;
-        else uses1 += 1;
+    // edge terms over the staged values: cells -2..n (uniform), -1..n-1 (coefficient rows
+    // 0..n of the dp-weighted edges)
+    for (int p = (int)ty - 2; p <= n; p += blockDim.y) {
+      const df Dp{RS_P(Dh, p), RS_P(Dl, p)};
+      const df Sp{RS_P(Sh, p), RS_P(Sl, p)}, Sp1{RS_P(Sh, p + 1), RS_P(Sl, p + 1)};
+      df e{0.0f, 0.0f};
+      if (DIR == 1) {
+        e = edge_u(Dp, Sp, Sp1);
+      } else if (p >= -1 && p <= n - 1 && live) {
+        const size_t x = bck(T, (size_t)(p + 1) * ncol + col, (long long)(n + 1) * ncol);
+        e = edge_n(Dp, Sp, Sp1, df_ld2(T.veAB2, x), df_ld2(T.veC2, x), df_ld2(T.veD2, x));
       }
-      for (int r = ty; r < 6; r += blockDim.y) {  // mirrored ghost levels
-        const int p = r < 3 ? r - 3 : n + r - 3;
-        const int pp = p < 0 ? -1 - p : 2 * n - 1 - p;
-        RS_Z(H, p) = live ? T.qhi[pb + (size_t)pp * ncol] : 0.0f;
-        RS_Z(Lo, p) = live ? T.qlo[pb + (size_t)pp * ncol] : 0.0f;
-      }
-      const bool ok = mbar_wait_bounded(bar + b, (uint32_t)((it >> 1) & 1));
-      if (__syncthreads_or(!ok)) {
-        staging_abort(T.tma_err, sel.ctl, bar, uses0, uses1);
-        return;
-      }
-    } else {
-      for (int p = (int)ty - 3; p <= n + 2; p += blockDim.y) {
-        const int pp = p < 0 ? -1 - p : (p >= n ? 2 * n - 1 - p : p);
-        RS_Z(H, p) = live ? T.qhi[pb + (size_t)pp * ncol] : 0.0f;
-        RS_Z(Lo, p) = live ? T.qlo[pb + (size_t)pp * ncol] : 0.0f;
-      }
-      __syncthreads();
-    }
-    for (int p = (int)ty - 3; p <= n + 1; p += blockDim.y)
-      RS_Z(Dl, p) = (RS_Z(H, p + 1) - RS_Z(H, p)) + (RS_Z(Lo, p + 1) - RS_Z(Lo, p));
-    __syncthreads();
-    for (int p = (int)ty - 1; p <= n; p += blockDim.y) {  // slopes of cells -1..n (coefficient row p+1)
-      const float sA = live ? T.vsA32[(size_t)(p + 1) * ncol + col] : 0.0f;
-      const float sB = live ? T.vsB32[(size_t)(p + 1) * ncol + col] : 0.0f;
-      RS_Z(S, p) = slope_from_diff_n(RS_Z(Dl, p - 1), RS_Z(Dl, p), sA, sB);
+      RS_P(H, p) = e.h;
+      RS_P(Lo, p) = e.l;
     }
     __syncthreads();
     if (live) {
-      for (int kf = ty; kf <= n; kf += blockDim.y) {
-        if (kf == 0 || kf == n) {
-          T.fz[(size_t)s * fplane + (size_t)kf * ncol + col] = 0.0;
-          continue;
-        }
-        const double M = Mf[kf * kPencil + tx];
-        const bool right = __double_as_longlong(M) > 0;
-        const int up = right ? kf - 1 : kf;
-        const float lab = T.veAB32[(size_t)up * ncol + col], lc = T.veC32[(size_t)up * ncol + col],
-                    ld = T.veD32[(size_t)up * ncol + col];
-        const float rab = T.veAB32[(size_t)(up + 1) * ncol + col],
-                    rc = T.veC32[(size_t)(up + 1) * ncol + col],
-                    rd = T.veD32[(size_t)(up + 1) * ncol + col];
-        float aL = (lab - 1.0f) * RS_Z(Dl, up - 1) + lc * RS_Z(S, up) + ld * RS_Z(S, up - 1);
-        float aR = rab * RS_Z(Dl, up) + rc * RS_Z(S, up + 1) + rd * RS_Z(S, up);
-        limitf(0.0f, aL, aR);
-        const double a2 = Q[pb + (size_t)up * ncol];
-        T.fz[(size_t)s * fplane + (size_t)kf * ncol + col] =
-            mixed_flux(M, Mf32[kf * kPencil + tx], a2, right ? aR : aL);
+      for (int p = ty; p < n; p += blockDim.y) {
+        df psi, phi;
+        cell_faces(df{Mh[bck(T, p * kPencil + tx, mb)], Ml[bck(T, p * kPencil + tx, mb)]},
+                   df{Mh[bck(T, (p + 1) * kPencil + tx, mb)], Ml[bck(T, (p + 1) * kPencil + tx, mb)]},
+                   [&](int o) { return df{RS_P(H, p + o), RS_P(Lo, p + o)}; },
+                   [&](int o) { return df{RS_P(Dh, p + o), RS_P(Dl, p + o)}; }, psi, phi);
+        df a;
+        if (DIR == 1)
+          a = df_neg(df_add(df_mul(df_ld2(T.gyhi2, p), phi), df_mul(df_ld2(T.gylo2, p), psi)));
+        else
+          a = df_neg(df_add(phi, psi));
+        const size_t x = bck(T, pb + (size_t)p * stride, nall);
+        const float2 o = T.acc[x];
+        const df t = df_add(df{o.x, o.y}, a);
+        T.acc[x] = make_float2(t.h, t.l);
       }
     }
     __syncthreads();
   }
-#undef RS_Z
+#undef RS_P
 }
 
 // ------------------------------------------------------------------ stage kernel
@@ -1222,6 +1157,16 @@ __device__ __forceinline__ void split_store(const DevTransport<double>& T, size_
 #endif
   T.qhi[x] = hi;
   T.qlo[x] = lo;
+}
+__device__ __forceinline__ df split_df(double v) {
+  df r;
+#if RS_STRICT
+  r.h = (float)v;
+  r.l = (float)(v - (double)r.h);
+#else
+  split_bits(v, r.h, r.l);
+#endif
+  return r;
 }
 
 // split the attempt's input state U[cur] (stage 1's RHS argument) into hi/lo planes
@@ -1409,7 +1354,22 @@ __global__ void __launch_bounds__(kRedThreads) k_stage(DevTransport<double> T,
       double scale = dt_2;
       bool per_m = false;  // du is the tendency times m (1/m folded into the scale)
 #endif
-      if (s < T.ntr) {
+      if (s < T.ntr && T.mixed) {
+        // compensated FP32 transport: the pencils accumulated m dq/dt as a pair
+        const double ab = df_to_d(T.acc[x]);
+#if RS_STRICT
+        du = ab / m;
+        if (T.pbl) du = du + pbl_term(T, c, col, s, q);
+#else
+        if (T.pbl) {
+          du = fma(ab, rm, pbl_term(T, c, col, s, q));
+        } else {
+          du = ab;
+          scale = sc;
+          per_m = true;
+        }
+#endif
+      } else if (s < T.ntr) {
         double fw = T.fx[s * fxp + fxi], fe = T.fx[s * fxp + fxi + 1];
         double fs = T.fy[s * fyp + fyi], fn = T.fy[s * fyp + fyi + T.nlon];
         double fb = T.fz[s * fzp + fzi], ft = T.fz[s * fzp + fzi + ncol];
@@ -1515,7 +1475,12 @@ __global__ void __launch_bounds__(kRedThreads) k_rhs_eval(DevTransport<double> T
   const size_t fzi = (size_t)k * ncol + col;
   for (int s = 0; s < T.nsp; ++s) {
     size_t x = (size_t)s * nc + c;
-    if (s < T.ntr) {
+    if (s < T.ntr && T.mixed) {  // the pencils accumulated m dq/dt as a pair
+      const double ab = df_to_d(T.acc[x]);
+      const double adv = has_m ? ab / m : ab;
+      dU[x] = T.pbl ? adv + pbl_term(T, c, col, s, Qin[x]) : adv;
+      if (dUadv) dUadv[x] = adv;
+    } else if (s < T.ntr) {
       double fw = T.fx[s * fxp + fxi], fe = T.fx[s * fxp + fxi + 1];
       double fs = T.fy[s * fyp + fyi], fn = T.fy[s * fyp + fyi + T.nlon];
       double fb = T.fz[s * fzp + fzi], ft = T.fz[s * fzp + fzi + ncol];
@@ -1548,16 +1513,16 @@ static void allow_big_smem() {
   cudaFuncSetAttribute(k_flux_z_fused<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
   cudaFuncSetAttribute(k_flux_z_fused<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
   cudaFuncSetAttribute(k_flux_z_fused<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
-  cudaFuncSetAttribute(k_flux_x_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
-  cudaFuncSetAttribute(k_flux_x_mixed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
-  cudaFuncSetAttribute(k_flux_y_mixed<16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
-  cudaFuncSetAttribute(k_flux_y_mixed<32, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
-  cudaFuncSetAttribute(k_flux_y_mixed<16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
-  cudaFuncSetAttribute(k_flux_y_mixed<32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
-  cudaFuncSetAttribute(k_flux_z_mixed<16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
-  cudaFuncSetAttribute(k_flux_z_mixed<32, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
-  cudaFuncSetAttribute(k_flux_z_mixed<16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
-  cudaFuncSetAttribute(k_flux_z_mixed<32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_adv_x_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_adv_x_mixed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_adv_yz_mixed<1, 16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_adv_yz_mixed<1, 16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_adv_yz_mixed<1, 32, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_adv_yz_mixed<1, 32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_adv_yz_mixed<2, 16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_adv_yz_mixed<2, 16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_adv_yz_mixed<2, 32, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(k_adv_yz_mixed<2, 32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
   done = true;
 }
 
@@ -1628,21 +1593,16 @@ static void launch_flux_one(cudaStream_t st, const DevTransport<double>& T, cons
   }
 }
 
-// Mixed-precision pencils: four FP32 rows (hi, lo, neighbour differences, slopes; six with the
-// second hi / lo set of the bulk-copy staging) plus the n+1 face fluxes as float and double, per
-// pencil.  A direction that does not fit uses the per-face FP32 kernel (the same deviation-form
-// reconstruction, evaluated per face).
-static size_t mixed_pencil_bytes(int n, int pw, bool tma) {
-  const int rows = tma ? 6 : 4;
-  if (pw == 1) {
-    const int L = mixed_rows_x(n);
-    return (size_t)rows * L * sizeof(float) + (size_t)((n + 2) / 2 * 2) * sizeof(float) +
-           (size_t)(n + 1) * sizeof(double) + kSmemAlignPad;
-  }
-  const int L = mixed_rows_p(n);
-  return ((size_t)rows * L * sizeof(float) + (size_t)(n + 1) * (sizeof(float) + sizeof(double))) * pw +
-         kSmemAlignPad;
+// Mixed-precision pencils: the staged hi / lo rows (four with the second set of the bulk-copy
+// staging), the pair rows of the differences and slopes, and the face fluxes as pairs.
+size_t mixed_pencil_bytes(int n, int pw, bool tma) {
+  const int rows = tma ? 8 : 6;
+  if (pw == 1)
+    return (size_t)rows * mixed_rows_x(n) * sizeof(float) + 2 * (size_t)mixed_frows(n) * sizeof(float) +
+           kSmemAlignPad;
+  return ((size_t)rows * mixed_rows_p(n) + 2 * (size_t)(n + 1)) * pw * sizeof(float) + kSmemAlignPad;
 }
+size_t mixed_pencil_cap() { return (size_t)kPencilSmemCap; }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link to the driver
 // library); null when the entry point is unavailable.
@@ -1686,10 +1646,11 @@ MixedTmaps* mixed_tmaps_create(const DevTransport<double>& T, const char** why) 
   auto* m = new MixedTmaps();
   const uint64_t ncol = (uint64_t)T.nlon * T.nlat;
   // 1-D bulk copies of lon rows: 16-byte aligned starts and sizes need nlon % 4 == 0
-  m->x_ok = T.nlon % 4 == 0;
+  const size_t cap = (size_t)kPencilSmemCap;
+  m->x_ok = T.nlon % 4 == 0 && mixed_pencil_bytes(T.nlon, 1, true) <= cap;
   // tensor strides must be multiples of 16 bytes; boxes at most 256 rows
-  m->y_ok = T.nlon % 4 == 0 && T.nlat <= 256;
-  m->z_ok = ncol % 4 == 0 && T.nlev <= 256;
+  m->y_ok = T.nlon % 4 == 0 && T.nlat <= 256 && mixed_pencil_bytes(T.nlat, 16, true) <= cap;
+  m->z_ok = ncol % 4 == 0 && T.nlev <= 256 && mixed_pencil_bytes(T.nlev, 16, true) <= cap;
   for (int w = 0; w < 2 && m->y_ok; ++w) {
     const uint32_t pw = w ? 32 : 16;
     m->y_ok = encode_f32_3d(&m->yh[w], T.qhi, T.nlon, T.nlat, (uint64_t)T.nlev * T.ntr, pw, T.nlat) &&
@@ -1731,48 +1692,34 @@ static void launch_fluxes_mixed(cudaStream_t st, const DevTransport<double>& T, 
   const size_t shx = mixed_pencil_bytes(T.nlon, 1, tx), shy = mixed_pencil_bytes(T.nlat, pw, ty),
                shz = mixed_pencil_bytes(T.nlev, pw, tz);
   static const CUtensorMap kNoMap{};  // placeholder argument of the plain-load variants
+  // rs_create refuses mixed precision on grids whose pencils do not fit at width 16
   if (only_dir < 0 || only_dir == 0) {
-    if (shx <= (size_t)kPencilSmemCap) {
-      dim3 grid((unsigned)(T.nlat * T.nlev), groups(sx));
-      if (tx) k_flux_x_mixed<true><<<grid, xt, shx, st>>>(T, sel, sx);
-      else k_flux_x_mixed<false><<<grid, xt, shx, st>>>(T, sel, sx);
-    } else {
-      long long nx = (long long)(T.nlon + 1) * T.nlat * T.nlev;
-      k_flux_x<<<(unsigned)((nx + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);
-    }
+    dim3 grid((unsigned)(T.nlat * T.nlev), groups(sx));
+    if (tx) k_adv_x_mixed<true><<<grid, xt, shx, st>>>(T, sel, sx);
+    else k_adv_x_mixed<false><<<grid, xt, shx, st>>>(T, sel, sx);
   }
   if (only_dir < 0 || only_dir == 1) {
-    if (shy <= (size_t)kPencilSmemCap) {
-      dim3 grid((unsigned)((T.nlon + pw - 1) / pw) * (unsigned)T.nlev, groups(syz));
-      const CUtensorMap& mh = ty ? tm->yh[w] : kNoMap;
-      const CUtensorMap& ml = ty ? tm->yl[w] : kNoMap;
-      if (pw == 16) {
-        if (ty) k_flux_y_mixed<16, true><<<grid, dim3(16, rows), shy, st>>>(T, sel, syz, mh, ml);
-        else k_flux_y_mixed<16, false><<<grid, dim3(16, rows), shy, st>>>(T, sel, syz, mh, ml);
-      } else {
-        if (ty) k_flux_y_mixed<32, true><<<grid, dim3(32, rows), shy, st>>>(T, sel, syz, mh, ml);
-        else k_flux_y_mixed<32, false><<<grid, dim3(32, rows), shy, st>>>(T, sel, syz, mh, ml);
-      }
+    dim3 grid((unsigned)((T.nlon + pw - 1) / pw) * (unsigned)T.nlev, groups(syz));
+    const CUtensorMap& mh = ty ? tm->yh[w] : kNoMap;
+    const CUtensorMap& ml = ty ? tm->yl[w] : kNoMap;
+    if (pw == 16) {
+      if (ty) k_adv_yz_mixed<1, 16, true><<<grid, dim3(16, rows), shy, st>>>(T, sel, syz, mh, ml);
+      else k_adv_yz_mixed<1, 16, false><<<grid, dim3(16, rows), shy, st>>>(T, sel, syz, mh, ml);
     } else {
-      long long ny = (long long)T.nlon * (T.nlat + 1) * T.nlev;
-      k_flux_y<<<(unsigned)((ny + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);
+      if (ty) k_adv_yz_mixed<1, 32, true><<<grid, dim3(32, rows), shy, st>>>(T, sel, syz, mh, ml);
+      else k_adv_yz_mixed<1, 32, false><<<grid, dim3(32, rows), shy, st>>>(T, sel, syz, mh, ml);
     }
   }
   if (only_dir < 0 || only_dir == 2) {
-    if (shz <= (size_t)kPencilSmemCap) {
-      dim3 grid((unsigned)((ncol + pw - 1) / pw), groups(syz));
-      const CUtensorMap& mh = tz ? tm->zh[w] : kNoMap;
-      const CUtensorMap& ml = tz ? tm->zl[w] : kNoMap;
-      if (pw == 16) {
-        if (tz) k_flux_z_mixed<16, true><<<grid, dim3(16, rows), shz, st>>>(T, sel, syz, mh, ml);
-        else k_flux_z_mixed<16, false><<<grid, dim3(16, rows), shz, st>>>(T, sel, syz, mh, ml);
-      } else {
-        if (tz) k_flux_z_mixed<32, true><<<grid, dim3(32, rows), shz, st>>>(T, sel, syz, mh, ml);
-        else k_flux_z_mixed<32, false><<<grid, dim3(32, rows), shz, st>>>(T, sel, syz, mh, ml);
-      }
+    dim3 grid((unsigned)((ncol + pw - 1) / pw), groups(syz));
+    const CUtensorMap& mh = tz ? tm->zh[w] : kNoMap;
+    const CUtensorMap& ml = tz ? tm->zl[w] : kNoMap;
+    if (pw == 16) {
+      if (tz) k_adv_yz_mixed<2, 16, true><<<grid, dim3(16, rows), shz, st>>>(T, sel, syz, mh, ml);
+      else k_adv_yz_mixed<2, 16, false><<<grid, dim3(16, rows), shz, st>>>(T, sel, syz, mh, ml);
     } else {
-      long long nz = (long long)T.nlon * T.nlat * (T.nlev + 1);
-      k_flux_z<<<(unsigned)((nz + kFluxThreads - 1) / kFluxThreads), kFluxThreads, 0, st>>>(T, sel);
+      if (tz) k_adv_yz_mixed<2, 32, true><<<grid, dim3(32, rows), shz, st>>>(T, sel, syz, mh, ml);
+      else k_adv_yz_mixed<2, 32, false><<<grid, dim3(32, rows), shz, st>>>(T, sel, syz, mh, ml);
     }
   }
 }
