@@ -1311,10 +1311,26 @@ int or_macro_step(or_model* h, double* u, double t0, double t1, double* dtT, dou
   return 0;
 }
 
+// Step sizes of the per-cell form rounded down to 4 fraction bits (16 sizes per octave), as the
+// batched kernel does: the per-cell trajectories then move by roundoff, not by the integration
+// tolerance, under roundoff-sized input changes.  No reference counterpart (the reference has
+// one global dt).
+static double quant_dt(double d) {
+  uint64_t b;
+  std::memcpy(&b, &d, sizeof b);
+  b &= ~((uint64_t(1) << 48) - 1);
+  std::memcpy(&d, &b, sizeof b);
+  return d;
+}
+
 // Per-cell adaptive chemistry (each cell its own ROS23 + PI controller over [t0,t1]), the
 // algorithm of the batched persistent kernel; error norm over the cell's own states.
-int or_chem_per_cell(or_model* h, double* u, double t0, double t1, double dt0, double* dt_out,
+// dt_io (may be null): per-cell step sizes carried in (a cell with dt_io <= 0 starts from dt0)
+// and out, as the batched kernel carries them from one macro step to the next.
+int or_chem_per_cell(or_model* h, double* u, double t0, double t1, double dt0, double* dt_io,
                      double* steps_out) {
+  const double* dt_in = dt_io;
+  double* dt_out = dt_io;
   Model& md = *reinterpret_cast<Model*>(h);
   size_t nc = md.G.nc;
   int ns = md.M.ns, nsp = md.nsp;
@@ -1328,7 +1344,8 @@ int or_chem_per_cell(or_model* h, double* u, double t0, double t1, double dt0, d
     for (int r = 0; r < md.M.nr; ++r) kr[r] = md.krates[(size_t)r * nc + cell];
     if (he)
       for (int s = 0; s < ns; ++s) em[s] = md.F.emis[(size_t)s * nc + cell];
-    double t = t0, dt = dt0, qold = c.qoldinit, iters = 0, nacc = 0;
+    double t = t0, dt = quant_dt(dt_in && dt_in[cell] > 0.0 ? dt_in[cell] : dt0), qold = c.qoldinit,
+           iters = 0, nacc = 0;
     double tlim = t1 - 1.0e-9;
     double invqmax = 1.0 / c.qmax, invqmin = 1.0 / c.qmin;
     while ((t < tlim) && (iters < md.cfg.maxiters)) {
@@ -1350,11 +1367,11 @@ int or_chem_per_cell(or_model* h, double* u, double t0, double t1, double dt0, d
         for (int s = 0; s < ns; ++s) x[s] = md.cfg.clamp_nonneg ? std::max(xn[s], 0.0) : xn[s];
         t = t + dtc;
         bool insteady = (c.qsteady_min <= q) && (q <= c.qsteady_max);
-        dt = dtc / (insteady ? 1.0 : q);
+        dt = quant_dt(dtc / (insteady ? 1.0 : q));
         qold = std::max(EEst, c.qoldinit);
         nacc += 1.0;
       } else {
-        dt = dtc / std::min(invqmin, q11 / c.gamma);
+        dt = quant_dt(dtc / std::min(invqmin, q11 / c.gamma));
       }
       iters += 1.0;
     }

@@ -145,13 +145,15 @@ class Oracle:
         rc = lib().or_macro_step(self.h, _p(u), t0, t1, C.byref(a), C.byref(b), _p(st))
         return rc, a.value, b.value, st
 
-    def chem_per_cell(self, u, t0, t1, dt0):
+    def chem_per_cell(self, u, t0, t1, dt0, dt_cell=None):
+        """Per-cell adaptive chemistry over [t0, t1], in place on u (grid SoA).  dt_cell (may be
+        None): per-cell step sizes carried in (<= 0: start from dt0); returns (status, the
+        carried step sizes, accepted steps per cell)."""
         assert u.flags.c_contiguous and u.dtype == np.float64
-        dt = np.empty(self.nc)
+        dt = np.zeros(self.nc) if dt_cell is None else np.array(dt_cell, dtype=np.float64)
         steps = np.empty(self.nc)
         rc = lib().or_chem_per_cell(self.h, _p(u), t0, t1, dt0, _p(dt), _p(steps))
         return rc, dt, steps
-
 
     # ---------------------------------------------------------------- discrete adjoint
     def record_clear(self):

@@ -202,7 +202,9 @@ __global__ void k_block_jac(DevMech M, int nc, int nsp, const double* __restrict
 // its own ROS23 + PI controller over [t0, t1] (the reference controller,
 // rx_traced_integrator.jl:455-507, applied per cell with the cell's own hairer norm).  Lanes
 // of a warp run the same attempt code on different cells, so uneven step counts do not idle
-// lanes: a lane whose cell finishes takes the next one from the queue.
+// lanes: a lane whose cell finishes takes the next one from the queue.  Step sizes are rounded
+// down to 4 fraction bits (quant_dt), which keeps per-cell trajectories insensitive to
+// roundoff-sized input changes.
 template <int MS, int MR, int MLU, int MP>
 __global__ void __launch_bounds__(256) k_chem_per_cell(
     DevMech M, int nc, int nsp, double* __restrict__ U, const double* __restrict__ krates,
@@ -224,7 +226,7 @@ __global__ void __launch_bounds__(256) k_chem_per_cell(
       if (emission)
         for (int s = 0; s < M.ns; ++s) w.em[s] = emission[(size_t)s * nc + c];
       t = a.t0;
-      dt = dt_cell[c] > 0.0 ? dt_cell[c] : a.dt0;
+      dt = quant_dt(dt_cell[c] > 0.0 ? dt_cell[c] : a.dt0);
       qold = a.qoldinit;
       iters = 0;
       nacc = 0;
@@ -242,11 +244,11 @@ __global__ void __launch_bounds__(256) k_chem_per_cell(
         for (int s = 0; s < M.ns; ++s) w.x[s] = a.clamp ? fmax(w.xn[s], 0.0) : w.xn[s];
         t = t + dtc;
         bool insteady = (a.qsmin <= q) && (q <= a.qsmax);
-        dt = dtc / (insteady ? 1.0 : q);
+        dt = quant_dt(dtc / (insteady ? 1.0 : q));
         qold = fmax(EEst, a.qoldinit);
         nacc += 1.0;
       } else {
-        dt = dtc / fmin(a.invqmin, q11 / a.gamma);
+        dt = quant_dt(dtc / fmin(a.invqmin, q11 / a.gamma));
       }
       iters += 1.0;
     } else {

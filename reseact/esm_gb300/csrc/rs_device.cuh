@@ -18,6 +18,25 @@ namespace rs {
 
 constexpr int kRedThreads = 256;  // fixed reduction chunk (cells per level-1 partial)
 
+// Step sizes of the per-cell adaptive form are rounded down to 4 fraction bits (16 sizes per
+// octave).  The per-cell controller alone decides each cell's step sequence, and on stiff
+// mechanisms a roundoff-sized input change flips some cells' accept / reject decisions and moves
+// them by up to the integration tolerance (a 1-ulp change of dt0 moves ~0.4 % of the C3 cells
+// by more than 1e-6 relative).  On the lattice a sequence changes only where a proposal lies
+// within the perturbation of a lattice point, at the price of ~3 % more steps.  The global-dt
+// (reference) controller is not rounded.
+__host__ __device__ inline double quant_dt(double d) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double(__double_as_longlong(d) & ~((1ll << 48) - 1));
+#else
+  unsigned long long b;
+  __builtin_memcpy(&b, &d, sizeof b);
+  b &= ~((1ull << 48) - 1);
+  __builtin_memcpy(&d, &b, sizeof b);
+  return d;
+#endif
+}
+
 // ------------------------------------------------------------------ mechanism tables
 // Derived on the host from rs_mechanism (derive_tables in rs_api.cu); all index arrays are warp-uniform
 // reads (every thread walks the same table), served by the L1/texture path.

@@ -413,6 +413,14 @@ __device__ __forceinline__ double amax_bits(double a, double b) {
   return __hiloint2double((int)(bl ? hb : ha), (int)(bl ? lb : la));
 }
 
+// Per-cell step sizes are rounded down to 4 fraction bits (16 sizes per octave): a perturbation
+// of the inputs then changes a cell's step sequence only where a proposal sits within the
+// perturbation of a lattice point, so per-cell trajectories stay within roundoff of each other
+// under roundoff-sized changes.
+__device__ __forceinline__ double quant_dt(double d) {
+  return __longlong_as_double(__double_as_longlong(d) & ~((1ll << 48) - 1));
+}
+
 // pairwise tree over 256 lanes, v[t] += v[t+s] for s = 128 ... 1; total in thread 0
 __device__ __forceinline__ double tree256(double v, double* sm) {
   const int t = threadIdx.x;
@@ -638,7 +646,7 @@ __device__ __forceinline__ void per_cell_body(int nc, int nsp, double* __restric
       for (int s = 0; s < NS; ++s) x[s] = U[(u64)s * N + c];
       have = false;
       t = a.t0;
-      dt = dt_cell[c] > 0.0 ? dt_cell[c] : a.dt0;
+      dt = quant_dt(dt_cell[c] > 0.0 ? dt_cell[c] : a.dt0);
       qold = a.qoldinit;
       iters = 0;
       nacc = 0;
@@ -669,11 +677,11 @@ __device__ __forceinline__ void per_cell_body(int nc, int nsp, double* __restric
         have = same;
         t = t + dtc;
         const bool insteady = (a.qsmin <= q) && (q <= a.qsmax);
-        dt = dtc / (insteady ? 1.0 : q);
+        dt = quant_dt(dtc / (insteady ? 1.0 : q));
         qold = fmax(EEst, a.qoldinit);
         nacc += 1.0;
       } else {
-        dt = dtc / fmin(a.invqmin, q11 / a.gamma);
+        dt = quant_dt(dtc / fmin(a.invqmin, q11 / a.gamma));
       }
       iters += 1.0;
     } else {

@@ -2,16 +2,16 @@
 import numpy as np
 
 
-def per_cell_agreement(got, ref, cfg, nsp):
-    """Per-cell adaptive integrations of a stiff problem agree to roundoff in cells that take
-    the same accept/reject sequence; a cell whose sequence flips (an error estimate within
-    roundoff of 1) ends at a different but equally valid point of the same tolerance.  So:
-    every entry within 10 x (rtol |u| + atol), at most 1 % of cells with any entry beyond
-    1 x that bound, and a median relative difference at roundoff level."""
+def per_cell_agreement(got, ref, cfg, nsp, flip_frac=1e-3):
+    """Per-cell adaptive integrations on the step-size lattice (4 fraction bits, 16 sizes per
+    octave) agree to roundoff: a cell's step sequence changes only where a step proposal lies
+    within roundoff of a lattice point or an error estimate within roundoff of 1.  So: every
+    cell within 1e-6 relative (the absolute tolerance as the floor) except at most `flip_frac`
+    of the cells, those within 10 x (rtol |u| + atol), and a median at roundoff level."""
+    rel = np.abs(got - ref) / np.maximum(np.abs(ref), cfg.atol_C)
+    cellmax = rel.reshape(-1, nsp).max(axis=1)
+    assert np.mean(cellmax > 1e-6) <= flip_frac, (np.mean(cellmax > 1e-6), cellmax.max())
     bound = cfg.rtol_C * np.abs(ref) + cfg.atol_C
     d = np.abs(got - ref) / bound
     assert d.max() <= 10.0, d.max()
-    flipped = np.any(d.reshape(-1, nsp) > 1.0, axis=1)
-    assert flipped.mean() <= 0.01, flipped.mean()
-    rel = np.abs(got - ref) / np.maximum(np.abs(ref), cfg.atol_C)
     assert np.median(rel) < 1e-12, np.median(rel)

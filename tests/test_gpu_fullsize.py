@@ -95,6 +95,7 @@ def test_c3_fullsize_per_cell_sample_vs_oracle():
     u = np.ascontiguousarray(sub.u0.copy())
     orc, _, steps = o.chem_per_cell(u, 0.0, 600.0, 1e-3)
     assert orc == 0
-    ref = u
-    gsub = got[:, :, j:j + 1, :]
+    # per cell: both in the cell-major layout
+    ref = workloads.soa_to_cellmajor(u, 1024, 1, 1)
+    gsub = workloads.soa_to_cellmajor(np.ascontiguousarray(got[:, :, j:j + 1, :]), 1024, 1, 1)
     per_cell_agreement(gsub, ref, cfg, sub.nsp)
