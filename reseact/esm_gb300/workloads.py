@@ -8,8 +8,8 @@ and value ranges of the benchmark configurations:
 * C1  36x18x10 global, 10 deg, levels 1000->100 hPa, solid-body u = 20 cos(lat) m/s,
       SuperFast, lognormal ICs (median = mechanism default, sigma 0.5), dt 600 s x 144.
 * C2  144x91x47 global (2.5 x 2 deg, pole-centred), deformational
-      u = 40 sin^2(lon) sin(2 lat) cos(pi t / 86400), w = +-0.05 Pa/s (seeded sign per
-      column), dt 600 s x 144 (24 h).
+      u = 40 sin^2(lon) sin(2 lat) cos(pi t / 86400), w = +-0.05 Pa/s sin(pi p / p_s) (seeded
+      sign per column), dt 600 s x 144 (24 h).
 * C3  2^20 independent cells, synthetic 30-species / 60-reaction mechanism, T ~ U(200,310) K,
       concentrations log-uniform 1e-12..1e-6 mol/mol, chemistry only.
 * C4  72x46x47 (5 x 4 deg), C2 winds, 24 h; surface NO emission field for the adjoint.
@@ -253,7 +253,11 @@ def c2(seed=2, mech=None, nlon=144, nlat=91, nlev=47, steps=144):
     g = latlon_grid(nlon, nlat, nlev, lon0=0.0, dlon=360.0 / nlon)
     dp, pm = pressure_levels(nlev)
     dp3, p3, t3 = _column_fields(g, dp, pm)
-    mx, my, mz = winds_deformational(g, dp, seed=seed + 100)
+    # w = +-0.05 Pa/s shaped as sin(pi p / p_s): a constant +-0.05 Pa/s takes ~1,300 of the
+    # 1,915 Pa out of the surface layer of every upward column by t = 9.3 h and the transport
+    # step then collapses (the oracle stalls there in a 24 h C4 run); the sine keeps the
+    # amplitude in the mid troposphere and bounds each layer's mass change to a few per cent
+    mx, my, mz = winds_deformational(g, dp, seed=seed + 100, w_shape="sine")
     u0 = lognormal_state(mech, g, dp3, seed)
     forcing = dict(mx=mx, my=my, mz=mz, dp=dp3, temperature=t3, pressure=p3,
                    flux_omega=math.pi / 86400.0)
