@@ -362,6 +362,13 @@ int32_t rs_record_taped(const rs_handle* h);
 rs_status rs_adjoint_set_lambda(rs_handle* h, const double* lambda, size_t n);
 rs_status rs_adjoint_get_lambda(rs_handle* h, double* lambda, size_t n);
 rs_status rs_backward_macro_step(rs_handle* h, int32_t k);
+/* Frozen-dt replay (replay_fixed, tools/adjoint_gradient.jl:647-669): re-run recorded macro
+ * step k on the resident state with its recorded accepted (t, dt) sequence of both halves
+ * (every step accepted, the clamp as recorded) and the forcing installed now -- the map
+ * whose derivative the discrete adjoint computes.  Central differences of a chain of these
+ * replays from a perturbed input check the adjoint (the reference's fdtape stage,
+ * tools/adjoint_gradient.jl:116-132).  FP64 global-dt handles only (RS_ERR_UNSUPPORTED). */
+rs_status rs_replay_macro_step(rs_handle* h, int32_t k);
 /* dJ/d(emission) accumulated so far, [n_species][nlev][nlat][nlon] (grid order) */
 rs_status rs_adjoint_get_grad_emission(rs_handle* h, double* grad, size_t n);
 rs_status rs_adjoint_reset_grad(rs_handle* h);
@@ -372,9 +379,16 @@ rs_status rs_adjoint_reset_grad(rs_handle* h);
  * No counterpart in the reference.  It allocates nothing, for callers that cannot allocate
  * device memory when they step (a host whose own memory pool owns the device, or a loop that
  * must not synchronise on an allocation): its scratch is a 524,800-byte array fixed in the
- * library, resolved per device on the first call on that device (make that first call before
- * any stream capture).  Limit: 16,777,216 cells (RS_ERR_INVALID beyond).  All calls share the
- * scratch, so calls that overlap on the GPU (other threads or streams) race; serialise them. */
+ * library, whose device address rs_create resolves for the handle's device (rs_create fails
+ * if it cannot).  Limit: 16,777,216 cells (RS_ERR_INVALID beyond).
+ * Ordering: the attempt runs on the handle's stream (rs_stream).  d_u_in must be complete on
+ * the device before the call -- synchronise the stream that wrote it, or make rs_stream wait
+ * on an event recorded after the write; the call returns after the handle's stream has
+ * finished, so d_u_out and *eest are ready on return.  The first call after a forcing change
+ * of temperature or pressure also launches the rate-constant kernel on that stream (into the
+ * handle's own buffers, allocated at rs_create).  All calls share the scratch, so calls that
+ * overlap on the GPU (other threads or streams) race; serialise them.  After cudaDeviceReset
+ * the library must be reloaded before this entry point is used again. */
 rs_status rs_ros23_attempt_noalloc(rs_handle* h, double dt, const double* d_u_in,
                                    double* d_u_out, double* eest);
 

@@ -9,7 +9,7 @@
 module ReseactGPU
 
 const LIB = Ref{String}(get(ENV, "RESEACT_GB300_LIB",
-    joinpath(@__DIR__, "..", "reseact", "esm_gb300", "_build", "libreseact_gb300.so")))
+    joinpath(@__DIR__, "..", "..", "reseact", "esm_gb300", "_build", "libreseact_gb300.so")))
 
 const RS_OK = Int32(0)
 const RS_ERR_MAXITERS = Int32(3)

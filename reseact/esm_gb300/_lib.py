@@ -20,6 +20,7 @@ SYMBOLS = [
     "rs_record", "rs_record_count", "rs_set_adjoint_tape", "rs_record_taped",
     "rs_adjoint_set_lambda", "rs_adjoint_get_lambda",
     "rs_backward_macro_step", "rs_adjoint_get_grad_emission", "rs_adjoint_reset_grad",
+    "rs_replay_macro_step",
     "rs_autotune", "rs_set_chem_kernel", "rs_get_chem_kernel", "rs_chem_kernel_source",
     "rs_chem_kernel_compile", "rs_chem_kernel_reciprocal", "rs_lu_order",
     "rs_mechanism_lu_order", "rs_continuity_drift", "rs_lie_trotter_solve",
@@ -91,6 +92,8 @@ def _declare(L):
         getattr(L, f).restype = C.c_int
     L.rs_backward_macro_step.argtypes = [vp, i32]
     L.rs_backward_macro_step.restype = C.c_int
+    L.rs_replay_macro_step.argtypes = [vp, i32]
+    L.rs_replay_macro_step.restype = C.c_int
     L.rs_adjoint_reset_grad.argtypes = [vp]
     L.rs_adjoint_reset_grad.restype = C.c_int
     L.rs_autotune.argtypes = [vp, C.c_char_p, sz]
@@ -313,6 +316,13 @@ class Solver:
         g = np.empty(ns * self.nc)
         self._check(self.L.rs_adjoint_get_grad_emission(self.h, _p(g), g.size))
         return out, g.reshape(ns, self.nlev, self.nlat, self.nlon)
+
+    def replay(self, steps=None):
+        """Frozen-dt replay of the recorded macro steps 0 .. steps-1 (all by default) on the
+        resident state with the forcing installed now (replay_fixed)."""
+        n = self.record_count() if steps is None else steps
+        for k in range(n):
+            self._check(self.L.rs_replay_macro_step(self.h, k))
 
     def autotune(self):
         """Pick the launch shapes of this handle's kernels by timing; returns the report."""

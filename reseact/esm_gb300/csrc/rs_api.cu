@@ -309,6 +309,7 @@ struct rs_handle {
   DevBuf<float> qhi, qlo;  // mixed-precision transport: split planes
   DevBuf<float> gx2, gylo2, gyhi2, vsA2, vsB2, veAB2, veC2, veD2;  // (hi, lo) pairs
   rs::MixedTmaps* tmaps = nullptr;  // bulk-copy staging of the mixed pencils (null: unavailable)
+  void* noalloc_base = nullptr;     // this device's scratch of rs_ros23_attempt_noalloc
   std::string tmaps_why;
   int staging = RS_STAGING_AUTO;
   DevBuf<int> tma_err;              // set by a pencil kernel whose staging wait ran out
@@ -906,6 +907,9 @@ rs_status guard(rs_handle* h, const std::function<void()>& fn) {
   }
 }
 thread_local std::string g_create_err;
+// Device address of the allocation-free attempt's scratch array on a device (defined with it
+// at the end of this file); rs_create resolves it for its device.
+void* noalloc_scratch(int dev);
 }  // namespace
 
 extern "C" {
@@ -937,6 +941,10 @@ rs_status rs_create(const rs_config* cfg, rs_handle** out) {
     }
     if (cfg->maxiters < 1) throw RsError(RS_ERR_INVALID, "maxiters");
     CK(cudaSetDevice(cfg->device));
+    // Resolve the scratch array of rs_ros23_attempt_noalloc on this device now: with lazy
+    // module loading the first lookup loads the module that holds the array (allocating and
+    // possibly synchronising), which must not happen inside the allocation-free call.
+    h->noalloc_base = noalloc_scratch(cfg->device);
     CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
     h->mt = derive_tables(cfg->mech, RS_STRICT != 0);
     auto& T = h->mt;
@@ -1753,6 +1761,51 @@ rs_status rs_adjoint_reset_grad(rs_handle* h) {
   });
 }
 
+// Frozen-dt replay of recorded macro step k on the RESIDENT state (replay_fixed,
+// tools/adjoint_gradient.jl:647-669): the recorded accepted (t, dt) of both halves, each step
+// accepted whatever its error, clamp as in the forward, with the forcing installed now.  The
+// composed map of these replays is the map the discrete adjoint differentiates; the reference
+// checks its gradient against central differences of it (the fdtape stage,
+// adjoint_gradient.jl:116-132).
+rs_status rs_replay_macro_step(rs_handle* h, int32_t k) {
+  if (!h) return RS_ERR_INVALID;
+  return guard(h, [&] {
+    if (k < 0 || k >= (int)h->recs.size()) throw RsError(RS_ERR_INVALID, "no such recorded step");
+    if (h->cfg.precision != RS_PREC_FP64 || h->cfg.chem_mode != RS_CHEM_GLOBAL_DT)
+      throw RsError(RS_ERR_UNSUPPORTED, "the replay is of the FP64 global-dt scheme");
+    ensure_rates(h);
+    const auto& r = h->recs[k];
+    const int nT = (int)(r.seqT.size() / 2), nC = (int)(r.seqC.size() / 2);
+    cudaStream_t st = h->st;
+    const int clamp = h->cfg.clamp_nonneg;
+    Ctl* c = h->ctl.p + 2;
+    const double ntot = (double)(h->nc * h->nsp);
+    int cur = h->cur;
+    for (int j = 0; j < nT + nC; ++j) {
+      const bool tr = j < nT;
+      const double tj = tr ? r.seqT[2 * j] : r.seqC[2 * (j - nT)];
+      const double dj = tr ? r.seqT[2 * j + 1] : r.seqC[2 * (j - nT) + 1];
+      // tend well past t + dt so that dtc = min(dt, tend - t) is the recorded dt exactly
+      Ctl init = make_ctl(h, tj, tj + 4.0 * dj + 1.0, dj, tr ? h->cfg.ctrl_T : h->cfg.ctrl_C, ntot);
+      init.cur = cur;
+      rs::launch_ctl_init(st, c, init);
+      if (tr) {
+        rs::TransportBufs B{h->U[0].p, h->U[1].p, h->S1.p, h->S2.p, h->S3.p, h->partial.p};
+        rs::launch_ssprk43_attempt(st, h->dt, c, B, h->cfg.rtol_T, h->cfg.atol_T, clamp);
+      } else {
+        rs::launch_ros23_step(h->lc, c, h->U[0].p, h->U[1].p, h->krates.p,
+                              h->have_emis ? h->emis.p : nullptr, h->partial.p,
+                              h->cfg.rtol_C, h->cfg.atol_C, clamp);
+      }
+      rs::launch_replay_accept(st, c);
+      cur ^= 1;
+    }
+    h->cur = cur;
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(st));
+  });
+}
+
 rs_status rs_backward_macro_step(rs_handle* h, int32_t k) {
   if (!h) return RS_ERR_INVALID;
   return guard(h, [&] {
@@ -2496,9 +2549,11 @@ constexpr int kNoAllocMaxDevices = 64;
 void* g_noalloc_addr[kNoAllocMaxDevices] = {nullptr};
 std::mutex g_noalloc_mu;
 
-// Device address of the scratch array for device `dev`, resolved on first use with that
-// device current.  Host code must not take the array's address directly: on the host the
-// symbol is only a stand-in.
+// Device address of the scratch array for device `dev`, resolved once per device by rs_create
+// with that device current (a failed lookup fails rs_create).  Host code must not take the
+// array's address directly: on the host the symbol is only a stand-in.  The cached address
+// belongs to the device's primary context; after cudaDeviceReset the library must be
+// reloaded before the entry point is used again.
 void* noalloc_scratch(int dev) {
   if (dev < 0 || dev >= kNoAllocMaxDevices) throw RsError(RS_ERR_INVALID, "device ordinal");
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
@@ -2529,7 +2584,7 @@ extern "C" rs_status rs_ros23_attempt_noalloc(rs_handle* h, double dt, const dou
         if (p >= 0 && p != d) cudaSetDevice(p);
       }
     } restore{h->cfg.device, prev};
-    unsigned char* base = static_cast<unsigned char*>(noalloc_scratch(h->cfg.device));
+    unsigned char* base = static_cast<unsigned char*>(h->noalloc_base);  // resolved by rs_create
     double* part = reinterpret_cast<double*>(base);
     Ctl* ctl = reinterpret_cast<Ctl*>(base + kNoAllocParts * sizeof(double));
     ensure_rates(h);

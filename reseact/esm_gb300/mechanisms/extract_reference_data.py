@@ -10,13 +10,17 @@ unchanged, prose descriptions dropped) for use where the reference tree is absen
 
 The 72-level table is ``prototypes/reseact_3d_chem/hybrid_coefs_L72.json`` (dA, dB, Ap, Bp).
 
-    python reseact/esm_gb300/mechanisms/extract_reference_data.py /root/reference
+    python reseact/esm_gb300/mechanisms/extract_reference_data.py REFERENCE_CHECKOUT
+
+REFERENCE_CHECKOUT is the root of an EarthSciML/reseact.esm checkout (required).
 """
 import json
 import os
 import sys
 
-ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: extract_reference_data.py REFERENCE_CHECKOUT")
+ref = sys.argv[1]
 src = os.path.join(ref, "prototypes", "g2_depsink", "g2_nodep.esm")
 with open(src) as fh:
     doc = json.load(fh)

@@ -42,6 +42,30 @@ def test_noalloc_attempt_matches_single_step_twice():
         assert e.value == pytest.approx(e_ref, rel=1e-12)
 
 
+def test_noalloc_second_call_allocates_no_device_memory():
+    """The property the entry point exists for: once the handle exists (rs_create resolved the
+    scratch array's address), a call changes the device's free memory by nothing."""
+    torch = pytest.importorskip("torch")
+    w = workloads.c2(nlon=16, nlat=9, nlev=6)
+    s = Solver.for_workload(w)
+    g = w.grid
+    u_soa = workloads.cellmajor_to_soa(w.u0_cellmajor(), w.nsp, g["nlon"], g["nlat"], g["nlev"])
+    d_in = torch.tensor(u_soa, dtype=torch.float64, device="cuda")
+    d_out = torch.empty_like(d_in)
+    e = C.c_double()
+    torch.cuda.synchronize()
+    rc = s.L.rs_ros23_attempt_noalloc(s.h, 3.0, _dptr(d_in), _dptr(d_out), C.byref(e))
+    assert rc == abi.RS_OK, s.L.rs_last_error(s.h)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        rc = s.L.rs_ros23_attempt_noalloc(s.h, 3.0, _dptr(d_in), _dptr(d_out), C.byref(e))
+        assert rc == abi.RS_OK
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
+
+
 def test_noalloc_rejects_grids_beyond_its_limit():
     torch = pytest.importorskip("torch")
     # one species, one first-order loss: just enough to build a handle of 2^24 + 4096 cells
