@@ -224,6 +224,9 @@ function get_lambda!(h::Handle, lam::Vector{Float64})
 end
 backward_macro_step!(h::Handle, k::Integer) =
     check(h, ccall((:rs_backward_macro_step, LIB[]), Int32, (Ptr{Cvoid}, Int32), h.ptr, Int32(k)))
+"Frozen-dt replay of recorded macro step k on the resident state (replay_fixed)."
+replay_macro_step!(h::Handle, k::Integer) =
+    check(h, ccall((:rs_replay_macro_step, LIB[]), Int32, (Ptr{Cvoid}, Int32), h.ptr, Int32(k)))
 function grad_emission!(h::Handle, g::Vector{Float64})
     check(h, ccall((:rs_adjoint_get_grad_emission, LIB[]), Int32,
                    (Ptr{Cvoid}, Ptr{Float64}, Csize_t), h.ptr, g, length(g)))
