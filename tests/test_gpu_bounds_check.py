@@ -25,8 +25,10 @@ def _regional(n=7):
                    qbc_s=qb_lat, qbc_n=qb_lat[::-1].copy(), temperature=np.full((n, n, n), 280.0),
                    pressure=np.full((n, n, n), 8e4), flux_omega=0.0)
     u0 = np.concatenate([1.0 + rng.random((mech.ns, n, n, n)), dp3[None]])
+    # transport only: the checks guard the pencils, and these tracer values are not a
+    # chemical state
     return workloads.Workload("regional %d^3" % n, g, mech, forcing, np.ascontiguousarray(u0),
-                              600.0, 1)
+                              600.0, 1, do_chemistry=False)
 
 
 CASES = {
@@ -38,7 +40,8 @@ CASES = {
 
 
 def _steps(w, check, n, staging=None, **kw):
-    s = Solver.for_workload(w, check=check, **kw)
+    s = Solver.for_workload(w, check=check, do_transport=w.do_transport,
+                            do_chemistry=w.do_chemistry, **kw)
     if staging is not None:
         s.set_transport_staging(staging)
     s.set_state(w.u0_cellmajor())
