@@ -246,7 +246,8 @@ rs_status rs_autotune(rs_handle* h, char* buf, size_t buf_len);
  * timing again (no reference counterpart).  Keys: "xthreads", "pencil", "rows",
  * "x_tracer_groups", "yz_tracer_groups" (FP64 pencils);
  * "mixed_xthreads", "mixed_x_tracers", "mixed_pencil", "mixed_rows", "mixed_yz_tracers",
- * "mixed_x_bulk", "mixed_yz_bulk" (mixed pencils); "per_cell_threads",
+ * "mixed_x_bulk", "mixed_yz_bulk" (mixed pencils); "mixed_x_stream", "mixed_yz_stream" (1: the
+ * streaming forms of the mixed kernels instead of the pencils); "per_cell_threads",
  * "per_cell_blocks_per_sm" (per-cell chemistry).  Values outside a key's candidates are
  * RS_ERR_INVALID.  Every shape gives bit-identical results. */
 rs_status rs_set_launch_shape(rs_handle* h, const char* key, int32_t value);
@@ -264,7 +265,11 @@ enum { RS_CHEM_KERNEL_AUTO = 0, RS_CHEM_KERNEL_TABLE = 1, RS_CHEM_KERNEL_SPECIAL
 rs_status rs_set_chem_kernel(rs_handle* h, int32_t kind);
 /* The kernel kind in use (TABLE or SPECIALIZED) and a one-line JSON description of it. */
 rs_status rs_get_chem_kernel(rs_handle* h, int32_t* kind, char* info, size_t info_len);
-/* Staging of the mixed-precision transport pencils (no reference counterpart).
+/* Staging of the mixed-precision transport pencils (no reference counterpart).  Beside the
+ * pencils, the mixed transport has streaming forms without shared memory (a warp of shuffles
+ * per lon-row segment, one thread per lat / vertical line with a register window) that form the
+ * same pairs in the same order; in AUTO mode rs_autotune picks per direction among all of them,
+ * PLAIN and BULK select the pencils.
  * BULK: the interior of every lat / vertical pencil is copied into shared memory by one
  *   tensor-map bulk copy (TMA) per split plane and every lon row by a 1-D bulk copy, double
  *   buffered across tracers; the ghost cells are loaded by the threads.  Used where the grid

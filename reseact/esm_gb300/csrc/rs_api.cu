@@ -380,6 +380,7 @@ struct rs_handle {
     int mpencil = 16, mrows = 16, mxthreads = 128;    // mixed-precision pencil kernels
     int msper_x = 1 << 20, msper_yz = 1;             // tracers per block (clamped to ntr)
     int mbulk_x = 1, mbulk_yz = 1;                    // bulk-copy staging per direction
+    int mstream_x = 1, mstream_yz = 1;                // streaming kernels instead of pencils
   } tune;
   // mechanism-specialised chemistry kernels (null: not built) and the kind in use
   // full PBL mixing: host inputs, and the derived per-layer fraction / weight and column
@@ -622,6 +623,9 @@ void refresh_dt(rs_handle* h) {
   T.tma_err = h->tma_err.p;
   T.mbulk_x = h->staging == RS_STAGING_BULK ? 1 : h->tune.mbulk_x;
   T.mbulk_yz = h->staging == RS_STAGING_BULK ? 1 : h->tune.mbulk_yz;
+  // a staging mode set by rs_set_transport_staging selects the pencils
+  T.mstream_x = h->staging == RS_STAGING_AUTO ? h->tune.mstream_x : 0;
+  T.mstream_yz = h->staging == RS_STAGING_AUTO ? h->tune.mstream_yz : 0;
   T.pbl = h->pbl_on;
   T.pbl_f = h->pbl_f.p; T.pbl_w = h->pbl_w.p; T.pbl_den = h->pbl_den.p; T.pbl_qbar = h->pbl_qbar.p;
   T.pbl_tau = h->tau_pbl;
@@ -1985,6 +1989,8 @@ extern "C" rs_status rs_set_launch_shape(rs_handle* h, const char* key, int32_t 
     else if (k == "mixed_yz_tracers") ok = value >= 1 && value <= ntr && (t.msper_yz = value, true);
     else if (k == "mixed_x_bulk") ok = in({0, 1}) && (t.mbulk_x = value, true);
     else if (k == "mixed_yz_bulk") ok = in({0, 1}) && (t.mbulk_yz = value, true);
+    else if (k == "mixed_x_stream") ok = in({0, 1}) && (t.mstream_x = value, true);
+    else if (k == "mixed_yz_stream") ok = in({0, 1}) && (t.mstream_yz = value, true);
     else if (k == "per_cell_threads") ok = in({64, 128, 256}) && (t.pc_threads = value, true);
     else if (k == "per_cell_blocks_per_sm") ok = in({1, 2, 4, 8}) && (t.pc_blocks_per_sm = value, true);
     else throw RsError(RS_ERR_INVALID, "unknown launch-shape key: " + k);
@@ -2455,6 +2461,25 @@ extern "C" rs_status rs_autotune(rs_handle* h, char* buf, size_t buf_len) {
         float bmx = 1e30f, bmyz = 1e30f;
         int mode_x = modes[0], mode_yz = modes[0];
         T.tma = h->tmaps;
+        const bool auto_mode = h->staging == RS_STAGING_AUTO;
+        bool stream_x = false, stream_yz = false;
+        if (auto_mode) {  // the streaming forms first: a warp per lon row segment, x tracers
+          T.mstream_x = 1;
+          for (int sp : spers) {
+            T.msper_x = sp;
+            float ms = time_min(h->st, 3, [&] { rs::launch_flux_dir_mixed(h->st, T, Q, 0, false); });
+            std::snprintf(line, sizeof line, "%s{\"staging\": \"stream\", \"tracers\": %d, \"ms\": %.4f}",
+                          first ? "" : ", ", sp, ms);
+            rep += line;
+            first = false;
+            if (ms < bmx) {
+              bmx = ms;
+              stream_x = true;
+              h->tune.msper_x = sp;
+            }
+          }
+        }
+        T.mstream_x = 0;
         for (int md : modes) {
           T.mbulk_x = md == RS_STAGING_BULK;
           for (int xt : {64, 128, 256})
@@ -2470,6 +2495,7 @@ extern "C" rs_status rs_autotune(rs_handle* h, char* buf, size_t buf_len) {
               if (ms < bmx) {
                 bmx = ms;
                 mode_x = md;
+                stream_x = false;
                 h->tune.mxthreads = xt;
                 h->tune.msper_x = sp;
               }
@@ -2477,6 +2503,26 @@ extern "C" rs_status rs_autotune(rs_handle* h, char* buf, size_t buf_len) {
         }
         rep += "], \"mixed_pencils\": [";
         first = true;
+        if (auto_mode) {  // the streaming forms: one thread per lat / vertical line
+          T.mstream_yz = 1;
+          for (int sp : spers) {
+            T.msper_yz = sp;
+            float ms = time_min(h->st, 3, [&] {
+              rs::launch_flux_dir_mixed(h->st, T, Q, 1, false);
+              rs::launch_flux_dir_mixed(h->st, T, Q, 2, false);
+            });
+            std::snprintf(line, sizeof line, "%s{\"staging\": \"stream\", \"tracers\": %d, \"ms\": %.4f}",
+                          first ? "" : ", ", sp, ms);
+            rep += line;
+            first = false;
+            if (ms < bmyz) {
+              bmyz = ms;
+              stream_yz = true;
+              h->tune.msper_yz = sp;
+            }
+          }
+        }
+        T.mstream_yz = 0;
         for (int md : modes) {
           T.mbulk_yz = md == RS_STAGING_BULK;
           for (int pw : {16, 32})
@@ -2499,6 +2545,7 @@ extern "C" rs_status rs_autotune(rs_handle* h, char* buf, size_t buf_len) {
                 if (ms < bmyz) {
                   bmyz = ms;
                   mode_yz = md;
+                  stream_yz = false;
                   h->tune.mpencil = pw;
                   h->tune.mrows = rows;
                   h->tune.msper_yz = sp;
@@ -2507,13 +2554,16 @@ extern "C" rs_status rs_autotune(rs_handle* h, char* buf, size_t buf_len) {
         }
         h->tune.mbulk_x = mode_x == RS_STAGING_BULK;
         h->tune.mbulk_yz = mode_yz == RS_STAGING_BULK;
+        h->tune.mstream_x = stream_x;
+        h->tune.mstream_yz = stream_yz;
         std::snprintf(line, sizeof line,
                       "], \"mixed_choice\": {\"xthreads\": %d, \"x_tracers\": %d, \"x_staging\": "
                       "\"%s\", \"pencil\": %d, \"rows\": %d, \"yz_tracers\": %d, "
                       "\"yz_staging\": \"%s\"}",
                       h->tune.mxthreads, std::min(h->tune.msper_x, ntr),
-                      mode_x == RS_STAGING_BULK ? "bulk" : "plain", h->tune.mpencil, h->tune.mrows,
-                      h->tune.msper_yz, mode_yz == RS_STAGING_BULK ? "bulk" : "plain");
+                      stream_x ? "stream" : (mode_x == RS_STAGING_BULK ? "bulk" : "plain"),
+                      h->tune.mpencil, h->tune.mrows, h->tune.msper_yz,
+                      stream_yz ? "stream" : (mode_yz == RS_STAGING_BULK ? "bulk" : "plain"));
         rep += line;
       }
       refresh_dt(h);

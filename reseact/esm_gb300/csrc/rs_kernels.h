@@ -95,6 +95,9 @@ struct DevTransport {
   const MixedTmaps* tma;
   int* tma_err;
   int mbulk_x, mbulk_yz;  // use the bulk copies for lon rows / lat and vertical pencils
+  // streaming forms instead of the pencils (no shared memory): a warp of shuffles per lon row
+  // segment, one thread per lat / vertical line
+  int mstream_x, mstream_yz;
 };
 
 // chemistry (rs_chem.cu)

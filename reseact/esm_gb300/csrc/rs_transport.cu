@@ -1122,6 +1122,185 @@ __global__ void __launch_bounds__(512) k_adv_yz_mixed(DevTransport<double> T, St
 #undef RS_P
 }
 
+// ---- streaming forms of the mixed pencils (no shared memory, no barriers).  The same pair
+// operations in the same order as k_adv_x_mixed / k_adv_yz_mixed, so the accumulators are bit
+// for bit those of the pencils; rs_autotune picks per direction.
+//
+// Lon rows: one warp per segment of kSegX = 26 cells of a row; lane l holds cell
+// p = base - 3 + l, and the neighbour values the stencil needs move between lanes by shuffles.
+// Lane l computes the limited deviation of face p (its west face); cells at lanes 3..28 have
+// all of D(p-2..p), E(p-2..p+1) and their east face's Phi from lane l+1.
+constexpr int kSegX = 26;
+__device__ __forceinline__ df shfl_up_df(df v, int d) {
+  return {__shfl_up_sync(0xffffffffu, v.h, d), __shfl_up_sync(0xffffffffu, v.l, d)};
+}
+__device__ __forceinline__ df shfl_down_df(df v, int d) {
+  return {__shfl_down_sync(0xffffffffu, v.h, d), __shfl_down_sync(0xffffffffu, v.l, d)};
+}
+// Face f's two pair terms from the upwind cell's edges: Psi_f (for cell f) and Phi_f (for cell
+// f-1).  E(o), D(o) give E_{f+o}, D_{f+o}.  The expressions of cell_faces, so the same bits.
+template <class FE, class FD>
+__device__ __forceinline__ void face_terms(df M, FE E, FD D, df& psi, df& phi) {
+  psi = df{0.0f, 0.0f};
+  phi = df{0.0f, 0.0f};
+  if (M.h > 0.0f) {  // upwind f-1: its right edge
+    const df dev = lim_pick(df_sub(E(-2), D(-2)), E(-1), true);
+    psi = df_mul(M, df_sub(D(-1), dev));
+    phi = df_mul(M, dev);
+  } else if (M.h < 0.0f) {  // upwind f: its left edge
+    const df dev = lim_pick(df_sub(E(-1), D(-1)), E(0), false);
+    psi = df_mul(M, df_neg(dev));
+    phi = df_mul(M, df_add(D(-1), dev));
+  }
+}
+
+__global__ void __launch_bounds__(128) k_adv_x_stream(DevTransport<double> T, StageSel sel,
+                                                      int sper) {
+  const double* Q;
+  double g;
+  if (!resolve_stage(sel, Q, g)) return;
+  const int n = T.nlon, nf = n + 1;
+  const int nseg = (n + kSegX - 1) / kSegX;
+  const int lane = threadIdx.x & 31;
+  const long long wg = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (wg >= (long long)nseg * T.nlat * T.nlev) return;  // whole warps leave together
+  const int row = (int)(wg / nseg), seg = (int)(wg % nseg);
+  const int j = row % T.nlat, k = row / T.nlat;
+  const int p = seg * kSegX - 3 + lane;  // this lane's cell (and west face)
+  const size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
+  const long long nall = (long long)T.ntr * nc;
+  const size_t rbase = ((size_t)k * T.nlat + j) * n;
+  const bool periodic = T.lon_bc == 0;
+  const df G = df_ld2(T.gx2, j);
+  const df M = (p >= 0 && p <= n) ? split_df(g * T.mx[((size_t)k * T.nlat + j) * nf + p])
+                                   : df{0.0f, 0.0f};
+  const bool out = lane >= 3 && lane <= 28 && p >= 0 && p < n;
+  const int s0 = blockIdx.y * sper, s1 = min(T.ntr, s0 + sper);
+  for (int s = s0; s < s1; ++s) {
+    const size_t pb = (size_t)s * nc + rbase;
+    df q;
+    if (p >= 0 && p < n) {
+      q = df{T.qhi[bck(T, pb + p, nall)], T.qlo[bck(T, pb + p, nall)]};
+    } else if (periodic) {
+      const int w = ((p % n) + n) % n;
+      q = df{T.qhi[bck(T, pb + w, nall)], T.qlo[bck(T, pb + w, nall)]};
+    } else {
+      split_d((p < 0 ? T.qw : T.qe)[bck(T, ((size_t)s * T.nlev + k) * T.nlat + j,
+                                        (long long)T.ntr * T.nlev * T.nlat)], q.h, q.l);
+    }
+    const df D = df_sub(shfl_down_df(q, 1), q);                 // D(p), lanes 0..30
+    const df S = mc_slope(shfl_up_df(D, 1), D);                 // S(p), lanes 1..30
+    const df E = edge_u(D, S, shfl_down_df(S, 1));              // E(p), lanes 1..29
+    const df Dm1 = shfl_up_df(D, 1), Dm2 = shfl_up_df(D, 2);
+    const df Em1 = shfl_up_df(E, 1), Em2 = shfl_up_df(E, 2);
+    df psi, phi;
+    face_terms(M, [&](int o) { return o == 0 ? E : (o == -1 ? Em1 : Em2); },
+               [&](int o) { return o == -1 ? Dm1 : Dm2; }, psi, phi);
+    const df phie = shfl_down_df(phi, 1);  // the east face's Phi, computed by lane + 1
+    if (out) {
+      const df a = df_neg(df_mul(G, df_add(phie, psi)));
+      T.acc[bck(T, pb + p, nall)] = make_float2(a.h, a.l);
+    }
+  }
+}
+
+// Lat (DIR 1) and vertical (DIR 2) lines: one thread per line (consecutive lon points at one
+// level, or consecutive columns), walking the line once per tracer with a register window:
+// when q(p) arrives, D(p-1), S(p-1), E(p-2) are formed and face p-2 is complete; its Phi
+// closes cell p-3 and its Psi opens cell p-2.
+template <int DIR>
+__global__ void __launch_bounds__(128) k_adv_yz_stream(DevTransport<double> T, StageSel sel,
+                                                       int sper) {
+  const double* Q;
+  double g;
+  if (!resolve_stage(sel, Q, g)) return;
+  const int n = DIR == 1 ? T.nlat : T.nlev;
+  const size_t ncol = (size_t)T.nlon * T.nlat;
+  const size_t nc = ncol * T.nlev;
+  const long long nall = (long long)T.ntr * nc;
+  const int ntile = (T.nlon + (int)blockDim.x - 1) / (int)blockDim.x;
+  const int k = DIR == 1 ? (int)(blockIdx.x / ntile) : 0;
+  const int i = DIR == 1 ? (int)(blockIdx.x % ntile) * (int)blockDim.x + (int)threadIdx.x : 0;
+  const size_t col = DIR == 2 ? (size_t)blockIdx.x * blockDim.x + threadIdx.x : 0;
+  if (DIR == 1 ? i >= T.nlon : col >= ncol) return;
+  const size_t stride = DIR == 1 ? (size_t)T.nlon : ncol;
+  const size_t cbase = DIR == 1 ? (size_t)k * ncol + i : col;
+  const bool open = DIR == 1 && T.lat_bc == 1;
+  auto flux = [&](int f) -> df {  // face f's air-mass flux, zero through closed walls
+    if (DIR == 1) {
+      if (open || (f > 0 && f < n)) return split_df(g * T.my[((size_t)k * (n + 1) + f) * T.nlon + i]);
+    } else if (f > 0 && f < n) {
+      return split_df(g * T.mz[(size_t)f * ncol + col]);
+    }
+    return df{0.0f, 0.0f};
+  };
+  const int s0 = blockIdx.y * sper, s1 = min(T.ntr, s0 + sper);
+  for (int s = s0; s < s1; ++s) {
+    const size_t pb = (size_t)s * nc + cbase;
+    auto load = [&](int p) -> df {
+      if (p < 0 || p >= n) {
+        if (open) {
+          df v;
+          split_d((p < 0 ? T.qs : T.qn)[bck(T, ((size_t)s * T.nlev + k) * T.nlon + i,
+                                            (long long)T.ntr * T.nlev * T.nlon)], v.h, v.l);
+          return v;
+        }
+        p = p < 0 ? -1 - p : 2 * n - 1 - p;  // mirror ghosts at the walls
+      }
+      const size_t x = bck(T, pb + (size_t)p * stride, nall);
+      return df{T.qhi[x], T.qlo[x]};
+    };
+    const df z{0.0f, 0.0f};
+    // window: qp = q(p-1); D4..D1 = D(p-4..p-1); S2, S1 = S(p-2), S(p-1); E4..E2 = E(p-4..p-2)
+    df qp = load(-3), D4 = z, D3 = z, D2 = z, D1 = z, S2 = z, S1 = z, E4 = z, E3 = z, E2 = z;
+    df psi_prev = z;  // Psi of the previous face (the open cell's west face)
+    for (int p = -2; p <= n + 2; ++p) {
+      const df qn = load(p);
+      D4 = D3; D3 = D2; D2 = D1;
+      D1 = df_sub(qn, qp);  // D(p-1)
+      qp = qn;
+      S2 = S1;
+      const int ps = p - 1;  // the slope formed now
+      if (DIR == 1) {
+        S1 = mc_slope(D2, D1);
+      } else if (ps >= -1 && ps <= n) {  // slopes of cells -1..n (coefficient row ps+1)
+        const size_t x = bck(T, (size_t)(ps + 1) * ncol + col, (long long)(n + 2) * ncol);
+        S1 = mc_slope_n(D2, D1, df_ld2(T.vsA2, x), df_ld2(T.vsB2, x));
+      } else {
+        S1 = z;
+      }
+      E4 = E3; E3 = E2;
+      const int pe = p - 2;  // the edge term formed now: E(pe) from D(pe), S(pe), S(pe+1)
+      if (DIR == 1) {
+        E2 = edge_u(D2, S2, S1);
+      } else if (pe >= -1 && pe <= n - 1) {
+        const size_t x = bck(T, (size_t)(pe + 1) * ncol + col, (long long)(n + 1) * ncol);
+        E2 = edge_n(D2, S2, S1, df_ld2(T.veAB2, x), df_ld2(T.veC2, x), df_ld2(T.veD2, x));
+      } else {
+        E2 = z;
+      }
+      const int f = p - 2;  // the face now complete (needs E(f-2..f), D(f-2..f-1))
+      if (f < 0 || f > n) continue;
+      df psi, phi;
+      face_terms(flux(f), [&](int o) { return o == 0 ? E2 : (o == -1 ? E3 : E4); },
+                 [&](int o) { return o == -1 ? D3 : D4; }, psi, phi);
+      if (f >= 1) {  // cell f-1 is complete: its east face f, west face f-1
+        const int c = f - 1;
+        df a;
+        if (DIR == 1)
+          a = df_neg(df_add(df_mul(df_ld2(T.gyhi2, c), phi), df_mul(df_ld2(T.gylo2, c), psi_prev)));
+        else
+          a = df_neg(df_add(phi, psi_prev));
+        const size_t x = bck(T, pb + (size_t)c * stride, nall);
+        const float2 o = T.acc[x];
+        const df t = df_add(df{o.x, o.y}, a);
+        T.acc[x] = make_float2(t.h, t.l);
+      }
+      psi_prev = psi;
+    }
+  }
+}
+
 // ------------------------------------------------------------------ stage kernel
 #if !RS_STRICT
 // hi + lo split without FP64-pipe conversions (production build): hi = v truncated to 24
@@ -1255,7 +1434,14 @@ __global__ void __launch_bounds__(kRedThreads) k_pbl_mean(DevTransport<double> T
   const size_t s = id / ncol, col = id % ncol;
   const double* q = Q + s * nc + col;
   double acc = 0.0;
-  for (int k = 0; k < T.nlev; ++k) acc = acc + T.pbl_w[(size_t)k * ncol + col] * q[(size_t)k * ncol];
+  if (T.mixed) {  // the stage input is the pencils' (hi, lo) planes
+    for (int k = 0; k < T.nlev; ++k) {
+      const size_t x = s * nc + (size_t)k * ncol + col;
+      acc = acc + T.pbl_w[(size_t)k * ncol + col] * df_to_d(make_float2(T.qhi[x], T.qlo[x]));
+    }
+  } else {
+    for (int k = 0; k < T.nlev; ++k) acc = acc + T.pbl_w[(size_t)k * ncol + col] * q[(size_t)k * ncol];
+  }
   T.pbl_qbar[id] = acc / T.pbl_den[col];
 }
 
@@ -1354,22 +1540,7 @@ __global__ void __launch_bounds__(kRedThreads) k_stage(DevTransport<double> T,
       double scale = dt_2;
       bool per_m = false;  // du is the tendency times m (1/m folded into the scale)
 #endif
-      if (s < T.ntr && T.mixed) {
-        // compensated FP32 transport: the pencils accumulated m dq/dt as a pair
-        const double ab = df_to_d(T.acc[x]);
-#if RS_STRICT
-        du = ab / m;
-        if (T.pbl) du = du + pbl_term(T, c, col, s, q);
-#else
-        if (T.pbl) {
-          du = fma(ab, rm, pbl_term(T, c, col, s, q));
-        } else {
-          du = ab;
-          scale = sc;
-          per_m = true;
-        }
-#endif
-      } else if (s < T.ntr) {
+      if (s < T.ntr) {
         double fw = T.fx[s * fxp + fxi], fe = T.fx[s * fxp + fxi + 1];
         double fs = T.fy[s * fyp + fyi], fn = T.fy[s * fyp + fyi + T.nlon];
         double fb = T.fz[s * fzp + fzi], ft = T.fz[s * fzp + fzi + ncol];
@@ -1404,11 +1575,9 @@ __global__ void __launch_bounds__(kRedThreads) k_stage(DevTransport<double> T,
       if (STAGE == 1) {
         B.S1[x] = nx;
         if (Vo) Vo[x] = nx;
-        if (T.mixed && s < T.ntr) split_store(T, x, nx);
       } else if (STAGE == 2) {
         B.S2[x] = nx;
         if (Vo) Vo[x] = nx;
-        if (T.mixed && s < T.ntr) split_store(T, x, nx);
       } else if (STAGE == 3) {
         double u3 = nx;
         double u0 = U[x];
@@ -1416,7 +1585,6 @@ __global__ void __launch_bounds__(kRedThreads) k_stage(DevTransport<double> T,
         double u4 = (2.0 / 3.0) * u0 + (1.0 / 3.0) * u3;
         B.S3[x] = u4;
         if (Vo) Vo[x] = u4;
-        if (T.mixed && s < T.ntr) split_store(T, x, u4);
       } else {
         double u0 = U[x];
         double u3 = B.S1[x];
@@ -1447,6 +1615,112 @@ __global__ void __launch_bounds__(kRedThreads) k_stage(DevTransport<double> T,
 #endif
   if (STAGE == 4) {
     double tot = block_tree256(e, sm);
+    if (threadIdx.x == 0) B.partial[blockIdx.x] = tot;
+  }
+}
+
+// Compensated-FP32 stage kernel (mixed precision).  The tracers of stages 1-3 stay pairs:
+// the stage input is the pencils' own (hi, lo) planes, the update q + dt/2 * (m dq/dt) / m is
+// formed in pairs and written back into those planes (in place: the update is pointwise), u3
+// is kept as pairs in the tracer part of S1; only stage 4 returns to FP64 -- the candidate
+// state, the embedded error and the hairer norm, as the benchmark spec keeps them.  The air-mass
+// row is the FP64 scheme's, stage by stage (m in the air-mass planes of U, S1, S2, S3).
+//   1: P = U + dt/2 f(U)          2: P = P + dt/2 f(P)
+//   3: u3 = P + dt/2 f(P) -> S1 (pairs), P = u4 = 2/3 U + 1/3 u3
+//   4: unew = P + dt/2 f(P); err = 1/2 (1/3 U + 2/3 u3 - unew); candidate = clamp(unew)
+constexpr float kTwoThirdsH = (float)(2.0 / 3.0);
+constexpr float kTwoThirdsL = (float)(2.0 / 3.0 - (double)(float)(2.0 / 3.0));
+constexpr float kThirdH = (float)(1.0 / 3.0);
+constexpr float kThirdL = (float)(1.0 / 3.0 - (double)(float)(1.0 / 3.0));
+template <int STAGE>
+__global__ void __launch_bounds__(kRedThreads) k_stage_mixed(DevTransport<double> T,
+                                                             const Ctl* __restrict__ ctl,
+                                                             TransportBufs B, double rtol,
+                                                             double atol, int clamp) {
+  __shared__ double sm[kRedThreads];
+  if (ctl->done) return;
+  const double g = ctl->g[STAGE - 1];
+  const int cur = ctl->cur;
+  const double* U = cur ? B.U1 : B.U0;
+  double* Un = cur ? B.U0 : B.U1;
+  const double dt_2 = ctl->dtc / 2;
+  // air mass of the stage input
+  const double* Qm = STAGE == 1 ? U : (STAGE == 2 ? B.S1 : (STAGE == 3 ? B.S2 : B.S3));
+  const size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
+  float2* u3p = reinterpret_cast<float2*>(B.S1);  // u3 of the tracers as pairs, [ntr][nc]
+  const df c23{kTwoThirdsH, kTwoThirdsL}, c13{kThirdH, kThirdL};
+  const size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double e = 0.0;
+  if (c < nc) {
+    const int i = (int)(c % T.nlon);
+    const int j = (int)((c / T.nlon) % T.nlat);
+    const int k = (int)(c / ((size_t)T.nlon * T.nlat));
+    const CellGeo G{T.gx[j], T.gylo[j], T.gyhi[j]};
+    const MassFluxes F = mass_fluxes(T, i, j, k, g);
+    double hz, vz;
+    div_parts(F, G, hz, vz);
+    const double dmdt = T.mcorr ? -((hz + T.mcorr[c]) + vz) : -(hz + vz);
+    const size_t xm = (size_t)(T.nsp - 1) * nc + c;
+    const double m = Qm[xm];
+#if RS_STRICT
+    const double rm = 1.0 / m;
+#else
+    const double rm = rcp_nr(m);  // m > 0
+#endif
+    const df sc = split_df(dt_2 * rm);  // the tracer increment is (m dq/dt) * dt/2 / m
+    const size_t col = (size_t)j * T.nlon + i;
+    // the air-mass row, in FP64 as the FP64 scheme forms it
+    const double mn = fma(dmdt, dt_2, m);
+    if (STAGE == 1) B.S1[xm] = mn;
+    if (STAGE == 2) B.S2[xm] = mn;
+    if (STAGE == 3) {
+      B.S1[xm] = mn;
+      B.S3[xm] = (2.0 / 3.0) * U[xm] + (1.0 / 3.0) * mn;
+    }
+    if (STAGE == 4) {
+      const double u0 = U[xm], u3 = B.S1[xm];
+      const double err = fma(2.0 / 3.0, u3, fma(1.0 / 3.0, u0, -mn));
+      const double den = fma(amax_bits(u0, mn), rtol, atol);
+      const double at = err * rcp_nr1(den);
+      e = fma(at, at, e);
+      Un[xm] = (clamp && __double2hiint(mn) < 0) ? 0.0 : mn;
+    }
+    for (int s = 0; s < T.ntr; ++s) {
+      const size_t x = (size_t)s * nc + c;
+      const df q{T.qhi[x], T.qlo[x]};
+      df nx;
+      if (T.pbl) {  // with full PBL mixing the tendency is formed in FP64 (rare combination)
+        const double qd = df_to_d(make_float2(q.h, q.l));
+        const double du = fma(df_to_d(T.acc[x]), rm, pbl_term(T, c, col, s, qd));
+        nx = split_df(fma(du, dt_2, qd));
+      } else {
+        nx = df_add(q, df_mul(df_ld2(T.acc, x), sc));
+      }
+      if (STAGE == 1 || STAGE == 2) {
+        T.qhi[x] = nx.h;
+        T.qlo[x] = nx.l;
+      } else if (STAGE == 3) {
+        u3p[x] = make_float2(nx.h, nx.l);
+        const df u4 = df_add(df_mul(c23, split_df(U[x])), df_mul(c13, nx));
+        T.qhi[x] = u4.h;
+        T.qlo[x] = u4.l;
+      } else {
+        const double u0 = U[x];
+        const double un = df_to_d(make_float2(nx.h, nx.l));
+        // (1/3 u0 + 2/3 u3) - un in pairs, then FP64 for the norm; its factor 1/2 goes onto
+        // the cell's sum as an exact 1/4
+        const df ut = df_add(df_mul(c13, split_df(u0)), df_mul(c23, df_ld2(u3p, x)));
+        const df d = df_sub(ut, nx);
+        const double err = df_to_d(make_float2(d.h, d.l));
+        const double den = fma(amax_bits(u0, un), rtol, atol);
+        const double at = err * rcp_nr1(den);  // den >= atol > 0
+        e = fma(at, at, e);
+        Un[x] = (clamp && __double2hiint(un) < 0) ? 0.0 : un;
+      }
+    }
+  }
+  if (STAGE == 4) {
+    const double tot = block_tree256(0.25 * e, sm);
     if (threadIdx.x == 0) B.partial[blockIdx.x] = tot;
   }
 }
@@ -1693,10 +1967,22 @@ static void launch_fluxes_mixed(cudaStream_t st, const DevTransport<double>& T, 
                shz = mixed_pencil_bytes(T.nlev, pw, tz);
   static const CUtensorMap kNoMap{};  // placeholder argument of the plain-load variants
   // rs_create refuses mixed precision on grids whose pencils do not fit at width 16
-  if (only_dir < 0 || only_dir == 0) {
+  if ((only_dir < 0 || only_dir == 0) && T.mstream_x) {
+    const long long warps = (long long)((T.nlon + kSegX - 1) / kSegX) * T.nlat * T.nlev;
+    k_adv_x_stream<<<dim3((unsigned)((warps + 3) / 4), groups(sx)), 128, 0, st>>>(T, sel, sx);
+  } else if (only_dir < 0 || only_dir == 0) {
     dim3 grid((unsigned)(T.nlat * T.nlev), groups(sx));
     if (tx) k_adv_x_mixed<true><<<grid, xt, shx, st>>>(T, sel, sx);
     else k_adv_x_mixed<false><<<grid, xt, shx, st>>>(T, sel, sx);
+  }
+  if (T.mstream_yz) {
+    if (only_dir < 0 || only_dir == 1)
+      k_adv_yz_stream<1><<<dim3((unsigned)((T.nlon + 127) / 128) * (unsigned)T.nlev, groups(syz)),
+                           128, 0, st>>>(T, sel, syz);
+    if (only_dir < 0 || only_dir == 2)
+      k_adv_yz_stream<2><<<dim3((unsigned)((ncol + 127) / 128), groups(syz)), 128, 0, st>>>(
+          T, sel, syz);
+    return;
   }
   if (only_dir < 0 || only_dir == 1) {
     dim3 grid((unsigned)((T.nlon + pw - 1) / pw) * (unsigned)T.nlev, groups(syz));
@@ -1766,6 +2052,24 @@ void launch_ssprk43_attempt(cudaStream_t st, const DevTransport<double>& T, cons
     size_t n = (size_t)T.ntr * nc;
     k_split_input<<<(unsigned)((n + kRedThreads - 1) / kRedThreads), kRedThreads, 0, st>>>(
         T, ctl, B.U0, B.U1, nullptr);
+  }
+  if (T.mixed) {  // compensated FP32: the stages stay pairs until stage 4
+    launch_fluxes(st, T, sel);
+    if (T.pbl) launch_pbl_mean(st, T, sel);
+    k_stage_mixed<1><<<nb, kRedThreads, 0, st>>>(T, ctl, B, rtol, atol, clamp);
+    sel.stage = 2;
+    launch_fluxes(st, T, sel);
+    if (T.pbl) launch_pbl_mean(st, T, sel);
+    k_stage_mixed<2><<<nb, kRedThreads, 0, st>>>(T, ctl, B, rtol, atol, clamp);
+    sel.stage = 3;
+    launch_fluxes(st, T, sel);
+    if (T.pbl) launch_pbl_mean(st, T, sel);
+    k_stage_mixed<3><<<nb, kRedThreads, 0, st>>>(T, ctl, B, rtol, atol, clamp);
+    sel.stage = 4;
+    launch_fluxes(st, T, sel);
+    if (T.pbl) launch_pbl_mean(st, T, sel);
+    k_stage_mixed<4><<<nb, kRedThreads, 0, st>>>(T, ctl, B, rtol, atol, clamp);
+    return;
   }
   launch_fluxes(st, T, sel);
   if (T.pbl) launch_pbl_mean(st, T, sel);

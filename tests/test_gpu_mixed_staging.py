@@ -1,4 +1,5 @@
-"""Bulk-copy (TMA) staging of the mixed-precision transport pencils against plain loads.
+"""Bulk-copy (TMA) staging of the mixed-precision transport pencils against plain loads, and
+the streaming forms (no shared memory) against the pencils.
 
 The two stagings load the same values into the same shared-memory rows, so the fluxes and
 every state after them are bit-identical.  The cases cover every tracer grouping (one tracer
@@ -84,12 +85,13 @@ def _regional(n, q, qb):
     return g, mech, cfg, mabi, f, workloads.soa_to_cellmajor(u, n, n, n)
 
 
-def _regional_steps(staging, n, q, qb):
+def _regional_steps(staging, n, q, qb, stream=0):
     g, mech, cfg, mabi, f, u0 = _regional(n, q, qb)
     s = Solver(cfg, mabi)
     s.set_forcing(f)
     s.set_transport_staging(staging)
-    s.set_launch_shape(mixed_x_tracers=3, mixed_yz_tracers=3)
+    s.set_launch_shape(mixed_x_tracers=3, mixed_yz_tracers=3, mixed_x_stream=stream,
+                       mixed_yz_stream=stream)
     s.set_state(u0)
     dtT = 0.05
     for k in range(4):
@@ -112,4 +114,30 @@ def test_open_boundaries_bulk_equals_plain_and_freestream_is_exact():
     a = _regional_steps(STAGING_BULK, n, q, qb)
     b = _regional_steps(STAGING_PLAIN, n, q, qb)
     assert np.all(np.isfinite(a))
+    assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("sper", [1, 4, 12])
+def test_streaming_forms_are_bit_identical_to_the_pencils(sper):
+    """The streaming kernels (a warp of shuffles per lon-row segment, one thread per lat /
+    vertical line) form the same pairs in the same order as the pencils: the same bits, on a
+    global grid (periodic rows, mirrored poles and levels) and on open walls."""
+    w = workloads.c2(nlon=36, nlat=19, nlev=10)
+    a, _ = _run(w, STAGING_AUTO, dict(mixed_x_stream=1, mixed_yz_stream=1, mixed_x_tracers=sper,
+                                      mixed_yz_tracers=sper))
+    b, _ = _run(w, STAGING_PLAIN, dict(mixed_x_tracers=sper, mixed_yz_tracers=sper))
+    assert np.all(np.isfinite(a))
+    assert np.array_equal(a, b)
+
+
+def test_streaming_forms_open_boundaries_and_freestream():
+    n = 8
+    ns = mechanism.superfast().ns
+    out = _regional_steps(STAGING_AUTO, n, np.ones((ns, n, n, n)), np.ones((ns, n, n)), stream=1)
+    assert np.all(out[:, :-1] == 1.0)
+    rng = np.random.default_rng(6)
+    q = 1e-9 * (1 + rng.random((ns, n, n, n)))
+    qb = 1e-9 * (1 + rng.random((ns, n, n)))
+    a = _regional_steps(STAGING_AUTO, n, q, qb, stream=1)
+    b = _regional_steps(STAGING_PLAIN, n, q, qb)
     assert np.array_equal(a, b)
