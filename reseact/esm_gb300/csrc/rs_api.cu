@@ -308,6 +308,7 @@ struct rs_handle {
       stepcell, totals;
   DevBuf<float> qhi, qlo;  // mixed-precision transport: split planes
   DevBuf<float> gx2, gylo2, gyhi2, vsA2, vsB2, veAB2, veC2, veD2;  // (hi, lo) pairs
+  DevBuf<float> mx2, my2, mz2;  // the face fluxes as (hi, lo) pairs (mixed precision)
   rs::MixedTmaps* tmaps = nullptr;  // bulk-copy staging of the mixed pencils (null: unavailable)
   void* noalloc_base = nullptr;     // this device's scratch of rs_ros23_attempt_noalloc
   std::string tmaps_why;
@@ -513,6 +514,18 @@ void upload_pairs(const std::vector<double>& v, DevBuf<float>& d, cudaStream_t s
   CK(cudaStreamSynchronize(st));  // w is a temporary
 }
 
+// The air-mass face fluxes as (hi, lo) pairs for the compensated FP32 kernels (after every
+// flux change, including the pressure fixer's diagnosed Mz).
+void make_flux_pairs(rs_handle* h) {
+  h->mx2.alloc(2 * h->mx.n);
+  h->my2.alloc(2 * h->my.n);
+  h->mz2.alloc(2 * h->mz.n);
+  rs::launch_make_pairs(h->st, h->mx.p, reinterpret_cast<float2*>(h->mx2.p), h->mx.n);
+  rs::launch_make_pairs(h->st, h->my.p, reinterpret_cast<float2*>(h->my2.p), h->my.n);
+  rs::launch_make_pairs(h->st, h->mz.p, reinterpret_cast<float2*>(h->mz2.p), h->mz.n);
+  CK(cudaGetLastError());
+}
+
 // Lat-lon geometry on the unit sphere (same formulas and order as the CPU restatement).
 void build_geometry(rs_handle* h) {
   const rs_grid& g = h->cfg.grid;
@@ -609,6 +622,7 @@ void refresh_dt(rs_handle* h) {
   T.vsA2 = f2(h->vsA2); T.vsB2 = f2(h->vsB2); T.veAB2 = f2(h->veAB2); T.veC2 = f2(h->veC2);
   T.veD2 = f2(h->veD2);
   T.acc = T.mixed ? reinterpret_cast<float2*>(h->fx.p) : nullptr;  // ntr*nc pairs fit in fx
+  T.mx2 = f2(h->mx2); T.my2 = f2(h->my2); T.mz2 = f2(h->mz2);
   T.pencil = h->tune.pencil;
   T.rows = h->tune.rows;
   T.xthreads = h->tune.xthreads;
@@ -1012,6 +1026,7 @@ rs_status rs_create(const rs_config* cfg, rs_handle** out) {
       h->dp_host.assign(h->nc, 1.0);
       build_vertical(h);
     }
+    if (cfg->do_transport && cfg->precision == RS_PREC_MIXED) make_flux_pairs(h);  // zero fluxes
     refresh_dt(h);
     if (cfg->do_transport && cfg->precision == RS_PREC_MIXED) {
       const char* why = nullptr;
@@ -1038,7 +1053,7 @@ void rs_destroy(rs_handle* h) {
   for (auto& b : h->itabs) b.release();
   for (auto& b : h->dtabs) b.release();
   DevBuf<float>* fbufs[] = {&h->qhi, &h->qlo, &h->gx2, &h->gylo2, &h->gyhi2, &h->vsA2,
-                            &h->vsB2, &h->veAB2, &h->veC2, &h->veD2};
+                            &h->vsB2, &h->veAB2, &h->veC2, &h->veD2, &h->mx2, &h->my2, &h->mz2};
   for (auto* b : fbufs) b->release();
   DevBuf<double>* bufs[] = {&h->U[0], &h->U[1], &h->S1, &h->S2, &h->S3, &h->fx, &h->fy, &h->fz,
                             &h->partial, &h->krates, &h->T, &h->P, &h->emis, &h->io, &h->io2,
@@ -1159,6 +1174,7 @@ rs_status rs_set_forcing(rs_handle* h, const rs_forcing* f) {
       if (pbl_inputs) build_pbl(h);
       if (f->dps_dt) h->dpsdt_host.assign(f->dps_dt, f->dps_dt + ncol);
       if (f->dps_dt || f->hyb_b || f->mx || f->my || f->mz || f->dp) build_fixer(h);
+      if (h->cfg.precision == RS_PREC_MIXED) make_flux_pairs(h);
     }
     if (f->temperature) {
       h->T.upload(f->temperature, nc, st);

@@ -70,6 +70,9 @@ struct DevTransport {
   const float2* veC2;
   const float2* veD2;
   float2* acc;
+  const float2* mx2;    // the air-mass face fluxes as pairs (shapes of mx, my, mz)
+  const float2* my2;
+  const float2* mz2;
   int mixed;
   // full PBL mixing (transport half): per-layer fraction f and weight w = dp*f, the column
   // normaliser max(sum_k w, 1 Pa), scratch for the per-tracer column means, 1/tau
@@ -148,6 +151,8 @@ size_t mixed_pencil_cap();
 void mixed_tmaps_destroy(MixedTmaps* m);
 bool mixed_tmaps_dir_ok(const MixedTmaps* m, int dir);  // dir 0 lon rows, 1 lat, 2 vertical
 void launch_flux_dir(cudaStream_t st, const DevTransport<double>& T, const double* Q, int dir);
+// (hi, lo) float pairs of n doubles (the mixed kernels' face fluxes)
+void launch_make_pairs(cudaStream_t st, const double* src, float2* dst, size_t n);
 void launch_flux_dir_mixed(cudaStream_t st, const DevTransport<double>& T, const double* Q, int dir,
                            bool split);
 

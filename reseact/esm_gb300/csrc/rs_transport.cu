@@ -809,6 +809,7 @@ __global__ void __launch_bounds__(256) k_adv_x_mixed(DevTransport<double> T, Sta
   const double* Q;
   double g;
   if (!resolve_stage(sel, Q, g)) return;
+  const df gd = split_df(g);  // the stage time factor as a pair
   const int s0 = blockIdx.y * sper, s1 = min(T.ntr, s0 + sper);  // this block's tracers
   extern __shared__ __align__(16) unsigned char smx32_raw[];
   float* smx32 = align128(smx32_raw);
@@ -852,7 +853,7 @@ __global__ void __launch_bounds__(256) k_adv_x_mixed(DevTransport<double> T, Sta
     uses0 = s0 < s1;
   }
   for (int f = tid; f <= n; f += blockDim.x) {
-    const df M = split_df(g * T.mx[((size_t)k * T.nlat + j) * nf + f]);
+    const df M = df_mul(gd, df_ld2(T.mx2, ((size_t)k * T.nlat + j) * nf + f));
     Mh[bck(T, f, mixed_frows(n))] = M.h;
     Ml[bck(T, f, mixed_frows(n))] = M.l;
   }
@@ -945,6 +946,7 @@ __global__ void __launch_bounds__(512) k_adv_yz_mixed(DevTransport<double> T, St
   const double* Q;
   double g;
   if (!resolve_stage(sel, Q, g)) return;
+  const df gd = split_df(g);  // the stage time factor as a pair
   const int s0 = blockIdx.y * sper, s1 = min(T.ntr, s0 + sper);  // this block's tracers
   extern __shared__ __align__(16) unsigned char smp32_raw[];
   float* smp32 = align128(smp32_raw);
@@ -1010,9 +1012,9 @@ __global__ void __launch_bounds__(512) k_adv_yz_mixed(DevTransport<double> T, St
       df M{0.0f, 0.0f};
       if (DIR == 1) {
         if (open || (f > 0 && f < n))  // closed walls: no flux through the poles
-          M = split_df(g * T.my[((size_t)k * (n + 1) + f) * T.nlon + i]);
+          M = df_mul(gd, df_ld2(T.my2, ((size_t)k * (n + 1) + f) * T.nlon + i));
       } else if (f > 0 && f < n) {  // no flux through the surface and the model top
-        M = split_df(g * T.mz[(size_t)f * ncol + col]);
+        M = df_mul(gd, df_ld2(T.mz2, (size_t)f * ncol + col));
       }
       Mh[bck(T, f * kPencil + tx, mb)] = M.h;
       Ml[bck(T, f * kPencil + tx, mb)] = M.l;
@@ -1159,6 +1161,7 @@ __global__ void __launch_bounds__(128) k_adv_x_stream(DevTransport<double> T, St
   const double* Q;
   double g;
   if (!resolve_stage(sel, Q, g)) return;
+  const df gd = split_df(g);  // the stage time factor as a pair
   const int n = T.nlon, nf = n + 1;
   const int nseg = (n + kSegX - 1) / kSegX;
   const int lane = threadIdx.x & 31;
@@ -1172,7 +1175,7 @@ __global__ void __launch_bounds__(128) k_adv_x_stream(DevTransport<double> T, St
   const size_t rbase = ((size_t)k * T.nlat + j) * n;
   const bool periodic = T.lon_bc == 0;
   const df G = df_ld2(T.gx2, j);
-  const df M = (p >= 0 && p <= n) ? split_df(g * T.mx[((size_t)k * T.nlat + j) * nf + p])
+  const df M = (p >= 0 && p <= n) ? df_mul(gd, df_ld2(T.mx2, ((size_t)k * T.nlat + j) * nf + p))
                                    : df{0.0f, 0.0f};
   const bool out = lane >= 3 && lane <= 28 && p >= 0 && p < n;
   const int s0 = blockIdx.y * sper, s1 = min(T.ntr, s0 + sper);
@@ -1214,6 +1217,7 @@ __global__ void __launch_bounds__(128) k_adv_yz_stream(DevTransport<double> T, S
   const double* Q;
   double g;
   if (!resolve_stage(sel, Q, g)) return;
+  const df gd = split_df(g);  // the stage time factor as a pair
   const int n = DIR == 1 ? T.nlat : T.nlev;
   const size_t ncol = (size_t)T.nlon * T.nlat;
   const size_t nc = ncol * T.nlev;
@@ -1228,9 +1232,9 @@ __global__ void __launch_bounds__(128) k_adv_yz_stream(DevTransport<double> T, S
   const bool open = DIR == 1 && T.lat_bc == 1;
   auto flux = [&](int f) -> df {  // face f's air-mass flux, zero through closed walls
     if (DIR == 1) {
-      if (open || (f > 0 && f < n)) return split_df(g * T.my[((size_t)k * (n + 1) + f) * T.nlon + i]);
+      if (open || (f > 0 && f < n)) return df_mul(gd, df_ld2(T.my2, ((size_t)k * (n + 1) + f) * T.nlon + i));
     } else if (f > 0 && f < n) {
-      return split_df(g * T.mz[(size_t)f * ncol + col]);
+      return df_mul(gd, df_ld2(T.mz2, (size_t)f * ncol + col));
     }
     return df{0.0f, 0.0f};
   };
@@ -1254,8 +1258,15 @@ __global__ void __launch_bounds__(128) k_adv_yz_stream(DevTransport<double> T, S
     // window: qp = q(p-1); D4..D1 = D(p-4..p-1); S2, S1 = S(p-2), S(p-1); E4..E2 = E(p-4..p-2)
     df qp = load(-3), D4 = z, D3 = z, D2 = z, D1 = z, S2 = z, S1 = z, E4 = z, E3 = z, E2 = z;
     df psi_prev = z;  // Psi of the previous face (the open cell's west face)
+    // one iteration ahead: q(p), the flux of face p-2 and the accumulator of cell p-3
+    df q_nx = load(-2), m_nx = z;
+    float2 a_nx = make_float2(0.0f, 0.0f);
     for (int p = -2; p <= n + 2; ++p) {
-      const df qn = load(p);
+      const df qn = q_nx, Mf = m_nx;
+      const float2 o = a_nx;
+      if (p < n + 2) q_nx = load(p + 1);
+      if (p - 1 >= 0 && p - 1 <= n) m_nx = flux(p - 1);
+      if (p - 2 >= 0 && p - 2 < n) a_nx = T.acc[bck(T, pb + (size_t)(p - 2) * stride, nall)];
       D4 = D3; D3 = D2; D2 = D1;
       D1 = df_sub(qn, qp);  // D(p-1)
       qp = qn;
@@ -1282,7 +1293,7 @@ __global__ void __launch_bounds__(128) k_adv_yz_stream(DevTransport<double> T, S
       const int f = p - 2;  // the face now complete (needs E(f-2..f), D(f-2..f-1))
       if (f < 0 || f > n) continue;
       df psi, phi;
-      face_terms(flux(f), [&](int o) { return o == 0 ? E2 : (o == -1 ? E3 : E4); },
+      face_terms(Mf, [&](int o) { return o == 0 ? E2 : (o == -1 ? E3 : E4); },
                  [&](int o) { return o == -1 ? D3 : D4; }, psi, phi);
       if (f >= 1) {  // cell f-1 is complete: its east face f, west face f-1
         const int c = f - 1;
@@ -1292,7 +1303,6 @@ __global__ void __launch_bounds__(128) k_adv_yz_stream(DevTransport<double> T, S
         else
           a = df_neg(df_add(phi, psi_prev));
         const size_t x = bck(T, pb + (size_t)c * stride, nall);
-        const float2 o = T.acc[x];
         const df t = df_add(df{o.x, o.y}, a);
         T.acc[x] = make_float2(t.h, t.l);
       }
@@ -1346,6 +1356,18 @@ __device__ __forceinline__ df split_df(double v) {
   split_bits(v, r.h, r.l);
 #endif
   return r;
+}
+
+// (hi, lo) pairs of a double array (the air-mass face fluxes of the mixed kernels)
+__global__ void k_make_pairs(const double* __restrict__ src, float2* __restrict__ dst, size_t n) {
+  const size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (x < n) {
+    const df v = split_df(src[x]);
+    dst[x] = make_float2(v.h, v.l);
+  }
+}
+void launch_make_pairs(cudaStream_t st, const double* src, float2* dst, size_t n) {
+  if (n) k_make_pairs<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(src, dst, n);
 }
 
 // split the attempt's input state U[cur] (stage 1's RHS argument) into hi/lo planes
