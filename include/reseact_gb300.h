@@ -237,9 +237,11 @@ void* rs_stream(rs_handle* h);
 
 /* Project-written autotuner (no reference counterpart): times candidate launch shapes on the
  * handle's current state and forcing -- threads per block x blocks per SM ("cells per block")
- * of the per-cell chemistry kernel (three attempts per cell on scratch copies), threads per
- * lon row and pencil width x rows per block (the halo tile) of the transport kernels -- keeps
- * the fastest for this handle and writes a JSON report of every candidate into buf. */
+ * of the per-cell chemistry kernel (three attempts per cell on scratch copies) and, for the
+ * table-walking kernels of the production build, the form with G = 4, 8 or 16 lanes per cell
+ * and its work arrays in shared memory; threads per lon row and pencil width x rows per block
+ * (the halo tile) of the transport kernels -- keeps the fastest for this handle and writes a
+ * JSON report of every candidate into buf. */
 rs_status rs_autotune(rs_handle* h, char* buf, size_t buf_len);
 
 /* Set one launch shape that rs_autotune would choose, e.g. to replay an earlier tuning without
@@ -248,8 +250,9 @@ rs_status rs_autotune(rs_handle* h, char* buf, size_t buf_len);
  * "mixed_xthreads", "mixed_x_tracers", "mixed_pencil", "mixed_rows", "mixed_yz_tracers",
  * "mixed_x_bulk", "mixed_yz_bulk" (mixed pencils); "mixed_x_stream", "mixed_yz_stream" (1: the
  * streaming forms of the mixed kernels instead of the pencils); "per_cell_threads",
- * "per_cell_blocks_per_sm" (per-cell chemistry).  Values outside a key's candidates are
- * RS_ERR_INVALID.  Every shape gives bit-identical results. */
+ * "per_cell_blocks_per_sm", "per_cell_group" (per-cell chemistry; group 0 = one thread per
+ * cell, 4 / 8 / 16 = lanes per cell, production build only).  Values outside a key's
+ * candidates are RS_ERR_INVALID.  Every shape gives bit-identical results. */
 rs_status rs_set_launch_shape(rs_handle* h, const char* key, int32_t value);
 
 /* Chemistry kernel selection (no reference counterpart; the reference compiles its RHS and

@@ -238,14 +238,37 @@ MechTables derive_tables(const rs_mechanism& m, bool natural_order) {
       }
     T.low_ptr.push_back((int)T.low_row.size());
   }
+  // Back substitution, row i: x_i = (b_i - sum_j U_ij x_j) U_ii^-1.  The natural order (the
+  // strict build) sums in ascending j, as blocksolve; the production order in descending j, the
+  // order in which the x_j become known, so that a column sweep (the G-lanes-per-cell kernels:
+  // subtract U_ij x_j from every row of column j as soon as x_j is known) adds each row's terms
+  // in the same order as the row loop of the thread-per-cell kernels -- the same bits.
   T.up_ptr.push_back(0);
   for (int i = 0; i < ns; ++i) {
-    for (int j = i + 1; j < ns; ++j)
+    for (int jj = i + 1; jj < ns; ++jj) {
+      const int j = natural_order ? jj : ns - 1 - (jj - i - 1);
       if (fill.count({i, j})) {
         T.up_col.push_back(ord[j]);
         T.up_slot.push_back(slot[{i, j}]);
       }
+    }
     T.up_ptr.push_back((int)T.up_col.size());
+  }
+  // the same schedule for kernels that spread one cell over several lanes: the updates of
+  // pivot k (each dst slot at most once per pivot) with their multiplier slots, and the
+  // upper factor by columns
+  for (int k = 0; k <= ns; ++k) T.pupd_ptr.push_back(T.upd_ptr[T.elim_ptr[k]]);
+  T.upd_lik.assign(T.upd_dst.size(), 0);
+  for (size_t mm = 0; mm < T.elim_lik.size(); ++mm)
+    for (int u = T.upd_ptr[mm]; u < T.upd_ptr[mm + 1]; ++u) T.upd_lik[u] = T.elim_lik[mm];
+  T.upc_ptr.push_back(0);
+  for (int j = 0; j < ns; ++j) {
+    for (int i = 0; i < j; ++i)
+      if (fill.count({i, j})) {
+        T.upc_row.push_back(ord[i]);
+        T.upc_slot.push_back(slot[{i, j}]);
+      }
+    T.upc_ptr.push_back((int)T.upc_row.size());
   }
   // rate programs: validate stack discipline
   T.prog_ptr.assign(m.prog_ptr, m.prog_ptr + nr + 1);
@@ -376,6 +399,7 @@ struct rs_handle {
   // launch shapes picked by rs_autotune (defaults until it runs)
   struct Tune {
     int pc_threads = 128, pc_blocks_per_sm = 4;      // per-cell chemistry kernel
+    int pc_group = 0;  // lanes per cell of the table-walking per-cell kernel (0: one thread)
     int pencil = 32, rows = 8, xthreads = 128;        // transport pencil kernels
     int xgroups = 1, yzgroups = 1;                    // their tracer groups
     int mpencil = 16, mrows = 16, mxthreads = 128;    // mixed-precision pencil kernels
@@ -492,6 +516,8 @@ void build_device_mech(rs_handle* h) {
   D.upd_dst = ui(T.upd_dst); D.upd_src = ui(T.upd_src);
   D.low_ptr = ui(T.low_ptr); D.low_row = ui(T.low_row); D.low_slot = ui(T.low_slot);
   D.up_ptr = ui(T.up_ptr); D.up_col = ui(T.up_col); D.up_slot = ui(T.up_slot);
+  D.pupd_ptr = ui(T.pupd_ptr); D.upd_lik = ui(T.upd_lik);
+  D.upc_ptr = ui(T.upc_ptr); D.upc_row = ui(T.upc_row); D.upc_slot = ui(T.upc_slot);
   D.prog_ptr = ui(T.prog_ptr); D.prog_op = ui(T.prog_op); D.prog_val = ud(T.prog_val);
   D.params = ud(T.params);
   D.combinatoric = T.comb;
@@ -1357,11 +1383,23 @@ rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double*
         int thr = h->tune.pc_threads;
         int nblocks = std::max(1, std::min(nsm * h->tune.pc_blocks_per_sm,
                                            (int)((h->nc + thr - 1) / thr)));
+        const int G = h->lc.jit ? 0 : h->tune.pc_group;
+        if (G > 0) {  // a persistent grid of resident blocks, one cell per G lanes
+          thr = rs::chem_group_threads(h->lc, G);
+          const int bps = rs::chem_group_blocks_per_sm(h->lc, G, thr);
+          if (thr == 0 || bps == 0) throw RsError(RS_ERR_UNSUPPORTED, "per-cell group kernel does not fit");
+          nblocks = std::max(1, std::min(nsm * bps, (int)((h->nc + thr / G - 1) / (thr / G))));
+        }
         {
           Scope s(h, "chem_per_cell");
-          rs::launch_chem_per_cell(h->lc, nblocks, thr, h->U[h->cur].p, h->krates.p,
-                                   h->have_emis ? h->emis.p : nullptr, h->dtcell.p,
-                                   h->stepcell.p, h->queue.p, h->flag.p, a);
+          if (G > 0)
+            rs::launch_chem_per_cell_group(h->lc, G, nblocks, thr, h->U[h->cur].p, h->krates.p,
+                                           h->have_emis ? h->emis.p : nullptr, h->dtcell.p,
+                                           h->stepcell.p, h->queue.p, h->flag.p, a);
+          else
+            rs::launch_chem_per_cell(h->lc, nblocks, thr, h->U[h->cur].p, h->krates.p,
+                                     h->have_emis ? h->emis.p : nullptr, h->dtcell.p,
+                                     h->stepcell.p, h->queue.p, h->flag.p, a);
         }
         h->launches += 1;
         CK(cudaGetLastError());
@@ -2009,6 +2047,12 @@ extern "C" rs_status rs_set_launch_shape(rs_handle* h, const char* key, int32_t 
     else if (k == "mixed_yz_stream") ok = in({0, 1}) && (t.mstream_yz = value, true);
     else if (k == "per_cell_threads") ok = in({64, 128, 256}) && (t.pc_threads = value, true);
     else if (k == "per_cell_blocks_per_sm") ok = in({1, 2, 4, 8}) && (t.pc_blocks_per_sm = value, true);
+    else if (k == "per_cell_group") {
+      // G lanes per cell: the production build's (minimum-fill, descending back substitution)
+      // table-walking kernels only, and only where a block of them fits in shared memory
+      ok = in({0, 4, 8, 16}) && (value == 0 || (!RS_STRICT && rs::chem_group_threads(h->lc, value) > 0));
+      if (ok) t.pc_group = value;
+    }
     else throw RsError(RS_ERR_INVALID, "unknown launch-shape key: " + k);
     if (!ok) throw RsError(RS_ERR_INVALID, "value out of range for " + k);
     refresh_dt(h);
@@ -2345,10 +2389,39 @@ extern "C" rs_status rs_autotune(rs_handle* h, char* buf, size_t buf_len) {
             best = ms;
             h->tune.pc_threads = thr;
             h->tune.pc_blocks_per_sm = bps;
+            h->tune.pc_group = 0;
           }
         }
-      std::snprintf(line, sizeof line, "], \"per_cell_choice\": {\"threads\": %d, \"blocks_per_sm\": %d}",
-                    h->tune.pc_threads, h->tune.pc_blocks_per_sm);
+      // G lanes per cell (table-walking kernels of the production build): every resident
+      // block of the persistent grid
+      if (!RS_STRICT && !h->lc.jit)
+        for (int G : {4, 8, 16}) {
+          const int thr = rs::chem_group_threads(h->lc, G);
+          const int bps = thr ? rs::chem_group_blocks_per_sm(h->lc, G, thr) : 0;
+          if (bps == 0) continue;
+          const int cpb = thr / G;
+          int nb = std::max(1, std::min(nsm * bps, (int)((h->nc + cpb - 1) / cpb)));
+          float ms = time_min(h->st, 2, [&] {
+            cudaMemcpyAsync(h->io2.p, h->U[h->cur].p, n * sizeof(double),
+                            cudaMemcpyDeviceToDevice, h->st);
+            cudaMemsetAsync(h->io.p, 0, h->nc * sizeof(double), h->st);
+            cudaMemsetAsync(h->queue.p, 0, sizeof(unsigned long long), h->st);
+            rs::launch_chem_per_cell_group(h->lc, G, nb, thr, h->io2.p, h->krates.p,
+                                           h->have_emis ? h->emis.p : nullptr, h->io.p, nullptr,
+                                           h->queue.p, h->flag.p, a);
+          });
+          std::snprintf(line, sizeof line,
+                        ", {\"group\": %d, \"threads\": %d, \"blocks_per_sm\": %d, \"ms\": %.4f}",
+                        G, thr, bps, ms);
+          rep += line;
+          if (ms < best) {
+            best = ms;
+            h->tune.pc_group = G;
+          }
+        }
+      std::snprintf(line, sizeof line,
+                    "], \"per_cell_choice\": {\"threads\": %d, \"blocks_per_sm\": %d, \"group\": %d}",
+                    h->tune.pc_threads, h->tune.pc_blocks_per_sm, h->tune.pc_group);
       rep += line;
     }
     if (h->cfg.do_chemistry && h->cfg.chem_mode == RS_CHEM_GLOBAL_DT && h->lc.jit) {

@@ -268,6 +268,292 @@ __global__ void __launch_bounds__(256) k_chem_per_cell(
   }
 }
 
+// ------------------------------------------------------------------ per-cell, G lanes per cell
+// The per-cell adaptive form with one cell spread over G lanes (G = 4, 8, 16) and its work
+// arrays in shared memory instead of thread-local memory: the lanes split the rate products,
+// RHS sums, partials and Jacobian entries, each pivot's multipliers and updates (every update
+// of one pivot writes a different slot), each column of the forward solve, and the back
+// substitution as a column sweep (descending columns: see the table derivation).  Every value
+// is formed by the same operations in the same order as in k_chem_per_cell, so both give the
+// same bits; rs_autotune times both.  Scalars that all lanes need (pivot reciprocals, the
+// error norm, the controller) are formed redundantly by every lane of the group: this GPU
+// charges an FP64 warp instruction the same time whatever the number of active lanes.
+// Shared memory per cell (doubles): x, xn, f0, k1, f1, k2, b, em, piv, norm terms [ns each],
+// rate constants [nr], velocities / partials (never live together) [max(nr, npart)], W [nlu].
+struct GroupOff {
+  int x, xn, f0, k1, f1, k2, b, em, piv, at, kc, pv, w;
+};
+__device__ __forceinline__ GroupOff group_off(const DevMech& M) {
+  const int n = M.ns;
+  GroupOff o;
+  o.x = 0; o.xn = n; o.f0 = 2 * n; o.k1 = 3 * n; o.f1 = 4 * n; o.k2 = 5 * n; o.b = 6 * n;
+  o.em = 7 * n; o.piv = 8 * n; o.at = 9 * n; o.kc = 10 * n; o.pv = 10 * n + M.nr;
+  o.w = o.pv + (M.nr > M.npart ? M.nr : M.npart);
+  return o;
+}
+
+template <int G>
+struct Grp {
+  int l;        // lane within the group
+  unsigned m;   // the group's lanes in the warp
+  __device__ __forceinline__ void sync() const { __syncwarp(m); }
+};
+
+// v[r] = k_r prod x^nu (velocities), lanes split the reactions
+template <int G>
+__device__ __forceinline__ void g_velocities(const DevMech& M, const Grp<G>& g, const double* kc,
+                                             const double* x, double* v) {
+  for (int r = g.l; r < M.nr; r += G) {
+    double a = kc[r];
+    int e1 = ldi(M.rptr + r + 1);
+    for (int e = ldi(M.rptr + r); e < e1; ++e) {
+      double xs = x[ldi(M.rsp + e)];
+      int nu = ldi(M.rnu + e);
+      for (int t = 0; t < nu; ++t) a = a * xs;
+    }
+    v[r] = a;
+  }
+}
+template <int G>
+__device__ __forceinline__ void g_rhs(const DevMech& M, const Grp<G>& g, const double* v,
+                                      const double* emis, double* f) {
+  for (int s = g.l; s < M.ns; s += G) {
+    double acc = 0.0;
+    int e1 = ldi(M.rhs_ptr + s + 1);
+    for (int e = ldi(M.rhs_ptr + s); e < e1; ++e) acc = acc + ld(M.rhs_c + e) * v[ldi(M.rhs_r + e)];
+    f[s] = emis ? acc + emis[s] : acc;
+  }
+}
+template <int G>
+__device__ __forceinline__ void g_partials(const DevMech& M, const Grp<G>& g, const double* k,
+                                           const double* x, double* P) {
+  for (int p = g.l; p < M.npart; p += G) {
+    int r = ldi(M.part_r + p), q = ldi(M.part_q + p);
+    double d = k[r];
+    int e1 = ldi(M.rptr + r + 1);
+    for (int e = ldi(M.rptr + r); e < e1; ++e) {
+      int s = ldi(M.rsp + e), nu = ldi(M.rnu + e);
+      double xs = x[s];
+      if (s == q) {
+        if (nu >= 2) {
+          double f = (double)nu;
+          for (int t = 1; t < nu; ++t) f = f * xs;
+          d = d * f;
+        }
+      } else {
+        for (int t = 0; t < nu; ++t) d = d * xs;
+      }
+    }
+    P[p] = d;
+  }
+}
+template <int G>
+__device__ __forceinline__ void g_build_w(const DevMech& M, const Grp<G>& g, const double* P,
+                                          double dtgamma, double* W) {
+  for (int e = g.l; e < M.nlu; e += G) W[e] = 0.0;
+  g.sync();
+  for (int i = g.l; i < M.ns; i += G) W[ldi(M.lu_diag + i)] = 1.0;
+  g.sync();
+  for (int e = g.l; e < M.njac; e += G) {
+    double acc = 0.0;
+    int t1 = ldi(M.jac_ptr + e + 1);
+    for (int t = ldi(M.jac_ptr + e); t < t1; ++t)
+      acc = acc + ld(M.jac_coef + t) * P[ldi(M.jac_part + t)];
+    double tmp = dtgamma * acc;
+    W[ldi(M.jac_slot + e)] = (ldi(M.jac_diag + e) ? 1.0 : 0.0) - tmp;
+  }
+  g.sync();
+}
+template <int G>
+__device__ __forceinline__ void g_lu_factor(const DevMech& M, const Grp<G>& g, double* W,
+                                            double* piv) {
+  for (int k = 0; k < M.ns; ++k) {
+    const double pk = 1.0 / W[ldi(M.lu_diag + k)];
+    if (g.l == 0) piv[k] = pk;
+    const int i1 = ldi(M.elim_ptr + k + 1);
+    for (int ii = ldi(M.elim_ptr + k) + g.l; ii < i1; ii += G) {
+      const int sl = ldi(M.elim_lik + ii);
+      W[sl] = W[sl] * pk;
+    }
+    g.sync();
+    const int u1 = ldi(M.pupd_ptr + k + 1);
+    for (int u = ldi(M.pupd_ptr + k) + g.l; u < u1; u += G) {
+      const int dst = ldi(M.upd_dst + u);
+      double mw = W[ldi(M.upd_lik + u)] * W[ldi(M.upd_src + u)];
+      W[dst] = W[dst] - mw;
+    }
+    g.sync();
+  }
+}
+// in place b -> x; entry at the group's sync state, leaves synced
+template <int G>
+__device__ __forceinline__ void g_lu_solve(const DevMech& M, const Grp<G>& g, const double* W,
+                                           const double* piv, double* b) {
+  for (int k = 0; k < M.ns; ++k) {
+    const double bk = b[ldi(M.ord + k)];
+    const int e1 = ldi(M.low_ptr + k + 1);
+    for (int e = ldi(M.low_ptr + k) + g.l; e < e1; e += G) {
+      const int i = ldi(M.low_row + e);
+      double mb = W[ldi(M.low_slot + e)] * bk;
+      b[i] = b[i] - mb;
+    }
+    g.sync();
+  }
+  for (int j = M.ns - 1; j >= 0; --j) {
+    const int sj = ldi(M.ord + j);
+#if RS_STRICT
+    const double xj = b[sj] / W[ldi(M.lu_diag + j)];
+#else
+    const double xj = b[sj] * piv[j];
+#endif
+    const int e1 = ldi(M.upc_ptr + j + 1);
+    for (int e = ldi(M.upc_ptr + j) + g.l; e < e1; e += G) {
+      const int i = ldi(M.upc_row + e);
+      double wx = W[ldi(M.upc_slot + e)] * xj;
+      b[i] = b[i] - wx;
+    }
+    g.sync();
+    if (g.l == 0) b[sj] = xj;  // nobody reads b[sj] again in this sweep
+  }
+  g.sync();
+}
+
+// One attempt from S[x] with step sizes h: S[xn] (unclamped); returns the sum of squared scaled
+// errors (the same value in every lane of the group).
+template <int G>
+__device__ __forceinline__ double ros23_group(const DevMech& M, const Grp<G>& g, double* S,
+                                              const GroupOff& o, bool emis,
+                                              const StepScalars& h, double rtol, double atol) {
+  const int n = M.ns;
+  const double dt = h.dt;
+  double *x = S + o.x, *xn = S + o.xn, *f0 = S + o.f0, *k1 = S + o.k1, *f1 = S + o.f1,
+         *k2 = S + o.k2, *b = S + o.b, *piv = S + o.piv, *at = S + o.at, *kc = S + o.kc,
+         *pv = S + o.pv, *W = S + o.w;
+  const double* em = emis ? S + o.em : nullptr;
+  g_velocities(M, g, kc, x, pv);
+  g.sync();
+  g_rhs(M, g, pv, em, f0);
+  g.sync();
+  g_partials(M, g, kc, x, pv);
+  g.sync();
+  g_build_w(M, g, pv, h.dtgamma, W);
+  g_lu_factor(M, g, W, piv);
+  for (int s = g.l; s < n; s += G) k1[s] = f0[s];
+  g.sync();
+  g_lu_solve(M, g, W, piv, k1);  // k1 = W \ f0
+  for (int s = g.l; s < n; s += G) xn[s] = x[s] + h.dto2 * k1[s];  // u1
+  g.sync();
+  g_velocities(M, g, kc, xn, pv);
+  g.sync();
+  g_rhs(M, g, pv, em, f1);  // f1 = f(u1)
+  for (int s = g.l; s < n; s += G) k2[s] = f1[s] - k1[s];
+  g.sync();
+  g_lu_solve(M, g, W, piv, k2);
+  for (int s = g.l; s < n; s += G) k2[s] = k2[s] + k1[s];  // k2 = W\(f1-k1) + k1
+  for (int s = g.l; s < n; s += G) xn[s] = x[s] + dt * k2[s];  // unew
+  g.sync();
+  g_velocities(M, g, kc, xn, pv);
+  g.sync();
+  g_rhs(M, g, pv, em, b);  // f2
+  for (int s = g.l; s < n; s += G) {
+    double a = M.ros_c32 * (k2[s] - f1[s]);
+    double c = 2.0 * (k1[s] - f0[s]);
+    b[s] = (b[s] - a) - c;
+  }
+  g.sync();
+  g_lu_solve(M, g, W, piv, b);  // k3
+  for (int s = g.l; s < n; s += G) {
+    double ut = h.dto6 * ((k1[s] - 2.0 * k2[s]) + b[s]);
+    double am = fmax(fabs(x[s]), fabs(xn[s]));
+    double den = am * rtol + atol;
+    at[s] = ut / den;
+  }
+  g.sync();
+  double acc = 0.0;
+  for (int s = 0; s < n; ++s) {
+    const double a = at[s];
+    acc = acc + a * a;
+  }
+  return acc;
+}
+
+template <int G>
+__global__ void __launch_bounds__(128) k_chem_per_cell_group(
+    DevMech M, int nc, int nsp, double* __restrict__ U, const double* __restrict__ krates,
+    const double* __restrict__ emission, double* __restrict__ dt_cell,
+    double* __restrict__ steps_cell, unsigned long long* __restrict__ queue,
+    int* __restrict__ status, PerCellArgs a, int cell_doubles) {
+  extern __shared__ double gsm[];
+  const int wl = threadIdx.x & 31;
+  Grp<G> g;
+  g.l = threadIdx.x % G;
+  g.m = (G == 32 ? 0xffffffffu : ((1u << G) - 1u)) << (wl & ~(G - 1));
+  const int lead = wl & ~(G - 1);
+  double* S = gsm + (size_t)(threadIdx.x / G) * cell_doubles;
+  const GroupOff o = group_off(M);
+  const bool emis = emission != nullptr;
+  double my_steps = 0.0, my_attempts = 0.0;
+  double t = 0, dt = 0, qold = 0, iters = 0, nacc = 0;
+  int c = -1;
+  const double tlim = a.t1 - 1.0e-9;
+  for (;;) {
+    if (c < 0) {
+      unsigned long long nxt = 0;
+      if (g.l == 0) nxt = atomicAdd(queue, 1ull);
+      nxt = __shfl_sync(g.m, nxt, lead);
+      if (nxt >= (unsigned long long)nc) break;
+      c = (int)nxt;
+      for (int s = g.l; s < M.ns; s += G) S[o.x + s] = U[(size_t)s * nc + c];
+      for (int r = g.l; r < M.nr; r += G) S[o.kc + r] = krates[(size_t)r * nc + c];
+      if (emis)
+        for (int s = g.l; s < M.ns; s += G) S[o.em + s] = emission[(size_t)s * nc + c];
+      g.sync();
+      t = a.t0;
+      dt = quant_dt(dt_cell[c] > 0.0 ? dt_cell[c] : a.dt0);
+      qold = a.qoldinit;
+      iters = 0;
+      nacc = 0;
+    }
+    if ((t < tlim) && (iters < a.maxiters)) {
+      double dtc = fmin(dt, a.t1 - t);
+      double sse = ros23_group(M, g, S, o, emis, step_scalars(M, dtc), a.rtol, a.atol);
+      double EEst = sqrt(sse / (double)nsp);
+      if (isnan(EEst)) EEst = 1.0e10;
+      double q11 = pow(fmax(EEst, 1.0e-35), a.beta1);
+      double q = q11 / pow(qold, a.beta2);
+      q = fmax(a.invqmax, fmin(a.invqmin, q / a.gamma));
+      if (EEst <= 1.0) {
+        for (int s = g.l; s < M.ns; s += G)
+          S[o.x + s] = a.clamp ? fmax(S[o.xn + s], 0.0) : S[o.xn + s];
+        g.sync();
+        t = t + dtc;
+        bool insteady = (a.qsmin <= q) && (q <= a.qsmax);
+        dt = quant_dt(dtc / (insteady ? 1.0 : q));
+        qold = fmax(EEst, a.qoldinit);
+        nacc += 1.0;
+      } else {
+        dt = quant_dt(dtc / fmin(a.invqmin, q11 / a.gamma));
+      }
+      iters += 1.0;
+    } else {
+      if (g.l == 0 && t < tlim) atomicOr(status, 1);
+      for (int s = g.l; s < M.ns; s += G) U[(size_t)s * nc + c] = S[o.x + s];
+      if (g.l == 0) {
+        dt_cell[c] = dt;
+        if (steps_cell) steps_cell[c] = nacc;
+        my_steps += nacc;
+        my_attempts += iters;
+      }
+      g.sync();  // the next cell's loads overwrite S
+      c = -1;
+    }
+  }
+  if (a.totals && g.l == 0) {
+    atomicAdd(a.totals, my_steps);
+    atomicAdd(a.totals + 1, my_attempts);
+  }
+}
+
 // ------------------------------------------------------------------ launch helpers
 template <int MS, int MR, int MLU, int MP>
 struct ChemLaunch {
@@ -333,6 +619,67 @@ void launch_block_jac(const LaunchCtx& L, const double* U, const double* kr, con
                       const int* scol, double* J) {
   if (L.size_class == 0) Small::jac(L, U, kr, srow, scol, J);
   else Large::jac(L, U, kr, srow, scol, J);
+}
+int group_cell_doubles(const DevMech& M) {
+  int d = 10 * M.ns + M.nr + (M.nr > M.npart ? M.nr : M.npart) + M.nlu;
+  return d + (d & 1);  // even: 16-byte aligned cells
+}
+template <int G>
+static int group_threads_t(const DevMech& M) {
+  int maxdyn = 0, dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&maxdyn, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+    return 0;
+  for (int thr : {128, 64, 32})
+    if (thr >= G && (size_t)(thr / G) * group_cell_doubles(M) * sizeof(double) <= (size_t)maxdyn)
+      return thr;
+  return 0;
+}
+int chem_group_threads(const LaunchCtx& L, int G) {
+  switch (G) {
+    case 4: return group_threads_t<4>(L.mech);
+    case 8: return group_threads_t<8>(L.mech);
+    case 16: return group_threads_t<16>(L.mech);
+    default: return 0;
+  }
+}
+template <int G>
+static int group_occupancy_t(const DevMech& M, int thr) {
+  const size_t smem = (size_t)(thr / G) * group_cell_doubles(M) * sizeof(double);
+  if (cudaFuncSetAttribute(k_chem_per_cell_group<G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess)
+    return 0;
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_chem_per_cell_group<G>, thr, smem) !=
+      cudaSuccess)
+    return 0;
+  return nb;
+}
+int chem_group_blocks_per_sm(const LaunchCtx& L, int G, int thr) {
+  switch (G) {
+    case 4: return group_occupancy_t<4>(L.mech, thr);
+    case 8: return group_occupancy_t<8>(L.mech, thr);
+    case 16: return group_occupancy_t<16>(L.mech, thr);
+    default: return 0;
+  }
+}
+void launch_chem_per_cell_group(const LaunchCtx& L, int G, int nblocks, int thr, double* U,
+                                const double* kr, const double* em, double* dtc, double* steps,
+                                unsigned long long* queue, int* status, const PerCellArgs& a) {
+  const int cd = group_cell_doubles(L.mech);
+  const size_t smem = (size_t)(thr / G) * cd * sizeof(double);
+#define RS_GROUP_LAUNCH(GG)                                                                    \
+  cudaFuncSetAttribute(k_chem_per_cell_group<GG>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                       (int)smem);                                                             \
+  k_chem_per_cell_group<GG><<<nblocks, thr, smem, L.stream>>>(L.mech, L.nc, L.nsp, U, kr, em, \
+                                                              dtc, steps, queue, status, a, cd)
+  switch (G) {
+    case 4: RS_GROUP_LAUNCH(4); break;
+    case 8: RS_GROUP_LAUNCH(8); break;
+    case 16: RS_GROUP_LAUNCH(16); break;
+    default: break;
+  }
+#undef RS_GROUP_LAUNCH
 }
 void launch_chem_per_cell(const LaunchCtx& L, int nblocks, int threads, double* U,
                           const double* kr, const double* em, double* dtc, double* steps,

@@ -69,6 +69,11 @@ struct DevMech {
   const int* up_ptr;    // [ns+1] backward solve, pivot row i: columns after i ascending
   const int* up_col;    //   (species index of the column)
   const int* up_slot;
+  const int* pupd_ptr;  // [ns+1] updates of pivot k (ranges of upd_dst / upd_src)
+  const int* upd_lik;   // multiplier slot (i,k) of each update
+  const int* upc_ptr;   // [ns+1] upper factor by columns: column j's entries (rows i < j)
+  const int* upc_row;   //   (species index of the row)
+  const int* upc_slot;
   const int* prog_ptr;  // rate programs
   const int* prog_op;
   const double* prog_val;

@@ -123,6 +123,15 @@ void launch_block_jac(const LaunchCtx& L, const double* U, const double* kr, con
 void launch_chem_per_cell(const LaunchCtx& L, int nblocks, int threads, double* U,
                           const double* kr, const double* em, double* dtc, double* steps,
                           unsigned long long* queue, int* status, const PerCellArgs& a);
+// the per-cell form with G lanes per cell (G = 4, 8, 16; table mechanisms, minimum-fill order):
+// doubles of shared memory per cell, the threads per block that fit (0: none), resident blocks
+// per SM, and the launch
+int group_cell_doubles(const DevMech& M);
+int chem_group_threads(const LaunchCtx& L, int G);
+int chem_group_blocks_per_sm(const LaunchCtx& L, int G, int threads);
+void launch_chem_per_cell_group(const LaunchCtx& L, int G, int nblocks, int threads, double* U,
+                                const double* kr, const double* em, double* dtc, double* steps,
+                                unsigned long long* queue, int* status, const PerCellArgs& a);
 
 // transport (rs_transport.cu).  Stage s in 1..4 of one SSPRK43 attempt; buffers:
 // U0/U1 accepted/candidate (selected by ctl->cur), S1..S3 stage scratch.

@@ -16,7 +16,10 @@ struct MechTables {
       ord,                          // species eliminated at position k
       elim_ptr, elim_lik, upd_ptr, upd_dst, upd_src,  // natural-order elimination schedule
       low_ptr, low_row, low_slot,   // forward solve, column k: rows i>k
-      up_ptr, up_col, up_slot,      // backward solve, row i: columns j>i ascending
+      up_ptr, up_col, up_slot,      // backward solve, row i: columns j>i (ascending in the
+                                    // natural order, descending in the minimum-fill order)
+      pupd_ptr, upd_lik,            // per pivot: range of its updates; each update's multiplier
+      upc_ptr, upc_row, upc_slot,   // upper factor by columns: column j's rows i<j
       prog_ptr, prog_op,            // rate programs
       slot_row, slot_col;           // (row, col) of each LU slot
   std::vector<double> rhs_c, jac_coef, prog_val, params;
