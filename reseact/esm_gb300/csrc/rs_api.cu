@@ -400,6 +400,7 @@ struct rs_handle {
   struct Tune {
     int pc_threads = 128, pc_blocks_per_sm = 4;      // per-cell chemistry kernel
     int pc_group = 0;  // lanes per cell of the table-walking per-cell kernel (0: one thread)
+    int pc_regcap = 0;  // 1: the table-walking per-cell kernel capped at 32 registers
     int pencil = 32, rows = 8, xthreads = 128;        // transport pencil kernels
     int xgroups = 1, yzgroups = 1;                    // their tracer groups
     int mpencil = 16, mrows = 16, mxthreads = 128;    // mixed-precision pencil kernels
@@ -1399,7 +1400,8 @@ rs_status rs_macro_step(rs_handle* h, double t0, double t1, double* dtT, double*
           else
             rs::launch_chem_per_cell(h->lc, nblocks, thr, h->U[h->cur].p, h->krates.p,
                                      h->have_emis ? h->emis.p : nullptr, h->dtcell.p,
-                                     h->stepcell.p, h->queue.p, h->flag.p, a);
+                                     h->stepcell.p, h->queue.p, h->flag.p, a,
+                                     h->tune.pc_regcap != 0);
         }
         h->launches += 1;
         CK(cudaGetLastError());
@@ -2046,7 +2048,8 @@ extern "C" rs_status rs_set_launch_shape(rs_handle* h, const char* key, int32_t 
     else if (k == "mixed_x_stream") ok = in({0, 1}) && (t.mstream_x = value, true);
     else if (k == "mixed_yz_stream") ok = in({0, 1}) && (t.mstream_yz = value, true);
     else if (k == "per_cell_threads") ok = in({64, 128, 256}) && (t.pc_threads = value, true);
-    else if (k == "per_cell_blocks_per_sm") ok = in({1, 2, 4, 8}) && (t.pc_blocks_per_sm = value, true);
+    else if (k == "per_cell_blocks_per_sm") ok = in({1, 2, 4, 8, 16}) && (t.pc_blocks_per_sm = value, true);
+    else if (k == "per_cell_regcap") ok = in({0, 1}) && (t.pc_regcap = value, true);
     else if (k == "per_cell_group") {
       // G lanes per cell: the production build's (minimum-fill, descending back substitution)
       // table-walking kernels only, and only where a block of them fits in shared memory
@@ -2390,6 +2393,33 @@ extern "C" rs_status rs_autotune(rs_handle* h, char* buf, size_t buf_len) {
             h->tune.pc_threads = thr;
             h->tune.pc_blocks_per_sm = bps;
             h->tune.pc_group = 0;
+            h->tune.pc_regcap = 0;
+          }
+        }
+      // the table-walking kernel capped at 32 registers, at full occupancy
+      if (!h->lc.jit)
+        for (int thr : {128, 256}) {
+          const int bps = 2048 / thr;
+          int nb = std::max(1, std::min(nsm * bps, (int)((h->nc + thr - 1) / thr)));
+          float ms = time_min(h->st, 2, [&] {
+            cudaMemcpyAsync(h->io2.p, h->U[h->cur].p, n * sizeof(double),
+                            cudaMemcpyDeviceToDevice, h->st);
+            cudaMemsetAsync(h->io.p, 0, h->nc * sizeof(double), h->st);
+            cudaMemsetAsync(h->queue.p, 0, sizeof(unsigned long long), h->st);
+            rs::launch_chem_per_cell(h->lc, nb, thr, h->io2.p, h->krates.p,
+                                     h->have_emis ? h->emis.p : nullptr, h->io.p, nullptr,
+                                     h->queue.p, h->flag.p, a, true);
+          });
+          std::snprintf(line, sizeof line,
+                        ", {\"threads\": %d, \"blocks_per_sm\": %d, \"regcap\": 1, \"ms\": %.4f}",
+                        thr, bps, ms);
+          rep += line;
+          if (ms < best) {
+            best = ms;
+            h->tune.pc_threads = thr;
+            h->tune.pc_blocks_per_sm = bps;
+            h->tune.pc_group = 0;
+            h->tune.pc_regcap = 1;
           }
         }
       // G lanes per cell (table-walking kernels of the production build): every resident
@@ -2417,11 +2447,13 @@ extern "C" rs_status rs_autotune(rs_handle* h, char* buf, size_t buf_len) {
           if (ms < best) {
             best = ms;
             h->tune.pc_group = G;
+            h->tune.pc_regcap = 0;
           }
         }
       std::snprintf(line, sizeof line,
-                    "], \"per_cell_choice\": {\"threads\": %d, \"blocks_per_sm\": %d, \"group\": %d}",
-                    h->tune.pc_threads, h->tune.pc_blocks_per_sm, h->tune.pc_group);
+                    "], \"per_cell_choice\": {\"threads\": %d, \"blocks_per_sm\": %d, \"group\": %d, "
+                    "\"regcap\": %d}",
+                    h->tune.pc_threads, h->tune.pc_blocks_per_sm, h->tune.pc_group, h->tune.pc_regcap);
       rep += line;
     }
     if (h->cfg.do_chemistry && h->cfg.chem_mode == RS_CHEM_GLOBAL_DT && h->lc.jit) {

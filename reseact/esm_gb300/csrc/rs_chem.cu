@@ -64,12 +64,29 @@ __global__ void k_rates(DevMech M, int nc, const double* __restrict__ T,
 // Per-cell work arrays live in thread-local memory (L1-resident at the occupancy used).
 template <int MS, int MR, int MLU, int MP>
 struct RosWork {
-  double x[MS], f0[MS], k1[MS], f1[MS], k2[MS], xn[MS], b[MS], piv[MS], em[MS];
+  double x[MS], f0[MS], k1[MS], f1[MS], k2[MS], xn[MS], b[MS], piv[MS], em[MS], f2[MS];
   double kc[MR], v[MR], P[MP], W[MLU];
 };
 
+// A scaled error term ut / (max(|x|, |xn|) rtol + atol); the production build multiplies by a
+// one-Newton-step reciprocal and takes the magnitude max on the bit patterns (the norm only
+// steers the controller), the strict build divides as the reference does.
+__device__ __forceinline__ double norm_term(double ut, double x, double xn, double rtol,
+                                            double atol) {
+#if RS_STRICT
+  double am = fmax(fabs(x), fabs(xn));
+  double den = am * rtol + atol;
+  return ut / den;
+#else
+  return ut * rcp_nr1(fma(amax_bits(x, xn), rtol, atol));  // den >= atol > 0
+#endif
+}
+
 // One attempt for one cell from x with step dt: xn (unclamped) and the cell's sum of squared
-// scaled errors over its chemistry species (the inert air-mass row contributes 0).
+// scaled errors over its chemistry species (the inert air-mass row contributes 0).  have_f0:
+// w.f0 already holds f(x); have_p: w.P already holds the partials at x (the per-cell loop
+// after a rejected attempt, or after an accepted one whose clamp left the candidate as it
+// was: f(x) is then the attempt's f2) -- the same bits as evaluating them again.
 struct StepScalars {
   double dt, dto2, dto6, dtgamma;
 };
@@ -80,12 +97,15 @@ __device__ __forceinline__ StepScalars step_scalars(const DevMech& M, double dt)
 template <int MS, int MR, int MLU, int MP>
 __device__ __forceinline__ double ros23_cell(const DevMech& M, RosWork<MS, MR, MLU, MP>& w,
                                              const double* emis, const StepScalars& h,
-                                             double rtol, double atol) {
+                                             double rtol, double atol, bool have_f0 = false,
+                                             bool have_p = false) {
   const int n = M.ns;
   const double dt = h.dt;
-  velocities(M, w.kc, w.x, w.v);
-  rhs_from_v(M, w.v, emis, w.f0);
-  partials(M, w.kc, w.x, w.P);
+  if (!have_f0) {
+    velocities(M, w.kc, w.x, w.v);
+    rhs_from_v(M, w.v, emis, w.f0);
+  }
+  if (!have_p) partials(M, w.kc, w.x, w.P);
   build_w(M, w.P, h.dtgamma, w.W);
   lu_factor(M, w.W, w.piv);
   for (int s = 0; s < n; ++s) w.k1[s] = w.f0[s];
@@ -98,19 +118,17 @@ __device__ __forceinline__ double ros23_cell(const DevMech& M, RosWork<MS, MR, M
   for (int s = 0; s < n; ++s) w.k2[s] = w.k2[s] + w.k1[s];  // k2 = W\(f1-k1) + k1
   for (int s = 0; s < n; ++s) w.xn[s] = w.x[s] + dt * w.k2[s];  // unew
   velocities(M, w.kc, w.xn, w.v);
-  rhs_from_v(M, w.v, emis, w.b);  // f2
+  rhs_from_v(M, w.v, emis, w.f2);  // f2 = f(unew)
   for (int s = 0; s < n; ++s) {
     double a = M.ros_c32 * (w.k2[s] - w.f1[s]);
     double c = 2.0 * (w.k1[s] - w.f0[s]);
-    w.b[s] = (w.b[s] - a) - c;
+    w.b[s] = (w.f2[s] - a) - c;
   }
   lu_solve(M, w.W, w.piv, w.b);  // k3
   double acc = 0.0;
   for (int s = 0; s < n; ++s) {
     double ut = h.dto6 * ((w.k1[s] - 2.0 * w.k2[s]) + w.b[s]);
-    double am = fmax(fabs(w.x[s]), fabs(w.xn[s]));
-    double den = am * rtol + atol;
-    double at = ut / den;
+    double at = norm_term(ut, w.x[s], w.xn[s], rtol, atol);
     acc = acc + at * at;
   }
   return acc;
@@ -204,9 +222,11 @@ __global__ void k_block_jac(DevMech M, int nc, int nsp, const double* __restrict
 // of a warp run the same attempt code on different cells, so uneven step counts do not idle
 // lanes: a lane whose cell finishes takes the next one from the queue.  Step sizes are rounded
 // down to 4 fraction bits (quant_dt), which keeps per-cell trajectories insensitive to
-// roundoff-sized input changes.
-template <int MS, int MR, int MLU, int MP>
-__global__ void __launch_bounds__(256) k_chem_per_cell(
+// roundoff-sized input changes.  MINB bounds the registers: 5 blocks of 256 threads (51
+// registers, 1280 resident threads per SM) or 8 (32 registers, 2048 threads: more local-memory
+// requests in flight for large mechanisms); the same arithmetic.
+template <int MS, int MR, int MLU, int MP, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_chem_per_cell(
     DevMech M, int nc, int nsp, double* __restrict__ U, const double* __restrict__ krates,
     const double* __restrict__ emission, double* __restrict__ dt_cell,
     double* __restrict__ steps_cell, unsigned long long* __restrict__ queue,
@@ -214,6 +234,7 @@ __global__ void __launch_bounds__(256) k_chem_per_cell(
   RosWork<MS, MR, MLU, MP> w;
   double my_steps = 0.0, my_attempts = 0.0;  // this thread's totals (exact small integers)
   double t = 0, dt = 0, qold = 0, iters = 0, nacc = 0;
+  bool have_f0 = false, have_p = false;  // w.f0 == f(x), w.P == partials at x
   int c = -1;
   const double tlim = a.t1 - 1.0e-9;
   for (;;) {
@@ -230,18 +251,29 @@ __global__ void __launch_bounds__(256) k_chem_per_cell(
       qold = a.qoldinit;
       iters = 0;
       nacc = 0;
+      have_f0 = have_p = false;
     }
     if ((t < tlim) && (iters < a.maxiters)) {
       double dtc = fmin(dt, a.t1 - t);
       double sse = ros23_cell(M, w, emission ? w.em : nullptr, step_scalars(M, dtc), a.rtol,
-                              a.atol);
+                              a.atol, have_f0, have_p);
+      have_f0 = have_p = true;  // for x; replaced below if x moves
       double EEst = sqrt(sse / (double)nsp);
       if (isnan(EEst)) EEst = 1.0e10;
       double q11 = pow(fmax(EEst, 1.0e-35), a.beta1);
       double q = q11 / pow(qold, a.beta2);
       q = fmax(a.invqmax, fmin(a.invqmin, q / a.gamma));
       if (EEst <= 1.0) {
-        for (int s = 0; s < M.ns; ++s) w.x[s] = a.clamp ? fmax(w.xn[s], 0.0) : w.xn[s];
+        bool same = true;  // the clamp left the candidate as it was: f(x) is f2
+        for (int s = 0; s < M.ns; ++s) {
+          const double xs = a.clamp ? fmax(w.xn[s], 0.0) : w.xn[s];
+          same = same && (__double_as_longlong(xs) == __double_as_longlong(w.xn[s]));
+          w.x[s] = xs;
+        }
+        if (same)
+          for (int s = 0; s < M.ns; ++s) w.f0[s] = w.f2[s];
+        have_f0 = same;
+        have_p = false;
         t = t + dtc;
         bool insteady = (a.qsmin <= q) && (q <= a.qsmax);
         dt = quant_dt(dtc / (insteady ? 1.0 : q));
@@ -278,16 +310,16 @@ __global__ void __launch_bounds__(256) k_chem_per_cell(
 // same bits; rs_autotune times both.  Scalars that all lanes need (pivot reciprocals, the
 // error norm, the controller) are formed redundantly by every lane of the group: this GPU
 // charges an FP64 warp instruction the same time whatever the number of active lanes.
-// Shared memory per cell (doubles): x, xn, f0, k1, f1, k2, b, em, piv, norm terms [ns each],
+// Shared memory per cell (doubles): x, xn, f0, k1, f1, k2, b, em, piv, norm terms, f2 [ns each],
 // rate constants [nr], velocities / partials (never live together) [max(nr, npart)], W [nlu].
 struct GroupOff {
-  int x, xn, f0, k1, f1, k2, b, em, piv, at, kc, pv, w;
+  int x, xn, f0, k1, f1, k2, b, em, piv, at, f2, kc, pv, w;
 };
 __device__ __forceinline__ GroupOff group_off(const DevMech& M) {
   const int n = M.ns;
   GroupOff o;
   o.x = 0; o.xn = n; o.f0 = 2 * n; o.k1 = 3 * n; o.f1 = 4 * n; o.k2 = 5 * n; o.b = 6 * n;
-  o.em = 7 * n; o.piv = 8 * n; o.at = 9 * n; o.kc = 10 * n; o.pv = 10 * n + M.nr;
+  o.em = 7 * n; o.piv = 8 * n; o.at = 9 * n; o.f2 = 10 * n; o.kc = 11 * n; o.pv = 11 * n + M.nr;
   o.w = o.pv + (M.nr > M.npart ? M.nr : M.npart);
   return o;
 }
@@ -368,7 +400,11 @@ template <int G>
 __device__ __forceinline__ void g_lu_factor(const DevMech& M, const Grp<G>& g, double* W,
                                             double* piv) {
   for (int k = 0; k < M.ns; ++k) {
+#if RS_STRICT
     const double pk = 1.0 / W[ldi(M.lu_diag + k)];
+#else
+    const double pk = rcp_nr(W[ldi(M.lu_diag + k)]);
+#endif
     if (g.l == 0) piv[k] = pk;
     const int i1 = ldi(M.elim_ptr + k + 1);
     for (int ii = ldi(M.elim_ptr + k) + g.l; ii < i1; ii += G) {
@@ -423,17 +459,20 @@ __device__ __forceinline__ void g_lu_solve(const DevMech& M, const Grp<G>& g, co
 template <int G>
 __device__ __forceinline__ double ros23_group(const DevMech& M, const Grp<G>& g, double* S,
                                               const GroupOff& o, bool emis,
-                                              const StepScalars& h, double rtol, double atol) {
+                                              const StepScalars& h, double rtol, double atol,
+                                              bool have_f0) {
   const int n = M.ns;
   const double dt = h.dt;
   double *x = S + o.x, *xn = S + o.xn, *f0 = S + o.f0, *k1 = S + o.k1, *f1 = S + o.f1,
-         *k2 = S + o.k2, *b = S + o.b, *piv = S + o.piv, *at = S + o.at, *kc = S + o.kc,
-         *pv = S + o.pv, *W = S + o.w;
+         *k2 = S + o.k2, *b = S + o.b, *piv = S + o.piv, *at = S + o.at, *f2 = S + o.f2,
+         *kc = S + o.kc, *pv = S + o.pv, *W = S + o.w;
   const double* em = emis ? S + o.em : nullptr;
-  g_velocities(M, g, kc, x, pv);
-  g.sync();
-  g_rhs(M, g, pv, em, f0);
-  g.sync();
+  if (!have_f0) {
+    g_velocities(M, g, kc, x, pv);
+    g.sync();
+    g_rhs(M, g, pv, em, f0);
+    g.sync();
+  }
   g_partials(M, g, kc, x, pv);
   g.sync();
   g_build_w(M, g, pv, h.dtgamma, W);
@@ -454,19 +493,17 @@ __device__ __forceinline__ double ros23_group(const DevMech& M, const Grp<G>& g,
   g.sync();
   g_velocities(M, g, kc, xn, pv);
   g.sync();
-  g_rhs(M, g, pv, em, b);  // f2
+  g_rhs(M, g, pv, em, f2);  // f2 = f(unew)
   for (int s = g.l; s < n; s += G) {
     double a = M.ros_c32 * (k2[s] - f1[s]);
     double c = 2.0 * (k1[s] - f0[s]);
-    b[s] = (b[s] - a) - c;
+    b[s] = (f2[s] - a) - c;
   }
   g.sync();
   g_lu_solve(M, g, W, piv, b);  // k3
   for (int s = g.l; s < n; s += G) {
     double ut = h.dto6 * ((k1[s] - 2.0 * k2[s]) + b[s]);
-    double am = fmax(fabs(x[s]), fabs(xn[s]));
-    double den = am * rtol + atol;
-    at[s] = ut / den;
+    at[s] = norm_term(ut, x[s], xn[s], rtol, atol);
   }
   g.sync();
   double acc = 0.0;
@@ -494,6 +531,7 @@ __global__ void __launch_bounds__(128) k_chem_per_cell_group(
   const bool emis = emission != nullptr;
   double my_steps = 0.0, my_attempts = 0.0;
   double t = 0, dt = 0, qold = 0, iters = 0, nacc = 0;
+  bool have_f0 = false;  // S[f0] == f(S[x])
   int c = -1;
   const double tlim = a.t1 - 1.0e-9;
   for (;;) {
@@ -513,18 +551,28 @@ __global__ void __launch_bounds__(128) k_chem_per_cell_group(
       qold = a.qoldinit;
       iters = 0;
       nacc = 0;
+      have_f0 = false;
     }
     if ((t < tlim) && (iters < a.maxiters)) {
       double dtc = fmin(dt, a.t1 - t);
-      double sse = ros23_group(M, g, S, o, emis, step_scalars(M, dtc), a.rtol, a.atol);
+      double sse = ros23_group(M, g, S, o, emis, step_scalars(M, dtc), a.rtol, a.atol, have_f0);
+      have_f0 = true;
       double EEst = sqrt(sse / (double)nsp);
       if (isnan(EEst)) EEst = 1.0e10;
       double q11 = pow(fmax(EEst, 1.0e-35), a.beta1);
       double q = q11 / pow(qold, a.beta2);
       q = fmax(a.invqmax, fmin(a.invqmin, q / a.gamma));
       if (EEst <= 1.0) {
-        for (int s = g.l; s < M.ns; s += G)
-          S[o.x + s] = a.clamp ? fmax(S[o.xn + s], 0.0) : S[o.xn + s];
+        bool same = true;  // the clamp left the candidate as it was: f(x) is f2
+        for (int s = g.l; s < M.ns; s += G) {
+          const double xv = S[o.xn + s];
+          const double xs = a.clamp ? fmax(xv, 0.0) : xv;
+          same = same && (__double_as_longlong(xs) == __double_as_longlong(xv));
+          S[o.x + s] = xs;
+        }
+        have_f0 = __all_sync(g.m, same);
+        if (have_f0)
+          for (int s = g.l; s < M.ns; s += G) S[o.f0 + s] = S[o.f2 + s];
         g.sync();
         t = t + dtc;
         bool insteady = (a.qsmin <= q) && (q <= a.qsmax);
@@ -577,9 +625,14 @@ struct ChemLaunch {
   }
   static void per_cell(const LaunchCtx& L, int nblocks, int threads, double* U,
                        const double* kr, const double* em, double* dtc, double* steps,
-                       unsigned long long* queue, int* status, const PerCellArgs& a) {
-    k_chem_per_cell<MS, MR, MLU, MP><<<nblocks, threads, 0, L.stream>>>(
-        L.mech, L.nc, L.nsp, U, kr, em, dtc, steps, queue, status, a);
+                       unsigned long long* queue, int* status, const PerCellArgs& a,
+                       bool regcap) {
+    if (regcap)
+      k_chem_per_cell<MS, MR, MLU, MP, 8><<<nblocks, threads, 0, L.stream>>>(
+          L.mech, L.nc, L.nsp, U, kr, em, dtc, steps, queue, status, a);
+    else
+      k_chem_per_cell<MS, MR, MLU, MP, 5><<<nblocks, threads, 0, L.stream>>>(
+          L.mech, L.nc, L.nsp, U, kr, em, dtc, steps, queue, status, a);
   }
 };
 
@@ -621,7 +674,7 @@ void launch_block_jac(const LaunchCtx& L, const double* U, const double* kr, con
   else Large::jac(L, U, kr, srow, scol, J);
 }
 int group_cell_doubles(const DevMech& M) {
-  int d = 10 * M.ns + M.nr + (M.nr > M.npart ? M.nr : M.npart) + M.nlu;
+  int d = 11 * M.ns + M.nr + (M.nr > M.npart ? M.nr : M.npart) + M.nlu;
   return d + (d & 1);  // even: 16-byte aligned cells
 }
 template <int G>
@@ -683,16 +736,17 @@ void launch_chem_per_cell_group(const LaunchCtx& L, int G, int nblocks, int thr,
 }
 void launch_chem_per_cell(const LaunchCtx& L, int nblocks, int threads, double* U,
                           const double* kr, const double* em, double* dtc, double* steps,
-                          unsigned long long* queue, int* status, const PerCellArgs& a) {
+                          unsigned long long* queue, int* status, const PerCellArgs& a,
+                          bool regcap) {
   if (L.jit) {
     jit_launch_per_cell(*L.jit, L.stream, L.nc, L.nsp, nblocks, threads, U, kr, em, dtc, steps,
                         queue, status, a);
     return;
   }
   if (L.size_class == 0)
-    Small::per_cell(L, nblocks, threads, U, kr, em, dtc, steps, queue, status, a);
+    Small::per_cell(L, nblocks, threads, U, kr, em, dtc, steps, queue, status, a, regcap);
   else
-    Large::per_cell(L, nblocks, threads, U, kr, em, dtc, steps, queue, status, a);
+    Large::per_cell(L, nblocks, threads, U, kr, em, dtc, steps, queue, status, a, regcap);
 }
 
 }  // namespace rs

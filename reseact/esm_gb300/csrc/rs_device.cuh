@@ -127,6 +127,32 @@ struct Ctl {
 __device__ __forceinline__ double ld(const double* p) { return __ldg(p); }
 __device__ __forceinline__ int ldi(const int* p) { return __ldg(p); }
 
+// Reciprocal from the hardware approximation r (PTX rcp.approx.ftz.f64) by one third-order
+// correction: with e = 1 - d r, 1/d = r / (1 - e) = r (1 + e + e^2 + ...), so r (1 + e + e^2)
+// leaves e^3 -- below an ulp for the approximation's |e| -- in three FMAs (two Newton steps
+// take four).  The production build uses it where d > 0 and normal (LU pivots, m, error-norm
+// denominators >= atol).
+__device__ __forceinline__ double rcp_nr(double d) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(d));
+  const double e = fma(-d, r, 1.0);
+  return fma(r, fma(e, e, e), r);
+}
+
+// One Newton step (relative error ~1e-12 or better) and max(|a|, |b|) on the magnitude bits:
+// the production build's forms for error-norm terms, whose only use is the step-size controller.
+__device__ __forceinline__ double rcp_nr1(double d) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(d));
+  return fma(r, fma(-d, r, 1.0), r);
+}
+__device__ __forceinline__ double amax_bits(double a, double b) {  // on 32-bit halves
+  const unsigned ha = (unsigned)__double2hiint(a) & 0x7fffffffu, la = (unsigned)__double2loint(a);
+  const unsigned hb = (unsigned)__double2hiint(b) & 0x7fffffffu, lb = (unsigned)__double2loint(b);
+  const bool bl = ha < hb || (ha == hb && la < lb);
+  return __hiloint2double((int)(bl ? hb : ha), (int)(bl ? lb : la));
+}
+
 // ------------------------------------------------------------------ chemistry core
 // v_r = k_r * prod x^nu over the reactant entries, in table order
 __device__ __forceinline__ void velocities(const DevMech& M, const double* k, const double* x,
@@ -194,11 +220,16 @@ __device__ __forceinline__ void build_w(const DevMech& M, const double* P, doubl
 }
 
 // Pivot-free sparse LU in elimination order (natural, as blocksolve, in the strict build; zero
-// updates skipped); L multipliers overwrite their slots, piv[k] = 1 / U[k,k] for pivot k.
+// updates skipped); L multipliers overwrite their slots, piv[k] = 1 / U[k,k] for pivot k (the
+// production build's reciprocal rcp_nr).
 __device__ __forceinline__ void lu_factor(const DevMech& M, double* W, double* piv) {
   int m = 0;
   for (int k = 0; k < M.ns; ++k) {
+#if RS_STRICT
     double pk = 1.0 / W[ldi(M.lu_diag + k)];
+#else
+    double pk = rcp_nr(W[ldi(M.lu_diag + k)]);  // within 2 ulp of 1/U_kk
+#endif
     piv[k] = pk;
     int i1 = ldi(M.elim_ptr + k + 1);
     for (int ii = ldi(M.elim_ptr + k); ii < i1; ++ii, ++m) {
@@ -242,32 +273,6 @@ __device__ __forceinline__ void lu_solve(const DevMech& M, const double* W, cons
     b[si] = acc * piv[i];
 #endif
   }
-}
-
-// Reciprocal from the hardware approximation r (PTX rcp.approx.ftz.f64) by one third-order
-// correction: with e = 1 - d r, 1/d = r / (1 - e) = r (1 + e + e^2 + ...), so r (1 + e + e^2)
-// leaves e^3 -- below an ulp for the approximation's |e| -- in three FMAs (two Newton steps
-// take four).  The production build uses it where d > 0 and normal (LU pivots, m, error-norm
-// denominators >= atol).
-__device__ __forceinline__ double rcp_nr(double d) {
-  double r;
-  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(d));
-  const double e = fma(-d, r, 1.0);
-  return fma(r, fma(e, e, e), r);
-}
-
-// One Newton step (relative error ~1e-12 or better) and max(|a|, |b|) on the magnitude bits:
-// the production build's forms for error-norm terms, whose only use is the step-size controller.
-__device__ __forceinline__ double rcp_nr1(double d) {
-  double r;
-  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(d));
-  return fma(r, fma(-d, r, 1.0), r);
-}
-__device__ __forceinline__ double amax_bits(double a, double b) {  // on 32-bit halves
-  const unsigned ha = (unsigned)__double2hiint(a) & 0x7fffffffu, la = (unsigned)__double2loint(a);
-  const unsigned hb = (unsigned)__double2hiint(b) & 0x7fffffffu, lb = (unsigned)__double2loint(b);
-  const bool bl = ha < hb || (ha == hb && la < lb);
-  return __hiloint2double((int)(bl ? hb : ha), (int)(bl ? lb : la));
 }
 
 // ------------------------------------------------------------------ integer-pipe FP64 helpers

@@ -120,9 +120,11 @@ void launch_chem_rhs(const LaunchCtx& L, const double* U, const double* kr, cons
                      double* dU);
 void launch_block_jac(const LaunchCtx& L, const double* U, const double* kr, const int* srow,
                       const int* scol, double* J);
+// regcap: the form capped at 32 registers (2048 resident threads per SM)
 void launch_chem_per_cell(const LaunchCtx& L, int nblocks, int threads, double* U,
                           const double* kr, const double* em, double* dtc, double* steps,
-                          unsigned long long* queue, int* status, const PerCellArgs& a);
+                          unsigned long long* queue, int* status, const PerCellArgs& a,
+                          bool regcap = false);
 // the per-cell form with G lanes per cell (G = 4, 8, 16; table mechanisms, minimum-fill order):
 // doubles of shared memory per cell, the threads per block that fit (0: none), resident blocks
 // per SM, and the launch

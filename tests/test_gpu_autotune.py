@@ -57,7 +57,8 @@ def test_autotune_per_cell_is_bitwise_neutral():
     w = workloads.c3(ncells=8192)
     ref, _ = _run(w, False, steps=1)
     got, rep = _run(w, True, steps=1)
-    # 3 x 4 thread-per-cell shapes, then 4 / 8 / 16 lanes per cell (shared-memory work arrays)
-    assert "per_cell_choice" in rep and len(rep["per_cell"]) == 15
+    # 3 x 4 thread-per-cell shapes, 2 capped at 32 registers, then 4 / 8 / 16 lanes per cell
+    # (shared-memory work arrays)
+    assert "per_cell_choice" in rep and len(rep["per_cell"]) == 17
     assert sorted(c["group"] for c in rep["per_cell"] if "group" in c) == [4, 8, 16]
     assert np.array_equal(ref, got)

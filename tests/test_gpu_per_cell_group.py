@@ -1,7 +1,8 @@
-"""Per-cell adaptive chemistry with G lanes per cell (work arrays in shared memory) against the
-thread-per-cell kernel: the same operations in the same order, so the same bits -- states,
-accepted and attempted step counts -- for every G, with and without emissions and the clamp,
-on the large synthetic mechanism and on SuperFast's table kernels."""
+"""Per-cell adaptive chemistry with G lanes per cell (work arrays in shared memory), and the
+thread-per-cell kernel capped at 32 registers, against the thread-per-cell kernel: the same
+operations in the same order, so the same bits -- states, accepted and attempted step counts --
+for every G, with and without emissions and the clamp, on the large synthetic mechanism and on
+SuperFast's table kernels."""
 import numpy as np
 import pytest
 
@@ -59,6 +60,22 @@ def test_group_kernel_superfast_tables(group):
     rc0, ref, n0 = _window(w, 0, kind=CHEM_KERNEL_TABLE, **kw)
     rc1, got, n1 = _window(w, group, kind=CHEM_KERNEL_TABLE, **kw)
     assert rc0 == rc1 == 0 and n0 == n1
+    assert np.array_equal(ref, got)
+
+
+@pytest.mark.parametrize("threads", [128, 256])
+def test_register_capped_kernel_matches(threads):
+    """The thread-per-cell kernel capped at 32 registers (2048 resident threads per SM)."""
+    w = workloads.c3(ncells=4096)
+    rc0, ref, n0 = _window(w, 0)
+    s = Solver.for_workload(w)
+    s.set_launch_shape(per_cell_threads=threads, per_cell_blocks_per_sm=2048 // threads,
+                       per_cell_regcap=1)
+    s.set_state(w.u0_cellmajor())
+    rc1, _, _, st = s.macro_step(0.0, 600.0, 1.0, w.dt0_C, check=False)
+    got = s.get_state()
+    s.close()
+    assert rc0 == rc1 == 0 and n0 == (st.naC, st.nrC)
     assert np.array_equal(ref, got)
 
 
