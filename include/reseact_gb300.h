@@ -251,7 +251,9 @@ rs_status rs_autotune(rs_handle* h, char* buf, size_t buf_len);
  * "mixed_x_bulk", "mixed_yz_bulk" (mixed pencils); "mixed_x_stream", "mixed_yz_stream" (1: the
  * streaming forms of the mixed kernels instead of the pencils); "per_cell_threads",
  * "per_cell_blocks_per_sm", "per_cell_group" (per-cell chemistry; group 0 = one thread per
- * cell, 4 / 8 / 16 = lanes per cell, production build only).  Values outside a key's
+ * cell, 4 / 8 / 16 = lanes per cell, production build only), "per_cell_regcap" (1: the
+ * table-walking per-cell kernel at 32 registers); "chem_attempt_variant" (0 "regs", 1 "smem",
+ * 2 "regs2", 3 "split": how the specialised attempt kernel keeps W, where built).  Values outside a key's
  * candidates are RS_ERR_INVALID.  Every shape gives bit-identical results. */
 rs_status rs_set_launch_shape(rs_handle* h, const char* key, int32_t value);
 

@@ -2007,11 +2007,11 @@ extern "C" rs_status rs_get_chem_kernel(rs_handle* h, int32_t* kind, char* info,
       char line[768];
       if (h->jit)
         std::snprintf(line, sizeof line,
-                      "{\"kind\": \"%s\", \"variant\": \"%s\", \"regs\": [%d, %d, %d], "
-                      "\"smem_bytes\": %zu, \"compile_ms\": %.1f}",
+                      "{\"kind\": \"%s\", \"variant\": \"%s\", \"regs\": [%d, %d, %d, %d], "
+                      "\"smem_bytes\": %zu, \"split_smem_bytes\": %zu, \"compile_ms\": %.1f}",
                       spec ? "specialized" : "table", rs::kJitVariantNames[h->jit->variant],
-                      h->jit->regs[0], h->jit->regs[1], h->jit->regs[2], h->jit->attempt_smem,
-                      h->jit->compile_ms);
+                      h->jit->regs[0], h->jit->regs[1], h->jit->regs[2], h->jit->regs[3],
+                      h->jit->attempt_smem[1], h->jit->attempt_smem[3], h->jit->compile_ms);
       else
         std::snprintf(line, sizeof line, "{\"kind\": \"table\", \"why\": \"%.600s\"}", why.c_str());
       std::strncpy(info, line, info_len - 1);
@@ -2050,6 +2050,10 @@ extern "C" rs_status rs_set_launch_shape(rs_handle* h, const char* key, int32_t 
     else if (k == "per_cell_threads") ok = in({64, 128, 256}) && (t.pc_threads = value, true);
     else if (k == "per_cell_blocks_per_sm") ok = in({1, 2, 4, 8, 16}) && (t.pc_blocks_per_sm = value, true);
     else if (k == "per_cell_regcap") ok = in({0, 1}) && (t.pc_regcap = value, true);
+    else if (k == "chem_attempt_variant") {  // the specialised attempt kernel's variant
+      ok = value >= 0 && value < rs::kJitVariants && h->jit && h->jit->attempt[value][0];
+      if (ok) h->jit->variant = value;
+    }
     else if (k == "per_cell_group") {
       // G lanes per cell: the production build's (minimum-fill, descending back substitution)
       // table-walking kernels only, and only where a block of them fits in shared memory

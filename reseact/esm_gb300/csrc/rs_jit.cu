@@ -98,6 +98,13 @@ constexpr int kBlock = 256;
 constexpr size_t kSmemCap = 227 * 1024 - kBlock * sizeof(double);
 
 size_t smem_bytes(const MechTables& T) { return (size_t)T.nlu * kBlock * sizeof(double); }
+// "split" variant: the last split_slots(T) LU slots of W in shared memory, the others in
+// registers, two 256-thread blocks per SM (each block's shared part within half an SM's
+// 228 KB, its static reduction array and the per-block reserve included)
+int split_slots(const MechTables& T) {
+  const int cap = (int)((113 * 1024 - 3 * 1024) / (kBlock * sizeof(double)));  // 55
+  return T.nlu >= 16 ? (T.nlu < cap ? T.nlu : cap) : 0;
+}
 
 struct Gen {
   const MechTables& T;
@@ -444,12 +451,14 @@ __device__ __forceinline__ double tree256(double v, double* sm) {
 
 std::string generate(const MechTables& T, double ros_d, double ros_c32, bool strict,
                      bool with_smem) {
+  const int nsplit = split_slots(T);
   Gen g{T, strict, {}};
   auto& o = g.o;
   o << "// generated: " << T.ns << " species, " << T.nr << " reactions, " << T.nlu
     << " LU slots\n";
   o << "#define NS " << T.ns << "\n#define NRA " << (T.nr > 0 ? T.nr : 1) << "\n#define NPA "
-    << (T.npart > 0 ? T.npart : 1) << "\n#define NLU " << T.nlu << "\n";
+    << (T.npart > 0 ? T.npart : 1) << "\n#define NLU " << T.nlu << "\n#define NLU_R "
+    << (T.nlu - nsplit) << "  // LU slots in registers in the split variant\n";
   o << "#define ROS_D " << lit(ros_d) << "\n#define ROS_C32 " << lit(ros_c32) << "\n";
   o << "#define OFF_DONE " << offsetof(Ctl, done) << "\n#define OFF_CUR " << offsetof(Ctl, cur)
     << "\n#define OFF_DTC " << offsetof(Ctl, dtc) << "\n#define OFF_DTO2 "
@@ -485,16 +494,19 @@ __device__ __forceinline__ double* stage_slot(const unsigned char* __restrict__ 
   const int slot = (int)*(const double*)(ctl + OFF_NACC);
   return (kz && slot >= 0 && slot < cap) ? kz + (u64)slot * 2 * NS * N : nullptr;
 }
-// SOL: the step's solution only (a replay along recorded accepted steps needs no error norm)
-template <bool HE, int WS, bool KEEP, bool SOL = false>
+// SOL: the step's solution only (a replay along recorded accepted steps needs no error norm).
+// W storage: LU slots e < KR in the register array W, the others in shared memory at
+// WSM[(e - KR) * 256] (this thread's column of a [slot][thread] array); every slot index is a
+// compile-time constant, so each access resolves to one of the two when compiled.
+template <bool HE, int KR, bool KEEP, bool SOL = false>
 __device__ __forceinline__ double ros23_cell(const double* __restrict__ kr,
     const double* __restrict__ em, u64 N, int c, const double* x, double* xn, double* W,
-    double* f0, bool have_f0, double* __restrict__ fout, int clamp, double* f2,
+    double* WSM, double* f0, bool have_f0, double* __restrict__ fout, int clamp, double* f2,
     double dt, double dto2, double dto6, double dtg, double rtol, double atol,
     double* __restrict__ kzo) {
 #define K(r) __ldg(kr + (u64)(r) * N + c)
 #define EM(s) __ldg(em + (u64)(s) * N + c)
-#define WV(e) W[(e) * WS]
+#define WV(e) (*((e) < KR ? &W[(e)] : &WSM[((e) - KR) * 256]))
   RS_VDECL
   double P[NPA], k1[NS], f1[NS], k2[NS], b[NS], pv[NS];
   if (!have_f0) {
@@ -567,7 +579,8 @@ __device__ __forceinline__ double ros23_cell(const double* __restrict__ kr,
 // F0/F1 (may be null) pair with U0/U1: F[cur] holds f(U[cur]) per cell (NaN in plane 0 where
 // unknown); from the second attempt of a solve on, a cell reuses it instead of evaluating
 // f(x) again (the first attempt of a solve starts from a state written elsewhere).
-template <bool HE, bool SMEM>
+// MODE 0: W in registers; 1: W in shared memory; 2: split (NLU_R slots in registers)
+template <bool HE, int MODE>
 __device__ __forceinline__ void attempt_body(const unsigned char* __restrict__ ctl,
     double* __restrict__ U0, double* __restrict__ U1, const double* __restrict__ kr,
     const double* __restrict__ em, double* __restrict__ partial, int nc, int nsp,
@@ -598,15 +611,22 @@ __device__ __forceinline__ void attempt_body(const unsigned char* __restrict__ c
       for (int s = 0; s < NS; ++s) f0[s] = Fin[(u64)s * N + c];
       have = f0[0] == f0[0];
     }
-    if constexpr (SMEM) {
+    if constexpr (MODE == 1) {
       extern __shared__ double wsm[];
-      e = ros23_cell<HE, 256, false>(kr, em, N, c, x, xn, wsm + threadIdx.x, f0, have,
-                                     F0 ? Fout : nullptr, clamp, nullptr, dt, dto2, dto6, dtg,
-                                     rtol, atol, kzo);
+      e = ros23_cell<HE, 0, false>(kr, em, N, c, x, xn, nullptr, wsm + threadIdx.x, f0, have,
+                                   F0 ? Fout : nullptr, clamp, nullptr, dt, dto2, dto6, dtg,
+                                   rtol, atol, kzo);
+    } else if constexpr (MODE == 2) {
+      extern __shared__ double wsm[];
+      double W[NLU_R > 0 ? NLU_R : 1];
+      e = ros23_cell<HE, NLU_R, false>(kr, em, N, c, x, xn, W, wsm + threadIdx.x, f0, have,
+                                       F0 ? Fout : nullptr, clamp, nullptr, dt, dto2, dto6,
+                                       dtg, rtol, atol, kzo);
     } else {
       double W[NLU];
-      e = ros23_cell<HE, 1, false>(kr, em, N, c, x, xn, W, f0, have, F0 ? Fout : nullptr,
-                                   clamp, nullptr, dt, dto2, dto6, dtg, rtol, atol, kzo);
+      e = ros23_cell<HE, NLU, false>(kr, em, N, c, x, xn, W, nullptr, f0, have,
+                                     F0 ? Fout : nullptr, clamp, nullptr, dt, dto2, dto6, dtg,
+                                     rtol, atol, kzo);
     }
     if (F0 && !have) {  // keep f(x) for a retry of this state after a rejection
 #pragma unroll
@@ -653,7 +673,7 @@ __device__ __forceinline__ void per_cell_body(int nc, int nsp, double* __restric
     }
     if ((t < tlim) && (iters < a.maxiters)) {
       const double dtc = fmin(dt, a.t1 - t);
-      const double sse = ros23_cell<HE, 1, true>(kr, em, N, c, x, xn, W, f0, have, nullptr,
+      const double sse = ros23_cell<HE, NLU, true>(kr, em, N, c, x, xn, W, nullptr, f0, have, nullptr,
                                                  a.clamp, f2, dtc, dtc / 2, dtc / 6,
                                                  dtc * ROS_D, a.rtol, a.atol, nullptr);
       have = true;  // f0 == f(x) after the call; replaced below if x moves
@@ -701,20 +721,20 @@ __device__ __forceinline__ void per_cell_body(int nc, int nsp, double* __restric
   }
 }
 
-#define RS_ATTEMPT(NAME, HE, SMEM, MINB)                                                    \
+#define RS_ATTEMPT(NAME, HE, MODE, MINB)                                                    \
   extern "C" __global__ void __launch_bounds__(256, MINB) NAME(                             \
       const unsigned char* __restrict__ ctl, double* __restrict__ U0,                       \
       double* __restrict__ U1, const double* __restrict__ kr,                               \
       const double* __restrict__ em, double* __restrict__ partial, int nc, int nsp,         \
       double rtol, double atol, int clamp, double* __restrict__ F0,                         \
       double* __restrict__ F1) {                                                            \
-    attempt_body<HE, SMEM>(ctl, U0, U1, kr, em, partial, nc, nsp, rtol, atol, clamp, F0,    \
+    attempt_body<HE, MODE>(ctl, U0, U1, kr, em, partial, nc, nsp, rtol, atol, clamp, F0,    \
                            F1);                                                             \
   }
-RS_ATTEMPT(rs_jit_attempt_r0, false, false, 1)
-RS_ATTEMPT(rs_jit_attempt_r1, true, false, 1)
-RS_ATTEMPT(rs_jit_attempt_q0, false, false, 2)
-RS_ATTEMPT(rs_jit_attempt_q1, true, false, 2)
+RS_ATTEMPT(rs_jit_attempt_r0, false, 0, 1)
+RS_ATTEMPT(rs_jit_attempt_r1, true, 0, 1)
+RS_ATTEMPT(rs_jit_attempt_q0, false, 0, 2)
+RS_ATTEMPT(rs_jit_attempt_q1, true, 0, 2)
 
 // one accepted step at the controller's dtc without the error estimate: the attempt's own
 // arithmetic up to the new state (the same bits), for the fixed-sequence replay of a recorded
@@ -736,7 +756,7 @@ __device__ __forceinline__ void step_body(const unsigned char* __restrict__ ctl,
   double x[NS], xn[NS], f0[NS], W[NLU];
 #pragma unroll
   for (int s = 0; s < NS; ++s) x[s] = U[(u64)s * N + c];
-  ros23_cell<HE, 1, false, true>(kr, em, N, c, x, xn, W, f0, false, nullptr, clamp, nullptr,
+  ros23_cell<HE, NLU, false, true>(kr, em, N, c, x, xn, W, nullptr, f0, false, nullptr, clamp, nullptr,
                                  dt, dto2, 0.0, dtg, 0.0, 0.0, stage_slot(ctl, N));
 #pragma unroll
   for (int s = 0; s < NS; ++s) Un[(u64)s * N + c] = clamp ? fmax(xn[s], 0.0) : xn[s];
@@ -756,7 +776,9 @@ RS_STEP(rs_jit_step_0, false)
 RS_STEP(rs_jit_step_1, true)
 )";
   if (with_smem)
-    o << "RS_ATTEMPT(rs_jit_attempt_s0, false, true, 1)\nRS_ATTEMPT(rs_jit_attempt_s1, true, true, 1)\n";
+    o << "RS_ATTEMPT(rs_jit_attempt_s0, false, 1, 1)\nRS_ATTEMPT(rs_jit_attempt_s1, true, 1, 1)\n";
+  if (nsplit > 0)
+    o << "RS_ATTEMPT(rs_jit_attempt_h0, false, 2, 2)\nRS_ATTEMPT(rs_jit_attempt_h1, true, 2, 2)\n";
   o << R"(
 #define RS_PER_CELL(NAME, HE)                                                                \
   extern "C" __global__ void __launch_bounds__(256) NAME(int nc, int nsp,                   \
@@ -955,7 +977,7 @@ bool compile_and_load(const std::string& src, bool strict, Compiled* out, std::s
 
 }  // namespace
 
-const char* const kJitVariantNames[kJitVariants] = {"regs", "smem", "regs2"};
+const char* const kJitVariantNames[kJitVariants] = {"regs", "smem", "regs2", "split"};
 
 bool jit_chem_eligible(const MechTables& T) {
   return T.ns >= 1 && T.ns <= 32 && T.nlu <= 256 && T.nr <= 160 && T.npart <= 320;
@@ -1004,21 +1026,29 @@ std::shared_ptr<JitChem> jit_chem_build(const MechTables& T, double ros_d, doubl
             get(&J->step[1], "rs_jit_step_1") && get(&J->vjpk[0], "rs_jit_vjpk_0") &&
             get(&J->vjpk[1], "rs_jit_vjpk_1");
   if (!ok) return nullptr;
-  if (with_smem && get(&J->attempt[1][0], "rs_jit_attempt_s0") &&
-      get(&J->attempt[1][1], "rs_jit_attempt_s1")) {
-    J->attempt_smem = smem_bytes(T);
+  // the shared-memory variants: their dynamic shared memory, or dropped where it cannot be set
+  auto shared_variant = [&](int v, const char* n0, const char* n1, size_t bytes) {
+    if (!get(&J->attempt[v][0], n0) || !get(&J->attempt[v][1], n1)) {
+      J->attempt[v][0] = J->attempt[v][1] = nullptr;
+      return;
+    }
+    J->attempt_smem[v] = bytes;
     for (int he = 0; he < 2; ++he) {
-      cudaError_t e = cudaFuncSetAttribute((const void*)J->attempt[1][he],
+      cudaError_t e = cudaFuncSetAttribute((const void*)J->attempt[v][he],
                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)J->attempt_smem);
-      if (e != cudaSuccess) {  // keep the register variant only
+                                           (int)bytes);
+      if (e != cudaSuccess) {
         cudaGetLastError();
-        J->attempt[1][0] = J->attempt[1][1] = nullptr;
-        J->attempt_smem = 0;
-        break;
+        J->attempt[v][0] = J->attempt[v][1] = nullptr;
+        J->attempt_smem[v] = 0;
+        return;
       }
     }
-  }
+  };
+  if (with_smem) shared_variant(1, "rs_jit_attempt_s0", "rs_jit_attempt_s1", smem_bytes(T));
+  if (split_slots(T) > 0)
+    shared_variant(3, "rs_jit_attempt_h0", "rs_jit_attempt_h1",
+                   (size_t)split_slots(T) * kBlock * sizeof(double));
   for (int v = 0; v < kJitVariants; ++v) {
     cudaFuncAttributes fa{};
     if (J->attempt[v][0] && cudaFuncGetAttributes(&fa, (const void*)J->attempt[v][0]) == cudaSuccess)
@@ -1035,13 +1065,12 @@ void jit_launch_attempt(const JitChem& J, cudaStream_t st, int nc, int nsp, cons
                         double* part, double rtol, double atol, int clamp, double* F0,
                         double* F1) {
   const int v = J.attempt[J.variant][0] ? J.variant : 0;
-  const int sm = v == 1;
   cudaKernel_t k = J.attempt[v][em ? 1 : 0];
   const unsigned char* c = reinterpret_cast<const unsigned char*>(ctl);
   if (!F0 || !F1) F0 = F1 = nullptr;
   void* args[] = {&c, &U0, &U1, &kr, &em, &part, &nc, &nsp, &rtol, &atol, &clamp, &F0, &F1};
   int nb = (nc + kBlock - 1) / kBlock;
-  cudaLaunchKernel((const void*)k, dim3(nb), dim3(kBlock), args, sm ? J.attempt_smem : 0, st);
+  cudaLaunchKernel((const void*)k, dim3(nb), dim3(kBlock), args, J.attempt_smem[v], st);
 }
 
 void jit_launch_step(const JitChem& J, cudaStream_t st, int nc, int nsp, const Ctl* ctl,

@@ -25,7 +25,9 @@ struct PerCellArgs;
 //   0 "regs"   W in registers (spilled by ptxas where needed), one 256-thread block per SM
 //   1 "smem"   W in dynamic shared memory, [slot][thread] so a warp's accesses are contiguous
 //   2 "regs2"  as 0 but capped at 128 registers for two blocks per SM
-constexpr int kJitVariants = 3;
+//   3 "split"  the last half of W's LU slots (at most 55) in shared memory, the rest in
+//              registers, capped at 128 registers for two blocks per SM
+constexpr int kJitVariants = 4;
 extern const char* const kJitVariantNames[kJitVariants];
 
 struct JitChem {
@@ -35,10 +37,10 @@ struct JitChem {
   cudaKernel_t vjp[2] = {};                    // ROS23 step VJP [has emission]
   cudaKernel_t step[2] = {};                   // accepted step, no error estimate [has emission]
   cudaKernel_t vjpk[2] = {};                   // step VJP reading k1, z2 from the stage tape
-  size_t attempt_smem = 0;  // dynamic shared bytes of the shared-memory variant
+  size_t attempt_smem[kJitVariants] = {};  // dynamic shared bytes of each attempt variant
   int variant = 0;          // variant used for global-dt attempts
   double compile_ms = 0;    // NVRTC time (0 when the compiled image came from cache)
-  int regs[kJitVariants] = {0, 0, 0};  // registers per thread of each attempt variant
+  int regs[kJitVariants] = {};  // registers per thread of each attempt variant
 };
 
 // True when the mechanism is small enough for straight-line code (all work arrays of one

@@ -141,8 +141,8 @@ def test_autotuned_chemistry_variant_is_bitwise_neutral():
         s.set_state(w.u0_cellmajor())
         rep = s.autotune() if tune else None
         if tune:
-            assert rep["chem_choice"] in ("regs", "smem", "regs2")
-            assert len(rep["chem_attempt"]) == 3
+            assert rep["chem_choice"] in ("regs", "smem", "regs2", "split")
+            assert len(rep["chem_attempt"]) == 4
         t, a, b = 0.0, 15.0, 0.5
         for _ in range(2):
             _, a, b, _ = s.macro_step(t, t + 600.0, a, b)
@@ -150,6 +150,27 @@ def test_autotuned_chemistry_variant_is_bitwise_neutral():
         res.append(s.get_state())
         s.close()
     assert np.array_equal(res[0], res[1])
+
+
+@pytest.mark.parametrize("strict", [False, True])
+def test_every_attempt_variant_gives_the_same_bits(strict):
+    """W in registers, in shared memory, capped at 128 registers, or split between shared
+    memory and registers: the same generated arithmetic, so the same bits after adaptive
+    macro steps."""
+    w = _small_c2(emission=True)
+    res = []
+    for v in range(4):
+        s = Solver.for_workload(w, strict=strict)
+        s.set_launch_shape(chem_attempt_variant=v)
+        s.set_state(w.u0_cellmajor())
+        t, a, b = 0.0, 15.0, 0.5
+        for _ in range(2):
+            _, a, b, _ = s.macro_step(t, t + 600.0, a, b)
+            t += 600.0
+        res.append(s.get_state())
+        s.close()
+    for r in res[1:]:
+        assert np.array_equal(res[0], r)
 
 
 def test_production_reciprocal_within_two_ulp():
