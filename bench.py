@@ -458,11 +458,12 @@ def run_gb300(args):
         roofline = {"kernel": "ros23 attempt (%s, %s)" % (kinfo.get("kind"), kinfo.get("variant", "-")),
                     "bound": "fp64", "achieved": round(achieved, 4),
                     "peak": peak, "unit": "TFLOP/s", "frac": round(achieved / peak, 4) if peak else None,
-                    # DRAM bytes per launch from one ncu capture of this kernel on this
-                    # workload (dram__bytes_read.sum + dram__bytes_write.sum: 302.1 MB + 1055.1 MB,
-                    # mostly the 128-register variant's spill stores); null for other kernels
-                    "traffic": (1357.2e6 if (kinfo.get("kind") == "specialized" and not args.small
-                                             and kinfo.get("variant") == "regs2") else None),
+                    # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
+                    # one ncu capture of each variant's first launch on this workload: the
+                    # 128-register variant 235.7 + 606.6 MB (mostly spill stores), the split
+                    # variant (part of W in shared memory) 204.5 + 265.1 MB; null otherwise
+                    "traffic": ({"regs2": 842.4e6, "split": 469.6e6}.get(kinfo.get("variant"))
+                                if (kinfo.get("kind") == "specialized" and not args.small) else None),
                     "traffic_source": "ncu capture summarised in profiles/rs_jit_attempt_c2_144x91x47.md",
                     "flops_per_cell_attempt": round(f_exec, 1),
                     # FP64 issue: instructions / (peak flops / 2 per FMA instruction); the flop

@@ -62,9 +62,12 @@ def test_transport_rhs_with_pbl(oracle_mod, strict):
             assert err.max() < 1e-12, err.max()
 
 
-def test_macro_steps_with_pbl(oracle_mod):
+@pytest.mark.parametrize("precision", [abi.RS_PREC_FP64, abi.RS_PREC_MIXED])
+def test_macro_steps_with_pbl(oracle_mod, precision):
+    """FP64 and the compensated FP32 transport (whose stage kernel forms the tendency with the
+    PBL term in FP64 from the pair accumulator) against the FP64 oracle."""
     w = _w(tau=900.0)
-    s, o = _pair(w, oracle_mod)
+    s, o = _pair(w, oracle_mod, precision=precision)
     s.set_state(w.u0_cellmajor())
     u = np.ascontiguousarray(w.u0.copy())
     a_g = a_o = 15.0

@@ -58,9 +58,12 @@ def test_transport_rhs_with_fixer(oracle_mod, strict):
     assert (np.abs(dm - want) / np.asarray(f["dp"])).max() < 1e-17
 
 
-def test_macro_steps_with_fixer(oracle_mod):
+@pytest.mark.parametrize("precision", [abi.RS_PREC_FP64, abi.RS_PREC_MIXED])
+def test_macro_steps_with_fixer(oracle_mod, precision):
+    """FP64 and the compensated FP32 transport (face fluxes, the diagnosed Mz included, as
+    float pairs; the air-mass row and its fixer correction in FP64) against the FP64 oracle."""
     w = _w()
-    s, o = _pair(w, oracle_mod)
+    s, o = _pair(w, oracle_mod, precision=precision)
     s.set_state(w.u0_cellmajor())
     u = np.ascontiguousarray(w.u0.copy())
     a_g = a_o = 15.0
