@@ -691,6 +691,22 @@ def measure_c5(local, barrier, steps=1):
         out[name]["speedup_vs_fp64"] = round(out["fp64"]["ms_per_step"] / out[name]["ms_per_step"], 3)
     out["transport_mixed"]["speedup_vs_transport_fp64"] = round(
         out["transport_fp64"]["ms_per_step"] / out["transport_mixed"]["ms_per_step"], 3)
+    # HBM roofline of the transport attempts: compulsory bytes per cell-attempt against the
+    # measured copy bandwidth -- the state read and written once plus three face-flux fields,
+    # 2*S*8 + 3*8 = 520 B as this build keeps the state (FP64 in HBM, the FP32 pairs formed on
+    # chip), and the 2*S*4 + 3*4 = 260 B of an FP32 state
+    hbm = measured_peaks().get("hbm_gbs")
+    for name in ("transport_fp64", "transport_mixed"):
+        n_att = sum(c[0] + c[1] for c in out[name]["attempts"])
+        if n_att > 0:
+            t_att = out[name]["ms_per_step"] * steps / n_att * 1e-3
+            for label, per_cell in (("fp64_state", transport_bytes_per_cell(w.nsp)),
+                                    ("fp32_state", 2 * w.nsp * 4 + 3 * 4)):
+                gbs = per_cell * w.ncells / t_att / 1e9
+                out[name]["hbm_" + label] = {
+                    "bytes_per_cell_attempt": per_cell, "achieved_gbs": round(gbs, 1),
+                    "frac": round(gbs / hbm, 4) if hbm else None}
+            out[name]["ms_per_attempt"] = round(t_att * 1e3, 3)
     nsp = w.nsp
     out["errors"] = {
         # the precision change alone: same method, compensated FP32 vs FP64 transport
