@@ -606,9 +606,16 @@ __device__ __forceinline__ df df_two_sum(float a, float b) {  // a + b = s + e e
   const float s = a + b, bb = s - a;
   return {s, (a - (s - bb)) + (b - bb)};
 }
+// Sum of pairs: TwoSum of the high parts, the low parts added to its error, then the fast
+// renormalisation (h = s + e, l = e - (h - s)).  The renormalisation is exact unless the high
+// parts cancel below the low parts; its error is then below 2^-46 max(|a|, |b|), a few times
+// the operands' own representation error, so the sum keeps the pairs' accuracy at 11
+// operations instead of the 14 of a second TwoSum.
 __device__ __forceinline__ df df_add(df a, df b) {
   const df s = df_two_sum(a.h, b.h);
-  return df_two_sum(s.h, s.l + (a.l + b.l));
+  const float e = s.l + (a.l + b.l);
+  const float h = s.h + e;
+  return {h, e - (h - s.h)};
 }
 __device__ __forceinline__ df df_neg(df a) { return {-a.h, -a.l}; }
 __device__ __forceinline__ df df_sub(df a, df b) { return df_add(a, df_neg(b)); }
