@@ -1390,9 +1390,21 @@ __global__ void __launch_bounds__(kRedThreads) k_split_input(DevTransport<double
   } else {
     U = Qd;
   }
-  size_t n = (size_t)T.ntr * T.nlon * T.nlat * T.nlev;
-  size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (x < n) split_store(T, x, U[x]);
+  // four elements per thread, a block's 4 x 256 consecutive values: the loads go out
+  // together
+  const size_t n = (size_t)T.ntr * T.nlon * T.nlat * T.nlev;
+  const size_t x0 = (size_t)blockIdx.x * (4 * blockDim.x) + threadIdx.x;
+  double v[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const size_t x = x0 + (size_t)r * blockDim.x;
+    v[r] = x < n ? U[x] : 0.0;
+  }
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const size_t x = x0 + (size_t)r * blockDim.x;
+    if (x < n) split_store(T, x, v[r]);
+  }
 }
 // Divergence of the air-mass flux at cell (i,j,k) at time factor g.
 struct CellGeo {
@@ -1714,31 +1726,30 @@ __global__ void __launch_bounds__(kRedThreads) k_stage_mixed(DevTransport<double
       e = fma(at, at, e);
       Un[xm] = (clamp && __double2hiint(mn) < 0) ? 0.0 : mn;
     }
-    for (int s = 0; s < T.ntr; ++s) {
-      const size_t x = (size_t)s * nc + c;
-      const df q{T.qhi[x], T.qlo[x]};
+    // one tracer from its loaded inputs (q, the accumulator, and for stages 3-4 the attempt's
+    // input u0 and stage 4's u3); the norm terms are added in tracer order
+    auto tracer = [&](int s, size_t x, df q, float2 a, double u0, float2 u3) {
       df nx;
       if (T.pbl) {  // with full PBL mixing the tendency is formed in FP64 (rare combination)
         const double qd = df_to_d(make_float2(q.h, q.l));
-        const double du = fma(df_to_d(T.acc[x]), rm, pbl_term(T, c, col, s, qd));
+        const double du = fma(df_to_d(a), rm, pbl_term(T, c, col, s, qd));
         nx = split_df(fma(du, dt_2, qd));
       } else {
-        nx = df_add(q, df_mul(df_ld2(T.acc, x), sc));
+        nx = df_add(q, df_mul(df{a.x, a.y}, sc));
       }
       if (STAGE == 1 || STAGE == 2) {
         T.qhi[x] = nx.h;
         T.qlo[x] = nx.l;
       } else if (STAGE == 3) {
         u3p[x] = make_float2(nx.h, nx.l);
-        const df u4 = df_add(df_mul(c23, split_df(U[x])), df_mul(c13, nx));
+        const df u4 = df_add(df_mul(c23, split_df(u0)), df_mul(c13, nx));
         T.qhi[x] = u4.h;
         T.qlo[x] = u4.l;
       } else {
-        const double u0 = U[x];
         const double un = df_to_d(make_float2(nx.h, nx.l));
         // (1/3 u0 + 2/3 u3) - un in pairs, then FP64 for the norm; its factor 1/2 goes onto
         // the cell's sum as an exact 1/4
-        const df ut = df_add(df_mul(c13, split_df(u0)), df_mul(c23, df_ld2(u3p, x)));
+        const df ut = df_add(df_mul(c13, split_df(u0)), df_mul(c23, df{u3.x, u3.y}));
         const df d = df_sub(ut, nx);
         const double err = df_to_d(make_float2(d.h, d.l));
         const double den = fma(amax_bits(u0, un), rtol, atol);
@@ -1746,6 +1757,30 @@ __global__ void __launch_bounds__(kRedThreads) k_stage_mixed(DevTransport<double
         e = fma(at, at, e);
         Un[x] = (clamp && __double2hiint(un) < 0) ? 0.0 : un;
       }
+    };
+    // tracers in groups of four: every load of a group is issued before its arithmetic, so a
+    // thread keeps four tracers' loads in flight (the same arithmetic, in the same order)
+    constexpr int kGrp = 4;
+    int s = 0;
+    for (; s + kGrp <= T.ntr; s += kGrp) {
+      df q[kGrp];
+      float2 a[kGrp], u3[kGrp];
+      double u0[kGrp];
+#pragma unroll
+      for (int r = 0; r < kGrp; ++r) {
+        const size_t x = (size_t)(s + r) * nc + c;
+        q[r] = df{T.qhi[x], T.qlo[x]};
+        a[r] = T.acc[x];
+        u0[r] = STAGE >= 3 ? U[x] : 0.0;
+        u3[r] = STAGE == 4 ? u3p[x] : make_float2(0.0f, 0.0f);
+      }
+#pragma unroll
+      for (int r = 0; r < kGrp; ++r) tracer(s + r, (size_t)(s + r) * nc + c, q[r], a[r], u0[r], u3[r]);
+    }
+    for (; s < T.ntr; ++s) {
+      const size_t x = (size_t)s * nc + c;
+      tracer(s, x, df{T.qhi[x], T.qlo[x]}, T.acc[x], STAGE >= 3 ? U[x] : 0.0,
+             STAGE == 4 ? u3p[x] : make_float2(0.0f, 0.0f));
     }
   }
   if (STAGE == 4) {
@@ -2057,7 +2092,7 @@ void launch_flux_dir_mixed(cudaStream_t st, const DevTransport<double>& T, const
   allow_big_smem();
   if (split) {
     size_t n = (size_t)T.ntr * T.nlon * T.nlat * T.nlev;
-    k_split_input<<<(unsigned)((n + kRedThreads - 1) / kRedThreads), kRedThreads, 0, st>>>(
+    k_split_input<<<(unsigned)((n + 4 * kRedThreads - 1) / (4 * kRedThreads)), kRedThreads, 0, st>>>(
         T, nullptr, nullptr, nullptr, Q);
   }
   launch_fluxes_mixed(st, T, sel, dir);
@@ -2079,7 +2114,7 @@ void launch_ssprk43_attempt(cudaStream_t st, const DevTransport<double>& T, cons
   StageSel sel{ctl, 1, B.U0, B.U1, B.S1, B.S2, B.S3, nullptr, 1.0};
   if (T.mixed) {
     size_t n = (size_t)T.ntr * nc;
-    k_split_input<<<(unsigned)((n + kRedThreads - 1) / kRedThreads), kRedThreads, 0, st>>>(
+    k_split_input<<<(unsigned)((n + 4 * kRedThreads - 1) / (4 * kRedThreads)), kRedThreads, 0, st>>>(
         T, ctl, B.U0, B.U1, nullptr);
   }
   if (T.mixed) {  // compensated FP32: the stages stay pairs until stage 4
@@ -2123,7 +2158,7 @@ void launch_transport_rhs(cudaStream_t st, const DevTransport<double>& T, const 
   size_t nc = (size_t)T.nlon * T.nlat * T.nlev;
   if (T.mixed) {
     size_t n = (size_t)T.ntr * nc;
-    k_split_input<<<(unsigned)((n + kRedThreads - 1) / kRedThreads), kRedThreads, 0, st>>>(
+    k_split_input<<<(unsigned)((n + 4 * kRedThreads - 1) / (4 * kRedThreads)), kRedThreads, 0, st>>>(
         T, nullptr, nullptr, nullptr, U);
   }
   launch_fluxes(st, T, sel);
