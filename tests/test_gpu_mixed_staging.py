@@ -117,11 +117,12 @@ def test_open_boundaries_bulk_equals_plain_and_freestream_is_exact():
     assert np.array_equal(a, b)
 
 
-@pytest.mark.parametrize("sper", [1, 4, 12])
+@pytest.mark.parametrize("sper", [1, 2, 3, 4, 5, 12])
 def test_streaming_forms_are_bit_identical_to_the_pencils(sper):
     """The streaming kernels (a warp of shuffles per lon-row segment, one thread per lat /
     vertical line) form the same pairs in the same order as the pencils: the same bits, on a
-    global grid (periodic rows, mirrored poles and levels) and on open walls."""
+    global grid (periodic rows, mirrored poles and levels) and on open walls, for tracer
+    groupings that divide the 12 tracers evenly and that leave a shorter last group."""
     w = workloads.c2(nlon=36, nlat=19, nlev=10)
     a, _ = _run(w, STAGING_AUTO, dict(mixed_x_stream=1, mixed_yz_stream=1, mixed_x_tracers=sper,
                                       mixed_yz_tracers=sper))
