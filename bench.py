@@ -753,6 +753,33 @@ def measure_c5(local, barrier, steps=1):
             state_diff(gcm, ocm, nsp), cells=len(J) * g["nlev"], oracle_status=orc,
             oracle_wall_s=round(wall, 2),
             note="48 seeded columns x 72 levels, the library's LU order and rate constants")
+        # the CPU path timed on a bounded sample: the oracle's per-cell chemistry (the part
+        # that takes ~95 % of the GPU's batched step) over one macro step on 960 seeded
+        # columns, on all host threads, against the GPU's batched chemistry over all cells
+        J2 = rng.integers(0, g["nlat"], 960)
+        I2 = rng.integers(0, g["nlon"], 960)
+        sub2 = workloads.latlon_grid(len(J2), 1, g["nlev"], pole_centred=False)
+        cfg2 = abi.make_config(sub2, mabi, has_air_mass=True, do_transport=False,
+                               chem_mode=abi.RS_CHEM_PER_CELL)
+        col2 = lambda a: np.ascontiguousarray(a[..., J2, I2][..., None, :])
+        f2 = abi.ForcingABI(temperature=col2(w.forcing["temperature"]),
+                            pressure=col2(w.forcing["pressure"]), dp=col2(w.forcing["dp"]))
+        o2 = oracle.Oracle(cfg2, f2, mabi)
+        o2.set_lu_order(lu_order)
+        o2.set_rates(col2(rates))
+        u2 = col2(pre)
+        t0 = time.perf_counter()
+        orc2, _, _ = o2.chem_per_cell(u2, 0.0, w.dt_macro, w.dt0_C)
+        wall2 = time.perf_counter() - t0
+        ncell2 = len(J2) * g["nlev"]
+        gpu_chem_ms = out["batched_fp64"]["ms_per_step"] - out["transport_fp64"]["ms_per_step"]
+        out["cpu_reference"] = {
+            "sample": "per-cell chemistry of one %g s macro step on %d seeded columns x %d levels "
+                      "(%d cells), the oracle on all host threads" % (w.dt_macro, len(J2), g["nlev"], ncell2),
+            "cores": os.cpu_count(), "kind": "port", "status": orc2, "wall_s": round(wall2, 3),
+            "cells_per_s": round(ncell2 / wall2, 1),
+            "gpu_batched_fp64_chemistry_cells_per_s": round(w.ncells / (gpu_chem_ms * 1e-3), 1),
+            "gpu_over_cpu": round((w.ncells / (gpu_chem_ms * 1e-3)) / (ncell2 / wall2), 1)}
     bm = out["errors"]["batched_mixed_vs_batched_fp64"]
     cond = out["errors"]["batched_fp64_ulp_vs_batched_fp64"]
     out["target"] = {
