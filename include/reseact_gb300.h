@@ -212,6 +212,12 @@ rs_status rs_set_forcing(rs_handle* h, const rs_forcing* f);
 rs_status rs_get_rate_constants(rs_handle* h, double* k, size_t n);
 rs_status rs_set_rate_constants(rs_handle* h, const double* k, size_t n);
 
+/* Per-cell chemistry (RS_CHEM_PER_CELL) diagnostics, cell in grid order: the accepted substeps
+ * of each cell in the last macro step (steps, may be NULL) and the step size each cell carries
+ * into the next (dt, may be NULL; 0 before the first window).  n = the cell count.  No
+ * reference counterpart (the reference has one global step size). */
+rs_status rs_get_cell_steps(rs_handle* h, double* steps, double* dt, size_t n);
+
 /* One Lie-Trotter macro step over [t0, t1] on the resident state.  *dtT / *dtC are the
  * carried step sizes in and out.  Returns RS_ERR_MAXITERS / RS_ERR_NONFINITE on failure
  * (the state then holds whatever the halves reached; bisection stays with the caller, as

@@ -14,7 +14,8 @@ _LIBS = {}
 SYMBOLS = [
     "rs_default_config", "rs_create", "rs_destroy", "rs_last_error", "rs_state_size",
     "rs_species_per_cell", "rs_set_state", "rs_get_state", "rs_set_forcing",
-    "rs_get_rate_constants", "rs_set_rate_constants", "rs_macro_step", "rs_rhs_transport",
+    "rs_get_rate_constants", "rs_set_rate_constants", "rs_get_cell_steps", "rs_macro_step",
+    "rs_rhs_transport",
     "rs_rhs_chem", "rs_block_jac", "rs_single_step", "rs_state_device_ptr", "rs_stream",
     "rs_set_profiling", "rs_get_profile", "rs_reset_profile", "rs_ros23_attempt_noalloc",
     "rs_record", "rs_record_count", "rs_set_adjoint_tape", "rs_record_taped",
@@ -58,6 +59,8 @@ def _declare(L):
     for f in ("rs_get_rate_constants", "rs_set_rate_constants"):
         getattr(L, f).argtypes = [vp, dp, sz]
         getattr(L, f).restype = C.c_int
+    L.rs_get_cell_steps.argtypes = [vp, dp, dp, sz]
+    L.rs_get_cell_steps.restype = C.c_int
     L.rs_macro_step.argtypes = [vp, C.c_double, C.c_double, dp, dp, C.POINTER(abi.rs_stats)]
     L.rs_macro_step.restype = C.c_int
     for f in ("rs_rhs_transport", "rs_rhs_chem"):
@@ -245,6 +248,14 @@ class Solver:
         k = np.empty(self.nr * self.nc)
         self._check(self.L.rs_get_rate_constants(self.h, _p(k), k.size))
         return k.reshape(self.nr, self.nlev, self.nlat, self.nlon)
+
+    def cell_steps(self):
+        """Per-cell mode: (accepted substeps of each cell in the last macro step, the step
+        size each cell carries), both in grid order [nlev][nlat][nlon]."""
+        steps, dt = np.empty(self.nc), np.empty(self.nc)
+        self._check(self.L.rs_get_cell_steps(self.h, _p(steps), _p(dt), self.nc))
+        shape = (self.nlev, self.nlat, self.nlon)
+        return steps.reshape(shape), dt.reshape(shape)
 
     def set_rates(self, k):
         k = np.ascontiguousarray(k, dtype=np.float64).reshape(-1)

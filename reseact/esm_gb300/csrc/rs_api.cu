@@ -1234,6 +1234,18 @@ rs_status rs_get_rate_constants(rs_handle* h, double* k, size_t n) {
   });
 }
 
+rs_status rs_get_cell_steps(rs_handle* h, double* steps, double* dt, size_t n) {
+  if (!h) return RS_ERR_INVALID;
+  return guard(h, [&] {
+    if (n != h->nc) throw RsError(RS_ERR_INVALID, "cell array size");
+    if (h->cfg.chem_mode != RS_CHEM_PER_CELL)
+      throw RsError(RS_ERR_UNSUPPORTED, "per-cell step counts exist in the per-cell mode only");
+    if (steps) CK(cudaMemcpyAsync(steps, h->stepcell.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    if (dt) CK(cudaMemcpyAsync(dt, h->dtcell.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+  });
+}
+
 rs_status rs_set_rate_constants(rs_handle* h, const double* k, size_t n) {
   if (!h || !k) return RS_ERR_INVALID;
   return guard(h, [&] {

@@ -100,3 +100,19 @@ def test_strict_build_refuses_group_kernel():
     with pytest.raises(RsError):
         s.set_launch_shape(per_cell_group=8)
     s.close()
+
+
+def test_cell_steps_diagnostics():
+    """rs_get_cell_steps: each cell's accepted substeps of the last window sum to the macro
+    step's total, and the carried step sizes are on the step-size lattice."""
+    w = workloads.c3(ncells=2048)
+    s = Solver.for_workload(w)
+    s.set_state(w.u0_cellmajor())
+    _, _, _, st = s.macro_step(0.0, 600.0, 1.0, w.dt0_C)
+    steps, dt = s.cell_steps()
+    assert steps.shape == (1, w.grid["nlat"], w.grid["nlon"])
+    assert steps.min() >= 1 and steps.sum() == st.chem_cell_steps
+    bits = dt.reshape(-1).view(np.uint64)
+    assert np.all(dt > 0) and np.all(bits & np.uint64((1 << 48) - 1) == 0)
+    s.close()
+
